@@ -1,0 +1,116 @@
+"""ctypes front end of the CPU oracle (oracle/plb_oracle.c).
+
+TEST INFRASTRUCTURE.  Only the tests, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py`` use this module, as the checker or as the
+timed CPU baseline.  The product library never calls it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libplboracle.so")
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+                ("periodic", ctypes.c_int * 3),
+                ("omega", ctypes.c_double), ("rho0", ctypes.c_double), ("bbRho", ctypes.c_double)]
+
+
+_lib = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        _lib = ctypes.CDLL(LIB_PATH)
+        dp = ctypes.POINTER(ctypes.c_double)
+        u8 = ctypes.POINTER(ctypes.c_uint8)
+        for name in ("orc_run",):
+            fn = getattr(_lib, name)
+            fn.argtypes = [ctypes.POINTER(_Params), u8, dp, dp, dp, ctypes.c_int, dp]
+            fn.restype = ctypes.c_int
+        _lib.orc_initialize.argtypes = [ctypes.POINTER(_Params), u8, dp, dp, dp]
+        _lib.orc_reduce.argtypes = [ctypes.POINTER(_Params), u8, dp, dp, dp, dp, dp]
+        _lib.orc_mebb_masks.argtypes = [ctypes.POINTER(_Params), u8, ctypes.POINTER(ctypes.c_uint32)]
+        _lib.orc_set_threads.argtypes = [ctypes.c_int]
+        _lib.orc_max_threads.restype = ctypes.c_int
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class OracleLattice:
+    """A lattice description for the oracle (same fields as the golden cases)."""
+
+    def __init__(self, nx, ny, nz, periodic, omega, flags, bcval=None, force=None,
+                 rho0=1.0, bb_rho=0.0):
+        self.shape = (nx, ny, nz)
+        n = nx * ny * nz
+        self.p = _Params(nx, ny, nz, (ctypes.c_int * 3)(*[int(v) for v in periodic]),
+                         float(omega), float(rho0), float(bb_rho))
+        self.flags = np.ascontiguousarray(flags, np.uint8).reshape(n)
+        self.bcval = np.ascontiguousarray(
+            np.zeros((n, 3)) if bcval is None else bcval, np.float64).reshape(n * 3)
+        self.force = np.ascontiguousarray(
+            np.zeros((n, 3)) if force is None else force, np.float64).reshape(n * 3)
+
+    @classmethod
+    def from_golden(cls, g, meta):
+        return cls(meta["nx"], meta["ny"], meta["nz"], meta["periodic"], meta["omega"],
+                   g["flags"], g["bcval"], g["force"], meta.get("rho0", 1.0),
+                   meta.get("bb_rho", 0.0))
+
+    def _u8(self):
+        return self.flags.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
+
+    def initialize(self, f):
+        f = np.ascontiguousarray(f, np.float64).copy()
+        lib().orc_initialize(ctypes.byref(self.p), self._u8(), _dp(self.bcval), _dp(self.force),
+                             _dp(f))
+        return f
+
+    def run(self, f, nsteps, with_stats=True):
+        """Advance f ([x][y][z][19] f-bar) by nsteps; returns (f, stats[nsteps, 7])."""
+        f = np.ascontiguousarray(f, np.float64).copy()
+        stats = np.zeros((max(nsteps, 1), 7)) if with_stats else None
+        rc = lib().orc_run(ctypes.byref(self.p), self._u8(), _dp(self.bcval), _dp(self.force),
+                           _dp(f), int(nsteps), _dp(stats) if with_stats else None)
+        if rc != 0:
+            raise MemoryError("oracle allocation failed")
+        return f, stats
+
+    def reduce(self, f):
+        f = np.ascontiguousarray(f, np.float64)
+        e = ctypes.c_double()
+        d = ctypes.c_double()
+        lib().orc_reduce(ctypes.byref(self.p), self._u8(), _dp(self.bcval), _dp(self.force),
+                         _dp(f), ctypes.byref(e), ctypes.byref(d))
+        return e.value, d.value
+
+    def mebb_masks(self):
+        out = np.zeros(self.flags.size, np.uint32)
+        lib().orc_mebb_masks(ctypes.byref(self.p), self._u8(),
+                             out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)))
+        return out
+
+
+def set_threads(n: int):
+    lib().orc_set_threads(int(n))
+
+
+def max_threads() -> int:
+    return int(lib().orc_max_threads())

@@ -1,0 +1,363 @@
+"""Parity cases for the D3Q19 collide-and-stream path, described cell by cell.
+
+Every case is deterministic (seeded) and small enough for the CPU oracle to
+finish in well under a second.  ``make_golden.py`` feeds them to the reference
+driver; the tests feed the same inputs to the oracle and to the CUDA path.
+
+Cell kinds (one byte per cell) follow the numbering shared by the reference
+driver (oracle/ref_drivers/common.h), the oracle and the CUDA library:
+
+  0 BGK, 1 Guo-forced BGK, 2 incompressible BGK, 3 bounce-back,
+  4 momentum-exchange bounce-back, 5 no-dynamics,
+  6 + 2*d + (o>0)   regularized velocity face (normal direction d, orientation o)
+  12 + 2*d + (o>0)  regularized pressure face
+  18 + 2*d + (o>0)  Zou/He velocity face
+  24 + 2*d + (o>0)  Zou/He pressure face
+"""
+from __future__ import annotations
+
+import dataclasses
+import struct
+
+import numpy as np
+
+# D3Q19 velocity set in the reference's ordering
+# (latticeBoltzmann/nearestNeighborLattices3D.hh:168-180).
+C = np.array([
+    [0, 0, 0],
+    [-1, 0, 0], [0, -1, 0], [0, 0, -1], [-1, -1, 0], [-1, 1, 0], [-1, 0, -1],
+    [-1, 0, 1], [0, -1, -1], [0, -1, 1],
+    [1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 1, 0], [1, -1, 0], [1, 0, 1],
+    [1, 0, -1], [0, 1, 1], [0, 1, -1]], dtype=np.int64)
+T = np.array([1 / 3] + [1 / 18] * 3 + [1 / 36] * 6 + [1 / 18] * 3 + [1 / 36] * 6)
+
+BGK, GUO, INCBGK, BB, MEBB, NODYN = 0, 1, 2, 3, 4, 5
+REGVEL, REGPRESS, ZHVEL, ZHPRESS = 6, 12, 18, 24
+
+
+def face_kind(family: int, direction: int, orientation: int) -> int:
+    return family + 2 * direction + (1 if orientation > 0 else 0)
+
+
+@dataclasses.dataclass
+class CaseSpec:
+    name: str
+    nx: int
+    ny: int
+    nz: int
+    periodic: tuple
+    omega: float
+    nsteps: int
+    flags: np.ndarray
+    bcval: np.ndarray
+    force: np.ndarray
+    f0: np.ndarray
+    forced: int = 0
+    blocks: tuple = (1, 1, 1)
+    stats_every: int = 1
+    rho0: float = 1.0
+    bb_rho: float = 0.0
+
+    def meta(self):
+        return dict(name=self.name, nx=self.nx, ny=self.ny, nz=self.nz,
+                    periodic=list(self.periodic), omega=self.omega, nsteps=self.nsteps,
+                    forced=self.forced, blocks=list(self.blocks),
+                    stats_every=self.stats_every, rho0=self.rho0, bb_rho=self.bb_rho)
+
+
+def equilibrium(rho, u):
+    """f-bar at equilibrium: t_i (rhoBar + 3 c.j + invRho (4.5 (c.j)^2 - 1.5 j^2)), j = rho u."""
+    j = rho[..., None] * u
+    rho_bar = rho - 1.0
+    inv_rho = 1.0 / rho
+    cj = np.einsum("qd,...d->...q", C.astype(np.float64), j)
+    jsq = (j * j).sum(-1)
+    return T * (rho_bar[..., None] + 3.0 * cj
+                + inv_rho[..., None] * (4.5 * cj * cj - 1.5 * jsq[..., None]))
+
+
+def smooth_fields(shape, rng, u_amp, rho_amp):
+    nx, ny, nz = shape
+    x = np.arange(nx)[:, None, None] / nx
+    y = np.arange(ny)[None, :, None] / ny
+    z = np.arange(nz)[None, None, :] / nz
+    ph = rng.uniform(0, 2 * np.pi, size=6)
+    u = np.zeros(shape + (3,))
+    u[..., 0] = u_amp * np.sin(2 * np.pi * y + ph[0]) * np.cos(2 * np.pi * z + ph[1])
+    u[..., 1] = u_amp * np.sin(2 * np.pi * z + ph[2]) * np.cos(2 * np.pi * x + ph[3])
+    u[..., 2] = u_amp * np.sin(2 * np.pi * x + ph[4]) * np.cos(2 * np.pi * y + ph[5])
+    rho = 1.0 + rho_amp * np.cos(2 * np.pi * (x + y + z) + ph[0])
+    return rho, u
+
+
+def initial_state(shape, rng, u_amp=0.03, rho_amp=0.01, noise=2e-4):
+    rho, u = smooth_fields(shape, rng, u_amp, rho_amp)
+    f = equilibrium(rho, u)
+    f += noise * T * rng.standard_normal(f.shape)
+    return np.ascontiguousarray(f)
+
+
+def empty(shape):
+    n = shape[0] * shape[1] * shape[2]
+    return (np.zeros(shape, np.uint8), np.zeros(shape + (3,)), np.zeros(shape + (3,)), n)
+
+
+def _spec(name, shape, periodic, omega, nsteps, flags, bcval, force, f0, **kw):
+    return CaseSpec(name=name, nx=shape[0], ny=shape[1], nz=shape[2], periodic=tuple(periodic),
+                    omega=omega, nsteps=nsteps, flags=np.ascontiguousarray(flags, np.uint8),
+                    bcval=np.ascontiguousarray(bcval), force=np.ascontiguousarray(force),
+                    f0=f0, **kw)
+
+
+# ---------------------------------------------------------------- small cases
+
+def case_periodic_bgk():
+    shape = (12, 10, 8)
+    rng = np.random.default_rng(101)
+    flags, bcval, force, _ = empty(shape)
+    return _spec("periodic_bgk", shape, (1, 1, 1), 1.6, 40, flags, bcval, force,
+                 initial_state(shape, rng))
+
+
+def case_periodic_bgk_multiblock():
+    s = case_periodic_bgk()
+    s.name = "periodic_bgk_multiblock"
+    s.blocks = (2, 2, 2)
+    return s
+
+
+def cavity(shape, lid_u, omega, nsteps, name, rng, blocks=(1, 1, 1), f0=None, stats_every=1):
+    nx, ny, nz = shape
+    flags, bcval, force, _ = empty(shape)
+    flags[0, :, :] = BB
+    flags[-1, :, :] = BB
+    flags[:, 0, :] = BB
+    flags[:, -1, :] = BB
+    flags[:, :, 0] = BB
+    lid = face_kind(REGVEL, 2, +1)
+    flags[1:-1, 1:-1, -1] = lid
+    bcval[1:-1, 1:-1, -1, 0] = lid_u
+    flags[0, :, -1] = BB
+    flags[-1, :, -1] = BB
+    flags[:, 0, -1] = BB
+    flags[:, -1, -1] = BB
+    if f0 is None:
+        f0 = initial_state(shape, rng, u_amp=0.01, rho_amp=0.002)
+    return _spec(name, shape, (0, 0, 0), omega, nsteps, flags, bcval, force, f0,
+                 blocks=blocks, stats_every=stats_every)
+
+
+def case_cavity():
+    return cavity((12, 11, 10), 0.05, 1.857355126300999, 60, "cavity_bb_lid",
+                  np.random.default_rng(102))
+
+
+def case_cavity_multiblock():
+    return cavity((12, 11, 10), 0.05, 1.857355126300999, 60, "cavity_bb_lid_multiblock",
+                  np.random.default_rng(102), blocks=(2, 2, 2))
+
+
+def channel_sphere(shape, center, radius, u_max, omega, nsteps, name, rng, blocks=(1, 1, 1)):
+    nx, ny, nz = shape
+    flags, bcval, force, _ = empty(shape)
+    x = np.arange(nx)[:, None, None]
+    y = np.arange(ny)[None, :, None]
+    z = np.arange(nz)[None, None, :]
+    flags[:, 0, :] = BB
+    flags[:, -1, :] = BB
+    flags[:, :, 0] = BB
+    flags[:, :, -1] = BB
+    inlet = face_kind(REGVEL, 0, -1)
+    outlet = face_kind(REGPRESS, 0, +1)
+    flags[0, 1:-1, 1:-1] = inlet
+    flags[-1, 1:-1, 1:-1] = outlet
+    yy = (np.arange(ny) - 0.5) / (ny - 1)
+    zz = (np.arange(nz) - 0.5) / (nz - 1)
+    prof = 16.0 * u_max * (yy[:, None] * (1 - yy[:, None])) * (zz[None, :] * (1 - zz[None, :]))
+    bcval[0, 1:-1, 1:-1, 0] = prof[1:-1, 1:-1]
+    bcval[-1, 1:-1, 1:-1, 0] = 1.0
+    r2 = (x - center[0]) ** 2 + (y - center[1]) ** 2 + (z - center[2]) ** 2
+    flags[(r2 <= radius * radius) & (flags == BGK)] = MEBB
+    f0 = initial_state(shape, rng, u_amp=0.02, rho_amp=0.003)
+    return _spec(name, shape, (0, 0, 0), omega, nsteps, flags, bcval, force, f0, blocks=blocks)
+
+
+def case_channel_sphere():
+    return channel_sphere((24, 12, 12), (8, 6, 6), 2.5, 0.05, 1.8, 50, "channel_sphere",
+                          np.random.default_rng(103))
+
+
+def case_channel_sphere_multiblock():
+    return channel_sphere((24, 12, 12), (8, 6, 6), 2.5, 0.05, 1.8, 50,
+                          "channel_sphere_multiblock", np.random.default_rng(103), blocks=(3, 2, 1))
+
+
+def case_guo_channel():
+    shape = (16, 10, 10)
+    rng = np.random.default_rng(104)
+    flags, bcval, force, _ = empty(shape)
+    flags[...] = GUO
+    flags[:, 0, :] = BB
+    flags[:, -1, :] = BB
+    flags[:, :, 0] = BB
+    flags[:, :, -1] = BB
+    force[...] = 1e-4 * rng.standard_normal(shape + (3,))
+    force[..., 0] += 1e-3
+    f0 = initial_state(shape, rng)
+    return _spec("guo_channel", shape, (1, 0, 0), 1.6, 40, flags, bcval, force, f0, forced=1)
+
+
+def case_guo_periodic_multiblock():
+    shape = (12, 10, 8)
+    rng = np.random.default_rng(105)
+    flags, bcval, force, _ = empty(shape)
+    flags[...] = GUO
+    force[...] = 2e-4 * rng.standard_normal(shape + (3,))
+    force[..., 0] += 1e-3
+    f0 = initial_state(shape, rng)
+    return _spec("guo_periodic_multiblock", shape, (1, 1, 1), 1.3, 30, flags, bcval, force, f0,
+                 forced=1, blocks=(2, 1, 2))
+
+
+def six_faces(family, name, seed, omega=1.5, nsteps=30):
+    shape = (11, 10, 9)
+    rng = np.random.default_rng(seed)
+    flags, bcval, force, _ = empty(shape)
+    nx, ny, nz = shape
+    sl = {0: (slice(None), slice(1, -1), slice(1, -1)),
+          1: (slice(1, -1), slice(None), slice(1, -1)),
+          2: (slice(1, -1), slice(1, -1), slice(None))}
+    for d in range(3):
+        for o in (-1, 1):
+            idx = list(sl[d])
+            idx[d] = 0 if o < 0 else -1
+            idx = tuple(idx)
+            flags[idx] = face_kind(family, d, o)
+            if family in (REGVEL, ZHVEL):
+                v = 0.02 * rng.standard_normal(flags[idx].shape + (3,))
+                v[..., d] += -0.02 * o  # net inflow through every face
+                bcval[idx] = v
+            else:
+                bcval[idx + (0,)] = 1.0 + 0.002 * rng.standard_normal(flags[idx].shape)
+    # edges and corners are plain walls
+    edge = np.zeros(shape, bool)
+    for a in range(3):
+        for b in range(a + 1, 3):
+            for ia in (0, shape[a] - 1):
+                for ib in (0, shape[b] - 1):
+                    idx = [slice(None)] * 3
+                    idx[a] = ia
+                    idx[b] = ib
+                    edge[tuple(idx)] = True
+    flags[edge] = BB
+    f0 = initial_state(shape, rng, u_amp=0.02, rho_amp=0.003)
+    return _spec(name, shape, (0, 0, 0), omega, nsteps, flags, bcval, force, f0)
+
+
+def case_regvel_faces():
+    return six_faces(REGVEL, "regvel_faces", 106)
+
+
+def case_regpress_faces():
+    return six_faces(REGPRESS, "regpress_faces", 107)
+
+
+def case_zhvel_faces():
+    return six_faces(ZHVEL, "zhvel_faces", 108)
+
+
+def case_zhpress_faces():
+    return six_faces(ZHPRESS, "zhpress_faces", 109)
+
+
+def case_incbgk_nodyn():
+    shape = (10, 10, 10)
+    rng = np.random.default_rng(110)
+    flags, bcval, force, _ = empty(shape)
+    flags[...] = INCBGK
+    flags[3:5, 3:6, 4:7] = NODYN
+    flags[6:8, 6:8, 1:3] = BB
+    f0 = initial_state(shape, rng)
+    return _spec("incbgk_nodyn", shape, (1, 1, 1), 1.7, 30, flags, bcval, force, f0,
+                 rho0=1.02, bb_rho=1.0)
+
+
+def case_mebb_walls():
+    shape = (10, 8, 8)
+    rng = np.random.default_rng(111)
+    flags, bcval, force, _ = empty(shape)
+    flags[0, :, :] = MEBB
+    flags[-1, :, :] = MEBB
+    flags[4:6, 3:5, 3:6] = MEBB
+    flags[7, 1, 1] = NODYN
+    flags[2, 6, 5] = BB
+    f0 = initial_state(shape, rng, u_amp=0.04)
+    return _spec("mebb_walls", shape, (0, 1, 1), 1.4, 30, flags, bcval, force, f0)
+
+
+CASES = [
+    case_periodic_bgk, case_periodic_bgk_multiblock, case_cavity, case_cavity_multiblock,
+    case_channel_sphere, case_channel_sphere_multiblock, case_guo_channel,
+    case_guo_periodic_multiblock, case_regvel_faces, case_regpress_faces, case_zhvel_faces,
+    case_zhpress_faces, case_incbgk_nodyn, case_mebb_walls,
+]
+
+
+# ---------------------------------------------------------------- full-size case
+
+def case_cavity64():
+    """Lid-driven cavity, 64^3, 1000 steps, Re=100 with nu=0.02*64/100, from rest."""
+    shape = (64, 64, 64)
+    nu = 0.02 * 64 / 100
+    omega = 1.0 / (3.0 * nu + 0.5)
+    f0 = np.zeros(shape + (19,))
+    s = cavity(shape, 0.02, omega, 1000, "cavity64", None, f0=f0, stats_every=100)
+    return s
+
+
+BIG_CASES = [case_cavity64]
+
+
+def case_by_name(name):
+    for b in CASES + BIG_CASES:
+        s = b()
+        if s.name == name:
+            return s
+    raise KeyError(name)
+
+
+# ---------------------------------------------------------------- file formats
+
+def write_case_file(spec: CaseSpec, path: str):
+    with open(path, "wb") as f:
+        f.write(b"PLBCASE1")
+        f.write(struct.pack("<13i", spec.nx, spec.ny, spec.nz, *spec.periodic, spec.forced,
+                            *spec.blocks, spec.nsteps, spec.stats_every, 0))
+        f.write(struct.pack("<3d", spec.omega, spec.rho0, spec.bb_rho))
+        f.write(np.ascontiguousarray(spec.flags, np.uint8).tobytes())
+        f.write(np.ascontiguousarray(spec.bcval, np.float64).tobytes())
+        f.write(np.ascontiguousarray(spec.force, np.float64).tobytes())
+        f.write(np.ascontiguousarray(spec.f0, np.float64).tobytes())
+
+
+def read_result_file(path: str, spec: CaseSpec):
+    with open(path, "rb") as f:
+        data = f.read()
+    assert data[:8] == b"PLBRES01"
+    nx, ny, nz, nsteps, nstat = struct.unpack_from("<5i", data, 8)
+    off = 28
+    n = nx * ny * nz * 19
+    f_init = np.frombuffer(data, np.float64, n, off).reshape(nx, ny, nz, 19)
+    off += 8 * n
+    f_final = np.frombuffer(data, np.float64, n, off).reshape(nx, ny, nz, 19)
+    off += 8 * n
+    stats = np.zeros((nstat, 7))
+    for k in range(nstat):
+        (step,) = struct.unpack_from("<i", data, off)
+        vals = struct.unpack_from("<6d", data, off + 4)
+        stats[k, 0] = step
+        stats[k, 1:] = vals
+        off += 4 + 48
+    energy, density = struct.unpack_from("<2d", data, off)
+    return dict(f_init=f_init.copy(), f_final=f_final.copy(), stats=stats,
+                energy=energy, density=density)
