@@ -1,0 +1,371 @@
+"""Benchmark of the D3Q19 collide-and-stream hot path on GB300.
+
+Workload (the configuration the metric is quoted on that fits one GPU):
+channel flow past a sphere, D3Q19 BGK, 256x128x128, regularized parabolic
+velocity inlet at x=0 (u_max 0.05), regularized pressure outlet rho=1 at
+x=255, bounce-back channel walls, momentum-exchange bounce-back sphere of
+radius 16 at (64,64,64), omega 1.8; the momentum-exchange drag is reduced in
+FP64 every 100 steps.  Synthetic, deterministic geometry; the flow starts at
+rest.  One benchmark step = one collide-and-stream time step of the whole
+lattice.  The lattice state (637 MB in FP64) is larger than the 129 MB L2, so
+no explicit flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line (rank 0).  `value` = MLUPS of the FP64 form with the
+state resident in HBM; `e2e` = the same metric through the C ABI with host
+buffers (state sent from pinned host memory at the start, drag read back every
+100 steps, state received at the end, all inside the timed region).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MLUPS & %HBM roofline: FP64 plain vs FP32/BF16-store at stated L2 err; adjoint/fwd"
+SHAPE = (256, 128, 128)
+OMEGA = 1.8
+STATS_EVERY = 100
+FALLBACK_HBM_GBS = 6800.0
+# Algorithmic bytes per cell and step (AA pattern: every population read once
+# and written once, plus the one-byte cell kind).
+B_CELL = {"fp64": 305, "fp32": 153, "bf16": 77, "fp16": 77}
+
+
+def workload_geometry():
+    """Cell kinds and face values of the channel (same construction as the
+    parity cases, at full size)."""
+    from palabos_gb300 import native as N
+    nx, ny, nz = SHAPE
+    kinds = np.zeros(SHAPE, np.uint8)
+    bc = np.zeros(SHAPE + (3,))
+    kinds[:, 0, :] = N.BOUNCEBACK
+    kinds[:, -1, :] = N.BOUNCEBACK
+    kinds[:, :, 0] = N.BOUNCEBACK
+    kinds[:, :, -1] = N.BOUNCEBACK
+    kinds[0, 1:-1, 1:-1] = N.face_kind(N.REG_VELOCITY, 0, -1)
+    kinds[-1, 1:-1, 1:-1] = N.face_kind(N.REG_PRESSURE, 0, +1)
+    yy = (np.arange(ny) - 0.5) / (ny - 1)
+    zz = (np.arange(nz) - 0.5) / (nz - 1)
+    prof = 16.0 * 0.05 * (yy[:, None] * (1 - yy[:, None])) * (zz[None, :] * (1 - zz[None, :]))
+    bc[0, 1:-1, 1:-1, 0] = prof[1:-1, 1:-1]
+    bc[-1, 1:-1, 1:-1, 0] = 1.0
+    x = np.arange(nx)[:, None, None]
+    y = np.arange(ny)[None, :, None]
+    z = np.arange(nz)[None, None, :]
+    sphere = ((x - 64) ** 2 + (y - 64) ** 2 + (z - 64) ** 2 <= 16 * 16) & (kinds == N.BGK)
+    kinds[sphere] = N.MOMENTUM_EXCHANGE
+    return kinds, bc
+
+
+def build_lattice(precision, ctx=None):
+    from palabos_gb300 import lattice_from_description
+    kinds, bc = workload_geometry()
+    lat = lattice_from_description(*SHAPE, (0, 0, 0), OMEGA, kinds, bc, None, precision=precision, ctx=ctx)
+    lat.initialize_at_equilibrium(None, 1.0, (0.0, 0.0, 0.0))
+    lat.initialize()
+    return lat, kinds
+
+
+def algorithmic_bytes(kinds, precision):
+    from palabos_gb300 import native as N
+    cells = kinds.size
+    faces = int(((kinds >= N.REG_VELOCITY) & (kinds < 30)).sum())
+    mebb = int((kinds == N.MOMENTUM_EXCHANGE).sum())
+    # faces also read their 3 FP64 boundary values
+    return cells * B_CELL[precision] + faces * 24, dict(cells=cells, faces=faces, mebb=mebb)
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def load_traffic(kernel_key):
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    return d.get(kernel_key)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ distributed
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def init_dist(ws):
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group("gloo")
+    return dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ CPU baseline
+
+def cpu_baseline(steps_cap=None, seconds=15.0):
+    """The oracle (plain-C restatement of the reference path) on the host
+    cores, on the same workload, all OpenMP threads."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    kinds, bc = workload_geometry()
+    lat = O.OracleLattice(*SHAPE, (0, 0, 0), OMEGA, kinds, bc)
+    f = lat.initialize(np.zeros(SHAPE + (19,)))
+    threads = O.max_threads()
+    O.set_threads(threads)
+    f, _ = lat.run(f, 1, with_stats=False)   # warm-up
+    t0 = time.perf_counter()
+    f, _ = lat.run(f, 1, with_stats=False)
+    one = time.perf_counter() - t0
+    n = max(1, int(seconds / max(one, 1e-6)))
+    if steps_cap:
+        n = min(n, steps_cap)
+    t0 = time.perf_counter()
+    f, _ = lat.run(f, n, with_stats=True)
+    dt = time.perf_counter() - t0
+    cells = kinds.size
+    return {"value": round(cells * n / dt / 1e6, 3), "unit": "MLUPS", "cores": threads, "kind": "port",
+            "sample": f"{n} collide-and-stream steps of the full 256x128x128 lattice with statistics "
+                      f"({dt:.1f} s on {threads} OpenMP threads)"}
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    dist = init_dist(ws)
+    if rank != 0:
+        barrier(dist)
+        return
+    budget = 60.0
+    cb = cpu_baseline(seconds=budget / max(args.steps, 1) * args.steps)
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "MLUPS", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "channel_sphere_256x128x128_bgk_fp64", "shape": list(SHAPE),
+                       "omega": OMEGA, "drag_every": STATS_EVERY},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    barrier(dist)
+
+
+# ------------------------------------------------------------------ GPU arm
+
+def time_form(lat, steps, warmup):
+    lat.collide_and_stream(warmup, stats=False)
+    lat.ctx.synchronize()
+    return lat.time_steps(steps, stats=False)
+
+
+def run_gpu(args):
+    ws, rank, local = dist_env()
+    dist = init_dist(ws)
+    from palabos_gb300 import Context
+    ctx = Context(local)
+    peak, peak_src = load_peaks()
+
+    lat, kinds = build_lattice("fp64", ctx)
+    bytes_step, counts = algorithmic_bytes(kinds, "fp64")
+    cells = counts["cells"]
+    K, W = args.steps, args.warmup
+
+    # warm-up, then the timed region: K steps, drag reduced every 100 steps
+    for _ in range(W):
+        lat.collide_and_stream(1, stats=False)
+    ctx.synchronize()
+    launches0 = ctx.launch_count()
+    barrier(dist)
+    with ClockSampler(local) as clk:
+        ms_total = 0.0
+        done = 0
+        while done < K:
+            chunk = min(STATS_EVERY, K - done)
+            ms_total += lat.time_steps(chunk, stats=(chunk == STATS_EVERY))
+            done += chunk
+        ctx.synchronize()
+    launches = ctx.launch_count() - launches0
+    barrier(dist)
+    t_max = max_over_ranks(dist, ms_total)
+    value = ws * cells * K / (t_max * 1e-3) / 1e6
+    drag = lat.internal_statistics()["drag"].tolist() if K >= STATS_EVERY else None
+
+    # dominant kernel alone: average launch duration of the fused step kernel
+    k_ms = time_form(lat, min(K, 400), 10) / min(K, 400)
+    achieved = bytes_step / (k_ms * 1e-3) / 1e9
+    traffic = load_traffic("stepKernel_fp64_channel_sphere")
+
+    # e2e through the C ABI with host buffers
+    f_host = lat.receive()
+    e2e_steps = K
+    barrier(dist)
+    t0 = time.perf_counter()
+    lat.send(f_host)
+    done = 0
+    while done < e2e_steps:
+        chunk = min(STATS_EVERY, e2e_steps - done)
+        lat.collide_and_stream(chunk, stats=True)
+        lat.internal_statistics()      # drag to the host (synchronizes)
+        done += chunk
+    f_host = lat.receive()
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+    state_bytes = cells * 19 * 8
+    nread = (e2e_steps + STATS_EVERY - 1) // STATS_EVERY
+    e2e = {"value": round(ws * cells * e2e_steps / e2e_s / 1e6, 2), "unit": "MLUPS",
+           "h2d_bytes_per_step": round(state_bytes / e2e_steps, 1),
+           "d2h_bytes_per_step": round((state_bytes + 56 * nread) / e2e_steps, 1),
+           "note": "state sent once and received once per run of K steps; drag read every 100 steps"}
+    lat.close()
+
+    # the other storage forms on the same workload (kernel-only rate)
+    forms = {"fp64": {"mlups": round(cells / (k_ms * 1e-3) / 1e6, 1), "bytes_per_cell": B_CELL["fp64"],
+                      "hbm_frac": round(achieved / peak, 4)}}
+    if not args.skip_forms:
+        for prec in ("fp32", "bf16", "fp16"):
+            l2, _ = build_lattice(prec, ctx)
+            n = min(K, 400)
+            ms = time_form(l2, n, 10) / n
+            b, _ = algorithmic_bytes(kinds, prec)
+            forms[prec] = {"mlups": round(cells / (ms * 1e-3) / 1e6, 1), "bytes_per_cell": B_CELL[prec],
+                           "hbm_frac": round(b / (ms * 1e-3) / 1e9 / peak, 4)}
+            l2.close()
+
+    if rank == 0:
+        clocks = clk.summary()
+        line = {
+            "metric": METRIC, "value": round(value, 2), "unit": "MLUPS", "n_gpus": ws, "steps": K,
+            "warmup": W, "ms_per_step": round(t_max / K, 5), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "channel_sphere_256x128x128_bgk_fp64", "shape": list(SHAPE), "omega": OMEGA,
+                       "inlet": "regularized velocity, parabolic u_max=0.05", "outlet": "regularized pressure rho=1",
+                       "obstacle": "momentum-exchange bounce-back sphere r=16 at (64,64,64)",
+                       "drag_every": STATS_EVERY, "cells": cells, "faces": counts["faces"],
+                       "mebb_cells": counts["mebb"], "l2": "state (637 MB) larger than L2, no flush",
+                       "parallelism": f"replicas{ws}"},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": traffic,
+                         "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                         "kernel": "stepKernel<double> (fused collide+stream+faces, AA pattern)",
+                         "bytes_per_launch": bytes_step},
+            "forms": forms,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "clocks": clocks,
+            "drag_last": drag,
+        }
+        if not args.skip_cpu:
+            line["cpu_baseline"] = cpu_baseline()
+        print(json.dumps(line), flush=True)
+    barrier(dist)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-forms", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

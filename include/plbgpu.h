@@ -1,0 +1,199 @@
+/*
+ * plbgpu -- C ABI of the GB300 D3Q19 lattice library.
+ *
+ * One context drives one GPU through one CUDA stream.  A context owns any
+ * number of domains; a domain is one rectangular D3Q19 lattice (the bounding
+ * box of a MultiBlockLattice3D, or one block handed to a co-processor) held in
+ * a single device allocation.  Every call is synchronous with respect to the
+ * host unless stated otherwise, takes plain pointers and sizes, and returns an
+ * int status: PLBGPU_OK (0) or a negative PLBGPU_ERR_* code; the message of
+ * the last failure is available from plbgpu_last_error().  No C++ exception
+ * crosses this interface.
+ *
+ * Populations cross the interface as f-bar = f - t_i (the reference's stored
+ * representation, latticeBoltzmann/roundOffPolicy.h:40-89) in FP64, in the
+ * co-processor transfer layout: z fastest, then y, then x, and the 19
+ * populations of a cell contiguous in the D3Q19 order of
+ * latticeBoltzmann/nearestNeighborLattices3D.hh:168-180
+ * (coProcessors/coProcessor3D.h:84-91).
+ *
+ * Reference paths in the comments are relative to the reference's src/.
+ */
+#ifndef PLBGPU_H
+#define PLBGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct plbgpu_ctx plbgpu_ctx;
+
+/* Status codes. */
+#define PLBGPU_OK 0
+#define PLBGPU_ERR_ARG (-1)      /* bad argument (size, box, kind, precision) */
+#define PLBGPU_ERR_HANDLE (-2)   /* unknown domain handle */
+#define PLBGPU_ERR_CUDA (-3)     /* CUDA runtime error */
+#define PLBGPU_ERR_NOMEM (-4)    /* device allocation failed */
+#define PLBGPU_ERR_STATE (-5)    /* call not valid in the domain's current state */
+
+/* Storage precision of the populations.  FP64 computes in FP64 and
+ * reproduces the reference bit for bit; the other forms compute in FP32 and
+ * store f-bar in FP32, BF16 or FP16 (the FP64 reductions are kept). */
+#define PLBGPU_FP64 0
+#define PLBGPU_FP32 1
+#define PLBGPU_BF16 2
+#define PLBGPU_FP16 3
+
+/* Cell kinds (dynamics) -- one byte per cell.  Face kinds are
+ * base + 2*direction + (orientation > 0 ? 1 : 0). */
+#define PLBGPU_BGK 0          /* BGKdynamics, basicDynamics/isoThermalDynamics.hh:319-330 */
+#define PLBGPU_GUO 1          /* GuoExternalForceBGKdynamics, basicDynamics/externalForceDynamics.hh:215-234 */
+#define PLBGPU_INCBGK 2       /* IncBGKdynamics, basicDynamics/isoThermalDynamics.hh:1408-1419 */
+#define PLBGPU_BOUNCEBACK 3   /* BounceBack, core/dynamics.hh:783-790 */
+#define PLBGPU_MOMENTUM_EXCHANGE 4 /* MomentumExchangeBounceBack, boundaryCondition/bounceBackModels.hh:100-136 */
+#define PLBGPU_NODYNAMICS 5   /* NoDynamics, core/dynamics.hh:968-971 */
+#define PLBGPU_REG_VELOCITY 6 /* RegularizedVelocityBoundaryDynamics (wrapped), regularizedBoundaryDynamics.hh:96-110 */
+#define PLBGPU_REG_PRESSURE 12 /* RegularizedDensityBoundaryDynamics (wrapped), regularizedBoundaryDynamics.hh:160-175 */
+#define PLBGPU_ZOUHE_VELOCITY 18 /* ZouHeVelocityDynamics (wrapped), zouHeDynamics.hh:44-113, 166-169 */
+#define PLBGPU_ZOUHE_PRESSURE 24 /* ZouHePressureDynamics (wrapped), zouHeDynamics.hh:222-225 */
+
+/* ------------------------------------------------------------ context */
+
+/* Create a context on CUDA device `device`.  Replaces the singleton
+ * global::defaultCoProcessor3D<T>() (coProcessors/coProcessor3D.h:178-186). */
+int plbgpu_create(int device, plbgpu_ctx** out);
+int plbgpu_destroy(plbgpu_ctx* ctx);
+/* Message of the last failing call on this context ("" if none). */
+const char* plbgpu_last_error(const plbgpu_ctx* ctx);
+/* Number of kernels this context has launched so far. */
+int plbgpu_launch_count(const plbgpu_ctx* ctx, unsigned long long* count);
+/* The CUDA stream (cudaStream_t) all work of the context is issued on. */
+int plbgpu_get_stream(const plbgpu_ctx* ctx, void** stream);
+int plbgpu_synchronize(plbgpu_ctx* ctx);
+
+/* ------------------------------------------------------------ domains */
+
+/* Allocate a domain of nx*ny*nz cells (all BGK, non-periodic, omega 1).
+ * Replaces MultiBlockLattice3D construction (multiBlock/multiBlockLattice3D.hh:60-87)
+ * together with CoProcessor3D::addDomain (coProcessors/coProcessor3D.h:75). */
+int plbgpu_add_domain(plbgpu_ctx* ctx, int nx, int ny, int nz, int precision, int* handle);
+int plbgpu_remove_domain(plbgpu_ctx* ctx, int handle);
+int plbgpu_domain_info(plbgpu_ctx* ctx, int handle, int* nx, int* ny, int* nz, int* precision,
+                       unsigned long long* device_bytes);
+
+/* Periodicity per axis (PeriodicitySwitch3D::toggle, multiBlock/multiBlock3D.h:167-168). */
+int plbgpu_set_periodicity(plbgpu_ctx* ctx, int handle, int px, int py, int pz);
+
+/* omega of every BGK-family dynamics, rho0 of IncBGKdynamics (its invRho0 =
+ * 1/rho0, isoThermalDynamics.hh:1353-1356), and the rho given to the
+ * BounceBack / MomentumExchangeBounceBack constructors (core/dynamics.h:574). */
+int plbgpu_set_params(plbgpu_ctx* ctx, int handle, double omega, double rho0, double bb_rho);
+
+/* defineDynamics(lattice, box, dynamics) for a whole box
+ * (dataProcessors/dataInitializerWrapper3D.h:170-171), and the per-cell
+ * form for an arbitrary mask (`kinds` has one byte per cell of the box,
+ * z fastest).  Face kinds set this way are the wrapped boundary conditions of
+ * createLocalBoundaryCondition3D / createZouHeBoundaryCondition3D
+ * (boundaryCondition/boundaryCondition3D.hh:1163-1167, zouHeBoundary3D.hh:338-342). */
+int plbgpu_define_dynamics(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1, int z0, int z1,
+                           int kind);
+int plbgpu_set_kinds(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1, int z0, int z1,
+                     const uint8_t* kinds, size_t n);
+int plbgpu_get_kinds(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1, int z0, int z1,
+                     uint8_t* kinds, size_t n);
+
+/* setBoundaryVelocity / setBoundaryDensity (dataInitializerWrapper3D.h:99-118),
+ * constant over a box or one value per cell of the box (`values`: 3 doubles
+ * per cell for velocity, 1 per cell for density). */
+int plbgpu_set_boundary_velocity(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1, int z0,
+                                 int z1, double ux, double uy, double uz);
+int plbgpu_set_boundary_velocity_field(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1,
+                                       int z0, int z1, const double* values, size_t n);
+int plbgpu_set_boundary_density(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1, int z0,
+                                int z1, double rho);
+int plbgpu_set_boundary_density_field(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1,
+                                      int z0, int z1, const double* values, size_t n);
+
+/* setExternalVector(lattice, box, forceBeginsAt, F) for the Guo force
+ * (dataInitializerWrapper3D.h:154-155), constant or per cell (3 doubles). */
+int plbgpu_set_force(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1, int z0, int z1,
+                     double fx, double fy, double fz);
+int plbgpu_set_force_field(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1, int z0, int z1,
+                           const double* values, size_t n);
+
+/* initializeMomentumExchange(lattice, boundingBox)
+ * (boundaryCondition/bounceBackModels3D.hh:248-271): record, for every
+ * momentum-exchange cell, the directions pointing to fluid. */
+int plbgpu_initialize_momentum_exchange(plbgpu_ctx* ctx, int handle);
+
+/* initializeAtEquilibrium(lattice, box, rho, u) (dataInitializerWrapper3D.h:122-123,
+ * core/cell.hh iniCellAtEquilibrium), constant or per cell (`rho_u`: 4 doubles
+ * per cell: rho, ux, uy, uz). */
+int plbgpu_initialize_at_equilibrium(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1, int z0,
+                                     int z1, double rho, double ux, double uy, double uz);
+int plbgpu_initialize_at_equilibrium_field(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1,
+                                           int z0, int z1, const double* rho_u, size_t n);
+
+/* lattice.initialize() (multiBlock/multiBlock3D.cpp:330-332): run the
+ * boundary-face completion once on the current state. */
+int plbgpu_initialize(plbgpu_ctx* ctx, int handle);
+
+/* ------------------------------------------------------------ transfer */
+
+/* Host -> device / device -> host of the populations of a sub-box, FP64
+ * f-bar, transfer layout above; n = number of doubles in buf (19 per cell).
+ * CoProcessor3D::send / receive (coProcessors/coProcessor3D.h:80-96). */
+int plbgpu_send(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1, int z0, int z1,
+                const double* buf, size_t n);
+int plbgpu_receive(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1, int z0, int z1,
+                   double* buf, size_t n);
+
+/* ------------------------------------------------------------ time stepping */
+
+/* nsteps collide-and-stream steps of the whole domain: collision, streaming,
+ * boundary-face completion, periodic wrap -- the full
+ * MultiBlockLattice3D::collideAndStream() (multiBlock/multiBlockLattice3D.hh:318-357)
+ * including executeInternalProcessors and the envelope update.  When
+ * collect_stats is non-zero the internal statistics (average rho-bar,
+ * average u^2, max u^2, momentum-exchange force) are gathered during the last
+ * of the nsteps steps.  Asynchronous: returns once the work is queued. */
+int plbgpu_collide_and_stream(plbgpu_ctx* ctx, int handle, int nsteps, int collect_stats);
+
+/* Statistics of the last step that gathered them (BlockStatistics::evaluate,
+ * core/blockStatistics.cpp:77-110; MultiBlock3D::getInternalStatistics):
+ * out[0] average rho-bar, out[1] average u^2, out[2] max u^2,
+ * out[3..5] sum of -momentum exchange (drag on the obstacle) x,y,z,
+ * out[6] number of cells that gathered statistics. */
+int plbgpu_get_stats(plbgpu_ctx* ctx, int handle, double out[7]);
+
+/* computeAverageEnergy / computeAverageDensity over a box
+ * (dataProcessors/dataAnalysisWrapper3D.hh:1226-1262). */
+int plbgpu_reduce(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1, int z0, int z1,
+                  double* avg_energy, double* avg_density);
+
+/* Run nsteps steps and time them with CUDA events recorded on the context's
+ * stream (milliseconds). */
+int plbgpu_time_steps(plbgpu_ctx* ctx, int handle, int nsteps, int collect_stats, float* ms);
+
+/* ------------------------------------------------------------ co-processor form */
+
+/* The four calls of plb::CoProcessor3D<double> (coProcessors/coProcessor3D.h:41-116)
+ * with its return convention: 1 = success, 0 = failure.  A domain created
+ * by plbgpu_cp_add_domain is all BGK with the given omega, non-periodic,
+ * FP64, exactly like D3Q19ExampleCoProcessor3D (coProcessor3D.hh:36-76);
+ * `data` holds 19 doubles per cell of the sub-box, so nbytes = 152 * cells. */
+int plbgpu_cp_add_domain(plbgpu_ctx* ctx, long nx, long ny, long nz, double omega, int* handle);
+int plbgpu_cp_send(plbgpu_ctx* ctx, int handle, long x0, long x1, long y0, long y1, long z0, long z1,
+                   const char* data, size_t nbytes);
+int plbgpu_cp_receive(plbgpu_ctx* ctx, int handle, long x0, long x1, long y0, long y1, long z0, long z1,
+                      char* data, size_t nbytes);
+int plbgpu_cp_collide_and_stream(plbgpu_ctx* ctx, int handle);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PLBGPU_H */

@@ -1,0 +1,767 @@
+// C-ABI implementation (include/plbgpu.h): contexts, domains, transfers,
+// time stepping and reductions on one GPU.
+//
+// A domain is one rectangular lattice in a single device allocation:
+//   [ 19 population planes | cell kinds ]
+// plus, allocated on first need, the face values (3 FP64 planes), the Guo
+// force (3 planes, FP64 for the FP64 form and FP32 otherwise) and the
+// momentum-exchange fluid-direction masks.
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/plbgpu.h"
+#include "launch.h"
+
+using namespace plbgpu;
+
+namespace {
+
+struct Domain {
+    int nx = 0, ny = 0, nz = 0;
+    int precision = PLBGPU_FP64;
+    int per[3] = {0, 0, 0};
+    double omega = 1.0, rho0 = 1.0, bbRho = 0.0;
+    long long n = 0, stride = 0;
+    size_t elemSize = 8;
+    void* arena = nullptr;       // populations + kinds
+    uint8_t* flags = nullptr;
+    double* bc = nullptr;        // 3 * n
+    void* force = nullptr;       // 3 * n of FP64 or FP32
+    uint32_t* mebb = nullptr;    // n
+    StatsAcc* stats = nullptr;   // device accumulator
+    ReduceAcc* red = nullptr;
+    bool odd = false;            // AA parity of the stored state
+    bool pending = false;        // faces still need their post-stream completion
+    bool statsValid = false;
+    double lastStats[7] = {0, 0, 0, 0, 0, 0, 0};
+    unsigned long long deviceBytes = 0;
+
+    DevLattice view() const {
+        DevLattice L;
+        L.pop = arena;
+        L.stride = stride;
+        L.flags = flags;
+        L.mebb = mebb;
+        L.bc = bc;
+        L.force = force;
+        L.nx = nx; L.ny = ny; L.nz = nz;
+        L.per[0] = per[0]; L.per[1] = per[1]; L.per[2] = per[2];
+        L.n = n;
+        return L;
+    }
+};
+
+}  // namespace
+
+struct plbgpu_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string lastError;
+    std::map<int, std::unique_ptr<Domain>> domains;
+    int nextHandle = 0;
+    unsigned long long launches = 0;
+    void* staging = nullptr;     // device staging buffer for transfers
+    size_t stagingBytes = 0;
+};
+
+namespace {
+
+int fail(plbgpu_ctx* c, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (c) c->lastError = buf;
+    return code;
+}
+
+#define CUDA_TRY(ctx, call)                                                                       \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? PLBGPU_ERR_NOMEM : PLBGPU_ERR_CUDA,  \
+                        "%s failed: %s", #call, cudaGetErrorString(e_));                           \
+    } while (0)
+
+const Launchers& launchers(int precision) {
+    switch (precision) {
+    case PLBGPU_FP32: return launchersFp32();
+    case PLBGPU_BF16: return launchersBf16();
+    case PLBGPU_FP16: return launchersFp16();
+    default: return launchersFp64();
+    }
+}
+
+size_t elemSizeOf(int precision) {
+    return precision == PLBGPU_FP64 ? 8 : precision == PLBGPU_FP32 ? 4 : 2;
+}
+
+int lookup(plbgpu_ctx* c, int h, Domain** d) {
+    if (!c) return PLBGPU_ERR_ARG;
+    auto it = c->domains.find(h);
+    if (it == c->domains.end()) return fail(c, PLBGPU_ERR_HANDLE, "unknown domain handle %d", h);
+    *d = it->second.get();
+    return PLBGPU_OK;
+}
+
+int checkBox(plbgpu_ctx* c, const Domain* d, int x0, int x1, int y0, int y1, int z0, int z1, Box* b) {
+    if (x0 < 0 || y0 < 0 || z0 < 0 || x1 >= d->nx || y1 >= d->ny || z1 >= d->nz || x0 > x1 || y0 > y1 ||
+        z0 > z1)
+        return fail(c, PLBGPU_ERR_ARG, "box [%d,%d]x[%d,%d]x[%d,%d] outside the %dx%dx%d domain", x0, x1, y0,
+                    y1, z0, z1, d->nx, d->ny, d->nz);
+    b->x0 = x0; b->x1 = x1; b->y0 = y0; b->y1 = y1; b->z0 = z0; b->z1 = z1;
+    return PLBGPU_OK;
+}
+
+long long boxCells(const Box& b) {
+    return (long long)(b.x1 - b.x0 + 1) * (b.y1 - b.y0 + 1) * (b.z1 - b.z0 + 1);
+}
+
+int ensureStaging(plbgpu_ctx* c, size_t bytes) {
+    if (c->stagingBytes >= bytes) return PLBGPU_OK;
+    if (c->staging) {
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+        cudaFree(c->staging);
+        c->staging = nullptr;
+        c->stagingBytes = 0;
+    }
+    CUDA_TRY(c, cudaMalloc(&c->staging, bytes));
+    c->stagingBytes = bytes;
+    return PLBGPU_OK;
+}
+
+// ---------------------------------------------------------------- small kernels
+
+__global__ void fillKindsKernel(uint8_t* flags, int ny, int nz, Box b, uint8_t k) {
+    const int bnz = b.z1 - b.z0 + 1;
+    const int dz = blockIdx.x * blockDim.x + threadIdx.x;
+    if (dz >= bnz) return;
+    long long idx = ((long long)(b.x0 + blockIdx.z) * ny + (b.y0 + blockIdx.y)) * nz + b.z0 + dz;
+    flags[idx] = k;
+}
+
+// Scatter (dir=0) or gather (dir=1) of `comps` values of type V per cell
+// between a packed box buffer and `planes` (component c at planes[c*n + idx]).
+template <typename V, typename W>
+__global__ void boxPlanesKernel(V* planes, long long n, int ny, int nz, Box b, W* packed, int comps,
+                                int gather) {
+    const int bnz = b.z1 - b.z0 + 1, bny = b.y1 - b.y0 + 1;
+    const int dz = blockIdx.x * blockDim.x + threadIdx.x;
+    if (dz >= bnz) return;
+    long long idx = ((long long)(b.x0 + blockIdx.z) * ny + (b.y0 + blockIdx.y)) * nz + b.z0 + dz;
+    long long o = (((long long)blockIdx.z * bny + blockIdx.y) * bnz + dz) * comps;
+    for (int c = 0; c < comps; ++c) {
+        if (gather) packed[o + c] = (W)planes[c * n + idx];
+        else planes[c * n + idx] = (V)packed[o + c];
+    }
+}
+
+template <typename V>
+__global__ void boxPlanesConstKernel(V* planes, long long n, int ny, int nz, Box b, double v0, double v1,
+                                     double v2, int comps) {
+    const int bnz = b.z1 - b.z0 + 1;
+    const int dz = blockIdx.x * blockDim.x + threadIdx.x;
+    if (dz >= bnz) return;
+    long long idx = ((long long)(b.x0 + blockIdx.z) * ny + (b.y0 + blockIdx.y)) * nz + b.z0 + dz;
+    double v[3] = {v0, v1, v2};
+    for (int c = 0; c < comps; ++c) planes[c * n + idx] = (V)v[c];
+}
+
+// InitializeMomentumExchangeFunctional3D (bounceBackModels3D.hh:42-90): fluid
+// directions of every momentum-exchange cell.  A neighbour outside a
+// non-periodic domain is an envelope cell with the background dynamics,
+// which counts as fluid.
+__global__ void mebbMaskKernel(DevLattice L, uint32_t* out) {
+    const int z = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, x = blockIdx.z;
+    if (z >= L.nz) return;
+    const long long idx = ((long long)x * L.ny + y) * L.nz + z;
+    uint32_t m = 0;
+    if (L.flags[idx] == K_MEBB) {
+        Neighbourhood nb = neighbourhood(L, x, y, z);
+        for (int i = 1; i < 19; ++i) {
+            long long off;
+            int pk = nb.move(i, +1, off) ? L.flags[idx + off] : K_BGK;
+            if (pk != K_MEBB && pk != K_BB && pk != K_NODYN) m |= 1u << i;
+        }
+    }
+    out[idx] = m;
+}
+
+__global__ void kindMaskKernel(const uint8_t* flags, long long n, unsigned long long* mask) {
+    unsigned long long m = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        int k = flags[i];
+        m |= 1ull << (k < 63 ? k : 63);
+    }
+    for (int o = 16; o > 0; o >>= 1) m |= __shfl_down_sync(0xffffffffu, m, o);
+    if ((threadIdx.x & 31) == 0 && m) atomicOr(mask, m);
+}
+
+int launchBox(plbgpu_ctx* c) {
+    c->launches += 1;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(c, PLBGPU_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
+    return PLBGPU_OK;
+}
+
+// Allocate the optional per-cell arrays the current kinds need.
+int ensureAux(plbgpu_ctx* c, Domain* d, bool needBc, bool needForce, bool needMebb) {
+    if (needBc && !d->bc) {
+        CUDA_TRY(c, cudaMalloc(&d->bc, sizeof(double) * 3 * d->n));
+        CUDA_TRY(c, cudaMemsetAsync(d->bc, 0, sizeof(double) * 3 * d->n, c->stream));
+        d->deviceBytes += sizeof(double) * 3 * d->n;
+    }
+    if (needForce && !d->force) {
+        size_t fs = d->precision == PLBGPU_FP64 ? sizeof(double) : sizeof(float);
+        CUDA_TRY(c, cudaMalloc(&d->force, fs * 3 * d->n));
+        CUDA_TRY(c, cudaMemsetAsync(d->force, 0, fs * 3 * d->n, c->stream));
+        d->deviceBytes += fs * 3 * d->n;
+    }
+    if (needMebb && !d->mebb) {
+        CUDA_TRY(c, cudaMalloc(&d->mebb, sizeof(uint32_t) * d->n));
+        CUDA_TRY(c, cudaMemsetAsync(d->mebb, 0, sizeof(uint32_t) * d->n, c->stream));
+        d->deviceBytes += sizeof(uint32_t) * d->n;
+    }
+    return PLBGPU_OK;
+}
+
+// Which kinds occur in the domain (bit k set for kind k).
+int kindMask(plbgpu_ctx* c, Domain* d, unsigned long long* mask) {
+    int rc = ensureStaging(c, 64);
+    if (rc) return rc;
+    unsigned long long* dm = static_cast<unsigned long long*>(c->staging);
+    CUDA_TRY(c, cudaMemsetAsync(dm, 0, sizeof(unsigned long long), c->stream));
+    kindMaskKernel<<<1024, 256, 0, c->stream>>>(d->flags, d->n, dm);
+    if ((rc = launchBox(c))) return rc;
+    CUDA_TRY(c, cudaMemcpyAsync(mask, dm, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return PLBGPU_OK;
+}
+
+int syncKinds(plbgpu_ctx* c, Domain* d) {
+    unsigned long long m = 0;
+    int rc = kindMask(c, d, &m);
+    if (rc) return rc;
+    bool faces = false;
+    for (int k = K_REGVEL; k < K_NKINDS; ++k) faces |= (m >> k) & 1;
+    return ensureAux(c, d, faces, (m >> K_GUO) & 1, (m >> K_MEBB) & 1);
+}
+
+StepConsts consts(const Domain* d) {
+    StepConsts s;
+    // bgk_ma2_collision_base (dynamicsTemplates3D.h:2290-2293) with
+    // t_0 = 1/3, t_1 = 1/18, t_4 = 1/36.
+    s.omega = d->omega;
+    s.one_m_omega = (double)1 - d->omega;
+    s.t0_omega = ((double)1 / (double)3) * d->omega;
+    s.t1_omega = ((double)1 / (double)18) * d->omega;
+    s.t4_omega = ((double)1 / (double)36) * d->omega;
+    s.invRho0 = (double)1 / d->rho0;
+    s.pending = d->pending ? 1 : 0;
+    return s;
+}
+
+// Complete pending faces in place so that the stored state is the
+// reference's post-step state again.
+int materialize(plbgpu_ctx* c, Domain* d) {
+    if (!d->pending) return PLBGPU_OK;
+    if (d->bc) {
+        int n = launchers(d->precision).completeFaces(d->view(), d->odd, c->stream);
+        c->launches += n - 1;
+        int rc = launchBox(c);
+        if (rc) return rc;
+    }
+    d->pending = false;
+    return PLBGPU_OK;
+}
+
+}  // namespace
+
+// =================================================================== C ABI
+
+extern "C" {
+
+int plbgpu_create(int device, plbgpu_ctx** out) {
+    if (!out) return PLBGPU_ERR_ARG;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return PLBGPU_ERR_CUDA;
+    if (device < 0 || device >= count) return PLBGPU_ERR_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) return PLBGPU_ERR_CUDA;
+    plbgpu_ctx* c = new (std::nothrow) plbgpu_ctx();
+    if (!c) return PLBGPU_ERR_NOMEM;
+    c->device = device;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return PLBGPU_ERR_CUDA;
+    }
+    *out = c;
+    return PLBGPU_OK;
+}
+
+int plbgpu_destroy(plbgpu_ctx* c) {
+    if (!c) return PLBGPU_ERR_ARG;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    std::vector<int> hs;
+    for (auto& kv : c->domains) hs.push_back(kv.first);
+    for (int h : hs) plbgpu_remove_domain(c, h);
+    if (c->staging) cudaFree(c->staging);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return PLBGPU_OK;
+}
+
+const char* plbgpu_last_error(const plbgpu_ctx* c) { return c ? c->lastError.c_str() : "null context"; }
+
+int plbgpu_launch_count(const plbgpu_ctx* c, unsigned long long* count) {
+    if (!c || !count) return PLBGPU_ERR_ARG;
+    *count = c->launches;
+    return PLBGPU_OK;
+}
+
+int plbgpu_get_stream(const plbgpu_ctx* c, void** stream) {
+    if (!c || !stream) return PLBGPU_ERR_ARG;
+    *stream = (void*)c->stream;
+    return PLBGPU_OK;
+}
+
+int plbgpu_synchronize(plbgpu_ctx* c) {
+    if (!c) return PLBGPU_ERR_ARG;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return PLBGPU_OK;
+}
+
+int plbgpu_add_domain(plbgpu_ctx* c, int nx, int ny, int nz, int precision, int* handle) {
+    if (!c || !handle) return PLBGPU_ERR_ARG;
+    // x and y index the grid's z and y dimensions (at most 65535 blocks each).
+    if (nx < 1 || ny < 1 || nz < 1 || nx > 65535 || ny > 65535)
+        return fail(c, PLBGPU_ERR_ARG, "domain extent %dx%dx%d (nx, ny must be in [1, 65535])", nx, ny, nz);
+    if (precision < PLBGPU_FP64 || precision > PLBGPU_FP16)
+        return fail(c, PLBGPU_ERR_ARG, "unknown precision %d", precision);
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    std::unique_ptr<Domain> d(new Domain());
+    d->nx = nx; d->ny = ny; d->nz = nz;
+    d->precision = precision;
+    d->n = (long long)nx * ny * nz;
+    d->stride = (d->n + 127) / 128 * 128;   // every plane starts on a 256-byte boundary
+    d->elemSize = elemSizeOf(precision);
+    size_t popBytes = d->elemSize * 19 * (size_t)d->stride;
+    size_t bytes = popBytes + (size_t)d->stride;
+    CUDA_TRY(c, cudaMalloc(&d->arena, bytes));
+    d->flags = static_cast<uint8_t*>(d->arena) + popBytes;
+    d->deviceBytes = bytes;
+    CUDA_TRY(c, cudaMemsetAsync(d->arena, 0, bytes, c->stream));   // f-bar = 0 (rest), all BGK
+    CUDA_TRY(c, cudaMalloc(&d->stats, sizeof(StatsAcc)));
+    CUDA_TRY(c, cudaMalloc(&d->red, sizeof(ReduceAcc)));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    int h = c->nextHandle++;
+    c->domains[h] = std::move(d);
+    *handle = h;
+    return PLBGPU_OK;
+}
+
+int plbgpu_remove_domain(plbgpu_ctx* c, int h) {
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    cudaStreamSynchronize(c->stream);
+    cudaFree(d->arena);
+    if (d->bc) cudaFree(d->bc);
+    if (d->force) cudaFree(d->force);
+    if (d->mebb) cudaFree(d->mebb);
+    cudaFree(d->stats);
+    cudaFree(d->red);
+    c->domains.erase(h);
+    return PLBGPU_OK;
+}
+
+int plbgpu_domain_info(plbgpu_ctx* c, int h, int* nx, int* ny, int* nz, int* precision,
+                       unsigned long long* device_bytes) {
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if (nx) *nx = d->nx;
+    if (ny) *ny = d->ny;
+    if (nz) *nz = d->nz;
+    if (precision) *precision = d->precision;
+    if (device_bytes) *device_bytes = d->deviceBytes;
+    return PLBGPU_OK;
+}
+
+int plbgpu_set_periodicity(plbgpu_ctx* c, int h, int px, int py, int pz) {
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    // The stored AA state of an odd step depends on the neighbourhood: bring
+    // it back to natural order first.
+    if (d->odd) {
+        std::vector<double> tmp((size_t)d->n * 19);
+        if ((rc = plbgpu_receive(c, h, 0, d->nx - 1, 0, d->ny - 1, 0, d->nz - 1, tmp.data(), tmp.size()))) return rc;
+        d->per[0] = px != 0; d->per[1] = py != 0; d->per[2] = pz != 0;
+        d->odd = false;
+        return plbgpu_send(c, h, 0, d->nx - 1, 0, d->ny - 1, 0, d->nz - 1, tmp.data(), tmp.size());
+    }
+    d->per[0] = px != 0; d->per[1] = py != 0; d->per[2] = pz != 0;
+    return PLBGPU_OK;
+}
+
+int plbgpu_set_params(plbgpu_ctx* c, int h, double omega, double rho0, double bb_rho) {
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if (!(rho0 != 0.0)) return fail(c, PLBGPU_ERR_ARG, "rho0 must be non-zero");
+    d->omega = omega;
+    d->rho0 = rho0;
+    d->bbRho = bb_rho;
+    return PLBGPU_OK;
+}
+
+int plbgpu_define_dynamics(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, int kind) {
+    Domain* d;
+    Box b;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if ((rc = checkBox(c, d, x0, x1, y0, y1, z0, z1, &b))) return rc;
+    if (kind < 0 || kind >= K_NKINDS) return fail(c, PLBGPU_ERR_ARG, "unknown cell kind %d", kind);
+    if ((rc = materialize(c, d))) return rc;
+    fillKindsKernel<<<rowGrid(z1 - z0 + 1, y1 - y0 + 1, x1 - x0 + 1, 128), 128, 0, c->stream>>>(
+        d->flags, d->ny, d->nz, b, (uint8_t)kind);
+    if ((rc = launchBox(c))) return rc;
+    return syncKinds(c, d);
+}
+
+int plbgpu_set_kinds(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, const uint8_t* kinds,
+                     size_t n) {
+    Domain* d;
+    Box b;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if ((rc = checkBox(c, d, x0, x1, y0, y1, z0, z1, &b))) return rc;
+    long long cells = boxCells(b);
+    if (!kinds || (long long)n != cells) return fail(c, PLBGPU_ERR_ARG, "kinds: %zu values for %lld cells", n, cells);
+    for (size_t i = 0; i < n; ++i)
+        if (kinds[i] >= K_NKINDS && kinds[i] != K_NONE) return fail(c, PLBGPU_ERR_ARG, "unknown cell kind %d", kinds[i]);
+    if ((rc = materialize(c, d))) return rc;
+    if ((rc = ensureStaging(c, n))) return rc;
+    CUDA_TRY(c, cudaMemcpyAsync(c->staging, kinds, n, cudaMemcpyHostToDevice, c->stream));
+    boxPlanesKernel<uint8_t, uint8_t><<<rowGrid(z1 - z0 + 1, y1 - y0 + 1, x1 - x0 + 1, 128), 128, 0, c->stream>>>(
+        d->flags, d->n, d->ny, d->nz, b, static_cast<uint8_t*>(c->staging), 1, 0);
+    if ((rc = launchBox(c))) return rc;
+    return syncKinds(c, d);
+}
+
+int plbgpu_get_kinds(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, uint8_t* kinds,
+                     size_t n) {
+    Domain* d;
+    Box b;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if ((rc = checkBox(c, d, x0, x1, y0, y1, z0, z1, &b))) return rc;
+    long long cells = boxCells(b);
+    if (!kinds || (long long)n != cells) return fail(c, PLBGPU_ERR_ARG, "kinds: %zu values for %lld cells", n, cells);
+    if ((rc = ensureStaging(c, n))) return rc;
+    boxPlanesKernel<uint8_t, uint8_t><<<rowGrid(z1 - z0 + 1, y1 - y0 + 1, x1 - x0 + 1, 128), 128, 0, c->stream>>>(
+        d->flags, d->n, d->ny, d->nz, b, static_cast<uint8_t*>(c->staging), 1, 1);
+    if ((rc = launchBox(c))) return rc;
+    CUDA_TRY(c, cudaMemcpyAsync(kinds, c->staging, n, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return PLBGPU_OK;
+}
+
+namespace {
+
+// Values for the face / force planes of a box.  comps = 3 (velocity, force) or
+// 1 (density); `field` non-null = one set of values per cell.
+int setPlanes(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, bool forcePlanes, int comps,
+              const double* field, size_t n, double v0, double v1, double v2) {
+    Domain* d;
+    Box b;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if ((rc = checkBox(c, d, x0, x1, y0, y1, z0, z1, &b))) return rc;
+    long long cells = boxCells(b);
+    if (field && (long long)n != cells * comps)
+        return fail(c, PLBGPU_ERR_ARG, "expected %lld values, got %zu", cells * comps, n);
+    if ((rc = materialize(c, d))) return rc;   // faces pending on old values complete with the old values
+    if ((rc = ensureAux(c, d, !forcePlanes, forcePlanes, false))) return rc;
+    dim3 g = rowGrid(z1 - z0 + 1, y1 - y0 + 1, x1 - x0 + 1, 128);
+    bool f32 = forcePlanes && d->precision != PLBGPU_FP64;
+    if (field) {
+        if ((rc = ensureStaging(c, sizeof(double) * n))) return rc;
+        CUDA_TRY(c, cudaMemcpyAsync(c->staging, field, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+        double* src = static_cast<double*>(c->staging);
+        if (f32)
+            boxPlanesKernel<float, double><<<g, 128, 0, c->stream>>>(static_cast<float*>(d->force), d->n, d->ny, d->nz, b, src, comps, 0);
+        else
+            boxPlanesKernel<double, double><<<g, 128, 0, c->stream>>>(
+                forcePlanes ? static_cast<double*>(d->force) : d->bc, d->n, d->ny, d->nz, b, src, comps, 0);
+    } else {
+        if (f32)
+            boxPlanesConstKernel<float><<<g, 128, 0, c->stream>>>(static_cast<float*>(d->force), d->n, d->ny, d->nz, b, v0, v1, v2, comps);
+        else
+            boxPlanesConstKernel<double><<<g, 128, 0, c->stream>>>(
+                forcePlanes ? static_cast<double*>(d->force) : d->bc, d->n, d->ny, d->nz, b, v0, v1, v2, comps);
+    }
+    if ((rc = launchBox(c))) return rc;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return PLBGPU_OK;
+}
+
+}  // namespace
+
+int plbgpu_set_boundary_velocity(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, double ux,
+                                 double uy, double uz) {
+    return setPlanes(c, h, x0, x1, y0, y1, z0, z1, false, 3, nullptr, 0, ux, uy, uz);
+}
+int plbgpu_set_boundary_velocity_field(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1,
+                                       const double* values, size_t n) {
+    if (!values) return fail(c, PLBGPU_ERR_ARG, "null values");
+    return setPlanes(c, h, x0, x1, y0, y1, z0, z1, false, 3, values, n, 0, 0, 0);
+}
+int plbgpu_set_boundary_density(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, double rho) {
+    return setPlanes(c, h, x0, x1, y0, y1, z0, z1, false, 1, nullptr, 0, rho, 0, 0);
+}
+int plbgpu_set_boundary_density_field(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1,
+                                      const double* values, size_t n) {
+    if (!values) return fail(c, PLBGPU_ERR_ARG, "null values");
+    return setPlanes(c, h, x0, x1, y0, y1, z0, z1, false, 1, values, n, 0, 0, 0);
+}
+int plbgpu_set_force(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, double fx, double fy,
+                     double fz) {
+    return setPlanes(c, h, x0, x1, y0, y1, z0, z1, true, 3, nullptr, 0, fx, fy, fz);
+}
+int plbgpu_set_force_field(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1,
+                           const double* values, size_t n) {
+    if (!values) return fail(c, PLBGPU_ERR_ARG, "null values");
+    return setPlanes(c, h, x0, x1, y0, y1, z0, z1, true, 3, values, n, 0, 0, 0);
+}
+
+int plbgpu_initialize_momentum_exchange(plbgpu_ctx* c, int h) {
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if ((rc = ensureAux(c, d, false, false, true))) return rc;
+    mebbMaskKernel<<<rowGrid(d->nz, d->ny, d->nx, 128), 128, 0, c->stream>>>(d->view(), d->mebb);
+    if ((rc = launchBox(c))) return rc;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return PLBGPU_OK;
+}
+
+namespace {
+int equilibrium(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, const double* field, size_t n,
+                double rho, double ux, double uy, double uz) {
+    Domain* d;
+    Box b;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if ((rc = checkBox(c, d, x0, x1, y0, y1, z0, z1, &b))) return rc;
+    long long cells = boxCells(b);
+    if (field && (long long)n != 4 * cells) return fail(c, PLBGPU_ERR_ARG, "expected %lld values, got %zu", 4 * cells, n);
+    if ((rc = materialize(c, d))) return rc;
+    const double* src = nullptr;
+    if (field) {
+        if ((rc = ensureStaging(c, sizeof(double) * n))) return rc;
+        CUDA_TRY(c, cudaMemcpyAsync(c->staging, field, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+        src = static_cast<const double*>(c->staging);
+    }
+    double cst[4] = {rho, ux, uy, uz};
+    int k = launchers(d->precision).equilibrium(d->view(), d->odd, b, src, cst, (double)1 / d->rho0, c->stream);
+    c->launches += k - 1;
+    if ((rc = launchBox(c))) return rc;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    d->statsValid = false;
+    return PLBGPU_OK;
+}
+}  // namespace
+
+int plbgpu_initialize_at_equilibrium(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1,
+                                     double rho, double ux, double uy, double uz) {
+    return equilibrium(c, h, x0, x1, y0, y1, z0, z1, nullptr, 0, rho, ux, uy, uz);
+}
+int plbgpu_initialize_at_equilibrium_field(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1,
+                                           const double* rho_u, size_t n) {
+    if (!rho_u) return fail(c, PLBGPU_ERR_ARG, "null values");
+    return equilibrium(c, h, x0, x1, y0, y1, z0, z1, rho_u, n, 0, 0, 0, 0);
+}
+
+int plbgpu_initialize(plbgpu_ctx* c, int h) {
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    // initialize() twice completes twice, like the reference.
+    if ((rc = materialize(c, d))) return rc;
+    d->pending = true;
+    return PLBGPU_OK;
+}
+
+int plbgpu_send(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, const double* buf, size_t n) {
+    Domain* d;
+    Box b;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if ((rc = checkBox(c, d, x0, x1, y0, y1, z0, z1, &b))) return rc;
+    long long cells = boxCells(b);
+    if (!buf || (long long)n != 19 * cells) return fail(c, PLBGPU_ERR_ARG, "send: %zu doubles for %lld cells", n, cells);
+    if ((rc = materialize(c, d))) return rc;
+    if ((rc = ensureStaging(c, sizeof(double) * n))) return rc;
+    CUDA_TRY(c, cudaMemcpyAsync(c->staging, buf, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    int k = launchers(d->precision).insert(d->view(), d->odd, b, static_cast<const double*>(c->staging), c->stream);
+    c->launches += k - 1;
+    if ((rc = launchBox(c))) return rc;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    d->statsValid = false;
+    return PLBGPU_OK;
+}
+
+int plbgpu_receive(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, double* buf, size_t n) {
+    Domain* d;
+    Box b;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if ((rc = checkBox(c, d, x0, x1, y0, y1, z0, z1, &b))) return rc;
+    long long cells = boxCells(b);
+    if (!buf || (long long)n != 19 * cells) return fail(c, PLBGPU_ERR_ARG, "receive: %zu doubles for %lld cells", n, cells);
+    if ((rc = ensureStaging(c, sizeof(double) * n))) return rc;
+    int k = launchers(d->precision).extract(d->view(), d->odd, b, d->pending && d->bc ? 1 : 0,
+                                            static_cast<double*>(c->staging), c->stream);
+    c->launches += k - 1;
+    if ((rc = launchBox(c))) return rc;
+    CUDA_TRY(c, cudaMemcpyAsync(buf, c->staging, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return PLBGPU_OK;
+}
+
+int plbgpu_collide_and_stream(plbgpu_ctx* c, int h, int nsteps, int collect_stats) {
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if (nsteps < 0) return fail(c, PLBGPU_ERR_ARG, "nsteps %d", nsteps);
+    if (nsteps == 0) return PLBGPU_OK;
+    const Launchers& L = launchers(d->precision);
+    bool hasFaces = d->bc != nullptr;
+    for (int s = 0; s < nsteps; ++s) {
+        bool stats = collect_stats && s == nsteps - 1;
+        if (stats) CUDA_TRY(c, cudaMemsetAsync(d->stats, 0, sizeof(StatsAcc), c->stream));
+        StepConsts k = consts(d);
+        int nl = L.step(d->view(), d->odd, stats, k, d->stats, c->stream);
+        c->launches += nl - 1;
+        if ((rc = launchBox(c))) return rc;
+        d->odd = !d->odd;
+        d->pending = hasFaces;
+    }
+    if (collect_stats) d->statsValid = true;
+    return PLBGPU_OK;
+}
+
+int plbgpu_get_stats(plbgpu_ctx* c, int h, double out[7]) {
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if (!out) return PLBGPU_ERR_ARG;
+    if (!d->statsValid) return fail(c, PLBGPU_ERR_STATE, "no step has gathered statistics since the last change");
+    StatsAcc a;
+    CUDA_TRY(c, cudaMemcpyAsync(&a, d->stats, sizeof(StatsAcc), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    double cnt = (double)a.count;
+    double mx;
+    memcpy(&mx, &a.maxBits, sizeof(double));
+    out[0] = a.count ? a.sumRhoBar / cnt : 0.;
+    out[1] = a.count ? a.sumUSqr / cnt : 0.;
+    out[2] = a.count ? mx : -1.79769313486231570815e+308;
+    out[3] = a.drag[0];
+    out[4] = a.drag[1];
+    out[5] = a.drag[2];
+    out[6] = cnt;
+    return PLBGPU_OK;
+}
+
+int plbgpu_reduce(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, double* avg_energy,
+                  double* avg_density) {
+    Domain* d;
+    Box b;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if ((rc = checkBox(c, d, x0, x1, y0, y1, z0, z1, &b))) return rc;
+    CUDA_TRY(c, cudaMemsetAsync(d->red, 0, sizeof(ReduceAcc), c->stream));
+    int k = launchers(d->precision).reduce(d->view(), d->odd, b, d->pending && d->bc ? 1 : 0, (double)1 / d->rho0,
+                                           d->bbRho - (double)1, d->red, c->stream);
+    c->launches += k - 1;
+    if ((rc = launchBox(c))) return rc;
+    ReduceAcc a;
+    CUDA_TRY(c, cudaMemcpyAsync(&a, d->red, sizeof(ReduceAcc), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    double cells = (double)boxCells(b);
+    if (avg_energy) *avg_energy = a.sumEnergy / (double)2 / cells;
+    if (avg_density) *avg_density = a.sumRhoBar / cells + (double)1;
+    return PLBGPU_OK;
+}
+
+int plbgpu_time_steps(plbgpu_ctx* c, int h, int nsteps, int collect_stats, float* ms) {
+    if (!c || !ms) return PLBGPU_ERR_ARG;
+    cudaEvent_t e0, e1;
+    CUDA_TRY(c, cudaEventCreate(&e0));
+    CUDA_TRY(c, cudaEventCreate(&e1));
+    CUDA_TRY(c, cudaEventRecord(e0, c->stream));
+    int rc = plbgpu_collide_and_stream(c, h, nsteps, collect_stats);
+    if (rc) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return rc;
+    }
+    CUDA_TRY(c, cudaEventRecord(e1, c->stream));
+    CUDA_TRY(c, cudaEventSynchronize(e1));
+    CUDA_TRY(c, cudaEventElapsedTime(ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return PLBGPU_OK;
+}
+
+// ------------------------------------------------------------ co-processor form
+
+int plbgpu_cp_add_domain(plbgpu_ctx* c, long nx, long ny, long nz, double omega, int* handle) {
+    if (!c || !handle || nx < 1 || ny < 1 || nz < 1 || nx > (1 << 30) || ny > (1 << 30) || nz > (1 << 30)) return 0;
+    int h;
+    if (plbgpu_add_domain(c, (int)nx, (int)ny, (int)nz, PLBGPU_FP64, &h) != PLBGPU_OK) return 0;
+    if (plbgpu_set_params(c, h, omega, 1.0, 0.0) != PLBGPU_OK) return 0;
+    *handle = h;
+    return 1;
+}
+
+int plbgpu_cp_send(plbgpu_ctx* c, int handle, long x0, long x1, long y0, long y1, long z0, long z1, const char* data,
+                   size_t nbytes) {
+    if (nbytes % (19 * sizeof(double))) {
+        fail(c, PLBGPU_ERR_ARG, "co-processor send: %zu bytes is not a whole number of D3Q19 cells", nbytes);
+        return 0;
+    }
+    return plbgpu_send(c, handle, (int)x0, (int)x1, (int)y0, (int)y1, (int)z0, (int)z1,
+                       reinterpret_cast<const double*>(data), nbytes / sizeof(double)) == PLBGPU_OK;
+}
+
+int plbgpu_cp_receive(plbgpu_ctx* c, int handle, long x0, long x1, long y0, long y1, long z0, long z1, char* data,
+                      size_t nbytes) {
+    if (nbytes % (19 * sizeof(double))) {
+        fail(c, PLBGPU_ERR_ARG, "co-processor receive: %zu bytes is not a whole number of D3Q19 cells", nbytes);
+        return 0;
+    }
+    return plbgpu_receive(c, handle, (int)x0, (int)x1, (int)y0, (int)y1, (int)z0, (int)z1,
+                          reinterpret_cast<double*>(data), nbytes / sizeof(double)) == PLBGPU_OK;
+}
+
+int plbgpu_cp_collide_and_stream(plbgpu_ctx* c, int handle) {
+    // Blocking, as the interface requires (coProcessor3D.h:107-115).
+    if (plbgpu_collide_and_stream(c, handle, 1, 0) != PLBGPU_OK) return 0;
+    return plbgpu_synchronize(c) == PLBGPU_OK;
+}
+
+}  // extern "C"

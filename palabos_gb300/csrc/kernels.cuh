@@ -1,0 +1,446 @@
+// Device kernels of the D3Q19 lattice: fused collide-and-stream in the AA
+// pattern, state transfer in the canonical co-processor layout, reductions.
+//
+// Storage: structure of arrays.  Population i of cell c lives at
+// pop[i * stride + c], c = (x * ny + y) * nz + z.  Values are f-bar (f - t_i),
+// the reference's own stored representation (roundOffPolicy.h:40-89), in the
+// storage type S (double, float, bfloat16 or half).
+//
+// AA pattern (in place, one array):
+//   even step  read slot i of cell x, collide, write f*_i to slot opp(i) of x;
+//   odd step   read slot opp(i) of x - c_i, collide, write f*_i to slot i of
+//              x + c_i.
+// After an odd step the array is in natural order again.  A population whose
+// source or destination lies outside a non-periodic domain stays in its own
+// cell with the direction reversed, which is the reference swap algorithm's
+// border rule (atomicBlock/blockLattice3D.hh:403-427).  Periodic axes wrap,
+// which is what the periodic envelopes of MultiBlockLattice3D amount to
+// (multiBlock/multiBlockLattice3D.hh:253-357).
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cstdint>
+
+#include "d3q19.cuh"
+
+namespace plbgpu {
+
+template <typename S> struct StoreT;
+template <> struct StoreT<double> {
+    using R = double; using F = double;
+    static __device__ __forceinline__ double ld(const double* p) { return *p; }
+    static __device__ __forceinline__ void st(double* p, double v) { *p = v; }
+};
+template <> struct StoreT<float> {
+    using R = float; using F = float;
+    static __device__ __forceinline__ float ld(const float* p) { return *p; }
+    static __device__ __forceinline__ void st(float* p, float v) { *p = v; }
+};
+template <> struct StoreT<__nv_bfloat16> {
+    using R = float; using F = float;
+    static __device__ __forceinline__ float ld(const __nv_bfloat16* p) { return __bfloat162float(*p); }
+    static __device__ __forceinline__ void st(__nv_bfloat16* p, float v) { *p = __float2bfloat16_rn(v); }
+};
+template <> struct StoreT<__half> {
+    using R = float; using F = float;
+    static __device__ __forceinline__ float ld(const __half* p) { return __half2float(*p); }
+    static __device__ __forceinline__ void st(__half* p, float v) { *p = __float2half_rn(v); }
+};
+
+struct DevLattice {
+    void* pop;              // 19 planes of `stride` elements of the storage type
+    long long stride;       // elements per plane (>= n, padded)
+    const uint8_t* flags;   // n
+    const uint32_t* mebb;   // n, fluid-direction masks of momentum-exchange cells (or null)
+    const double* bc;       // 3 planes of n: face velocity / density (or null)
+    const void* force;      // 3 planes of n: Guo force in F (or null)
+    int nx, ny, nz;
+    int per[3];
+    long long n;
+};
+
+template <typename R>
+struct StepParams {
+    BgkConst<R> bgk;
+    R invRho0;      // incompressible BGK 1/rho0
+    int pending;    // boundary faces still need their post-stream completion
+};
+
+struct StatsAcc {
+    double sumRhoBar;
+    double sumUSqr;
+    unsigned long long count;
+    unsigned long long maxBits;   // bit pattern of the max (non-negative doubles order as integers)
+    double drag[3];
+    double pad;
+};
+
+struct ReduceAcc {
+    double sumEnergy;   // sum |u|^2
+    double sumRhoBar;
+};
+
+// Offsets along one axis for a move of -1 / +1, or "invalid" outside a
+// non-periodic domain.
+struct AxisMoves {
+    long long offM, offP;
+    bool okM, okP;
+};
+
+__device__ __forceinline__ AxisMoves axisMoves(int p, int n, int per, long long stride) {
+    AxisMoves a;
+    a.okM = (p > 0) || per;
+    a.okP = (p < n - 1) || per;
+    a.offM = (p > 0) ? -stride : (long long)(n - 1) * stride;
+    a.offP = (p < n - 1) ? stride : -(long long)(n - 1) * stride;
+    return a;
+}
+
+struct Neighbourhood {
+    AxisMoves ax, ay, az;
+    // Move by s * c_i; returns false when leaving a non-periodic domain.
+    __device__ __forceinline__ bool move(int i, int s, long long& off) const {
+        int cx = s * cdir(i, 0), cy = s * cdir(i, 1), cz = s * cdir(i, 2);
+        bool ok = true;
+        off = 0;
+        if (cx < 0) { ok &= ax.okM; off += ax.offM; } else if (cx > 0) { ok &= ax.okP; off += ax.offP; }
+        if (cy < 0) { ok &= ay.okM; off += ay.offM; } else if (cy > 0) { ok &= ay.okP; off += ay.offP; }
+        if (cz < 0) { ok &= az.okM; off += az.offM; } else if (cz > 0) { ok &= az.okP; off += az.offP; }
+        return ok;
+    }
+};
+
+__device__ __forceinline__ Neighbourhood neighbourhood(const DevLattice& L, int x, int y, int z) {
+    Neighbourhood nb;
+    nb.ax = axisMoves(x, L.nx, L.per[0], (long long)L.ny * L.nz);
+    nb.ay = axisMoves(y, L.ny, L.per[1], (long long)L.nz);
+    nb.az = axisMoves(z, L.nz, L.per[2], 1);
+    return nb;
+}
+
+// Read the 19 post-stream populations of cell idx for the given parity.
+template <typename S, bool ODD>
+__device__ __forceinline__ void loadCell(const DevLattice& L, const Neighbourhood& nb, long long idx,
+                                         typename StoreT<S>::R* f) {
+    const S* P = static_cast<const S*>(L.pop);
+    const long long st = L.stride;
+    f[0] = StoreT<S>::ld(P + idx);
+#pragma unroll
+    for (int i = 1; i < 19; ++i) {
+        if (!ODD) {
+            f[i] = StoreT<S>::ld(P + i * st + idx);
+        } else {
+            long long off;
+            bool ok = nb.move(i, -1, off);
+            f[i] = ok ? StoreT<S>::ld(P + opp(i) * st + idx + off) : StoreT<S>::ld(P + i * st + idx);
+        }
+    }
+}
+
+// Write the 19 post-collision populations of cell idx for the given parity.
+template <typename S, bool ODD>
+__device__ __forceinline__ void storeCell(const DevLattice& L, const Neighbourhood& nb, long long idx,
+                                          const typename StoreT<S>::R* f) {
+    S* P = static_cast<S*>(L.pop);
+    const long long st = L.stride;
+    StoreT<S>::st(P + idx, f[0]);
+#pragma unroll
+    for (int i = 1; i < 19; ++i) {
+        if (!ODD) {
+            StoreT<S>::st(P + opp(i) * st + idx, f[i]);
+        } else {
+            long long off;
+            bool ok = nb.move(i, +1, off);
+            if (ok) StoreT<S>::st(P + i * st + idx + off, f[i]);
+            else StoreT<S>::st(P + opp(i) * st + idx, f[i]);
+        }
+    }
+}
+
+// Where f_i(x) of the post-stream state lives for the given parity (used by
+// the transfer kernels, which read and write the state in place).
+template <bool ODD>
+__device__ __forceinline__ long long slotOf(const DevLattice& L, const Neighbourhood& nb, long long idx, int i) {
+    if (!ODD || i == 0) return (long long)i * L.stride + idx;
+    long long off;
+    bool ok = nb.move(i, -1, off);
+    return ok ? (long long)opp(i) * L.stride + idx + off : (long long)i * L.stride + idx;
+}
+
+template <typename R>
+__device__ __forceinline__ void swapHalves(R* f) {
+#pragma unroll
+    for (int i = 1; i <= 9; ++i) {
+        R t = f[i]; f[i] = f[i + 9]; f[i + 9] = t;
+    }
+}
+
+template <typename R>
+__device__ __forceinline__ void completeIfFace(const DevLattice& L, long long idx, int k, R* f) {
+    double v[3] = {L.bc[idx], L.bc[L.n + idx], L.bc[2 * L.n + idx]};
+    R tmp[19];
+#pragma unroll
+    for (int i = 0; i < 19; ++i) tmp[i] = f[i];
+    completeFace<R>(tmp, k, v);
+#pragma unroll
+    for (int i = 0; i < 19; ++i) f[i] = tmp[i];
+}
+
+__device__ __forceinline__ double warpSum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ unsigned long long warpSumU(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ unsigned long long warpMaxU(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long w = __shfl_down_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+
+// One cell's collision; returns true when the cell gathers statistics.
+template <typename S>
+__device__ __forceinline__ bool collideCell(const DevLattice& L, const StepParams<typename StoreT<S>::R>& P,
+                                            long long idx, int k, typename StoreT<S>::R* f,
+                                            typename StoreT<S>::R& rhoBar, typename StoreT<S>::R& uSqr,
+                                            StatsAcc* acc, bool stats) {
+    using R = typename StoreT<S>::R;
+    using F = typename StoreT<S>::F;
+    R j[3];
+    if (k == K_BGK || isFace(k)) {
+        // isoThermalDynamics.hh:319-330; faces use their BGK base collide.
+        rhoBarJ<R>(f, rhoBar, j);
+        uSqr = bgkCollide<R>(f, rhoBar, j, P.bgk, invRhoOf(rhoBar));
+        return true;
+    }
+    switch (k) {
+    case K_GUO: {  // externalForceDynamics.hh:215-234
+        const F* fp = static_cast<const F*>(L.force);
+        R Fv[3] = {(R)fp[idx], (R)fp[L.n + idx], (R)fp[2 * L.n + idx]};
+        R rb = rhoBarSeq<R>(f);
+        R rb2, jj[3], u[3];
+        rhoBarJ<R>(f, rb2, jj);
+        R invRho = invRhoOf(rb2);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) u[d] = jj[d] * invRho + Fv[d] / (R)2;
+        R rho = rb + (R)1;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) j[d] = rho * u[d];
+        uSqr = bgkCollide<R>(f, rb, j, P.bgk, invRhoOf(rb));
+        addGuoForce<R>(f, Fv, u, P.bgk.omega);
+        rhoBar = rb;
+        return true;
+    }
+    case K_INCBGK:  // isoThermalDynamics.hh:1408-1419
+        rhoBarJ<R>(f, rhoBar, j);
+        uSqr = bgkCollide<R>(f, rhoBar, j, P.bgk, P.invRho0);
+        return true;
+    case K_BB:  // core/dynamics.hh:783-790
+        swapHalves(f);
+        return false;
+    case K_MEBB: {  // bounceBackModels.hh:100-136
+        if (stats) {
+            uint32_t mask = L.mebb[idx];
+            double mom[3] = {0., 0., 0.};
+#pragma unroll
+            for (int i = 1; i < 19; ++i) {
+                if (!(mask & (1u << i))) continue;
+                double fo = (double)f[opp(i)];
+                if (cdir(i, 0)) mom[0] += (double)2 * cdir(i, 0) * fo;
+                if (cdir(i, 1)) mom[1] += (double)2 * cdir(i, 1) * fo;
+                if (cdir(i, 2)) mom[2] += (double)2 * cdir(i, 2) * fo;
+            }
+            atomicAdd(&acc->drag[0], -mom[0]);
+            atomicAdd(&acc->drag[1], -mom[1]);
+            atomicAdd(&acc->drag[2], -mom[2]);
+        }
+        swapHalves(f);
+        return false;
+    }
+    default:  // K_NODYN, K_NONE
+        return false;
+    }
+}
+
+// Fused collide-and-stream for one time step.  One thread per cell; threads
+// run along z (the contiguous axis) so every population plane is read and
+// written in coalesced rows.
+template <typename S, bool ODD, bool STATS>
+__global__ void __launch_bounds__(128) stepKernel(DevLattice L, StepParams<typename StoreT<S>::R> P,
+                                                  StatsAcc* acc) {
+    using R = typename StoreT<S>::R;
+    const int z = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    const int x = blockIdx.z;
+    const bool active = z < L.nz;
+    R rhoBar = R(0), uSqr = R(0);
+    bool gathers = false;
+    if (active) {
+        const long long idx = ((long long)x * L.ny + y) * L.nz + z;
+        const int k = L.flags[idx];
+        if (k != K_NONE) {
+            Neighbourhood nb = neighbourhood(L, x, y, z);
+            R f[19];
+            loadCell<S, ODD>(L, nb, idx, f);
+            if (P.pending && isFace(k)) completeIfFace<R>(L, idx, k, f);
+            gathers = collideCell<S>(L, P, idx, k, f, rhoBar, uSqr, acc, STATS);
+            storeCell<S, ODD>(L, nb, idx, f);
+        }
+    }
+    if (STATS) {
+        double sR = gathers ? (double)rhoBar : 0.;
+        double sU = gathers ? (double)uSqr : 0.;
+        unsigned long long c = gathers ? 1ull : 0ull;
+        unsigned long long m = gathers ? (unsigned long long)__double_as_longlong((double)uSqr) : 0ull;
+        sR = warpSum(sR);
+        sU = warpSum(sU);
+        c = warpSumU(c);
+        m = warpMaxU(m);
+        if ((threadIdx.x & 31) == 0 && c > 0) {
+            atomicAdd(&acc->sumRhoBar, sR);
+            atomicAdd(&acc->sumUSqr, sU);
+            atomicAdd(&acc->count, c);
+            atomicMax(&acc->maxBits, m);
+        }
+    }
+}
+
+// Complete the boundary faces in place (used before a transfer into a state
+// whose faces are still pending).
+template <typename S, bool ODD>
+__global__ void completeFacesKernel(DevLattice L) {
+    using R = typename StoreT<S>::R;
+    const int z = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, x = blockIdx.z;
+    if (z >= L.nz) return;
+    const long long idx = ((long long)x * L.ny + y) * L.nz + z;
+    const int k = L.flags[idx];
+    if (!isFace(k)) return;
+    Neighbourhood nb = neighbourhood(L, x, y, z);
+    S* Pp = static_cast<S*>(L.pop);
+    R f[19];
+#pragma unroll
+    for (int i = 0; i < 19; ++i) f[i] = StoreT<S>::ld(Pp + slotOf<ODD>(L, nb, idx, i));
+    completeIfFace<R>(L, idx, k, f);
+#pragma unroll
+    for (int i = 0; i < 19; ++i) StoreT<S>::st(Pp + slotOf<ODD>(L, nb, idx, i), f[i]);
+}
+
+struct Box { int x0, x1, y0, y1, z0, z1; };
+
+// Canonical transfer layout: [x][y][z][19] over the box, z fastest, FP64.
+template <typename S, bool ODD>
+__global__ void extractKernel(DevLattice L, Box b, int pending, double* out) {
+    using R = typename StoreT<S>::R;
+    const int bnz = b.z1 - b.z0 + 1, bny = b.y1 - b.y0 + 1;
+    const int dz = blockIdx.x * blockDim.x + threadIdx.x;
+    if (dz >= bnz) return;
+    const int z = b.z0 + dz, y = b.y0 + blockIdx.y, x = b.x0 + blockIdx.z;
+    const long long idx = ((long long)x * L.ny + y) * L.nz + z;
+    const long long o = (((long long)blockIdx.z * bny + blockIdx.y) * bnz + dz) * 19;
+    const int k = L.flags[idx];
+    Neighbourhood nb = neighbourhood(L, x, y, z);
+    const S* Pp = static_cast<const S*>(L.pop);
+    R f[19];
+#pragma unroll
+    for (int i = 0; i < 19; ++i) f[i] = StoreT<S>::ld(Pp + slotOf<ODD>(L, nb, idx, i));
+    if (pending && isFace(k)) completeIfFace<R>(L, idx, k, f);
+#pragma unroll
+    for (int i = 0; i < 19; ++i) out[o + i] = (double)f[i];
+}
+
+template <typename S, bool ODD>
+__global__ void insertKernel(DevLattice L, Box b, const double* in) {
+    const int bnz = b.z1 - b.z0 + 1, bny = b.y1 - b.y0 + 1;
+    const int dz = blockIdx.x * blockDim.x + threadIdx.x;
+    if (dz >= bnz) return;
+    const int z = b.z0 + dz, y = b.y0 + blockIdx.y, x = b.x0 + blockIdx.z;
+    const long long idx = ((long long)x * L.ny + y) * L.nz + z;
+    const long long o = (((long long)blockIdx.z * bny + blockIdx.y) * bnz + dz) * 19;
+    Neighbourhood nb = neighbourhood(L, x, y, z);
+    S* Pp = static_cast<S*>(L.pop);
+#pragma unroll
+    for (int i = 0; i < 19; ++i)
+        StoreT<S>::st(Pp + slotOf<ODD>(L, nb, idx, i), (typename StoreT<S>::R)in[o + i]);
+}
+
+// computeAverageEnergy / computeAverageDensity (dataAnalysisWrapper3D.hh:1226-1262)
+// on the post-stream, face-completed state.  Accumulation is in FP64.
+template <typename S, bool ODD>
+__global__ void reduceKernel(DevLattice L, Box b, int pending, typename StoreT<S>::R invRho0,
+                             double bbRhoBar, ReduceAcc* acc) {
+    using R = typename StoreT<S>::R;
+    using F = typename StoreT<S>::F;
+    const int bnz = b.z1 - b.z0 + 1;
+    const int dz = blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0., r = 0.;
+    if (dz < bnz) {
+        const int z = b.z0 + dz, y = b.y0 + blockIdx.y, x = b.x0 + blockIdx.z;
+        const long long idx = ((long long)x * L.ny + y) * L.nz + z;
+        const int k = L.flags[idx];
+        if (k != K_NONE) {
+            Neighbourhood nb = neighbourhood(L, x, y, z);
+            const S* Pp = static_cast<const S*>(L.pop);
+            R f[19];
+#pragma unroll
+            for (int i = 0; i < 19; ++i) f[i] = StoreT<S>::ld(Pp + slotOf<ODD>(L, nb, idx, i));
+            if (pending && isFace(k)) completeIfFace<R>(L, idx, k, f);
+            R u[3] = {R(0), R(0), R(0)};
+            R rb = R(0);
+            if (k == K_BB || k == K_MEBB) {
+                rb = (R)bbRhoBar;
+            } else if (k == K_NODYN) {
+                rb = R(0);
+            } else if (k == K_BGK) {  // momentTemplates3D.h:402-408 compute_uLb
+                R jj[3], rr;
+                rhoBarJ<R>(f, rr, jj);
+                rb = rhoBarSeq<R>(f);
+                R invRho = invRhoOf(rb);
+                for (int d = 0; d < 3; ++d) u[d] = jj[d] * invRho;
+            } else if (k == K_GUO) {  // externalForceDynamics.hh:58-73
+                const F* fp = static_cast<const F*>(L.force);
+                R jj[3], rr;
+                rhoBarJ<R>(f, rr, jj);
+                R invRho = invRhoOf(rr);
+                R Fv[3] = {(R)fp[idx], (R)fp[L.n + idx], (R)fp[2 * L.n + idx]};
+                for (int d = 0; d < 3; ++d) u[d] = jj[d] * invRho + Fv[d] / (R)2;
+                rb = rhoBarSeq<R>(f);
+            } else if (k == K_INCBGK) {  // isoThermalDynamics.hh:1388-1395
+                R jj[3], rr;
+                rhoBarJ<R>(f, rr, jj);
+                for (int d = 0; d < 3; ++d) u[d] = jj[d] * invRho0;
+                rb = rhoBarSeq<R>(f);
+            } else if (isFace(k)) {
+                int fam = faceFamily(k), dir = faceDir(k), ori = faceOri(k);
+                double v[3] = {L.bc[idx], L.bc[L.n + idx], L.bc[2 * L.n + idx]};
+                if (fam == 0 || fam == 2) {  // stored velocity, boundaryDynamics.hh:324-330
+                    for (int d = 0; d < 3; ++d) u[d] = (R)v[d];
+                    rb = velFaceRhoBar<R>(f, dir, ori, (R)v[dir]);
+                } else {  // boundaryDynamics.hh:790-812
+                    rb = (R)v[0] - (R)1;
+                    pressFaceJ<R>(f, dir, ori, rb, u);
+                    R invRho = invRhoOf(rb);
+                    for (int d = 0; d < 3; ++d) { u[d] *= invRho; u[d] += (R)0.5 * (R)0; }
+                }
+            }
+            e = (double)(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+            r = (double)rb;
+        }
+    }
+    e = warpSum(e);
+    r = warpSum(r);
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&acc->sumEnergy, e);
+        atomicAdd(&acc->sumRhoBar, r);
+    }
+}
+
+}  // namespace plbgpu

@@ -1,0 +1,40 @@
+// Host-side launchers of the lattice kernels, one set per storage precision.
+// The FP64 set lives in a translation unit compiled without FMA contraction
+// (bit-exact with the reference); the FP32 / BF16 / FP16 sets in one compiled
+// with contraction.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "kernels.cuh"
+
+namespace plbgpu {
+
+struct StepConsts {
+    double omega, one_m_omega, t0_omega, t1_omega, t4_omega;
+    double invRho0;
+    int pending;
+};
+
+// Each launcher returns the number of kernels it launched.
+struct Launchers {
+    int (*step)(const DevLattice&, bool odd, bool stats, const StepConsts&, StatsAcc*, cudaStream_t);
+    int (*completeFaces)(const DevLattice&, bool odd, cudaStream_t);
+    int (*extract)(const DevLattice&, bool odd, Box, int pending, double* out, cudaStream_t);
+    int (*insert)(const DevLattice&, bool odd, Box, const double* in, cudaStream_t);
+    int (*reduce)(const DevLattice&, bool odd, Box, int pending, double invRho0, double bbRhoBar,
+                  ReduceAcc*, cudaStream_t);
+    int (*equilibrium)(const DevLattice&, bool odd, Box, const double* rhou, const double* cst,
+                       double invRho0, cudaStream_t);
+};
+
+const Launchers& launchersFp64();
+const Launchers& launchersFp32();
+const Launchers& launchersBf16();
+const Launchers& launchersFp16();
+
+inline dim3 rowGrid(int nz, int ny, int nx, int block) {
+    return dim3((unsigned)((nz + block - 1) / block), (unsigned)ny, (unsigned)nx);
+}
+
+}  // namespace plbgpu

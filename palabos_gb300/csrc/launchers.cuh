@@ -1,0 +1,108 @@
+// Launcher bodies, instantiated per storage type by step_fp64.cu and
+// step_mixed.cu.
+#pragma once
+
+#include "launch.h"
+
+namespace plbgpu {
+
+// initializeAtEquilibrium (dataInitializerWrapper3D.h:122-130 and
+// core/cell.hh iniCellAtEquilibrium): j = u * rho, f-bar_i = the cell's
+// computeEquilibrium(i, rho - 1, j, |j|^2); bounce-back and no-dynamics
+// cells return 0 (core/dynamics.hh:797-801).
+template <typename S, bool ODD>
+__global__ void equilibriumKernel(DevLattice L, Box b, const double* rhou, double c0, double c1,
+                                  double c2, double c3, double invRho0) {
+    using R = typename StoreT<S>::R;
+    const int bnz = b.z1 - b.z0 + 1, bny = b.y1 - b.y0 + 1;
+    const int dz = blockIdx.x * blockDim.x + threadIdx.x;
+    if (dz >= bnz) return;
+    const int z = b.z0 + dz, y = b.y0 + blockIdx.y, x = b.x0 + blockIdx.z;
+    const long long idx = ((long long)x * L.ny + y) * L.nz + z;
+    const int k = L.flags[idx];
+    if (k == K_NONE) return;
+    double rho = c0, ux = c1, uy = c2, uz = c3;
+    if (rhou) {
+        const long long o = (((long long)blockIdx.z * bny + blockIdx.y) * bnz + dz) * 4;
+        rho = rhou[o]; ux = rhou[o + 1]; uy = rhou[o + 2]; uz = rhou[o + 3];
+    }
+    R j[3] = {(R)ux * (R)rho, (R)uy * (R)rho, (R)uz * (R)rho};
+    R jSqr = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
+    R rhoBar = (R)rho - (R)1;
+    R invRho = (k == K_INCBGK) ? (R)invRho0 : invRhoOf(rhoBar);
+    Neighbourhood nb = neighbourhood(L, x, y, z);
+    S* Pp = static_cast<S*>(L.pop);
+    const bool zero = (k == K_BB || k == K_MEBB || k == K_NODYN);
+#pragma unroll
+    for (int i = 0; i < 19; ++i) {
+        R v = zero ? R(0) : bgkEq<R>(i, rhoBar, invRho, j, jSqr);
+        StoreT<S>::st(Pp + slotOf<ODD>(L, nb, idx, i), v);
+    }
+}
+
+template <typename S>
+struct LaunchImpl {
+    using R = typename StoreT<S>::R;
+    static constexpr int kBlock = 128;
+
+    static int step(const DevLattice& L, bool odd, bool stats, const StepConsts& c, StatsAcc* acc,
+                    cudaStream_t s) {
+        StepParams<R> p;
+        p.bgk.omega = (R)c.omega;
+        p.bgk.one_m_omega = (R)c.one_m_omega;
+        p.bgk.t0_omega = (R)c.t0_omega;
+        p.bgk.t1_omega = (R)c.t1_omega;
+        p.bgk.t4_omega = (R)c.t4_omega;
+        p.invRho0 = (R)c.invRho0;
+        p.pending = c.pending;
+        dim3 g = rowGrid(L.nz, L.ny, L.nx, kBlock);
+        if (odd) {
+            if (stats) stepKernel<S, true, true><<<g, kBlock, 0, s>>>(L, p, acc);
+            else stepKernel<S, true, false><<<g, kBlock, 0, s>>>(L, p, acc);
+        } else {
+            if (stats) stepKernel<S, false, true><<<g, kBlock, 0, s>>>(L, p, acc);
+            else stepKernel<S, false, false><<<g, kBlock, 0, s>>>(L, p, acc);
+        }
+        return 1;
+    }
+    static int completeFaces(const DevLattice& L, bool odd, cudaStream_t s) {
+        dim3 g = rowGrid(L.nz, L.ny, L.nx, kBlock);
+        if (odd) completeFacesKernel<S, true><<<g, kBlock, 0, s>>>(L);
+        else completeFacesKernel<S, false><<<g, kBlock, 0, s>>>(L);
+        return 1;
+    }
+    static int extract(const DevLattice& L, bool odd, Box b, int pending, double* out, cudaStream_t s) {
+        dim3 g = rowGrid(b.z1 - b.z0 + 1, b.y1 - b.y0 + 1, b.x1 - b.x0 + 1, kBlock);
+        if (odd) extractKernel<S, true><<<g, kBlock, 0, s>>>(L, b, pending, out);
+        else extractKernel<S, false><<<g, kBlock, 0, s>>>(L, b, pending, out);
+        return 1;
+    }
+    static int insert(const DevLattice& L, bool odd, Box b, const double* in, cudaStream_t s) {
+        dim3 g = rowGrid(b.z1 - b.z0 + 1, b.y1 - b.y0 + 1, b.x1 - b.x0 + 1, kBlock);
+        if (odd) insertKernel<S, true><<<g, kBlock, 0, s>>>(L, b, in);
+        else insertKernel<S, false><<<g, kBlock, 0, s>>>(L, b, in);
+        return 1;
+    }
+    static int reduce(const DevLattice& L, bool odd, Box b, int pending, double invRho0, double bbRhoBar,
+                      ReduceAcc* acc, cudaStream_t s) {
+        dim3 g = rowGrid(b.z1 - b.z0 + 1, b.y1 - b.y0 + 1, b.x1 - b.x0 + 1, kBlock);
+        if (odd) reduceKernel<S, true><<<g, kBlock, 0, s>>>(L, b, pending, (R)invRho0, bbRhoBar, acc);
+        else reduceKernel<S, false><<<g, kBlock, 0, s>>>(L, b, pending, (R)invRho0, bbRhoBar, acc);
+        return 1;
+    }
+    static int equilibrium(const DevLattice& L, bool odd, Box b, const double* rhou, const double* cst,
+                           double invRho0, cudaStream_t s) {
+        dim3 g = rowGrid(b.z1 - b.z0 + 1, b.y1 - b.y0 + 1, b.x1 - b.x0 + 1, kBlock);
+        if (odd)
+            equilibriumKernel<S, true><<<g, kBlock, 0, s>>>(L, b, rhou, cst[0], cst[1], cst[2], cst[3], invRho0);
+        else
+            equilibriumKernel<S, false><<<g, kBlock, 0, s>>>(L, b, rhou, cst[0], cst[1], cst[2], cst[3], invRho0);
+        return 1;
+    }
+    static const Launchers& table() {
+        static const Launchers t = {step, completeFaces, extract, insert, reduce, equilibrium};
+        return t;
+    }
+};
+
+}  // namespace plbgpu

@@ -1,0 +1,262 @@
+"""Python mirror of the reference's lattice construction API over the C ABI.
+
+    lat = DeviceLattice3D(nx, ny, nz, omega)             # MultiBlockLattice3D(nx,ny,nz,new BGKdynamics(omega))
+    lat.periodicity(True, False, False)                  # lattice.periodicity().toggle(...)
+    lat.define_dynamics(box, BOUNCEBACK)                 # defineDynamics(lattice, box, new BounceBack)
+    lat.add_velocity_boundary(box, 0, -1)                # bc->addVelocityBoundary0N(box, lattice)
+    lat.set_boundary_velocity(box, (u, 0, 0))            # setBoundaryVelocity(lattice, box, u)
+    lat.initialize_at_equilibrium(box, 1.0, (0, 0, 0))   # initializeAtEquilibrium(...)
+    lat.initialize()                                     # lattice.initialize()
+    lat.collide_and_stream()                             # lattice.collideAndStream()
+    e = lat.compute_average_energy()                     # computeAverageEnergy(lattice)
+
+Boxes are inclusive (x0, x1, y0, y1, z0, z1), like Box3D.  Populations are
+exchanged as FP64 f-bar in [x][y][z][19] order.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import native as N
+
+
+class Context:
+    """One GPU, one stream (plbgpu_create)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = N.load()
+        h = ctypes.c_void_p()
+        rc = self.lib.plbgpu_create(device, ctypes.byref(h))
+        if rc != N.OK:
+            raise N.PlbGpuError(rc, f"cannot create a context on CUDA device {device}")
+        self.h = h
+
+    def launch_count(self) -> int:
+        v = ctypes.c_ulonglong()
+        N.check(self.h, self.lib.plbgpu_launch_count(self.h, ctypes.byref(v)))
+        return int(v.value)
+
+    def stream(self) -> int:
+        v = ctypes.c_void_p()
+        N.check(self.h, self.lib.plbgpu_get_stream(self.h, ctypes.byref(v)))
+        return int(v.value or 0)
+
+    def synchronize(self):
+        N.check(self.h, self.lib.plbgpu_synchronize(self.h))
+
+    def close(self):
+        if self.h:
+            self.lib.plbgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class DeviceLattice3D:
+    def __init__(self, nx, ny, nz, omega=1.0, precision="fp64", ctx: Context | None = None,
+                 rho0=1.0, bb_rho=0.0):
+        self.ctx = ctx or default_context()
+        self.lib = self.ctx.lib
+        self.shape = (int(nx), int(ny), int(nz))
+        self.precision = N.PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        h = ctypes.c_int()
+        self._check(self.lib.plbgpu_add_domain(self.ctx.h, *self.shape, self.precision, ctypes.byref(h)))
+        self.handle = h.value
+        self.set_params(omega, rho0, bb_rho)
+
+    # ----------------------------------------------------------------- helpers
+    def _check(self, rc):
+        return N.check(self.ctx.h, rc)
+
+    @property
+    def bounding_box(self):
+        nx, ny, nz = self.shape
+        return (0, nx - 1, 0, ny - 1, 0, nz - 1)
+
+    def _box(self, box):
+        return tuple(int(v) for v in (self.bounding_box if box is None else box))
+
+    @staticmethod
+    def _cells(box):
+        return (box[1] - box[0] + 1) * (box[3] - box[2] + 1) * (box[5] - box[4] + 1)
+
+    # ----------------------------------------------------------------- setup
+    def set_params(self, omega, rho0=1.0, bb_rho=0.0):
+        self.omega, self.rho0, self.bb_rho = float(omega), float(rho0), float(bb_rho)
+        self._check(self.lib.plbgpu_set_params(self.ctx.h, self.handle, self.omega, self.rho0, self.bb_rho))
+
+    def periodicity(self, px, py, pz):
+        self._check(self.lib.plbgpu_set_periodicity(self.ctx.h, self.handle, int(bool(px)), int(bool(py)),
+                                                    int(bool(pz))))
+
+    def define_dynamics(self, box, kind):
+        self._check(self.lib.plbgpu_define_dynamics(self.ctx.h, self.handle, *self._box(box), int(kind)))
+
+    def set_kinds(self, kinds, box=None):
+        box = self._box(box)
+        k = np.ascontiguousarray(kinds, np.uint8).reshape(-1)
+        self._check(self.lib.plbgpu_set_kinds(self.ctx.h, self.handle, *box,
+                                              k.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), k.size))
+
+    def get_kinds(self, box=None):
+        box = self._box(box)
+        out = np.zeros(self._cells(box), np.uint8)
+        self._check(self.lib.plbgpu_get_kinds(self.ctx.h, self.handle, *box,
+                                              out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), out.size))
+        return out.reshape(box[1] - box[0] + 1, box[3] - box[2] + 1, box[5] - box[4] + 1)
+
+    def add_velocity_boundary(self, box, direction, orientation, zou_he=False):
+        fam = N.ZOUHE_VELOCITY if zou_he else N.REG_VELOCITY
+        self.define_dynamics(box, N.face_kind(fam, direction, orientation))
+
+    def add_pressure_boundary(self, box, direction, orientation, zou_he=False):
+        fam = N.ZOUHE_PRESSURE if zou_he else N.REG_PRESSURE
+        self.define_dynamics(box, N.face_kind(fam, direction, orientation))
+
+    def set_boundary_velocity(self, box, u):
+        box = self._box(box)
+        u = np.asarray(u, np.float64)
+        if u.size == 3:
+            self._check(self.lib.plbgpu_set_boundary_velocity(self.ctx.h, self.handle, *box, *map(float, u.ravel())))
+        else:
+            u = np.ascontiguousarray(u).reshape(-1)
+            self._check(self.lib.plbgpu_set_boundary_velocity_field(self.ctx.h, self.handle, *box, _dp(u), u.size))
+
+    def set_boundary_density(self, box, rho):
+        box = self._box(box)
+        r = np.asarray(rho, np.float64)
+        if r.size == 1:
+            self._check(self.lib.plbgpu_set_boundary_density(self.ctx.h, self.handle, *box, float(r)))
+        else:
+            r = np.ascontiguousarray(r).reshape(-1)
+            self._check(self.lib.plbgpu_set_boundary_density_field(self.ctx.h, self.handle, *box, _dp(r), r.size))
+
+    def set_external_vector(self, box, force):
+        box = self._box(box)
+        f = np.asarray(force, np.float64)
+        if f.size == 3:
+            self._check(self.lib.plbgpu_set_force(self.ctx.h, self.handle, *box, *map(float, f.ravel())))
+        else:
+            f = np.ascontiguousarray(f).reshape(-1)
+            self._check(self.lib.plbgpu_set_force_field(self.ctx.h, self.handle, *box, _dp(f), f.size))
+
+    def initialize_momentum_exchange(self):
+        self._check(self.lib.plbgpu_initialize_momentum_exchange(self.ctx.h, self.handle))
+
+    def initialize_at_equilibrium(self, box, rho, u):
+        box = self._box(box)
+        r = np.asarray(rho, np.float64)
+        if r.size == 1:
+            self._check(self.lib.plbgpu_initialize_at_equilibrium(self.ctx.h, self.handle, *box, float(r),
+                                                                  *map(float, np.asarray(u, np.float64).ravel())))
+        else:
+            ru = np.concatenate([r.reshape(-1, 1), np.asarray(u, np.float64).reshape(-1, 3)], axis=1)
+            ru = np.ascontiguousarray(ru).reshape(-1)
+            self._check(self.lib.plbgpu_initialize_at_equilibrium_field(self.ctx.h, self.handle, *box, _dp(ru),
+                                                                        ru.size))
+
+    def initialize(self):
+        self._check(self.lib.plbgpu_initialize(self.ctx.h, self.handle))
+
+    # ----------------------------------------------------------------- transfer
+    def send(self, f, box=None):
+        box = self._box(box)
+        a = np.ascontiguousarray(f, np.float64).reshape(-1)
+        self._check(self.lib.plbgpu_send(self.ctx.h, self.handle, *box, _dp(a), a.size))
+
+    def receive(self, box=None):
+        box = self._box(box)
+        out = np.empty(self._cells(box) * 19, np.float64)
+        self._check(self.lib.plbgpu_receive(self.ctx.h, self.handle, *box, _dp(out), out.size))
+        return out.reshape(box[1] - box[0] + 1, box[3] - box[2] + 1, box[5] - box[4] + 1, 19)
+
+    # ----------------------------------------------------------------- stepping
+    def collide_and_stream(self, nsteps=1, stats=False):
+        self._check(self.lib.plbgpu_collide_and_stream(self.ctx.h, self.handle, int(nsteps), int(bool(stats))))
+
+    def time_steps(self, nsteps, stats=False) -> float:
+        ms = ctypes.c_float()
+        self._check(self.lib.plbgpu_time_steps(self.ctx.h, self.handle, int(nsteps), int(bool(stats)),
+                                               ctypes.byref(ms)))
+        return float(ms.value)
+
+    def internal_statistics(self):
+        out = np.zeros(7)
+        self._check(self.lib.plbgpu_get_stats(self.ctx.h, self.handle, _dp(out)))
+        return dict(avRhoBar=out[0], avUSqr=out[1], maxUSqr=out[2], drag=out[3:6].copy(), count=int(out[6]),
+                    raw=out)
+
+    def reduce(self, box=None):
+        box = self._box(box)
+        e = ctypes.c_double()
+        r = ctypes.c_double()
+        self._check(self.lib.plbgpu_reduce(self.ctx.h, self.handle, *box, ctypes.byref(e), ctypes.byref(r)))
+        return e.value, r.value
+
+    def compute_average_energy(self, box=None):
+        return self.reduce(box)[0]
+
+    def compute_average_density(self, box=None):
+        return self.reduce(box)[1]
+
+    def device_bytes(self) -> int:
+        b = ctypes.c_ulonglong()
+        self._check(self.lib.plbgpu_domain_info(self.ctx.h, self.handle, None, None, None, None, ctypes.byref(b)))
+        return int(b.value)
+
+    def close(self):
+        if self.handle is not None and self.ctx.h:
+            self.lib.plbgpu_remove_domain(self.ctx.h, self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def lattice_from_description(nx, ny, nz, periodic, omega, flags, bcval=None, force=None, rho0=1.0,
+                             bb_rho=0.0, precision="fp64", ctx=None):
+    """Configure a device lattice from per-cell arrays (kinds, face values in
+    3 components -- velocity, or density in component 0 -- and Guo force)."""
+    from .native import REG_VELOCITY, REG_PRESSURE, ZOUHE_VELOCITY, ZOUHE_PRESSURE
+    lat = DeviceLattice3D(nx, ny, nz, omega, precision, ctx, rho0, bb_rho)
+    lat.periodicity(*periodic)
+    flags = np.ascontiguousarray(flags, np.uint8).reshape(nx, ny, nz)
+    lat.set_kinds(flags)
+    kinds = set(np.unique(flags).tolist())
+    if bcval is not None and any(6 <= k < 30 for k in kinds):
+        bc = np.asarray(bcval, np.float64).reshape(nx, ny, nz, 3)
+        vel = np.zeros_like(bc)
+        is_press = ((flags >= REG_PRESSURE) & (flags < REG_PRESSURE + 6)) | (flags >= ZOUHE_PRESSURE)
+        is_vel = ((flags >= REG_VELOCITY) & (flags < REG_PRESSURE)) | \
+                 ((flags >= ZOUHE_VELOCITY) & (flags < ZOUHE_PRESSURE))
+        vel[is_vel] = bc[is_vel]
+        vel[is_press, 0] = bc[is_press, 0]
+        lat.set_boundary_velocity(None, vel)   # the three planes; density lives in component 0
+    if force is not None and N.GUO in kinds:
+        lat.set_external_vector(None, force)
+    if N.MOMENTUM_EXCHANGE in kinds:
+        lat.initialize_momentum_exchange()
+    return lat

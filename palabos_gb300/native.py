@@ -1,0 +1,119 @@
+"""ctypes binding of libplbgpu.so (include/plbgpu.h).
+
+The library is built in-tree by palabos_gb300/build.py.  There is no CPU
+fallback: if the shared library cannot be loaded, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+LIB_PATH = os.path.join(HERE, "_lib", "libplbgpu.so")
+HEADER = os.path.join(ROOT, "include", "plbgpu.h")
+
+OK = 0
+ERRORS = {-1: "PLBGPU_ERR_ARG", -2: "PLBGPU_ERR_HANDLE", -3: "PLBGPU_ERR_CUDA",
+          -4: "PLBGPU_ERR_NOMEM", -5: "PLBGPU_ERR_STATE"}
+
+FP64, FP32, BF16, FP16 = 0, 1, 2, 3
+PRECISIONS = {"fp64": FP64, "fp32": FP32, "bf16": BF16, "fp16": FP16}
+
+BGK, GUO, INCBGK, BOUNCEBACK, MOMENTUM_EXCHANGE, NODYNAMICS = 0, 1, 2, 3, 4, 5
+REG_VELOCITY, REG_PRESSURE, ZOUHE_VELOCITY, ZOUHE_PRESSURE = 6, 12, 18, 24
+
+
+def face_kind(family: int, direction: int, orientation: int) -> int:
+    """Kind of a face boundary: family + 2*direction + (orientation > 0)."""
+    return family + 2 * direction + (1 if orientation > 0 else 0)
+
+
+class PlbGpuError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_c_int_p = ctypes.POINTER(ctypes.c_int)
+_c_dbl_p = ctypes.POINTER(ctypes.c_double)
+_c_u8_p = ctypes.POINTER(ctypes.c_uint8)
+_vp = ctypes.c_void_p
+_i = ctypes.c_int
+_l = ctypes.c_long
+_d = ctypes.c_double
+_sz = ctypes.c_size_t
+BOX = [_i] * 6
+LBOX = [_l] * 6
+
+SIGNATURES = {
+    "plbgpu_create": [_i, ctypes.POINTER(_vp)],
+    "plbgpu_destroy": [_vp],
+    "plbgpu_launch_count": [_vp, ctypes.POINTER(ctypes.c_ulonglong)],
+    "plbgpu_get_stream": [_vp, ctypes.POINTER(_vp)],
+    "plbgpu_synchronize": [_vp],
+    "plbgpu_add_domain": [_vp, _i, _i, _i, _i, _c_int_p],
+    "plbgpu_remove_domain": [_vp, _i],
+    "plbgpu_domain_info": [_vp, _i, _c_int_p, _c_int_p, _c_int_p, _c_int_p, ctypes.POINTER(ctypes.c_ulonglong)],
+    "plbgpu_set_periodicity": [_vp, _i, _i, _i, _i],
+    "plbgpu_set_params": [_vp, _i, _d, _d, _d],
+    "plbgpu_define_dynamics": [_vp, _i, *BOX, _i],
+    "plbgpu_set_kinds": [_vp, _i, *BOX, _c_u8_p, _sz],
+    "plbgpu_get_kinds": [_vp, _i, *BOX, _c_u8_p, _sz],
+    "plbgpu_set_boundary_velocity": [_vp, _i, *BOX, _d, _d, _d],
+    "plbgpu_set_boundary_velocity_field": [_vp, _i, *BOX, _c_dbl_p, _sz],
+    "plbgpu_set_boundary_density": [_vp, _i, *BOX, _d],
+    "plbgpu_set_boundary_density_field": [_vp, _i, *BOX, _c_dbl_p, _sz],
+    "plbgpu_set_force": [_vp, _i, *BOX, _d, _d, _d],
+    "plbgpu_set_force_field": [_vp, _i, *BOX, _c_dbl_p, _sz],
+    "plbgpu_initialize_momentum_exchange": [_vp, _i],
+    "plbgpu_initialize_at_equilibrium": [_vp, _i, *BOX, _d, _d, _d, _d],
+    "plbgpu_initialize_at_equilibrium_field": [_vp, _i, *BOX, _c_dbl_p, _sz],
+    "plbgpu_initialize": [_vp, _i],
+    "plbgpu_send": [_vp, _i, *BOX, _c_dbl_p, _sz],
+    "plbgpu_receive": [_vp, _i, *BOX, _c_dbl_p, _sz],
+    "plbgpu_collide_and_stream": [_vp, _i, _i, _i],
+    "plbgpu_get_stats": [_vp, _i, _c_dbl_p],
+    "plbgpu_reduce": [_vp, _i, *BOX, _c_dbl_p, _c_dbl_p],
+    "plbgpu_time_steps": [_vp, _i, _i, _i, ctypes.POINTER(ctypes.c_float)],
+    "plbgpu_cp_add_domain": [_vp, _l, _l, _l, _d, _c_int_p],
+    "plbgpu_cp_send": [_vp, _i, *LBOX, ctypes.c_char_p, _sz],
+    "plbgpu_cp_receive": [_vp, _i, *LBOX, ctypes.c_char_p, _sz],
+    "plbgpu_cp_collide_and_stream": [_vp, _i],
+}
+
+_lib = None
+
+
+def header_symbols() -> list[str]:
+    """Every function the C header declares."""
+    with open(HEADER) as f:
+        text = f.read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(plbgpu_\w+)\s*\(", text, re.M)))
+
+
+def load(path: str = LIB_PATH):
+    """Load libplbgpu.so.  Raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with `python -m palabos_gb300.build` "
+                           "(the GPU path has no CPU fallback)")
+    lib = ctypes.CDLL(path)
+    for name, args in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = _i
+    lib.plbgpu_last_error.argtypes = [_vp]
+    lib.plbgpu_last_error.restype = ctypes.c_char_p
+    _lib = lib
+    return lib
+
+
+def check(ctx, rc):
+    if rc != OK:
+        msg = load().plbgpu_last_error(ctx).decode() if ctx else ""
+        raise PlbGpuError(rc, msg)
+    return rc
