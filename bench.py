@@ -256,8 +256,9 @@ def run_gpu(args):
     ctx = Context(local)
     peak, peak_src = load_peaks()
 
-    lat, kinds = build_lattice("fp64", ctx)
-    bytes_step, counts = algorithmic_bytes(kinds, "fp64")
+    head = args.precision
+    lat, kinds = build_lattice(head, ctx)
+    bytes_step, counts = algorithmic_bytes(kinds, head)
     cells = counts["cells"]
     K, W = args.steps, args.warmup
 
@@ -284,7 +285,7 @@ def run_gpu(args):
     # dominant kernel alone: average launch duration of the fused step kernel
     k_ms = time_form(lat, min(K, 400), 10) / min(K, 400)
     achieved = bytes_step / (k_ms * 1e-3) / 1e9
-    traffic = load_traffic("stepKernel_fp64_channel_sphere")
+    traffic = load_traffic(f"stepKernel_{head}_channel_sphere")
 
     # e2e through the C ABI with host buffers
     f_host = lat.receive()
@@ -300,7 +301,7 @@ def run_gpu(args):
         done += chunk
     f_host = lat.receive()
     e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
-    state_bytes = cells * 19 * 8
+    state_bytes = cells * 19 * 8   # the ABI exchanges FP64 f-bar
     nread = (e2e_steps + STATS_EVERY - 1) // STATS_EVERY
     e2e = {"value": round(ws * cells * e2e_steps / e2e_s / 1e6, 2), "unit": "MLUPS",
            "h2d_bytes_per_step": round(state_bytes / e2e_steps, 1),
@@ -309,10 +310,10 @@ def run_gpu(args):
     lat.close()
 
     # the other storage forms on the same workload (kernel-only rate)
-    forms = {"fp64": {"mlups": round(cells / (k_ms * 1e-3) / 1e6, 1), "bytes_per_cell": B_CELL["fp64"],
-                      "hbm_frac": round(achieved / peak, 4)}}
+    forms = {head: {"mlups": round(cells / (k_ms * 1e-3) / 1e6, 1), "bytes_per_cell": B_CELL[head],
+                    "hbm_frac": round(achieved / peak, 4)}}
     if not args.skip_forms:
-        for prec in ("fp32", "bf16", "fp16"):
+        for prec in [p for p in ("fp64", "fp32", "bf16", "fp16") if p != head]:
             l2, _ = build_lattice(prec, ctx)
             n = min(K, 400)
             ms = time_form(l2, n, 10) / n
@@ -326,8 +327,9 @@ def run_gpu(args):
         line = {
             "metric": METRIC, "value": round(value, 2), "unit": "MLUPS", "n_gpus": ws, "steps": K,
             "warmup": W, "ms_per_step": round(t_max / K, 5), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "channel_sphere_256x128x128_bgk_fp64", "shape": list(SHAPE), "omega": OMEGA,
+            "vs_baseline": None, "dtype": "f64" if head == "fp64" else "f32", "data": "synthetic",
+            "config": {"workload": f"channel_sphere_256x128x128_bgk_{head}", "shape": list(SHAPE), "omega": OMEGA,
+                       "storage": head,
                        "inlet": "regularized velocity, parabolic u_max=0.05", "outlet": "regularized pressure rho=1",
                        "obstacle": "momentum-exchange bounce-back sphere r=16 at (64,64,64)",
                        "drag_every": STATS_EVERY, "cells": cells, "faces": counts["faces"],
@@ -336,7 +338,7 @@ def run_gpu(args):
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": traffic,
                          "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
-                         "kernel": "stepKernel<double> (fused collide+stream+faces, AA pattern)",
+                         "kernel": f"stepKernel<{head}> (fused collide+stream+faces, AA pattern)",
                          "bytes_per_launch": bytes_step},
             "forms": forms,
             "e2e": e2e,
@@ -358,6 +360,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-forms", action="store_true")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32", "bf16", "fp16"])
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
