@@ -192,6 +192,36 @@ int plbgpu_cp_receive(plbgpu_ctx* ctx, int handle, long x0, long x1, long y0, lo
                       char* data, size_t nbytes);
 int plbgpu_cp_collide_and_stream(plbgpu_ctx* ctx, int handle);
 
+/* ------------------------------------------------------------ allocation-free form */
+
+/* Rows of scratch available to plbgpu_reduce_noalloc: nx * ny may not exceed it. */
+#define PLBGPU_NOALLOC_MAX_ROWS 262144
+
+/* Average energy and density of a lattice held in caller-owned device memory,
+ * computed without allocating any device memory.  No counterpart in the
+ * reference: it serves callers that cannot call cudaMalloc (work recorded into
+ * a CUDA graph under capture, applications with their own device-memory pool
+ * or a fixed budget).
+ *
+ * populations: 19 planes of FP64 f-bar, plane i at populations + i * stride,
+ *              cell (x, y, z) at index (x * ny + y) * nz + z, post-stream
+ *              (natural) order -- device memory.
+ * kinds:       one byte per cell (PLBGPU_BGK, PLBGPU_INCBGK, PLBGPU_BOUNCEBACK,
+ *              PLBGPU_MOMENTUM_EXCHANGE, PLBGPU_NODYNAMICS) -- device memory.
+ *              Any other kind makes both results NaN.
+ * result:      device memory for 2 doubles: average energy, average density.
+ * stream:      cudaStream_t the two kernels are queued on (NULL = default).
+ *
+ * The scratch is a 4 MiB array of PLBGPU_NOALLOC_MAX_ROWS row sums in the
+ * library's device image, kept by every GPU that loads the library until the
+ * process exits.  Sizes with nx * ny > PLBGPU_NOALLOC_MAX_ROWS are rejected
+ * with PLBGPU_ERR_ARG.  All calls share the array; calls whose kernels overlap
+ * on the GPU race on it.  The first call on a device looks up the array's
+ * address with that device current: make it before any stream capture.
+ * Asynchronous: returns once both kernels are queued. */
+int plbgpu_reduce_noalloc(const double* populations, long long stride, const uint8_t* kinds, int nx, int ny,
+                          int nz, double bb_rho, double rho0, double* result, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

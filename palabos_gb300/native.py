@@ -81,6 +81,7 @@ SIGNATURES = {
     "plbgpu_cp_send": [_vp, _i, *LBOX, ctypes.c_char_p, _sz],
     "plbgpu_cp_receive": [_vp, _i, *LBOX, ctypes.c_char_p, _sz],
     "plbgpu_cp_collide_and_stream": [_vp, _i],
+    "plbgpu_reduce_noalloc": [_vp, ctypes.c_longlong, _vp, _i, _i, _i, _d, _d, _vp, _vp],
 }
 
 _lib = None
