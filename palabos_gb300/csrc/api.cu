@@ -354,6 +354,8 @@ int plbgpu_add_domain(plbgpu_ctx* c, int nx, int ny, int nz, int precision, int*
     d->nx = nx; d->ny = ny; d->nz = nz;
     d->precision = precision;
     d->n = (long long)nx * ny * nz;
+    // The interior kernels index cells with 32-bit integers.
+    if (d->n >= (1LL << 31)) return fail(c, PLBGPU_ERR_ARG, "domain of %lld cells: split it below 2^31 cells", d->n);
     d->stride = (d->n + 127) / 128 * 128;   // every plane starts on a 256-byte boundary
     d->elemSize = elemSizeOf(precision);
     size_t popBytes = d->elemSize * 19 * (size_t)d->stride;

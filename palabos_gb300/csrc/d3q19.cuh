@@ -48,8 +48,11 @@ __device__ __forceinline__ R tw(int i) {
     return i == 0 ? (R)1 / (R)3 : (cnorm2(i) == 1 ? (R)1 / (R)18 : (R)1 / (R)36);
 }
 
-template <typename R>
-__device__ __forceinline__ R invRhoOf(R rhoBar) { return (R)1 / (rhoBar + (R)1); }
+// 1 / (rhoBar + 1) (roundOffPolicy.h:85-87).  The round-to-nearest reciprocal
+// intrinsics return the correctly rounded quotient, i.e. the same bits as the
+// IEEE division 1/x.
+__device__ __forceinline__ double invRhoOf(double rhoBar) { return __drcp_rn(rhoBar + 1.0); }
+__device__ __forceinline__ float invRhoOf(float rhoBar) { return __frcp_rn(rhoBar + 1.0f); }
 
 // momentTemplates3D.h:351-365, 411-425
 template <typename R>
@@ -189,42 +192,61 @@ __device__ __forceinline__ void addGuoForce(R* f, const R* F, const R* u, R omeg
 // kernels apply the completion when the cell is loaded for the next collision
 // (and when the state is read back), which is the same sequence of operations.
 
+// The direction and orientation of a face are template parameters, so every
+// loop over the populations unrolls with compile-time index sets.
+
+// i-th population (ascending) with c[DIR] == VAL (indexTemplates.h:81-97).
+template <int DIR, int VAL>
+__host__ __device__ constexpr int subIndex(int a) {
+    int n = 0;
+    for (int i = 0; i < 19; ++i)
+        if (cdir(i, DIR) == VAL) {
+            if (n == a) return i;
+            ++n;
+        }
+    return -1;
+}
+template <int DIR, int VAL>
+__host__ __device__ constexpr int subIndexCount() {
+    int n = 0;
+    for (int i = 0; i < 19; ++i) n += (cdir(i, DIR) == VAL) ? 1 : 0;
+    return n;
+}
+
 // boundaryDynamics.hh:639-669 (VelocityDirichletBoundaryDynamics::computeRhoBar)
-template <typename R>
-__device__ R velFaceRhoBar(const R* f, int dir, int ori, R velN_in) {
+template <typename R, int DIR, int ORI>
+__device__ __forceinline__ R velFaceRhoBar(const R* f, R velDir) {
     R rhoOnWall = R(0), rhoNormal = R(0);
-    for (int i = 0; i < 19; ++i) {
-        int c = cdir(i, dir);
-        if (c == 0) rhoOnWall += f[i];
-    }
-    for (int i = 0; i < 19; ++i) {
-        int c = cdir(i, dir);
-        if (c == ori) rhoNormal += f[i];
-    }
-    R velNormal = (R)ori * (velN_in - (R)0.5 * (R)0);
+#pragma unroll
+    for (int a = 0; a < subIndexCount<DIR, 0>(); ++a) rhoOnWall += f[subIndex<DIR, 0>(a)];
+#pragma unroll
+    for (int a = 0; a < subIndexCount<DIR, ORI>(); ++a) rhoNormal += f[subIndex<DIR, ORI>(a)];
+    R velNormal = (R)ORI * (velDir - (R)0.5 * (R)0);
     return ((R)2 * rhoNormal + rhoOnWall - (R)1 * velNormal) / ((R)1 + velNormal);
 }
 
 // boundaryDynamics.hh:775-800 (DensityDirichletBoundaryDynamics::computeJ)
-template <typename R>
-__device__ void pressFaceJ(const R* f, int dir, int ori, R rhoBar, R* j) {
+template <typename R, int DIR, int ORI>
+__device__ __forceinline__ void pressFaceJ(const R* f, R rhoBar, R* j) {
     R rhoOnWall = R(0), rhoNormal = R(0);
-    for (int i = 0; i < 19; ++i)
-        if (cdir(i, dir) == 0) rhoOnWall += f[i];
-    for (int i = 0; i < 19; ++i)
-        if (cdir(i, dir) == ori) rhoNormal += f[i];
+#pragma unroll
+    for (int a = 0; a < subIndexCount<DIR, 0>(); ++a) rhoOnWall += f[subIndex<DIR, 0>(a)];
+#pragma unroll
+    for (int a = 0; a < subIndexCount<DIR, ORI>(); ++a) rhoNormal += f[subIndex<DIR, ORI>(a)];
     j[0] = j[1] = j[2] = R(0);
-    j[dir] = (R)ori * ((R)2 * rhoNormal + rhoOnWall - rhoBar);
+    j[DIR] = (R)ORI * ((R)2 * rhoNormal + rhoOnWall - rhoBar);
 }
 
 // offEquilibriumTemplates.h:91-115
 template <typename R>
-__device__ R piToFneq(int i, const R* Pi) {
+__device__ __forceinline__ R piToFneq(int i, const R* Pi) {
     R fNeq = R(0);
     int iPi = 0;
+#pragma unroll
     for (int a = 0; a < 3; ++a) {
         fNeq += Pi[iPi] * ((R)(cdir(i, a) * cdir(i, a)) - (R)1 / (R)3);
         ++iPi;
+#pragma unroll
         for (int b = a + 1; b < 3; ++b) {
             fNeq += Pi[iPi] * (R)2 * (R)cdir(i, a) * (R)cdir(i, b);
             ++iPi;
@@ -236,27 +258,37 @@ __device__ R piToFneq(int i, const R* Pi) {
 
 // regularizedBoundaryDynamics.hh:96-110 with boundaryTemplates.h:42-84 and
 // isoThermalDynamics.hh:55-69
-template <typename R>
-__device__ void regularizedComplete(R* f, int dir, int ori, R rhoBar, const R* j) {
+template <typename R, int DIR, int ORI>
+__device__ __forceinline__ void regularizedComplete(R* f, R rhoBar, const R* j) {
     R jSqr = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
     R invRho = invRhoOf(rhoBar);
     R fNeq[19];
+#pragma unroll
     for (int i = 0; i < 19; ++i) {
-        int c = cdir(i, dir);
-        fNeq[i] = (c == 0 || (c == ori && i != 0)) ? f[i] - bgkEq<R>(i, rhoBar, invRho, j, jSqr) : R(0);
+        const int c = cdir(i, DIR);
+        fNeq[i] = (c == 0 || (c == ORI && i != 0)) ? f[i] - bgkEq<R>(i, rhoBar, invRho, j, jSqr) : R(0);
     }
     R Pi[6];
     int iPi = 0;
+#pragma unroll
     for (int al = 0; al < 3; ++al)
+#pragma unroll
         for (int be = al; be < 3; ++be) {
             R s = R(0);
-            for (int i = 0; i < 19; ++i)
-                if (cdir(i, dir) == 0) s += (R)(cdir(i, al) * cdir(i, be)) * fNeq[i];
-            for (int i = 0; i < 19; ++i)
-                if (cdir(i, dir) == ori) s += (R)2 * (R)cdir(i, al) * (R)cdir(i, be) * fNeq[i];
+#pragma unroll
+            for (int a = 0; a < subIndexCount<DIR, 0>(); ++a) {
+                const int i = subIndex<DIR, 0>(a);
+                s += (R)(cdir(i, al) * cdir(i, be)) * fNeq[i];
+            }
+#pragma unroll
+            for (int a = 0; a < subIndexCount<DIR, ORI>(); ++a) {
+                const int i = subIndex<DIR, ORI>(a);
+                s += (R)2 * (R)cdir(i, al) * (R)cdir(i, be) * fNeq[i];
+            }
             Pi[iPi++] = s;
         }
     f[0] = bgkEq<R>(0, rhoBar, invRho, j, jSqr) + piToFneq<R>(0, Pi);
+#pragma unroll
     for (int i = 1; i <= 9; ++i) {
         f[i] = bgkEq<R>(i, rhoBar, invRho, j, jSqr);
         f[i + 9] = bgkEq<R>(i + 9, rhoBar, invRho, j, jSqr);
@@ -266,23 +298,34 @@ __device__ void regularizedComplete(R* f, int dir, int ori, R rhoBar, const R* j
     }
 }
 
-// zouHeDynamics.hh:44-113 (ZouHeClosure)
-template <typename R>
-__device__ void zouHeComplete(R* f, int dir, int ori, R rhoBar, const R* j) {
-    int missing[5], diag[4];
-    int nm = 0, nd = 0;
+// Missing populations of a Zou/He face: opposites of the c[DIR]==ORI set
+// (indexTemplates.h:110-133), and the same list without the first population
+// that has a single non-zero component (zouHeDynamics.hh:58-71).
+template <int DIR, int ORI>
+__host__ __device__ constexpr int zhMissing(int a) { return opp(subIndex<DIR, ORI>(a)); }
+template <int DIR, int ORI>
+__host__ __device__ constexpr int zhDiag(int a) {
+    int n = 0;
     bool erased = false;
-    for (int i = 0; i < 19; ++i)
-        if (cdir(i, dir) == ori) missing[nm++] = opp(i);
-    for (int a = 0; a < nm; ++a) {
-        int p = missing[a];
+    for (int b = 0; b < subIndexCount<DIR, ORI>(); ++b) {
+        int p = zhMissing<DIR, ORI>(b);
         if (!erased && cnorm2(p) == 1) { erased = true; continue; }
-        diag[nd++] = p;
+        if (n == a) return p;
+        ++n;
     }
+    return -1;
+}
+
+// zouHeDynamics.hh:44-113 (ZouHeClosure)
+template <typename R, int DIR, int ORI>
+__device__ __forceinline__ void zouHeComplete(R* f, R rhoBar, const R* j) {
+    constexpr int nm = subIndexCount<DIR, ORI>();
+    constexpr int nd = nm - 1;
     R jSqr = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
     R invRho = invRhoOf(rhoBar);
+#pragma unroll
     for (int a = 0; a < nm; ++a) {
-        int p = missing[a], o = opp(p);
+        const int p = zhMissing<DIR, ORI>(a), o = opp(p);
         f[p] = f[o] - bgkEq<R>(o, rhoBar, invRho, j, jSqr) + bgkEq<R>(p, rhoBar, invRho, j, jSqr);
     }
     R rb, jj[3];
@@ -290,34 +333,87 @@ __device__ void zouHeComplete(R* f, int dir, int ori, R rhoBar, const R* j) {
     R invR = invRhoOf(rb);
     R falseRho = rb + (R)1;
     R diff[3];
+#pragma unroll
     for (int d = 0; d < 3; ++d) diff[d] = (j[d] - falseRho * (jj[d] * invR)) / (R)nd;
+#pragma unroll
     for (int a = 0; a < nd; ++a) {
-        int p = diag[a];
+        const int p = zhDiag<DIR, ORI>(a);
+#pragma unroll
         for (int s = 1; s < 3; ++s) {
-            int d = (dir + s) % 3;
+            const int d = (DIR + s) % 3;
             f[p] += (R)cdir(p, d) * diff[d];
         }
     }
 }
 
-// Completion of one face cell.  v = (ux, uy, uz) for velocity faces, (rho, -, -)
-// for pressure faces.
-template <typename R>
-__device__ __noinline__ void completeFace(R* f, int kind, const double* v) {
-    int dir = faceDir(kind), ori = faceOri(kind), fam = faceFamily(kind);
+// Completion of one face cell; v = (ux, uy, uz) for velocity faces,
+// (rho, -, -) for pressure faces.  FAM: 0 regularized velocity, 1 regularized
+// pressure, 2 Zou/He velocity, 3 Zou/He pressure.
+template <typename R, int FAM, int DIR, int ORI>
+__device__ __forceinline__ void completeFaceT(R* f, const double* v) {
     R rhoBar, j[3];
-    if (fam == 0 || fam == 2) {
-        rhoBar = velFaceRhoBar<R>(f, dir, ori, (R)v[dir]);
+    if (FAM == 0 || FAM == 2) {
+        rhoBar = velFaceRhoBar<R, DIR, ORI>(f, (R)v[DIR]);
         R rho = rhoBar + (R)1;
+#pragma unroll
         for (int d = 0; d < 3; ++d) j[d] = rho * ((R)v[d] - (R)0.5 * (R)0);
     } else {
         rhoBar = (R)v[0] - (R)1;
-        pressFaceJ<R>(f, dir, ori, rhoBar, j);
+        pressFaceJ<R, DIR, ORI>(f, rhoBar, j);
     }
-    if (fam < 2)
-        regularizedComplete<R>(f, dir, ori, rhoBar, j);
-    else
-        zouHeComplete<R>(f, dir, ori, rhoBar, j);
+    if (FAM < 2) regularizedComplete<R, DIR, ORI>(f, rhoBar, j);
+    else zouHeComplete<R, DIR, ORI>(f, rhoBar, j);
+}
+
+template <typename R, int FAM>
+__device__ __forceinline__ void completeFaceFam(R* f, int sub, const double* v) {
+    switch (sub) {
+    case 0: completeFaceT<R, FAM, 0, -1>(f, v); break;
+    case 1: completeFaceT<R, FAM, 0, 1>(f, v); break;
+    case 2: completeFaceT<R, FAM, 1, -1>(f, v); break;
+    case 3: completeFaceT<R, FAM, 1, 1>(f, v); break;
+    case 4: completeFaceT<R, FAM, 2, -1>(f, v); break;
+    default: completeFaceT<R, FAM, 2, 1>(f, v); break;
+    }
+}
+
+template <typename R>
+__device__ __noinline__ void completeFace(R* f, int kind, const double* v) {
+    const int fam = faceFamily(kind), sub = (kind - K_REGVEL) % 6;
+    switch (fam) {
+    case 0: completeFaceFam<R, 0>(f, sub, v); break;
+    case 1: completeFaceFam<R, 1>(f, sub, v); break;
+    case 2: completeFaceFam<R, 2>(f, sub, v); break;
+    default: completeFaceFam<R, 3>(f, sub, v); break;
+    }
+}
+
+// Rho-bar of a velocity face cell (VelocityDirichletBoundaryDynamics::computeRhoBar)
+// for a runtime direction / orientation.
+template <typename R>
+__device__ __noinline__ R velFaceRhoBarAny(const R* f, int kind, R velDir) {
+    switch ((kind - K_REGVEL) % 6) {
+    case 0: return velFaceRhoBar<R, 0, -1>(f, velDir);
+    case 1: return velFaceRhoBar<R, 0, 1>(f, velDir);
+    case 2: return velFaceRhoBar<R, 1, -1>(f, velDir);
+    case 3: return velFaceRhoBar<R, 1, 1>(f, velDir);
+    case 4: return velFaceRhoBar<R, 2, -1>(f, velDir);
+    default: return velFaceRhoBar<R, 2, 1>(f, velDir);
+    }
+}
+
+// Momentum of a pressure face cell (DensityDirichletBoundaryDynamics::computeJ)
+// for a runtime direction / orientation.
+template <typename R>
+__device__ __noinline__ void pressFaceJAny(const R* f, int kind, R rhoBar, R* j) {
+    switch ((kind - K_REGVEL) % 6) {
+    case 0: pressFaceJ<R, 0, -1>(f, rhoBar, j); break;
+    case 1: pressFaceJ<R, 0, 1>(f, rhoBar, j); break;
+    case 2: pressFaceJ<R, 1, -1>(f, rhoBar, j); break;
+    case 3: pressFaceJ<R, 1, 1>(f, rhoBar, j); break;
+    case 4: pressFaceJ<R, 2, -1>(f, rhoBar, j); break;
+    default: pressFaceJ<R, 2, 1>(f, rhoBar, j); break;
+    }
 }
 
 }  // namespace plbgpu

@@ -270,47 +270,157 @@ __device__ __forceinline__ bool collideCell(const DevLattice& L, const StepParam
     }
 }
 
-// Fused collide-and-stream for one time step.  One thread per cell; threads
-// run along z (the contiguous axis) so every population plane is read and
-// written in coalesced rows.
+template <bool STATS>
+__device__ __forceinline__ void accumulateStats(bool gathers, double rhoBar, double uSqr, StatsAcc* acc) {
+    if (!STATS) return;
+    double sR = gathers ? rhoBar : 0.;
+    double sU = gathers ? uSqr : 0.;
+    unsigned long long c = gathers ? 1ull : 0ull;
+    unsigned long long m = gathers ? (unsigned long long)__double_as_longlong(uSqr) : 0ull;
+    sR = warpSum(sR);
+    sU = warpSum(sU);
+    c = warpSumU(c);
+    m = warpMaxU(m);
+    if ((threadIdx.x & 31) == 0 && c > 0) {
+        atomicAdd(&acc->sumRhoBar, sR);
+        atomicAdd(&acc->sumUSqr, sU);
+        atomicAdd(&acc->count, c);
+        atomicMax(&acc->maxBits, m);
+    }
+}
+
+// General cell update: any position, periodic wrap and the domain-edge rule.
 template <typename S, bool ODD, bool STATS>
-__global__ void __launch_bounds__(128) stepKernel(DevLattice L, StepParams<typename StoreT<S>::R> P,
-                                                  StatsAcc* acc) {
+__device__ __forceinline__ bool processCellGeneral(const DevLattice& L, const StepParams<typename StoreT<S>::R>& P,
+                                                   int x, int y, int z, StatsAcc* acc,
+                                                   typename StoreT<S>::R& rhoBar, typename StoreT<S>::R& uSqr) {
+    using R = typename StoreT<S>::R;
+    const long long idx = ((long long)x * L.ny + y) * L.nz + z;
+    const int k = L.flags[idx];
+    if (k == K_NONE) return false;
+    Neighbourhood nb = neighbourhood(L, x, y, z);
+    R f[19];
+    loadCell<S, ODD>(L, nb, idx, f);
+    if (P.pending && isFace(k)) completeIfFace<R>(L, idx, k, f);
+    bool g = collideCell<S>(L, P, idx, k, f, rhoBar, uSqr, acc, STATS);
+    storeCell<S, ODD>(L, nb, idx, f);
+    return g;
+}
+
+// Population planes and the neighbour offsets c_i . (ny*nz, nz, 1) passed by
+// value (kernel parameters live in the constant bank).
+template <typename S>
+struct Planes {
+    S* p[19];
+};
+struct Deltas {
+    int d[19];
+};
+
+template <typename S> struct RowOccupancy { static constexpr int blocks = 8; };
+template <> struct RowOccupancy<double> { static constexpr int blocks = 5; };
+
+// Cell of a row with 1 <= x <= nx-2 and 1 <= y <= ny-2: a neighbour can only
+// leave the domain (or wrap) along z, so every population address is
+// plane_i + idx +- delta_i with uniform deltas and a 32-bit cell index; only
+// the ten populations that move along z carry a per-thread wrap / reflection
+// select.
+template <typename S, bool ODD, bool STATS>
+__device__ __forceinline__ bool processCellRow(const DevLattice& L, const Planes<S>& Pl, const Deltas& D,
+                                               const StepParams<typename StoreT<S>::R>& P, int x, int y, int z,
+                                               StatsAcc* acc, typename StoreT<S>::R& rhoBar,
+                                               typename StoreT<S>::R& uSqr) {
+    using R = typename StoreT<S>::R;
+    const int idx = (x * L.ny + y) * L.nz + z;
+    const int k = L.flags[idx];
+    if (k == K_NONE) return false;
+    const bool zlo = (z == 0), zhi = (z == L.nz - 1);
+    const int wrapM = zlo ? L.nz : 0;    // a -1 move along z at z = 0 wraps to nz-1
+    const int wrapP = zhi ? -L.nz : 0;   // a +1 move along z at z = nz-1 wraps to 0
+    const bool okM = !zlo || L.per[2];
+    const bool okP = !zhi || L.per[2];
+    R f[19];
+    f[0] = StoreT<S>::ld(Pl.p[0] + idx);
+#pragma unroll
+    for (int i = 1; i < 19; ++i) {
+        if (!ODD) {
+            f[i] = StoreT<S>::ld(Pl.p[i] + idx);
+        } else {
+            const int mz = -cdir(i, 2);   // the source is x - c_i
+            if (mz == 0) {
+                f[i] = StoreT<S>::ld(Pl.p[opp(i)] + (idx - D.d[i]));
+            } else {
+                const bool ok = mz < 0 ? okM : okP;
+                const int off = -D.d[i] + (mz < 0 ? wrapM : wrapP);
+                const S* a = ok ? Pl.p[opp(i)] + (idx + off) : Pl.p[i] + idx;
+                f[i] = StoreT<S>::ld(a);
+            }
+        }
+    }
+    if (P.pending && isFace(k)) completeIfFace<R>(L, idx, k, f);
+    bool g = collideCell<S>(L, P, idx, k, f, rhoBar, uSqr, acc, STATS);
+    StoreT<S>::st(Pl.p[0] + idx, f[0]);
+#pragma unroll
+    for (int i = 1; i < 19; ++i) {
+        if (!ODD) {
+            StoreT<S>::st(Pl.p[opp(i)] + idx, f[i]);
+        } else {
+            const int cz = cdir(i, 2);    // the destination is x + c_i
+            if (cz == 0) {
+                StoreT<S>::st(Pl.p[i] + (idx + D.d[i]), f[i]);
+            } else {
+                const bool ok = cz < 0 ? okM : okP;
+                const int off = D.d[i] + (cz < 0 ? wrapM : wrapP);
+                S* a = ok ? Pl.p[i] + (idx + off) : Pl.p[opp(i)] + idx;
+                StoreT<S>::st(a, f[i]);
+            }
+        }
+    }
+    return g;
+}
+
+// Rows with 1 <= x <= nx-2 and 1 <= y <= ny-2 (all z): nearly all of the time
+// step.  Blocks are rows along z (128 threads, coalesced population planes).
+template <typename S, bool ODD, bool STATS>
+__global__ void __launch_bounds__(128, RowOccupancy<S>::blocks)
+    rowStepKernel(DevLattice L, Planes<S> Pl, Deltas D, StepParams<typename StoreT<S>::R> P, StatsAcc* acc) {
     using R = typename StoreT<S>::R;
     const int z = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y;
-    const int x = blockIdx.z;
-    const bool active = z < L.nz;
     R rhoBar = R(0), uSqr = R(0);
-    bool gathers = false;
-    if (active) {
-        const long long idx = ((long long)x * L.ny + y) * L.nz + z;
-        const int k = L.flags[idx];
-        if (k != K_NONE) {
-            Neighbourhood nb = neighbourhood(L, x, y, z);
-            R f[19];
-            loadCell<S, ODD>(L, nb, idx, f);
-            if (P.pending && isFace(k)) completeIfFace<R>(L, idx, k, f);
-            gathers = collideCell<S>(L, P, idx, k, f, rhoBar, uSqr, acc, STATS);
-            storeCell<S, ODD>(L, nb, idx, f);
-        }
+    bool g = false;
+    if (z < L.nz)
+        g = processCellRow<S, ODD, STATS>(L, Pl, D, P, blockIdx.z + 1, blockIdx.y + 1, z, acc, rhoBar, uSqr);
+    accumulateStats<STATS>(g, (double)rhoBar, (double)uSqr, acc);
+}
+
+// Rows on the x or y border of the domain, with the general addressing
+// (periodic wrap and the domain-edge rule on every axis).  blockIdx.y
+// enumerates the border rows: x = 0, x = nx-1 (all y), then y = 0, y = ny-1
+// (1 <= x <= nx-2); when nx < 3 or ny < 3 every row is a border row.
+template <typename S, bool ODD, bool STATS>
+__global__ void __launch_bounds__(128) edgeRowStepKernel(DevLattice L, StepParams<typename StoreT<S>::R> P,
+                                                          StatsAcc* acc) {
+    using R = typename StoreT<S>::R;
+    const int z = blockIdx.x * blockDim.x + threadIdx.x;
+    const int row = blockIdx.y;
+    const int nx = L.nx, ny = L.ny;
+    int x, y;
+    if (nx < 3 || ny < 3) {
+        x = row / ny;
+        y = row - x * ny;
+    } else if (row < ny) {
+        x = 0; y = row;
+    } else if (row < 2 * ny) {
+        x = nx - 1; y = row - ny;
+    } else if (row < 2 * ny + (nx - 2)) {
+        x = 1 + row - 2 * ny; y = 0;
+    } else {
+        x = 1 + row - 2 * ny - (nx - 2); y = ny - 1;
     }
-    if (STATS) {
-        double sR = gathers ? (double)rhoBar : 0.;
-        double sU = gathers ? (double)uSqr : 0.;
-        unsigned long long c = gathers ? 1ull : 0ull;
-        unsigned long long m = gathers ? (unsigned long long)__double_as_longlong((double)uSqr) : 0ull;
-        sR = warpSum(sR);
-        sU = warpSum(sU);
-        c = warpSumU(c);
-        m = warpMaxU(m);
-        if ((threadIdx.x & 31) == 0 && c > 0) {
-            atomicAdd(&acc->sumRhoBar, sR);
-            atomicAdd(&acc->sumUSqr, sU);
-            atomicAdd(&acc->count, c);
-            atomicMax(&acc->maxBits, m);
-        }
-    }
+    R rhoBar = R(0), uSqr = R(0);
+    bool g = false;
+    if (z < L.nz) g = processCellGeneral<S, ODD, STATS>(L, P, x, y, z, acc, rhoBar, uSqr);
+    accumulateStats<STATS>(g, (double)rhoBar, (double)uSqr, acc);
 }
 
 // Complete the boundary faces in place (used before a transfer into a state
@@ -423,10 +533,10 @@ __global__ void reduceKernel(DevLattice L, Box b, int pending, typename StoreT<S
                 double v[3] = {L.bc[idx], L.bc[L.n + idx], L.bc[2 * L.n + idx]};
                 if (fam == 0 || fam == 2) {  // stored velocity, boundaryDynamics.hh:324-330
                     for (int d = 0; d < 3; ++d) u[d] = (R)v[d];
-                    rb = velFaceRhoBar<R>(f, dir, ori, (R)v[dir]);
+                    rb = velFaceRhoBarAny<R>(f, k, (R)v[dir]);
                 } else {  // boundaryDynamics.hh:790-812
                     rb = (R)v[0] - (R)1;
-                    pressFaceJ<R>(f, dir, ori, rb, u);
+                    pressFaceJAny<R>(f, k, rb, u);
                     R invRho = invRhoOf(rb);
                     for (int d = 0; d < 3; ++d) { u[d] *= invRho; u[d] += (R)0.5 * (R)0; }
                 }

@@ -45,6 +45,25 @@ struct LaunchImpl {
     using R = typename StoreT<S>::R;
     static constexpr int kBlock = 128;
 
+    template <bool ODD, bool STATS>
+    static int stepSplit(const DevLattice& L, const StepParams<R>& p, StatsAcc* acc, cudaStream_t s) {
+        int launched = 0;
+        int edgeRows = (L.nx < 3 || L.ny < 3) ? L.nx * L.ny : 2 * L.ny + 2 * (L.nx - 2);
+        if (L.nx >= 3 && L.ny >= 3) {
+            Planes<S> pl;
+            Deltas d;
+            for (int i = 0; i < 19; ++i) {
+                pl.p[i] = static_cast<S*>(L.pop) + (long long)i * L.stride;
+                d.d[i] = cdir(i, 0) * L.ny * L.nz + cdir(i, 1) * L.nz + cdir(i, 2);
+            }
+            rowStepKernel<S, ODD, STATS><<<rowGrid(L.nz, L.ny - 2, L.nx - 2, kBlock), kBlock, 0, s>>>(L, pl, d, p, acc);
+            ++launched;
+        }
+        dim3 g((unsigned)((L.nz + kBlock - 1) / kBlock), (unsigned)edgeRows, 1);
+        edgeRowStepKernel<S, ODD, STATS><<<g, kBlock, 0, s>>>(L, p, acc);
+        return launched + 1;
+    }
+
     static int step(const DevLattice& L, bool odd, bool stats, const StepConsts& c, StatsAcc* acc,
                     cudaStream_t s) {
         StepParams<R> p;
@@ -55,15 +74,8 @@ struct LaunchImpl {
         p.bgk.t4_omega = (R)c.t4_omega;
         p.invRho0 = (R)c.invRho0;
         p.pending = c.pending;
-        dim3 g = rowGrid(L.nz, L.ny, L.nx, kBlock);
-        if (odd) {
-            if (stats) stepKernel<S, true, true><<<g, kBlock, 0, s>>>(L, p, acc);
-            else stepKernel<S, true, false><<<g, kBlock, 0, s>>>(L, p, acc);
-        } else {
-            if (stats) stepKernel<S, false, true><<<g, kBlock, 0, s>>>(L, p, acc);
-            else stepKernel<S, false, false><<<g, kBlock, 0, s>>>(L, p, acc);
-        }
-        return 1;
+        if (odd) return stats ? stepSplit<true, true>(L, p, acc, s) : stepSplit<true, false>(L, p, acc, s);
+        return stats ? stepSplit<false, true>(L, p, acc, s) : stepSplit<false, false>(L, p, acc, s);
     }
     static int completeFaces(const DevLattice& L, bool odd, cudaStream_t s) {
         dim3 g = rowGrid(L.nz, L.ny, L.nx, kBlock);
