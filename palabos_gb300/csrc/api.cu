@@ -37,6 +37,7 @@ struct Domain {
     void* force = nullptr;       // 3 * n of FP64 or FP32
     uint32_t* mebb = nullptr;    // n
     StatsAcc* stats = nullptr;   // device accumulator
+    unsigned* status = nullptr;  // device error word written by the kernels
     ReduceAcc* red = nullptr;
     bool odd = false;            // AA parity of the stored state
     bool pending = false;        // faces still need their post-stream completion
@@ -55,6 +56,7 @@ struct Domain {
         L.nx = nx; L.ny = ny; L.nz = nz;
         L.per[0] = per[0]; L.per[1] = per[1]; L.per[2] = per[2];
         L.n = n;
+        L.status = status;
         return L;
     }
 };
@@ -271,6 +273,19 @@ StepConsts consts(const Domain* d) {
     return s;
 }
 
+// The kernels record failures (a bulk-copy wait that gave up) in a device
+// status word; report and clear it.
+int checkStatus(plbgpu_ctx* c, Domain* d) {
+    unsigned st = 0;
+    CUDA_TRY(c, cudaMemcpyAsync(&st, d->status, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if (st) {
+        CUDA_TRY(c, cudaMemsetAsync(d->status, 0, sizeof(unsigned), c->stream));
+        return fail(c, PLBGPU_ERR_CUDA, "device status 0x%x: a staged-copy wait timed out, results are invalid", st);
+    }
+    return PLBGPU_OK;
+}
+
 // Complete pending faces in place so that the stored state is the
 // reference's post-step state again.
 int materialize(plbgpu_ctx* c, Domain* d) {
@@ -339,6 +354,10 @@ int plbgpu_get_stream(const plbgpu_ctx* c, void** stream) {
 int plbgpu_synchronize(plbgpu_ctx* c) {
     if (!c) return PLBGPU_ERR_ARG;
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    for (auto& kv : c->domains) {
+        int rc = checkStatus(c, kv.second.get());
+        if (rc) return rc;
+    }
     return PLBGPU_OK;
 }
 
@@ -365,6 +384,8 @@ int plbgpu_add_domain(plbgpu_ctx* c, int nx, int ny, int nz, int precision, int*
     d->deviceBytes = bytes;
     CUDA_TRY(c, cudaMemsetAsync(d->arena, 0, bytes, c->stream));   // f-bar = 0 (rest), all BGK
     CUDA_TRY(c, cudaMalloc(&d->stats, sizeof(StatsAcc)));
+    CUDA_TRY(c, cudaMalloc(&d->status, sizeof(unsigned)));
+    CUDA_TRY(c, cudaMemsetAsync(d->status, 0, sizeof(unsigned), c->stream));
     CUDA_TRY(c, cudaMalloc(&d->red, sizeof(ReduceAcc)));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     int h = c->nextHandle++;
@@ -383,6 +404,7 @@ int plbgpu_remove_domain(plbgpu_ctx* c, int h) {
     if (d->force) cudaFree(d->force);
     if (d->mebb) cudaFree(d->mebb);
     cudaFree(d->stats);
+    cudaFree(d->status);
     cudaFree(d->red);
     c->domains.erase(h);
     return PLBGPU_OK;
@@ -634,6 +656,7 @@ int plbgpu_receive(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0,
     if ((rc = checkBox(c, d, x0, x1, y0, y1, z0, z1, &b))) return rc;
     long long cells = boxCells(b);
     if (!buf || (long long)n != 19 * cells) return fail(c, PLBGPU_ERR_ARG, "receive: %zu doubles for %lld cells", n, cells);
+    if ((rc = checkStatus(c, d))) return rc;
     if ((rc = ensureStaging(c, sizeof(double) * n))) return rc;
     int k = launchers(d->precision).extract(d->view(), d->odd, b, d->pending && d->bc ? 1 : 0,
                                             static_cast<double*>(c->staging), c->stream);
@@ -672,6 +695,7 @@ int plbgpu_get_stats(plbgpu_ctx* c, int h, double out[7]) {
     if (rc) return rc;
     if (!out) return PLBGPU_ERR_ARG;
     if (!d->statsValid) return fail(c, PLBGPU_ERR_STATE, "no step has gathered statistics since the last change");
+    if ((rc = checkStatus(c, d))) return rc;
     StatsAcc a;
     CUDA_TRY(c, cudaMemcpyAsync(&a, d->stats, sizeof(StatsAcc), cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
@@ -726,7 +750,9 @@ int plbgpu_time_steps(plbgpu_ctx* c, int h, int nsteps, int collect_stats, float
     CUDA_TRY(c, cudaEventElapsedTime(ms, e0, e1));
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    return PLBGPU_OK;
+    Domain* d;
+    if ((rc = lookup(c, h, &d))) return rc;
+    return checkStatus(c, d);
 }
 
 // ------------------------------------------------------------ co-processor form

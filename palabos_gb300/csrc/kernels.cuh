@@ -41,11 +41,26 @@ template <> struct StoreT<__nv_bfloat16> {
     using R = float; using F = float;
     static __device__ __forceinline__ float ld(const __nv_bfloat16* p) { return __bfloat162float(*p); }
     static __device__ __forceinline__ void st(__nv_bfloat16* p, float v) { *p = __float2bfloat16_rn(v); }
+    // two adjacent values; p is 4-byte aligned
+    static __device__ __forceinline__ void ld2(const __nv_bfloat16* p, float& a, float& b) {
+        float2 v = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(p));
+        a = v.x; b = v.y;
+    }
+    static __device__ __forceinline__ void st2(__nv_bfloat16* p, float a, float b) {
+        *reinterpret_cast<__nv_bfloat162*>(p) = __floats2bfloat162_rn(a, b);
+    }
 };
 template <> struct StoreT<__half> {
     using R = float; using F = float;
     static __device__ __forceinline__ float ld(const __half* p) { return __half2float(*p); }
     static __device__ __forceinline__ void st(__half* p, float v) { *p = __float2half_rn(v); }
+    static __device__ __forceinline__ void ld2(const __half* p, float& a, float& b) {
+        float2 v = __half22float2(*reinterpret_cast<const __half2*>(p));
+        a = v.x; b = v.y;
+    }
+    static __device__ __forceinline__ void st2(__half* p, float a, float b) {
+        *reinterpret_cast<__half2*>(p) = __floats2half2_rn(a, b);
+    }
 };
 
 struct DevLattice {
@@ -58,6 +73,7 @@ struct DevLattice {
     int nx, ny, nz;
     int per[3];
     long long n;
+    unsigned* status;       // device error word (bit 0: a bulk-copy wait timed out)
 };
 
 template <typename R>
@@ -317,80 +333,229 @@ struct Deltas {
     int d[19];
 };
 
-template <typename S> struct RowOccupancy { static constexpr int blocks = 8; };
-template <> struct RowOccupancy<double> { static constexpr int blocks = 5; };
-
-// Cell of a row with 1 <= x <= nx-2 and 1 <= y <= ny-2: a neighbour can only
+// Cells of a row with 1 <= x <= nx-2 and 1 <= y <= ny-2: a neighbour can only
 // leave the domain (or wrap) along z, so every population address is
 // plane_i + idx +- delta_i with uniform deltas and a 32-bit cell index; only
 // the ten populations that move along z carry a per-thread wrap / reflection
 // select.
-template <typename S, bool ODD, bool STATS>
-__device__ __forceinline__ bool processCellRow(const DevLattice& L, const Planes<S>& Pl, const Deltas& D,
-                                               const StepParams<typename StoreT<S>::R>& P, int x, int y, int z,
-                                               StatsAcc* acc, typename StoreT<S>::R& rhoBar,
-                                               typename StoreT<S>::R& uSqr) {
-    using R = typename StoreT<S>::R;
-    const int idx = (x * L.ny + y) * L.nz + z;
-    const int k = L.flags[idx];
-    if (k == K_NONE) return false;
-    const bool zlo = (z == 0), zhi = (z == L.nz - 1);
-    const int wrapM = zlo ? L.nz : 0;    // a -1 move along z at z = 0 wraps to nz-1
-    const int wrapP = zhi ? -L.nz : 0;   // a +1 move along z at z = nz-1 wraps to 0
-    const bool okM = !zlo || L.per[2];
-    const bool okP = !zhi || L.per[2];
-    R f[19];
-    f[0] = StoreT<S>::ld(Pl.p[0] + idx);
+template <typename S, bool ODD>
+struct RowCell {
+    int idx, wrapM, wrapP;
+    bool okM, okP;
+
+    __device__ __forceinline__ RowCell(const DevLattice& L, int x, int y, int z) {
+        idx = (x * L.ny + y) * L.nz + z;
+        const bool zlo = (z == 0), zhi = (z == L.nz - 1);
+        wrapM = zlo ? L.nz : 0;    // a -1 move along z at z = 0 wraps to nz-1
+        wrapP = zhi ? -L.nz : 0;   // a +1 move along z at z = nz-1 wraps to 0
+        okM = !zlo || L.per[2];
+        okP = !zhi || L.per[2];
+    }
+
+    __device__ __forceinline__ void load(const Planes<S>& Pl, const Deltas& D, typename StoreT<S>::R* f) const {
+        f[0] = StoreT<S>::ld(Pl.p[0] + idx);
 #pragma unroll
-    for (int i = 1; i < 19; ++i) {
-        if (!ODD) {
-            f[i] = StoreT<S>::ld(Pl.p[i] + idx);
-        } else {
-            const int mz = -cdir(i, 2);   // the source is x - c_i
-            if (mz == 0) {
-                f[i] = StoreT<S>::ld(Pl.p[opp(i)] + (idx - D.d[i]));
+        for (int i = 1; i < 19; ++i) {
+            if (!ODD) {
+                f[i] = StoreT<S>::ld(Pl.p[i] + idx);
             } else {
-                const bool ok = mz < 0 ? okM : okP;
-                const int off = -D.d[i] + (mz < 0 ? wrapM : wrapP);
-                const S* a = ok ? Pl.p[opp(i)] + (idx + off) : Pl.p[i] + idx;
-                f[i] = StoreT<S>::ld(a);
+                const int mz = -cdir(i, 2);   // the source is x - c_i
+                if (mz == 0) {
+                    f[i] = StoreT<S>::ld(Pl.p[opp(i)] + (idx - D.d[i]));
+                } else {
+                    const bool ok = mz < 0 ? okM : okP;
+                    const int off = -D.d[i] + (mz < 0 ? wrapM : wrapP);
+                    const S* a = ok ? Pl.p[opp(i)] + (idx + off) : Pl.p[i] + idx;
+                    f[i] = StoreT<S>::ld(a);
+                }
             }
         }
     }
-    if (P.pending && isFace(k)) completeIfFace<R>(L, idx, k, f);
-    bool g = collideCell<S>(L, P, idx, k, f, rhoBar, uSqr, acc, STATS);
-    StoreT<S>::st(Pl.p[0] + idx, f[0]);
+
+    __device__ __forceinline__ void store(const Planes<S>& Pl, const Deltas& D,
+                                          const typename StoreT<S>::R* f) const {
+        StoreT<S>::st(Pl.p[0] + idx, f[0]);
 #pragma unroll
-    for (int i = 1; i < 19; ++i) {
-        if (!ODD) {
-            StoreT<S>::st(Pl.p[opp(i)] + idx, f[i]);
-        } else {
-            const int cz = cdir(i, 2);    // the destination is x + c_i
-            if (cz == 0) {
-                StoreT<S>::st(Pl.p[i] + (idx + D.d[i]), f[i]);
+        for (int i = 1; i < 19; ++i) {
+            if (!ODD) {
+                StoreT<S>::st(Pl.p[opp(i)] + idx, f[i]);
             } else {
-                const bool ok = cz < 0 ? okM : okP;
-                const int off = D.d[i] + (cz < 0 ? wrapM : wrapP);
-                S* a = ok ? Pl.p[i] + (idx + off) : Pl.p[opp(i)] + idx;
-                StoreT<S>::st(a, f[i]);
+                const int cz = cdir(i, 2);    // the destination is x + c_i
+                if (cz == 0) {
+                    StoreT<S>::st(Pl.p[i] + (idx + D.d[i]), f[i]);
+                } else {
+                    const bool ok = cz < 0 ? okM : okP;
+                    const int off = D.d[i] + (cz < 0 ? wrapM : wrapP);
+                    S* a = ok ? Pl.p[i] + (idx + off) : Pl.p[opp(i)] + idx;
+                    StoreT<S>::st(a, f[i]);
+                }
             }
         }
     }
-    return g;
-}
+};
+
+// Cells per thread of the row kernel and its residency target (blocks of 128
+// threads per SM).
+template <typename S> struct RowShape { static constexpr int cells = 1, blocks = 8; };
+template <> struct RowShape<double> { static constexpr int cells = 1, blocks = 5; };
 
 // Rows with 1 <= x <= nx-2 and 1 <= y <= ny-2 (all z): nearly all of the time
-// step.  Blocks are rows along z (128 threads, coalesced population planes).
+// step.  A block covers RowShape::cells * blockDim.x consecutive cells of one
+// row; thread t owns cells t, t + blockDim.x, ... (coalesced planes).
 template <typename S, bool ODD, bool STATS>
-__global__ void __launch_bounds__(128, RowOccupancy<S>::blocks)
+__global__ void __launch_bounds__(128, RowShape<S>::blocks)
     rowStepKernel(DevLattice L, Planes<S> Pl, Deltas D, StepParams<typename StoreT<S>::R> P, StatsAcc* acc) {
     using R = typename StoreT<S>::R;
-    const int z = blockIdx.x * blockDim.x + threadIdx.x;
-    R rhoBar = R(0), uSqr = R(0);
-    bool g = false;
-    if (z < L.nz)
-        g = processCellRow<S, ODD, STATS>(L, Pl, D, P, blockIdx.z + 1, blockIdx.y + 1, z, acc, rhoBar, uSqr);
-    accumulateStats<STATS>(g, (double)rhoBar, (double)uSqr, acc);
+    constexpr int NC = RowShape<S>::cells;
+    const int x = blockIdx.z + 1, y = blockIdx.y + 1;
+    const int z0 = blockIdx.x * blockDim.x * NC + threadIdx.x;
+    R f[NC][19];
+    int kind[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+        const int z = z0 + c * blockDim.x;
+        kind[c] = K_NONE;
+        if (z < L.nz) {
+            RowCell<S, ODD> rc(L, x, y, z);
+            kind[c] = L.flags[rc.idx];
+            if (kind[c] != K_NONE) rc.load(Pl, D, f[c]);
+        }
+    }
+    double sR = 0., sU = 0.;
+    unsigned long long cnt = 0, mx = 0;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+        if (kind[c] == K_NONE) continue;
+        RowCell<S, ODD> rc(L, x, y, z0 + c * blockDim.x);
+        R rhoBar = R(0), uSqr = R(0);
+        if (P.pending && isFace(kind[c])) completeIfFace<R>(L, rc.idx, kind[c], f[c]);
+        bool g = collideCell<S>(L, P, rc.idx, kind[c], f[c], rhoBar, uSqr, acc, STATS);
+        rc.store(Pl, D, f[c]);
+        if (STATS && g) {
+            sR += (double)rhoBar;
+            sU += (double)uSqr;
+            cnt += 1;
+            unsigned long long b = (unsigned long long)__double_as_longlong((double)uSqr);
+            mx = b > mx ? b : mx;
+        }
+    }
+    if (STATS) {
+        sR = warpSum(sR);
+        sU = warpSum(sU);
+        cnt = warpSumU(cnt);
+        mx = warpMaxU(mx);
+        if ((threadIdx.x & 31) == 0 && cnt > 0) {
+            atomicAdd(&acc->sumRhoBar, sR);
+            atomicAdd(&acc->sumUSqr, sU);
+            atomicAdd(&acc->count, cnt);
+            atomicMax(&acc->maxBits, mx);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- paired row kernel
+//
+// 2-byte storage forms: each thread owns two adjacent cells (z even, z + 1).
+// Populations that stay in the same z column (c_z = 0) move as one aligned
+// 32-bit word for both cells -- every population in the even step, nine of
+// nineteen in the odd step -- halving the memory instructions and doubling
+// the bytes per request; the other ten go as 16-bit values with the row-end
+// wrap / reflection selects of RowCell.  Needs nz even (rows and planes start
+// on 4-byte boundaries).
+template <typename S, bool ODD, bool STATS>
+__global__ void __launch_bounds__(128, 5)
+    pairRowStepKernel(DevLattice L, Planes<S> Pl, Deltas D, StepParams<typename StoreT<S>::R> P, StatsAcc* acc) {
+    using R = typename StoreT<S>::R;
+    const int x = blockIdx.z + 1, y = blockIdx.y + 1;
+    const int zA = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    double sR = 0., sU = 0.;
+    unsigned long long cnt = 0, mx = 0;
+    if (zA < L.nz) {
+        RowCell<S, ODD> ca(L, x, y, zA), cb(L, x, y, zA + 1);
+        const int kA = L.flags[ca.idx], kB = L.flags[cb.idx];
+        R fa[19], fb[19];
+        StoreT<S>::ld2(Pl.p[0] + ca.idx, fa[0], fb[0]);
+#pragma unroll
+        for (int i = 1; i < 19; ++i) {
+            if (!ODD) {
+                StoreT<S>::ld2(Pl.p[i] + ca.idx, fa[i], fb[i]);
+            } else if (cdir(i, 2) == 0) {
+                StoreT<S>::ld2(Pl.p[opp(i)] + (ca.idx - D.d[i]), fa[i], fb[i]);
+            } else {
+                const int mz = -cdir(i, 2);
+                {
+                    const bool ok = mz < 0 ? ca.okM : ca.okP;
+                    const int off = -D.d[i] + (mz < 0 ? ca.wrapM : ca.wrapP);
+                    fa[i] = StoreT<S>::ld(ok ? Pl.p[opp(i)] + (ca.idx + off) : Pl.p[i] + ca.idx);
+                }
+                {
+                    const bool ok = mz < 0 ? cb.okM : cb.okP;
+                    const int off = -D.d[i] + (mz < 0 ? cb.wrapM : cb.wrapP);
+                    fb[i] = StoreT<S>::ld(ok ? Pl.p[opp(i)] + (cb.idx + off) : Pl.p[i] + cb.idx);
+                }
+            }
+        }
+        const bool liveA = kA != K_NONE, liveB = kB != K_NONE;
+        R rbA = R(0), usA = R(0), rbB = R(0), usB = R(0);
+        bool gA = false, gB = false;
+        if (liveA) {
+            if (P.pending && isFace(kA)) completeIfFace<R>(L, ca.idx, kA, fa);
+            gA = collideCell<S>(L, P, ca.idx, kA, fa, rbA, usA, acc, STATS);
+        }
+        if (liveB) {
+            if (P.pending && isFace(kB)) completeIfFace<R>(L, cb.idx, kB, fb);
+            gB = collideCell<S>(L, P, cb.idx, kB, fb, rbB, usB, acc, STATS);
+        }
+        if (liveA && liveB) {
+            StoreT<S>::st2(Pl.p[0] + ca.idx, fa[0], fb[0]);
+#pragma unroll
+            for (int i = 1; i < 19; ++i) {
+                if (!ODD) {
+                    StoreT<S>::st2(Pl.p[opp(i)] + ca.idx, fa[i], fb[i]);
+                } else if (cdir(i, 2) == 0) {
+                    StoreT<S>::st2(Pl.p[i] + (ca.idx + D.d[i]), fa[i], fb[i]);
+                } else {
+                    const int cz = cdir(i, 2);
+                    {
+                        const bool ok = cz < 0 ? ca.okM : ca.okP;
+                        const int off = D.d[i] + (cz < 0 ? ca.wrapM : ca.wrapP);
+                        StoreT<S>::st(ok ? Pl.p[i] + (ca.idx + off) : Pl.p[opp(i)] + ca.idx, fa[i]);
+                    }
+                    {
+                        const bool ok = cz < 0 ? cb.okM : cb.okP;
+                        const int off = D.d[i] + (cz < 0 ? cb.wrapM : cb.wrapP);
+                        StoreT<S>::st(ok ? Pl.p[i] + (cb.idx + off) : Pl.p[opp(i)] + cb.idx, fb[i]);
+                    }
+                }
+            }
+        } else {
+            if (liveA) ca.store(Pl, D, fa);
+            if (liveB) cb.store(Pl, D, fb);
+        }
+        if (STATS) {
+            if (gA) {
+                sR += (double)rbA; sU += (double)usA; cnt += 1;
+                mx = (unsigned long long)__double_as_longlong((double)usA);
+            }
+            if (gB) {
+                sR += (double)rbB; sU += (double)usB; cnt += 1;
+                unsigned long long b = (unsigned long long)__double_as_longlong((double)usB);
+                mx = b > mx ? b : mx;
+            }
+        }
+    }
+    if (STATS) {
+        sR = warpSum(sR);
+        sU = warpSum(sU);
+        cnt = warpSumU(cnt);
+        mx = warpMaxU(mx);
+        if ((threadIdx.x & 31) == 0 && cnt > 0) {
+            atomicAdd(&acc->sumRhoBar, sR);
+            atomicAdd(&acc->sumUSqr, sU);
+            atomicAdd(&acc->count, cnt);
+            atomicMax(&acc->maxBits, mx);
+        }
+    }
 }
 
 // Rows on the x or y border of the domain, with the general addressing
