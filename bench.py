@@ -44,38 +44,16 @@ B_CELL = {"fp64": 305, "fp32": 153, "bf16": 77, "fp16": 77}
 
 
 def workload_geometry():
-    """Cell kinds and face values of the channel (same construction as the
-    parity cases, at full size)."""
-    from palabos_gb300 import native as N
-    nx, ny, nz = SHAPE
-    kinds = np.zeros(SHAPE, np.uint8)
-    bc = np.zeros(SHAPE + (3,))
-    kinds[:, 0, :] = N.BOUNCEBACK
-    kinds[:, -1, :] = N.BOUNCEBACK
-    kinds[:, :, 0] = N.BOUNCEBACK
-    kinds[:, :, -1] = N.BOUNCEBACK
-    kinds[0, 1:-1, 1:-1] = N.face_kind(N.REG_VELOCITY, 0, -1)
-    kinds[-1, 1:-1, 1:-1] = N.face_kind(N.REG_PRESSURE, 0, +1)
-    yy = (np.arange(ny) - 0.5) / (ny - 1)
-    zz = (np.arange(nz) - 0.5) / (nz - 1)
-    prof = 16.0 * 0.05 * (yy[:, None] * (1 - yy[:, None])) * (zz[None, :] * (1 - zz[None, :]))
-    bc[0, 1:-1, 1:-1, 0] = prof[1:-1, 1:-1]
-    bc[-1, 1:-1, 1:-1, 0] = 1.0
-    x = np.arange(nx)[:, None, None]
-    y = np.arange(ny)[None, :, None]
-    z = np.arange(nz)[None, None, :]
-    sphere = ((x - 64) ** 2 + (y - 64) ** 2 + (z - 64) ** 2 <= 16 * 16) & (kinds == N.BGK)
-    kinds[sphere] = N.MOMENTUM_EXCHANGE
-    return kinds, bc
+    """Cell kinds and face values of the channel (palabos_gb300.workloads.channel_sphere)."""
+    from palabos_gb300 import workloads
+    wl = workloads.channel_sphere(SHAPE, omega=OMEGA)
+    return wl.kinds, wl.bcval
 
 
 def build_lattice(precision, ctx=None):
-    from palabos_gb300 import lattice_from_description
-    kinds, bc = workload_geometry()
-    lat = lattice_from_description(*SHAPE, (0, 0, 0), OMEGA, kinds, bc, None, precision=precision, ctx=ctx)
-    lat.initialize_at_equilibrium(None, 1.0, (0.0, 0.0, 0.0))
-    lat.initialize()
-    return lat, kinds
+    from palabos_gb300 import workloads
+    wl = workloads.channel_sphere(SHAPE, omega=OMEGA)
+    return wl.lattice(precision, ctx), wl.kinds
 
 
 def algorithmic_bytes(kinds, precision):
@@ -321,6 +299,11 @@ def run_gpu(args):
             forms[prec] = {"mlups": round(cells / (ms * 1e-3) / 1e6, 1), "bytes_per_cell": B_CELL[prec],
                            "hbm_frac": round(b / (ms * 1e-3) / 1e9 / peak, 4)}
             l2.close()
+        # accuracy of each storage form against FP64 on a 128^3 Taylor-Green vortex
+        from palabos_gb300.accuracy import taylor_green_study
+        tg = taylor_green_study(n=128, steps=1000, every=250, slab=32, ctx=ctx)
+        for prec, acc in tg["forms"].items():
+            forms[prec]["taylor_green_128_1000steps"] = {k: round(v, 9) for k, v in acc.items()}
 
     if rank == 0:
         clocks = clk.summary()
@@ -361,9 +344,20 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-forms", action="store_true")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32", "bf16", "fp16"])
+    ap.add_argument("--accuracy", action="store_true",
+                    help="run only the Taylor-Green accuracy study (512^3, 5000 steps) and print its JSON")
+    ap.add_argument("--accuracy-n", type=int, default=512)
+    ap.add_argument("--accuracy-steps", type=int, default=5000)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.accuracy:
+        from palabos_gb300 import Context
+        from palabos_gb300.accuracy import taylor_green_study
+        ctx = Context(dist_env()[2])
+        r = taylor_green_study(n=args.accuracy_n, steps=args.accuracy_steps, every=500, slab=8, ctx=ctx)
+        print(json.dumps({"study": "taylor_green_storage_forms", **r}))
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

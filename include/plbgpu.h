@@ -174,6 +174,14 @@ int plbgpu_get_stats(plbgpu_ctx* ctx, int handle, double out[7]);
 int plbgpu_reduce(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1, int z0, int z1,
                   double* avg_energy, double* avg_density);
 
+/* computeVelocity / computeDensity (dataProcessors/dataAnalysisWrapper3D.h:80-132):
+ * the velocity (3 doubles per cell) or density (1 per cell) each cell's
+ * dynamics reports, over a box, in the transfer order (z fastest). */
+int plbgpu_compute_velocity(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1, int z0, int z1,
+                            double* out, size_t n);
+int plbgpu_compute_density(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1, int z0, int z1,
+                           double* out, size_t n);
+
 /* Run nsteps steps and time them with CUDA events recorded on the context's
  * stream (milliseconds). */
 int plbgpu_time_steps(plbgpu_ctx* ctx, int handle, int nsteps, int collect_stats, float* ms);

@@ -721,7 +721,7 @@ int plbgpu_reduce(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, 
     if ((rc = checkBox(c, d, x0, x1, y0, y1, z0, z1, &b))) return rc;
     CUDA_TRY(c, cudaMemsetAsync(d->red, 0, sizeof(ReduceAcc), c->stream));
     int k = launchers(d->precision).reduce(d->view(), d->odd, b, d->pending && d->bc ? 1 : 0, (double)1 / d->rho0,
-                                           d->bbRho - (double)1, d->red, c->stream);
+                                           d->bbRho, d->red, c->stream);
     c->launches += k - 1;
     if ((rc = launchBox(c))) return rc;
     ReduceAcc a;
@@ -731,6 +731,38 @@ int plbgpu_reduce(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, 
     if (avg_energy) *avg_energy = a.sumEnergy / (double)2 / cells;
     if (avg_density) *avg_density = a.sumRhoBar / cells + (double)1;
     return PLBGPU_OK;
+}
+
+namespace {
+int field(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, int what, double* out, size_t n) {
+    Domain* d;
+    Box b;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if ((rc = checkBox(c, d, x0, x1, y0, y1, z0, z1, &b))) return rc;
+    long long cells = boxCells(b);
+    const int comps = what == 0 ? 3 : 1;
+    if (!out || (long long)n != comps * cells)
+        return fail(c, PLBGPU_ERR_ARG, "expected %lld values, got %zu", comps * cells, n);
+    if ((rc = ensureStaging(c, sizeof(double) * n))) return rc;
+    int k = launchers(d->precision).field(d->view(), d->odd, b, d->pending && d->bc ? 1 : 0, (double)1 / d->rho0,
+                                          d->bbRho, what, static_cast<double*>(c->staging), c->stream);
+    c->launches += k - 1;
+    if ((rc = launchBox(c))) return rc;
+    CUDA_TRY(c, cudaMemcpyAsync(out, c->staging, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return PLBGPU_OK;
+}
+}  // namespace
+
+int plbgpu_compute_velocity(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, double* out,
+                            size_t n) {
+    return field(c, h, x0, x1, y0, y1, z0, z1, 0, out, n);
+}
+
+int plbgpu_compute_density(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, double* out,
+                           size_t n) {
+    return field(c, h, x0, x1, y0, y1, z0, z1, 1, out, n);
 }
 
 int plbgpu_time_steps(plbgpu_ctx* c, int h, int nsteps, int collect_stats, float* ms) {

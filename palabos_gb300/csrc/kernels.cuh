@@ -647,65 +647,87 @@ __global__ void insertKernel(DevLattice L, Box b, const double* in) {
         StoreT<S>::st(Pp + slotOf<ODD>(L, nb, idx, i), (typename StoreT<S>::R)in[o + i]);
 }
 
-// computeAverageEnergy / computeAverageDensity (dataAnalysisWrapper3D.hh:1226-1262)
-// on the post-stream, face-completed state.  Accumulation is in FP64.
+// Macroscopic values of one cell the way each dynamics reports them
+// (Cell::computeVelocity / computeRhoBar / computeDensity), on the
+// post-stream, face-completed state.  Returns false for cells outside the
+// lattice.  rho is computeDensity, rb is computeRhoBar.
 template <typename S, bool ODD>
-__global__ void reduceKernel(DevLattice L, Box b, int pending, typename StoreT<S>::R invRho0,
-                             double bbRhoBar, ReduceAcc* acc) {
+__device__ __forceinline__ bool cellMacroscopic(const DevLattice& L, int x, int y, int z, int pending,
+                                                typename StoreT<S>::R invRho0, double bbRho,
+                                                typename StoreT<S>::R* u, typename StoreT<S>::R& rb,
+                                                double& rho) {
     using R = typename StoreT<S>::R;
     using F = typename StoreT<S>::F;
+    const long long idx = ((long long)x * L.ny + y) * L.nz + z;
+    const int k = L.flags[idx];
+    if (k == K_NONE) return false;
+    Neighbourhood nb = neighbourhood(L, x, y, z);
+    const S* Pp = static_cast<const S*>(L.pop);
+    R f[19];
+#pragma unroll
+    for (int i = 0; i < 19; ++i) f[i] = StoreT<S>::ld(Pp + slotOf<ODD>(L, nb, idx, i));
+    if (pending && isFace(k)) completeIfFace<R>(L, idx, k, f);
+    u[0] = u[1] = u[2] = R(0);
+    rb = R(0);
+    if (k == K_BB || k == K_MEBB) {  // core/dynamics.hh:814-829, 875-877
+        rb = (R)(bbRho - 1.0);
+        rho = bbRho;
+        return true;
+    }
+    if (k == K_NODYN) {  // core/dynamics.hh:994-1008, 1055-1058
+        rho = bbRho;
+        return true;
+    }
+    if (k == K_BGK) {  // momentTemplates3D.h:402-408 compute_uLb
+        R jj[3], rr;
+        rhoBarJ<R>(f, rr, jj);
+        rb = rhoBarSeq<R>(f);
+        R invRho = invRhoOf(rb);
+        for (int d = 0; d < 3; ++d) u[d] = jj[d] * invRho;
+    } else if (k == K_GUO) {  // externalForceDynamics.hh:58-73
+        const F* fp = static_cast<const F*>(L.force);
+        R jj[3], rr;
+        rhoBarJ<R>(f, rr, jj);
+        R invRho = invRhoOf(rr);
+        R Fv[3] = {(R)fp[idx], (R)fp[L.n + idx], (R)fp[2 * L.n + idx]};
+        for (int d = 0; d < 3; ++d) u[d] = jj[d] * invRho + Fv[d] / (R)2;
+        rb = rhoBarSeq<R>(f);
+    } else if (k == K_INCBGK) {  // isoThermalDynamics.hh:1388-1395
+        R jj[3], rr;
+        rhoBarJ<R>(f, rr, jj);
+        for (int d = 0; d < 3; ++d) u[d] = jj[d] * invRho0;
+        rb = rhoBarSeq<R>(f);
+    } else if (isFace(k)) {
+        const int fam = faceFamily(k), dir = faceDir(k);
+        double v[3] = {L.bc[idx], L.bc[L.n + idx], L.bc[2 * L.n + idx]};
+        if (fam == 0 || fam == 2) {  // stored velocity, boundaryDynamics.hh:324-330
+            for (int d = 0; d < 3; ++d) u[d] = (R)v[d];
+            rb = velFaceRhoBarAny<R>(f, k, (R)v[dir]);
+        } else {  // boundaryDynamics.hh:790-812
+            rb = (R)v[0] - (R)1;
+            pressFaceJAny<R>(f, k, rb, u);
+            R invRho = invRhoOf(rb);
+            for (int d = 0; d < 3; ++d) { u[d] *= invRho; u[d] += (R)0.5 * (R)0; }
+        }
+    }
+    rho = (double)rb + 1.0;   // fullRho(rhoBar)
+    return true;
+}
+
+// computeAverageEnergy / computeAverageDensity (dataAnalysisWrapper3D.hh:1226-1262).
+// Accumulation is in FP64.
+template <typename S, bool ODD>
+__global__ void reduceKernel(DevLattice L, Box b, int pending, typename StoreT<S>::R invRho0, double bbRho,
+                             ReduceAcc* acc) {
+    using R = typename StoreT<S>::R;
     const int bnz = b.z1 - b.z0 + 1;
     const int dz = blockIdx.x * blockDim.x + threadIdx.x;
     double e = 0., r = 0.;
     if (dz < bnz) {
-        const int z = b.z0 + dz, y = b.y0 + blockIdx.y, x = b.x0 + blockIdx.z;
-        const long long idx = ((long long)x * L.ny + y) * L.nz + z;
-        const int k = L.flags[idx];
-        if (k != K_NONE) {
-            Neighbourhood nb = neighbourhood(L, x, y, z);
-            const S* Pp = static_cast<const S*>(L.pop);
-            R f[19];
-#pragma unroll
-            for (int i = 0; i < 19; ++i) f[i] = StoreT<S>::ld(Pp + slotOf<ODD>(L, nb, idx, i));
-            if (pending && isFace(k)) completeIfFace<R>(L, idx, k, f);
-            R u[3] = {R(0), R(0), R(0)};
-            R rb = R(0);
-            if (k == K_BB || k == K_MEBB) {
-                rb = (R)bbRhoBar;
-            } else if (k == K_NODYN) {
-                rb = R(0);
-            } else if (k == K_BGK) {  // momentTemplates3D.h:402-408 compute_uLb
-                R jj[3], rr;
-                rhoBarJ<R>(f, rr, jj);
-                rb = rhoBarSeq<R>(f);
-                R invRho = invRhoOf(rb);
-                for (int d = 0; d < 3; ++d) u[d] = jj[d] * invRho;
-            } else if (k == K_GUO) {  // externalForceDynamics.hh:58-73
-                const F* fp = static_cast<const F*>(L.force);
-                R jj[3], rr;
-                rhoBarJ<R>(f, rr, jj);
-                R invRho = invRhoOf(rr);
-                R Fv[3] = {(R)fp[idx], (R)fp[L.n + idx], (R)fp[2 * L.n + idx]};
-                for (int d = 0; d < 3; ++d) u[d] = jj[d] * invRho + Fv[d] / (R)2;
-                rb = rhoBarSeq<R>(f);
-            } else if (k == K_INCBGK) {  // isoThermalDynamics.hh:1388-1395
-                R jj[3], rr;
-                rhoBarJ<R>(f, rr, jj);
-                for (int d = 0; d < 3; ++d) u[d] = jj[d] * invRho0;
-                rb = rhoBarSeq<R>(f);
-            } else if (isFace(k)) {
-                int fam = faceFamily(k), dir = faceDir(k), ori = faceOri(k);
-                double v[3] = {L.bc[idx], L.bc[L.n + idx], L.bc[2 * L.n + idx]};
-                if (fam == 0 || fam == 2) {  // stored velocity, boundaryDynamics.hh:324-330
-                    for (int d = 0; d < 3; ++d) u[d] = (R)v[d];
-                    rb = velFaceRhoBarAny<R>(f, k, (R)v[dir]);
-                } else {  // boundaryDynamics.hh:790-812
-                    rb = (R)v[0] - (R)1;
-                    pressFaceJAny<R>(f, k, rb, u);
-                    R invRho = invRhoOf(rb);
-                    for (int d = 0; d < 3; ++d) { u[d] *= invRho; u[d] += (R)0.5 * (R)0; }
-                }
-            }
+        R u[3], rb;
+        double rho;
+        if (cellMacroscopic<S, ODD>(L, b.x0 + blockIdx.z, b.y0 + blockIdx.y, b.z0 + dz, pending, invRho0, bbRho, u,
+                                    rb, rho)) {
             e = (double)(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
             r = (double)rb;
         }
@@ -715,6 +737,28 @@ __global__ void reduceKernel(DevLattice L, Box b, int pending, typename StoreT<S
     if ((threadIdx.x & 31) == 0) {
         atomicAdd(&acc->sumEnergy, e);
         atomicAdd(&acc->sumRhoBar, r);
+    }
+}
+
+// computeVelocity (what = 0, 3 values per cell) / computeDensity (what = 1)
+// (dataAnalysisWrapper3D.h:80-132) into a packed box buffer, FP64.
+template <typename S, bool ODD>
+__global__ void fieldKernel(DevLattice L, Box b, int pending, typename StoreT<S>::R invRho0, double bbRho, int what,
+                            double* out) {
+    using R = typename StoreT<S>::R;
+    const int bnz = b.z1 - b.z0 + 1, bny = b.y1 - b.y0 + 1;
+    const int dz = blockIdx.x * blockDim.x + threadIdx.x;
+    if (dz >= bnz) return;
+    const long long o = ((long long)blockIdx.z * bny + blockIdx.y) * bnz + dz;
+    R u[3] = {R(0), R(0), R(0)}, rb = R(0);
+    double rho = 0.;
+    cellMacroscopic<S, ODD>(L, b.x0 + blockIdx.z, b.y0 + blockIdx.y, b.z0 + dz, pending, invRho0, bbRho, u, rb, rho);
+    if (what == 0) {
+        out[3 * o] = (double)u[0];
+        out[3 * o + 1] = (double)u[1];
+        out[3 * o + 2] = (double)u[2];
+    } else {
+        out[o] = rho;
     }
 }
 

@@ -22,10 +22,12 @@ struct Launchers {
     int (*completeFaces)(const DevLattice&, bool odd, cudaStream_t);
     int (*extract)(const DevLattice&, bool odd, Box, int pending, double* out, cudaStream_t);
     int (*insert)(const DevLattice&, bool odd, Box, const double* in, cudaStream_t);
-    int (*reduce)(const DevLattice&, bool odd, Box, int pending, double invRho0, double bbRhoBar,
+    int (*reduce)(const DevLattice&, bool odd, Box, int pending, double invRho0, double bbRho,
                   ReduceAcc*, cudaStream_t);
     int (*equilibrium)(const DevLattice&, bool odd, Box, const double* rhou, const double* cst,
                        double invRho0, cudaStream_t);
+    int (*field)(const DevLattice&, bool odd, Box, int pending, double invRho0, double bbRho, int what,
+                 double* out, cudaStream_t);
 };
 
 const Launchers& launchersFp64();

@@ -119,11 +119,18 @@ struct LaunchImpl {
         else insertKernel<S, false><<<g, kBlock, 0, s>>>(L, b, in);
         return 1;
     }
-    static int reduce(const DevLattice& L, bool odd, Box b, int pending, double invRho0, double bbRhoBar,
+    static int reduce(const DevLattice& L, bool odd, Box b, int pending, double invRho0, double bbRho,
                       ReduceAcc* acc, cudaStream_t s) {
         dim3 g = rowGrid(b.z1 - b.z0 + 1, b.y1 - b.y0 + 1, b.x1 - b.x0 + 1, kBlock);
-        if (odd) reduceKernel<S, true><<<g, kBlock, 0, s>>>(L, b, pending, (R)invRho0, bbRhoBar, acc);
-        else reduceKernel<S, false><<<g, kBlock, 0, s>>>(L, b, pending, (R)invRho0, bbRhoBar, acc);
+        if (odd) reduceKernel<S, true><<<g, kBlock, 0, s>>>(L, b, pending, (R)invRho0, bbRho, acc);
+        else reduceKernel<S, false><<<g, kBlock, 0, s>>>(L, b, pending, (R)invRho0, bbRho, acc);
+        return 1;
+    }
+    static int field(const DevLattice& L, bool odd, Box b, int pending, double invRho0, double bbRho, int what,
+                     double* out, cudaStream_t s) {
+        dim3 g = rowGrid(b.z1 - b.z0 + 1, b.y1 - b.y0 + 1, b.x1 - b.x0 + 1, kBlock);
+        if (odd) fieldKernel<S, true><<<g, kBlock, 0, s>>>(L, b, pending, (R)invRho0, bbRho, what, out);
+        else fieldKernel<S, false><<<g, kBlock, 0, s>>>(L, b, pending, (R)invRho0, bbRho, what, out);
         return 1;
     }
     static int equilibrium(const DevLattice& L, bool odd, Box b, const double* rhou, const double* cst,
@@ -136,7 +143,7 @@ struct LaunchImpl {
         return 1;
     }
     static const Launchers& table() {
-        static const Launchers t = {step, completeFaces, extract, insert, reduce, equilibrium};
+        static const Launchers t = {step, completeFaces, extract, insert, reduce, equilibrium, field};
         return t;
     }
 };

@@ -213,6 +213,20 @@ class DeviceLattice3D:
         self._check(self.lib.plbgpu_reduce(self.ctx.h, self.handle, *box, ctypes.byref(e), ctypes.byref(r)))
         return e.value, r.value
 
+    def compute_velocity(self, box=None):
+        """computeVelocity(lattice, box): (nx, ny, nz, 3) FP64."""
+        box = self._box(box)
+        out = np.empty(self._cells(box) * 3, np.float64)
+        self._check(self.lib.plbgpu_compute_velocity(self.ctx.h, self.handle, *box, _dp(out), out.size))
+        return out.reshape(box[1] - box[0] + 1, box[3] - box[2] + 1, box[5] - box[4] + 1, 3)
+
+    def compute_density(self, box=None):
+        """computeDensity(lattice, box): (nx, ny, nz) FP64."""
+        box = self._box(box)
+        out = np.empty(self._cells(box), np.float64)
+        self._check(self.lib.plbgpu_compute_density(self.ctx.h, self.handle, *box, _dp(out), out.size))
+        return out.reshape(box[1] - box[0] + 1, box[3] - box[2] + 1, box[5] - box[4] + 1)
+
     def compute_average_energy(self, box=None):
         return self.reduce(box)[0]
 

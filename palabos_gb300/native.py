@@ -76,6 +76,8 @@ SIGNATURES = {
     "plbgpu_collide_and_stream": [_vp, _i, _i, _i],
     "plbgpu_get_stats": [_vp, _i, _c_dbl_p],
     "plbgpu_reduce": [_vp, _i, *BOX, _c_dbl_p, _c_dbl_p],
+    "plbgpu_compute_velocity": [_vp, _i, *BOX, _c_dbl_p, _sz],
+    "plbgpu_compute_density": [_vp, _i, *BOX, _c_dbl_p, _sz],
     "plbgpu_time_steps": [_vp, _i, _i, _i, ctypes.POINTER(ctypes.c_float)],
     "plbgpu_cp_add_domain": [_vp, _l, _l, _l, _d, _c_int_p],
     "plbgpu_cp_send": [_vp, _i, *LBOX, ctypes.c_char_p, _sz],

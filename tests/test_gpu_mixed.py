@@ -57,3 +57,37 @@ def test_staged_rows_match_unstaged_geometry(precision):
         f = lat.receive()
         out.append(f[:, :, :8].astype(np.float64))   # depends only on y
     assert np.abs(out[0] - out[1]).max() < TOL[precision] * 0.03 + 1e-7
+
+
+def test_taylor_green_velocity_error_of_storage_forms():
+    """Small Taylor-Green vortex (64^3, 400 steps, omega close to 2): relative
+    velocity L2 error against the FP64 path of FP32 storage (measured 1.2e-5)
+    below 1e-4, FP16 storage (measured 1.2e-3) below 1e-2, BF16 storage below
+    2e-1, ordered by storage precision; kinetic energy of FP32 storage within
+    1e-4 of FP64 at every sampled time."""
+    from palabos_gb300.accuracy import taylor_green_study
+    r = taylor_green_study(n=64, steps=400, every=100, slab=16)
+    f = r["forms"]
+    print({p: v["vel_l2_rel"] for p, v in f.items()})
+    assert f["fp32"]["vel_l2_rel"] < 1e-4, f
+    assert f["fp16"]["vel_l2_rel"] < 1e-2, f
+    assert f["bf16"]["vel_l2_rel"] < 2e-1, f
+    assert f["fp32"]["vel_l2_rel"] < f["fp16"]["vel_l2_rel"] < f["bf16"]["vel_l2_rel"]
+    assert f["fp32"]["ke_rel_max"] < 1e-4, f
+    assert 0.0 < r["ke_decay_fp64"] < 1.0
+
+
+def test_compute_velocity_and_density_match_reductions():
+    """computeVelocity / computeDensity fields average to computeAverageEnergy /
+    computeAverageDensity."""
+    g, meta = goldens.load("channel_sphere")
+    lat = lattice_from_description(meta["nx"], meta["ny"], meta["nz"], meta["periodic"], meta["omega"],
+                                   g["flags"], g["bcval"], g["force"])
+    lat.send(g["f_init"])
+    lat.collide_and_stream(9)
+    u = lat.compute_velocity()
+    rho = lat.compute_density()
+    e, d = lat.reduce()
+    assert 0.5 * np.mean(np.sum(u * u, axis=-1)) == pytest.approx(e, rel=1e-12)
+    # BounceBack(rho=0) cells report density 0 and rho-bar -1: the averages agree
+    assert np.mean(rho) == pytest.approx(d, rel=1e-12)
