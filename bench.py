@@ -40,7 +40,7 @@ STATS_EVERY = 100
 FALLBACK_HBM_GBS = 6800.0
 # Algorithmic bytes per cell and step (AA pattern: every population read once
 # and written once, plus the one-byte cell kind).
-B_CELL = {"fp64": 305, "fp32": 153, "bf16": 77, "fp16": 77}
+B_CELL = {"fp64": 305, "fp32": 153, "bf16": 77, "fp16": 77, "bf16sr": 77}
 
 
 def workload_geometry():
@@ -291,7 +291,7 @@ def run_gpu(args):
     forms = {head: {"mlups": round(cells / (k_ms * 1e-3) / 1e6, 1), "bytes_per_cell": B_CELL[head],
                     "hbm_frac": round(achieved / peak, 4)}}
     if not args.skip_forms:
-        for prec in [p for p in ("fp64", "fp32", "bf16", "fp16") if p != head]:
+        for prec in [p for p in ("fp64", "fp32", "bf16", "fp16", "bf16sr") if p != head]:
             l2, _ = build_lattice(prec, ctx)
             n = min(K, 400)
             ms = time_form(l2, n, 10) / n
@@ -343,7 +343,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-forms", action="store_true")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32", "bf16", "fp16"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32", "bf16", "fp16", "bf16sr"])
     ap.add_argument("--accuracy", action="store_true",
                     help="run only the Taylor-Green accuracy study (512^3, 5000 steps) and print its JSON")
     ap.add_argument("--accuracy-n", type=int, default=512)

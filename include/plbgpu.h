@@ -46,6 +46,9 @@ typedef struct plbgpu_ctx plbgpu_ctx;
 #define PLBGPU_FP32 1
 #define PLBGPU_BF16 2
 #define PLBGPU_FP16 3
+/* BF16 storage written with stochastic rounding (zero-mean rounding error;
+ * reproducible: the random bits hash the slot address and the step count). */
+#define PLBGPU_BF16_SR 4
 
 /* Cell kinds (dynamics) -- one byte per cell.  Face kinds are
  * base + 2*direction + (orientation > 0 ? 1 : 0). */

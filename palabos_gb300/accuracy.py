@@ -1,7 +1,8 @@
 """Accuracy of the reduced-precision storage forms on the Taylor-Green vortex.
 
 Runs the FP64 form (the reference-exact path) and the FP32-compute forms with
-FP32, BF16 and FP16 f-bar storage side by side on the same periodic
+FP32, BF16 (round to nearest and stochastic rounding) and FP16 f-bar storage
+side by side on the same periodic
 Taylor-Green vortex, and reports for each form
 
   vel_l2_rel   ||u - u_fp64||_2 / ||u_fp64||_2 over all cells at the end,
@@ -22,7 +23,7 @@ from . import workloads
 from .lattice import DeviceLattice3D
 
 
-def taylor_green_study(n=512, steps=5000, forms=("fp32", "bf16", "fp16"), every=500, slab=8, ctx=None):
+def taylor_green_study(n=512, steps=5000, forms=("fp32", "bf16", "fp16", "bf16sr"), every=500, slab=8, ctx=None):
     wl = workloads.taylor_green(n)
     names = ("fp64",) + tuple(forms)
     lats = {}

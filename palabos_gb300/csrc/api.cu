@@ -42,6 +42,7 @@ struct Domain {
     bool odd = false;            // AA parity of the stored state
     bool pending = false;        // faces still need their post-stream completion
     bool statsValid = false;
+    unsigned long long steps = 0;   // time steps taken (salt of stochastic rounding)
     double lastStats[7] = {0, 0, 0, 0, 0, 0, 0};
     unsigned long long deviceBytes = 0;
 
@@ -99,12 +100,13 @@ const Launchers& launchers(int precision) {
     case PLBGPU_FP32: return launchersFp32();
     case PLBGPU_BF16: return launchersBf16();
     case PLBGPU_FP16: return launchersFp16();
+    case PLBGPU_BF16_SR: return launchersBf16Sr();
     default: return launchersFp64();
     }
 }
 
 size_t elemSizeOf(int precision) {
-    return precision == PLBGPU_FP64 ? 8 : precision == PLBGPU_FP32 ? 4 : 2;
+    return precision == PLBGPU_FP64 ? 8 : precision == PLBGPU_FP32 ? 4 : 2;   // BF16, FP16, BF16_SR: 2
 }
 
 int lookup(plbgpu_ctx* c, int h, Domain** d) {
@@ -270,6 +272,7 @@ StepConsts consts(const Domain* d) {
     s.t4_omega = ((double)1 / (double)36) * d->omega;
     s.invRho0 = (double)1 / d->rho0;
     s.pending = d->pending ? 1 : 0;
+    s.seed = (unsigned)(d->steps * 0x9E3779B97F4A7C15ull >> 32);
     return s;
 }
 
@@ -366,7 +369,7 @@ int plbgpu_add_domain(plbgpu_ctx* c, int nx, int ny, int nz, int precision, int*
     // x and y index the grid's z and y dimensions (at most 65535 blocks each).
     if (nx < 1 || ny < 1 || nz < 1 || nx > 65535 || ny > 65535)
         return fail(c, PLBGPU_ERR_ARG, "domain extent %dx%dx%d (nx, ny must be in [1, 65535])", nx, ny, nz);
-    if (precision < PLBGPU_FP64 || precision > PLBGPU_FP16)
+    if (precision < PLBGPU_FP64 || precision > PLBGPU_BF16_SR)
         return fail(c, PLBGPU_ERR_ARG, "unknown precision %d", precision);
     CUDA_TRY(c, cudaSetDevice(c->device));
     std::unique_ptr<Domain> d(new Domain());
@@ -684,6 +687,7 @@ int plbgpu_collide_and_stream(plbgpu_ctx* c, int h, int nsteps, int collect_stat
         if ((rc = launchBox(c))) return rc;
         d->odd = !d->odd;
         d->pending = hasFaces;
+        d->steps += 1;
     }
     if (collect_stats) d->statsValid = true;
     return PLBGPU_OK;

@@ -27,15 +27,19 @@
 namespace plbgpu {
 
 template <typename S> struct StoreT;
+// Every storage type has a store with a `salt` argument; only the
+// stochastically rounded BF16 type uses it.
 template <> struct StoreT<double> {
     using R = double; using F = double;
     static __device__ __forceinline__ double ld(const double* p) { return *p; }
     static __device__ __forceinline__ void st(double* p, double v) { *p = v; }
+    static __device__ __forceinline__ void st(double* p, double v, unsigned) { *p = v; }
 };
 template <> struct StoreT<float> {
     using R = float; using F = float;
     static __device__ __forceinline__ float ld(const float* p) { return *p; }
     static __device__ __forceinline__ void st(float* p, float v) { *p = v; }
+    static __device__ __forceinline__ void st(float* p, float v, unsigned) { *p = v; }
 };
 template <> struct StoreT<__nv_bfloat16> {
     using R = float; using F = float;
@@ -49,6 +53,8 @@ template <> struct StoreT<__nv_bfloat16> {
     static __device__ __forceinline__ void st2(__nv_bfloat16* p, float a, float b) {
         *reinterpret_cast<__nv_bfloat162*>(p) = __floats2bfloat162_rn(a, b);
     }
+    static __device__ __forceinline__ void st(__nv_bfloat16* p, float v, unsigned) { st(p, v); }
+    static __device__ __forceinline__ void st2(__nv_bfloat16* p, float a, float b, unsigned) { st2(p, a, b); }
 };
 template <> struct StoreT<__half> {
     using R = float; using F = float;
@@ -61,6 +67,53 @@ template <> struct StoreT<__half> {
     static __device__ __forceinline__ void st2(__half* p, float a, float b) {
         *reinterpret_cast<__half2*>(p) = __floats2half2_rn(a, b);
     }
+    static __device__ __forceinline__ void st(__half* p, float v, unsigned) { st(p, v); }
+    static __device__ __forceinline__ void st2(__half* p, float a, float b, unsigned) { st2(p, a, b); }
+};
+
+// BF16 storage written with stochastic rounding: the 16 bits dropped from the
+// FP32 value are compared with 16 pseudo-random bits, so a value rounds up
+// with probability equal to its distance from the lower BF16 neighbour and
+// the rounding error has zero mean.  Round-to-nearest makes the error of the
+// stored populations a deterministic function of the state, which biases the
+// conserved moments the same way step after step.  The random bits come from
+// a short multiplicative integer hash of the slot address and a per-step
+// salt (high half of the product after an xorshift), so a run is
+// reproducible.
+struct bf16sr {
+    __nv_bfloat16 v;
+};
+
+__device__ __forceinline__ unsigned srBits(const void* p, unsigned salt) {
+    unsigned h = ((unsigned)(reinterpret_cast<unsigned long long>(p) >> 1) ^ salt) * 0x9E3779B1u;
+    h ^= h >> 15;
+    return h * 0x85EBCA77u;
+}
+
+// FP32 -> BF16 rounding up when the dropped 16 bits plus 16 random bits carry.
+__device__ __forceinline__ unsigned short bf16Stochastic(float v, unsigned bits) {
+    unsigned u = __float_as_uint(v);
+    u += bits >> 16;
+    return (unsigned short)(u >> 16);
+}
+
+template <> struct StoreT<bf16sr> {
+    using R = float; using F = float;
+    static __device__ __forceinline__ float ld(const bf16sr* p) { return __bfloat162float(p->v); }
+    static __device__ __forceinline__ void st(bf16sr* p, float v, unsigned salt) {
+        *reinterpret_cast<unsigned short*>(p) = bf16Stochastic(v, srBits(p, salt));
+    }
+    static __device__ __forceinline__ void st(bf16sr* p, float v) { st(p, v, 0u); }
+    static __device__ __forceinline__ void ld2(const bf16sr* p, float& a, float& b) {
+        float2 v = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(p));
+        a = v.x; b = v.y;
+    }
+    static __device__ __forceinline__ void st2(bf16sr* p, float a, float b, unsigned salt) {
+        const unsigned h = srBits(p, salt);
+        const unsigned lo = bf16Stochastic(a, h), hi = bf16Stochastic(b, h << 16);
+        *reinterpret_cast<unsigned*>(p) = lo | (hi << 16);
+    }
+    static __device__ __forceinline__ void st2(bf16sr* p, float a, float b) { st2(p, a, b, 0u); }
 };
 
 struct DevLattice {
@@ -81,6 +134,7 @@ struct StepParams {
     BgkConst<R> bgk;
     R invRho0;      // incompressible BGK 1/rho0
     int pending;    // boundary faces still need their post-stream completion
+    unsigned seed;  // per-step salt of the stochastically rounded storage
 };
 
 struct StatsAcc {
@@ -157,19 +211,19 @@ __device__ __forceinline__ void loadCell(const DevLattice& L, const Neighbourhoo
 // Write the 19 post-collision populations of cell idx for the given parity.
 template <typename S, bool ODD>
 __device__ __forceinline__ void storeCell(const DevLattice& L, const Neighbourhood& nb, long long idx,
-                                          const typename StoreT<S>::R* f) {
+                                          const typename StoreT<S>::R* f, unsigned salt) {
     S* P = static_cast<S*>(L.pop);
     const long long st = L.stride;
-    StoreT<S>::st(P + idx, f[0]);
+    StoreT<S>::st(P + idx, f[0], salt);
 #pragma unroll
     for (int i = 1; i < 19; ++i) {
         if (!ODD) {
-            StoreT<S>::st(P + opp(i) * st + idx, f[i]);
+            StoreT<S>::st(P + opp(i) * st + idx, f[i], salt);
         } else {
             long long off;
             bool ok = nb.move(i, +1, off);
-            if (ok) StoreT<S>::st(P + i * st + idx + off, f[i]);
-            else StoreT<S>::st(P + opp(i) * st + idx, f[i]);
+            if (ok) StoreT<S>::st(P + i * st + idx + off, f[i], salt);
+            else StoreT<S>::st(P + opp(i) * st + idx, f[i], salt);
         }
     }
 }
@@ -319,7 +373,7 @@ __device__ __forceinline__ bool processCellGeneral(const DevLattice& L, const St
     loadCell<S, ODD>(L, nb, idx, f);
     if (P.pending && isFace(k)) completeIfFace<R>(L, idx, k, f);
     bool g = collideCell<S>(L, P, idx, k, f, rhoBar, uSqr, acc, STATS);
-    storeCell<S, ODD>(L, nb, idx, f);
+    storeCell<S, ODD>(L, nb, idx, f, P.seed);
     return g;
 }
 
@@ -372,22 +426,22 @@ struct RowCell {
         }
     }
 
-    __device__ __forceinline__ void store(const Planes<S>& Pl, const Deltas& D,
-                                          const typename StoreT<S>::R* f) const {
-        StoreT<S>::st(Pl.p[0] + idx, f[0]);
+    __device__ __forceinline__ void store(const Planes<S>& Pl, const Deltas& D, const typename StoreT<S>::R* f,
+                                          unsigned salt) const {
+        StoreT<S>::st(Pl.p[0] + idx, f[0], salt);
 #pragma unroll
         for (int i = 1; i < 19; ++i) {
             if (!ODD) {
-                StoreT<S>::st(Pl.p[opp(i)] + idx, f[i]);
+                StoreT<S>::st(Pl.p[opp(i)] + idx, f[i], salt);
             } else {
                 const int cz = cdir(i, 2);    // the destination is x + c_i
                 if (cz == 0) {
-                    StoreT<S>::st(Pl.p[i] + (idx + D.d[i]), f[i]);
+                    StoreT<S>::st(Pl.p[i] + (idx + D.d[i]), f[i], salt);
                 } else {
                     const bool ok = cz < 0 ? okM : okP;
                     const int off = D.d[i] + (cz < 0 ? wrapM : wrapP);
                     S* a = ok ? Pl.p[i] + (idx + off) : Pl.p[opp(i)] + idx;
-                    StoreT<S>::st(a, f[i]);
+                    StoreT<S>::st(a, f[i], salt);
                 }
             }
         }
@@ -430,7 +484,7 @@ __global__ void __launch_bounds__(128, RowShape<S>::blocks)
         R rhoBar = R(0), uSqr = R(0);
         if (P.pending && isFace(kind[c])) completeIfFace<R>(L, rc.idx, kind[c], f[c]);
         bool g = collideCell<S>(L, P, rc.idx, kind[c], f[c], rhoBar, uSqr, acc, STATS);
-        rc.store(Pl, D, f[c]);
+        rc.store(Pl, D, f[c], P.seed);
         if (STATS && g) {
             sR += (double)rhoBar;
             sU += (double)uSqr;
@@ -507,30 +561,30 @@ __global__ void __launch_bounds__(128, 5)
             gB = collideCell<S>(L, P, cb.idx, kB, fb, rbB, usB, acc, STATS);
         }
         if (liveA && liveB) {
-            StoreT<S>::st2(Pl.p[0] + ca.idx, fa[0], fb[0]);
+            StoreT<S>::st2(Pl.p[0] + ca.idx, fa[0], fb[0], P.seed);
 #pragma unroll
             for (int i = 1; i < 19; ++i) {
                 if (!ODD) {
-                    StoreT<S>::st2(Pl.p[opp(i)] + ca.idx, fa[i], fb[i]);
+                    StoreT<S>::st2(Pl.p[opp(i)] + ca.idx, fa[i], fb[i], P.seed);
                 } else if (cdir(i, 2) == 0) {
-                    StoreT<S>::st2(Pl.p[i] + (ca.idx + D.d[i]), fa[i], fb[i]);
+                    StoreT<S>::st2(Pl.p[i] + (ca.idx + D.d[i]), fa[i], fb[i], P.seed);
                 } else {
                     const int cz = cdir(i, 2);
                     {
                         const bool ok = cz < 0 ? ca.okM : ca.okP;
                         const int off = D.d[i] + (cz < 0 ? ca.wrapM : ca.wrapP);
-                        StoreT<S>::st(ok ? Pl.p[i] + (ca.idx + off) : Pl.p[opp(i)] + ca.idx, fa[i]);
+                        StoreT<S>::st(ok ? Pl.p[i] + (ca.idx + off) : Pl.p[opp(i)] + ca.idx, fa[i], P.seed);
                     }
                     {
                         const bool ok = cz < 0 ? cb.okM : cb.okP;
                         const int off = D.d[i] + (cz < 0 ? cb.wrapM : cb.wrapP);
-                        StoreT<S>::st(ok ? Pl.p[i] + (cb.idx + off) : Pl.p[opp(i)] + cb.idx, fb[i]);
+                        StoreT<S>::st(ok ? Pl.p[i] + (cb.idx + off) : Pl.p[opp(i)] + cb.idx, fb[i], P.seed);
                     }
                 }
             }
         } else {
-            if (liveA) ca.store(Pl, D, fa);
-            if (liveB) cb.store(Pl, D, fb);
+            if (liveA) ca.store(Pl, D, fa, P.seed);
+            if (liveB) cb.store(Pl, D, fb, P.seed);
         }
         if (STATS) {
             if (gA) {

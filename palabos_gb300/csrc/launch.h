@@ -14,6 +14,7 @@ struct StepConsts {
     double omega, one_m_omega, t0_omega, t1_omega, t4_omega;
     double invRho0;
     int pending;
+    unsigned seed;
 };
 
 // Each launcher returns the number of kernels it launched.
@@ -34,6 +35,7 @@ const Launchers& launchersFp64();
 const Launchers& launchersFp32();
 const Launchers& launchersBf16();
 const Launchers& launchersFp16();
+const Launchers& launchersBf16Sr();
 
 inline dim3 rowGrid(int nz, int ny, int nx, int block) {
     return dim3((unsigned)((nz + block - 1) / block), (unsigned)ny, (unsigned)nx);

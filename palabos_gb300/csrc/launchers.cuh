@@ -98,6 +98,7 @@ struct LaunchImpl {
         p.bgk.t4_omega = (R)c.t4_omega;
         p.invRho0 = (R)c.invRho0;
         p.pending = c.pending;
+        p.seed = c.seed;
         if (odd) return stats ? stepSplit<true, true>(L, p, acc, s) : stepSplit<true, false>(L, p, acc, s);
         return stats ? stepSplit<false, true>(L, p, acc, s) : stepSplit<false, false>(L, p, acc, s);
     }

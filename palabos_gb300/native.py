@@ -18,8 +18,8 @@ OK = 0
 ERRORS = {-1: "PLBGPU_ERR_ARG", -2: "PLBGPU_ERR_HANDLE", -3: "PLBGPU_ERR_CUDA",
           -4: "PLBGPU_ERR_NOMEM", -5: "PLBGPU_ERR_STATE"}
 
-FP64, FP32, BF16, FP16 = 0, 1, 2, 3
-PRECISIONS = {"fp64": FP64, "fp32": FP32, "bf16": BF16, "fp16": FP16}
+FP64, FP32, BF16, FP16, BF16_SR = 0, 1, 2, 3, 4
+PRECISIONS = {"fp64": FP64, "fp32": FP32, "bf16": BF16, "fp16": FP16, "bf16sr": BF16_SR}
 
 BGK, GUO, INCBGK, BOUNCEBACK, MOMENTUM_EXCHANGE, NODYNAMICS = 0, 1, 2, 3, 4, 5
 REG_VELOCITY, REG_PRESSURE, ZOUHE_VELOCITY, ZOUHE_PRESSURE = 6, 12, 18, 24
