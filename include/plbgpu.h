@@ -189,6 +189,31 @@ int plbgpu_compute_density(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, 
  * stream (milliseconds). */
 int plbgpu_time_steps(plbgpu_ctx* ctx, int handle, int nsteps, int collect_stats, float* ms);
 
+/* ------------------------------------------------------------ adjoint */
+
+/* Discrete adjoint of the collide-and-stream step (no counterpart in the
+ * reference), for domains of BGK, Guo, incompressible BGK, bounce-back and
+ * no-dynamics cells.  The objective is J = 1/2 sum over cells |u(T) - u*|^2
+ * with u the velocity each cell's dynamics reports (computeVelocity,
+ * dataProcessors/dataAnalysisWrapper3D.h:127-132).
+ *
+ * plbgpu_adjoint_forward: run T steps from the current state, keeping a
+ * checkpoint every K steps (K divides T); the domain ends at step T.
+ * plbgpu_adjoint_backward: J, dJ/dF per cell (3 doubles per cell, transfer
+ * order; may be NULL) and dJ/domega for that run, recomputing each segment
+ * of K steps from its checkpoint; `ms` (may be NULL) receives the device time
+ * of the backward sweep, recomputation included.
+ * plbgpu_tangent_linear (FP64 domains): J and the directional derivative
+ * dJ = grad J . (dforce, domega) from a dual-number run of T steps from the
+ * current state, which it leaves unchanged. */
+int plbgpu_adjoint_forward(plbgpu_ctx* ctx, int handle, int T, int K);
+int plbgpu_adjoint_backward(plbgpu_ctx* ctx, int handle, const double* u_target, size_t n_target,
+                            double* objective, double* grad_force, size_t n_grad, double* grad_omega,
+                            float* ms);
+int plbgpu_tangent_linear(plbgpu_ctx* ctx, int handle, int T, const double* dforce, size_t n_dforce,
+                          double domega, const double* u_target, size_t n_target, double* objective,
+                          double* directional);
+
 /* ------------------------------------------------------------ co-processor form */
 
 /* The four calls of plb::CoProcessor3D<double> (coProcessors/coProcessor3D.h:41-116)

@@ -43,6 +43,7 @@ def lib():
             fn.restype = ctypes.c_int
         _lib.orc_initialize.argtypes = [ctypes.POINTER(_Params), u8, dp, dp, dp]
         _lib.orc_reduce.argtypes = [ctypes.POINTER(_Params), u8, dp, dp, dp, dp, dp]
+        _lib.orc_velocity.argtypes = [ctypes.POINTER(_Params), u8, dp, dp, dp, dp]
         _lib.orc_mebb_masks.argtypes = [ctypes.POINTER(_Params), u8, ctypes.POINTER(ctypes.c_uint32)]
         _lib.orc_set_threads.argtypes = [ctypes.c_int]
         _lib.orc_max_threads.restype = ctypes.c_int
@@ -100,6 +101,13 @@ class OracleLattice:
         lib().orc_reduce(ctypes.byref(self.p), self._u8(), _dp(self.bcval), _dp(self.force),
                          _dp(f), ctypes.byref(e), ctypes.byref(d))
         return e.value, d.value
+
+    def velocity(self, f):
+        """computeVelocity of every cell, shape (nx, ny, nz, 3)."""
+        f = np.ascontiguousarray(f, np.float64)
+        out = np.zeros(self.flags.size * 3)
+        lib().orc_velocity(ctypes.byref(self.p), self._u8(), _dp(self.bcval), _dp(self.force), _dp(f), _dp(out))
+        return out.reshape(self.shape + (3,))
 
     def mebb_masks(self):
         out = np.zeros(self.flags.size, np.uint32)

@@ -672,6 +672,17 @@ int orc_reduce(const orc_params* p, const uint8_t* flags, const double* bcval, c
     return 0;
 }
 
+/* computeVelocity of every cell (3 doubles per cell). */
+int orc_velocity(const orc_params* p, const uint8_t* flags, const double* bcval, const double* force,
+                 const double* f, double* u) {
+    orc_lattice L;
+    setup(&L, p, flags, bcval, force);
+    long n = (long)p->nx * p->ny * p->nz;
+    for (long id = 0; id < n; ++id) cell_velocity(&L, id, f + id * 19, u + 3 * id);
+    free(L.mebbMask);
+    return 0;
+}
+
 /* Expose the fluid-direction masks (for tests of the device-side masks). */
 int orc_mebb_masks(const orc_params* p, const uint8_t* flags, uint32_t* out) {
     orc_lattice L;

@@ -24,7 +24,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
           "-I", os.path.join(ROOT, "include")]
 # (source, fmad)
-UNITS = [("api.cu", False), ("step_fp64.cu", False), ("step_mixed.cu", True), ("noalloc.cu", False)]
+UNITS = [("api.cu", False), ("step_fp64.cu", False), ("step_mixed.cu", True), ("noalloc.cu", False), ("adjoint.cu", False)]
 
 
 def nvcc() -> str:

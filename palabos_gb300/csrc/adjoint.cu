@@ -1,0 +1,676 @@
+// Discrete adjoint of the collide-and-stream step, with checkpointing, and a
+// forward-mode (dual-number) tangent of the same step.  No counterpart in the
+// reference: it differentiates the reference's step exactly as the fused
+// kernels compute it.
+//
+// State: f-bar in natural (post-stream) order, structure of arrays, in the
+// arithmetic type R (double for the FP64 form, float otherwise); plane i of
+// state k lives at buf + (k * 19 + i) * n.  The step used here is a two-buffer
+// push step with the same per-cell collision code as the fused kernels, so
+// the FP64 trajectory is bit-identical to the domain's own.
+//
+// Objective: J = 1/2 sum over cells |u(T) - u*|^2, u the velocity each cell's
+// dynamics reports (computeVelocity).  Dynamics: BGK, Guo-forced BGK,
+// incompressible BGK, bounce-back, no-dynamics.
+//
+// Reverse step at cell x, given lambda^{n+1}:
+//   mu_i(x)  = lambda^{n+1}_i(x + c_i), or lambda^{n+1}_opp(i)(x) where the
+//              push step reflected the population (transpose of streaming);
+//   lambda^n = (d collide / d f)^T mu at the pre-collision state f^n(x),
+//              recomputed from the last checkpoint;
+//   dJ/dF(x) += (d collide / d F)^T mu,   dJ/domega += (d collide / d omega)^T mu.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <new>
+#include <vector>
+
+#include "../../include/plbgpu.h"
+#include "launch.h"
+
+namespace plbgpu {
+
+// ---------------------------------------------------------------- dual numbers
+
+struct Dual {
+    double v, d;
+    __host__ __device__ Dual() : v(0.), d(0.) {}
+    __host__ __device__ Dual(double x) : v(x), d(0.) {}
+    __host__ __device__ Dual(double x, double y) : v(x), d(y) {}
+    __host__ __device__ Dual& operator+=(const Dual& o) { v += o.v; d += o.d; return *this; }
+    __host__ __device__ Dual& operator-=(const Dual& o) { v -= o.v; d -= o.d; return *this; }
+    __host__ __device__ Dual& operator*=(const Dual& o) { d = d * o.v + v * o.d; v *= o.v; return *this; }
+};
+__host__ __device__ inline Dual operator+(Dual a, const Dual& b) { return a += b; }
+__host__ __device__ inline Dual operator-(Dual a, const Dual& b) { return a -= b; }
+__host__ __device__ inline Dual operator*(Dual a, const Dual& b) { return a *= b; }
+__host__ __device__ inline Dual operator-(const Dual& a) { return Dual(-a.v, -a.d); }
+__host__ __device__ inline Dual operator/(const Dual& a, const Dual& b) {
+    const double q = a.v / b.v;
+    return Dual(q, (a.d - q * b.d) / b.v);
+}
+__device__ inline Dual invRhoOf(Dual rhoBar) {
+    const double r = 1.0 / (rhoBar.v + 1.0);
+    return Dual(r, -rhoBar.d * r * r);
+}
+
+template <typename R> __device__ inline double valueOf(const R& x) { return (double)x; }
+template <> __device__ inline double valueOf<Dual>(const Dual& x) { return x.v; }
+template <typename R> __device__ inline double tangentOf(const R&) { return 0.; }
+template <> __device__ inline double tangentOf<Dual>(const Dual& x) { return x.d; }
+
+// ---------------------------------------------------------------- per-cell forward
+
+template <typename R>
+__device__ __forceinline__ void adjCollide(int k, R* f, const R* F, const BgkConst<R>& bc, R invRho0) {
+    R rhoBar, j[3];
+    switch (k) {
+    case K_BGK:
+        rhoBarJ<R>(f, rhoBar, j);
+        bgkCollide<R>(f, rhoBar, j, bc, invRhoOf(rhoBar));
+        break;
+    case K_GUO: {
+        R rb = rhoBarSeq<R>(f);
+        R rb2, jj[3], u[3];
+        rhoBarJ<R>(f, rb2, jj);
+        R invRho = invRhoOf(rb2);
+        for (int d = 0; d < 3; ++d) u[d] = jj[d] * invRho + F[d] / (R)2;
+        R rho = rb + (R)1;
+        for (int d = 0; d < 3; ++d) j[d] = rho * u[d];
+        bgkCollide<R>(f, rb, j, bc, invRhoOf(rb));
+        addGuoForce<R>(f, F, u, bc.omega);
+        break;
+    }
+    case K_INCBGK:
+        rhoBarJ<R>(f, rhoBar, j);
+        bgkCollide<R>(f, rhoBar, j, bc, invRho0);
+        break;
+    case K_BB:
+        for (int i = 1; i <= 9; ++i) {
+            R t = f[i]; f[i] = f[i + 9]; f[i + 9] = t;
+        }
+        break;
+    default:
+        break;
+    }
+}
+
+template <typename R>
+__device__ __forceinline__ BgkConst<R> bgkConsts(R omega) {
+    BgkConst<R> b;
+    b.omega = omega;
+    b.one_m_omega = (R)1 - omega;
+    b.t0_omega = tw<R>(0) * omega;
+    b.t1_omega = tw<R>(1) * omega;
+    b.t4_omega = tw<R>(4) * omega;
+    return b;
+}
+
+// Guo force of a cell: FP64 planes for the FP64 form, FP32 otherwise; `dF`
+// (tangent runs only) gives its direction.
+template <typename R>
+__device__ __forceinline__ void cellForce(const DevLattice& L, bool fp64Force, long long idx, const double* dF, R* F) {
+    for (int d = 0; d < 3; ++d) F[d] = R(0);
+    if (L.force) {
+        if (fp64Force) {
+            const double* fp = static_cast<const double*>(L.force);
+            for (int d = 0; d < 3; ++d) F[d] = R(fp[d * L.n + idx]);
+        } else {
+            const float* fp = static_cast<const float*>(L.force);
+            for (int d = 0; d < 3; ++d) F[d] = R(fp[d * L.n + idx]);
+        }
+    }
+}
+__device__ __forceinline__ void cellForce(const DevLattice& L, bool fp64Force, long long idx, const double* dF,
+                                          Dual* F) {
+    double v[3] = {0., 0., 0.};
+    if (L.force) {
+        const double* fp = static_cast<const double*>(L.force);
+        for (int d = 0; d < 3; ++d) v[d] = fp[d * L.n + idx];
+    }
+    for (int d = 0; d < 3; ++d) F[d] = Dual(v[d], dF ? dF[d * L.n + idx] : 0.);
+}
+
+// Velocity the way computeVelocity reports it (momentTemplates3D.h:402-408,
+// externalForceDynamics.hh:58-73, isoThermalDynamics.hh:1388-1395); zero on
+// walls and no-dynamics cells.
+template <typename R>
+__device__ __forceinline__ void cellVelocity(int k, const R* f, const R* F, R invRho0, R* u) {
+    u[0] = u[1] = u[2] = R(0);
+    if (k == K_BGK || k == K_GUO || k == K_INCBGK) {
+        R rb, j[3];
+        rhoBarJ<R>(f, rb, j);
+        if (k == K_INCBGK) {
+            for (int d = 0; d < 3; ++d) u[d] = j[d] * invRho0;
+        } else {
+            R invRho = invRhoOf(k == K_BGK ? rhoBarSeq<R>(f) : rb);
+            for (int d = 0; d < 3; ++d) u[d] = j[d] * invRho + (k == K_GUO ? F[d] / (R)2 : R(0));
+        }
+    }
+}
+
+// ---------------------------------------------------------------- per-cell reverse
+
+// lam = (d out / d f)^T mu for out = collide(f; F, omega); gF += (d out / d F)^T mu;
+// returns (d out / d omega)^T mu.  BGK in shifted variables:
+//   out_i = (1 - w) f_i + w feq_i(rhoBar, J) + a G_i,  a = 1 - w/2,
+//   feq_i = t_i (rhoBar + 3 e_i + v (4.5 e_i^2 - 1.5 |J|^2)),  e_i = c_i.J,
+//   v = 1/rho (1/rho0 for incompressible BGK),  rho = rhoBar + 1,
+//   Guo: u = j/rho + F/2, J = rho u, G_i = t_i (3 (c_i - u).F + 9 (c_i.u)(c_i.F));
+//   otherwise J = j, G = 0.
+template <typename R>
+__device__ R adjCell(int k, const R* f, const R* F, R omega, R invRho0, const R* mu, R* lam, R* gF) {
+    if (k == K_BB) {
+        lam[0] = mu[0];
+        for (int i = 1; i < 19; ++i) lam[i] = mu[opp(i)];
+        return R(0);
+    }
+    if (k != K_BGK && k != K_GUO && k != K_INCBGK) {
+        for (int i = 0; i < 19; ++i) lam[i] = mu[i];
+        return R(0);
+    }
+    const bool guo = (k == K_GUO), inc = (k == K_INCBGK);
+    R rhoBar = R(0), j[3] = {R(0), R(0), R(0)};
+    for (int i = 0; i < 19; ++i) {
+        rhoBar += f[i];
+        for (int d = 0; d < 3; ++d) j[d] += (R)cdir(i, d) * f[i];
+    }
+    const R rho = rhoBar + (R)1;
+    R u[3], Jp[3];
+    for (int d = 0; d < 3; ++d) {
+        u[d] = j[d] / rho + (guo ? F[d] / (R)2 : R(0));
+        Jp[d] = guo ? rho * u[d] : j[d];
+    }
+    const R v = inc ? invRho0 : (R)1 / rho;
+    const R Q = Jp[0] * Jp[0] + Jp[1] * Jp[1] + Jp[2] * Jp[2];
+    const R a = (R)1 - omega / (R)2;
+    const R uF = u[0] * F[0] + u[1] * F[1] + u[2] * F[2];
+    R rhoBarBar = R(0), vBar = R(0), QBar = R(0), gOmega = R(0);
+    R JpBar[3] = {R(0), R(0), R(0)}, uBar[3] = {R(0), R(0), R(0)}, FBar[3] = {R(0), R(0), R(0)};
+    for (int i = 0; i < 19; ++i) {
+        const R t = tw<R>(i);
+        const R e = (R)cdir(i, 0) * Jp[0] + (R)cdir(i, 1) * Jp[1] + (R)cdir(i, 2) * Jp[2];
+        const R feq = t * (rhoBar + (R)3 * e + v * ((R)4.5 * e * e - (R)1.5 * Q));
+        R G = R(0);
+        if (guo) {
+            const R cu = (R)cdir(i, 0) * u[0] + (R)cdir(i, 1) * u[1] + (R)cdir(i, 2) * u[2];
+            const R cF = (R)cdir(i, 0) * F[0] + (R)cdir(i, 1) * F[1] + (R)cdir(i, 2) * F[2];
+            G = t * ((R)3 * (cF - uF) + (R)9 * cu * cF);
+            const R gam = a * mu[i] * t;
+            for (int d = 0; d < 3; ++d) {
+                uBar[d] += gam * (-(R)3 * F[d] + (R)9 * cF * (R)cdir(i, d));
+                FBar[d] += gam * ((R)3 * (R)cdir(i, d) - (R)3 * u[d] + (R)9 * cu * (R)cdir(i, d));
+            }
+        }
+        gOmega += mu[i] * (feq - f[i] - G / (R)2);
+        const R phi = omega * mu[i] * t;
+        rhoBarBar += phi;
+        const R eBar = phi * ((R)3 + (R)9 * v * e);
+        for (int d = 0; d < 3; ++d) JpBar[d] += eBar * (R)cdir(i, d);
+        vBar += phi * ((R)4.5 * e * e - (R)1.5 * Q);
+        QBar += -(R)1.5 * v * phi;
+    }
+    for (int d = 0; d < 3; ++d) JpBar[d] += (R)2 * QBar * Jp[d];
+    R rhoBar_ = inc ? R(0) : -v * v * vBar;   // d/d rho through v = 1/rho
+    R jBar[3];
+    for (int d = 0; d < 3; ++d) jBar[d] = JpBar[d];
+    if (guo) {
+        // J = j + (rho/2) F
+        rhoBar_ += (F[0] * JpBar[0] + F[1] * JpBar[1] + F[2] * JpBar[2]) / (R)2;
+        for (int d = 0; d < 3; ++d) FBar[d] += rho / (R)2 * JpBar[d];
+        // u = j / rho + F / 2
+        const R ju = j[0] * uBar[0] + j[1] * uBar[1] + j[2] * uBar[2];
+        for (int d = 0; d < 3; ++d) {
+            jBar[d] += uBar[d] / rho;
+            FBar[d] += uBar[d] / (R)2;
+        }
+        rhoBar_ += -ju / (rho * rho);
+        for (int d = 0; d < 3; ++d) gF[d] += FBar[d];
+    }
+    rhoBarBar += rhoBar_;
+    for (int i = 0; i < 19; ++i)
+        lam[i] = ((R)1 - omega) * mu[i] + rhoBarBar + (R)cdir(i, 0) * jBar[0] + (R)cdir(i, 1) * jBar[1] +
+                 (R)cdir(i, 2) * jBar[2];
+    return gOmega;
+}
+
+// ---------------------------------------------------------------- kernels
+
+struct AdjAcc {
+    double objective;
+    double gOmega;
+    double tangent;
+    double pad;
+};
+
+__device__ __forceinline__ void blockAdd(double v, double* dst) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v != 0.) atomicAdd(dst, v);
+}
+
+// Natural-order copy of the domain's state (either AA parity) and back.
+template <typename S, typename R, bool ODD>
+__global__ void stateOutKernel(DevLattice L, R* out) {
+    const int z = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, x = blockIdx.z;
+    if (z >= L.nz) return;
+    const long long idx = ((long long)x * L.ny + y) * L.nz + z;
+    Neighbourhood nb = neighbourhood(L, x, y, z);
+    const S* P = static_cast<const S*>(L.pop);
+    for (int i = 0; i < 19; ++i) out[i * L.n + idx] = R(StoreT<S>::ld(P + slotOf<ODD>(L, nb, idx, i)));
+}
+
+template <typename S, typename R>
+__global__ void stateInKernel(DevLattice L, const R* in) {
+    const int z = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, x = blockIdx.z;
+    if (z >= L.nz) return;
+    const long long idx = ((long long)x * L.ny + y) * L.nz + z;
+    S* P = static_cast<S*>(L.pop);
+    for (int i = 0; i < 19; ++i) StoreT<S>::st(P + i * L.stride + idx, (typename StoreT<S>::R)in[i * L.n + idx]);
+}
+
+// Push step fin -> fout (natural order): collide, then send f*_i to x + c_i
+// or, leaving a non-periodic domain, back into slot opp(i) of x.
+template <typename R>
+__global__ void pushStepKernel(DevLattice L, bool fp64Force, const R* fin, R* fout, R omega, R invRho0,
+                               const double* dF) {
+    const int z = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, x = blockIdx.z;
+    if (z >= L.nz) return;
+    const long long idx = ((long long)x * L.ny + y) * L.nz + z;
+    const int k = L.flags[idx];
+    R f[19], F[3];
+    for (int i = 0; i < 19; ++i) f[i] = fin[i * L.n + idx];
+    cellForce(L, fp64Force, idx, dF, F);
+    adjCollide<R>(k, f, F, bgkConsts<R>(omega), invRho0);
+    Neighbourhood nb = neighbourhood(L, x, y, z);
+    fout[idx] = f[0];
+    for (int i = 1; i < 19; ++i) {
+        long long off;
+        if (nb.move(i, +1, off)) fout[i * L.n + idx + off] = f[i];
+        else fout[opp(i) * L.n + idx] = f[i];
+    }
+}
+
+// J, lambda^T = dJ/df^T and the explicit dJ/dF of the Guo velocity u = j/rho + F/2.
+template <typename R>
+__global__ void objectiveKernel(DevLattice L, bool fp64Force, const R* f, const double* uTarget, R invRho0, R* lam,
+                                R* gF, AdjAcc* acc) {
+    const int z = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, x = blockIdx.z;
+    double jsum = 0.;
+    if (z < L.nz) {
+        const long long idx = ((long long)x * L.ny + y) * L.nz + z;
+        const int k = L.flags[idx];
+        R fc[19], F[3], u[3];
+        for (int i = 0; i < 19; ++i) fc[i] = f[i * L.n + idx];
+        cellForce(L, fp64Force, idx, nullptr, F);
+        cellVelocity<R>(k, fc, F, invRho0, u);
+        R dv[3];
+        for (int d = 0; d < 3; ++d) {
+            dv[d] = u[d] - (R)uTarget[3 * idx + d];
+            jsum += 0.5 * (double)dv[d] * (double)dv[d];
+        }
+        if (k == K_BGK || k == K_GUO || k == K_INCBGK) {
+            R rho = R(1), jv[3] = {R(0), R(0), R(0)};
+            for (int i = 0; i < 19; ++i) {
+                rho += fc[i];
+                for (int d = 0; d < 3; ++d) jv[d] += (R)cdir(i, d) * fc[i];
+            }
+            const R s = (k == K_INCBGK) ? invRho0 : (R)1 / rho;
+            const R dj = (k == K_INCBGK) ? R(0) : (dv[0] * jv[0] + dv[1] * jv[1] + dv[2] * jv[2]) * s;
+            for (int i = 0; i < 19; ++i)
+                lam[i * L.n + idx] = ((R)cdir(i, 0) * dv[0] + (R)cdir(i, 1) * dv[1] + (R)cdir(i, 2) * dv[2] - dj) * s;
+            if (k == K_GUO)
+                for (int d = 0; d < 3; ++d) gF[d * L.n + idx] += dv[d] / (R)2;
+        } else {
+            for (int i = 0; i < 19; ++i) lam[i * L.n + idx] = R(0);
+        }
+    }
+    blockAdd(jsum, &acc->objective);
+}
+
+// One reverse step: lamIn = lambda^{n+1}, f = f^n (pre-collision), lamOut = lambda^n.
+template <typename R>
+__global__ void adjointStepKernel(DevLattice L, bool fp64Force, const R* f, const R* lamIn, R* lamOut, R* gF,
+                                  R omega, R invRho0, AdjAcc* acc) {
+    const int z = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, x = blockIdx.z;
+    double go = 0.;
+    if (z < L.nz) {
+        const long long idx = ((long long)x * L.ny + y) * L.nz + z;
+        const int k = L.flags[idx];
+        Neighbourhood nb = neighbourhood(L, x, y, z);
+        R mu[19], fc[19], F[3], lam[19], g[3] = {R(0), R(0), R(0)};
+        mu[0] = lamIn[idx];
+        for (int i = 1; i < 19; ++i) {
+            long long off;
+            mu[i] = nb.move(i, +1, off) ? lamIn[i * L.n + idx + off] : lamIn[opp(i) * L.n + idx];
+        }
+        for (int i = 0; i < 19; ++i) fc[i] = f[i * L.n + idx];
+        cellForce(L, fp64Force, idx, nullptr, F);
+        go = (double)adjCell<R>(k, fc, F, omega, invRho0, mu, lam, g);
+        for (int i = 0; i < 19; ++i) lamOut[i * L.n + idx] = lam[i];
+        if (k == K_GUO)
+            for (int d = 0; d < 3; ++d) gF[d * L.n + idx] += g[d];
+    }
+    blockAdd(go, &acc->gOmega);
+}
+
+// J and its tangent from a dual state.
+__global__ void dualObjectiveKernel(DevLattice L, const Dual* f, const double* dF, const double* uTarget,
+                                    double invRho0, AdjAcc* acc) {
+    const int z = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, x = blockIdx.z;
+    double jv = 0., jd = 0.;
+    if (z < L.nz) {
+        const long long idx = ((long long)x * L.ny + y) * L.nz + z;
+        const int k = L.flags[idx];
+        Dual fc[19], F[3], u[3];
+        for (int i = 0; i < 19; ++i) fc[i] = f[i * L.n + idx];
+        cellForce(L, true, idx, dF, F);
+        cellVelocity<Dual>(k, fc, F, Dual(invRho0), u);
+        for (int d = 0; d < 3; ++d) {
+            const Dual dv = u[d] - Dual(uTarget[3 * idx + d]);
+            jv += 0.5 * dv.v * dv.v;
+            jd += dv.v * dv.d;
+        }
+    }
+    blockAdd(jv, &acc->objective);
+    blockAdd(jd, &acc->tangent);
+}
+
+template <typename R>
+__global__ void toDualKernel(long long n19, const double* in, Dual* out) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n19) out[i] = Dual(in[i], 0.);
+}
+
+// ---------------------------------------------------------------- host side
+
+namespace {
+
+struct AdjointState {
+    int precision = -1;
+    long long n = 0;
+    int T = 0, K = 0, nckpt = 0;
+    void* ckpt = nullptr;      // (nckpt) states
+    void* seg = nullptr;       // (K + 1) states
+    void* lam = nullptr;       // 2 states
+    void* gF = nullptr;        // 3 planes
+    double* uT = nullptr;      // target velocity, n * 3
+    AdjAcc* acc = nullptr;
+    bool ready = false;        // a forward run is recorded
+    ~AdjointState() {
+        cudaFree(ckpt); cudaFree(seg); cudaFree(lam); cudaFree(gF); cudaFree(uT); cudaFree(acc);
+    }
+};
+
+void freeAdjoint(void* p) { delete static_cast<AdjointState*>(p); }
+
+dim3 cellGrid(const DevLattice& L) { return rowGrid(L.nz, L.ny, L.nx, 128); }
+
+template <typename S, typename R>
+void stateOut(const DevLattice& L, bool odd, R* out, cudaStream_t s) {
+    if (odd) stateOutKernel<S, R, true><<<cellGrid(L), 128, 0, s>>>(L, out);
+    else stateOutKernel<S, R, false><<<cellGrid(L), 128, 0, s>>>(L, out);
+}
+
+template <typename R>
+void stateOutAny(int prec, const DevLattice& L, bool odd, R* out, cudaStream_t s) {
+    switch (prec) {
+    case PLBGPU_FP64: stateOut<double, R>(L, odd, out, s); break;
+    case PLBGPU_FP32: stateOut<float, R>(L, odd, out, s); break;
+    case PLBGPU_BF16: stateOut<__nv_bfloat16, R>(L, odd, out, s); break;
+    case PLBGPU_FP16: stateOut<__half, R>(L, odd, out, s); break;
+    default: stateOut<bf16sr, R>(L, odd, out, s); break;
+    }
+}
+
+template <typename R>
+void stateInAny(int prec, const DevLattice& L, const R* in, cudaStream_t s) {
+    dim3 g = cellGrid(L);
+    switch (prec) {
+    case PLBGPU_FP64: stateInKernel<double, R><<<g, 128, 0, s>>>(L, in); break;
+    case PLBGPU_FP32: stateInKernel<float, R><<<g, 128, 0, s>>>(L, in); break;
+    case PLBGPU_BF16: stateInKernel<__nv_bfloat16, R><<<g, 128, 0, s>>>(L, in); break;
+    case PLBGPU_FP16: stateInKernel<__half, R><<<g, 128, 0, s>>>(L, in); break;
+    default: stateInKernel<bf16sr, R><<<g, 128, 0, s>>>(L, in); break;
+    }
+}
+
+int checkKinds(plbgpu_ctx* c, const DomainAccess& a) {
+    std::vector<uint8_t> k((size_t)a.L.n);
+    if (cudaMemcpyAsync(k.data(), a.L.flags, k.size(), cudaMemcpyDeviceToHost, a.stream) != cudaSuccess ||
+        cudaStreamSynchronize(a.stream) != cudaSuccess)
+        return domainFail(c, PLBGPU_ERR_CUDA, "reading cell kinds failed");
+    for (uint8_t v : k)
+        if (v != K_BGK && v != K_GUO && v != K_INCBGK && v != K_BB && v != K_NODYN)
+            return domainFail(c, PLBGPU_ERR_ARG,
+                              "the adjoint supports BGK, Guo, incompressible BGK, bounce-back and no-dynamics cells");
+    return PLBGPU_OK;
+}
+
+#define ADJ_TRY(call)                                                                          \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess) {                                                               \
+            char m_[256];                                                                      \
+            snprintf(m_, sizeof(m_), "%s failed: %s", #call, cudaGetErrorString(e_));          \
+            return domainFail(c, e_ == cudaErrorMemoryAllocation ? PLBGPU_ERR_NOMEM : PLBGPU_ERR_CUDA, m_); \
+        }                                                                                      \
+    } while (0)
+
+template <typename R>
+int forwardImpl(plbgpu_ctx* c, int h, DomainAccess& a, AdjointState* st, int T, int K) {
+    const long long n = a.L.n, sz = 19 * n;
+    const bool fp64Force = a.precision == PLBGPU_FP64;
+    R* ck = static_cast<R*>(st->ckpt);
+    R* sg = static_cast<R*>(st->seg);
+    stateOutAny<R>(a.precision, a.L, a.odd, ck, a.stream);
+    *a.launches += 1;
+    R* cur = ck;
+    R* bufs[2] = {sg, sg + sz};
+    const R omega = (R)a.omega, invRho0 = (R)(1.0 / a.rho0);
+    for (int t = 0; t < T; ++t) {
+        R* out = ((t + 1) % K == 0) ? ck + ((t + 1) / K) * sz : bufs[t & 1];
+        pushStepKernel<R><<<cellGrid(a.L), 128, 0, a.stream>>>(a.L, fp64Force, cur, out, omega, invRho0, nullptr);
+        *a.launches += 1;
+        cur = out;
+    }
+    ADJ_TRY(cudaGetLastError());
+    // the domain continues from f^T, in natural order
+    stateInAny<R>(a.precision, a.L, cur, a.stream);
+    *a.launches += 1;
+    ADJ_TRY(cudaGetLastError());
+    ADJ_TRY(cudaStreamSynchronize(a.stream));
+    domainSetState(c, h, false, false);
+    return PLBGPU_OK;
+}
+
+template <typename R>
+int backwardImpl(DomainAccess& a, AdjointState* st, double* objective, double* gOmega, float* ms) {
+    const long long n = a.L.n, sz = 19 * n;
+    const bool fp64Force = a.precision == PLBGPU_FP64;
+    R* ck = static_cast<R*>(st->ckpt);
+    R* sg = static_cast<R*>(st->seg);
+    R* lam = static_cast<R*>(st->lam);
+    R* gF = static_cast<R*>(st->gF);
+    const R omega = (R)a.omega, invRho0 = (R)(1.0 / a.rho0);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, a.stream);
+    cudaMemsetAsync(gF, 0, sizeof(R) * 3 * n, a.stream);
+    cudaMemsetAsync(st->acc, 0, sizeof(AdjAcc), a.stream);
+    const int T = st->T, K = st->K;
+    objectiveKernel<R><<<cellGrid(a.L), 128, 0, a.stream>>>(a.L, fp64Force, ck + (long long)(T / K) * sz, st->uT,
+                                                            invRho0, lam, gF, st->acc);
+    *a.launches += 1;
+    int cur = 0;   // lam + cur * sz holds lambda^{t+1}
+    for (int s = T / K - 1; s >= 0; --s) {
+        // recompute f^{sK} .. f^{sK+K-1} into seg
+        cudaMemcpyAsync(sg, ck + (long long)s * sz, sizeof(R) * sz, cudaMemcpyDeviceToDevice, a.stream);
+        for (int k = 0; k + 1 < K; ++k) {
+            pushStepKernel<R><<<cellGrid(a.L), 128, 0, a.stream>>>(a.L, fp64Force, sg + k * sz, sg + (k + 1) * sz,
+                                                                   omega, invRho0, nullptr);
+            *a.launches += 1;
+        }
+        for (int k = K - 1; k >= 0; --k) {
+            adjointStepKernel<R><<<cellGrid(a.L), 128, 0, a.stream>>>(a.L, fp64Force, sg + k * sz, lam + cur * sz,
+                                                                      lam + (1 - cur) * sz, gF, omega, invRho0,
+                                                                      st->acc);
+            *a.launches += 1;
+            cur = 1 - cur;
+        }
+    }
+    cudaEventRecord(e1, a.stream);
+    cudaEventSynchronize(e1);
+    if (ms) cudaEventElapsedTime(ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    AdjAcc h;
+    cudaMemcpyAsync(&h, st->acc, sizeof(AdjAcc), cudaMemcpyDeviceToHost, a.stream);
+    cudaStreamSynchronize(a.stream);
+    *objective = h.objective;
+    *gOmega = h.gOmega;
+    return cudaGetLastError() == cudaSuccess ? PLBGPU_OK : PLBGPU_ERR_CUDA;
+}
+
+}  // namespace
+}  // namespace plbgpu
+
+using namespace plbgpu;
+
+extern "C" {
+
+int plbgpu_adjoint_forward(plbgpu_ctx* c, int h, int T, int K) {
+    DomainAccess a;
+    int rc = domainAccess(c, h, &a);
+    if (rc) return rc;
+    if (T < 1 || K < 1 || T % K != 0) return domainFail(c, PLBGPU_ERR_ARG, "adjoint: need T >= 1, K >= 1, K divides T");
+    if ((rc = checkKinds(c, a))) return rc;
+    if (a.pending) return domainFail(c, PLBGPU_ERR_STATE, "adjoint: boundary faces are not supported");
+    AdjointState* st = static_cast<AdjointState*>(*a.adjointSlot);
+    const size_t rs = a.precision == PLBGPU_FP64 ? sizeof(double) : sizeof(float);
+    const long long n = a.L.n, sz = 19 * n;
+    const int nckpt = T / K + 1;
+    if (!st || st->precision != a.precision || st->n != n || st->nckpt != nckpt || st->K != K) {
+        if (st) freeAdjoint(st);
+        *a.adjointSlot = nullptr;
+        st = new (std::nothrow) AdjointState();
+        if (!st) return domainFail(c, PLBGPU_ERR_NOMEM, "adjoint: host allocation failed");
+        *a.adjointSlot = st;
+        *a.adjointFree = freeAdjoint;
+        st->precision = a.precision;
+        st->n = n;
+        st->nckpt = nckpt;
+        st->K = K;
+        ADJ_TRY(cudaMalloc(&st->ckpt, rs * sz * nckpt));
+        ADJ_TRY(cudaMalloc(&st->seg, rs * sz * std::max(K, 2)));
+        ADJ_TRY(cudaMalloc(&st->lam, rs * sz * 2));
+        ADJ_TRY(cudaMalloc(&st->gF, rs * 3 * n));
+        ADJ_TRY(cudaMalloc(&st->uT, sizeof(double) * 3 * n));
+        ADJ_TRY(cudaMalloc(&st->acc, sizeof(AdjAcc)));
+    }
+    st->T = T;
+    st->ready = false;
+    rc = a.precision == PLBGPU_FP64 ? forwardImpl<double>(c, h, a, st, T, K) : forwardImpl<float>(c, h, a, st, T, K);
+    if (rc == PLBGPU_OK) st->ready = true;
+    return rc;
+}
+
+int plbgpu_adjoint_backward(plbgpu_ctx* c, int h, const double* u_target, size_t n3, double* objective,
+                            double* grad_force, size_t ng, double* grad_omega, float* ms) {
+    DomainAccess a;
+    int rc = domainAccess(c, h, &a);
+    if (rc) return rc;
+    AdjointState* st = static_cast<AdjointState*>(*a.adjointSlot);
+    if (!st || !st->ready) return domainFail(c, PLBGPU_ERR_STATE, "adjoint: no recorded forward run");
+    const long long n = a.L.n;
+    if (!u_target || (long long)n3 != 3 * n || !objective || !grad_omega)
+        return domainFail(c, PLBGPU_ERR_ARG, "adjoint: u_target needs 3 values per cell");
+    if (grad_force && (long long)ng != 3 * n) return domainFail(c, PLBGPU_ERR_ARG, "adjoint: grad_force needs 3 values per cell");
+    ADJ_TRY(cudaMemcpyAsync(st->uT, u_target, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, a.stream));
+    rc = a.precision == PLBGPU_FP64 ? backwardImpl<double>(a, st, objective, grad_omega, ms)
+                                    : backwardImpl<float>(a, st, objective, grad_omega, ms);
+    if (rc) return domainFail(c, rc, "adjoint: backward sweep failed");
+    if (grad_force) {
+        // planes [3][n] -> [cell][3]
+        std::vector<double> planes((size_t)3 * n);
+        if (a.precision == PLBGPU_FP64) {
+            ADJ_TRY(cudaMemcpyAsync(planes.data(), st->gF, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, a.stream));
+            ADJ_TRY(cudaStreamSynchronize(a.stream));
+        } else {
+            std::vector<float> pf((size_t)3 * n);
+            ADJ_TRY(cudaMemcpyAsync(pf.data(), st->gF, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, a.stream));
+            ADJ_TRY(cudaStreamSynchronize(a.stream));
+            for (size_t i = 0; i < pf.size(); ++i) planes[i] = pf[i];
+        }
+        for (long long i = 0; i < n; ++i)
+            for (int d = 0; d < 3; ++d) grad_force[3 * i + d] = planes[d * n + i];
+    }
+    return PLBGPU_OK;
+}
+
+int plbgpu_tangent_linear(plbgpu_ctx* c, int h, int T, const double* dforce, size_t ndf, double domega,
+                          const double* u_target, size_t n3, double* objective, double* directional) {
+    DomainAccess a;
+    int rc = domainAccess(c, h, &a);
+    if (rc) return rc;
+    if (a.precision != PLBGPU_FP64) return domainFail(c, PLBGPU_ERR_ARG, "tangent: FP64 domains only");
+    const long long n = a.L.n, sz = 19 * n;
+    if (T < 0 || !u_target || (long long)n3 != 3 * n || !objective || !directional || (dforce && (long long)ndf != 3 * n))
+        return domainFail(c, PLBGPU_ERR_ARG, "tangent: bad arguments");
+    if ((rc = checkKinds(c, a))) return rc;
+    if (a.pending) return domainFail(c, PLBGPU_ERR_STATE, "tangent: boundary faces are not supported");
+    double *f0 = nullptr, *dF = nullptr, *uT = nullptr;
+    Dual* buf = nullptr;
+    AdjAcc* acc = nullptr;
+    std::vector<double> planes((size_t)3 * n, 0.);
+    if (dforce)
+        for (long long i = 0; i < n; ++i)
+            for (int d = 0; d < 3; ++d) planes[d * n + i] = dforce[3 * i + d];
+    cudaError_t e = cudaMalloc(&f0, sizeof(double) * sz);
+    if (e == cudaSuccess) e = cudaMalloc(&buf, sizeof(Dual) * sz * 2);
+    if (e == cudaSuccess) e = cudaMalloc(&dF, sizeof(double) * 3 * n);
+    if (e == cudaSuccess) e = cudaMalloc(&uT, sizeof(double) * 3 * n);
+    if (e == cudaSuccess) e = cudaMalloc(&acc, sizeof(AdjAcc));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dF, planes.data(), sizeof(double) * 3 * n, cudaMemcpyHostToDevice, a.stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(uT, u_target, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, a.stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(acc, 0, sizeof(AdjAcc), a.stream);
+    if (e == cudaSuccess) {
+        stateOutAny<double>(a.precision, a.L, a.odd, f0, a.stream);
+        toDualKernel<double><<<(unsigned)((sz + 255) / 256), 256, 0, a.stream>>>(sz, f0, buf);
+        *a.launches += 2;
+        Dual* cur = buf;
+        Dual* nxt = buf + sz;
+        const Dual om(a.omega, domega), inv0(1.0 / a.rho0);
+        for (int t = 0; t < T; ++t) {
+            pushStepKernel<Dual><<<cellGrid(a.L), 128, 0, a.stream>>>(a.L, true, cur, nxt, om, inv0, dF);
+            *a.launches += 1;
+            std::swap(cur, nxt);
+        }
+        dualObjectiveKernel<<<cellGrid(a.L), 128, 0, a.stream>>>(a.L, cur, dF, uT, 1.0 / a.rho0, acc);
+        *a.launches += 1;
+        e = cudaGetLastError();
+        AdjAcc hacc;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&hacc, acc, sizeof(AdjAcc), cudaMemcpyDeviceToHost, a.stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(a.stream);
+        if (e == cudaSuccess) {
+            *objective = hacc.objective;
+            *directional = hacc.tangent;
+        }
+    }
+    cudaFree(f0); cudaFree(buf); cudaFree(dF); cudaFree(uT); cudaFree(acc);
+    if (e != cudaSuccess) {
+        char m[256];
+        snprintf(m, sizeof(m), "tangent: %s", cudaGetErrorString(e));
+        return domainFail(c, e == cudaErrorMemoryAllocation ? PLBGPU_ERR_NOMEM : PLBGPU_ERR_CUDA, m);
+    }
+    return PLBGPU_OK;
+}
+
+}  // extern "C"

@@ -45,6 +45,8 @@ struct Domain {
     unsigned long long steps = 0;   // time steps taken (salt of stochastic rounding)
     double lastStats[7] = {0, 0, 0, 0, 0, 0, 0};
     unsigned long long deviceBytes = 0;
+    void* adjoint = nullptr;              // adjoint checkpoints and buffers (adjoint.cu)
+    void (*adjointFree)(void*) = nullptr;
 
     DevLattice view() const {
         DevLattice L;
@@ -305,6 +307,40 @@ int materialize(plbgpu_ctx* c, Domain* d) {
 
 }  // namespace
 
+// =================================================================== adjoint hooks
+
+namespace plbgpu {
+
+int domainAccess(plbgpu_ctx* c, int h, DomainAccess* out) {
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if ((rc = materialize(c, d))) return rc;
+    out->L = d->view();
+    out->precision = d->precision;
+    out->odd = d->odd;
+    out->pending = d->pending;
+    out->omega = d->omega;
+    out->rho0 = d->rho0;
+    out->stream = c->stream;
+    out->adjointSlot = &d->adjoint;
+    out->adjointFree = &d->adjointFree;
+    out->launches = &c->launches;
+    return PLBGPU_OK;
+}
+
+int domainFail(plbgpu_ctx* c, int code, const char* msg) { return fail(c, code, "%s", msg); }
+
+void domainSetState(plbgpu_ctx* c, int h, bool odd, bool pending) {
+    Domain* d;
+    if (lookup(c, h, &d)) return;
+    d->odd = odd;
+    d->pending = pending;
+    d->statsValid = false;
+}
+
+}  // namespace plbgpu
+
 // =================================================================== C ABI
 
 extern "C" {
@@ -409,6 +445,7 @@ int plbgpu_remove_domain(plbgpu_ctx* c, int h) {
     cudaFree(d->stats);
     cudaFree(d->status);
     cudaFree(d->red);
+    if (d->adjoint && d->adjointFree) d->adjointFree(d->adjoint);
     c->domains.erase(h);
     return PLBGPU_OK;
 }

@@ -37,6 +37,28 @@ const Launchers& launchersBf16();
 const Launchers& launchersFp16();
 const Launchers& launchersBf16Sr();
 
+}  // namespace plbgpu
+
+struct plbgpu_ctx;
+
+namespace plbgpu {
+
+// A domain as the adjoint module sees it (implemented in api.cu).
+struct DomainAccess {
+    DevLattice L;
+    int precision;
+    bool odd, pending;
+    double omega, rho0;
+    cudaStream_t stream;
+    void** adjointSlot;            // per-domain storage owned by the adjoint module
+    void (**adjointFree)(void*);   // its release function, called when the domain goes away
+    unsigned long long* launches;  // the context's kernel-launch counter
+};
+int domainAccess(plbgpu_ctx* c, int handle, DomainAccess* out);
+int domainFail(plbgpu_ctx* c, int code, const char* msg);
+// After the adjoint module rewrote the populations in natural order.
+void domainSetState(plbgpu_ctx* c, int handle, bool odd, bool pending);
+
 inline dim3 rowGrid(int nz, int ny, int nx, int block) {
     return dim3((unsigned)((nz + block - 1) / block), (unsigned)ny, (unsigned)nx);
 }

@@ -227,6 +227,37 @@ class DeviceLattice3D:
         self._check(self.lib.plbgpu_compute_density(self.ctx.h, self.handle, *box, _dp(out), out.size))
         return out.reshape(box[1] - box[0] + 1, box[3] - box[2] + 1, box[5] - box[4] + 1)
 
+    # ----------------------------------------------------------------- adjoint
+    def adjoint_forward(self, T, K):
+        """Run T steps keeping a checkpoint every K steps (discrete adjoint)."""
+        self._check(self.lib.plbgpu_adjoint_forward(self.ctx.h, self.handle, int(T), int(K)))
+
+    def adjoint_backward(self, u_target, want_force=True):
+        """J = 1/2 sum |u(T) - u*|^2, dJ/dF (nx,ny,nz,3) and dJ/domega of the
+        last adjoint_forward run; also the device time of the sweep in ms."""
+        ut = np.ascontiguousarray(u_target, np.float64).reshape(-1)
+        n3 = 3 * self._cells(self.bounding_box)
+        J = ctypes.c_double()
+        go = ctypes.c_double()
+        ms = ctypes.c_float()
+        g = np.empty(n3 if want_force else 0, np.float64)
+        self._check(self.lib.plbgpu_adjoint_backward(self.ctx.h, self.handle, _dp(ut), ut.size, ctypes.byref(J),
+                                                     _dp(g) if want_force else None, g.size, ctypes.byref(go),
+                                                     ctypes.byref(ms)))
+        grad = g.reshape(self.shape + (3,)) if want_force else None
+        return J.value, grad, go.value, ms.value
+
+    def tangent_linear(self, T, dforce, domega, u_target):
+        """(J, grad J . (dforce, domega)) from a dual-number run of T steps."""
+        ut = np.ascontiguousarray(u_target, np.float64).reshape(-1)
+        df = None if dforce is None else np.ascontiguousarray(dforce, np.float64).reshape(-1)
+        J = ctypes.c_double()
+        dj = ctypes.c_double()
+        self._check(self.lib.plbgpu_tangent_linear(self.ctx.h, self.handle, int(T), None if df is None else _dp(df),
+                                                   0 if df is None else df.size, float(domega), _dp(ut), ut.size,
+                                                   ctypes.byref(J), ctypes.byref(dj)))
+        return J.value, dj.value
+
     def compute_average_energy(self, box=None):
         return self.reduce(box)[0]
 
