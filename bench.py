@@ -221,6 +221,38 @@ def run_reference(args):
 
 # ------------------------------------------------------------------ GPU arm
 
+def adjoint_cost(ctx, T=2000, K=100, precisions=("fp64", "fp32")):
+    """Config 4: Guo-forced 128x64x64 channel (periodic x, bounce-back walls),
+    omega 1.6, force N(0, 1e-12) + 1e-5 x-drive (seed 1234); target velocity
+    from a forward run with a second force field (seed 5678); objective
+    1/2 sum |u(T) - u*|^2, checkpoint every K steps.  Reports the device time
+    per time step of the forward recording and of the backward sweep
+    (recomputation included) against one fused forward step."""
+    from palabos_gb300 import workloads
+    out = {"workload": "forced_channel_128x64x64_guo", "T": T, "K": K}
+    for prec in precisions:
+        tgt = workloads.forced_channel(seed=5678).lattice(prec, ctx)
+        tgt.collide_and_stream(T)
+        u_target = tgt.compute_velocity()
+        tgt.close()
+        wl = workloads.forced_channel(seed=1234)
+        lat = wl.lattice(prec, ctx)
+        f0 = lat.receive()
+        fwd_ms = time_form(lat, 200, 10) / 200
+        lat.send(f0)
+        t0 = time.perf_counter()
+        lat.adjoint_forward(T, K)
+        rec_s = time.perf_counter() - t0
+        J, gF, gO, back_ms = lat.adjoint_backward(u_target)
+        out[prec] = {"forward_step_ms": round(fwd_ms, 5),
+                     "record_ms_per_step": round(rec_s * 1e3 / T, 5),
+                     "backward_ms_per_step": round(back_ms / T, 5),
+                     "adjoint_step_over_forward_step": round(back_ms / T / fwd_ms, 3),
+                     "objective": J, "grad_omega": gO, "grad_force_l2": float(np.sqrt(np.sum(gF * gF)))}
+        lat.close()
+    return out
+
+
 def time_form(lat, steps, warmup):
     lat.collide_and_stream(warmup, stats=False)
     lat.ctx.synchronize()
@@ -305,6 +337,8 @@ def run_gpu(args):
         for prec, acc in tg["forms"].items():
             forms[prec]["taylor_green_128_1000steps"] = {k: round(v, 9) for k, v in acc.items()}
 
+    adjoint = None if args.skip_adjoint else adjoint_cost(ctx)
+
     if rank == 0:
         clocks = clk.summary()
         line = {
@@ -324,6 +358,7 @@ def run_gpu(args):
                          "kernel": f"stepKernel<{head}> (fused collide+stream+faces, AA pattern)",
                          "bytes_per_launch": bytes_step},
             "forms": forms,
+            "adjoint": adjoint,
             "e2e": e2e,
             "gpu_launches": launches,
             "clocks": clocks,
@@ -343,6 +378,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-forms", action="store_true")
+    ap.add_argument("--skip-adjoint", action="store_true")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32", "bf16", "fp16", "bf16sr"])
     ap.add_argument("--accuracy", action="store_true",
                     help="run only the Taylor-Green accuracy study (512^3, 5000 steps) and print its JSON")

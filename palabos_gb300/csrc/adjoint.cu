@@ -159,83 +159,148 @@ __device__ __forceinline__ void cellVelocity(int k, const R* f, const R* F, R in
 //   v = 1/rho (1/rho0 for incompressible BGK),  rho = rhoBar + 1,
 //   Guo: u = j/rho + F/2, J = rho u, G_i = t_i (3 (c_i - u).F + 9 (c_i.u)(c_i.F));
 //   otherwise J = j, G = 0.
+// Every sum over populations of mu_i times these terms is a contraction with
+// the moments of nu_i = t_i mu_i: M0 = sum nu_i, M1 = sum nu_i c_i,
+// M2 = sum nu_i c_i c_i^T, so the reverse pass costs about as much as the
+// forward collision.
 template <typename R>
 __device__ R adjCell(int k, const R* f, const R* F, R omega, R invRho0, const R* mu, R* lam, R* gF) {
     if (k == K_BB) {
         lam[0] = mu[0];
+#pragma unroll
         for (int i = 1; i < 19; ++i) lam[i] = mu[opp(i)];
         return R(0);
     }
     if (k != K_BGK && k != K_GUO && k != K_INCBGK) {
+#pragma unroll
         for (int i = 0; i < 19; ++i) lam[i] = mu[i];
         return R(0);
     }
     const bool guo = (k == K_GUO), inc = (k == K_INCBGK);
-    R rhoBar = R(0), j[3] = {R(0), R(0), R(0)};
+    // forward moments of f
+    R rhoBar = R(0), j[3] = {R(0), R(0), R(0)}, muf = R(0);
+    // moments of nu = t mu
+    R M0 = R(0), M1[3] = {R(0), R(0), R(0)}, M2[6] = {R(0), R(0), R(0), R(0), R(0), R(0)};
+#pragma unroll
     for (int i = 0; i < 19; ++i) {
         rhoBar += f[i];
-        for (int d = 0; d < 3; ++d) j[d] += (R)cdir(i, d) * f[i];
+        muf += mu[i] * f[i];
+        const R nu = tw<R>(i) * mu[i];
+        M0 += nu;
+        const int cx = cdir(i, 0), cy = cdir(i, 1), cz = cdir(i, 2);
+        if (cx) { j[0] += cx > 0 ? f[i] : -f[i]; M1[0] += cx > 0 ? nu : -nu; M2[0] += nu; }
+        if (cy) { j[1] += cy > 0 ? f[i] : -f[i]; M1[1] += cy > 0 ? nu : -nu; M2[3] += nu; }
+        if (cz) { j[2] += cz > 0 ? f[i] : -f[i]; M1[2] += cz > 0 ? nu : -nu; M2[5] += nu; }
+        if (cx && cy) M2[1] += cx * cy > 0 ? nu : -nu;
+        if (cx && cz) M2[2] += cx * cz > 0 ? nu : -nu;
+        if (cy && cz) M2[4] += cy * cz > 0 ? nu : -nu;
     }
+    // M2 packed as xx, xy, xz, yy, yz, zz
+    auto m2v = [&](const R* a, R* out) {
+        out[0] = M2[0] * a[0] + M2[1] * a[1] + M2[2] * a[2];
+        out[1] = M2[1] * a[0] + M2[3] * a[1] + M2[4] * a[2];
+        out[2] = M2[2] * a[0] + M2[4] * a[1] + M2[5] * a[2];
+    };
     const R rho = rhoBar + (R)1;
+    const R invRho = (R)1 / rho;
     R u[3], Jp[3];
+#pragma unroll
     for (int d = 0; d < 3; ++d) {
-        u[d] = j[d] / rho + (guo ? F[d] / (R)2 : R(0));
+        u[d] = j[d] * invRho + (guo ? F[d] / (R)2 : R(0));
         Jp[d] = guo ? rho * u[d] : j[d];
     }
-    const R v = inc ? invRho0 : (R)1 / rho;
+    const R v = inc ? invRho0 : invRho;
     const R Q = Jp[0] * Jp[0] + Jp[1] * Jp[1] + Jp[2] * Jp[2];
-    const R a = (R)1 - omega / (R)2;
-    const R uF = u[0] * F[0] + u[1] * F[1] + u[2] * F[2];
-    R rhoBarBar = R(0), vBar = R(0), QBar = R(0), gOmega = R(0);
-    R JpBar[3] = {R(0), R(0), R(0)}, uBar[3] = {R(0), R(0), R(0)}, FBar[3] = {R(0), R(0), R(0)};
-    for (int i = 0; i < 19; ++i) {
-        const R t = tw<R>(i);
-        const R e = (R)cdir(i, 0) * Jp[0] + (R)cdir(i, 1) * Jp[1] + (R)cdir(i, 2) * Jp[2];
-        const R feq = t * (rhoBar + (R)3 * e + v * ((R)4.5 * e * e - (R)1.5 * Q));
-        R G = R(0);
-        if (guo) {
-            const R cu = (R)cdir(i, 0) * u[0] + (R)cdir(i, 1) * u[1] + (R)cdir(i, 2) * u[2];
-            const R cF = (R)cdir(i, 0) * F[0] + (R)cdir(i, 1) * F[1] + (R)cdir(i, 2) * F[2];
-            G = t * ((R)3 * (cF - uF) + (R)9 * cu * cF);
-            const R gam = a * mu[i] * t;
-            for (int d = 0; d < 3; ++d) {
-                uBar[d] += gam * (-(R)3 * F[d] + (R)9 * cF * (R)cdir(i, d));
-                FBar[d] += gam * ((R)3 * (R)cdir(i, d) - (R)3 * u[d] + (R)9 * cu * (R)cdir(i, d));
-            }
-        }
-        gOmega += mu[i] * (feq - f[i] - G / (R)2);
-        const R phi = omega * mu[i] * t;
-        rhoBarBar += phi;
-        const R eBar = phi * ((R)3 + (R)9 * v * e);
-        for (int d = 0; d < 3; ++d) JpBar[d] += eBar * (R)cdir(i, d);
-        vBar += phi * ((R)4.5 * e * e - (R)1.5 * Q);
-        QBar += -(R)1.5 * v * phi;
-    }
-    for (int d = 0; d < 3; ++d) JpBar[d] += (R)2 * QBar * Jp[d];
-    R rhoBar_ = inc ? R(0) : -v * v * vBar;   // d/d rho through v = 1/rho
-    R jBar[3];
-    for (int d = 0; d < 3; ++d) jBar[d] = JpBar[d];
+    R M2J[3];
+    m2v(Jp, M2J);
+    const R JM2J = Jp[0] * M2J[0] + Jp[1] * M2J[1] + Jp[2] * M2J[2];
+    const R M1J = M1[0] * Jp[0] + M1[1] * Jp[1] + M1[2] * Jp[2];
+    // feq part
+    const R sumMuFeq = rhoBar * M0 + (R)3 * M1J + v * ((R)4.5 * JM2J - (R)1.5 * Q * M0);
+    const R QBar = -(R)1.5 * omega * v * M0;
+    const R vBar = omega * ((R)4.5 * JM2J - (R)1.5 * Q * M0);
+    R JBar[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) JBar[d] = omega * ((R)3 * M1[d] + (R)9 * v * M2J[d]) + (R)2 * QBar * Jp[d];
+    R rhoBarBar = omega * M0 + (inc ? R(0) : -v * v * vBar);
+    R jBar[3] = {JBar[0], JBar[1], JBar[2]};
+    R sumMuG = R(0);
     if (guo) {
+        const R a = (R)1 - omega / (R)2;
+        R M2F[3], M2u[3];
+        m2v(F, M2F);
+        m2v(u, M2u);
+        const R uF = u[0] * F[0] + u[1] * F[1] + u[2] * F[2];
+        const R M1F = M1[0] * F[0] + M1[1] * F[1] + M1[2] * F[2];
+        const R uM2F = u[0] * M2F[0] + u[1] * M2F[1] + u[2] * M2F[2];
+        sumMuG = (R)3 * M1F - (R)3 * uF * M0 + (R)9 * uM2F;
+        R uBar[3], FBar[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            uBar[d] = a * (-(R)3 * M0 * F[d] + (R)9 * M2F[d]);
+            FBar[d] = a * ((R)3 * M1[d] - (R)3 * M0 * u[d] + (R)9 * M2u[d]);
+        }
         // J = j + (rho/2) F
-        rhoBar_ += (F[0] * JpBar[0] + F[1] * JpBar[1] + F[2] * JpBar[2]) / (R)2;
-        for (int d = 0; d < 3; ++d) FBar[d] += rho / (R)2 * JpBar[d];
+        rhoBarBar += (F[0] * JBar[0] + F[1] * JBar[1] + F[2] * JBar[2]) / (R)2;
         // u = j / rho + F / 2
         const R ju = j[0] * uBar[0] + j[1] * uBar[1] + j[2] * uBar[2];
+        rhoBarBar += -ju * invRho * invRho;
+#pragma unroll
         for (int d = 0; d < 3; ++d) {
-            jBar[d] += uBar[d] / rho;
-            FBar[d] += uBar[d] / (R)2;
+            FBar[d] += rho / (R)2 * JBar[d] + uBar[d] / (R)2;
+            jBar[d] += uBar[d] * invRho;
+            gF[d] += FBar[d];
         }
-        rhoBar_ += -ju / (rho * rho);
-        for (int d = 0; d < 3; ++d) gF[d] += FBar[d];
     }
-    rhoBarBar += rhoBar_;
-    for (int i = 0; i < 19; ++i)
-        lam[i] = ((R)1 - omega) * mu[i] + rhoBarBar + (R)cdir(i, 0) * jBar[0] + (R)cdir(i, 1) * jBar[1] +
-                 (R)cdir(i, 2) * jBar[2];
-    return gOmega;
+    const R om1 = (R)1 - omega;
+#pragma unroll
+    for (int i = 0; i < 19; ++i) {
+        R l = om1 * mu[i] + rhoBarBar;
+        const int cx = cdir(i, 0), cy = cdir(i, 1), cz = cdir(i, 2);
+        if (cx) l += cx > 0 ? jBar[0] : -jBar[0];
+        if (cy) l += cy > 0 ? jBar[1] : -jBar[1];
+        if (cz) l += cz > 0 ? jBar[2] : -jBar[2];
+        lam[i] = l;
+    }
+    return sumMuFeq - muf - sumMuG / (R)2;
 }
 
 // ---------------------------------------------------------------- kernels
+
+// Neighbour of a cell along +c_i: rows with 1 <= x <= nx-2, 1 <= y <= ny-2 use
+// the uniform offsets c_i . (ny*nz, nz, 1) and only check the z ends; border
+// rows use the general neighbourhood.  Returns false where a non-periodic
+// domain is left.
+struct CellMoves {
+    bool interior;
+    Neighbourhood nb;
+    long long wrapM, wrapP;
+    bool okM, okP;
+    __device__ __forceinline__ CellMoves(const DevLattice& L, int x, int y, int z) {
+        interior = x > 0 && x < L.nx - 1 && y > 0 && y < L.ny - 1;
+        nb = neighbourhood(L, x, y, z);
+        wrapM = z == 0 ? L.nz : 0;
+        wrapP = z == L.nz - 1 ? -L.nz : 0;
+        okM = z > 0 || L.per[2];
+        okP = z < L.nz - 1 || L.per[2];
+    }
+    __device__ __forceinline__ bool plus(int i, const int* D, long long& off) const {
+        if (!interior) return nb.move(i, +1, off);
+        const int cz = cdir(i, 2);
+        off = D[i] + (cz < 0 ? wrapM : cz > 0 ? wrapP : 0);
+        return cz < 0 ? okM : cz > 0 ? okP : true;
+    }
+};
+
+struct NeighbourDeltas {
+    int d[19];
+};
+
+inline NeighbourDeltas deltasOf(const DevLattice& L) {
+    NeighbourDeltas D;
+    for (int i = 0; i < 19; ++i) D.d[i] = cdir(i, 0) * L.ny * L.nz + cdir(i, 1) * L.nz + cdir(i, 2);
+    return D;
+}
 
 struct AdjAcc {
     double objective;
@@ -274,8 +339,8 @@ __global__ void stateInKernel(DevLattice L, const R* in) {
 // Push step fin -> fout (natural order): collide, then send f*_i to x + c_i
 // or, leaving a non-periodic domain, back into slot opp(i) of x.
 template <typename R>
-__global__ void pushStepKernel(DevLattice L, bool fp64Force, const R* fin, R* fout, R omega, R invRho0,
-                               const double* dF) {
+__global__ void pushStepKernel(DevLattice L, NeighbourDeltas D, bool fp64Force, const R* fin, R* fout, R omega,
+                               R invRho0, const double* dF) {
     const int z = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y, x = blockIdx.z;
     if (z >= L.nz) return;
@@ -285,11 +350,12 @@ __global__ void pushStepKernel(DevLattice L, bool fp64Force, const R* fin, R* fo
     for (int i = 0; i < 19; ++i) f[i] = fin[i * L.n + idx];
     cellForce(L, fp64Force, idx, dF, F);
     adjCollide<R>(k, f, F, bgkConsts<R>(omega), invRho0);
-    Neighbourhood nb = neighbourhood(L, x, y, z);
+    CellMoves mv(L, x, y, z);
     fout[idx] = f[0];
+#pragma unroll
     for (int i = 1; i < 19; ++i) {
         long long off;
-        if (nb.move(i, +1, off)) fout[i * L.n + idx + off] = f[i];
+        if (mv.plus(i, D.d, off)) fout[i * L.n + idx + off] = f[i];
         else fout[opp(i) * L.n + idx] = f[i];
     }
 }
@@ -334,20 +400,21 @@ __global__ void objectiveKernel(DevLattice L, bool fp64Force, const R* f, const 
 
 // One reverse step: lamIn = lambda^{n+1}, f = f^n (pre-collision), lamOut = lambda^n.
 template <typename R>
-__global__ void adjointStepKernel(DevLattice L, bool fp64Force, const R* f, const R* lamIn, R* lamOut, R* gF,
-                                  R omega, R invRho0, AdjAcc* acc) {
+__global__ void adjointStepKernel(DevLattice L, NeighbourDeltas D, bool fp64Force, const R* f, const R* lamIn,
+                                  R* lamOut, R* gF, R omega, R invRho0, AdjAcc* acc) {
     const int z = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y, x = blockIdx.z;
     double go = 0.;
     if (z < L.nz) {
         const long long idx = ((long long)x * L.ny + y) * L.nz + z;
         const int k = L.flags[idx];
-        Neighbourhood nb = neighbourhood(L, x, y, z);
+        CellMoves mv(L, x, y, z);
         R mu[19], fc[19], F[3], lam[19], g[3] = {R(0), R(0), R(0)};
         mu[0] = lamIn[idx];
+#pragma unroll
         for (int i = 1; i < 19; ++i) {
             long long off;
-            mu[i] = nb.move(i, +1, off) ? lamIn[i * L.n + idx + off] : lamIn[opp(i) * L.n + idx];
+            mu[i] = mv.plus(i, D.d, off) ? lamIn[i * L.n + idx + off] : lamIn[opp(i) * L.n + idx];
         }
         for (int i = 0; i < 19; ++i) fc[i] = f[i * L.n + idx];
         cellForce(L, fp64Force, idx, nullptr, F);
@@ -474,9 +541,10 @@ int forwardImpl(plbgpu_ctx* c, int h, DomainAccess& a, AdjointState* st, int T, 
     R* cur = ck;
     R* bufs[2] = {sg, sg + sz};
     const R omega = (R)a.omega, invRho0 = (R)(1.0 / a.rho0);
+    const NeighbourDeltas D = deltasOf(a.L);
     for (int t = 0; t < T; ++t) {
         R* out = ((t + 1) % K == 0) ? ck + ((t + 1) / K) * sz : bufs[t & 1];
-        pushStepKernel<R><<<cellGrid(a.L), 128, 0, a.stream>>>(a.L, fp64Force, cur, out, omega, invRho0, nullptr);
+        pushStepKernel<R><<<cellGrid(a.L), 128, 0, a.stream>>>(a.L, D, fp64Force, cur, out, omega, invRho0, nullptr);
         *a.launches += 1;
         cur = out;
     }
@@ -499,6 +567,7 @@ int backwardImpl(DomainAccess& a, AdjointState* st, double* objective, double* g
     R* lam = static_cast<R*>(st->lam);
     R* gF = static_cast<R*>(st->gF);
     const R omega = (R)a.omega, invRho0 = (R)(1.0 / a.rho0);
+    const NeighbourDeltas D = deltasOf(a.L);
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -514,14 +583,14 @@ int backwardImpl(DomainAccess& a, AdjointState* st, double* objective, double* g
         // recompute f^{sK} .. f^{sK+K-1} into seg
         cudaMemcpyAsync(sg, ck + (long long)s * sz, sizeof(R) * sz, cudaMemcpyDeviceToDevice, a.stream);
         for (int k = 0; k + 1 < K; ++k) {
-            pushStepKernel<R><<<cellGrid(a.L), 128, 0, a.stream>>>(a.L, fp64Force, sg + k * sz, sg + (k + 1) * sz,
-                                                                   omega, invRho0, nullptr);
+            pushStepKernel<R><<<cellGrid(a.L), 128, 0, a.stream>>>(a.L, D, fp64Force, sg + k * sz,
+                                                                   sg + (k + 1) * sz, omega, invRho0, nullptr);
             *a.launches += 1;
         }
         for (int k = K - 1; k >= 0; --k) {
-            adjointStepKernel<R><<<cellGrid(a.L), 128, 0, a.stream>>>(a.L, fp64Force, sg + k * sz, lam + cur * sz,
-                                                                      lam + (1 - cur) * sz, gF, omega, invRho0,
-                                                                      st->acc);
+            adjointStepKernel<R><<<cellGrid(a.L), 128, 0, a.stream>>>(a.L, D, fp64Force, sg + k * sz,
+                                                                      lam + cur * sz, lam + (1 - cur) * sz, gF, omega,
+                                                                      invRho0, st->acc);
             *a.launches += 1;
             cur = 1 - cur;
         }
@@ -648,8 +717,9 @@ int plbgpu_tangent_linear(plbgpu_ctx* c, int h, int T, const double* dforce, siz
         Dual* cur = buf;
         Dual* nxt = buf + sz;
         const Dual om(a.omega, domega), inv0(1.0 / a.rho0);
+        const NeighbourDeltas D = deltasOf(a.L);
         for (int t = 0; t < T; ++t) {
-            pushStepKernel<Dual><<<cellGrid(a.L), 128, 0, a.stream>>>(a.L, true, cur, nxt, om, inv0, dF);
+            pushStepKernel<Dual><<<cellGrid(a.L), 128, 0, a.stream>>>(a.L, D, true, cur, nxt, om, inv0, dF);
             *a.launches += 1;
             std::swap(cur, nxt);
         }

@@ -103,3 +103,37 @@ def test_adjoint_rejects_unsupported_cells():
         lat2.adjoint_forward(5, 2)      # K must divide T
     with pytest.raises(PlbGpuError):
         lat2.adjoint_backward(np.zeros((6, 6, 6, 3)))   # no forward run yet
+
+
+@pytest.mark.slow
+def test_config4_gradient_full_size():
+    """Config 4 at full size (128x64x64, Guo forcing, T = 2000, checkpoint
+    every 100 steps): adjoint gradient against central finite differences of
+    the CPU oracle for omega and three force components, to 1e-5 relative."""
+    T, K = 2000, 100
+    tgt = workloads.forced_channel(seed=5678).lattice("fp64")
+    tgt.collide_and_stream(T)
+    u_target = tgt.compute_velocity()
+    wl = workloads.forced_channel(seed=1234)
+    lat = wl.lattice("fp64")
+    f0 = lat.receive()
+    lat.adjoint_forward(T, K)
+    J, gF, gO, _ = lat.adjoint_backward(u_target)
+    O.set_threads(O.max_threads())
+    assert J == pytest.approx(_oracle_objective(wl, f0, wl.force, wl.omega, T, u_target), rel=1e-10)
+    h = 1e-5
+    fd = (_oracle_objective(wl, f0, wl.force, wl.omega + h, T, u_target) -
+          _oracle_objective(wl, f0, wl.force, wl.omega - h, T, u_target)) / (2 * h)
+    assert gO == pytest.approx(fd, rel=1e-5), (gO, fd)
+    rng = np.random.default_rng(2)
+    fluid = np.argwhere(wl.kinds == 1)
+    hF = 1e-8
+    for _ in range(3):
+        x, y, z = fluid[rng.integers(len(fluid))]
+        fp = wl.force.copy()
+        fm = wl.force.copy()
+        fp[x, y, z, 0] += hF
+        fm[x, y, z, 0] -= hF
+        fd = (_oracle_objective(wl, f0, fp, wl.omega, T, u_target) -
+              _oracle_objective(wl, f0, fm, wl.omega, T, u_target)) / (2 * hF)
+        assert gF[x, y, z, 0] == pytest.approx(fd, rel=1e-5), (gF[x, y, z, 0], fd)
