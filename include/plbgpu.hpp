@@ -1,0 +1,177 @@
+// C++ front end of the GB300 D3Q19 lattice library (header only, over the C
+// ABI of plbgpu.h).  The names follow the reference's construction and
+// analysis calls so that host code reads like a Palabos program:
+//
+//   plbgpu::Context ctx(0);
+//   plbgpu::Lattice3D lattice(ctx, nx, ny, nz, omega);          // MultiBlockLattice3D(nx,ny,nz,new BGKdynamics(omega))
+//   lattice.periodicity(true, false, false);                    // lattice.periodicity().toggle(0, true)
+//   lattice.defineDynamics(box, PLBGPU_BOUNCEBACK);              // defineDynamics(lattice, box, new BounceBack<T,D>)
+//   lattice.addVelocityBoundary(box, 0, -1);                    // bc->addVelocityBoundary0N(box, lattice)
+//   lattice.setBoundaryVelocity(box, 0.02, 0., 0.);             // setBoundaryVelocity(lattice, box, u)
+//   lattice.initializeAtEquilibrium(lattice.boundingBox(), 1., 0., 0., 0.);
+//   lattice.initialize();                                       // lattice.initialize()
+//   lattice.collideAndStream();                                 // lattice.collideAndStream()
+//   double e = lattice.computeAverageEnergy();                  // computeAverageEnergy(lattice)
+//
+// Failures of the C ABI are thrown as plbgpu::Error (a std::runtime_error
+// carrying the status code and the library's message).
+#ifndef PLBGPU_HPP
+#define PLBGPU_HPP
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "plbgpu.h"
+
+namespace plbgpu {
+
+class Error : public std::runtime_error {
+public:
+    Error(int code, const std::string& msg) : std::runtime_error(msg), code_(code) {}
+    int code() const { return code_; }
+
+private:
+    int code_;
+};
+
+// Inclusive box, like plb::Box3D.
+struct Box {
+    int x0, x1, y0, y1, z0, z1;
+    long cells() const { return (long)(x1 - x0 + 1) * (y1 - y0 + 1) * (z1 - z0 + 1); }
+};
+
+class Context {
+public:
+    explicit Context(int device = 0) {
+        int rc = plbgpu_create(device, &ctx_);
+        if (rc != PLBGPU_OK) throw Error(rc, "plbgpu_create failed for CUDA device " + std::to_string(device));
+    }
+    ~Context() {
+        if (ctx_) plbgpu_destroy(ctx_);
+    }
+    Context(const Context&) = delete;
+    Context& operator=(const Context&) = delete;
+    plbgpu_ctx* get() const { return ctx_; }
+    void check(int rc) const {
+        if (rc != PLBGPU_OK) throw Error(rc, plbgpu_last_error(ctx_));
+    }
+    void synchronize() const { check(plbgpu_synchronize(ctx_)); }
+    unsigned long long launchCount() const {
+        unsigned long long n = 0;
+        check(plbgpu_launch_count(ctx_, &n));
+        return n;
+    }
+
+private:
+    plbgpu_ctx* ctx_ = nullptr;
+};
+
+class Lattice3D {
+public:
+    Lattice3D(Context& ctx, int nx, int ny, int nz, double omega, int precision = PLBGPU_FP64, double rho0 = 1.0,
+              double bbRho = 0.0)
+        : ctx_(ctx), nx_(nx), ny_(ny), nz_(nz) {
+        ctx_.check(plbgpu_add_domain(ctx_.get(), nx, ny, nz, precision, &h_));
+        ctx_.check(plbgpu_set_params(ctx_.get(), h_, omega, rho0, bbRho));
+    }
+    ~Lattice3D() { plbgpu_remove_domain(ctx_.get(), h_); }
+    Lattice3D(const Lattice3D&) = delete;
+    Lattice3D& operator=(const Lattice3D&) = delete;
+
+    int handle() const { return h_; }
+    Box boundingBox() const { return Box{0, nx_ - 1, 0, ny_ - 1, 0, nz_ - 1}; }
+
+    void periodicity(bool px, bool py, bool pz) {
+        ctx_.check(plbgpu_set_periodicity(ctx_.get(), h_, px, py, pz));
+    }
+    void setParameters(double omega, double rho0 = 1.0, double bbRho = 0.0) {
+        ctx_.check(plbgpu_set_params(ctx_.get(), h_, omega, rho0, bbRho));
+    }
+    void defineDynamics(const Box& b, int kind) {
+        ctx_.check(plbgpu_define_dynamics(ctx_.get(), h_, b.x0, b.x1, b.y0, b.y1, b.z0, b.z1, kind));
+    }
+    void setKinds(const Box& b, const std::vector<uint8_t>& kinds) {
+        ctx_.check(plbgpu_set_kinds(ctx_.get(), h_, b.x0, b.x1, b.y0, b.y1, b.z0, b.z1, kinds.data(), kinds.size()));
+    }
+    // Wrapped regularized (or Zou/He) face conditions: direction 0/1/2, orientation -1/+1.
+    void addVelocityBoundary(const Box& b, int direction, int orientation, bool zouHe = false) {
+        defineDynamics(b, (zouHe ? PLBGPU_ZOUHE_VELOCITY : PLBGPU_REG_VELOCITY) + 2 * direction + (orientation > 0));
+    }
+    void addPressureBoundary(const Box& b, int direction, int orientation, bool zouHe = false) {
+        defineDynamics(b, (zouHe ? PLBGPU_ZOUHE_PRESSURE : PLBGPU_REG_PRESSURE) + 2 * direction + (orientation > 0));
+    }
+    void setBoundaryVelocity(const Box& b, double ux, double uy, double uz) {
+        ctx_.check(plbgpu_set_boundary_velocity(ctx_.get(), h_, b.x0, b.x1, b.y0, b.y1, b.z0, b.z1, ux, uy, uz));
+    }
+    void setBoundaryVelocity(const Box& b, const std::vector<double>& u) {
+        ctx_.check(plbgpu_set_boundary_velocity_field(ctx_.get(), h_, b.x0, b.x1, b.y0, b.y1, b.z0, b.z1, u.data(),
+                                                      u.size()));
+    }
+    void setBoundaryDensity(const Box& b, double rho) {
+        ctx_.check(plbgpu_set_boundary_density(ctx_.get(), h_, b.x0, b.x1, b.y0, b.y1, b.z0, b.z1, rho));
+    }
+    void setBoundaryDensity(const Box& b, const std::vector<double>& rho) {
+        ctx_.check(plbgpu_set_boundary_density_field(ctx_.get(), h_, b.x0, b.x1, b.y0, b.y1, b.z0, b.z1, rho.data(),
+                                                     rho.size()));
+    }
+    void setExternalVector(const Box& b, double fx, double fy, double fz) {
+        ctx_.check(plbgpu_set_force(ctx_.get(), h_, b.x0, b.x1, b.y0, b.y1, b.z0, b.z1, fx, fy, fz));
+    }
+    void setExternalVector(const Box& b, const std::vector<double>& f) {
+        ctx_.check(plbgpu_set_force_field(ctx_.get(), h_, b.x0, b.x1, b.y0, b.y1, b.z0, b.z1, f.data(), f.size()));
+    }
+    void initializeMomentumExchange() { ctx_.check(plbgpu_initialize_momentum_exchange(ctx_.get(), h_)); }
+    void initializeAtEquilibrium(const Box& b, double rho, double ux, double uy, double uz) {
+        ctx_.check(plbgpu_initialize_at_equilibrium(ctx_.get(), h_, b.x0, b.x1, b.y0, b.y1, b.z0, b.z1, rho, ux, uy,
+                                                    uz));
+    }
+    void initialize() { ctx_.check(plbgpu_initialize(ctx_.get(), h_)); }
+
+    // Populations (FP64 f-bar, [x][y][z][19]) in and out.
+    void send(const Box& b, const std::vector<double>& f) {
+        ctx_.check(plbgpu_send(ctx_.get(), h_, b.x0, b.x1, b.y0, b.y1, b.z0, b.z1, f.data(), f.size()));
+    }
+    std::vector<double> receive(const Box& b) const {
+        std::vector<double> f((size_t)b.cells() * 19);
+        ctx_.check(plbgpu_receive(ctx_.get(), h_, b.x0, b.x1, b.y0, b.y1, b.z0, b.z1, f.data(), f.size()));
+        return f;
+    }
+
+    void collideAndStream(int steps = 1, bool gatherStatistics = true) {
+        ctx_.check(plbgpu_collide_and_stream(ctx_.get(), h_, steps, gatherStatistics));
+    }
+    // getInternalStatistics(): average rho-bar, average u^2, max u^2, drag x/y/z, cell count.
+    std::vector<double> internalStatistics() const {
+        std::vector<double> s(7);
+        ctx_.check(plbgpu_get_stats(ctx_.get(), h_, s.data()));
+        return s;
+    }
+    double computeAverageEnergy(const Box& b) const {
+        double e, r;
+        ctx_.check(plbgpu_reduce(ctx_.get(), h_, b.x0, b.x1, b.y0, b.y1, b.z0, b.z1, &e, &r));
+        return e;
+    }
+    double computeAverageDensity(const Box& b) const {
+        double e, r;
+        ctx_.check(plbgpu_reduce(ctx_.get(), h_, b.x0, b.x1, b.y0, b.y1, b.z0, b.z1, &e, &r));
+        return r;
+    }
+    double computeAverageEnergy() const { return computeAverageEnergy(boundingBox()); }
+    double computeAverageDensity() const { return computeAverageDensity(boundingBox()); }
+    std::vector<double> computeVelocity(const Box& b) const {
+        std::vector<double> u((size_t)b.cells() * 3);
+        ctx_.check(plbgpu_compute_velocity(ctx_.get(), h_, b.x0, b.x1, b.y0, b.y1, b.z0, b.z1, u.data(), u.size()));
+        return u;
+    }
+
+private:
+    Context& ctx_;
+    int nx_, ny_, nz_;
+    int h_ = -1;
+};
+
+}  // namespace plbgpu
+
+#endif  // PLBGPU_HPP

@@ -507,19 +507,29 @@ static void step(const orc_lattice* L, double* f, double* tmp, orc_stats* st) {
     }
     st->sumRhoBar = sR; st->sumUSqr = sU; st->maxUSqr = mU; st->count = cnt;
     st->drag[0] = d0; st->drag[1] = d1; st->drag[2] = d2;
+    const long sx = (long)L->ny * L->nz, sy = L->nz;
+    long dlt[19];
+    for (int i = 0; i < 19; ++i) dlt[i] = C[i][0] * sx + C[i][1] * sy + C[i][2];
 #pragma omp parallel for collapse(2) schedule(static)
     for (int x = 0; x < L->nx; ++x)
-        for (int y = 0; y < L->ny; ++y)
+        for (int y = 0; y < L->ny; ++y) {
+            const int inner = x > 0 && x < L->nx - 1 && y > 0 && y < L->ny - 1;
             for (int z = 0; z < L->nz; ++z) {
                 long id = lid(L, x, y, z);
                 double* out = f + id * 19;
                 out[0] = tmp[id * 19];
-                for (int i = 1; i < 19; ++i) {
-                    long src = neighbour(L, x, y, z, i, -1);
-                    out[i] = (src >= 0) ? tmp[src * 19 + i] : tmp[id * 19 + opp(i)];
+                if (inner && z > 0 && z < L->nz - 1) {
+                    /* no source lies outside the box: plain offsets */
+                    for (int i = 1; i < 19; ++i) out[i] = tmp[(id - dlt[i]) * 19 + i];
+                } else {
+                    for (int i = 1; i < 19; ++i) {
+                        long src = neighbour(L, x, y, z, i, -1);
+                        out[i] = (src >= 0) ? tmp[src * 19 + i] : tmp[id * 19 + opp(i)];
+                    }
                 }
                 if (is_face(L->flags[id])) complete_face(L, id, out);
             }
+        }
 }
 
 /* ------------------------------------------------------------ public API */
