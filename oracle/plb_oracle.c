@@ -34,7 +34,10 @@
 
 enum {
     K_BGK = 0, K_GUO = 1, K_INCBGK = 2, K_BB = 3, K_MEBB = 4, K_NODYN = 5,
-    K_REGVEL = 6, K_REGPRESS = 12, K_ZHVEL = 18, K_ZHPRESS = 24, K_NKINDS = 30
+    K_REGVEL = 6, K_REGPRESS = 12, K_ZHVEL = 18, K_ZHPRESS = 24,
+    K_EDGE = 30,    /* 30..41: 30 + 4*plane + 2*(normal1>0) + (normal2>0) */
+    K_CORNER = 42,  /* 42..49: 42 + 4*(xNormal>0) + 2*(yNormal>0) + (zNormal>0) */
+    K_NKINDS = 50
 };
 
 /* latticeBoltzmann/nearestNeighborLattices3D.hh:168-180 */
@@ -69,6 +72,7 @@ typedef struct {
     const double* bcval; /* N*3 */
     const double* force; /* N*3 (Guo cells) */
     uint32_t* mebbMask;  /* N, bit i = fluid direction i (MEBB cells only) */
+    int hasEdges;        /* any edge or corner cell */
 } orc_lattice;
 
 /* ------------------------------------------------------------ moments */
@@ -484,7 +488,10 @@ static void build_mebb_masks(orc_lattice* L) {
             }
 }
 
-static int is_face(int k) { return k >= K_REGVEL && k < K_NKINDS; }
+static void complete_edges_corners(const orc_lattice* L, double* f);
+static int is_face(int k) { return k >= K_REGVEL && k < K_EDGE; }
+static int is_edge(int k) { return k >= K_EDGE && k < K_CORNER; }
+static int is_corner(int k) { return k >= K_CORNER && k < K_NKINDS; }
 
 /* One time step: collide every cell, stream (with the swap algorithm's
  * domain-edge rule: a population whose destination lies outside a
@@ -530,6 +537,7 @@ static void step(const orc_lattice* L, double* f, double* tmp, orc_stats* st) {
                 if (is_face(L->flags[id])) complete_face(L, id, out);
             }
         }
+    if (L->hasEdges) complete_edges_corners(L, f);
 }
 
 /* ------------------------------------------------------------ public API */
@@ -550,6 +558,9 @@ static void setup(orc_lattice* L, const orc_params* p, const uint8_t* flags, con
     long n = (long)p->nx * p->ny * p->nz;
     L->mebbMask = (uint32_t*)calloc((size_t)n, sizeof(uint32_t));
     build_mebb_masks(L);
+    L->hasEdges = 0;
+    for (long id = 0; id < n; ++id)
+        if (flags[id] >= K_EDGE && flags[id] < K_NKINDS) { L->hasEdges = 1; break; }
 }
 
 void orc_set_threads(int n) {
@@ -577,6 +588,7 @@ int orc_initialize(const orc_params* p, const uint8_t* flags, const double* bcva
     long n = (long)p->nx * p->ny * p->nz;
     for (long id = 0; id < n; ++id)
         if (is_face(flags[id])) complete_face(&L, id, f + id * 19);
+    if (L.hasEdges) complete_edges_corners(&L, f);
     free(L.mebbMask);
     return 0;
 }
@@ -636,8 +648,12 @@ static void cell_velocity(const orc_lattice* L, long id, const double* f, double
     }
     default: break;
     }
-    int fam = faceFamily(k), dir = faceDir(k), ori = faceOri(k);
     const double* v = L->bcval + 3 * id;
+    if (k >= K_EDGE) { /* StoreVelocityDynamics::computeVelocity */
+        for (int d = 0; d < 3; ++d) u[d] = v[d];
+        return;
+    }
+    int fam = faceFamily(k), dir = faceDir(k), ori = faceOri(k);
     if (fam == 0 || fam == 2) { /* StoreVelocityDynamics::computeVelocity, boundaryDynamics.hh:324-330 */
         for (int d = 0; d < 3; ++d) u[d] = v[d];
         return;
@@ -657,9 +673,156 @@ static double cell_rhoBar(const orc_lattice* L, long id, const double* f) {
     case K_BGK: case K_GUO: case K_INCBGK: return get_rhoBar(f); /* core/dynamics.hh:351-354 */
     default: break;
     }
+    /* StoreVelocityDynamics::computeRhoBar: rhoBar(computeDensity()) with the BGK
+     * base density (boundaryDynamics.hh:342-345) */
+    if (k >= K_EDGE) return (get_rhoBar(f) + (double)1) - (double)1;
     int fam = faceFamily(k);
     if (fam == 0 || fam == 2) return vel_face_rhoBar(f, faceDir(k), faceOri(k), L->bcval + 3 * id);
     return L->bcval[3 * id] - (double)1; /* StoreDensityDynamics::computeRhoBar */
+}
+
+/* ------------------------------------------------------------ edges and corners
+ *
+ * External velocity edges and corners of createLocalBoundaryCondition3D:
+ * StoreVelocityDynamics around the BGK base, completed by the finite-
+ * difference processors OuterVelocityEdgeFunctional3D /
+ * OuterVelocityCornerFunctional3D (finiteDifferenceBoundaryProcessor3D.hh:
+ * 141-316), which run after the face processors and before each other in the
+ * order faces, edges, corners (setVelocityConditionOnBlockBoundaries,
+ * boundaryCondition3D.hh:65-163). */
+
+/* Density the way Cell::computeDensity reports it. */
+static double cell_density(const orc_lattice* L, long id, const double* f) {
+    int k = L->flags[id];
+    switch (k) {
+    /* BounceBack / NoDynamics return their rho member (core/dynamics.hh:814-816,
+     * 994-996), constructed here with bbRho */
+    case K_BB: case K_MEBB: case K_NODYN: return L->bbRho;
+    case K_BGK: case K_GUO: case K_INCBGK: return get_rhoBar(f) + (double)1; /* compute_rho */
+    default: break;
+    }
+    if (k >= K_EDGE) return get_rhoBar(f) + (double)1; /* BoundaryCompositeDynamics -> base */
+    int fam = faceFamily(k);
+    if (fam == 0 || fam == 2) return vel_face_rhoBar(f, faceDir(k), faceOri(k), L->bcval + 3 * id) + (double)1;
+    return (L->bcval[3 * id] - (double)1) + (double)1; /* StoreDensityDynamics::computeDensity */
+}
+
+/* f-bar of the IsoThermalBulkDynamics::regularize (isoThermalDynamics.hh:55-69)
+ * with the BGK equilibrium and offEquilibriumTemplates::fromPiToFneq. */
+static void regularize_pi(double* f, double rhoBar, const double j[3], double jSqr, const double Pi[6]) {
+    double invRho = invRhoOf(rhoBar);
+    f[0] = bgk_eq(0, rhoBar, invRho, j, jSqr) + fromPiToFneq(0, Pi);
+    for (int i = 1; i <= 9; ++i) {
+        f[i] = bgk_eq(i, rhoBar, invRho, j, jSqr);
+        f[i + 9] = bgk_eq(i + 9, rhoBar, invRho, j, jSqr);
+        double fn = fromPiToFneq(i, Pi);
+        f[i] += fn;
+        f[i + 9] += fn;
+    }
+}
+
+static void velocity_at(const orc_lattice* L, const double* f, int x, int y, int z, double u[3]) {
+    long id = lid(L, x, y, z);
+    cell_velocity(L, id, f + id * 19, u);
+}
+
+static double density_at(const orc_lattice* L, const double* f, int x, int y, int z) {
+    long id = lid(L, x, y, z);
+    return cell_density(L, id, f + id * 19);
+}
+
+/* fd::DirectedGradients3D (finiteDifference/finiteDifference3D.h:61-190):
+ * o1 forward difference along the boundary normal, central difference along
+ * the boundary. */
+static void grad_normal(const orc_lattice* L, const double* f, int p[3], int dir, int ori, double g[3]) {
+    double u0[3], u1[3];
+    velocity_at(L, f, p[0], p[1], p[2], u0);
+    int q[3] = {p[0], p[1], p[2]};
+    q[dir] -= ori;
+    velocity_at(L, f, q[0], q[1], q[2], u1);
+    for (int d = 0; d < 3; ++d) g[d] = (double)(-ori) * (-u0[d] + u1[d]); /* fdStencils1D.h:58-60 */
+}
+
+static void grad_central(const orc_lattice* L, const double* f, int p[3], int dir, double g[3]) {
+    double up[3], um[3];
+    int a[3] = {p[0], p[1], p[2]}, b[3] = {p[0], p[1], p[2]};
+    a[dir] += 1;
+    b[dir] -= 1;
+    velocity_at(L, f, a[0], a[1], a[2], up);
+    velocity_at(L, f, b[0], b[1], b[2], um);
+    for (int d = 0; d < 3; ++d) g[d] = (up[d] - um[d]) / (double)2; /* fdStencils1D.h:39-42 */
+}
+
+/* pi from the velocity gradients dA_uB[A][B] = d_A u_B and rho
+ * (finiteDifferenceBoundaryProcessor3D.hh:180-191). */
+static void pi_from_gradients(double dAuB[3][3], double rho, double omega, double Pi[6]) {
+    double sToPi = -rho / INVCS2 / omega;
+    Pi[0] = (double)2 * dAuB[0][0] * sToPi;
+    Pi[3] = (double)2 * dAuB[1][1] * sToPi;
+    Pi[5] = (double)2 * dAuB[2][2] * sToPi;
+    Pi[1] = (dAuB[0][1] + dAuB[1][0]) * sToPi;
+    Pi[2] = (dAuB[0][2] + dAuB[2][0]) * sToPi;
+    Pi[4] = (dAuB[1][2] + dAuB[2][1]) * sToPi;
+}
+
+static void complete_edge(const orc_lattice* L, double* f, int x, int y, int z) {
+    long id = lid(L, x, y, z);
+    int e = L->flags[id] - K_EDGE;
+    int plane = e / 4, n1 = (e & 2) ? 1 : -1, n2 = (e & 1) ? 1 : -1;
+    int d1 = (plane + 1) % 3, d2 = (plane + 2) % 3;
+    int p[3] = {x, y, z};
+    /* getNeighborRho (finiteDifferenceBoundaryProcessor3D.hh:220-227) */
+    int a[3] = {x, y, z}, b[3] = {x, y, z};
+    a[d1] -= n1;
+    b[d2] -= n2;
+    double rho10 = density_at(L, f, a[0], a[1], a[2]);
+    double rho01 = density_at(L, f, b[0], b[1], b[2]);
+    double rho = (double)0.5 * (rho01 + rho10);
+    double dAuB[3][3];
+    grad_central(L, f, p, plane, dAuB[plane]);
+    grad_normal(L, f, p, d1, n1, dAuB[d1]);
+    grad_normal(L, f, p, d2, n2, dAuB[d2]);
+    double Pi[6];
+    pi_from_gradients(dAuB, rho, L->omega, Pi);
+    double vel[3], j[3];
+    cell_velocity(L, id, f + id * 19, vel);
+    for (int d = 0; d < 3; ++d) j[d] = rho * vel[d];
+    double jSqr = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
+    regularize_pi(f + id * 19, rho - (double)1, j, jSqr, Pi);
+}
+
+static void complete_corner(const orc_lattice* L, double* f, int x, int y, int z) {
+    long id = lid(L, x, y, z);
+    int c = L->flags[id] - K_CORNER;
+    int nx = (c & 4) ? 1 : -1, ny = (c & 2) ? 1 : -1, nz = (c & 1) ? 1 : -1;
+    double rho100 = density_at(L, f, x - nx, y, z);
+    double rho010 = density_at(L, f, x, y - ny, z);
+    double rho001 = density_at(L, f, x, y, z - nz);
+    double rho = (double)1 / (double)3 * (rho001 + rho010 + rho100);
+    int p[3] = {x, y, z};
+    double dAuB[3][3];
+    grad_normal(L, f, p, 0, nx, dAuB[0]);
+    grad_normal(L, f, p, 1, ny, dAuB[1]);
+    grad_normal(L, f, p, 2, nz, dAuB[2]);
+    double Pi[6];
+    pi_from_gradients(dAuB, rho, L->omega, Pi);
+    double vel[3], j[3];
+    cell_velocity(L, id, f + id * 19, vel);
+    for (int d = 0; d < 3; ++d) j[d] = rho * vel[d];
+    double jSqr = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
+    regularize_pi(f + id * 19, rho - (double)1, j, jSqr, Pi);
+}
+
+/* The non-local post-stream processors: edges, then corners. */
+static void complete_edges_corners(const orc_lattice* L, double* f) {
+    for (int pass = 0; pass < 2; ++pass)
+        for (int x = 0; x < L->nx; ++x)
+            for (int y = 0; y < L->ny; ++y)
+                for (int z = 0; z < L->nz; ++z) {
+                    int k = L->flags[lid(L, x, y, z)];
+                    if (pass == 0 && is_edge(k)) complete_edge(L, f, x, y, z);
+                    if (pass == 1 && is_corner(k)) complete_corner(L, f, x, y, z);
+                }
 }
 
 /* computeAverageEnergy / computeAverageDensity over the bounding box

@@ -13,6 +13,7 @@
 //   int32    blocks_x, blocks_y, blocks_z   (regular block decomposition)
 //   int32    nsteps
 //   int32    stats_every        (record stored statistics every k steps, 0 = never)
+//   int32    options            (bit 0: do not call lattice.initialize())
 //   float64  omega, rho0 (IncBGK reference density), bbRho
 //   uint8    flags[N]           (kind per cell, x-major, z fastest)
 //   float64  bcval[N*3]         (velocity for velocity faces, rho in [0] for pressure faces)
@@ -47,8 +48,13 @@ enum Kind {
     K_REGPRESS = 12,  // 12..17
     K_ZHVEL = 18,     // 18..23
     K_ZHPRESS = 24,   // 24..29
-    K_NKINDS = 30
+    K_EDGE = 30,      // 30..41 : 30 + 4*plane + 2*(normal1>0) + (normal2>0)
+    K_CORNER = 42,    // 42..49 : 42 + 4*(xNormal>0) + 2*(yNormal>0) + (zNormal>0)
+    K_NKINDS = 50
 };
+
+// Case options (header word 12).
+enum { OPT_NO_INITIALIZE = 1 };  // skip lattice.initialize() before the first step
 
 struct Case {
     int nx, ny, nz;
@@ -57,6 +63,7 @@ struct Case {
     int blocks[3];
     int nsteps;
     int statsEvery;
+    int options;
     double omega, rho0, bbRho;
     std::vector<uint8_t> flags;
     std::vector<double> bcval, force, f0;
@@ -88,7 +95,7 @@ inline Case readCase(const char* path) {
     c.forced = h[6];
     c.blocks[0] = h[7]; c.blocks[1] = h[8]; c.blocks[2] = h[9];
     c.nsteps = h[10]; c.statsEvery = h[11];
-    (void)h[12];
+    c.options = h[12];
     double d[3];
     rd(f, d, 3);
     c.omega = d[0]; c.rho0 = d[1]; c.bbRho = d[2];

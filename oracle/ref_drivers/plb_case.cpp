@@ -118,6 +118,44 @@ void addFace(OnLatticeBoundaryCondition3D<double,D>& bc, MultiBlockLattice3D<dou
     }
 }
 
+// External velocity edge (plane, normal1, normal2) of the local regularized
+// condition (boundaryCondition/boundaryInstantiator3D.h:76-98).
+template<template<typename U> class D>
+void addEdge(OnLatticeBoundaryCondition3D<double,D>& bc, MultiBlockLattice3D<double,D>& lat, int e,
+             Box3D const& b) {
+    switch (e) {
+        case 0: bc.addExternalVelocityEdge0NN(b, lat); break;
+        case 1: bc.addExternalVelocityEdge0NP(b, lat); break;
+        case 2: bc.addExternalVelocityEdge0PN(b, lat); break;
+        case 3: bc.addExternalVelocityEdge0PP(b, lat); break;
+        case 4: bc.addExternalVelocityEdge1NN(b, lat); break;
+        case 5: bc.addExternalVelocityEdge1NP(b, lat); break;
+        case 6: bc.addExternalVelocityEdge1PN(b, lat); break;
+        case 7: bc.addExternalVelocityEdge1PP(b, lat); break;
+        case 8: bc.addExternalVelocityEdge2NN(b, lat); break;
+        case 9: bc.addExternalVelocityEdge2NP(b, lat); break;
+        case 10: bc.addExternalVelocityEdge2PN(b, lat); break;
+        case 11: bc.addExternalVelocityEdge2PP(b, lat); break;
+    }
+}
+
+// External velocity corner (xNormal, yNormal, zNormal)
+// (boundaryCondition/boundaryInstantiator3D.h:126-141).
+template<template<typename U> class D>
+void addCorner(OnLatticeBoundaryCondition3D<double,D>& bc, MultiBlockLattice3D<double,D>& lat, int k, plint x,
+               plint y, plint z) {
+    switch (k) {
+        case 0: bc.addExternalVelocityCornerNNN(x, y, z, lat); break;
+        case 1: bc.addExternalVelocityCornerNNP(x, y, z, lat); break;
+        case 2: bc.addExternalVelocityCornerNPN(x, y, z, lat); break;
+        case 3: bc.addExternalVelocityCornerNPP(x, y, z, lat); break;
+        case 4: bc.addExternalVelocityCornerPNN(x, y, z, lat); break;
+        case 5: bc.addExternalVelocityCornerPNP(x, y, z, lat); break;
+        case 6: bc.addExternalVelocityCornerPPN(x, y, z, lat); break;
+        case 7: bc.addExternalVelocityCornerPPP(x, y, z, lat); break;
+    }
+}
+
 template<typename V>
 void wr(FILE* f, const V* p, size_t n) {
     if (std::fwrite(p, sizeof(V), n, f) != n) die("short write");
@@ -170,7 +208,7 @@ int run(const Case& c, const char* outPath) {
     // Boundary cells: composite dynamics wrapped around a BGK base.
     OnLatticeBoundaryCondition3D<double,D>* reg = createLocalBoundaryCondition3D<double,D>();
     OnLatticeBoundaryCondition3D<double,D>* zh = createZouHeBoundaryCondition3D<double,D>();
-    for (int k = K_REGVEL; k < K_NKINDS; ++k) {
+    for (int k = K_REGVEL; k < K_EDGE; ++k) {
         dots = dotsOfKind(c, k);
         if (dots.getN() == 0) continue;
         defineDynamics(lat, dots, new BGKdynamics<double,D>(c.omega));
@@ -190,6 +228,24 @@ int run(const Case& c, const char* outPath) {
             }
         }
     }
+    // Edges and corners after every face, so that their finite-difference
+    // processors run after the face processors, as setVelocityConditionOnBlockBoundaries
+    // orders them (boundaryCondition/boundaryCondition3D.hh:65-163).
+    for (int k = K_EDGE; k < K_NKINDS; ++k) {
+        dots = dotsOfKind(c, k);
+        if (dots.getN() == 0) continue;
+        defineDynamics(lat, dots, new BGKdynamics<double,D>(c.omega));
+        for (int x = 0; x < c.nx; ++x)
+            for (int y = 0; y < c.ny; ++y)
+                for (int z = 0; z < c.nz; ++z) {
+                    if (c.flags[c.idx(x, y, z)] != k) continue;
+                    Box3D b(x, x, y, y, z, z);
+                    if (k < K_CORNER) addEdge(*reg, lat, k - K_EDGE, b);
+                    else addCorner(*reg, lat, k - K_CORNER, x, y, z);
+                    CellValueVelocity fv = {&c};
+                    setBoundaryVelocity(lat, b, fv);
+                }
+    }
     if (haveMebb) initializeMomentumExchange(lat, lat.getBoundingBox());
 
     // Initial populations (and the Guo force field).
@@ -204,7 +260,7 @@ int run(const Case& c, const char* outPath) {
                     ext[0] = c.force[3 * id]; ext[1] = c.force[3 * id + 1]; ext[2] = c.force[3 * id + 2];
                 }
             }
-    lat.initialize();
+    if (!(c.options & OPT_NO_INITIALIZE)) lat.initialize();
 
     std::vector<double> fInit, fFinal;
     dumpPopulations(lat, c, fInit);

@@ -36,6 +36,9 @@ def test_oracle_initialize_matches_reference(name):
     reference's state after lattice.initialize()."""
     g, meta = goldens.load(name)
     spec = lbcases.case_by_name(name)
+    if meta.get("options", 0) & lbcases.OPT_NO_INITIALIZE:
+        assert np.array_equal(spec.f0, g["f_init"])
+        return
     lat = O.OracleLattice.from_golden(g, meta)
     f0 = lat.initialize(spec.f0)
     assert np.array_equal(f0.reshape(g["f_init"].shape), g["f_init"])
@@ -46,7 +49,8 @@ def test_multiblock_equals_single_block():
     the populations, so one global addressing scheme reproduces it."""
     for a, b in [("periodic_bgk", "periodic_bgk_multiblock"),
                  ("cavity_bb_lid", "cavity_bb_lid_multiblock"),
-                 ("channel_sphere", "channel_sphere_multiblock")]:
+                 ("channel_sphere", "channel_sphere_multiblock"),
+                 ("velocity_box", "velocity_box_multiblock")]:
         ga, _ = goldens.load(a)
         gb, _ = goldens.load(b)
         assert np.array_equal(ga["f_final"], gb["f_final"])
@@ -67,3 +71,20 @@ def test_oracle_cavity64_full_size():
     e, rho = lat.reduce(f)
     assert e == pytest.approx(fp["energy"], rel=1e-12)
     assert e == pytest.approx(7.114849642596e-06, rel=1e-12)
+
+
+@pytest.mark.parametrize("shape", sorted(lbcases.DOCTEST_CAVITY))
+def test_oracle_reproduces_published_cavity_regression(shape):
+    """The reference's own 3D cavity regression values (regularized velocity
+    conditions on faces, edges and corners; 30 steps from rest).  They were
+    printed to five significant digits by an older build: the density agrees
+    to one unit of the last printed digit, the energy to 3e-3 relative, which
+    is also how far the reference built from these sources lies from them."""
+    e_pub, rho_pub = lbcases.DOCTEST_CAVITY[shape]
+    s = lbcases.doctest_cavity(*shape)
+    lat = O.OracleLattice(s.nx, s.ny, s.nz, s.periodic, s.omega, s.flags, s.bcval, s.force,
+                          s.rho0, s.bb_rho)
+    f, _ = lat.run(lat.initialize(s.f0), s.nsteps)
+    e, rho = lat.reduce(f)
+    assert abs(round(e, 10) / e_pub - 1) < 3e-3
+    assert abs(round(rho, 10) - rho_pub) <= 1.5e-7
