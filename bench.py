@@ -59,7 +59,7 @@ def build_lattice(precision, ctx=None):
 def algorithmic_bytes(kinds, precision):
     from palabos_gb300 import native as N
     cells = kinds.size
-    faces = int(((kinds >= N.REG_VELOCITY) & (kinds < 30)).sum())
+    faces = int(((kinds >= N.REG_VELOCITY) & (kinds < N.VELOCITY_EDGE)).sum())
     mebb = int((kinds == N.MOMENTUM_EXCHANGE).sum())
     # faces also read their 3 FP64 boundary values
     return cells * B_CELL[precision] + faces * 24, dict(cells=cells, faces=faces, mebb=mebb)
@@ -355,7 +355,7 @@ def run_gpu(args):
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": traffic,
                          "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
-                         "kernel": f"stepKernel<{head}> (fused collide+stream+faces, AA pattern)",
+                         "kernel": f"rowStepKernel+edgeRowStepKernel<{head}>: one fused collide+stream+faces step, AA pattern; traffic scaled from the row kernel by cells",
                          "bytes_per_launch": bytes_step},
             "forms": forms,
             "adjoint": adjoint,

@@ -62,6 +62,17 @@ typedef struct plbgpu_ctx plbgpu_ctx;
 #define PLBGPU_REG_PRESSURE 12 /* RegularizedDensityBoundaryDynamics (wrapped), regularizedBoundaryDynamics.hh:160-175 */
 #define PLBGPU_ZOUHE_VELOCITY 18 /* ZouHeVelocityDynamics (wrapped), zouHeDynamics.hh:44-113, 166-169 */
 #define PLBGPU_ZOUHE_PRESSURE 24 /* ZouHePressureDynamics (wrapped), zouHeDynamics.hh:222-225 */
+/* External velocity edge of the local regularized condition along axis
+ * `plane`, base + 4*plane + 2*(normal1 > 0) + (normal2 > 0) with normal1 along
+ * (plane+1)%3 and normal2 along (plane+2)%3: StoreVelocityDynamics around BGK,
+ * finished after every step (and by plbgpu_initialize) by the finite-difference
+ * OuterVelocityEdgeFunctional3D (boundaryInstantiator3D.h:423-470,
+ * finiteDifferenceBoundaryProcessor3D.hh:145-228). */
+#define PLBGPU_VELOCITY_EDGE 30
+/* External velocity corner, base + 4*(xNormal > 0) + 2*(yNormal > 0) +
+ * (zNormal > 0): OuterVelocityCornerFunctional3D, run after the edges
+ * (finiteDifferenceBoundaryProcessor3D.hh:238-316). */
+#define PLBGPU_VELOCITY_CORNER 42
 
 /* ------------------------------------------------------------ context */
 
@@ -107,6 +118,16 @@ int plbgpu_set_kinds(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1
                      const uint8_t* kinds, size_t n);
 int plbgpu_get_kinds(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1, int z0, int z1,
                      uint8_t* kinds, size_t n);
+
+/* OnLatticeBoundaryCondition3D::setVelocityConditionOnBlockBoundaries(lattice,
+ * box) of createLocalBoundaryCondition3D (boundaryCondition3D.hh:65-163): the
+ * box's six faces become regularized velocity faces, its twelve edges and
+ * eight corners the external velocity edges and corners above; every extent
+ * of the box must be at least 3.  Edge and corner cells need their inward
+ * neighbours inside the domain; a layout that breaks this is reported by the
+ * next plbgpu_initialize / plbgpu_collide_and_stream as PLBGPU_ERR_ARG. */
+int plbgpu_set_velocity_condition_on_block_boundaries(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0,
+                                                      int y1, int z0, int z1);
 
 /* setBoundaryVelocity / setBoundaryDensity (dataInitializerWrapper3D.h:99-118),
  * constant over a box or one value per cell of the box (`values`: 3 doubles

@@ -45,6 +45,10 @@ def lib():
         _lib.orc_reduce.argtypes = [ctypes.POINTER(_Params), u8, dp, dp, dp, dp, dp]
         _lib.orc_velocity.argtypes = [ctypes.POINTER(_Params), u8, dp, dp, dp, dp]
         _lib.orc_mebb_masks.argtypes = [ctypes.POINTER(_Params), u8, ctypes.POINTER(ctypes.c_uint32)]
+        _lib.orc_rhobar_j.argtypes = [ctypes.POINTER(_Params), u8, dp, dp, dp, dp, dp]
+        _lib.orc_run_external.argtypes = [ctypes.POINTER(_Params), u8, dp, dp, dp, dp, dp, ctypes.c_int,
+                                          ctypes.c_int, dp]
+        _lib.orc_run_external.restype = ctypes.c_int
         _lib.orc_set_threads.argtypes = [ctypes.c_int]
         _lib.orc_max_threads.restype = ctypes.c_int
     return _lib
@@ -108,6 +112,29 @@ class OracleLattice:
         out = np.zeros(self.flags.size * 3)
         lib().orc_velocity(ctypes.byref(self.p), self._u8(), _dp(self.bcval), _dp(self.force), _dp(f), _dp(out))
         return out.reshape(self.shape + (3,))
+
+    def rhobar_j(self, f):
+        """BoxRhoBarJfunctional3D: (rho-bar (nx, ny, nz), j (nx, ny, nz, 3))."""
+        f = np.ascontiguousarray(f, np.float64)
+        rb = np.zeros(self.flags.size)
+        j = np.zeros(self.flags.size * 3)
+        lib().orc_rhobar_j(ctypes.byref(self.p), self._u8(), _dp(self.bcval), _dp(self.force), _dp(f),
+                           _dp(rb), _dp(j))
+        return rb.reshape(self.shape), j.reshape(self.shape + (3,))
+
+    def run_external(self, f, rho_bar, j, nsteps, recompute=True):
+        """ExternalRhoJcollideAndStream3D for nsteps with the given fields (and,
+        with recompute, BoxRhoBarJfunctional3D after each step); returns
+        (f, rho_bar, j, stats[nsteps, 7])."""
+        f = np.ascontiguousarray(f, np.float64).copy()
+        rb = np.ascontiguousarray(rho_bar, np.float64).reshape(self.shape).copy()
+        jj = np.ascontiguousarray(j, np.float64).reshape(self.shape + (3,)).copy()
+        stats = np.zeros((max(nsteps, 1), 7))
+        rc = lib().orc_run_external(ctypes.byref(self.p), self._u8(), _dp(self.bcval), _dp(self.force),
+                                    _dp(f), _dp(rb), _dp(jj), int(bool(recompute)), int(nsteps), _dp(stats))
+        if rc != 0:
+            raise MemoryError("oracle allocation failed")
+        return f, rb, jj, stats
 
     def mebb_masks(self):
         out = np.zeros(self.flags.size, np.uint32)

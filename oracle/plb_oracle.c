@@ -287,6 +287,40 @@ static void collide_cell(const orc_lattice* L, long id, double* f, orc_stats* st
     st->count += 1;
 }
 
+/* ExternalRhoJcollideAndStream3D (dynamicsProcessor3D.hh:41-56): every cell's
+ * Dynamics::collideExternal with rho-bar and j taken from the fields.  BGK (and
+ * the BGK base of boundary cells) and IncBGK run their collision on the given
+ * moments and gather no statistics (isoThermalDynamics.hh:333-338, 1422-1427);
+ * Guo-forced BGK takes the generic route, shifting every population by the
+ * change of equilibrium and then colliding as usual (core/dynamics.hh:131-145);
+ * bounce-back, momentum exchange and no-dynamics collide as usual
+ * (core/dynamics.hh:793-798, 974-977, bounceBackModels.hh:139-144). */
+static void collide_cell_external(const orc_lattice* L, long id, double* f, double rbExt, const double jExt[3],
+                                  orc_stats* st) {
+    int k = L->flags[id];
+    if (k == K_INCBGK) {
+        bgk_collision_base(f, rbExt, jExt, L->omega, (double)1 / L->rho0);
+        return;
+    }
+    if (k == K_BGK || (k >= K_REGVEL && k < K_NKINDS)) {
+        bgk_collision_base(f, rbExt, jExt, L->omega, invRhoOf(rbExt));
+        return;
+    }
+    if (k == K_GUO) {
+        double oldRb, oldJ[3];
+        get_rhoBar_j(f, &oldRb, oldJ); /* BasicBulkDynamics::computeRhoBarJ */
+        double oldJsqr = oldJ[0] * oldJ[0] + oldJ[1] * oldJ[1] + oldJ[2] * oldJ[2];
+        double jSqr = jExt[0] * jExt[0] + jExt[1] * jExt[1] + jExt[2] * jExt[2];
+        double oldInv = invRhoOf(oldRb), newInv = invRhoOf(rbExt);
+        for (int i = 0; i < 19; ++i) {
+            double oldEq = bgk_eq(i, oldRb, oldInv, oldJ, oldJsqr);
+            double newEq = bgk_eq(i, rbExt, newInv, jExt, jSqr);
+            f[i] += newEq - oldEq;
+        }
+    }
+    collide_cell(L, id, f, st);
+}
+
 /* ------------------------------------------------------------ boundary faces */
 
 static int faceDir(int k) { return ((k - K_REGVEL) % 6) / 2; }
@@ -497,8 +531,16 @@ static int is_corner(int k) { return k >= K_CORNER && k < K_NKINDS; }
  * domain-edge rule: a population whose destination lies outside a
  * non-periodic domain stays in the cell, reversed -- blockLattice3D.hh:403-427),
  * then complete the boundary faces. */
-static void step(const orc_lattice* L, double* f, double* tmp, orc_stats* st) {
+static void cell_rhoBar_j(const orc_lattice* L, long id, const double* f, double* rb, double j[3]);
+
+/* extRho / extJ non-null: collide with the external fields (collide_cell_external)
+ * and, after streaming, recompute them from the streamed populations before
+ * the boundary processors run (BoxRhoBarJfunctional3D integrated at a later
+ * processor level, dataAnalysisFunctional3D.hh:528-549) when recompute is set. */
+static void step(const orc_lattice* L, double* f, double* tmp, orc_stats* st, double* extRho, double* extJ,
+                 int recompute) {
     long n = (long)L->nx * L->ny * L->nz;
+    const int external = extRho != NULL;
     double sR = 0., sU = 0., mU = -1.79769313486231570815e+308;
     long cnt = 0;
     double d0 = 0., d1 = 0., d2 = 0.;
@@ -507,7 +549,8 @@ static void step(const orc_lattice* L, double* f, double* tmp, orc_stats* st) {
         orc_stats s = {0., 0., -1.79769313486231570815e+308, 0, {0., 0., 0.}};
         double* c = tmp + id * 19;
         memcpy(c, f + id * 19, 19 * sizeof(double));
-        collide_cell(L, id, c, &s);
+        if (external) collide_cell_external(L, id, c, extRho[id], extJ + 3 * id, &s);
+        else collide_cell(L, id, c, &s);
         sR += s.sumRhoBar; sU += s.sumUSqr; cnt += s.count;
         if (s.maxUSqr > mU) mU = s.maxUSqr;
         d0 += s.drag[0]; d1 += s.drag[1]; d2 += s.drag[2];
@@ -534,9 +577,16 @@ static void step(const orc_lattice* L, double* f, double* tmp, orc_stats* st) {
                         out[i] = (src >= 0) ? tmp[src * 19 + i] : tmp[id * 19 + opp(i)];
                     }
                 }
-                if (is_face(L->flags[id])) complete_face(L, id, out);
+                if (!external && is_face(L->flags[id])) complete_face(L, id, out);
             }
         }
+    if (external) {
+        if (recompute)
+#pragma omp parallel for schedule(static)
+            for (long id = 0; id < n; ++id) cell_rhoBar_j(L, id, f + id * 19, extRho + id, extJ + 3 * id);
+        for (long id = 0; id < n; ++id)
+            if (is_face(L->flags[id])) complete_face(L, id, f + id * 19);
+    }
     if (L->hasEdges) complete_edges_corners(L, f);
 }
 
@@ -606,7 +656,7 @@ int orc_run(const orc_params* p, const uint8_t* flags, const double* bcval, cons
     if (!tmp) { free(L.mebbMask); return -1; }
     for (int s = 0; s < nsteps; ++s) {
         orc_stats st;
-        step(&L, f, tmp, &st);
+        step(&L, f, tmp, &st, NULL, NULL, 0);
         if (stats) {
             double* r = stats + 7 * (long)s;
             r[0] = st.count ? st.sumRhoBar / (double)st.count : 0.;
@@ -823,6 +873,83 @@ static void complete_edges_corners(const orc_lattice* L, double* f) {
                     if (pass == 0 && is_edge(k)) complete_edge(L, f, x, y, z);
                     if (pass == 1 && is_corner(k)) complete_corner(L, f, x, y, z);
                 }
+}
+
+/* Dynamics::computeRhoBarJ the way each kind implements it: the bulk moments
+ * (core/dynamics.hh:357-361), the stored rho of bounce-back / momentum
+ * exchange with j = 0 (core/dynamics.hh:880-885, bounceBackModels.hh:226-231),
+ * rho-bar 0 and j = 0 for no-dynamics (core/dynamics.hh:1061-1066), the
+ * velocity-face and pressure-face formulas (boundaryDynamics.hh:682-702,
+ * 815-822) and, for edges and corners, the base density with the stored
+ * velocity (boundaryDynamics.hh:348-360). */
+static void cell_rhoBar_j(const orc_lattice* L, long id, const double* f, double* rb, double j[3]) {
+    int k = L->flags[id];
+    const double* v = L->bcval + 3 * id;
+    switch (k) {
+    case K_BB: case K_MEBB:
+        *rb = L->bbRho - (double)1;
+        j[0] = j[1] = j[2] = 0.;
+        return;
+    case K_NODYN:
+        *rb = (double)1 - (double)1;
+        j[0] = j[1] = j[2] = 0.;
+        return;
+    case K_BGK: case K_GUO: case K_INCBGK:
+        get_rhoBar_j(f, rb, j);
+        return;
+    default: break;
+    }
+    if (k >= K_EDGE) {
+        double rho = get_rhoBar(f) + (double)1;
+        *rb = rho - (double)1;
+        for (int d = 0; d < 3; ++d) j[d] = rho * (v[d] - 0.5 * 0.);
+        return;
+    }
+    int fam = faceFamily(k), dir = faceDir(k), ori = faceOri(k);
+    if (fam == 0 || fam == 2) {
+        vel_face_rhoBar_j(f, dir, ori, v, rb, j);
+    } else {
+        *rb = v[0] - (double)1;
+        press_face_j(f, dir, ori, *rb, j);
+    }
+}
+
+/* BoxRhoBarJfunctional3D over the bounding box: rho-bar (N) and j (N*3). */
+int orc_rhobar_j(const orc_params* p, const uint8_t* flags, const double* bcval, const double* force,
+                 const double* f, double* rhoBar, double* j) {
+    orc_lattice L;
+    setup(&L, p, flags, bcval, force);
+    long n = (long)p->nx * p->ny * p->nz;
+    for (long id = 0; id < n; ++id) cell_rhoBar_j(&L, id, f + id * 19, rhoBar + id, j + 3 * id);
+    free(L.mebbMask);
+    return 0;
+}
+
+/* nsteps of ExternalRhoJcollideAndStream3D with the fields rhoBar / j (updated
+ * in place when recompute is set); stats as orc_run (drag only: the BGK-family
+ * external collisions gather none). */
+int orc_run_external(const orc_params* p, const uint8_t* flags, const double* bcval, const double* force,
+                     double* f, double* rhoBar, double* j, int recompute, int nsteps, double* stats) {
+    orc_lattice L;
+    setup(&L, p, flags, bcval, force);
+    long n = (long)p->nx * p->ny * p->nz;
+    double* tmp = (double*)malloc((size_t)n * 19 * sizeof(double));
+    if (!tmp) { free(L.mebbMask); return -1; }
+    for (int s = 0; s < nsteps; ++s) {
+        orc_stats st;
+        step(&L, f, tmp, &st, rhoBar, j, recompute);
+        if (stats) {
+            double* r = stats + 7 * (long)s;
+            r[0] = st.count ? st.sumRhoBar / (double)st.count : 0.;
+            r[1] = st.count ? st.sumUSqr / (double)st.count : 0.;
+            r[2] = st.maxUSqr; /* the lowest double when no cell gathered statistics */
+            r[3] = st.drag[0]; r[4] = st.drag[1]; r[5] = st.drag[2];
+            r[6] = (double)st.count;
+        }
+    }
+    free(tmp);
+    free(L.mebbMask);
+    return 0;
 }
 
 /* computeAverageEnergy / computeAverageDensity over the bounding box

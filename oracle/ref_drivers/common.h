@@ -19,6 +19,7 @@
 //   float64  bcval[N*3]         (velocity for velocity faces, rho in [0] for pressure faces)
 //   float64  force[N*3]         (Guo force, only read when forced)
 //   float64  f0[N*19]           (initial f-bar, before lattice.initialize())
+//   float64  rhoBar0[N], j0[N*3] (only with OPT_EXTERNAL_RHOJ: initial fields)
 //
 // Result file:
 //   char[8]  "PLBRES01"
@@ -29,6 +30,7 @@
 //                                         maxUSqr, drag[3]
 //   float64  avgEnergy, avgDensity   (computeAverageEnergy / computeAverageDensity
 //                                     over the bounding box after nsteps)
+//   float64  rhoBar[N], j[N*3]   (only with OPT_EXTERNAL_RHOJ: the fields at the end)
 #ifndef PLB_REF_DRIVER_COMMON_H
 #define PLB_REF_DRIVER_COMMON_H
 
@@ -54,7 +56,11 @@ enum Kind {
 };
 
 // Case options (header word 12).
-enum { OPT_NO_INITIALIZE = 1 };  // skip lattice.initialize() before the first step
+enum {
+    OPT_NO_INITIALIZE = 1,   // skip lattice.initialize() before the first step
+    OPT_EXTERNAL_RHOJ = 2    // step with ExternalRhoJcollideAndStream3D (level 0) and
+                             // BoxRhoBarJfunctional3D (level 3) from the given fields
+};
 
 struct Case {
     int nx, ny, nz;
@@ -66,7 +72,7 @@ struct Case {
     int options;
     double omega, rho0, bbRho;
     std::vector<uint8_t> flags;
-    std::vector<double> bcval, force, f0;
+    std::vector<double> bcval, force, f0, rhoBar0, j0;
     long n() const { return (long)nx * ny * nz; }
     long idx(int x, int y, int z) const { return ((long)x * ny + y) * nz + z; }
 };
@@ -104,6 +110,10 @@ inline Case readCase(const char* path) {
     c.bcval.resize(n * 3); rd(f, c.bcval.data(), n * 3);
     c.force.resize(n * 3); rd(f, c.force.data(), n * 3);
     c.f0.resize(n * 19); rd(f, c.f0.data(), n * 19);
+    if (c.options & OPT_EXTERNAL_RHOJ) {
+        c.rhoBar0.resize(n); rd(f, c.rhoBar0.data(), n);
+        c.j0.resize(n * 3); rd(f, c.j0.data(), n * 3);
+    }
     std::fclose(f);
     return c;
 }

@@ -265,10 +265,46 @@ int run(const Case& c, const char* outPath) {
     std::vector<double> fInit, fFinal;
     dumpPopulations(lat, c, fInit);
 
+    // The external rho-bar / j form: the two processors of a lattice stepped
+    // by executeInternalProcessors() instead of collideAndStream().
+    const bool external = (c.options & OPT_EXTERNAL_RHOJ) != 0;
+    std::auto_ptr<MultiScalarField3D<double> > rhoBarF;
+    std::auto_ptr<MultiTensorField3D<double,3> > jF;
+    if (external) {
+        rhoBarF = generateMultiScalarField<double>(lat, 1);
+        jF = generateMultiTensorField<double,3>(lat, 1);
+        for (int a = 0; a < 3; ++a) {
+            rhoBarF->periodicity().toggle(a, c.periodic[a] != 0);
+            jF->periodicity().toggle(a, c.periodic[a] != 0);
+        }
+        for (int x = 0; x < c.nx; ++x)
+            for (int y = 0; y < c.ny; ++y)
+                for (int z = 0; z < c.nz; ++z) {
+                    long id = c.idx(x, y, z);
+                    rhoBarF->get(x, y, z) = c.rhoBar0[id];
+                    Array<double,3>& jj = jF->get(x, y, z);
+                    jj[0] = c.j0[3 * id]; jj[1] = c.j0[3 * id + 1]; jj[2] = c.j0[3 * id + 2];
+                }
+        rhoBarF->duplicateOverlaps(modif::staticVariables);
+        jF->duplicateOverlaps(modif::staticVariables);
+        std::vector<MultiBlock3D*> args;
+        args.push_back(&lat);
+        args.push_back(rhoBarF.get());
+        args.push_back(jF.get());
+        integrateProcessingFunctional(new ExternalRhoJcollideAndStream3D<double,D>(), lat.getBoundingBox(), args, 0);
+        integrateProcessingFunctional(new BoxRhoBarJfunctional3D<double,D>(), lat.getBoundingBox(), args, 3);
+    }
+
     struct Rec { int32_t step; double v[6]; };
     std::vector<Rec> recs;
     for (int s = 0; s < c.nsteps; ++s) {
-        lat.collideAndStream();
+        if (external) {
+            lat.executeInternalProcessors();
+            lat.evaluateStatistics();
+            lat.incrementTime();
+        } else {
+            lat.collideAndStream();
+        }
         if (c.statsEvery > 0 && (s + 1) % c.statsEvery == 0) {
             BlockStatistics const& st = lat.getInternalStatistics();
             Rec r;
@@ -297,6 +333,19 @@ int run(const Case& c, const char* outPath) {
     }
     double tail[2] = {energy, density};
     wr(f, tail, 2);
+    if (external) {   // the fields after the last BoxRhoBarJfunctional3D
+        std::vector<double> rb(c.n()), jj(3 * c.n());
+        for (int x = 0; x < c.nx; ++x)
+            for (int y = 0; y < c.ny; ++y)
+                for (int z = 0; z < c.nz; ++z) {
+                    long id = c.idx(x, y, z);
+                    rb[id] = rhoBarF->get(x, y, z);
+                    Array<double,3> const& v = jF->get(x, y, z);
+                    for (int d = 0; d < 3; ++d) jj[3 * id + d] = v[d];
+                }
+        wr(f, rb.data(), rb.size());
+        wr(f, jj.data(), jj.size());
+    }
     std::fclose(f);
     delete reg;
     delete zh;

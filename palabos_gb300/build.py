@@ -1,9 +1,11 @@
 """Build the CUDA library libplbgpu.so in-tree (palabos_gb300/_lib/).
 
-nvcc for sm_103a only; the three translation units compile in parallel.  The
-FP64 kernels and the host API are compiled with --fmad=false so that the FP64
-path rounds every multiply and add separately, exactly like the reference
-built without FMA contraction; the mixed-precision kernels use FMA.
+nvcc for sm_103a only; the translation units (host API, FP64 kernels, one unit
+per reduced storage type, the allocation-free reduction, the adjoint) compile
+in parallel.  The FP64 kernels and the host API are compiled with
+--fmad=false so that the FP64 path rounds every multiply and add separately,
+exactly like the reference built without FMA contraction; the mixed-precision
+kernels use FMA.
 """
 from __future__ import annotations
 
@@ -24,7 +26,13 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
           "-I", os.path.join(ROOT, "include")]
 # (source, fmad)
-UNITS = [("api.cu", False), ("step_fp64.cu", False), ("step_mixed.cu", True), ("noalloc.cu", False), ("adjoint.cu", False)]
+# Storage forms: (name, fmad).  Per form, the time-step kernels of each AA
+# parity (the costliest code) and the rest of its launcher table are separate
+# units; longest first.
+FORMS = [("fp64", False), ("fp32", True), ("bf16", True), ("fp16", True), ("bf16sr", True)]
+UNITS = ([(f"step_{f}_{p}.cu", fm) for f, fm in FORMS for p in ("even", "odd")]
+         + [(f"step_{f}.cu", fm) for f, fm in FORMS]
+         + [("adjoint.cu", False), ("api.cu", False), ("noalloc.cu", False)])
 
 
 def nvcc() -> str:
@@ -60,7 +68,7 @@ def build(force: bool = False, ptxas_verbose: bool = False) -> str:
     os.makedirs(OBJ, exist_ok=True)
     os.makedirs(LIB_DIR, exist_ok=True)
     extra = ["-Xptxas", "-v"] if ptxas_verbose else []
-    with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+    with cf.ThreadPoolExecutor(max_workers=min(len(UNITS), max(4, os.cpu_count() or 4))) as ex:
         objs = list(ex.map(lambda u: _compile(u[0], u[1], extra, force), UNITS))
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
         cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs]

@@ -3,9 +3,10 @@
 //
 // A domain is one rectangular lattice in a single device allocation:
 //   [ 19 population planes | cell kinds ]
-// plus, allocated on first need, the face values (3 FP64 planes), the Guo
-// force (3 planes, FP64 for the FP64 form and FP32 otherwise) and the
-// momentum-exchange fluid-direction masks.
+// plus, allocated on first need, the boundary values (3 FP64 planes), the Guo
+// force (3 planes, FP64 for the FP64 form and FP32 otherwise), the
+// momentum-exchange fluid-direction masks and the list of edge and corner
+// cells.
 #include <cuda_runtime.h>
 
 #include <cstdarg>
@@ -36,6 +37,10 @@ struct Domain {
     double* bc = nullptr;        // 3 * n
     void* force = nullptr;       // 3 * n of FP64 or FP32
     uint32_t* mebb = nullptr;    // n
+    int4* surf = nullptr;        // edge cells, then corner cells: (x, y, z, kind)
+    int surfCap = 0, nEdges = 0, nCorners = 0;
+    bool hasSurface = false;     // any edge or corner kind
+    bool surfDirty = false;      // the list needs rebuilding (kinds or periodicity changed)
     StatsAcc* stats = nullptr;   // device accumulator
     unsigned* status = nullptr;  // device error word written by the kernels
     ReduceAcc* red = nullptr;
@@ -213,6 +218,49 @@ __global__ void kindMaskKernel(const uint8_t* flags, long long n, unsigned long 
     if ((threadIdx.x & 31) == 0 && m) atomicOr(mask, m);
 }
 
+// Whether the edge / corner cell at (x, y, z) may read its neighbour one step
+// along `axis`: inside the domain after the periodic wrap, and -- for a
+// density read -- not a cell whose populations the same pass rewrites.
+__device__ bool surfaceReadOk(const DevLattice& L, int x, int y, int z, int axis, int step, int forbidFrom) {
+    int p[3] = {x, y, z};
+    const int n[3] = {L.nx, L.ny, L.nz};
+    p[axis] += step;
+    if (p[axis] < 0 || p[axis] >= n[axis]) {
+        if (!L.per[axis] || n[axis] < 2) return false;
+        p[axis] = p[axis] < 0 ? p[axis] + n[axis] : p[axis] - n[axis];
+    }
+    const int k = L.flags[((long long)p[0] * L.ny + p[1]) * L.nz + p[2]];
+    return !(forbidFrom >= 0 && k >= forbidFrom && k < K_NKINDS);
+}
+
+// Edge and corner cells (edges first) -- or, with out == nullptr, their
+// counts -- and the lowest cell index whose finite differences cannot be
+// taken (surfaceReadOk).
+__global__ void surfaceListKernel(DevLattice L, int4* out, int edgeCap, int* counts, unsigned long long* bad) {
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < L.n;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int k = L.flags[idx];
+        if (!isSurface(k)) continue;
+        const int z = (int)(idx % L.nz), y = (int)((idx / L.nz) % L.ny), x = (int)(idx / ((long long)L.ny * L.nz));
+        bool ok = true;
+        if (k < K_CORNER) {
+            const int e = k - K_EDGE, plane = e / 4, d1 = (plane + 1) % 3, d2 = (plane + 2) % 3;
+            const int n1 = (e & 2) ? 1 : -1, n2 = (e & 1) ? 1 : -1;
+            ok = surfaceReadOk(L, x, y, z, plane, 1, -1) && surfaceReadOk(L, x, y, z, plane, -1, -1) &&
+                 surfaceReadOk(L, x, y, z, d1, -n1, K_EDGE) && surfaceReadOk(L, x, y, z, d2, -n2, K_EDGE);
+        } else {
+            const int q = k - K_CORNER;
+            ok = surfaceReadOk(L, x, y, z, 0, (q & 4) ? -1 : 1, K_CORNER) &&
+                 surfaceReadOk(L, x, y, z, 1, (q & 2) ? -1 : 1, K_CORNER) &&
+                 surfaceReadOk(L, x, y, z, 2, (q & 1) ? -1 : 1, K_CORNER);
+        }
+        if (!ok) atomicMin(bad, (unsigned long long)idx);
+        const int which = k < K_CORNER ? 0 : 1;
+        const int slot = atomicAdd(&counts[which], 1);
+        if (out) out[which == 0 ? slot : edgeCap + slot] = make_int4(x, y, z, k);
+    }
+}
+
 int launchBox(plbgpu_ctx* c) {
     c->launches += 1;
     cudaError_t e = cudaGetLastError();
@@ -258,9 +306,60 @@ int syncKinds(plbgpu_ctx* c, Domain* d) {
     unsigned long long m = 0;
     int rc = kindMask(c, d, &m);
     if (rc) return rc;
-    bool faces = false;
+    bool faces = false, surface = false;
     for (int k = K_REGVEL; k < K_NKINDS; ++k) faces |= (m >> k) & 1;
+    for (int k = K_EDGE; k < K_NKINDS; ++k) surface |= (m >> k) & 1;
+    d->hasSurface = surface;
+    d->surfDirty = true;
     return ensureAux(c, d, faces, (m >> K_GUO) & 1, (m >> K_MEBB) & 1);
+}
+
+// Rebuild the edge / corner list, checking that every finite difference stays
+// inside the domain.
+int buildSurface(plbgpu_ctx* c, Domain* d) {
+    d->surfDirty = false;
+    d->nEdges = d->nCorners = 0;
+    if (!d->hasSurface) return PLBGPU_OK;
+    int rc = ensureStaging(c, 64);
+    if (rc) return rc;
+    int* counts = static_cast<int*>(c->staging);
+    unsigned long long* bad = reinterpret_cast<unsigned long long*>(static_cast<char*>(c->staging) + 16);
+    CUDA_TRY(c, cudaMemsetAsync(counts, 0, 2 * sizeof(int), c->stream));
+    CUDA_TRY(c, cudaMemsetAsync(bad, 0xff, sizeof(unsigned long long), c->stream));
+    surfaceListKernel<<<304, 256, 0, c->stream>>>(d->view(), nullptr, 0, counts, bad);
+    if ((rc = launchBox(c))) return rc;
+    int hc[2];
+    unsigned long long hbad;
+    CUDA_TRY(c, cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(&hbad, bad, sizeof(hbad), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if (hbad != ~0ull) {
+        d->surfDirty = true;
+        long long i = (long long)hbad;
+        return fail(c, PLBGPU_ERR_ARG,
+                    "edge/corner cell (%lld, %lld, %lld): its finite differences need neighbours inside the "
+                    "domain, and a face or bulk cell (edges) or a non-corner cell (corners) inward along each normal",
+                    i / ((long long)d->ny * d->nz), (i / d->nz) % d->ny, i % d->nz);
+    }
+    const int total = hc[0] + hc[1];
+    if (total > d->surfCap) {
+        if (d->surf) {
+            CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+            cudaFree(d->surf);
+            d->deviceBytes -= sizeof(int4) * (size_t)d->surfCap;
+            d->surf = nullptr;
+            d->surfCap = 0;
+        }
+        CUDA_TRY(c, cudaMalloc(&d->surf, sizeof(int4) * (size_t)total));
+        d->surfCap = total;
+        d->deviceBytes += sizeof(int4) * (size_t)total;
+    }
+    CUDA_TRY(c, cudaMemsetAsync(counts, 0, 2 * sizeof(int), c->stream));
+    surfaceListKernel<<<304, 256, 0, c->stream>>>(d->view(), d->surf, hc[0], counts, bad);
+    if ((rc = launchBox(c))) return rc;
+    d->nEdges = hc[0];
+    d->nCorners = hc[1];
+    return PLBGPU_OK;
 }
 
 StepConsts consts(const Domain* d) {
@@ -302,6 +401,31 @@ int materialize(plbgpu_ctx* c, Domain* d) {
         if (rc) return rc;
     }
     d->pending = false;
+    return PLBGPU_OK;
+}
+
+// The edge processors, then the corner processors, on the current state
+// (OuterVelocityEdgeFunctional3D / OuterVelocityCornerFunctional3D, which
+// setVelocityConditionOnBlockBoundaries adds after the faces:
+// boundaryCondition3D.hh:65-163).
+int finishSurface(plbgpu_ctx* c, Domain* d) {
+    int rc;
+    if (d->surfDirty && (rc = buildSurface(c, d))) return rc;
+    if (d->nEdges + d->nCorners == 0) return PLBGPU_OK;
+    const Launchers& L = launchers(d->precision);
+    const int pending = d->pending && d->bc ? 1 : 0;
+    const double invRho0 = (double)1 / d->rho0;
+    int n = L.surface(d->view(), d->odd, d->surf, d->nEdges, pending, invRho0, d->bbRho, d->omega, c->stream);
+    if (n) {
+        c->launches += n - 1;
+        if ((rc = launchBox(c))) return rc;
+    }
+    n = L.surface(d->view(), d->odd, d->surf + d->nEdges, d->nCorners, pending, invRho0, d->bbRho, d->omega,
+                  c->stream);
+    if (n) {
+        c->launches += n - 1;
+        if ((rc = launchBox(c))) return rc;
+    }
     return PLBGPU_OK;
 }
 
@@ -442,6 +566,7 @@ int plbgpu_remove_domain(plbgpu_ctx* c, int h) {
     if (d->bc) cudaFree(d->bc);
     if (d->force) cudaFree(d->force);
     if (d->mebb) cudaFree(d->mebb);
+    if (d->surf) cudaFree(d->surf);
     cudaFree(d->stats);
     cudaFree(d->status);
     cudaFree(d->red);
@@ -474,9 +599,11 @@ int plbgpu_set_periodicity(plbgpu_ctx* c, int h, int px, int py, int pz) {
         if ((rc = plbgpu_receive(c, h, 0, d->nx - 1, 0, d->ny - 1, 0, d->nz - 1, tmp.data(), tmp.size()))) return rc;
         d->per[0] = px != 0; d->per[1] = py != 0; d->per[2] = pz != 0;
         d->odd = false;
+        d->surfDirty = d->hasSurface;
         return plbgpu_send(c, h, 0, d->nx - 1, 0, d->ny - 1, 0, d->nz - 1, tmp.data(), tmp.size());
     }
     d->per[0] = px != 0; d->per[1] = py != 0; d->per[2] = pz != 0;
+    d->surfDirty = d->hasSurface;
     return PLBGPU_OK;
 }
 
@@ -523,6 +650,47 @@ int plbgpu_set_kinds(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z
         d->flags, d->n, d->ny, d->nz, b, static_cast<uint8_t*>(c->staging), 1, 0);
     if ((rc = launchBox(c))) return rc;
     return syncKinds(c, d);
+}
+
+int plbgpu_set_velocity_condition_on_block_boundaries(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1,
+                                                      int z0, int z1) {
+    Domain* d;
+    Box b;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if ((rc = checkBox(c, d, x0, x1, y0, y1, z0, z1, &b))) return rc;
+    if (x1 - x0 < 2 || y1 - y0 < 2 || z1 - z0 < 2)
+        return fail(c, PLBGPU_ERR_ARG, "velocity box [%d,%d]x[%d,%d]x[%d,%d]: every extent must be >= 3", x0, x1,
+                    y0, y1, z0, z1);
+    const int lo[3] = {x0, y0, z0}, hi[3] = {x1, y1, z1};
+    std::vector<uint8_t> kinds((size_t)boxCells(b));
+    if ((rc = plbgpu_get_kinds(c, h, x0, x1, y0, y1, z0, z1, kinds.data(), kinds.size()))) return rc;   // interior kept
+    for (int x = x0; x <= x1; ++x)
+        for (int y = y0; y <= y1; ++y)
+            for (int z = z0; z <= z1; ++z) {
+                const int p[3] = {x, y, z};
+                int side[3], nSides = 0;   // -1 low side, +1 high side, 0 inside
+                for (int a = 0; a < 3; ++a) {
+                    side[a] = p[a] == lo[a] ? -1 : (p[a] == hi[a] ? 1 : 0);
+                    nSides += side[a] != 0;
+                }
+                size_t o = ((size_t)(x - x0) * (y1 - y0 + 1) + (y - y0)) * (z1 - z0 + 1) + (z - z0);
+                int k;
+                if (nSides == 0) {
+                    continue;
+                } else if (nSides == 1) {
+                    int a = side[0] ? 0 : (side[1] ? 1 : 2);
+                    k = K_REGVEL + 2 * a + (side[a] > 0);
+                } else if (nSides == 2) {
+                    int plane = !side[0] ? 0 : (!side[1] ? 1 : 2);
+                    int n1 = side[(plane + 1) % 3], n2 = side[(plane + 2) % 3];
+                    k = K_EDGE + 4 * plane + 2 * (n1 > 0) + (n2 > 0);
+                } else {
+                    k = K_CORNER + 4 * (side[0] > 0) + 2 * (side[1] > 0) + (side[2] > 0);
+                }
+                kinds[o] = (uint8_t)k;
+            }
+    return plbgpu_set_kinds(c, h, x0, x1, y0, y1, z0, z1, kinds.data(), kinds.size());
 }
 
 int plbgpu_get_kinds(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, uint8_t* kinds,
@@ -666,7 +834,7 @@ int plbgpu_initialize(plbgpu_ctx* c, int h) {
     // initialize() twice completes twice, like the reference.
     if ((rc = materialize(c, d))) return rc;
     d->pending = true;
-    return PLBGPU_OK;
+    return finishSurface(c, d);
 }
 
 int plbgpu_send(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, const double* buf, size_t n) {
@@ -715,6 +883,7 @@ int plbgpu_collide_and_stream(plbgpu_ctx* c, int h, int nsteps, int collect_stat
     if (nsteps == 0) return PLBGPU_OK;
     const Launchers& L = launchers(d->precision);
     bool hasFaces = d->bc != nullptr;
+    if (d->surfDirty && (rc = buildSurface(c, d))) return rc;
     for (int s = 0; s < nsteps; ++s) {
         bool stats = collect_stats && s == nsteps - 1;
         if (stats) CUDA_TRY(c, cudaMemsetAsync(d->stats, 0, sizeof(StatsAcc), c->stream));
@@ -725,6 +894,7 @@ int plbgpu_collide_and_stream(plbgpu_ctx* c, int h, int nsteps, int collect_stat
         d->odd = !d->odd;
         d->pending = hasFaces;
         d->steps += 1;
+        if ((rc = finishSurface(c, d))) return rc;
     }
     if (collect_stats) d->statsValid = true;
     return PLBGPU_OK;

@@ -6,6 +6,8 @@
 // R = float is the FP32-compute form.  Citations are to the reference's src/.
 #pragma once
 
+#include <utility>
+
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -32,15 +34,23 @@ __host__ __device__ constexpr int cnorm2(int i) {
 // Cell kinds (one byte per cell).
 enum Kind : uint8_t {
     K_BGK = 0, K_GUO = 1, K_INCBGK = 2, K_BB = 3, K_MEBB = 4, K_NODYN = 5,
-    K_REGVEL = 6, K_REGPRESS = 12, K_ZHVEL = 18, K_ZHPRESS = 24, K_NKINDS = 30,
+    K_REGVEL = 6, K_REGPRESS = 12, K_ZHVEL = 18, K_ZHPRESS = 24,
+    K_EDGE = 30,    // 30..41: external velocity edge, 30 + 4*plane + 2*(normal1>0) + (normal2>0)
+    K_CORNER = 42,  // 42..49: external velocity corner, 42 + 4*(xNormal>0) + 2*(yNormal>0) + (zNormal>0)
+    K_NKINDS = 50,
     K_NONE = 255  // not part of the lattice (sparse storage)
 };
-__host__ __device__ inline bool isFace(int k) { return k >= K_REGVEL && k < K_NKINDS; }
+__host__ __device__ inline bool isFace(int k) { return k >= K_REGVEL && k < K_EDGE; }
+// Edge and corner cells: StoreVelocityDynamics around the BGK base, finished
+// after each step by the finite-difference processors.
+__host__ __device__ inline bool isSurface(int k) { return k >= K_EDGE && k < K_NKINDS; }
+// Kinds that collide with the plain BGK rule.
+__host__ __device__ inline bool bgkBase(int k) { return k == K_BGK || (k >= K_REGVEL && k < K_NKINDS); }
 __host__ __device__ inline int faceFamily(int k) { return (k - K_REGVEL) / 6; }
 __host__ __device__ inline int faceDir(int k) { return ((k - K_REGVEL) % 6) / 2; }
 __host__ __device__ inline int faceOri(int k) { return (((k - K_REGVEL) % 6) % 2) ? 1 : -1; }
 // Kinds whose collision gathers the lattice statistics (latticeStatistics.h:38-43).
-__host__ __device__ inline bool takesStats(int k) { return k == K_BGK || k == K_GUO || k == K_INCBGK || isFace(k); }
+__host__ __device__ inline bool takesStats(int k) { return k == K_GUO || k == K_INCBGK || bgkBase(k); }
 
 // Lattice weights, computed as (T)1/(T)3 etc. (nearestNeighborLattices3D.hh:183-205).
 template <typename R>
@@ -213,14 +223,30 @@ __host__ __device__ constexpr int subIndexCount() {
     return n;
 }
 
+// A population index known at compile time.
+template <int I>
+struct Idx {
+    __host__ __device__ constexpr operator int() const { return I; }
+};
+
+// fn(i) for each population i with c[DIR] == VAL, ascending, i a compile-time
+// constant (Idx): the index set is evaluated by the C++ front end, not by
+// unrolling subIndex's search in the optimizer.
+template <int DIR, int VAL, typename Fn, int... A>
+__device__ __forceinline__ void forSubImpl(Fn& fn, std::integer_sequence<int, A...>) {
+    (fn(Idx<subIndex<DIR, VAL>(A)>()), ...);
+}
+template <int DIR, int VAL, typename Fn>
+__device__ __forceinline__ void forSub(Fn&& fn) {
+    forSubImpl<DIR, VAL>(fn, std::make_integer_sequence<int, subIndexCount<DIR, VAL>()>());
+}
+
 // boundaryDynamics.hh:639-669 (VelocityDirichletBoundaryDynamics::computeRhoBar)
 template <typename R, int DIR, int ORI>
 __device__ __forceinline__ R velFaceRhoBar(const R* f, R velDir) {
     R rhoOnWall = R(0), rhoNormal = R(0);
-#pragma unroll
-    for (int a = 0; a < subIndexCount<DIR, 0>(); ++a) rhoOnWall += f[subIndex<DIR, 0>(a)];
-#pragma unroll
-    for (int a = 0; a < subIndexCount<DIR, ORI>(); ++a) rhoNormal += f[subIndex<DIR, ORI>(a)];
+    forSub<DIR, 0>([&](auto i) { rhoOnWall += f[i]; });
+    forSub<DIR, ORI>([&](auto i) { rhoNormal += f[i]; });
     R velNormal = (R)ORI * (velDir - (R)0.5 * (R)0);
     return ((R)2 * rhoNormal + rhoOnWall - (R)1 * velNormal) / ((R)1 + velNormal);
 }
@@ -229,10 +255,8 @@ __device__ __forceinline__ R velFaceRhoBar(const R* f, R velDir) {
 template <typename R, int DIR, int ORI>
 __device__ __forceinline__ void pressFaceJ(const R* f, R rhoBar, R* j) {
     R rhoOnWall = R(0), rhoNormal = R(0);
-#pragma unroll
-    for (int a = 0; a < subIndexCount<DIR, 0>(); ++a) rhoOnWall += f[subIndex<DIR, 0>(a)];
-#pragma unroll
-    for (int a = 0; a < subIndexCount<DIR, ORI>(); ++a) rhoNormal += f[subIndex<DIR, ORI>(a)];
+    forSub<DIR, 0>([&](auto i) { rhoOnWall += f[i]; });
+    forSub<DIR, ORI>([&](auto i) { rhoNormal += f[i]; });
     j[0] = j[1] = j[2] = R(0);
     j[DIR] = (R)ORI * ((R)2 * rhoNormal + rhoOnWall - rhoBar);
 }
@@ -258,6 +282,22 @@ __device__ __forceinline__ R piToFneq(int i, const R* Pi) {
 
 // regularizedBoundaryDynamics.hh:96-110 with boundaryTemplates.h:42-84 and
 // isoThermalDynamics.hh:55-69
+// IsoThermalBulkDynamics::regularize with the BGK equilibrium
+// (isoThermalDynamics.hh:55-69): f = f_eq(rhoBar, j) + fromPiToFneq(Pi).
+template <typename R>
+__device__ __forceinline__ void regularizeFromPi(R* f, R rhoBar, const R* j, R jSqr, const R* Pi) {
+    R invRho = invRhoOf(rhoBar);
+    f[0] = bgkEq<R>(0, rhoBar, invRho, j, jSqr) + piToFneq<R>(0, Pi);
+#pragma unroll
+    for (int i = 1; i <= 9; ++i) {
+        f[i] = bgkEq<R>(i, rhoBar, invRho, j, jSqr);
+        f[i + 9] = bgkEq<R>(i + 9, rhoBar, invRho, j, jSqr);
+        R fn = piToFneq<R>(i, Pi);
+        f[i] += fn;
+        f[i + 9] += fn;
+    }
+}
+
 template <typename R, int DIR, int ORI>
 __device__ __forceinline__ void regularizedComplete(R* f, R rhoBar, const R* j) {
     R jSqr = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
@@ -275,16 +315,8 @@ __device__ __forceinline__ void regularizedComplete(R* f, R rhoBar, const R* j) 
 #pragma unroll
         for (int be = al; be < 3; ++be) {
             R s = R(0);
-#pragma unroll
-            for (int a = 0; a < subIndexCount<DIR, 0>(); ++a) {
-                const int i = subIndex<DIR, 0>(a);
-                s += (R)(cdir(i, al) * cdir(i, be)) * fNeq[i];
-            }
-#pragma unroll
-            for (int a = 0; a < subIndexCount<DIR, ORI>(); ++a) {
-                const int i = subIndex<DIR, ORI>(a);
-                s += (R)2 * (R)cdir(i, al) * (R)cdir(i, be) * fNeq[i];
-            }
+            forSub<DIR, 0>([&](auto i) { s += (R)(cdir(i, al) * cdir(i, be)) * fNeq[i]; });
+            forSub<DIR, ORI>([&](auto i) { s += (R)2 * (R)cdir(i, al) * (R)cdir(i, be) * fNeq[i]; });
             Pi[iPi++] = s;
         }
     f[0] = bgkEq<R>(0, rhoBar, invRho, j, jSqr) + piToFneq<R>(0, Pi);
@@ -316,18 +348,27 @@ __host__ __device__ constexpr int zhDiag(int a) {
     return -1;
 }
 
+// fn(p) over zhMissing (DIAG false) or zhDiag (DIAG true), p a compile-time constant.
+template <int DIR, int ORI, bool DIAG, typename Fn, int... A>
+__device__ __forceinline__ void forEachZhImpl(Fn& fn, std::integer_sequence<int, A...>) {
+    (fn(Idx<DIAG ? zhDiag<DIR, ORI>(A) : zhMissing<DIR, ORI>(A)>()), ...);
+}
+template <int DIR, int ORI, bool DIAG, typename Fn>
+__device__ __forceinline__ void forEachZh(Fn&& fn) {
+    constexpr int n = subIndexCount<DIR, ORI>() - (DIAG ? 1 : 0);
+    forEachZhImpl<DIR, ORI, DIAG>(fn, std::make_integer_sequence<int, n>());
+}
+
 // zouHeDynamics.hh:44-113 (ZouHeClosure)
 template <typename R, int DIR, int ORI>
 __device__ __forceinline__ void zouHeComplete(R* f, R rhoBar, const R* j) {
-    constexpr int nm = subIndexCount<DIR, ORI>();
-    constexpr int nd = nm - 1;
+    constexpr int nd = subIndexCount<DIR, ORI>() - 1;
     R jSqr = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
     R invRho = invRhoOf(rhoBar);
-#pragma unroll
-    for (int a = 0; a < nm; ++a) {
-        const int p = zhMissing<DIR, ORI>(a), o = opp(p);
+    forEachZh<DIR, ORI, false>([&](auto p) {
+        const int o = opp(p);
         f[p] = f[o] - bgkEq<R>(o, rhoBar, invRho, j, jSqr) + bgkEq<R>(p, rhoBar, invRho, j, jSqr);
-    }
+    });
     R rb, jj[3];
     rhoBarJ<R>(f, rb, jj);
     R invR = invRhoOf(rb);
@@ -335,15 +376,13 @@ __device__ __forceinline__ void zouHeComplete(R* f, R rhoBar, const R* j) {
     R diff[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) diff[d] = (j[d] - falseRho * (jj[d] * invR)) / (R)nd;
-#pragma unroll
-    for (int a = 0; a < nd; ++a) {
-        const int p = zhDiag<DIR, ORI>(a);
+    forEachZh<DIR, ORI, true>([&](auto p) {
 #pragma unroll
         for (int s = 1; s < 3; ++s) {
             const int d = (DIR + s) % 3;
             f[p] += (R)cdir(p, d) * diff[d];
         }
-    }
+    });
 }
 
 // Completion of one face cell; v = (ux, uy, uz) for velocity faces,

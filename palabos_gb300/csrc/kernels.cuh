@@ -285,8 +285,9 @@ __device__ __forceinline__ bool collideCell(const DevLattice& L, const StepParam
     using R = typename StoreT<S>::R;
     using F = typename StoreT<S>::F;
     R j[3];
-    if (k == K_BGK || isFace(k)) {
-        // isoThermalDynamics.hh:319-330; faces use their BGK base collide.
+    if (bgkBase(k)) {
+        // isoThermalDynamics.hh:319-330; faces, edges and corners use their
+        // BGK base collide.
         rhoBarJ<R>(f, rhoBar, j);
         uSqr = bgkCollide<R>(f, rhoBar, j, P.bgk, invRhoOf(rhoBar));
         return true;
@@ -751,6 +752,12 @@ __device__ __forceinline__ bool cellMacroscopic(const DevLattice& L, int x, int 
         rhoBarJ<R>(f, rr, jj);
         for (int d = 0; d < 3; ++d) u[d] = jj[d] * invRho0;
         rb = rhoBarSeq<R>(f);
+    } else if (isSurface(k)) {  // StoreVelocityDynamics over BGK: stored u, base density
+        for (int d = 0; d < 3; ++d) u[d] = (R)L.bc[d * L.n + idx];
+        const R rs = rhoBarSeq<R>(f);
+        rho = (double)(rs + (R)1);             // BoundaryCompositeDynamics::computeDensity
+        rb = (rs + (R)1) - (R)1;               // StoreVelocityDynamics::computeRhoBar
+        return true;
     } else if (isFace(k)) {
         const int fam = faceFamily(k), dir = faceDir(k);
         double v[3] = {L.bc[idx], L.bc[L.n + idx], L.bc[2 * L.n + idx]};
@@ -766,6 +773,153 @@ __device__ __forceinline__ bool cellMacroscopic(const DevLattice& L, int x, int 
     }
     rho = (double)rb + 1.0;   // fullRho(rhoBar)
     return true;
+}
+
+// ---------------------------------------------------------------- edges and corners
+//
+// External velocity edges and corners of the local regularized condition:
+// after the faces, each edge cell, then each corner cell, is rebuilt as
+// f_eq(rho, rho u) + fNeq(Pi) from finite differences of its neighbours'
+// velocities and densities (OuterVelocityEdgeFunctional3D /
+// OuterVelocityCornerFunctional3D, finiteDifferenceBoundaryProcessor3D.hh:
+// 141-316).  The host lists the cells (x, y, z, kind) and has checked that
+// every neighbour read below lies inside the domain (after the periodic wrap),
+// and that an edge reads no edge's or corner's density and a corner no
+// corner's density, so that no thread reads populations another one writes.
+
+__device__ __forceinline__ int wrapAxis(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
+
+// cellMacroscopic as one out-of-line call: the finite differences read up to
+// five neighbours, and inlining the face completion into each would multiply
+// the kernel's code (and compile time) for no gain on a few thousand cells.
+template <typename S, bool ODD>
+__device__ __noinline__ void surfaceMacro(const DevLattice& L, int x, int y, int z, int pending,
+                                          typename StoreT<S>::R invRho0, double bbRho, typename StoreT<S>::R* u,
+                                          typename StoreT<S>::R& rb, double& rho) {
+    cellMacroscopic<S, ODD>(L, x, y, z, pending, invRho0, bbRho, u, rb, rho);
+}
+
+// Cell::computeVelocity of the cell at p (faces pending completion included).
+template <typename S, bool ODD>
+__device__ __forceinline__ void surfaceVelocity(const DevLattice& L, const int* p, int pending,
+                                                typename StoreT<S>::R invRho0, double bbRho,
+                                                typename StoreT<S>::R* u) {
+    using R = typename StoreT<S>::R;
+    const int x = wrapAxis(p[0], L.nx), y = wrapAxis(p[1], L.ny), z = wrapAxis(p[2], L.nz);
+    const long long idx = ((long long)x * L.ny + y) * L.nz + z;
+    if (isSurface(L.flags[idx])) {  // stored velocity: no population read
+#pragma unroll
+        for (int d = 0; d < 3; ++d) u[d] = (R)L.bc[d * L.n + idx];
+        return;
+    }
+    R rb;
+    double rho;
+    surfaceMacro<S, ODD>(L, x, y, z, pending, invRho0, bbRho, u, rb, rho);
+}
+
+// Cell::computeDensity of the cell at p.
+template <typename S, bool ODD>
+__device__ __forceinline__ typename StoreT<S>::R surfaceDensity(const DevLattice& L, const int* p, int pending,
+                                                               typename StoreT<S>::R invRho0, double bbRho) {
+    using R = typename StoreT<S>::R;
+    R u[3], rb;
+    double rho;
+    surfaceMacro<S, ODD>(L, wrapAxis(p[0], L.nx), wrapAxis(p[1], L.ny), wrapAxis(p[2], L.nz), pending, invRho0,
+                         bbRho, u, rb, rho);
+    return (R)rho;
+}
+
+// fd::DirectedGradients3D (finiteDifference/finiteDifference3D.h:61-190):
+// first-order one-sided difference into the domain along a normal,
+// d_A u = -normal (u(x - normal e_A) - u(x)); centred difference along the
+// boundary, d_A u = (u(x + e_A) - u(x - e_A)) / 2.
+template <typename S, bool ODD>
+__device__ __forceinline__ void normalGradient(const DevLattice& L, const int* p, int axis, int normal, int pending,
+                                               typename StoreT<S>::R invRho0, double bbRho,
+                                               const typename StoreT<S>::R* u0, typename StoreT<S>::R* g) {
+    using R = typename StoreT<S>::R;
+    int q[3] = {p[0], p[1], p[2]};
+    q[axis] -= normal;
+    R u1[3];
+    surfaceVelocity<S, ODD>(L, q, pending, invRho0, bbRho, u1);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) g[d] = (R)(-normal) * (-u0[d] + u1[d]);
+}
+
+template <typename S, bool ODD>
+__device__ __forceinline__ void centralGradient(const DevLattice& L, const int* p, int axis, int pending,
+                                                typename StoreT<S>::R invRho0, double bbRho,
+                                                typename StoreT<S>::R* g) {
+    using R = typename StoreT<S>::R;
+    int a[3] = {p[0], p[1], p[2]}, b[3] = {p[0], p[1], p[2]};
+    a[axis] += 1;
+    b[axis] -= 1;
+    R up[3], um[3];
+    surfaceVelocity<S, ODD>(L, a, pending, invRho0, bbRho, up);
+    surfaceVelocity<S, ODD>(L, b, pending, invRho0, bbRho, um);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) g[d] = (up[d] - um[d]) / (R)2;
+}
+
+// One launch finishes `count` edge cells or `count` corner cells.
+template <typename S, bool ODD>
+__global__ void surfaceKernel(DevLattice L, const int4* __restrict__ cells, int count, int pending,
+                              typename StoreT<S>::R invRho0, double bbRho, typename StoreT<S>::R omega) {
+    using R = typename StoreT<S>::R;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const int4 c = cells[t];
+    const int p[3] = {c.x, c.y, c.z};
+    const int k = c.w;
+    const long long idx = ((long long)c.x * L.ny + c.y) * L.nz + c.z;
+    R vel[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) vel[d] = (R)L.bc[d * L.n + idx];
+    R rho, g[3][3];
+    if (k < K_CORNER) {
+        const int e = k - K_EDGE, plane = e / 4;
+        const int n1 = (e & 2) ? 1 : -1, n2 = (e & 1) ? 1 : -1;
+        const int d1 = (plane + 1) % 3, d2 = (plane + 2) % 3;
+        int a[3] = {p[0], p[1], p[2]}, b[3] = {p[0], p[1], p[2]};
+        a[d1] -= n1;
+        b[d2] -= n2;
+        const R rho10 = surfaceDensity<S, ODD>(L, a, pending, invRho0, bbRho);
+        const R rho01 = surfaceDensity<S, ODD>(L, b, pending, invRho0, bbRho);
+        rho = (R)0.5 * (rho01 + rho10);
+        centralGradient<S, ODD>(L, p, plane, pending, invRho0, bbRho, g[plane]);
+        normalGradient<S, ODD>(L, p, d1, n1, pending, invRho0, bbRho, vel, g[d1]);
+        normalGradient<S, ODD>(L, p, d2, n2, pending, invRho0, bbRho, vel, g[d2]);
+    } else {
+        const int q = k - K_CORNER;
+        const int nrm[3] = {(q & 4) ? 1 : -1, (q & 2) ? 1 : -1, (q & 1) ? 1 : -1};
+        R r[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            int nbp[3] = {p[0], p[1], p[2]};
+            nbp[a] -= nrm[a];
+            r[a] = surfaceDensity<S, ODD>(L, nbp, pending, invRho0, bbRho);
+        }
+        rho = (R)1 / (R)3 * (r[2] + r[1] + r[0]);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) normalGradient<S, ODD>(L, p, a, nrm[a], pending, invRho0, bbRho, vel, g[a]);
+    }
+    // finiteDifferenceBoundaryProcessor3D.hh:180-206
+    const R sToPi = -rho / (R)3 / omega;
+    R Pi[6];
+    Pi[0] = (R)2 * g[0][0] * sToPi;
+    Pi[1] = (g[0][1] + g[1][0]) * sToPi;
+    Pi[2] = (g[0][2] + g[2][0]) * sToPi;
+    Pi[3] = (R)2 * g[1][1] * sToPi;
+    Pi[4] = (g[1][2] + g[2][1]) * sToPi;
+    Pi[5] = (R)2 * g[2][2] * sToPi;
+    R j[3] = {rho * vel[0], rho * vel[1], rho * vel[2]};
+    const R jSqr = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
+    R f[19];
+    regularizeFromPi<R>(f, rho - (R)1, j, jSqr, Pi);
+    Neighbourhood nb = neighbourhood(L, c.x, c.y, c.z);
+    S* Pp = static_cast<S*>(L.pop);
+#pragma unroll
+    for (int i = 0; i < 19; ++i) StoreT<S>::st(Pp + slotOf<ODD>(L, nb, idx, i), f[i]);
 }
 
 // computeAverageEnergy / computeAverageDensity (dataAnalysisWrapper3D.hh:1226-1262).

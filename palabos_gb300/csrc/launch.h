@@ -29,6 +29,9 @@ struct Launchers {
                        double invRho0, cudaStream_t);
     int (*field)(const DevLattice&, bool odd, Box, int pending, double invRho0, double bbRho, int what,
                  double* out, cudaStream_t);
+    // Edge or corner cells (x, y, z, kind) finished after a step.
+    int (*surface)(const DevLattice&, bool odd, const int4* cells, int count, int pending, double invRho0,
+                   double bbRho, double omega, cudaStream_t);
 };
 
 const Launchers& launchersFp64();

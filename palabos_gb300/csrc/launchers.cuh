@@ -1,5 +1,5 @@
-// Launcher bodies, instantiated per storage type by step_fp64.cu and
-// step_mixed.cu.
+// Launcher bodies, instantiated per storage type by step_<type>.cu (the time
+// step itself by step_<type>_<parity>.cu).
 #pragma once
 
 #include "launch.h"
@@ -40,53 +40,18 @@ __global__ void equilibriumKernel(DevLattice L, Box b, const double* rhou, doubl
     }
 }
 
+// One time step of the given AA parity.  Each (storage type, parity) pair is
+// instantiated in its own translation unit (step_<type>_even.cu /
+// step_<type>_odd.cu, from step_parity.cuh) so that the row kernels, the
+// costliest code to compile, build in parallel.
+template <typename S, bool ODD>
+int stepParity(const DevLattice& L, bool stats, const StepParams<typename StoreT<S>::R>& p, StatsAcc* acc,
+               cudaStream_t s);
+
 template <typename S>
 struct LaunchImpl {
     using R = typename StoreT<S>::R;
     static constexpr int kBlock = 128;
-
-    // Row kernel of this storage type: the paired kernel for the 2-byte forms
-    // when rows have an even length, the one-cell register kernel otherwise.
-    static bool pairedRows(const DevLattice& L) { return sizeof(S) == 2 && L.nz % 2 == 0; }
-
-    template <bool ODD, bool STATS>
-    static int stepSplit(const DevLattice& L, const StepParams<R>& p, StatsAcc* acc, cudaStream_t s) {
-        int launched = 0;
-        int edgeRows = (L.nx < 3 || L.ny < 3) ? L.nx * L.ny : 2 * L.ny + 2 * (L.nx - 2);
-        if (L.nx >= 3 && L.ny >= 3 && pairedRows(L)) {
-            Planes<S> pl;
-            Deltas d;
-            for (int i = 0; i < 19; ++i) {
-                pl.p[i] = static_cast<S*>(L.pop) + (long long)i * L.stride;
-                d.d[i] = cdir(i, 0) * L.ny * L.nz + cdir(i, 1) * L.nz + cdir(i, 2);
-            }
-            if constexpr (sizeof(S) == 2) {
-                const int pairs = L.nz / 2;
-                int tpb = (pairs + 31) / 32 * 32;
-                tpb = tpb < kBlock ? tpb : kBlock;
-                pairRowStepKernel<S, ODD, STATS><<<rowGrid(pairs, L.ny - 2, L.nx - 2, tpb), tpb, 0, s>>>(L, pl, d, p,
-                                                                                                      acc);
-                ++launched;
-            }
-        } else if (L.nx >= 3 && L.ny >= 3) {
-            Planes<S> pl;
-            Deltas d;
-            for (int i = 0; i < 19; ++i) {
-                pl.p[i] = static_cast<S*>(L.pop) + (long long)i * L.stride;
-                d.d[i] = cdir(i, 0) * L.ny * L.nz + cdir(i, 1) * L.nz + cdir(i, 2);
-            }
-            // one block per row segment of cells * threads cells; short rows get
-            // fewer threads so that every thread owns `cells` live cells
-            constexpr int NC = RowShape<S>::cells;
-            int tpb = ((L.nz + NC - 1) / NC + 31) / 32 * 32;
-            tpb = tpb < kBlock ? tpb : kBlock;
-            rowStepKernel<S, ODD, STATS><<<rowGrid(L.nz, L.ny - 2, L.nx - 2, tpb * NC), tpb, 0, s>>>(L, pl, d, p, acc);
-            ++launched;
-        }
-        dim3 g((unsigned)((L.nz + kBlock - 1) / kBlock), (unsigned)edgeRows, 1);
-        edgeRowStepKernel<S, ODD, STATS><<<g, kBlock, 0, s>>>(L, p, acc);
-        return launched + 1;
-    }
 
     static int step(const DevLattice& L, bool odd, bool stats, const StepConsts& c, StatsAcc* acc,
                     cudaStream_t s) {
@@ -99,8 +64,7 @@ struct LaunchImpl {
         p.invRho0 = (R)c.invRho0;
         p.pending = c.pending;
         p.seed = c.seed;
-        if (odd) return stats ? stepSplit<true, true>(L, p, acc, s) : stepSplit<true, false>(L, p, acc, s);
-        return stats ? stepSplit<false, true>(L, p, acc, s) : stepSplit<false, false>(L, p, acc, s);
+        return odd ? stepParity<S, true>(L, stats, p, acc, s) : stepParity<S, false>(L, stats, p, acc, s);
     }
     static int completeFaces(const DevLattice& L, bool odd, cudaStream_t s) {
         dim3 g = rowGrid(L.nz, L.ny, L.nx, kBlock);
@@ -143,8 +107,18 @@ struct LaunchImpl {
             equilibriumKernel<S, false><<<g, kBlock, 0, s>>>(L, b, rhou, cst[0], cst[1], cst[2], cst[3], invRho0);
         return 1;
     }
+    static int surface(const DevLattice& L, bool odd, const int4* cells, int count, int pending, double invRho0,
+                       double bbRho, double omega, cudaStream_t s) {
+        if (count <= 0) return 0;
+        const int tpb = 64, blocks = (count + tpb - 1) / tpb;
+        if (odd)
+            surfaceKernel<S, true><<<blocks, tpb, 0, s>>>(L, cells, count, pending, (R)invRho0, bbRho, (R)omega);
+        else
+            surfaceKernel<S, false><<<blocks, tpb, 0, s>>>(L, cells, count, pending, (R)invRho0, bbRho, (R)omega);
+        return 1;
+    }
     static const Launchers& table() {
-        static const Launchers t = {step, completeFaces, extract, insert, reduce, equilibrium, field};
+        static const Launchers t = {step, completeFaces, extract, insert, reduce, equilibrium, field, surface};
         return t;
     }
 };

@@ -1,0 +1,7 @@
+// Time step of the bf16sr storage form, even AA parity (see step_parity.cuh).
+#include "step_parity.cuh"
+
+namespace plbgpu {
+template int stepParity<bf16sr, false>(const DevLattice&, bool, const StepParams<StoreT<bf16sr>::R>&, StatsAcc*,
+                                        cudaStream_t);
+}  // namespace plbgpu

@@ -1,0 +1,7 @@
+// Time step of the fp16 storage form, even AA parity (see step_parity.cuh).
+#include "step_parity.cuh"
+
+namespace plbgpu {
+template int stepParity<__half, false>(const DevLattice&, bool, const StepParams<StoreT<__half>::R>&, StatsAcc*,
+                                        cudaStream_t);
+}  // namespace plbgpu

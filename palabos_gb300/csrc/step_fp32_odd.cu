@@ -1,0 +1,7 @@
+// Time step of the fp32 storage form, odd AA parity (see step_parity.cuh).
+#include "step_parity.cuh"
+
+namespace plbgpu {
+template int stepParity<float, true>(const DevLattice&, bool, const StepParams<StoreT<float>::R>&, StatsAcc*,
+                                        cudaStream_t);
+}  // namespace plbgpu

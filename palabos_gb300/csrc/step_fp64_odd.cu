@@ -1,0 +1,7 @@
+// Time step of the fp64 storage form, odd AA parity (see step_parity.cuh).
+#include "step_parity.cuh"
+
+namespace plbgpu {
+template int stepParity<double, true>(const DevLattice&, bool, const StepParams<StoreT<double>::R>&, StatsAcc*,
+                                        cudaStream_t);
+}  // namespace plbgpu

@@ -1,0 +1,68 @@
+// Time-step launchers of one storage type and AA parity: the row kernel of
+// the interior rows, then the edge-row kernel.  Included only by the
+// step_<type>_<parity>.cu translation units, each of which instantiates
+// stepParity<S, ODD> once.
+#pragma once
+
+#include "launchers.cuh"
+
+namespace plbgpu {
+
+template <typename S>
+struct StepLaunch {
+    using R = typename StoreT<S>::R;
+    static constexpr int kBlock = 128;
+
+    // Row kernel of this storage type: the paired kernel for the 2-byte forms
+    // when rows have an even length, the one-cell register kernel otherwise.
+    static bool pairedRows(const DevLattice& L) { return sizeof(S) == 2 && L.nz % 2 == 0; }
+
+    template <bool ODD, bool STATS>
+    static int stepSplit(const DevLattice& L, const StepParams<R>& p, StatsAcc* acc, cudaStream_t s) {
+        int launched = 0;
+        int edgeRows = (L.nx < 3 || L.ny < 3) ? L.nx * L.ny : 2 * L.ny + 2 * (L.nx - 2);
+        if (L.nx >= 3 && L.ny >= 3 && pairedRows(L)) {
+            Planes<S> pl;
+            Deltas d;
+            for (int i = 0; i < 19; ++i) {
+                pl.p[i] = static_cast<S*>(L.pop) + (long long)i * L.stride;
+                d.d[i] = cdir(i, 0) * L.ny * L.nz + cdir(i, 1) * L.nz + cdir(i, 2);
+            }
+            if constexpr (sizeof(S) == 2) {
+                const int pairs = L.nz / 2;
+                int tpb = (pairs + 31) / 32 * 32;
+                tpb = tpb < kBlock ? tpb : kBlock;
+                pairRowStepKernel<S, ODD, STATS><<<rowGrid(pairs, L.ny - 2, L.nx - 2, tpb), tpb, 0, s>>>(L, pl, d, p,
+                                                                                                      acc);
+                ++launched;
+            }
+        } else if (L.nx >= 3 && L.ny >= 3) {
+            Planes<S> pl;
+            Deltas d;
+            for (int i = 0; i < 19; ++i) {
+                pl.p[i] = static_cast<S*>(L.pop) + (long long)i * L.stride;
+                d.d[i] = cdir(i, 0) * L.ny * L.nz + cdir(i, 1) * L.nz + cdir(i, 2);
+            }
+            // one block per row segment of cells * threads cells; short rows get
+            // fewer threads so that every thread owns `cells` live cells
+            constexpr int NC = RowShape<S>::cells;
+            int tpb = ((L.nz + NC - 1) / NC + 31) / 32 * 32;
+            tpb = tpb < kBlock ? tpb : kBlock;
+            rowStepKernel<S, ODD, STATS><<<rowGrid(L.nz, L.ny - 2, L.nx - 2, tpb * NC), tpb, 0, s>>>(L, pl, d, p, acc);
+            ++launched;
+        }
+        dim3 g((unsigned)((L.nz + kBlock - 1) / kBlock), (unsigned)edgeRows, 1);
+        edgeRowStepKernel<S, ODD, STATS><<<g, kBlock, 0, s>>>(L, p, acc);
+        return launched + 1;
+    }
+
+};
+
+template <typename S, bool ODD>
+int stepParity(const DevLattice& L, bool stats, const StepParams<typename StoreT<S>::R>& p, StatsAcc* acc,
+               cudaStream_t s) {
+    return stats ? StepLaunch<S>::template stepSplit<ODD, true>(L, p, acc, s)
+                 : StepLaunch<S>::template stepSplit<ODD, false>(L, p, acc, s);
+}
+
+}  // namespace plbgpu

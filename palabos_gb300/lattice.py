@@ -129,6 +129,22 @@ class DeviceLattice3D:
         fam = N.ZOUHE_VELOCITY if zou_he else N.REG_VELOCITY
         self.define_dynamics(box, N.face_kind(fam, direction, orientation))
 
+    def add_external_velocity_edge(self, box, plane, normal1, normal2):
+        """addExternalVelocityEdge{plane}{N|P}{N|P}(box, lattice) of the local
+        regularized condition: finished after every step (and by
+        initialize()) by the finite-difference edge processor."""
+        self.define_dynamics(box, N.edge_kind(plane, normal1, normal2))
+
+    def add_external_velocity_corner(self, x, y, z, x_normal, y_normal, z_normal):
+        """addExternalVelocityCorner{N|P}{N|P}{N|P}(x, y, z, lattice)."""
+        self.define_dynamics((x, x, y, y, z, z), N.corner_kind(x_normal, y_normal, z_normal))
+
+    def set_velocity_condition_on_block_boundaries(self, box=None):
+        """setVelocityConditionOnBlockBoundaries(lattice, box): regularized
+        velocity faces, edges and corners on the box's surface."""
+        self._check(self.lib.plbgpu_set_velocity_condition_on_block_boundaries(self.ctx.h, self.handle,
+                                                                              *self._box(box)))
+
     def add_pressure_boundary(self, box, direction, orientation, zou_he=False):
         fam = N.ZOUHE_PRESSURE if zou_he else N.REG_PRESSURE
         self.define_dynamics(box, N.face_kind(fam, direction, orientation))
@@ -291,12 +307,14 @@ def lattice_from_description(nx, ny, nz, periodic, omega, flags, bcval=None, for
     flags = np.ascontiguousarray(flags, np.uint8).reshape(nx, ny, nz)
     lat.set_kinds(flags)
     kinds = set(np.unique(flags).tolist())
-    if bcval is not None and any(6 <= k < 30 for k in kinds):
+    if bcval is not None and any(REG_VELOCITY <= k < N.NKINDS for k in kinds):
         bc = np.asarray(bcval, np.float64).reshape(nx, ny, nz, 3)
         vel = np.zeros_like(bc)
-        is_press = ((flags >= REG_PRESSURE) & (flags < REG_PRESSURE + 6)) | (flags >= ZOUHE_PRESSURE)
+        is_press = ((flags >= REG_PRESSURE) & (flags < REG_PRESSURE + 6)) | \
+                   ((flags >= ZOUHE_PRESSURE) & (flags < ZOUHE_PRESSURE + 6))
         is_vel = ((flags >= REG_VELOCITY) & (flags < REG_PRESSURE)) | \
-                 ((flags >= ZOUHE_VELOCITY) & (flags < ZOUHE_PRESSURE))
+                 ((flags >= ZOUHE_VELOCITY) & (flags < ZOUHE_PRESSURE)) | \
+                 ((flags >= N.VELOCITY_EDGE) & (flags < N.NKINDS))
         vel[is_vel] = bc[is_vel]
         vel[is_press, 0] = bc[is_press, 0]
         lat.set_boundary_velocity(None, vel)   # the three planes; density lives in component 0

@@ -23,11 +23,23 @@ PRECISIONS = {"fp64": FP64, "fp32": FP32, "bf16": BF16, "fp16": FP16, "bf16sr": 
 
 BGK, GUO, INCBGK, BOUNCEBACK, MOMENTUM_EXCHANGE, NODYNAMICS = 0, 1, 2, 3, 4, 5
 REG_VELOCITY, REG_PRESSURE, ZOUHE_VELOCITY, ZOUHE_PRESSURE = 6, 12, 18, 24
+VELOCITY_EDGE, VELOCITY_CORNER, NKINDS = 30, 42, 50
 
 
 def face_kind(family: int, direction: int, orientation: int) -> int:
     """Kind of a face boundary: family + 2*direction + (orientation > 0)."""
     return family + 2 * direction + (1 if orientation > 0 else 0)
+
+
+def edge_kind(plane: int, normal1: int, normal2: int) -> int:
+    """External velocity edge along axis `plane`; normal1 is along (plane+1)%3,
+    normal2 along (plane+2)%3 (addExternalVelocityEdge{plane}{N|P}{N|P})."""
+    return VELOCITY_EDGE + 4 * plane + 2 * (normal1 > 0) + (normal2 > 0)
+
+
+def corner_kind(x_normal: int, y_normal: int, z_normal: int) -> int:
+    """External velocity corner (addExternalVelocityCorner{N|P}{N|P}{N|P})."""
+    return VELOCITY_CORNER + 4 * (x_normal > 0) + 2 * (y_normal > 0) + (z_normal > 0)
 
 
 class PlbGpuError(RuntimeError):
@@ -61,6 +73,7 @@ SIGNATURES = {
     "plbgpu_define_dynamics": [_vp, _i, *BOX, _i],
     "plbgpu_set_kinds": [_vp, _i, *BOX, _c_u8_p, _sz],
     "plbgpu_get_kinds": [_vp, _i, *BOX, _c_u8_p, _sz],
+    "plbgpu_set_velocity_condition_on_block_boundaries": [_vp, _i, *BOX],
     "plbgpu_set_boundary_velocity": [_vp, _i, *BOX, _d, _d, _d],
     "plbgpu_set_boundary_velocity_field": [_vp, _i, *BOX, _c_dbl_p, _sz],
     "plbgpu_set_boundary_density": [_vp, _i, *BOX, _d],

@@ -35,7 +35,7 @@ int main(int argc, char** argv) {
     if (guo) lattice.setExternalVector(all, c.force);
     if (mebb) lattice.initializeMomentumExchange();
     lattice.send(all, c.f0);
-    lattice.initialize();
+    if (!(c.options & OPT_NO_INITIALIZE)) lattice.initialize();
     std::vector<double> fInit = lattice.receive(all);
 
     struct Rec { int32_t step; double v[6]; };

@@ -38,6 +38,7 @@ BGK, GUO, INCBGK, BB, MEBB, NODYN = 0, 1, 2, 3, 4, 5
 REGVEL, REGPRESS, ZHVEL, ZHPRESS = 6, 12, 18, 24
 EDGE, CORNER = 30, 42
 OPT_NO_INITIALIZE = 1
+OPT_EXTERNAL_RHOJ = 2
 
 
 def face_kind(family: int, direction: int, orientation: int) -> int:
@@ -96,6 +97,8 @@ class CaseSpec:
     rho0: float = 1.0
     bb_rho: float = 0.0
     options: int = 0
+    rho_bar0: np.ndarray = None   # initial external rho-bar field (OPT_EXTERNAL_RHOJ)
+    j0: np.ndarray = None         # initial external j field
 
     def meta(self):
         return dict(name=self.name, nx=self.nx, ny=self.ny, nz=self.nz,
@@ -384,6 +387,45 @@ def case_velocity_box_noinit():
     return s
 
 
+def external_fields(spec, rng, amp=2e-3):
+    """Initial external rho-bar / j fields: the moments of the initial state
+    (bulk formula) plus a smooth perturbation, so that the first collision
+    really uses values the populations do not hold."""
+    f = spec.f0
+    rho_bar = f.sum(-1)
+    j = np.einsum("...q,qd->...d", f, C.astype(np.float64))
+    shape = (spec.nx, spec.ny, spec.nz)
+    _, du = smooth_fields(shape, rng, amp, 0.0)
+    rho_bar = rho_bar + amp * np.cos(2 * np.pi * np.arange(spec.nx) / spec.nx)[:, None, None]
+    return np.ascontiguousarray(rho_bar), np.ascontiguousarray(j + du)
+
+
+def with_external(spec, name, seed):
+    spec.name = name
+    spec.options |= OPT_EXTERNAL_RHOJ
+    spec.rho_bar0, spec.j0 = external_fields(spec, np.random.default_rng(seed))
+    return spec
+
+
+def case_external_periodic_bgk():
+    return with_external(case_periodic_bgk(), "external_periodic_bgk", 201)
+
+
+def case_external_incbgk_nodyn():
+    return with_external(case_incbgk_nodyn(), "external_incbgk_nodyn", 202)
+
+
+def case_external_guo_periodic():
+    return with_external(case_guo_periodic_multiblock(), "external_guo_periodic_multiblock", 203)
+
+
+def case_external_mebb_periodic():
+    """Momentum-exchange obstacle and bounce-back in a fully periodic box."""
+    s = case_mebb_walls()
+    s.periodic = (1, 1, 1)
+    return with_external(s, "external_mebb_periodic", 204)
+
+
 def case_doctest_cavity20():
     return doctest_cavity(20, 20, 20, name="doctest_cavity20")
 
@@ -405,6 +447,8 @@ CASES = [
     case_guo_periodic_multiblock, case_regvel_faces, case_regpress_faces, case_zhvel_faces,
     case_zhpress_faces, case_incbgk_nodyn, case_mebb_walls, case_velocity_box,
     case_velocity_box_multiblock, case_velocity_box_noinit, case_doctest_cavity20,
+    case_external_periodic_bgk, case_external_incbgk_nodyn, case_external_guo_periodic,
+    case_external_mebb_periodic,
 ]
 
 
@@ -443,6 +487,9 @@ def write_case_file(spec: CaseSpec, path: str):
         f.write(np.ascontiguousarray(spec.bcval, np.float64).tobytes())
         f.write(np.ascontiguousarray(spec.force, np.float64).tobytes())
         f.write(np.ascontiguousarray(spec.f0, np.float64).tobytes())
+        if spec.options & OPT_EXTERNAL_RHOJ:
+            f.write(np.ascontiguousarray(spec.rho_bar0, np.float64).tobytes())
+            f.write(np.ascontiguousarray(spec.j0, np.float64).tobytes())
 
 
 def read_result_file(path: str, spec: CaseSpec):
@@ -464,5 +511,11 @@ def read_result_file(path: str, spec: CaseSpec):
         stats[k, 1:] = vals
         off += 4 + 48
     energy, density = struct.unpack_from("<2d", data, off)
-    return dict(f_init=f_init.copy(), f_final=f_final.copy(), stats=stats,
-                energy=energy, density=density)
+    off += 16
+    out = dict(f_init=f_init.copy(), f_final=f_final.copy(), stats=stats, energy=energy, density=density)
+    if spec.options & OPT_EXTERNAL_RHOJ:
+        m = nx * ny * nz
+        out["rho_bar_final"] = np.frombuffer(data, np.float64, m, off).reshape(nx, ny, nz).copy()
+        off += 8 * m
+        out["j_final"] = np.frombuffer(data, np.float64, 3 * m, off).reshape(nx, ny, nz, 3).copy()
+    return out

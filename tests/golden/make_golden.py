@@ -63,12 +63,16 @@ def main(argv):
             if only and spec.name not in only:
                 continue
             res = run_reference(spec, tmp)
+            extra = {}
+            if spec.rho_bar0 is not None:
+                extra = dict(rho_bar0=spec.rho_bar0, j0=spec.j0, rho_bar_final=res["rho_bar_final"],
+                             j_final=res["j_final"])
             np.savez_compressed(
                 os.path.join(HERE, spec.name + ".npz"),
                 flags=spec.flags, bcval=spec.bcval, force=spec.force,
                 f_init=res["f_init"], f_final=res["f_final"], stats=res["stats"],
                 energy=res["energy"], density=res["density"],
-                meta=json.dumps(spec.meta()),
+                meta=json.dumps(spec.meta()), **extra,
             )
             print(f"{spec.name}: {spec.nx}x{spec.ny}x{spec.nz}, {spec.nsteps} steps, "
                   f"E={res['energy']:.12e} rho={res['density']:.12e}")

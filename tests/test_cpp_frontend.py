@@ -17,7 +17,8 @@ REFERENCE = "/root/reference"
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["cavity_bb_lid", "channel_sphere", "guo_channel", "zhpress_faces",
-                                  "incbgk_nodyn", "mebb_walls"])
+                                  "incbgk_nodyn", "mebb_walls", "velocity_box", "velocity_box_noinit",
+                                  "doctest_cavity20"])
 def test_cpp_driver_reproduces_reference_golden(name):
     """Same case file in, same result file out as the reference driver:
     populations bit for bit, reductions to summation rounding."""

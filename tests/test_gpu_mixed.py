@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 # max |f - f_ref| / max |f_ref| after the case's steps
 TOL = {"fp32": 2e-5, "fp16": 1e-2, "bf16": 6e-2, "bf16sr": 6e-2}
 CASES = ["periodic_bgk", "cavity_bb_lid", "channel_sphere", "guo_channel", "regvel_faces",
-         "zhpress_faces", "incbgk_nodyn", "mebb_walls"]
+         "zhpress_faces", "incbgk_nodyn", "mebb_walls", "velocity_box"]
 
 
 @pytest.mark.parametrize("precision", ["fp32", "bf16", "fp16", "bf16sr"])

@@ -23,7 +23,7 @@ def _lat(g, meta, precision="fp64"):
                                     meta.get("bb_rho", 0.0), precision)
 
 
-@pytest.mark.parametrize("name", goldens.case_names())
+@pytest.mark.parametrize("name", [n for n in goldens.case_names() if not n.startswith("external_")])
 def test_fp64_matches_reference(name):
     g, meta = goldens.load(name)
     lat = _lat(g, meta)
@@ -45,7 +45,8 @@ def test_fp64_matches_reference(name):
     assert rho == pytest.approx(float(g["density"]), rel=1e-12, abs=0)
 
 
-@pytest.mark.parametrize("name", ["cavity_bb_lid", "channel_sphere", "regpress_faces", "zhvel_faces"])
+@pytest.mark.parametrize("name", ["cavity_bb_lid", "channel_sphere", "regpress_faces", "zhvel_faces",
+                                  "velocity_box", "doctest_cavity20"])
 def test_initialize_completes_faces_like_reference(name):
     g, meta = goldens.load(name)
     spec = lbcases.case_by_name(name)
@@ -75,6 +76,41 @@ def test_multistep_calls_and_odd_parity_transfers(name):
     lat.send(part, box)   # odd parity: send must invert receive exactly
     lat.collide_and_stream(meta["nsteps"] - k)
     assert np.array_equal(lat.receive(), g["f_final"])
+
+
+def test_velocity_condition_on_block_boundaries_sets_faces_edges_corners():
+    """setVelocityConditionOnBlockBoundaries over a box: the kinds of the
+    reference's instantiation, interior kinds left alone."""
+    from palabos_gb300 import DeviceLattice3D, GUO
+    lat = DeviceLattice3D(11, 10, 9, 1.5)
+    lat.define_dynamics(None, GUO)
+    lat.set_velocity_condition_on_block_boundaries()
+    want = lbcases.velocity_box_kinds((11, 10, 9))
+    want[want == lbcases.BGK] = GUO
+    assert np.array_equal(lat.get_kinds(), want)
+    inner = DeviceLattice3D(12, 12, 12, 1.5)
+    inner.set_velocity_condition_on_block_boundaries((2, 8, 3, 9, 1, 10))
+    k = inner.get_kinds()
+    assert np.array_equal(k[2:9, 3:10, 1:11], lbcases.velocity_box_kinds((7, 7, 10)))
+    assert (k[:2] == 0).all() and (k[9:] == 0).all()
+
+
+def test_edge_without_inward_neighbours_is_reported_not_run():
+    """An edge whose finite differences would leave a non-periodic domain is
+    refused before any kernel reads it; made periodic, the same layout runs."""
+    from palabos_gb300 import DeviceLattice3D, PlbGpuError, edge_kind
+    lat = DeviceLattice3D(6, 6, 6, 1.5)
+    # plane-0 edge with outward normals +y, +z placed at y = z = 0: the inward
+    # neighbours y - 1 and z - 1 lie outside
+    lat.define_dynamics((1, 4, 0, 0, 0, 0), edge_kind(0, 1, 1))
+    with pytest.raises(PlbGpuError) as e:
+        lat.collide_and_stream(1)
+    assert e.value.code == -1 and "edge/corner cell" in str(e.value)
+    with pytest.raises(PlbGpuError):
+        lat.initialize()
+    lat.periodicity(0, 1, 1)
+    lat.collide_and_stream(2)
+    assert np.isfinite(lat.receive()).all()
 
 
 def test_cavity64_full_size_matches_reference_fingerprint():

@@ -18,7 +18,11 @@ import oracle as O
 def test_oracle_matches_reference(name):
     g, meta = goldens.load(name)
     lat = O.OracleLattice.from_golden(g, meta)
-    f, stats = lat.run(g["f_init"], meta["nsteps"])
+    if meta.get("options", 0) & lbcases.OPT_EXTERNAL_RHOJ:
+        f, rb, j, stats = lat.run_external(g["f_init"], g["rho_bar0"], g["j0"], meta["nsteps"])
+        assert np.array_equal(rb, g["rho_bar_final"]) and np.array_equal(j, g["j_final"])
+    else:
+        f, stats = lat.run(g["f_init"], meta["nsteps"])
     ref = g["f_final"]
     assert np.array_equal(f.reshape(ref.shape), ref), \
         f"max |diff| = {np.abs(f.reshape(ref.shape) - ref).max()}"
