@@ -210,6 +210,32 @@ int plbgpu_compute_density(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, 
  * stream (milliseconds). */
 int plbgpu_time_steps(plbgpu_ctx* ctx, int handle, int nsteps, int collect_stats, float* ms);
 
+/* ------------------------------------------------------------ external rho-bar / j */
+
+/* A domain's external moment fields: rho-bar and j (4 values per cell),
+ * FP64 for the FP64 form and FP32 otherwise -- the MultiScalarField3D /
+ * MultiTensorField3D<T,3> pair the reference passes to its processors.
+ * plbgpu_compute_rhobar_j fills them with BoxRhoBarJfunctional3D over the
+ * whole domain (each cell's computeRhoBarJ, dataAnalysisFunctional3D.hh:528-549);
+ * set/get move a box of (rho-bar, jx, jy, jz) per cell, z fastest. */
+int plbgpu_compute_rhobar_j(plbgpu_ctx* ctx, int handle);
+int plbgpu_set_rhobar_j(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1, int z0, int z1,
+                        const double* values, size_t n);
+int plbgpu_get_rhobar_j(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1, int z0, int z1,
+                        double* out, size_t n);
+
+/* nsteps steps of ExternalRhoJcollideAndStream3D (basicDynamics/dynamicsProcessor3D.hh:
+ * 41-200): each cell's collideExternal with rho-bar and j from the fields
+ * instead of its own moments, then streaming, the face completion and the
+ * edge / corner processors.  With recompute non-zero, BoxRhoBarJfunctional3D
+ * refreshes the fields from the streamed populations after every step, before
+ * the boundary processors -- the order of a lattice that integrates the two
+ * processors at levels 0 and 3 and is advanced by executeInternalProcessors().
+ * The BGK-family collisions gather no statistics in this form; the momentum
+ * exchange still does.  PLBGPU_ERR_STATE when the fields were never set. */
+int plbgpu_collide_and_stream_external(plbgpu_ctx* ctx, int handle, int nsteps, int recompute,
+                                       int collect_stats);
+
 /* ------------------------------------------------------------ adjoint */
 
 /* Discrete adjoint of the collide-and-stream step (no counterpart in the

@@ -157,6 +157,22 @@ public:
     void collideAndStream(int steps = 1, bool gatherStatistics = true) {
         ctx_.check(plbgpu_collide_and_stream(ctx_.get(), h_, steps, gatherStatistics));
     }
+    // External rho-bar / j fields and ExternalRhoJcollideAndStream3D steps
+    // (values: rho-bar, jx, jy, jz per cell, z fastest).
+    void computeRhoBarJ() { ctx_.check(plbgpu_compute_rhobar_j(ctx_.get(), h_)); }
+    void setRhoBarJ(const Box& b, const std::vector<double>& values) {
+        ctx_.check(plbgpu_set_rhobar_j(ctx_.get(), h_, b.x0, b.x1, b.y0, b.y1, b.z0, b.z1, values.data(),
+                                       values.size()));
+    }
+    std::vector<double> getRhoBarJ(const Box& b) const {
+        std::vector<double> v((size_t)b.cells() * 4);
+        ctx_.check(plbgpu_get_rhobar_j(ctx_.get(), h_, b.x0, b.x1, b.y0, b.y1, b.z0, b.z1, v.data(), v.size()));
+        return v;
+    }
+    void collideAndStreamExternal(int steps = 1, bool recompute = true, bool gatherStatistics = false) {
+        ctx_.check(plbgpu_collide_and_stream_external(ctx_.get(), h_, steps, recompute, gatherStatistics));
+    }
+
     // getInternalStatistics(): average rho-bar, average u^2, max u^2, drag x/y/z, cell count.
     std::vector<double> internalStatistics() const {
         std::vector<double> s(7);

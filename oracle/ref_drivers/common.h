@@ -58,8 +58,11 @@ enum Kind {
 // Case options (header word 12).
 enum {
     OPT_NO_INITIALIZE = 1,   // skip lattice.initialize() before the first step
-    OPT_EXTERNAL_RHOJ = 2    // step with ExternalRhoJcollideAndStream3D (level 0) and
+    OPT_EXTERNAL_RHOJ = 2,   // step with ExternalRhoJcollideAndStream3D (level 0) and
                              // BoxRhoBarJfunctional3D (level 3) from the given fields
+    OPT_SAVE_BINARY = 4      // after the run, saveBinaryBlock of the lattice, of
+                             // computeDensity and of computeVelocity into
+                             // <result>.lattice / .density / .velocity
 };
 
 struct Case {

@@ -319,6 +319,12 @@ int run(const Case& c, const char* outPath) {
     dumpPopulations(lat, c, fFinal);
     double energy = computeAverageEnergy(lat);
     double density = computeAverageDensity(lat);
+    if (c.options & OPT_SAVE_BINARY) {
+        std::string base(outPath);
+        saveBinaryBlock(lat, base + ".lattice");
+        saveBinaryBlock(*computeDensity(lat), base + ".density");
+        saveBinaryBlock(*computeVelocity(lat), base + ".velocity");
+    }
 
     FILE* f = std::fopen(outPath, "wb");
     if (!f) die("cannot open result file");

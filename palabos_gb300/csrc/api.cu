@@ -36,6 +36,7 @@ struct Domain {
     uint8_t* flags = nullptr;
     double* bc = nullptr;        // 3 * n
     void* force = nullptr;       // 3 * n of FP64 or FP32
+    void* ext = nullptr;         // 4 * n of FP64 or FP32: external rho-bar, jx, jy, jz
     uint32_t* mebb = nullptr;    // n
     int4* surf = nullptr;        // edge cells, then corner cells: (x, y, z, kind)
     int surfCap = 0, nEdges = 0, nCorners = 0;
@@ -61,6 +62,7 @@ struct Domain {
         L.mebb = mebb;
         L.bc = bc;
         L.force = force;
+        L.ext = ext;
         L.nx = nx; L.ny = ny; L.nz = nz;
         L.per[0] = per[0]; L.per[1] = per[1]; L.per[2] = per[2];
         L.n = n;
@@ -374,6 +376,7 @@ StepConsts consts(const Domain* d) {
     s.invRho0 = (double)1 / d->rho0;
     s.pending = d->pending ? 1 : 0;
     s.seed = (unsigned)(d->steps * 0x9E3779B97F4A7C15ull >> 32);
+    s.external = 0;
     return s;
 }
 
@@ -427,6 +430,28 @@ int finishSurface(plbgpu_ctx* c, Domain* d) {
         if ((rc = launchBox(c))) return rc;
     }
     return PLBGPU_OK;
+}
+
+// The external rho-bar / j planes, allocated (zero) on first use.
+int ensureExt(plbgpu_ctx* c, Domain* d) {
+    if (d->ext) return PLBGPU_OK;
+    size_t fs = d->precision == PLBGPU_FP64 ? sizeof(double) : sizeof(float);
+    CUDA_TRY(c, cudaMalloc(&d->ext, fs * 4 * d->n));
+    CUDA_TRY(c, cudaMemsetAsync(d->ext, 0, fs * 4 * d->n, c->stream));
+    d->deviceBytes += fs * 4 * d->n;
+    return PLBGPU_OK;
+}
+
+// Scatter (gather = 0) or gather a packed box of (rho-bar, jx, jy, jz) values.
+int extBox(plbgpu_ctx* c, Domain* d, const Box& b, double* packed, int gather) {
+    dim3 g = rowGrid(b.z1 - b.z0 + 1, b.y1 - b.y0 + 1, b.x1 - b.x0 + 1, 128);
+    if (d->precision == PLBGPU_FP64)
+        boxPlanesKernel<double, double><<<g, 128, 0, c->stream>>>(static_cast<double*>(d->ext), d->n, d->ny, d->nz,
+                                                                   b, packed, 4, gather);
+    else
+        boxPlanesKernel<float, double><<<g, 128, 0, c->stream>>>(static_cast<float*>(d->ext), d->n, d->ny, d->nz, b,
+                                                                  packed, 4, gather);
+    return launchBox(c);
 }
 
 }  // namespace
@@ -565,6 +590,7 @@ int plbgpu_remove_domain(plbgpu_ctx* c, int h) {
     cudaFree(d->arena);
     if (d->bc) cudaFree(d->bc);
     if (d->force) cudaFree(d->force);
+    if (d->ext) cudaFree(d->ext);
     if (d->mebb) cudaFree(d->mebb);
     if (d->surf) cudaFree(d->surf);
     cudaFree(d->stats);
@@ -974,6 +1000,86 @@ int plbgpu_compute_velocity(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1
 int plbgpu_compute_density(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, double* out,
                            size_t n) {
     return field(c, h, x0, x1, y0, y1, z0, z1, 1, out, n);
+}
+
+int plbgpu_compute_rhobar_j(plbgpu_ctx* c, int h) {
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if ((rc = ensureExt(c, d))) return rc;
+    int n = launchers(d->precision).rhoBarJ(d->view(), d->odd, d->pending && d->bc ? 1 : 0, d->bbRho, c->stream);
+    c->launches += n - 1;
+    return launchBox(c);
+}
+
+int plbgpu_set_rhobar_j(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, const double* values,
+                        size_t n) {
+    Domain* d;
+    Box b;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if ((rc = checkBox(c, d, x0, x1, y0, y1, z0, z1, &b))) return rc;
+    long long cells = boxCells(b);
+    if (!values || (long long)n != 4 * cells)
+        return fail(c, PLBGPU_ERR_ARG, "rho-bar/j: %zu values for %lld cells (4 per cell)", n, cells);
+    if ((rc = ensureExt(c, d))) return rc;
+    if ((rc = ensureStaging(c, sizeof(double) * n))) return rc;
+    CUDA_TRY(c, cudaMemcpyAsync(c->staging, values, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    if ((rc = extBox(c, d, b, static_cast<double*>(c->staging), 0))) return rc;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return PLBGPU_OK;
+}
+
+int plbgpu_get_rhobar_j(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, double* out,
+                        size_t n) {
+    Domain* d;
+    Box b;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if ((rc = checkBox(c, d, x0, x1, y0, y1, z0, z1, &b))) return rc;
+    long long cells = boxCells(b);
+    if (!out || (long long)n != 4 * cells)
+        return fail(c, PLBGPU_ERR_ARG, "rho-bar/j: %zu values for %lld cells (4 per cell)", n, cells);
+    if (!d->ext) return fail(c, PLBGPU_ERR_STATE, "no rho-bar/j fields yet");
+    if ((rc = ensureStaging(c, sizeof(double) * n))) return rc;
+    if ((rc = extBox(c, d, b, static_cast<double*>(c->staging), 1))) return rc;
+    CUDA_TRY(c, cudaMemcpyAsync(out, c->staging, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return PLBGPU_OK;
+}
+
+int plbgpu_collide_and_stream_external(plbgpu_ctx* c, int h, int nsteps, int recompute, int collect_stats) {
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if (nsteps < 0) return fail(c, PLBGPU_ERR_ARG, "nsteps %d", nsteps);
+    if (!d->ext)
+        return fail(c, PLBGPU_ERR_STATE,
+                    "no rho-bar/j fields: call plbgpu_compute_rhobar_j or plbgpu_set_rhobar_j first");
+    if (nsteps == 0) return PLBGPU_OK;
+    const Launchers& L = launchers(d->precision);
+    bool hasFaces = d->bc != nullptr;
+    if (d->surfDirty && (rc = buildSurface(c, d))) return rc;
+    for (int s = 0; s < nsteps; ++s) {
+        bool stats = collect_stats && s == nsteps - 1;
+        if (stats) CUDA_TRY(c, cudaMemsetAsync(d->stats, 0, sizeof(StatsAcc), c->stream));
+        StepConsts k = consts(d);
+        k.external = 1;
+        int nl = L.step(d->view(), d->odd, stats, k, d->stats, c->stream);
+        c->launches += nl - 1;
+        if ((rc = launchBox(c))) return rc;
+        d->odd = !d->odd;
+        d->pending = hasFaces;
+        d->steps += 1;
+        if (recompute) {   // the streamed state, before the boundary processors
+            nl = L.rhoBarJ(d->view(), d->odd, 0, d->bbRho, c->stream);
+            c->launches += nl - 1;
+            if ((rc = launchBox(c))) return rc;
+        }
+        if ((rc = finishSurface(c, d))) return rc;
+    }
+    if (collect_stats) d->statsValid = true;
+    return PLBGPU_OK;
 }
 
 int plbgpu_time_steps(plbgpu_ctx* c, int h, int nsteps, int collect_stats, float* ms) {

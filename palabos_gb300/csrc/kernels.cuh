@@ -123,6 +123,7 @@ struct DevLattice {
     const uint32_t* mebb;   // n, fluid-direction masks of momentum-exchange cells (or null)
     const double* bc;       // 3 planes of n: face velocity / density (or null)
     const void* force;      // 3 planes of n: Guo force in F (or null)
+    const void* ext;        // 4 planes of n in F: external rho-bar, jx, jy, jz (or null)
     int nx, ny, nz;
     int per[3];
     long long n;
@@ -135,6 +136,7 @@ struct StepParams {
     R invRho0;      // incompressible BGK 1/rho0
     int pending;    // boundary faces still need their post-stream completion
     unsigned seed;  // per-step salt of the stochastically rounded storage
+    int external;   // collide with rho-bar and j from L.ext (collideExternal)
 };
 
 struct StatsAcc {
@@ -285,6 +287,36 @@ __device__ __forceinline__ bool collideCell(const DevLattice& L, const StepParam
     using R = typename StoreT<S>::R;
     using F = typename StoreT<S>::F;
     R j[3];
+    if (P.external) {
+        // ExternalRhoJcollideAndStream3D (dynamicsProcessor3D.hh:41-56):
+        // Dynamics::collideExternal with the fields' rho-bar and j.  BGK (and
+        // the BGK base of boundary cells) and IncBGK collide on the given
+        // moments and gather no statistics (isoThermalDynamics.hh:333-338,
+        // 1422-1427); Guo-forced BGK shifts every population by the change of
+        // equilibrium, then collides as usual (core/dynamics.hh:131-145);
+        // bounce-back, momentum exchange and no-dynamics are unchanged.
+        const F* e = static_cast<const F*>(L.ext);
+        const R rbE = (R)e[idx];
+        const R jE[3] = {(R)e[L.n + idx], (R)e[2 * L.n + idx], (R)e[3 * L.n + idx]};
+        if (bgkBase(k) || k == K_INCBGK) {
+            uSqr = bgkCollide<R>(f, rbE, jE, P.bgk, k == K_INCBGK ? P.invRho0 : invRhoOf(rbE));
+            rhoBar = rbE;
+            return false;
+        }
+        if (k == K_GUO) {
+            R oldRb, oldJ[3];
+            rhoBarJ<R>(f, oldRb, oldJ);
+            const R oldJsqr = oldJ[0] * oldJ[0] + oldJ[1] * oldJ[1] + oldJ[2] * oldJ[2];
+            const R jSqr = jE[0] * jE[0] + jE[1] * jE[1] + jE[2] * jE[2];
+            const R oldInv = invRhoOf(oldRb), newInv = invRhoOf(rbE);
+#pragma unroll
+            for (int i = 0; i < 19; ++i) {
+                const R oldEq = bgkEq<R>(i, oldRb, oldInv, oldJ, oldJsqr);
+                const R newEq = bgkEq<R>(i, rbE, newInv, jE, jSqr);
+                f[i] += newEq - oldEq;
+            }
+        }
+    }
     if (bgkBase(k)) {
         // isoThermalDynamics.hh:319-330; faces, edges and corners use their
         // BGK base collide.
@@ -920,6 +952,58 @@ __global__ void surfaceKernel(DevLattice L, const int4* __restrict__ cells, int 
     S* Pp = static_cast<S*>(L.pop);
 #pragma unroll
     for (int i = 0; i < 19; ++i) StoreT<S>::st(Pp + slotOf<ODD>(L, nb, idx, i), f[i]);
+}
+
+// BoxRhoBarJfunctional3D (dataAnalysisFunctional3D.hh:528-549): each cell's
+// Dynamics::computeRhoBarJ into the external-field planes (rho-bar, jx, jy,
+// jz).  pending = 0 reads boundary faces as streamed (the functional running
+// at a later processor level than the face completion); pending = 1 reads the
+// completed state.
+template <typename S, bool ODD>
+__global__ void rhoBarJKernel(DevLattice L, int pending, double bbRho, typename StoreT<S>::F* out) {
+    using R = typename StoreT<S>::R;
+    const int z = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, x = blockIdx.z;
+    if (z >= L.nz) return;
+    const long long idx = ((long long)x * L.ny + y) * L.nz + z;
+    const int k = L.flags[idx];
+    if (k == K_NONE) return;
+    R rb = R(0), j[3] = {R(0), R(0), R(0)};
+    if (k == K_BB || k == K_MEBB) {  // core/dynamics.hh:880-885, bounceBackModels.hh:226-231
+        rb = (R)bbRho - (R)1;
+    } else if (k == K_NODYN) {       // core/dynamics.hh:1061-1066
+        rb = (R)1 - (R)1;
+    } else {
+        Neighbourhood nb = neighbourhood(L, x, y, z);
+        const S* Pp = static_cast<const S*>(L.pop);
+        R f[19];
+#pragma unroll
+        for (int i = 0; i < 19; ++i) f[i] = StoreT<S>::ld(Pp + slotOf<ODD>(L, nb, idx, i));
+        if (pending && isFace(k)) completeIfFace<R>(L, idx, k, f);
+        if (k == K_BGK || k == K_GUO || k == K_INCBGK) {  // core/dynamics.hh:357-361
+            rhoBarJ<R>(f, rb, j);
+        } else if (isSurface(k)) {   // boundaryDynamics.hh:348-360
+            const R rho = rhoBarSeq<R>(f) + (R)1;
+            rb = rho - (R)1;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) j[d] = rho * ((R)L.bc[d * L.n + idx] - (R)0.5 * (R)0);
+        } else {                     // faces: boundaryDynamics.hh:682-702, 815-822
+            const int fam = faceFamily(k), dir = faceDir(k);
+            if (fam == 0 || fam == 2) {
+                rb = velFaceRhoBarAny<R>(f, k, (R)L.bc[dir * L.n + idx]);
+                const R rho = rb + (R)1;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) j[d] = rho * ((R)L.bc[d * L.n + idx] - (R)0.5 * (R)0);
+            } else {
+                rb = (R)L.bc[idx] - (R)1;
+                pressFaceJAny<R>(f, k, rb, j);
+            }
+        }
+    }
+    out[idx] = rb;
+    out[L.n + idx] = j[0];
+    out[2 * L.n + idx] = j[1];
+    out[3 * L.n + idx] = j[2];
 }
 
 // computeAverageEnergy / computeAverageDensity (dataAnalysisWrapper3D.hh:1226-1262).

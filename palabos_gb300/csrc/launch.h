@@ -15,6 +15,7 @@ struct StepConsts {
     double invRho0;
     int pending;
     unsigned seed;
+    int external;   // collide with the external rho-bar / j planes (DevLattice::ext)
 };
 
 // Each launcher returns the number of kernels it launched.
@@ -29,6 +30,8 @@ struct Launchers {
                        double invRho0, cudaStream_t);
     int (*field)(const DevLattice&, bool odd, Box, int pending, double invRho0, double bbRho, int what,
                  double* out, cudaStream_t);
+    // BoxRhoBarJfunctional3D into the external planes (DevLattice::ext).
+    int (*rhoBarJ)(const DevLattice&, bool odd, int pending, double bbRho, cudaStream_t);
     // Edge or corner cells (x, y, z, kind) finished after a step.
     int (*surface)(const DevLattice&, bool odd, const int4* cells, int count, int pending, double invRho0,
                    double bbRho, double omega, cudaStream_t);

@@ -64,6 +64,7 @@ struct LaunchImpl {
         p.invRho0 = (R)c.invRho0;
         p.pending = c.pending;
         p.seed = c.seed;
+        p.external = c.external;
         return odd ? stepParity<S, true>(L, stats, p, acc, s) : stepParity<S, false>(L, stats, p, acc, s);
     }
     static int completeFaces(const DevLattice& L, bool odd, cudaStream_t s) {
@@ -107,6 +108,14 @@ struct LaunchImpl {
             equilibriumKernel<S, false><<<g, kBlock, 0, s>>>(L, b, rhou, cst[0], cst[1], cst[2], cst[3], invRho0);
         return 1;
     }
+    static int rhoBarJ(const DevLattice& L, bool odd, int pending, double bbRho, cudaStream_t s) {
+        using F = typename StoreT<S>::F;
+        F* out = static_cast<F*>(const_cast<void*>(L.ext));
+        dim3 g = rowGrid(L.nz, L.ny, L.nx, kBlock);
+        if (odd) rhoBarJKernel<S, true><<<g, kBlock, 0, s>>>(L, pending, bbRho, out);
+        else rhoBarJKernel<S, false><<<g, kBlock, 0, s>>>(L, pending, bbRho, out);
+        return 1;
+    }
     static int surface(const DevLattice& L, bool odd, const int4* cells, int count, int pending, double invRho0,
                        double bbRho, double omega, cudaStream_t s) {
         if (count <= 0) return 0;
@@ -118,7 +127,8 @@ struct LaunchImpl {
         return 1;
     }
     static const Launchers& table() {
-        static const Launchers t = {step, completeFaces, extract, insert, reduce, equilibrium, field, surface};
+        static const Launchers t = {step,  completeFaces, extract, insert, reduce,
+                                    equilibrium, field, rhoBarJ, surface};
         return t;
     }
 };

@@ -210,6 +210,34 @@ class DeviceLattice3D:
     def collide_and_stream(self, nsteps=1, stats=False):
         self._check(self.lib.plbgpu_collide_and_stream(self.ctx.h, self.handle, int(nsteps), int(bool(stats))))
 
+    def compute_rhobar_j(self):
+        """BoxRhoBarJfunctional3D over the domain into the external fields."""
+        self._check(self.lib.plbgpu_compute_rhobar_j(self.ctx.h, self.handle))
+
+    def set_rhobar_j(self, rho_bar, j, box=None):
+        """External fields over a box: rho_bar (cells), j (cells x 3)."""
+        box = self._box(box)
+        n = self._cells(box)
+        v = np.empty((n, 4))
+        v[:, 0] = np.asarray(rho_bar, np.float64).reshape(n)
+        v[:, 1:] = np.asarray(j, np.float64).reshape(n, 3)
+        self._check(self.lib.plbgpu_set_rhobar_j(self.ctx.h, self.handle, *box, _dp(v), v.size))
+
+    def get_rhobar_j(self, box=None):
+        """(rho_bar [x][y][z], j [x][y][z][3]) of the external fields."""
+        box = self._box(box)
+        n = self._cells(box)
+        v = np.empty((n, 4))
+        self._check(self.lib.plbgpu_get_rhobar_j(self.ctx.h, self.handle, *box, _dp(v), v.size))
+        shape = (box[1] - box[0] + 1, box[3] - box[2] + 1, box[5] - box[4] + 1)
+        return v[:, 0].reshape(shape), v[:, 1:].reshape(shape + (3,))
+
+    def collide_and_stream_external(self, nsteps=1, recompute=True, stats=False):
+        """ExternalRhoJcollideAndStream3D steps (with BoxRhoBarJfunctional3D
+        after each when recompute)."""
+        self._check(self.lib.plbgpu_collide_and_stream_external(self.ctx.h, self.handle, int(nsteps),
+                                                                int(bool(recompute)), int(bool(stats))))
+
     def time_steps(self, nsteps, stats=False) -> float:
         ms = ctypes.c_float()
         self._check(self.lib.plbgpu_time_steps(self.ctx.h, self.handle, int(nsteps), int(bool(stats)),

@@ -74,6 +74,10 @@ SIGNATURES = {
     "plbgpu_set_kinds": [_vp, _i, *BOX, _c_u8_p, _sz],
     "plbgpu_get_kinds": [_vp, _i, *BOX, _c_u8_p, _sz],
     "plbgpu_set_velocity_condition_on_block_boundaries": [_vp, _i, *BOX],
+    "plbgpu_compute_rhobar_j": [_vp, _i],
+    "plbgpu_set_rhobar_j": [_vp, _i, *BOX, _c_dbl_p, _sz],
+    "plbgpu_get_rhobar_j": [_vp, _i, *BOX, _c_dbl_p, _sz],
+    "plbgpu_collide_and_stream_external": [_vp, _i, _i, _i, _i],
     "plbgpu_set_boundary_velocity": [_vp, _i, *BOX, _d, _d, _d],
     "plbgpu_set_boundary_velocity_field": [_vp, _i, *BOX, _c_dbl_p, _sz],
     "plbgpu_set_boundary_density": [_vp, _i, *BOX, _d],

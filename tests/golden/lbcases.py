@@ -39,6 +39,7 @@ REGVEL, REGPRESS, ZHVEL, ZHPRESS = 6, 12, 18, 24
 EDGE, CORNER = 30, 42
 OPT_NO_INITIALIZE = 1
 OPT_EXTERNAL_RHOJ = 2
+OPT_SAVE_BINARY = 4
 
 
 def face_kind(family: int, direction: int, orientation: int) -> int:
@@ -426,6 +427,26 @@ def case_external_mebb_periodic():
     return with_external(s, "external_mebb_periodic", 204)
 
 
+def case_binary_channel_sphere():
+    """channel_sphere, then saveBinaryBlock of the lattice, its density and its
+    velocity (io/serializerIO_3D.cpp:37-49)."""
+    s = case_channel_sphere()
+    s.name = "binary_channel_sphere"
+    s.nsteps = 10
+    s.options |= OPT_SAVE_BINARY
+    return s
+
+
+def case_binary_guo_periodic():
+    """Forced descriptor: every serialized cell carries the force after its
+    19 populations."""
+    s = case_guo_periodic_multiblock()
+    s.name = "binary_guo_periodic_multiblock"
+    s.nsteps = 5
+    s.options |= OPT_SAVE_BINARY
+    return s
+
+
 def case_doctest_cavity20():
     return doctest_cavity(20, 20, 20, name="doctest_cavity20")
 
@@ -448,7 +469,7 @@ CASES = [
     case_zhpress_faces, case_incbgk_nodyn, case_mebb_walls, case_velocity_box,
     case_velocity_box_multiblock, case_velocity_box_noinit, case_doctest_cavity20,
     case_external_periodic_bgk, case_external_incbgk_nodyn, case_external_guo_periodic,
-    case_external_mebb_periodic,
+    case_external_mebb_periodic, case_binary_channel_sphere, case_binary_guo_periodic,
 ]
 
 
@@ -518,4 +539,8 @@ def read_result_file(path: str, spec: CaseSpec):
         out["rho_bar_final"] = np.frombuffer(data, np.float64, m, off).reshape(nx, ny, nz).copy()
         off += 8 * m
         out["j_final"] = np.frombuffer(data, np.float64, 3 * m, off).reshape(nx, ny, nz, 3).copy()
+    if spec.options & OPT_SAVE_BINARY:
+        for what in ("lattice", "density", "velocity"):
+            with open(path + "." + what, "rb") as f:
+                out["binary_" + what] = np.frombuffer(f.read(), np.uint8).copy()
     return out

@@ -67,6 +67,9 @@ def main(argv):
             if spec.rho_bar0 is not None:
                 extra = dict(rho_bar0=spec.rho_bar0, j0=spec.j0, rho_bar_final=res["rho_bar_final"],
                              j_final=res["j_final"])
+            for what in ("lattice", "density", "velocity"):
+                if "binary_" + what in res:
+                    extra["binary_" + what] = res["binary_" + what]
             np.savez_compressed(
                 os.path.join(HERE, spec.name + ".npz"),
                 flags=spec.flags, bcval=spec.bcval, force=spec.force,

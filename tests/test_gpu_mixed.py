@@ -40,6 +40,24 @@ def test_reduced_precision_tracks_reference(name, precision):
     assert e == pytest.approx(float(g["energy"]), rel=50 * TOL[precision])
 
 
+@pytest.mark.parametrize("precision", ["fp32", "bf16", "fp16"])
+@pytest.mark.parametrize("name", ["external_periodic_bgk", "external_mebb_periodic"])
+def test_reduced_precision_external_form(name, precision):
+    """The external rho-bar/j form in the reduced storage forms (fields in
+    FP32) against the reference's FP64 result."""
+    g, meta = goldens.load(name)
+    lat = lattice_from_description(meta["nx"], meta["ny"], meta["nz"], meta["periodic"], meta["omega"],
+                                   g["flags"], g["bcval"], g["force"], meta.get("rho0", 1.0),
+                                   meta.get("bb_rho", 0.0), precision)
+    lat.send(g["f_init"])
+    lat.set_rhobar_j(g["rho_bar0"], g["j0"])
+    lat.collide_and_stream_external(meta["nsteps"], recompute=True)
+    f = lat.receive()
+    ref = g["f_final"]
+    err = np.abs(f - ref).max() / np.abs(ref).max()
+    assert err < TOL[precision], err
+
+
 @pytest.mark.parametrize("precision", ["fp32", "bf16"])
 def test_staged_rows_match_unstaged_geometry(precision):
     """nz a multiple of the 16-byte copy granule (staged row kernel) and nz odd
