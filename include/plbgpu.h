@@ -236,6 +236,31 @@ int plbgpu_get_rhobar_j(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int
 int plbgpu_collide_and_stream_external(plbgpu_ctx* ctx, int handle, int nsteps, int recompute,
                                        int collect_stats);
 
+/* ------------------------------------------------------------ checkpoints */
+
+/* Block kinds of saveBinaryBlock / loadBinaryBlock (io/serializerIO_3D.cpp:37-66):
+ * the values per cell are the ones Block3D serialization writes -- the 19
+ * populations (f-bar) and, for the forced descriptor, the 3 force components
+ * after them (core/cell.hh:103-110); computeDensity / computeVelocity fields;
+ * the external rho-bar / j fields. */
+#define PLBGPU_BLOCK_LATTICE 0          /* D3Q19 lattice: 19 doubles per cell */
+#define PLBGPU_BLOCK_FORCED_LATTICE 1   /* ForcedD3Q19 lattice: 19 + 3 doubles per cell */
+#define PLBGPU_BLOCK_DENSITY 2          /* computeDensity field: 1 double per cell (save only) */
+#define PLBGPU_BLOCK_VELOCITY 3         /* computeVelocity field: 3 doubles per cell (save only) */
+#define PLBGPU_BLOCK_RHOBAR 4           /* external rho-bar field: 1 double per cell */
+#define PLBGPU_BLOCK_J 5                /* external j field: 3 doubles per cell */
+
+/* saveBinaryBlock(block, path, enforce_uint) / loadBinaryBlock: the file is
+ * base64 text -- the byte count (8 bytes, or 4 with enforce_uint), then the
+ * cell records x-major, z fastest, as the reference's default stream ordering
+ * writes them (io/serializerIO.cpp:64-115, multiBlock/multiBlockSerializer3D.cpp:
+ * 61-129).  The records are assembled and encoded (decoded) on the device in
+ * slabs of whole x-planes; only the text crosses to the host.  A file whose
+ * byte count does not match the domain, or that is not base64, is refused
+ * (PLBGPU_ERR_ARG). */
+int plbgpu_save_binary_block(plbgpu_ctx* ctx, int handle, int what, const char* path, int enforce_uint);
+int plbgpu_load_binary_block(plbgpu_ctx* ctx, int handle, int what, const char* path, int enforce_uint);
+
 /* ------------------------------------------------------------ adjoint */
 
 /* Discrete adjoint of the collide-and-stream step (no counterpart in the

@@ -149,3 +149,18 @@ def set_threads(n: int):
 
 def max_threads() -> int:
     return int(lib().orc_max_threads())
+
+
+def binary_block(records, enforce_uint=False):
+    """saveBinaryBlock's byte stream for a block whose cells serialize to
+    `records` (float64, cells in x-major order, z fastest, the values of one
+    cell contiguous): the byte count (uint64, or uint32 with enforce_uint) and
+    the data, each base64-encoded on its own with '=' padding and no line
+    breaks (io/serializerIO_3D.cpp:37-49, io/serializerIO.cpp:64-86,
+    io/base64.hh:35-115, multiBlock/multiBlockSerializer3D.cpp:61-129)."""
+    import base64
+    import struct
+    data = np.ascontiguousarray(records, dtype="<f8").tobytes()
+    head = struct.pack("<I" if enforce_uint else "<Q", len(data))
+    return base64.b64encode(head) + base64.b64encode(data)
+

@@ -1104,6 +1104,261 @@ int plbgpu_time_steps(plbgpu_ctx* c, int h, int nsteps, int collect_stats, float
     return checkStatus(c, d);
 }
 
+
+// ------------------------------------------------------------ binary-block checkpoints
+
+namespace {
+
+// Values per cell of each block kind (sizeOfCell / sizeof(T): the populations
+// and the external scalars of the descriptor, or the field's components).
+int blockWidth(int what) {
+    switch (what) {
+    case PLBGPU_BLOCK_LATTICE: return 19;
+    case PLBGPU_BLOCK_FORCED_LATTICE: return 22;
+    case PLBGPU_BLOCK_DENSITY: return 1;
+    case PLBGPU_BLOCK_VELOCITY: return 3;
+    case PLBGPU_BLOCK_RHOBAR: return 1;
+    case PLBGPU_BLOCK_J: return 3;
+    default: return 0;
+    }
+}
+
+void hostBase64(const unsigned char* in, size_t n, std::string& out) {
+    static const char a[] = "ABCDEFGHIJKLMNOPQRSTUVWXYZabcdefghijklmnopqrstuvwxyz0123456789+/";
+    for (size_t i = 0; i < n; i += 3) {
+        unsigned b0 = in[i], b1 = i + 1 < n ? in[i + 1] : 0u, b2 = i + 2 < n ? in[i + 2] : 0u;
+        out += a[b0 >> 2];
+        out += a[((b0 & 3u) << 4) | (b1 >> 4)];
+        out += i + 1 < n ? a[((b1 & 15u) << 2) | (b2 >> 6)] : '=';
+        out += i + 2 < n ? a[b2 & 63u] : '=';
+    }
+}
+
+// Device buffers of one save / load, freed on every exit path.
+struct Ckpt {
+    double* rec = nullptr;     // records of one slab
+    double* tmp = nullptr;     // gathered columns
+    uint8_t* bytes = nullptr;  // decoded bytes of one slab (+ the partial quads around it)
+    char* text = nullptr;      // base64 of one slab
+    uint8_t* head = nullptr;   // up to two bytes carried to the next slab
+    unsigned* bad = nullptr;
+    ~Ckpt() {
+        cudaFree(rec); cudaFree(tmp); cudaFree(bytes); cudaFree(text); cudaFree(head); cudaFree(bad);
+    }
+};
+
+struct FileCloser {
+    FILE* f;
+    ~FileCloser() { if (f) fclose(f); }
+};
+
+int ckptAlloc(plbgpu_ctx* c, Ckpt& k, long long cells, int w) {
+    const size_t recBytes = (size_t)cells * w * sizeof(double);
+    CUDA_TRY(c, cudaMalloc(&k.rec, recBytes));
+    CUDA_TRY(c, cudaMalloc(&k.tmp, (size_t)cells * 19 * sizeof(double)));
+    CUDA_TRY(c, cudaMalloc(&k.bytes, recBytes + 8));
+    CUDA_TRY(c, cudaMalloc(&k.text, 4 * ((recBytes + 2) / 3 + 2)));
+    CUDA_TRY(c, cudaMalloc(&k.head, 4));
+    CUDA_TRY(c, cudaMalloc(&k.bad, sizeof(unsigned)));
+    CUDA_TRY(c, cudaMemsetAsync(k.bad, 0, sizeof(unsigned), c->stream));
+    return PLBGPU_OK;
+}
+
+// Whole x-planes per slab: about 32 MB of records, at least one plane.
+int slabPlanes(const Domain* d, int w) {
+    long long plane = (long long)d->ny * d->nz * w * (long long)sizeof(double);
+    long long p = (32ll << 20) / (plane > 0 ? plane : 1);
+    return (int)(p < 1 ? 1 : (p > d->nx ? d->nx : p));
+}
+
+}  // namespace
+
+int plbgpu_save_binary_block(plbgpu_ctx* c, int h, int what, const char* path, int enforce_uint) {
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    const int w = blockWidth(what);
+    if (!w) return fail(c, PLBGPU_ERR_ARG, "unknown block kind %d", what);
+    if (!path) return fail(c, PLBGPU_ERR_ARG, "null path");
+    if ((what == PLBGPU_BLOCK_RHOBAR || what == PLBGPU_BLOCK_J) && !d->ext)
+        return fail(c, PLBGPU_ERR_STATE, "no rho-bar/j fields to save");
+    if ((rc = checkStatus(c, d))) return rc;
+    FileCloser fc{fopen(path, "wb")};
+    if (!fc.f) return fail(c, PLBGPU_ERR_ARG, "cannot open %s for writing", path);
+    // Size header, encoded on its own (io/serializerIO.cpp:64-80).
+    const unsigned long long size = (unsigned long long)d->n * w * sizeof(double);
+    std::string hdr;
+    if (enforce_uint) {
+        if (size > 0xffffffffull) return fail(c, PLBGPU_ERR_ARG, "%llu bytes do not fit a 32-bit header", size);
+        unsigned u = (unsigned)size;
+        hostBase64(reinterpret_cast<const unsigned char*>(&u), sizeof(u), hdr);
+    } else {
+        hostBase64(reinterpret_cast<const unsigned char*>(&size), sizeof(size), hdr);
+    }
+    if (fwrite(hdr.data(), 1, hdr.size(), fc.f) != hdr.size()) return fail(c, PLBGPU_ERR_ARG, "write to %s failed", path);
+    const int planes = slabPlanes(d, w);
+    Ckpt k;
+    if ((rc = ckptAlloc(c, k, (long long)planes * d->ny * d->nz, w))) return rc;
+    std::vector<char> text;
+    const Launchers& L = launchers(d->precision);
+    const int pending = d->pending && d->bc ? 1 : 0;
+    int headLen = 0;
+    for (int x0 = 0; x0 < d->nx; x0 += planes) {
+        const int x1 = x0 + planes - 1 < d->nx - 1 ? x0 + planes - 1 : d->nx - 1;
+        Box b{x0, x1, 0, d->ny - 1, 0, d->nz - 1};
+        const long long cells = boxCells(b);
+        int nl = 1;
+        if (what == PLBGPU_BLOCK_LATTICE) {
+            nl = L.extract(d->view(), d->odd, b, pending, k.rec, c->stream);
+        } else if (what == PLBGPU_BLOCK_FORCED_LATTICE) {
+            nl = L.extract(d->view(), d->odd, b, pending, k.tmp, c->stream);
+            launchColumns(k.tmp, 19, 0, 19, k.rec, 22, 0, cells, c->stream);
+            dim3 g = rowGrid(d->nz, d->ny, x1 - x0 + 1, 128);
+            if (!d->force)
+                CUDA_TRY(c, cudaMemsetAsync(k.tmp, 0, sizeof(double) * 3 * cells, c->stream));
+            else if (d->precision == PLBGPU_FP64)
+                boxPlanesKernel<double, double><<<g, 128, 0, c->stream>>>(static_cast<double*>(d->force), d->n, d->ny,
+                                                                          d->nz, b, k.tmp, 3, 1);
+            else
+                boxPlanesKernel<float, double><<<g, 128, 0, c->stream>>>(static_cast<float*>(d->force), d->n, d->ny,
+                                                                         d->nz, b, k.tmp, 3, 1);
+            launchColumns(k.tmp, 3, 0, 3, k.rec, 22, 19, cells, c->stream);
+            nl = 4;
+        } else if (what == PLBGPU_BLOCK_DENSITY || what == PLBGPU_BLOCK_VELOCITY) {
+            nl = L.field(d->view(), d->odd, b, pending, (double)1 / d->rho0, d->bbRho,
+                         what == PLBGPU_BLOCK_DENSITY ? 1 : 0, k.rec, c->stream);
+        } else {
+            if ((rc = extBox(c, d, b, k.tmp, 1))) return rc;
+            launchColumns(k.tmp, 4, what == PLBGPU_BLOCK_RHOBAR ? 0 : 1, w, k.rec, w, 0, cells, c->stream);
+            nl = 1;
+        }
+        c->launches += nl - 1;
+        if ((rc = launchBox(c))) return rc;
+        const size_t bodyLen = (size_t)cells * w * sizeof(double);
+        const size_t total = (size_t)headLen + bodyLen;
+        const bool last = x1 == d->nx - 1;
+        const size_t quads = last ? (total + 2) / 3 : total / 3;
+        launchBase64Encode(k.head, headLen, reinterpret_cast<const uint8_t*>(k.rec), bodyLen, quads, k.text,
+                           c->stream);
+        if ((rc = launchBox(c))) return rc;
+        const int carry = last ? 0 : (int)(total - 3 * quads);
+        if (carry)
+            CUDA_TRY(c, cudaMemcpyAsync(k.head, reinterpret_cast<const uint8_t*>(k.rec) + bodyLen - carry, carry,
+                                        cudaMemcpyDeviceToDevice, c->stream));
+        headLen = carry;
+        text.resize(4 * quads);
+        CUDA_TRY(c, cudaMemcpyAsync(text.data(), k.text, text.size(), cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+        if (fwrite(text.data(), 1, text.size(), fc.f) != text.size())
+            return fail(c, PLBGPU_ERR_ARG, "write to %s failed", path);
+    }
+    if (fflush(fc.f) != 0) return fail(c, PLBGPU_ERR_ARG, "write to %s failed", path);
+    return PLBGPU_OK;
+}
+
+int plbgpu_load_binary_block(plbgpu_ctx* c, int h, int what, const char* path, int enforce_uint) {
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    const int w = blockWidth(what);
+    if (!w) return fail(c, PLBGPU_ERR_ARG, "unknown block kind %d", what);
+    if (what == PLBGPU_BLOCK_DENSITY || what == PLBGPU_BLOCK_VELOCITY)
+        return fail(c, PLBGPU_ERR_ARG, "density and velocity blocks are derived data and cannot be loaded");
+    if (!path) return fail(c, PLBGPU_ERR_ARG, "null path");
+    FileCloser fc{fopen(path, "rb")};
+    if (!fc.f) return fail(c, PLBGPU_ERR_ARG, "cannot open %s", path);
+    const long hdrChars = enforce_uint ? 8 : 12;
+    char hdr[12];
+    if (fread(hdr, 1, hdrChars, fc.f) != (size_t)hdrChars) return fail(c, PLBGPU_ERR_ARG, "%s: short header", path);
+    unsigned long long size = 0;
+    {
+        unsigned char raw[9] = {0};
+        for (long q = 0; q < hdrChars / 4; ++q) {
+            unsigned v[4];
+            for (int i = 0; i < 4; ++i) {
+                unsigned char ch = (unsigned char)hdr[4 * q + i];
+                v[i] = ch >= 'A' && ch <= 'Z' ? ch - 'A' : ch >= 'a' && ch <= 'z' ? ch - 'a' + 26
+                     : ch >= '0' && ch <= '9' ? ch - '0' + 52 : ch == '+' ? 62u : ch == '/' ? 63u : 0u;
+            }
+            unsigned char b[3] = {(unsigned char)((v[0] << 2) | (v[1] >> 4)),
+                                  (unsigned char)(((v[1] & 15u) << 4) | (v[2] >> 2)),
+                                  (unsigned char)(((v[2] & 3u) << 6) | v[3])};
+            for (int i = 0; i < 3 && 3 * q + i < 9; ++i) raw[3 * q + i] = b[i];
+        }
+        if (enforce_uint) {
+            unsigned u;
+            memcpy(&u, raw, 4);
+            size = u;
+        } else {
+            memcpy(&size, raw, 8);
+        }
+    }
+    const unsigned long long want = (unsigned long long)d->n * w * sizeof(double);
+    if (size != want)
+        return fail(c, PLBGPU_ERR_ARG, "%s holds %llu bytes, the %dx%dx%d domain needs %llu", path, size, d->nx, d->ny,
+                    d->nz, want);
+    if ((rc = materialize(c, d))) return rc;
+    if (what == PLBGPU_BLOCK_FORCED_LATTICE && (rc = ensureAux(c, d, false, true, false))) return rc;
+    if ((what == PLBGPU_BLOCK_RHOBAR || what == PLBGPU_BLOCK_J) && (rc = ensureExt(c, d))) return rc;
+    const int planes = slabPlanes(d, w);
+    Ckpt k;
+    if ((rc = ckptAlloc(c, k, (long long)planes * d->ny * d->nz, w))) return rc;
+    const Launchers& L = launchers(d->precision);
+    const unsigned long long totalQuads = (size + 2) / 3;
+    std::vector<char> text;
+    for (int x0 = 0; x0 < d->nx; x0 += planes) {
+        const int x1 = x0 + planes - 1 < d->nx - 1 ? x0 + planes - 1 : d->nx - 1;
+        Box b{x0, x1, 0, d->ny - 1, 0, d->nz - 1};
+        const long long cells = boxCells(b);
+        const unsigned long long start = (unsigned long long)x0 * d->ny * d->nz * w * sizeof(double);
+        const unsigned long long end = start + (unsigned long long)cells * w * sizeof(double);
+        const unsigned long long q0 = start / 3, q1 = (end + 2) / 3 < totalQuads ? (end + 2) / 3 : totalQuads;
+        text.resize(4 * (q1 - q0));
+        if (fseek(fc.f, hdrChars + (long)(4 * q0), SEEK_SET) != 0 ||
+            fread(text.data(), 1, text.size(), fc.f) != text.size())
+            return fail(c, PLBGPU_ERR_ARG, "%s: truncated data", path);
+        CUDA_TRY(c, cudaMemcpyAsync(k.text, text.data(), text.size(), cudaMemcpyHostToDevice, c->stream));
+        const unsigned long long held = (3 * q1 < size ? 3 * q1 : size) - 3 * q0;
+        launchBase64Decode(k.text, q1 - q0, held, k.bytes, k.bad, c->stream);
+        if ((rc = launchBox(c))) return rc;
+        CUDA_TRY(c, cudaMemcpyAsync(k.rec, k.bytes + (start - 3 * q0), end - start, cudaMemcpyDeviceToDevice,
+                                    c->stream));
+        unsigned bad = 0;
+        CUDA_TRY(c, cudaMemcpyAsync(&bad, k.bad, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+        if (bad) return fail(c, PLBGPU_ERR_ARG, "%s: not base64 data", path);
+        int nl = 1;
+        dim3 g = rowGrid(d->nz, d->ny, x1 - x0 + 1, 128);
+        if (what == PLBGPU_BLOCK_LATTICE) {
+            nl = L.insert(d->view(), d->odd, b, k.rec, c->stream);
+        } else if (what == PLBGPU_BLOCK_FORCED_LATTICE) {
+            launchColumns(k.rec, 22, 0, 19, k.tmp, 19, 0, cells, c->stream);
+            nl = L.insert(d->view(), d->odd, b, k.tmp, c->stream);
+            launchColumns(k.rec, 22, 19, 3, k.tmp, 3, 0, cells, c->stream);
+            if (d->precision == PLBGPU_FP64)
+                boxPlanesKernel<double, double><<<g, 128, 0, c->stream>>>(static_cast<double*>(d->force), d->n, d->ny,
+                                                                          d->nz, b, k.tmp, 3, 0);
+            else
+                boxPlanesKernel<float, double><<<g, 128, 0, c->stream>>>(static_cast<float*>(d->force), d->n, d->ny,
+                                                                         d->nz, b, k.tmp, 3, 0);
+            nl += 3;
+        } else {
+            const long long off = what == PLBGPU_BLOCK_RHOBAR ? 0 : d->n;
+            if (d->precision == PLBGPU_FP64)
+                boxPlanesKernel<double, double><<<g, 128, 0, c->stream>>>(static_cast<double*>(d->ext) + off, d->n,
+                                                                          d->ny, d->nz, b, k.rec, w, 0);
+            else
+                boxPlanesKernel<float, double><<<g, 128, 0, c->stream>>>(static_cast<float*>(d->ext) + off, d->n,
+                                                                         d->ny, d->nz, b, k.rec, w, 0);
+        }
+        c->launches += nl - 1;
+        if ((rc = launchBox(c))) return rc;
+    }
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if (what == PLBGPU_BLOCK_LATTICE || what == PLBGPU_BLOCK_FORCED_LATTICE) d->statsValid = false;
+    return PLBGPU_OK;
+}
+
 // ------------------------------------------------------------ co-processor form
 
 int plbgpu_cp_add_domain(plbgpu_ctx* c, long nx, long ny, long nz, double omega, int* handle) {

@@ -65,6 +65,16 @@ int domainFail(plbgpu_ctx* c, int code, const char* msg);
 // After the adjoint module rewrote the populations in natural order.
 void domainSetState(plbgpu_ctx* c, int handle, bool odd, bool pending);
 
+// Binary-block checkpoints (checkpoint.cu): base64 of the byte stream
+// head[0..headLen) ++ body[0..bodyLen) as `quads` output quads (the last one
+// padded when the stream ends inside it), the inverse, and a column copy
+// between packed per-cell records.
+void launchBase64Encode(const uint8_t* head, int headLen, const uint8_t* body, size_t bodyLen, size_t quads,
+                        char* out, cudaStream_t s);
+void launchBase64Decode(const char* in, size_t quads, size_t bytes, uint8_t* out, unsigned* bad, cudaStream_t s);
+void launchColumns(const double* in, int inStride, int inOff, int m, double* out, int outStride, int outOff,
+                   long long cells, cudaStream_t s);
+
 inline dim3 rowGrid(int nz, int ny, int nx, int block) {
     return dim3((unsigned)((nz + block - 1) / block), (unsigned)ny, (unsigned)nx);
 }

@@ -16,6 +16,7 @@ exchanged as FP64 f-bar in [x][y][z][19] order.
 from __future__ import annotations
 
 import ctypes
+import os
 
 import numpy as np
 
@@ -237,6 +238,18 @@ class DeviceLattice3D:
         after each when recompute)."""
         self._check(self.lib.plbgpu_collide_and_stream_external(self.ctx.h, self.handle, int(nsteps),
                                                                 int(bool(recompute)), int(bool(stats))))
+
+    def save_binary_block(self, path, what="lattice", enforce_uint=False):
+        """saveBinaryBlock of the lattice (or "forced_lattice", "density",
+        "velocity", "rho_bar", "j") to `path`."""
+        self._check(self.lib.plbgpu_save_binary_block(self.ctx.h, self.handle, N.BLOCKS[what],
+                                                      os.fsencode(path), int(bool(enforce_uint))))
+
+    def load_binary_block(self, path, what="lattice", enforce_uint=False):
+        """loadBinaryBlock into the lattice ("lattice", "forced_lattice") or
+        the external fields ("rho_bar", "j")."""
+        self._check(self.lib.plbgpu_load_binary_block(self.ctx.h, self.handle, N.BLOCKS[what],
+                                                      os.fsencode(path), int(bool(enforce_uint))))
 
     def time_steps(self, nsteps, stats=False) -> float:
         ms = ctypes.c_float()
