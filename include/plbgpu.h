@@ -129,6 +129,19 @@ int plbgpu_get_kinds(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1
 int plbgpu_set_velocity_condition_on_block_boundaries(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0,
                                                       int y1, int z0, int z1);
 
+/* Sparse domain: computeSparseManagement(field) (offLattice/makeSparse3D.hh:
+ * 107-160) over the regular distribution createRegularDistribution3D(nx, ny,
+ * nz, bx, by, bz) (multiBlock/staticRepartitions3D.cpp:38-63).  A block is
+ * kept when any cell of it has a non-zero value in `field` (n = nx*ny*nz
+ * int32, z fastest); the cells of the other blocks leave the lattice: they are
+ * never updated, read back as zeros, count in no reduction or statistic, and
+ * their neighbours treat them like the outside of a non-periodic domain (the
+ * domain-edge rule).  keep (optional, bx*by*bz entries, x-major) receives the
+ * selection.  Steps on a sparse domain use the general addressing for every
+ * row. */
+int plbgpu_select_sparse_blocks(plbgpu_ctx* ctx, int handle, const int32_t* field, size_t n, int bx, int by,
+                                int bz, uint8_t* keep, size_t nblocks);
+
 /* setBoundaryVelocity / setBoundaryDensity (dataInitializerWrapper3D.h:99-118),
  * constant over a box or one value per cell of the box (`values`: 3 doubles
  * per cell for velocity, 1 per cell for density). */

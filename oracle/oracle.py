@@ -49,6 +49,10 @@ def lib():
         _lib.orc_run_external.argtypes = [ctypes.POINTER(_Params), u8, dp, dp, dp, dp, dp, ctypes.c_int,
                                           ctypes.c_int, dp]
         _lib.orc_run_external.restype = ctypes.c_int
+        _lib.orc_sparse_blocks.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_int32), ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_int, ctypes.POINTER(ctypes.c_uint8)]
+        _lib.orc_sparse_blocks.restype = ctypes.c_int
         _lib.orc_set_threads.argtypes = [ctypes.c_int]
         _lib.orc_max_threads.restype = ctypes.c_int
     return _lib
@@ -163,4 +167,36 @@ def binary_block(records, enforce_uint=False):
     data = np.ascontiguousarray(records, dtype="<f8").tobytes()
     head = struct.pack("<I" if enforce_uint else "<Q", len(data))
     return base64.b64encode(head) + base64.b64encode(data)
+
+
+def sparse_blocks(field, blocks):
+    """computeSparseManagement's block selection over the regular distribution
+    with blocks = (bx, by, bz): keep[bx, by, bz] (1 = kept)."""
+    field = np.ascontiguousarray(field, np.int32)
+    nx, ny, nz = field.shape
+    bx, by, bz = blocks
+    keep = np.zeros(bx * by * bz, np.uint8)
+    lib().orc_sparse_blocks(nx, ny, nz, field.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), bx, by, bz,
+                            keep.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)))
+    return keep.reshape(bx, by, bz)
+
+
+def regular_ranges(n, b):
+    """Block boundaries of createRegularDistribution3D along one axis."""
+    starts = [0]
+    for i in range(b):
+        starts.append(starts[-1] + n // b + (1 if i < n % b else 0))
+    return starts
+
+
+def sparse_cell_mask(shape, blocks, keep):
+    """Cells inside kept blocks (bool [nx, ny, nz])."""
+    mask = np.zeros(shape, bool)
+    r = [regular_ranges(n, b) for n, b in zip(shape, blocks)]
+    for ix in range(blocks[0]):
+        for iy in range(blocks[1]):
+            for iz in range(blocks[2]):
+                if keep[ix, iy, iz]:
+                    mask[r[0][ix]:r[0][ix + 1], r[1][iy]:r[1][iy + 1], r[2][iz]:r[2][iz + 1]] = True
+    return mask
 

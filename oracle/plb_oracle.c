@@ -37,7 +37,8 @@ enum {
     K_REGVEL = 6, K_REGPRESS = 12, K_ZHVEL = 18, K_ZHPRESS = 24,
     K_EDGE = 30,    /* 30..41: 30 + 4*plane + 2*(normal1>0) + (normal2>0) */
     K_CORNER = 42,  /* 42..49: 42 + 4*(xNormal>0) + 2*(yNormal>0) + (zNormal>0) */
-    K_NKINDS = 50
+    K_NKINDS = 50,
+    K_NONE = 255    /* not part of the lattice: outside every kept block of a sparse domain */
 };
 
 /* latticeBoltzmann/nearestNeighborLattices3D.hh:168-180 */
@@ -73,6 +74,7 @@ typedef struct {
     const double* force; /* N*3 (Guo cells) */
     uint32_t* mebbMask;  /* N, bit i = fluid direction i (MEBB cells only) */
     int hasEdges;        /* any edge or corner cell */
+    int hasNone;         /* any cell outside the lattice (sparse domain) */
 } orc_lattice;
 
 /* ------------------------------------------------------------ moments */
@@ -243,7 +245,7 @@ static void collide_cell(const orc_lattice* L, long id, double* f, orc_stats* st
     case K_BB:
         swap_halves(f);
         return;
-    case K_NODYN:
+    case K_NODYN: case K_NONE:
         return;
     case K_MEBB: {
         double mom[3] = {0., 0., 0.};
@@ -485,7 +487,7 @@ static inline long lid(const orc_lattice* L, int x, int y, int z) {
 }
 
 /* Neighbour of (x,y,z) along c_i (sign s = +1) or -c_i (s = -1).  Returns -1
- * when it leaves a non-periodic domain.  Periodic axes wrap, which is what the
+ * when it leaves a non-periodic domain or lands on a cell outside the lattice.  Periodic axes wrap, which is what the
  * periodic envelope overlaps of MultiBlockLattice3D::collideAndStream
  * (multiBlockLattice3D.hh:318-357, extendPeriodic :253-285) amount to. */
 static long neighbour(const orc_lattice* L, int x, int y, int z, int i, int s) {
@@ -497,7 +499,10 @@ static long neighbour(const orc_lattice* L, int x, int y, int z, int i, int s) {
             p[a] = (p[a] + n[a]) % n[a];
         }
     }
-    return lid(L, p[0], p[1], p[2]);
+    long id = lid(L, p[0], p[1], p[2]);
+    /* A cell outside every kept block of a sparse domain is treated like the
+     * outside of a non-periodic domain. */
+    return (L->hasNone && L->flags[id] == K_NONE) ? -1 : id;
 }
 
 /* InitializeMomentumExchangeFunctional3D (bounceBackModels3D.hh:42-90): a
@@ -563,10 +568,14 @@ static void step(const orc_lattice* L, double* f, double* tmp, orc_stats* st, do
 #pragma omp parallel for collapse(2) schedule(static)
     for (int x = 0; x < L->nx; ++x)
         for (int y = 0; y < L->ny; ++y) {
-            const int inner = x > 0 && x < L->nx - 1 && y > 0 && y < L->ny - 1;
+            const int inner = !L->hasNone && x > 0 && x < L->nx - 1 && y > 0 && y < L->ny - 1;
             for (int z = 0; z < L->nz; ++z) {
                 long id = lid(L, x, y, z);
                 double* out = f + id * 19;
+                if (L->hasNone && L->flags[id] == K_NONE) {
+                    for (int i = 0; i < 19; ++i) out[i] = 0.;
+                    continue;
+                }
                 out[0] = tmp[id * 19];
                 if (inner && z > 0 && z < L->nz - 1) {
                     /* no source lies outside the box: plain offsets */
@@ -606,6 +615,9 @@ static void setup(orc_lattice* L, const orc_params* p, const uint8_t* flags, con
     L->omega = p->omega; L->rho0 = p->rho0; L->bbRho = p->bbRho;
     L->flags = flags; L->bcval = bcval; L->force = force;
     long n = (long)p->nx * p->ny * p->nz;
+    L->hasNone = 0;
+    for (long id = 0; id < n; ++id)
+        if (flags[id] == K_NONE) { L->hasNone = 1; break; }
     L->mebbMask = (uint32_t*)calloc((size_t)n, sizeof(uint32_t));
     build_mebb_masks(L);
     L->hasEdges = 0;
@@ -676,7 +688,7 @@ static void cell_velocity(const orc_lattice* L, long id, const double* f, double
     int k = L->flags[id];
     double rb, j[3];
     switch (k) {
-    case K_BB: case K_MEBB: case K_NODYN:
+    case K_BB: case K_MEBB: case K_NODYN: case K_NONE:
         u[0] = u[1] = u[2] = 0.; /* core/dynamics.hh:824-829, bounceBackModels.hh:170-175 */
         return;
     case K_GUO: { /* externalForceDynamics.hh:58-73 */
@@ -960,14 +972,17 @@ int orc_reduce(const orc_params* p, const uint8_t* flags, const double* bcval, c
     setup(&L, p, flags, bcval, force);
     long n = (long)p->nx * p->ny * p->nz;
     double sE = 0., sR = 0.;
+    long cells = 0;   /* cells of the lattice (a sparse domain averages over its kept blocks) */
     for (long id = 0; id < n; ++id) {
+        if (flags[id] == K_NONE) continue;
         double u[3];
         cell_velocity(&L, id, f + id * 19, u);
         sE += u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
         sR += cell_rhoBar(&L, id, f + id * 19);
+        ++cells;
     }
-    *energy = sE / (double)2 / (double)n;
-    *density = sR / (double)n + (double)1;
+    *energy = sE / (double)2 / (double)cells;
+    *density = sR / (double)cells + (double)1;
     free(L.mebbMask);
     return 0;
 }
@@ -992,3 +1007,39 @@ int orc_mebb_masks(const orc_params* p, const uint8_t* flags, uint32_t* out) {
     free(L.mebbMask);
     return 0;
 }
+
+/* computeSparseManagement (offLattice/makeSparse3D.hh:47-160) over the
+ * regular block distribution createRegularDistribution3D(nx, ny, nz, bx, by,
+ * bz) (multiBlock/staticRepartitions3D.cpp:38-63, the first n % b blocks of an
+ * axis one cell longer): a block is kept when any cell of its bulk has a
+ * non-zero field value.  keep[(ix * by + iy) * bz + iz]; returns the number of
+ * kept blocks. */
+static void regular_ranges(int n, int b, int* start) {
+    int pos = 0;
+    for (int i = 0; i < b; ++i) {
+        start[i] = pos;
+        pos += n / b + (i < n % b ? 1 : 0);
+    }
+    start[b] = pos;
+}
+
+int orc_sparse_blocks(int nx, int ny, int nz, const int32_t* field, int bx, int by, int bz, uint8_t* keep) {
+    int sx[bx + 1], sy[by + 1], sz[bz + 1];
+    regular_ranges(nx, bx, sx);
+    regular_ranges(ny, by, sy);
+    regular_ranges(nz, bz, sz);
+    int kept = 0;
+    for (int ix = 0; ix < bx; ++ix)
+        for (int iy = 0; iy < by; ++iy)
+            for (int iz = 0; iz < bz; ++iz) {
+                int any = 0;
+                for (int x = sx[ix]; x < sx[ix + 1] && !any; ++x)
+                    for (int y = sy[iy]; y < sy[iy + 1] && !any; ++y)
+                        for (int z = sz[iz]; z < sz[iz + 1]; ++z)
+                            if (field[((long)x * ny + y) * nz + z] != 0) { any = 1; break; }
+                keep[(ix * by + iy) * bz + iz] = (uint8_t)any;
+                kept += any;
+            }
+    return kept;
+}
+

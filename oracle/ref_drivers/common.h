@@ -20,6 +20,7 @@
 //   float64  force[N*3]         (Guo force, only read when forced)
 //   float64  f0[N*19]           (initial f-bar, before lattice.initialize())
 //   float64  rhoBar0[N], j0[N*3] (only with OPT_EXTERNAL_RHOJ: initial fields)
+//   int32    sparse[N]           (only with OPT_SPARSE: the field of computeSparseManagement)
 //
 // Result file:
 //   char[8]  "PLBRES01"
@@ -31,6 +32,7 @@
 //   float64  avgEnergy, avgDensity   (computeAverageEnergy / computeAverageDensity
 //                                     over the bounding box after nsteps)
 //   float64  rhoBar[N], j[N*3]   (only with OPT_EXTERNAL_RHOJ: the fields at the end)
+//   uint8    inLattice[N]        (only with OPT_SPARSE: 1 for cells of kept blocks)
 #ifndef PLB_REF_DRIVER_COMMON_H
 #define PLB_REF_DRIVER_COMMON_H
 
@@ -60,9 +62,11 @@ enum {
     OPT_NO_INITIALIZE = 1,   // skip lattice.initialize() before the first step
     OPT_EXTERNAL_RHOJ = 2,   // step with ExternalRhoJcollideAndStream3D (level 0) and
                              // BoxRhoBarJfunctional3D (level 3) from the given fields
-    OPT_SAVE_BINARY = 4      // after the run, saveBinaryBlock of the lattice, of
+    OPT_SAVE_BINARY = 4,     // after the run, saveBinaryBlock of the lattice, of
                              // computeDensity and of computeVelocity into
                              // <result>.lattice / .density / .velocity
+    OPT_SPARSE = 8           // build the lattice on computeSparseManagement of the
+                             // given int field over the regular block distribution
 };
 
 struct Case {
@@ -76,6 +80,7 @@ struct Case {
     double omega, rho0, bbRho;
     std::vector<uint8_t> flags;
     std::vector<double> bcval, force, f0, rhoBar0, j0;
+    std::vector<int32_t> sparse;
     long n() const { return (long)nx * ny * nz; }
     long idx(int x, int y, int z) const { return ((long)x * ny + y) * nz + z; }
 };
@@ -116,6 +121,9 @@ inline Case readCase(const char* path) {
     if (c.options & OPT_EXTERNAL_RHOJ) {
         c.rhoBar0.resize(n); rd(f, c.rhoBar0.data(), n);
         c.j0.resize(n * 3); rd(f, c.j0.data(), n * 3);
+    }
+    if (c.options & OPT_SPARSE) {
+        c.sparse.resize(n); rd(f, c.sparse.data(), n);
     }
     std::fclose(f);
     return c;

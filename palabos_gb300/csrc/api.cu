@@ -41,6 +41,7 @@ struct Domain {
     int4* surf = nullptr;        // edge cells, then corner cells: (x, y, z, kind)
     int surfCap = 0, nEdges = 0, nCorners = 0;
     bool hasSurface = false;     // any edge or corner kind
+    bool sparse = false;         // any cell outside the lattice (K_NONE)
     bool surfDirty = false;      // the list needs rebuilding (kinds or periodicity changed)
     StatsAcc* stats = nullptr;   // device accumulator
     unsigned* status = nullptr;  // device error word written by the kernels
@@ -63,6 +64,7 @@ struct Domain {
         L.bc = bc;
         L.force = force;
         L.ext = ext;
+        L.sparse = sparse ? 1 : 0;
         L.nx = nx; L.ny = ny; L.nz = nz;
         L.per[0] = per[0]; L.per[1] = per[1]; L.per[2] = per[2];
         L.n = n;
@@ -220,8 +222,37 @@ __global__ void kindMaskKernel(const uint8_t* flags, long long n, unsigned long 
     if ((threadIdx.x & 31) == 0 && m) atomicOr(mask, m);
 }
 
+// Block of coordinate p along an axis of n cells cut into b blocks by
+// createRegularDistribution3D: the first n % b blocks are one cell longer.
+__device__ __forceinline__ int regularBlock(int p, int n, int b) {
+    const int q = n / b, r = n % b;
+    return p < r * (q + 1) ? p / (q + 1) : r + (p - r * (q + 1)) / q;
+}
+
+// ComputeSparsityFunctional3D (offLattice/makeSparse3D.hh:47-76): a block is
+// kept when some cell of its bulk has a non-zero field value.
+__global__ void sparseKeepKernel(const int32_t* field, DevLattice L, int bx, int by, int bz, uint8_t* keep) {
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < L.n;
+         idx += (long long)gridDim.x * blockDim.x) {
+        if (field[idx] == 0) continue;
+        const int z = (int)(idx % L.nz), y = (int)((idx / L.nz) % L.ny), x = (int)(idx / ((long long)L.ny * L.nz));
+        keep[(regularBlock(x, L.nx, bx) * by + regularBlock(y, L.ny, by)) * bz + regularBlock(z, L.nz, bz)] = 1;
+    }
+}
+
+// Cells of dropped blocks leave the lattice.
+__global__ void sparseMarkKernel(DevLattice L, int bx, int by, int bz, const uint8_t* keep) {
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < L.n;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int z = (int)(idx % L.nz), y = (int)((idx / L.nz) % L.ny), x = (int)(idx / ((long long)L.ny * L.nz));
+        if (!keep[(regularBlock(x, L.nx, bx) * by + regularBlock(y, L.ny, by)) * bz + regularBlock(z, L.nz, bz)])
+            const_cast<uint8_t*>(L.flags)[idx] = K_NONE;
+    }
+}
+
 // Whether the edge / corner cell at (x, y, z) may read its neighbour one step
-// along `axis`: inside the domain after the periodic wrap, and -- for a
+// along `axis`: inside the domain after the periodic wrap and part of the
+// lattice, and -- for a
 // density read -- not a cell whose populations the same pass rewrites.
 __device__ bool surfaceReadOk(const DevLattice& L, int x, int y, int z, int axis, int step, int forbidFrom) {
     int p[3] = {x, y, z};
@@ -232,6 +263,7 @@ __device__ bool surfaceReadOk(const DevLattice& L, int x, int y, int z, int axis
         p[axis] = p[axis] < 0 ? p[axis] + n[axis] : p[axis] - n[axis];
     }
     const int k = L.flags[((long long)p[0] * L.ny + p[1]) * L.nz + p[2]];
+    if (k == K_NONE) return false;
     return !(forbidFrom >= 0 && k >= forbidFrom && k < K_NKINDS);
 }
 
@@ -313,6 +345,7 @@ int syncKinds(plbgpu_ctx* c, Domain* d) {
     for (int k = K_EDGE; k < K_NKINDS; ++k) surface |= (m >> k) & 1;
     d->hasSurface = surface;
     d->surfDirty = true;
+    d->sparse = (m >> 63) & 1;   // kinds >= 63: only K_NONE
     return ensureAux(c, d, faces, (m >> K_GUO) & 1, (m >> K_MEBB) & 1);
 }
 
@@ -719,6 +752,40 @@ int plbgpu_set_velocity_condition_on_block_boundaries(plbgpu_ctx* c, int h, int 
     return plbgpu_set_kinds(c, h, x0, x1, y0, y1, z0, z1, kinds.data(), kinds.size());
 }
 
+int plbgpu_select_sparse_blocks(plbgpu_ctx* c, int h, const int32_t* field, size_t n, int bx, int by, int bz,
+                                uint8_t* keep, size_t nblocks) {
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if (!field || (long long)n != d->n) return fail(c, PLBGPU_ERR_ARG, "sparse field: %zu values for %lld cells", n, d->n);
+    if (bx < 1 || by < 1 || bz < 1 || bx > d->nx || by > d->ny || bz > d->nz)
+        return fail(c, PLBGPU_ERR_ARG, "%dx%dx%d blocks for a %dx%dx%d domain", bx, by, bz, d->nx, d->ny, d->nz);
+    const size_t nb = (size_t)bx * by * bz;
+    if (keep && nblocks != nb) return fail(c, PLBGPU_ERR_ARG, "keep: %zu entries for %zu blocks", nblocks, nb);
+    if ((rc = materialize(c, d))) return rc;
+    const size_t fieldBytes = sizeof(int32_t) * (size_t)d->n;
+    if ((rc = ensureStaging(c, fieldBytes + nb))) return rc;
+    int32_t* df = static_cast<int32_t*>(c->staging);
+    uint8_t* dk = static_cast<uint8_t*>(c->staging) + fieldBytes;
+    CUDA_TRY(c, cudaMemcpyAsync(df, field, fieldBytes, cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaMemsetAsync(dk, 0, nb, c->stream));
+    sparseKeepKernel<<<1216, 256, 0, c->stream>>>(df, d->view(), bx, by, bz, dk);
+    if ((rc = launchBox(c))) return rc;
+    std::vector<uint8_t> hk(nb);
+    CUDA_TRY(c, cudaMemcpyAsync(hk.data(), dk, nb, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    size_t kept = 0;
+    for (uint8_t v : hk) kept += v;
+    if (!kept) return fail(c, PLBGPU_ERR_ARG, "the sparse field is zero everywhere: no block would remain");
+    sparseMarkKernel<<<1216, 256, 0, c->stream>>>(d->view(), bx, by, bz, dk);
+    if ((rc = launchBox(c))) return rc;
+    if (keep) memcpy(keep, hk.data(), nb);
+    if ((rc = syncKinds(c, d))) return rc;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    d->statsValid = false;
+    return PLBGPU_OK;
+}
+
 int plbgpu_get_kinds(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, uint8_t* kinds,
                      size_t n) {
     Domain* d;
@@ -964,7 +1031,9 @@ int plbgpu_reduce(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, 
     ReduceAcc a;
     CUDA_TRY(c, cudaMemcpyAsync(&a, d->red, sizeof(ReduceAcc), cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-    double cells = (double)boxCells(b);
+    // computeAverage* over the cells of the lattice in the box (a sparse
+    // domain's kept blocks)
+    double cells = (double)a.cells;
     if (avg_energy) *avg_energy = a.sumEnergy / (double)2 / cells;
     if (avg_density) *avg_density = a.sumRhoBar / cells + (double)1;
     return PLBGPU_OK;

@@ -124,6 +124,7 @@ struct DevLattice {
     const double* bc;       // 3 planes of n: face velocity / density (or null)
     const void* force;      // 3 planes of n: Guo force in F (or null)
     const void* ext;        // 4 planes of n in F: external rho-bar, jx, jy, jz (or null)
+    int sparse;             // some cells are K_NONE (outside every kept block)
     int nx, ny, nz;
     int per[3];
     long long n;
@@ -151,6 +152,7 @@ struct StatsAcc {
 struct ReduceAcc {
     double sumEnergy;   // sum |u|^2
     double sumRhoBar;
+    unsigned long long cells;   // cells of the lattice in the box
 };
 
 // Offsets along one axis for a move of -1 / +1, or "invalid" outside a
@@ -171,7 +173,11 @@ __device__ __forceinline__ AxisMoves axisMoves(int p, int n, int per, long long 
 
 struct Neighbourhood {
     AxisMoves ax, ay, az;
-    // Move by s * c_i; returns false when leaving a non-periodic domain.
+    const uint8_t* flags;   // non-null on a sparse domain: the cell kinds
+    long long idx;          // the cell
+    // Move by s * c_i; returns false when leaving a non-periodic domain or
+    // landing on a cell outside the lattice (a sparse domain treats the
+    // outside of its kept blocks like the outside of the domain).
     __device__ __forceinline__ bool move(int i, int s, long long& off) const {
         int cx = s * cdir(i, 0), cy = s * cdir(i, 1), cz = s * cdir(i, 2);
         bool ok = true;
@@ -179,6 +185,7 @@ struct Neighbourhood {
         if (cx < 0) { ok &= ax.okM; off += ax.offM; } else if (cx > 0) { ok &= ax.okP; off += ax.offP; }
         if (cy < 0) { ok &= ay.okM; off += ay.offM; } else if (cy > 0) { ok &= ay.okP; off += ay.offP; }
         if (cz < 0) { ok &= az.okM; off += az.offM; } else if (cz > 0) { ok &= az.okP; off += az.offP; }
+        if (flags && ok && (cx | cy | cz) && flags[idx + off] == K_NONE) ok = false;
         return ok;
     }
 };
@@ -188,6 +195,8 @@ __device__ __forceinline__ Neighbourhood neighbourhood(const DevLattice& L, int 
     nb.ax = axisMoves(x, L.nx, L.per[0], (long long)L.ny * L.nz);
     nb.ay = axisMoves(y, L.ny, L.per[1], (long long)L.nz);
     nb.az = axisMoves(z, L.nz, L.per[2], 1);
+    nb.flags = L.sparse ? L.flags : nullptr;
+    nb.idx = ((long long)x * L.ny + y) * L.nz + z;
     return nb;
 }
 
@@ -646,18 +655,20 @@ __global__ void __launch_bounds__(128, 5)
 }
 
 // Rows on the x or y border of the domain, with the general addressing
-// (periodic wrap and the domain-edge rule on every axis).  blockIdx.y
-// enumerates the border rows: x = 0, x = nx-1 (all y), then y = 0, y = ny-1
-// (1 <= x <= nx-2); when nx < 3 or ny < 3 every row is a border row.
+// (periodic wrap and the domain-edge rule on every axis).  Row
+// blockIdx.y + gridDim.y * blockIdx.z enumerates the border rows: x = 0,
+// x = nx-1 (all y), then y = 0, y = ny-1 (1 <= x <= nx-2); when nx < 3 or
+// ny < 3, or on a sparse domain, every row is a border row.
 template <typename S, bool ODD, bool STATS>
 __global__ void __launch_bounds__(128) edgeRowStepKernel(DevLattice L, StepParams<typename StoreT<S>::R> P,
-                                                          StatsAcc* acc) {
+                                                          StatsAcc* acc, int rows) {
     using R = typename StoreT<S>::R;
     const int z = blockIdx.x * blockDim.x + threadIdx.x;
-    const int row = blockIdx.y;
+    const int row = blockIdx.y + gridDim.y * blockIdx.z;
+    if (row >= rows) return;   // whole blocks
     const int nx = L.nx, ny = L.ny;
     int x, y;
-    if (nx < 3 || ny < 3) {
+    if (L.sparse || nx < 3 || ny < 3) {
         x = row / ny;
         y = row - x * ny;
     } else if (row < ny) {
@@ -709,6 +720,11 @@ __global__ void extractKernel(DevLattice L, Box b, int pending, double* out) {
     const long long idx = ((long long)x * L.ny + y) * L.nz + z;
     const long long o = (((long long)blockIdx.z * bny + blockIdx.y) * bnz + dz) * 19;
     const int k = L.flags[idx];
+    if (k == K_NONE) {   // not part of the lattice: reads as zeros
+#pragma unroll
+        for (int i = 0; i < 19; ++i) out[o + i] = 0.;
+        return;
+    }
     Neighbourhood nb = neighbourhood(L, x, y, z);
     const S* Pp = static_cast<const S*>(L.pop);
     R f[19];
@@ -727,6 +743,7 @@ __global__ void insertKernel(DevLattice L, Box b, const double* in) {
     const int z = b.z0 + dz, y = b.y0 + blockIdx.y, x = b.x0 + blockIdx.z;
     const long long idx = ((long long)x * L.ny + y) * L.nz + z;
     const long long o = (((long long)blockIdx.z * bny + blockIdx.y) * bnz + dz) * 19;
+    if (L.flags[idx] == K_NONE) return;
     Neighbourhood nb = neighbourhood(L, x, y, z);
     S* Pp = static_cast<S*>(L.pop);
 #pragma unroll
@@ -1015,6 +1032,7 @@ __global__ void reduceKernel(DevLattice L, Box b, int pending, typename StoreT<S
     const int bnz = b.z1 - b.z0 + 1;
     const int dz = blockIdx.x * blockDim.x + threadIdx.x;
     double e = 0., r = 0.;
+    unsigned long long live = 0;
     if (dz < bnz) {
         R u[3], rb;
         double rho;
@@ -1022,13 +1040,16 @@ __global__ void reduceKernel(DevLattice L, Box b, int pending, typename StoreT<S
                                     rb, rho)) {
             e = (double)(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
             r = (double)rb;
+            live = 1;
         }
     }
     e = warpSum(e);
     r = warpSum(r);
+    live = warpSumU(live);
     if ((threadIdx.x & 31) == 0) {
         atomicAdd(&acc->sumEnergy, e);
         atomicAdd(&acc->sumRhoBar, r);
+        atomicAdd(&acc->cells, live);
     }
 }
 

@@ -20,8 +20,11 @@ struct StepLaunch {
     template <bool ODD, bool STATS>
     static int stepSplit(const DevLattice& L, const StepParams<R>& p, StatsAcc* acc, cudaStream_t s) {
         int launched = 0;
-        int edgeRows = (L.nx < 3 || L.ny < 3) ? L.nx * L.ny : 2 * L.ny + 2 * (L.nx - 2);
-        if (L.nx >= 3 && L.ny >= 3 && pairedRows(L)) {
+        // A sparse domain runs every row through the general addressing,
+        // which checks each neighbour's kind.
+        const bool general = L.sparse || L.nx < 3 || L.ny < 3;
+        const int edgeRows = general ? L.nx * L.ny : 2 * L.ny + 2 * (L.nx - 2);
+        if (!general && pairedRows(L)) {
             Planes<S> pl;
             Deltas d;
             for (int i = 0; i < 19; ++i) {
@@ -36,7 +39,7 @@ struct StepLaunch {
                                                                                                       acc);
                 ++launched;
             }
-        } else if (L.nx >= 3 && L.ny >= 3) {
+        } else if (!general) {
             Planes<S> pl;
             Deltas d;
             for (int i = 0; i < 19; ++i) {
@@ -51,8 +54,9 @@ struct StepLaunch {
             rowStepKernel<S, ODD, STATS><<<rowGrid(L.nz, L.ny - 2, L.nx - 2, tpb * NC), tpb, 0, s>>>(L, pl, d, p, acc);
             ++launched;
         }
-        dim3 g((unsigned)((L.nz + kBlock - 1) / kBlock), (unsigned)edgeRows, 1);
-        edgeRowStepKernel<S, ODD, STATS><<<g, kBlock, 0, s>>>(L, p, acc);
+        const int gy = edgeRows < 65535 ? edgeRows : 65535;
+        dim3 g((unsigned)((L.nz + kBlock - 1) / kBlock), (unsigned)gy, (unsigned)((edgeRows + gy - 1) / gy));
+        edgeRowStepKernel<S, ODD, STATS><<<g, kBlock, 0, s>>>(L, p, acc, edgeRows);
         return launched + 1;
     }
 

@@ -239,6 +239,17 @@ class DeviceLattice3D:
         self._check(self.lib.plbgpu_collide_and_stream_external(self.ctx.h, self.handle, int(nsteps),
                                                                 int(bool(recompute)), int(bool(stats))))
 
+    def select_sparse_blocks(self, field, blocks):
+        """computeSparseManagement over the regular distribution `blocks` =
+        (bx, by, bz): blocks without a non-zero `field` value leave the
+        lattice.  Returns the keep flags, shape blocks."""
+        f = np.ascontiguousarray(field, np.int32).reshape(-1)
+        keep = np.zeros(int(np.prod(blocks)), np.uint8)
+        self._check(self.lib.plbgpu_select_sparse_blocks(
+            self.ctx.h, self.handle, f.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), f.size, *map(int, blocks),
+            keep.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), keep.size))
+        return keep.reshape(tuple(blocks))
+
     def save_binary_block(self, path, what="lattice", enforce_uint=False):
         """saveBinaryBlock of the lattice (or "forced_lattice", "density",
         "velocity", "rho_bar", "j") to `path`."""
@@ -339,14 +350,18 @@ class DeviceLattice3D:
 
 
 def lattice_from_description(nx, ny, nz, periodic, omega, flags, bcval=None, force=None, rho0=1.0,
-                             bb_rho=0.0, precision="fp64", ctx=None):
+                             bb_rho=0.0, precision="fp64", ctx=None, sparse=None):
     """Configure a device lattice from per-cell arrays (kinds, face values in
-    3 components -- velocity, or density in component 0 -- and Guo force)."""
+    3 components -- velocity, or density in component 0 -- and Guo force).
+    sparse = (field, (bx, by, bz)) makes it a sparse lattice
+    (select_sparse_blocks) before the momentum-exchange masks are built."""
     from .native import REG_VELOCITY, REG_PRESSURE, ZOUHE_VELOCITY, ZOUHE_PRESSURE
     lat = DeviceLattice3D(nx, ny, nz, omega, precision, ctx, rho0, bb_rho)
     lat.periodicity(*periodic)
     flags = np.ascontiguousarray(flags, np.uint8).reshape(nx, ny, nz)
     lat.set_kinds(flags)
+    if sparse is not None:
+        lat.select_sparse_blocks(sparse[0], sparse[1])
     kinds = set(np.unique(flags).tolist())
     if bcval is not None and any(REG_VELOCITY <= k < N.NKINDS for k in kinds):
         bc = np.asarray(bcval, np.float64).reshape(nx, ny, nz, 3)

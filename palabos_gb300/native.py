@@ -24,6 +24,7 @@ PRECISIONS = {"fp64": FP64, "fp32": FP32, "bf16": BF16, "fp16": FP16, "bf16sr": 
 BGK, GUO, INCBGK, BOUNCEBACK, MOMENTUM_EXCHANGE, NODYNAMICS = 0, 1, 2, 3, 4, 5
 REG_VELOCITY, REG_PRESSURE, ZOUHE_VELOCITY, ZOUHE_PRESSURE = 6, 12, 18, 24
 VELOCITY_EDGE, VELOCITY_CORNER, NKINDS = 30, 42, 50
+NONE = 255   # not part of the lattice (sparse domains)
 BLOCKS = {"lattice": 0, "forced_lattice": 1, "density": 2, "velocity": 3, "rho_bar": 4, "j": 5}
 
 
@@ -79,6 +80,7 @@ SIGNATURES = {
     "plbgpu_set_rhobar_j": [_vp, _i, *BOX, _c_dbl_p, _sz],
     "plbgpu_get_rhobar_j": [_vp, _i, *BOX, _c_dbl_p, _sz],
     "plbgpu_collide_and_stream_external": [_vp, _i, _i, _i, _i],
+    "plbgpu_select_sparse_blocks": [_vp, _i, ctypes.POINTER(ctypes.c_int32), _sz, _i, _i, _i, _c_u8_p, _sz],
     "plbgpu_save_binary_block": [_vp, _i, _i, ctypes.c_char_p, _i],
     "plbgpu_load_binary_block": [_vp, _i, _i, ctypes.c_char_p, _i],
     "plbgpu_set_boundary_velocity": [_vp, _i, *BOX, _d, _d, _d],

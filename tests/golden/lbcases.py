@@ -40,6 +40,8 @@ EDGE, CORNER = 30, 42
 OPT_NO_INITIALIZE = 1
 OPT_EXTERNAL_RHOJ = 2
 OPT_SAVE_BINARY = 4
+OPT_SPARSE = 8
+NONE = 255   # not part of the lattice (outside every kept block)
 
 
 def face_kind(family: int, direction: int, orientation: int) -> int:
@@ -100,6 +102,8 @@ class CaseSpec:
     options: int = 0
     rho_bar0: np.ndarray = None   # initial external rho-bar field (OPT_EXTERNAL_RHOJ)
     j0: np.ndarray = None         # initial external j field
+    sparse: np.ndarray = None     # int field of computeSparseManagement (OPT_SPARSE)
+    compare: np.ndarray = None    # cells compared with the reference (default: all)
 
     def meta(self):
         return dict(name=self.name, nx=self.nx, ny=self.ny, nz=self.nz,
@@ -447,6 +451,34 @@ def case_binary_guo_periodic():
     return s
 
 
+def case_sparse_sealed_channel():
+    """A sparse lattice: computeSparseManagement over a 4 x 3 x 3 regular
+    distribution of 24 x 18 x 18 keeps the 12 blocks that touch a
+    bounce-back-sealed fluid box (with a momentum-exchange obstacle inside);
+    the other 24 blocks are not part of the lattice.  Kept cells outside the
+    seal are background BGK.  The fluid inside the seal never exchanges
+    populations with the outside, so it is compared with the reference bit
+    for bit; the seal and the outside (whose neighbours in dropped blocks the
+    reference represents by its blocks' envelopes) are not."""
+    shape = (24, 18, 18)
+    rng = np.random.default_rng(113)
+    flags, bcval, force, _ = empty(shape)
+    x0, x1, y0, y1, z0, z1 = 1, 14, 1, 10, 1, 10
+    seal = np.zeros(shape, bool)
+    seal[x0:x1 + 1, y0:y1 + 1, z0:z1 + 1] = True
+    fluid = np.zeros(shape, bool)
+    fluid[x0 + 1:x1, y0 + 1:y1, z0 + 1:z1] = True
+    flags[seal & ~fluid] = BB
+    flags[5:7, 4:6, 5:8] = MEBB
+    field = seal.astype(np.int32)
+    f0 = initial_state(shape, rng, u_amp=0.03, rho_amp=0.003)
+    spec = _spec("sparse_sealed_channel", shape, (0, 0, 0), 1.7, 30, flags, bcval, force, f0,
+                 blocks=(4, 3, 3), options=OPT_SPARSE)
+    spec.sparse = field
+    spec.compare = fluid
+    return spec
+
+
 def case_doctest_cavity20():
     return doctest_cavity(20, 20, 20, name="doctest_cavity20")
 
@@ -470,6 +502,7 @@ CASES = [
     case_velocity_box_multiblock, case_velocity_box_noinit, case_doctest_cavity20,
     case_external_periodic_bgk, case_external_incbgk_nodyn, case_external_guo_periodic,
     case_external_mebb_periodic, case_binary_channel_sphere, case_binary_guo_periodic,
+    case_sparse_sealed_channel,
 ]
 
 
@@ -511,6 +544,8 @@ def write_case_file(spec: CaseSpec, path: str):
         if spec.options & OPT_EXTERNAL_RHOJ:
             f.write(np.ascontiguousarray(spec.rho_bar0, np.float64).tobytes())
             f.write(np.ascontiguousarray(spec.j0, np.float64).tobytes())
+        if spec.options & OPT_SPARSE:
+            f.write(np.ascontiguousarray(spec.sparse, np.int32).tobytes())
 
 
 def read_result_file(path: str, spec: CaseSpec):
@@ -534,6 +569,10 @@ def read_result_file(path: str, spec: CaseSpec):
     energy, density = struct.unpack_from("<2d", data, off)
     off += 16
     out = dict(f_init=f_init.copy(), f_final=f_final.copy(), stats=stats, energy=energy, density=density)
+    if spec.options & OPT_SPARSE:
+        m = nx * ny * nz
+        out["in_lattice"] = np.frombuffer(data, np.uint8, m, off).reshape(nx, ny, nz).copy()
+        off += m
     if spec.options & OPT_EXTERNAL_RHOJ:
         m = nx * ny * nz
         out["rho_bar_final"] = np.frombuffer(data, np.float64, m, off).reshape(nx, ny, nz).copy()
