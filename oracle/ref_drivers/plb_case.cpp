@@ -9,6 +9,8 @@
 // Test infrastructure only; linked against the unmodified reference library.
 #include "common.h"
 
+#include <cstdlib>
+
 #include "parallelism/headers3D.h"
 #include "parallelism/headers3D.hh"
 #include "latticeBoltzmann/headers3D.h"
@@ -31,6 +33,11 @@
 #include "io/headers3D.hh"
 #include "coProcessors/headers3D.h"
 #include "coProcessors/headers3D.hh"
+#include "offLattice/makeSparse3D.h"
+#include "offLattice/makeSparse3D.hh"
+
+// The library's Palabos mirror (host part only: no GPU call is made here).
+#include "plbgpu_palabos3d.hh"
 
 using namespace plb;
 using namespace refcase;
@@ -162,11 +169,18 @@ void wr(FILE* f, const V* p, size_t n) {
 }
 
 template<template<typename U> class D>
+bool inLattice(MultiBlockLattice3D<double,D>& lat, int x, int y, int z) {
+    return lat.getMultiBlockManagement().getSparseBlockStructure().locate(x, y, z) >= 0;
+}
+
+// Cells outside every block of a sparse lattice are written as zeros.
+template<template<typename U> class D>
 void dumpPopulations(MultiBlockLattice3D<double,D>& lat, const Case& c, std::vector<double>& out) {
-    out.resize(c.n() * 19);
+    out.assign(c.n() * 19, 0.);
     for (int x = 0; x < c.nx; ++x)
         for (int y = 0; y < c.ny; ++y)
             for (int z = 0; z < c.nz; ++z) {
+                if (!inLattice(lat, x, y, z)) continue;
                 Cell<double,D>& cell = lat.get(x, y, z);
                 for (int i = 0; i < 19; ++i) out[c.idx(x, y, z) * 19 + i] = cell[i];
             }
@@ -176,10 +190,22 @@ template<template<typename U> class D, class BulkDynamics>
 int run(const Case& c, const char* outPath) {
     typedef MultiBlockLattice3D<double,D> Lattice;
     DefaultMultiBlockPolicy3D& policy = defaultMultiBlockPolicy3D();
-    Lattice lat(MultiBlockManagement3D(
-                    createRegularDistribution3D(c.nx, c.ny, c.nz, c.blocks[0], c.blocks[1], c.blocks[2]),
-                    policy.getThreadAttribution(), 1),
-                policy.getBlockCommunicator(), policy.getCombinedStatistics(),
+    MultiBlockManagement3D dense(
+        createRegularDistribution3D(c.nx, c.ny, c.nz, c.blocks[0], c.blocks[1], c.blocks[2]),
+        policy.getThreadAttribution(), 1);
+    const bool sparse = (c.options & OPT_SPARSE) != 0;
+    MultiBlockManagement3D management(dense);
+    if (sparse) {
+        // computeSparseManagement (offLattice/makeSparse3D.hh:107-160) of the
+        // case's int field on the same regular distribution.
+        MultiScalarField3D<int> field(dense, policy.getBlockCommunicator(), policy.getCombinedStatistics(),
+                                      policy.getMultiScalarAccess<int>(), 0);
+        for (int x = 0; x < c.nx; ++x)
+            for (int y = 0; y < c.ny; ++y)
+                for (int z = 0; z < c.nz; ++z) field.get(x, y, z) = c.sparse[c.idx(x, y, z)];
+        management = computeSparseManagement(field, 1);
+    }
+    Lattice lat(management, policy.getBlockCommunicator(), policy.getCombinedStatistics(),
                 policy.template getMultiCellAccess<double,D>(),
                 new BulkDynamics(c.omega));
     for (int a = 0; a < 3; ++a) lat.periodicity().toggle(a, c.periodic[a] != 0);
@@ -252,6 +278,7 @@ int run(const Case& c, const char* outPath) {
     for (int x = 0; x < c.nx; ++x)
         for (int y = 0; y < c.ny; ++y)
             for (int z = 0; z < c.nz; ++z) {
+                if (!inLattice(lat, x, y, z)) continue;
                 Cell<double,D>& cell = lat.get(x, y, z);
                 long id = c.idx(x, y, z);
                 for (int i = 0; i < 19; ++i) cell[i] = c.f0[id * 19 + i];
@@ -264,6 +291,24 @@ int run(const Case& c, const char* outPath) {
 
     std::vector<double> fInit, fFinal;
     dumpPopulations(lat, c, fInit);
+
+    // With PLB_DESCRIBE=<path>: what plbgpu::describe() reads from the lattice
+    // after initialize() -- kinds (uint8 N), values (float64 3N), force
+    // (float64 3N, zeros without a forced descriptor), f-bar (float64 19N),
+    // omega, bbRho.
+    if (const char* dpath = std::getenv("PLB_DESCRIBE")) {
+        plbgpu::PalabosDescription dsc = plbgpu::describe(lat, c.rho0);
+        FILE* df = std::fopen(dpath, "wb");
+        if (!df) die("cannot open description file");
+        wr(df, dsc.kinds.data(), dsc.kinds.size());
+        wr(df, dsc.bcval.data(), dsc.bcval.size());
+        std::vector<double> force(dsc.forced ? dsc.force : std::vector<double>(3 * c.n(), 0.));
+        wr(df, force.data(), force.size());
+        wr(df, dsc.f.data(), dsc.f.size());
+        double tail2[2] = {dsc.omega, dsc.bbRho};
+        wr(df, tail2, 2);
+        std::fclose(df);
+    }
 
     // The external rho-bar / j form: the two processors of a lattice stepped
     // by executeInternalProcessors() instead of collideAndStream().
@@ -339,6 +384,14 @@ int run(const Case& c, const char* outPath) {
     }
     double tail[2] = {energy, density};
     wr(f, tail, 2);
+    if (sparse) {     // cells of the kept blocks
+        std::vector<uint8_t> in(c.n());
+        for (int x = 0; x < c.nx; ++x)
+            for (int y = 0; y < c.ny; ++y)
+                for (int z = 0; z < c.nz; ++z)
+                    in[c.idx(x, y, z)] = management.getSparseBlockStructure().locate(x, y, z) >= 0 ? 1 : 0;
+        wr(f, in.data(), in.size());
+    }
     if (external) {   // the fields after the last BoxRhoBarJfunctional3D
         std::vector<double> rb(c.n()), jj(3 * c.n());
         for (int x = 0; x < c.nx; ++x)
