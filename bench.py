@@ -222,7 +222,7 @@ def run_reference(args):
 # ------------------------------------------------------------------ GPU arm
 
 def adjoint_cost(ctx, T=2000, K=100, precisions=("fp64", "fp32")):
-    """Config 4: Guo-forced 128x64x64 channel (periodic x, bounce-back walls),
+    """Guo-forced 128x64x64 channel (periodic x, bounce-back walls),
     omega 1.6, force N(0, 1e-12) + 1e-5 x-drive (seed 1234); target velocity
     from a forward run with a second force field (seed 5678); objective
     1/2 sum |u(T) - u*|^2, checkpoint every K steps.  Reports the device time

@@ -50,7 +50,7 @@ class Workload:
 
 
 def cavity(n=64, lid_u=0.02, re=100.0):
-    """Config 1: n^3 cavity, nu = lid_u * n / Re, omega = 1/(3 nu + 1/2)."""
+    """Lid-driven cavity, n^3, nu = lid_u * n / Re, omega = 1/(3 nu + 1/2)."""
     kinds = np.zeros((n, n, n), np.uint8)
     bc = np.zeros((n, n, n, 3))
     for sl in [(0, slice(None), slice(None)), (-1, slice(None), slice(None)),
@@ -65,7 +65,7 @@ def cavity(n=64, lid_u=0.02, re=100.0):
 
 
 def channel_sphere(shape=(256, 128, 128), center=(64, 64, 64), radius=16, u_max=0.05, omega=1.8):
-    """Config 2: parabolic regularized inlet at x=0, regularized pressure rho=1
+    """Channel past a sphere: parabolic regularized inlet at x=0, regularized pressure rho=1
     at x=nx-1, bounce-back channel walls, momentum-exchange sphere."""
     nx, ny, nz = shape
     kinds = np.zeros(shape, np.uint8)
@@ -87,7 +87,7 @@ def channel_sphere(shape=(256, 128, 128), center=(64, 64, 64), radius=16, u_max=
 
 
 def taylor_green(n=512, u0=0.04, re=1600.0):
-    """Config 3: u = u0 (sin kx cos ky cos kz, -cos kx sin ky cos kz, 0),
+    """Taylor-Green vortex: u = u0 (sin kx cos ky cos kz, -cos kx sin ky cos kz, 0),
     k = 2 pi / n, p = (u0^2/16)(cos 2kx + cos 2ky)(cos 2kz + 2), rho = 1 + 3p;
     Re = u0 / (k nu), i.e. the length scale is 1/k."""
     k = 2.0 * math.pi / n
@@ -110,7 +110,7 @@ def taylor_green(n=512, u0=0.04, re=1600.0):
 
 
 def forced_channel(shape=(128, 64, 64), omega=1.6, seed=1234, sigma=1e-6, drive=1e-5):
-    """Config 4 forward model: periodic x, bounce-back walls at y and z ends,
+    """Guo-forced channel (the adjoint's forward model): periodic x, bounce-back walls at y and z ends,
     Guo-forced BGK with F ~ N(0, sigma^2) i.i.d. per component plus (drive, 0, 0)."""
     rng = np.random.default_rng(seed)
     kinds = np.full(shape, N.GUO, np.uint8)
@@ -121,7 +121,7 @@ def forced_channel(shape=(128, 64, 64), omega=1.6, seed=1234, sigma=1e-6, drive=
 
 
 def sphere_packing(n=384, porosity=0.4, rmin=6.0, rmax=12.0, seed=77, force=1e-6):
-    """Config 5: periodic box, seeded non-overlapping spheres with radius
+    """Sphere packing: periodic box, seeded non-overlapping spheres with radius
     U[rmin, rmax] placed by rejection sampling until the porosity reaches the
     target, as bounce-back cells; Guo force along x in the fluid."""
     rng = np.random.default_rng(seed)

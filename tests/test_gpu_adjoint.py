@@ -106,8 +106,8 @@ def test_adjoint_rejects_unsupported_cells():
 
 
 @pytest.mark.slow
-def test_config4_gradient_full_size():
-    """Config 4 at full size (128x64x64, Guo forcing, T = 2000, checkpoint
+def test_forced_channel_gradient_full_size():
+    """The Guo-forced channel at full size (128x64x64, Guo forcing, T = 2000, checkpoint
     every 100 steps): adjoint gradient against central finite differences of
     the CPU oracle for omega and three force components, to 1e-5 relative."""
     T, K = 2000, 100

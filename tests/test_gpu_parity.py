@@ -163,7 +163,7 @@ def test_edge_without_inward_neighbours_is_reported_not_run():
 
 
 def test_cavity64_full_size_matches_reference_fingerprint():
-    """Config 1 at full size: 64^3 lid-driven cavity, 1000 steps, every bit."""
+    """The 64^3 lid-driven cavity at full size, 1000 steps, every bit."""
     fp = goldens.load_fingerprint("cavity64")
     s = lbcases.case_cavity64()
     lat = lattice_from_description(s.nx, s.ny, s.nz, s.periodic, s.omega, s.flags, s.bcval, s.force)

@@ -89,7 +89,7 @@ def test_multiblock_equals_single_block():
 
 @pytest.mark.slow
 def test_oracle_cavity64_full_size():
-    """Config-1 lid-driven cavity at full size (64^3, 1000 steps) against the
+    """The lid-driven cavity at full size (64^3, 1000 steps) against the
     reference's fingerprint: sha256 of every population bit, plus energy."""
     fp = goldens.load_fingerprint("cavity64")
     s = lbcases.case_cavity64()
