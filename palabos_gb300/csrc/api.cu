@@ -43,7 +43,7 @@ struct Domain {
     bool hasSurface = false;     // any edge or corner kind
     bool sparse = false;         // any cell outside the lattice (K_NONE)
     bool surfDirty = false;      // the list needs rebuilding (kinds or periodicity changed)
-    StatsAcc* stats = nullptr;   // device accumulator
+    StatsAcc* stats = nullptr;   // device accumulators (kStatsSlots of them)
     unsigned* status = nullptr;  // device error word written by the kernels
     ReduceAcc* red = nullptr;
     bool odd = false;            // AA parity of the stored state
@@ -604,7 +604,7 @@ int plbgpu_add_domain(plbgpu_ctx* c, int nx, int ny, int nz, int precision, int*
     d->flags = static_cast<uint8_t*>(d->arena) + popBytes;
     d->deviceBytes = bytes;
     CUDA_TRY(c, cudaMemsetAsync(d->arena, 0, bytes, c->stream));   // f-bar = 0 (rest), all BGK
-    CUDA_TRY(c, cudaMalloc(&d->stats, sizeof(StatsAcc)));
+    CUDA_TRY(c, cudaMalloc(&d->stats, sizeof(StatsAcc) * kStatsSlots));
     CUDA_TRY(c, cudaMalloc(&d->status, sizeof(unsigned)));
     CUDA_TRY(c, cudaMemsetAsync(d->status, 0, sizeof(unsigned), c->stream));
     CUDA_TRY(c, cudaMalloc(&d->red, sizeof(ReduceAcc)));
@@ -979,7 +979,7 @@ int plbgpu_collide_and_stream(plbgpu_ctx* c, int h, int nsteps, int collect_stat
     if (d->surfDirty && (rc = buildSurface(c, d))) return rc;
     for (int s = 0; s < nsteps; ++s) {
         bool stats = collect_stats && s == nsteps - 1;
-        if (stats) CUDA_TRY(c, cudaMemsetAsync(d->stats, 0, sizeof(StatsAcc), c->stream));
+        if (stats) CUDA_TRY(c, cudaMemsetAsync(d->stats, 0, sizeof(StatsAcc) * kStatsSlots, c->stream));
         StepConsts k = consts(d);
         int nl = L.step(d->view(), d->odd, stats, k, d->stats, c->stream);
         c->launches += nl - 1;
@@ -1000,9 +1000,17 @@ int plbgpu_get_stats(plbgpu_ctx* c, int h, double out[7]) {
     if (!out) return PLBGPU_ERR_ARG;
     if (!d->statsValid) return fail(c, PLBGPU_ERR_STATE, "no step has gathered statistics since the last change");
     if ((rc = checkStatus(c, d))) return rc;
-    StatsAcc a;
-    CUDA_TRY(c, cudaMemcpyAsync(&a, d->stats, sizeof(StatsAcc), cudaMemcpyDeviceToHost, c->stream));
+    StatsAcc slots[kStatsSlots];
+    CUDA_TRY(c, cudaMemcpyAsync(slots, d->stats, sizeof(slots), cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    StatsAcc a = {0., 0., 0ull, 0ull, {0., 0., 0.}, 0.};
+    for (const StatsAcc& s : slots) {
+        a.sumRhoBar += s.sumRhoBar;
+        a.sumUSqr += s.sumUSqr;
+        a.count += s.count;
+        a.maxBits = s.maxBits > a.maxBits ? s.maxBits : a.maxBits;
+        for (int k = 0; k < 3; ++k) a.drag[k] += s.drag[k];
+    }
     double cnt = (double)a.count;
     double mx;
     memcpy(&mx, &a.maxBits, sizeof(double));
@@ -1131,7 +1139,7 @@ int plbgpu_collide_and_stream_external(plbgpu_ctx* c, int h, int nsteps, int rec
     if (d->surfDirty && (rc = buildSurface(c, d))) return rc;
     for (int s = 0; s < nsteps; ++s) {
         bool stats = collect_stats && s == nsteps - 1;
-        if (stats) CUDA_TRY(c, cudaMemsetAsync(d->stats, 0, sizeof(StatsAcc), c->stream));
+        if (stats) CUDA_TRY(c, cudaMemsetAsync(d->stats, 0, sizeof(StatsAcc) * kStatsSlots, c->stream));
         StepConsts k = consts(d);
         k.external = 1;
         int nl = L.step(d->view(), d->odd, stats, k, d->stats, c->stream);

@@ -149,6 +149,16 @@ struct StatsAcc {
     double pad;
 };
 
+// The statistics are accumulated into kStatsSlots copies of StatsAcc, one per
+// block index modulo kStatsSlots, and summed on the host: atomics from
+// thousands of blocks on one address would serialize the whole step.
+constexpr int kStatsSlots = 64;
+
+__device__ __forceinline__ StatsAcc* statsSlot(StatsAcc* acc) {
+    const unsigned b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    return acc + (b & (kStatsSlots - 1));
+}
+
 struct ReduceAcc {
     double sumEnergy;   // sum |u|^2
     double sumRhoBar;
@@ -370,9 +380,10 @@ __device__ __forceinline__ bool collideCell(const DevLattice& L, const StepParam
                 if (cdir(i, 1)) mom[1] += (double)2 * cdir(i, 1) * fo;
                 if (cdir(i, 2)) mom[2] += (double)2 * cdir(i, 2) * fo;
             }
-            atomicAdd(&acc->drag[0], -mom[0]);
-            atomicAdd(&acc->drag[1], -mom[1]);
-            atomicAdd(&acc->drag[2], -mom[2]);
+            StatsAcc* a = statsSlot(acc);
+            atomicAdd(&a->drag[0], -mom[0]);
+            atomicAdd(&a->drag[1], -mom[1]);
+            atomicAdd(&a->drag[2], -mom[2]);
         }
         swapHalves(f);
         return false;
@@ -382,23 +393,48 @@ __device__ __forceinline__ bool collideCell(const DevLattice& L, const StepParam
     }
 }
 
+// Block-wide sum of the per-thread statistics, one set of atomics per block
+// on the block's slot.  Every thread of the block must call it.
+__device__ __forceinline__ void flushStats(double sR, double sU, unsigned long long cnt, unsigned long long mx,
+                                           StatsAcc* acc) {
+    __shared__ double shR[32], shU[32];
+    __shared__ unsigned long long shC[32], shM[32];
+    sR = warpSum(sR);
+    sU = warpSum(sU);
+    cnt = warpSumU(cnt);
+    mx = warpMaxU(mx);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
+    if (lane == 0) {
+        shR[w] = sR;
+        shU[w] = sU;
+        shC[w] = cnt;
+        shM[w] = mx;
+    }
+    __syncthreads();
+    if (w == 0) {
+        sR = lane < nw ? shR[lane] : 0.;
+        sU = lane < nw ? shU[lane] : 0.;
+        cnt = lane < nw ? shC[lane] : 0ull;
+        mx = lane < nw ? shM[lane] : 0ull;
+        sR = warpSum(sR);
+        sU = warpSum(sU);
+        cnt = warpSumU(cnt);
+        mx = warpMaxU(mx);
+        if (lane == 0 && cnt > 0) {
+            StatsAcc* a = statsSlot(acc);
+            atomicAdd(&a->sumRhoBar, sR);
+            atomicAdd(&a->sumUSqr, sU);
+            atomicAdd(&a->count, cnt);
+            atomicMax(&a->maxBits, mx);
+        }
+    }
+}
+
 template <bool STATS>
 __device__ __forceinline__ void accumulateStats(bool gathers, double rhoBar, double uSqr, StatsAcc* acc) {
     if (!STATS) return;
-    double sR = gathers ? rhoBar : 0.;
-    double sU = gathers ? uSqr : 0.;
-    unsigned long long c = gathers ? 1ull : 0ull;
-    unsigned long long m = gathers ? (unsigned long long)__double_as_longlong(uSqr) : 0ull;
-    sR = warpSum(sR);
-    sU = warpSum(sU);
-    c = warpSumU(c);
-    m = warpMaxU(m);
-    if ((threadIdx.x & 31) == 0 && c > 0) {
-        atomicAdd(&acc->sumRhoBar, sR);
-        atomicAdd(&acc->sumUSqr, sU);
-        atomicAdd(&acc->count, c);
-        atomicMax(&acc->maxBits, m);
-    }
+    flushStats(gathers ? rhoBar : 0., gathers ? uSqr : 0., gathers ? 1ull : 0ull,
+               gathers ? (unsigned long long)__double_as_longlong(uSqr) : 0ull, acc);
 }
 
 // General cell update: any position, periodic wrap and the domain-edge rule.
@@ -535,18 +571,7 @@ __global__ void __launch_bounds__(128, RowShape<S>::blocks)
             mx = b > mx ? b : mx;
         }
     }
-    if (STATS) {
-        sR = warpSum(sR);
-        sU = warpSum(sU);
-        cnt = warpSumU(cnt);
-        mx = warpMaxU(mx);
-        if ((threadIdx.x & 31) == 0 && cnt > 0) {
-            atomicAdd(&acc->sumRhoBar, sR);
-            atomicAdd(&acc->sumUSqr, sU);
-            atomicAdd(&acc->count, cnt);
-            atomicMax(&acc->maxBits, mx);
-        }
-    }
+    if (STATS) flushStats(sR, sU, cnt, mx, acc);
 }
 
 // ---------------------------------------------------------------- paired row kernel
@@ -559,7 +584,7 @@ __global__ void __launch_bounds__(128, RowShape<S>::blocks)
 // wrap / reflection selects of RowCell.  Needs nz even (rows and planes start
 // on 4-byte boundaries).
 template <typename S, bool ODD, bool STATS>
-__global__ void __launch_bounds__(128, 5)
+__global__ void __launch_bounds__(128, 8)
     pairRowStepKernel(DevLattice L, Planes<S> Pl, Deltas D, StepParams<typename StoreT<S>::R> P, StatsAcc* acc) {
     using R = typename StoreT<S>::R;
     const int x = blockIdx.z + 1, y = blockIdx.y + 1;
@@ -640,18 +665,7 @@ __global__ void __launch_bounds__(128, 5)
             }
         }
     }
-    if (STATS) {
-        sR = warpSum(sR);
-        sU = warpSum(sU);
-        cnt = warpSumU(cnt);
-        mx = warpMaxU(mx);
-        if ((threadIdx.x & 31) == 0 && cnt > 0) {
-            atomicAdd(&acc->sumRhoBar, sR);
-            atomicAdd(&acc->sumUSqr, sU);
-            atomicAdd(&acc->count, cnt);
-            atomicMax(&acc->maxBits, mx);
-        }
-    }
+    if (STATS) flushStats(sR, sU, cnt, mx, acc);
 }
 
 // Rows on the x or y border of the domain, with the general addressing
