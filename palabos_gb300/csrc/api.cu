@@ -607,7 +607,7 @@ int plbgpu_add_domain(plbgpu_ctx* c, int nx, int ny, int nz, int precision, int*
     CUDA_TRY(c, cudaMalloc(&d->stats, sizeof(StatsAcc) * kStatsSlots));
     CUDA_TRY(c, cudaMalloc(&d->status, sizeof(unsigned)));
     CUDA_TRY(c, cudaMemsetAsync(d->status, 0, sizeof(unsigned), c->stream));
-    CUDA_TRY(c, cudaMalloc(&d->red, sizeof(ReduceAcc)));
+    CUDA_TRY(c, cudaMalloc(&d->red, sizeof(ReduceAcc) * kStatsSlots));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     int h = c->nextHandle++;
     c->domains[h] = std::move(d);
@@ -1031,14 +1031,20 @@ int plbgpu_reduce(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, 
     int rc = lookup(c, h, &d);
     if (rc) return rc;
     if ((rc = checkBox(c, d, x0, x1, y0, y1, z0, z1, &b))) return rc;
-    CUDA_TRY(c, cudaMemsetAsync(d->red, 0, sizeof(ReduceAcc), c->stream));
+    CUDA_TRY(c, cudaMemsetAsync(d->red, 0, sizeof(ReduceAcc) * kStatsSlots, c->stream));
     int k = launchers(d->precision).reduce(d->view(), d->odd, b, d->pending && d->bc ? 1 : 0, (double)1 / d->rho0,
                                            d->bbRho, d->red, c->stream);
     c->launches += k - 1;
     if ((rc = launchBox(c))) return rc;
-    ReduceAcc a;
-    CUDA_TRY(c, cudaMemcpyAsync(&a, d->red, sizeof(ReduceAcc), cudaMemcpyDeviceToHost, c->stream));
+    ReduceAcc slots[kStatsSlots];
+    CUDA_TRY(c, cudaMemcpyAsync(slots, d->red, sizeof(slots), cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    ReduceAcc a = {0., 0., 0ull};
+    for (const ReduceAcc& s : slots) {
+        a.sumEnergy += s.sumEnergy;
+        a.sumRhoBar += s.sumRhoBar;
+        a.cells += s.cells;
+    }
     // computeAverage* over the cells of the lattice in the box (a sparse
     // domain's kept blocks)
     double cells = (double)a.cells;

@@ -183,11 +183,7 @@ __device__ __forceinline__ AxisMoves axisMoves(int p, int n, int per, long long 
 
 struct Neighbourhood {
     AxisMoves ax, ay, az;
-    const uint8_t* flags;   // non-null on a sparse domain: the cell kinds
-    long long idx;          // the cell
-    // Move by s * c_i; returns false when leaving a non-periodic domain or
-    // landing on a cell outside the lattice (a sparse domain treats the
-    // outside of its kept blocks like the outside of the domain).
+    // Move by s * c_i; returns false when leaving a non-periodic domain.
     __device__ __forceinline__ bool move(int i, int s, long long& off) const {
         int cx = s * cdir(i, 0), cy = s * cdir(i, 1), cz = s * cdir(i, 2);
         bool ok = true;
@@ -195,7 +191,6 @@ struct Neighbourhood {
         if (cx < 0) { ok &= ax.okM; off += ax.offM; } else if (cx > 0) { ok &= ax.okP; off += ax.offP; }
         if (cy < 0) { ok &= ay.okM; off += ay.offM; } else if (cy > 0) { ok &= ay.okP; off += ay.offP; }
         if (cz < 0) { ok &= az.okM; off += az.offM; } else if (cz > 0) { ok &= az.okP; off += az.offP; }
-        if (flags && ok && (cx | cy | cz) && flags[idx + off] == K_NONE) ok = false;
         return ok;
     }
 };
@@ -205,13 +200,24 @@ __device__ __forceinline__ Neighbourhood neighbourhood(const DevLattice& L, int 
     nb.ax = axisMoves(x, L.nx, L.per[0], (long long)L.ny * L.nz);
     nb.ay = axisMoves(y, L.ny, L.per[1], (long long)L.nz);
     nb.az = axisMoves(z, L.nz, L.per[2], 1);
-    nb.flags = L.sparse ? L.flags : nullptr;
-    nb.idx = ((long long)x * L.ny + y) * L.nz + z;
     return nb;
 }
 
+// The streaming move of cell idx: on a sparse domain a neighbour outside the
+// lattice counts like the outside of the domain (the domain-edge rule).
+// SPARSE = false compiles the check out (the step kernels of dense domains).
+template <bool SPARSE = true>
+__device__ __forceinline__ bool liveMove(const DevLattice& L, const Neighbourhood& nb, long long idx, int i, int s,
+                                         long long& off) {
+    bool ok = nb.move(i, s, off);
+    if constexpr (SPARSE) {
+        if (L.sparse && ok) ok = L.flags[idx + off] != K_NONE;
+    }
+    return ok;
+}
+
 // Read the 19 post-stream populations of cell idx for the given parity.
-template <typename S, bool ODD>
+template <typename S, bool ODD, bool SPARSE = true>
 __device__ __forceinline__ void loadCell(const DevLattice& L, const Neighbourhood& nb, long long idx,
                                          typename StoreT<S>::R* f) {
     const S* P = static_cast<const S*>(L.pop);
@@ -223,14 +229,14 @@ __device__ __forceinline__ void loadCell(const DevLattice& L, const Neighbourhoo
             f[i] = StoreT<S>::ld(P + i * st + idx);
         } else {
             long long off;
-            bool ok = nb.move(i, -1, off);
+            bool ok = liveMove<SPARSE>(L, nb, idx, i, -1, off);
             f[i] = ok ? StoreT<S>::ld(P + opp(i) * st + idx + off) : StoreT<S>::ld(P + i * st + idx);
         }
     }
 }
 
 // Write the 19 post-collision populations of cell idx for the given parity.
-template <typename S, bool ODD>
+template <typename S, bool ODD, bool SPARSE = true>
 __device__ __forceinline__ void storeCell(const DevLattice& L, const Neighbourhood& nb, long long idx,
                                           const typename StoreT<S>::R* f, unsigned salt) {
     S* P = static_cast<S*>(L.pop);
@@ -242,7 +248,7 @@ __device__ __forceinline__ void storeCell(const DevLattice& L, const Neighbourho
             StoreT<S>::st(P + opp(i) * st + idx, f[i], salt);
         } else {
             long long off;
-            bool ok = nb.move(i, +1, off);
+            bool ok = liveMove<SPARSE>(L, nb, idx, i, +1, off);
             if (ok) StoreT<S>::st(P + i * st + idx + off, f[i], salt);
             else StoreT<S>::st(P + opp(i) * st + idx, f[i], salt);
         }
@@ -255,7 +261,7 @@ template <bool ODD>
 __device__ __forceinline__ long long slotOf(const DevLattice& L, const Neighbourhood& nb, long long idx, int i) {
     if (!ODD || i == 0) return (long long)i * L.stride + idx;
     long long off;
-    bool ok = nb.move(i, -1, off);
+    bool ok = liveMove(L, nb, idx, i, -1, off);
     return ok ? (long long)opp(i) * L.stride + idx + off : (long long)i * L.stride + idx;
 }
 
@@ -297,8 +303,10 @@ __device__ __forceinline__ unsigned long long warpMaxU(unsigned long long v) {
     return v;
 }
 
-// One cell's collision; returns true when the cell gathers statistics.
-template <typename S>
+// One cell's collision; returns true when the cell gathers statistics.  EXT:
+// the external rho-bar / j form (a compile-time variant, so that the plain
+// step carries none of its code).
+template <typename S, bool EXT>
 __device__ __forceinline__ bool collideCell(const DevLattice& L, const StepParams<typename StoreT<S>::R>& P,
                                             long long idx, int k, typename StoreT<S>::R* f,
                                             typename StoreT<S>::R& rhoBar, typename StoreT<S>::R& uSqr,
@@ -306,7 +314,7 @@ __device__ __forceinline__ bool collideCell(const DevLattice& L, const StepParam
     using R = typename StoreT<S>::R;
     using F = typename StoreT<S>::F;
     R j[3];
-    if (P.external) {
+    if constexpr (EXT) {
         // ExternalRhoJcollideAndStream3D (dynamicsProcessor3D.hh:41-56):
         // Dynamics::collideExternal with the fields' rho-bar and j.  BGK (and
         // the BGK base of boundary cells) and IncBGK collide on the given
@@ -438,7 +446,7 @@ __device__ __forceinline__ void accumulateStats(bool gathers, double rhoBar, dou
 }
 
 // General cell update: any position, periodic wrap and the domain-edge rule.
-template <typename S, bool ODD, bool STATS>
+template <typename S, bool ODD, bool STATS, bool EXT, bool SPARSE>
 __device__ __forceinline__ bool processCellGeneral(const DevLattice& L, const StepParams<typename StoreT<S>::R>& P,
                                                    int x, int y, int z, StatsAcc* acc,
                                                    typename StoreT<S>::R& rhoBar, typename StoreT<S>::R& uSqr) {
@@ -448,10 +456,10 @@ __device__ __forceinline__ bool processCellGeneral(const DevLattice& L, const St
     if (k == K_NONE) return false;
     Neighbourhood nb = neighbourhood(L, x, y, z);
     R f[19];
-    loadCell<S, ODD>(L, nb, idx, f);
+    loadCell<S, ODD, SPARSE>(L, nb, idx, f);
     if (P.pending && isFace(k)) completeIfFace<R>(L, idx, k, f);
-    bool g = collideCell<S>(L, P, idx, k, f, rhoBar, uSqr, acc, STATS);
-    storeCell<S, ODD>(L, nb, idx, f, P.seed);
+    bool g = collideCell<S, EXT>(L, P, idx, k, f, rhoBar, uSqr, acc, STATS);
+    storeCell<S, ODD, SPARSE>(L, nb, idx, f, P.seed);
     return g;
 }
 
@@ -534,7 +542,7 @@ template <> struct RowShape<double> { static constexpr int cells = 1, blocks = 5
 // Rows with 1 <= x <= nx-2 and 1 <= y <= ny-2 (all z): nearly all of the time
 // step.  A block covers RowShape::cells * blockDim.x consecutive cells of one
 // row; thread t owns cells t, t + blockDim.x, ... (coalesced planes).
-template <typename S, bool ODD, bool STATS>
+template <typename S, bool ODD, bool STATS, bool EXT>
 __global__ void __launch_bounds__(128, RowShape<S>::blocks)
     rowStepKernel(DevLattice L, Planes<S> Pl, Deltas D, StepParams<typename StoreT<S>::R> P, StatsAcc* acc) {
     using R = typename StoreT<S>::R;
@@ -561,7 +569,7 @@ __global__ void __launch_bounds__(128, RowShape<S>::blocks)
         RowCell<S, ODD> rc(L, x, y, z0 + c * blockDim.x);
         R rhoBar = R(0), uSqr = R(0);
         if (P.pending && isFace(kind[c])) completeIfFace<R>(L, rc.idx, kind[c], f[c]);
-        bool g = collideCell<S>(L, P, rc.idx, kind[c], f[c], rhoBar, uSqr, acc, STATS);
+        bool g = collideCell<S, EXT>(L, P, rc.idx, kind[c], f[c], rhoBar, uSqr, acc, STATS);
         rc.store(Pl, D, f[c], P.seed);
         if (STATS && g) {
             sR += (double)rhoBar;
@@ -583,7 +591,7 @@ __global__ void __launch_bounds__(128, RowShape<S>::blocks)
 // the bytes per request; the other ten go as 16-bit values with the row-end
 // wrap / reflection selects of RowCell.  Needs nz even (rows and planes start
 // on 4-byte boundaries).
-template <typename S, bool ODD, bool STATS>
+template <typename S, bool ODD, bool STATS, bool EXT>
 __global__ void __launch_bounds__(128, 8)
     pairRowStepKernel(DevLattice L, Planes<S> Pl, Deltas D, StepParams<typename StoreT<S>::R> P, StatsAcc* acc) {
     using R = typename StoreT<S>::R;
@@ -621,11 +629,11 @@ __global__ void __launch_bounds__(128, 8)
         bool gA = false, gB = false;
         if (liveA) {
             if (P.pending && isFace(kA)) completeIfFace<R>(L, ca.idx, kA, fa);
-            gA = collideCell<S>(L, P, ca.idx, kA, fa, rbA, usA, acc, STATS);
+            gA = collideCell<S, EXT>(L, P, ca.idx, kA, fa, rbA, usA, acc, STATS);
         }
         if (liveB) {
             if (P.pending && isFace(kB)) completeIfFace<R>(L, cb.idx, kB, fb);
-            gB = collideCell<S>(L, P, cb.idx, kB, fb, rbB, usB, acc, STATS);
+            gB = collideCell<S, EXT>(L, P, cb.idx, kB, fb, rbB, usB, acc, STATS);
         }
         if (liveA && liveB) {
             StoreT<S>::st2(Pl.p[0] + ca.idx, fa[0], fb[0], P.seed);
@@ -673,7 +681,7 @@ __global__ void __launch_bounds__(128, 8)
 // blockIdx.y + gridDim.y * blockIdx.z enumerates the border rows: x = 0,
 // x = nx-1 (all y), then y = 0, y = ny-1 (1 <= x <= nx-2); when nx < 3 or
 // ny < 3, or on a sparse domain, every row is a border row.
-template <typename S, bool ODD, bool STATS>
+template <typename S, bool ODD, bool STATS, bool EXT, bool SPARSE>
 __global__ void __launch_bounds__(128) edgeRowStepKernel(DevLattice L, StepParams<typename StoreT<S>::R> P,
                                                           StatsAcc* acc, int rows) {
     using R = typename StoreT<S>::R;
@@ -682,7 +690,7 @@ __global__ void __launch_bounds__(128) edgeRowStepKernel(DevLattice L, StepParam
     if (row >= rows) return;   // whole blocks
     const int nx = L.nx, ny = L.ny;
     int x, y;
-    if (L.sparse || nx < 3 || ny < 3) {
+    if (SPARSE || nx < 3 || ny < 3) {
         x = row / ny;
         y = row - x * ny;
     } else if (row < ny) {
@@ -696,7 +704,7 @@ __global__ void __launch_bounds__(128) edgeRowStepKernel(DevLattice L, StepParam
     }
     R rhoBar = R(0), uSqr = R(0);
     bool g = false;
-    if (z < L.nz) g = processCellGeneral<S, ODD, STATS>(L, P, x, y, z, acc, rhoBar, uSqr);
+    if (z < L.nz) g = processCellGeneral<S, ODD, STATS, EXT, SPARSE>(L, P, x, y, z, acc, rhoBar, uSqr);
     accumulateStats<STATS>(g, (double)rhoBar, (double)uSqr, acc);
 }
 
@@ -1057,13 +1065,30 @@ __global__ void reduceKernel(DevLattice L, Box b, int pending, typename StoreT<S
             live = 1;
         }
     }
+    // block sum, then one set of atomics per block on slot block % kStatsSlots
+    __shared__ double shE[32], shR[32];
+    __shared__ unsigned long long shL[32];
     e = warpSum(e);
     r = warpSum(r);
     live = warpSumU(live);
-    if ((threadIdx.x & 31) == 0) {
-        atomicAdd(&acc->sumEnergy, e);
-        atomicAdd(&acc->sumRhoBar, r);
-        atomicAdd(&acc->cells, live);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
+    if (lane == 0) {
+        shE[w] = e;
+        shR[w] = r;
+        shL[w] = live;
+    }
+    __syncthreads();
+    if (w == 0) {
+        e = warpSum(lane < nw ? shE[lane] : 0.);
+        r = warpSum(lane < nw ? shR[lane] : 0.);
+        live = warpSumU(lane < nw ? shL[lane] : 0ull);
+        if (lane == 0) {
+            const unsigned b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+            ReduceAcc* a = acc + (b & (kStatsSlots - 1));
+            atomicAdd(&a->sumEnergy, e);
+            atomicAdd(&a->sumRhoBar, r);
+            atomicAdd(&a->cells, live);
+        }
     }
 }
 

@@ -17,7 +17,7 @@ struct StepLaunch {
     // when rows have an even length, the one-cell register kernel otherwise.
     static bool pairedRows(const DevLattice& L) { return sizeof(S) == 2 && L.nz % 2 == 0; }
 
-    template <bool ODD, bool STATS>
+    template <bool ODD, bool STATS, bool EXT>
     static int stepSplit(const DevLattice& L, const StepParams<R>& p, StatsAcc* acc, cudaStream_t s) {
         int launched = 0;
         // A sparse domain runs every row through the general addressing,
@@ -35,7 +35,7 @@ struct StepLaunch {
                 const int pairs = L.nz / 2;
                 int tpb = (pairs + 31) / 32 * 32;
                 tpb = tpb < kBlock ? tpb : kBlock;
-                pairRowStepKernel<S, ODD, STATS><<<rowGrid(pairs, L.ny - 2, L.nx - 2, tpb), tpb, 0, s>>>(L, pl, d, p,
+                pairRowStepKernel<S, ODD, STATS, EXT><<<rowGrid(pairs, L.ny - 2, L.nx - 2, tpb), tpb, 0, s>>>(L, pl, d, p,
                                                                                                       acc);
                 ++launched;
             }
@@ -51,12 +51,15 @@ struct StepLaunch {
             constexpr int NC = RowShape<S>::cells;
             int tpb = ((L.nz + NC - 1) / NC + 31) / 32 * 32;
             tpb = tpb < kBlock ? tpb : kBlock;
-            rowStepKernel<S, ODD, STATS><<<rowGrid(L.nz, L.ny - 2, L.nx - 2, tpb * NC), tpb, 0, s>>>(L, pl, d, p, acc);
+            rowStepKernel<S, ODD, STATS, EXT><<<rowGrid(L.nz, L.ny - 2, L.nx - 2, tpb * NC), tpb, 0, s>>>(L, pl, d, p, acc);
             ++launched;
         }
         const int gy = edgeRows < 65535 ? edgeRows : 65535;
         dim3 g((unsigned)((L.nz + kBlock - 1) / kBlock), (unsigned)gy, (unsigned)((edgeRows + gy - 1) / gy));
-        edgeRowStepKernel<S, ODD, STATS><<<g, kBlock, 0, s>>>(L, p, acc, edgeRows);
+        if (L.sparse)
+            edgeRowStepKernel<S, ODD, STATS, EXT, true><<<g, kBlock, 0, s>>>(L, p, acc, edgeRows);
+        else
+            edgeRowStepKernel<S, ODD, STATS, EXT, false><<<g, kBlock, 0, s>>>(L, p, acc, edgeRows);
         return launched + 1;
     }
 
@@ -65,8 +68,11 @@ struct StepLaunch {
 template <typename S, bool ODD>
 int stepParity(const DevLattice& L, bool stats, const StepParams<typename StoreT<S>::R>& p, StatsAcc* acc,
                cudaStream_t s) {
-    return stats ? StepLaunch<S>::template stepSplit<ODD, true>(L, p, acc, s)
-                 : StepLaunch<S>::template stepSplit<ODD, false>(L, p, acc, s);
+    if (p.external)
+        return stats ? StepLaunch<S>::template stepSplit<ODD, true, true>(L, p, acc, s)
+                     : StepLaunch<S>::template stepSplit<ODD, false, true>(L, p, acc, s);
+    return stats ? StepLaunch<S>::template stepSplit<ODD, true, false>(L, p, acc, s)
+                 : StepLaunch<S>::template stepSplit<ODD, false, false>(L, p, acc, s);
 }
 
 }  // namespace plbgpu
