@@ -78,6 +78,7 @@ struct Domain {
 struct plbgpu_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    SideStream side = {nullptr, nullptr, nullptr};   // border rows of a step run here
     std::string lastError;
     std::map<int, std::unique_ptr<Domain>> domains;
     int nextHandle = 0;
@@ -541,6 +542,15 @@ int plbgpu_create(int device, plbgpu_ctx** out) {
         delete c;
         return PLBGPU_ERR_CUDA;
     }
+    if (cudaStreamCreateWithFlags(&c->side.stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->side.fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->side.join, cudaEventDisableTiming) != cudaSuccess) {
+        if (c->side.stream) cudaStreamDestroy(c->side.stream);
+        if (c->side.fork) cudaEventDestroy(c->side.fork);
+        cudaStreamDestroy(c->stream);
+        delete c;
+        return PLBGPU_ERR_CUDA;
+    }
     *out = c;
     return PLBGPU_OK;
 }
@@ -553,6 +563,10 @@ int plbgpu_destroy(plbgpu_ctx* c) {
     for (auto& kv : c->domains) hs.push_back(kv.first);
     for (int h : hs) plbgpu_remove_domain(c, h);
     if (c->staging) cudaFree(c->staging);
+    cudaStreamSynchronize(c->side.stream);
+    cudaEventDestroy(c->side.fork);
+    cudaEventDestroy(c->side.join);
+    cudaStreamDestroy(c->side.stream);
     cudaStreamDestroy(c->stream);
     delete c;
     return PLBGPU_OK;
@@ -981,7 +995,7 @@ int plbgpu_collide_and_stream(plbgpu_ctx* c, int h, int nsteps, int collect_stat
         bool stats = collect_stats && s == nsteps - 1;
         if (stats) CUDA_TRY(c, cudaMemsetAsync(d->stats, 0, sizeof(StatsAcc) * kStatsSlots, c->stream));
         StepConsts k = consts(d);
-        int nl = L.step(d->view(), d->odd, stats, k, d->stats, c->stream);
+        int nl = L.step(d->view(), d->odd, stats, k, d->stats, c->stream, &c->side);
         c->launches += nl - 1;
         if ((rc = launchBox(c))) return rc;
         d->odd = !d->odd;
@@ -1148,7 +1162,7 @@ int plbgpu_collide_and_stream_external(plbgpu_ctx* c, int h, int nsteps, int rec
         if (stats) CUDA_TRY(c, cudaMemsetAsync(d->stats, 0, sizeof(StatsAcc) * kStatsSlots, c->stream));
         StepConsts k = consts(d);
         k.external = 1;
-        int nl = L.step(d->view(), d->odd, stats, k, d->stats, c->stream);
+        int nl = L.step(d->view(), d->odd, stats, k, d->stats, c->stream, &c->side);
         c->launches += nl - 1;
         if ((rc = launchBox(c))) return rc;
         d->odd = !d->odd;

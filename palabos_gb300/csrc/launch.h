@@ -18,9 +18,18 @@ struct StepConsts {
     int external;   // collide with the external rho-bar / j planes (DevLattice::ext)
 };
 
+// A second stream for the border rows of a step: they touch no population
+// slot of the interior rows in the same step, so the two kernels run
+// concurrently (fork and join through the two events).
+struct SideStream {
+    cudaStream_t stream;
+    cudaEvent_t fork, join;
+};
+
 // Each launcher returns the number of kernels it launched.
 struct Launchers {
-    int (*step)(const DevLattice&, bool odd, bool stats, const StepConsts&, StatsAcc*, cudaStream_t);
+    int (*step)(const DevLattice&, bool odd, bool stats, const StepConsts&, StatsAcc*, cudaStream_t,
+                const SideStream*);
     int (*completeFaces)(const DevLattice&, bool odd, cudaStream_t);
     int (*extract)(const DevLattice&, bool odd, Box, int pending, double* out, cudaStream_t);
     int (*insert)(const DevLattice&, bool odd, Box, const double* in, cudaStream_t);

@@ -46,7 +46,7 @@ __global__ void equilibriumKernel(DevLattice L, Box b, const double* rhou, doubl
 // costliest code to compile, build in parallel.
 template <typename S, bool ODD>
 int stepParity(const DevLattice& L, bool stats, const StepParams<typename StoreT<S>::R>& p, StatsAcc* acc,
-               cudaStream_t s);
+               cudaStream_t s, const SideStream* side);
 
 template <typename S>
 struct LaunchImpl {
@@ -54,7 +54,7 @@ struct LaunchImpl {
     static constexpr int kBlock = 128;
 
     static int step(const DevLattice& L, bool odd, bool stats, const StepConsts& c, StatsAcc* acc,
-                    cudaStream_t s) {
+                    cudaStream_t s, const SideStream* side) {
         StepParams<R> p;
         p.bgk.omega = (R)c.omega;
         p.bgk.one_m_omega = (R)c.one_m_omega;
@@ -65,7 +65,7 @@ struct LaunchImpl {
         p.pending = c.pending;
         p.seed = c.seed;
         p.external = c.external;
-        return odd ? stepParity<S, true>(L, stats, p, acc, s) : stepParity<S, false>(L, stats, p, acc, s);
+        return odd ? stepParity<S, true>(L, stats, p, acc, s, side) : stepParity<S, false>(L, stats, p, acc, s, side);
     }
     static int completeFaces(const DevLattice& L, bool odd, cudaStream_t s) {
         dim3 g = rowGrid(L.nz, L.ny, L.nx, kBlock);

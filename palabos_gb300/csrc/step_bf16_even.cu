@@ -3,5 +3,5 @@
 
 namespace plbgpu {
 template int stepParity<__nv_bfloat16, false>(const DevLattice&, bool, const StepParams<StoreT<__nv_bfloat16>::R>&, StatsAcc*,
-                                        cudaStream_t);
+                                        cudaStream_t, const SideStream*);
 }  // namespace plbgpu

@@ -3,5 +3,5 @@
 
 namespace plbgpu {
 template int stepParity<bf16sr, true>(const DevLattice&, bool, const StepParams<StoreT<bf16sr>::R>&, StatsAcc*,
-                                        cudaStream_t);
+                                        cudaStream_t, const SideStream*);
 }  // namespace plbgpu

@@ -3,5 +3,5 @@
 
 namespace plbgpu {
 template int stepParity<__half, false>(const DevLattice&, bool, const StepParams<StoreT<__half>::R>&, StatsAcc*,
-                                        cudaStream_t);
+                                        cudaStream_t, const SideStream*);
 }  // namespace plbgpu

@@ -3,5 +3,5 @@
 
 namespace plbgpu {
 template int stepParity<float, true>(const DevLattice&, bool, const StepParams<StoreT<float>::R>&, StatsAcc*,
-                                        cudaStream_t);
+                                        cudaStream_t, const SideStream*);
 }  // namespace plbgpu

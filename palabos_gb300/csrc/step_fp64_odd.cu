@@ -3,5 +3,5 @@
 
 namespace plbgpu {
 template int stepParity<double, true>(const DevLattice&, bool, const StepParams<StoreT<double>::R>&, StatsAcc*,
-                                        cudaStream_t);
+                                        cudaStream_t, const SideStream*);
 }  // namespace plbgpu

@@ -18,12 +18,25 @@ struct StepLaunch {
     static bool pairedRows(const DevLattice& L) { return sizeof(S) == 2 && L.nz % 2 == 0; }
 
     template <bool ODD, bool STATS, bool EXT>
-    static int stepSplit(const DevLattice& L, const StepParams<R>& p, StatsAcc* acc, cudaStream_t s) {
+    static int stepSplit(const DevLattice& L, const StepParams<R>& p, StatsAcc* acc, cudaStream_t s,
+                         const SideStream* side) {
         int launched = 0;
         // A sparse domain runs every row through the general addressing,
         // which checks each neighbour's kind.
         const bool general = L.sparse || L.nx < 3 || L.ny < 3;
         const int edgeRows = general ? L.nx * L.ny : 2 * L.ny + 2 * (L.nx - 2);
+        // Border rows first, on the side stream when there is one.
+        cudaStream_t es = s;
+        if (side && !general && cudaEventRecord(side->fork, s) == cudaSuccess &&
+            cudaStreamWaitEvent(side->stream, side->fork, 0) == cudaSuccess)
+            es = side->stream;
+        const int gy = edgeRows < 65535 ? edgeRows : 65535;
+        dim3 g((unsigned)((L.nz + kBlock - 1) / kBlock), (unsigned)gy, (unsigned)((edgeRows + gy - 1) / gy));
+        if (L.sparse)
+            edgeRowStepKernel<S, ODD, STATS, EXT, true><<<g, kBlock, 0, es>>>(L, p, acc, edgeRows);
+        else
+            edgeRowStepKernel<S, ODD, STATS, EXT, false><<<g, kBlock, 0, es>>>(L, p, acc, edgeRows);
+        ++launched;
         if (!general && pairedRows(L)) {
             Planes<S> pl;
             Deltas d;
@@ -54,25 +67,23 @@ struct StepLaunch {
             rowStepKernel<S, ODD, STATS, EXT><<<rowGrid(L.nz, L.ny - 2, L.nx - 2, tpb * NC), tpb, 0, s>>>(L, pl, d, p, acc);
             ++launched;
         }
-        const int gy = edgeRows < 65535 ? edgeRows : 65535;
-        dim3 g((unsigned)((L.nz + kBlock - 1) / kBlock), (unsigned)gy, (unsigned)((edgeRows + gy - 1) / gy));
-        if (L.sparse)
-            edgeRowStepKernel<S, ODD, STATS, EXT, true><<<g, kBlock, 0, s>>>(L, p, acc, edgeRows);
-        else
-            edgeRowStepKernel<S, ODD, STATS, EXT, false><<<g, kBlock, 0, s>>>(L, p, acc, edgeRows);
-        return launched + 1;
+        if (es != s) {   // join: the next step waits for both kernels
+            if (cudaEventRecord(side->join, es) != cudaSuccess || cudaStreamWaitEvent(s, side->join, 0) != cudaSuccess)
+                cudaStreamSynchronize(es);
+        }
+        return launched;
     }
 
 };
 
 template <typename S, bool ODD>
 int stepParity(const DevLattice& L, bool stats, const StepParams<typename StoreT<S>::R>& p, StatsAcc* acc,
-               cudaStream_t s) {
+               cudaStream_t s, const SideStream* side) {
     if (p.external)
-        return stats ? StepLaunch<S>::template stepSplit<ODD, true, true>(L, p, acc, s)
-                     : StepLaunch<S>::template stepSplit<ODD, false, true>(L, p, acc, s);
-    return stats ? StepLaunch<S>::template stepSplit<ODD, true, false>(L, p, acc, s)
-                 : StepLaunch<S>::template stepSplit<ODD, false, false>(L, p, acc, s);
+        return stats ? StepLaunch<S>::template stepSplit<ODD, true, true>(L, p, acc, s, side)
+                     : StepLaunch<S>::template stepSplit<ODD, false, true>(L, p, acc, s, side);
+    return stats ? StepLaunch<S>::template stepSplit<ODD, true, false>(L, p, acc, s, side)
+                 : StepLaunch<S>::template stepSplit<ODD, false, false>(L, p, acc, s, side);
 }
 
 }  // namespace plbgpu
