@@ -274,6 +274,19 @@ int plbgpu_collide_and_stream_external(plbgpu_ctx* ctx, int handle, int nsteps, 
 int plbgpu_save_binary_block(plbgpu_ctx* ctx, int handle, int what, const char* path, int enforce_uint);
 int plbgpu_load_binary_block(plbgpu_ctx* ctx, int handle, int what, const char* path, int enforce_uint);
 
+/* parallelIO::save(block, base, false) / parallelIO::load(plb, block, false)
+ * -- the files of saveState / loadState (io/utilIO_3D.cpp:45-75,
+ * io/multiBlockWriter3D.cpp:53-137, 201-213, io/multiBlockReader3D.cpp:135-270):
+ * <base>.dat holds the raw cell records of each component (x-major, z
+ * fastest, no header) and <base>.plb their XML description (block family,
+ * descriptor, cell size, bounding box, components, byte offsets, data file).
+ * Save writes one component, the whole domain; load accepts any number of
+ * components (the reference writes one per block) with a bounding box of the
+ * domain's size.  Static content only: a state saved with dynamic content
+ * (dynamics objects) is refused. */
+int plbgpu_save_state(plbgpu_ctx* ctx, int handle, int what, const char* base);
+int plbgpu_load_state(plbgpu_ctx* ctx, int handle, int what, const char* plb_path);
+
 /* ------------------------------------------------------------ adjoint */
 
 /* Discrete adjoint of the collide-and-stream step (no counterpart in the

@@ -200,3 +200,26 @@ def sparse_cell_mask(shape, blocks, keep):
                     mask[r[0][ix]:r[0][ix + 1], r[1][iy]:r[1][iy + 1], r[2][iz]:r[2][iz + 1]] = True
     return mask
 
+
+def state_files(records, shape, cell_dim, family, descriptor, dat_name):
+    """parallelIO::save(block, base, false) of a block as one component, the
+    whole bounding box: the description (<base>.plb, in the layout of the
+    reference's XML writer: io/multiBlockWriter3D.cpp:53-137,
+    libraryInterfaces/TINYXML_xmlIO.hh:229-272) and the raw records
+    (<base>.dat: cells x-major, z fastest, `cell_dim` float64 each, no header;
+    io/mpiParallelIO.cpp:92-150).  Returns (plb text, dat bytes)."""
+    data = np.ascontiguousarray(records, dtype="<f8").tobytes()
+    nx, ny, nz = shape
+    box = f"0 {nx - 1} 0 {ny - 1} 0 {nz - 1}"
+    lines = ['<?xml version="1.0" ?>', "<Block3D>", "    <General>",
+             f"        <Family> {family} </Family>", "        <Datatype> double </Datatype>"]
+    if descriptor:
+        lines.append(f"        <Descriptor> {descriptor} </Descriptor>")
+    lines += [f"        <cellDim> {cell_dim} </cellDim>", "        <dynamicContent> False </dynamicContent>",
+              "        <globalId> 0 </globalId>", "    </General>", "    <Structure>",
+              f"        <BoundingBox> {box} </BoundingBox>", "        <EnvelopeWidth> 1 </EnvelopeWidth>",
+              "        <GridLevel> 0 </GridLevel>", "        <NumComponents> 1 </NumComponents>", "    </Structure>",
+              "    <Data>", f"        <File> {dat_name} </File>", f"        <Component> {box} </Component>",
+              f"        <Offsets> {len(data)} </Offsets>", "    </Data>", "</Block3D>", ""]
+    return "\n".join(lines), data
+

@@ -65,8 +65,10 @@ enum {
     OPT_SAVE_BINARY = 4,     // after the run, saveBinaryBlock of the lattice, of
                              // computeDensity and of computeVelocity into
                              // <result>.lattice / .density / .velocity
-    OPT_SPARSE = 8           // build the lattice on computeSparseManagement of the
+    OPT_SPARSE = 8,          // build the lattice on computeSparseManagement of the
                              // given int field over the regular block distribution
+    OPT_SAVE_STATE = 16      // after the run, parallelIO::save(lattice, <base>_state, false)
+                             // with <base> the result path without its extension
 };
 
 struct Case {

@@ -289,6 +289,10 @@ int run(const Case& c, const char* outPath) {
             }
     if (!(c.options & OPT_NO_INITIALIZE)) lat.initialize();
 
+    // With PLB_LOAD_STATE=<base>: the populations come from a saved state
+    // (parallelIO::load of <base>.plb / <base>.dat, static content).
+    if (const char* lpath = std::getenv("PLB_LOAD_STATE")) parallelIO::load(lpath, lat, false);
+
     std::vector<double> fInit, fFinal;
     dumpPopulations(lat, c, fInit);
 
@@ -364,6 +368,12 @@ int run(const Case& c, const char* outPath) {
     dumpPopulations(lat, c, fFinal);
     double energy = computeAverageEnergy(lat);
     double density = computeAverageDensity(lat);
+    if (c.options & OPT_SAVE_STATE) {   // <result without extension>_state.plb / .dat
+        std::string base(outPath);
+        const size_t slash = base.rfind('/'), dot = base.rfind('.');
+        if (dot != std::string::npos && (slash == std::string::npos || dot > slash)) base.erase(dot);
+        parallelIO::save(lat, base + "_state", false);
+    }
     if (c.options & OPT_SAVE_BINARY) {
         std::string base(outPath);
         saveBinaryBlock(lat, base + ".lattice");

@@ -1268,6 +1268,83 @@ int slabPlanes(const Domain* d, int w) {
     return (int)(p < 1 ? 1 : (p > d->nx ? d->nx : p));
 }
 
+// Records of box b (one cell after another, x-major, z fastest) into k.rec.
+int buildRecords(plbgpu_ctx* c, Domain* d, int what, const Box& b, Ckpt& k) {
+    const Launchers& L = launchers(d->precision);
+    const int pending = d->pending && d->bc ? 1 : 0;
+    const int w = blockWidth(what);
+    const long long cells = boxCells(b);
+    int nl = 1, rc;
+    if (what == PLBGPU_BLOCK_LATTICE) {
+        nl = L.extract(d->view(), d->odd, b, pending, k.rec, c->stream);
+    } else if (what == PLBGPU_BLOCK_FORCED_LATTICE) {
+        nl = L.extract(d->view(), d->odd, b, pending, k.tmp, c->stream);
+        launchColumns(k.tmp, 19, 0, 19, k.rec, 22, 0, cells, c->stream);
+        dim3 g = rowGrid(b.z1 - b.z0 + 1, b.y1 - b.y0 + 1, b.x1 - b.x0 + 1, 128);
+        if (!d->force)
+            CUDA_TRY(c, cudaMemsetAsync(k.tmp, 0, sizeof(double) * 3 * cells, c->stream));
+        else if (d->precision == PLBGPU_FP64)
+            boxPlanesKernel<double, double><<<g, 128, 0, c->stream>>>(static_cast<double*>(d->force), d->n, d->ny,
+                                                                      d->nz, b, k.tmp, 3, 1);
+        else
+            boxPlanesKernel<float, double><<<g, 128, 0, c->stream>>>(static_cast<float*>(d->force), d->n, d->ny,
+                                                                     d->nz, b, k.tmp, 3, 1);
+        launchColumns(k.tmp, 3, 0, 3, k.rec, 22, 19, cells, c->stream);
+        nl = 4;
+    } else if (what == PLBGPU_BLOCK_DENSITY || what == PLBGPU_BLOCK_VELOCITY) {
+        nl = L.field(d->view(), d->odd, b, pending, (double)1 / d->rho0, d->bbRho,
+                     what == PLBGPU_BLOCK_DENSITY ? 1 : 0, k.rec, c->stream);
+    } else {
+        if ((rc = extBox(c, d, b, k.tmp, 1))) return rc;
+        launchColumns(k.tmp, 4, what == PLBGPU_BLOCK_RHOBAR ? 0 : 1, w, k.rec, w, 0, cells, c->stream);
+        nl = 1;
+    }
+    c->launches += nl - 1;
+    return launchBox(c);
+}
+
+// The records in k.rec become the contents of box b.
+int applyRecords(plbgpu_ctx* c, Domain* d, int what, const Box& b, Ckpt& k) {
+    const Launchers& L = launchers(d->precision);
+    const int w = blockWidth(what);
+    const long long cells = boxCells(b);
+    int nl = 1;
+    dim3 g = rowGrid(b.z1 - b.z0 + 1, b.y1 - b.y0 + 1, b.x1 - b.x0 + 1, 128);
+    if (what == PLBGPU_BLOCK_LATTICE) {
+        nl = L.insert(d->view(), d->odd, b, k.rec, c->stream);
+    } else if (what == PLBGPU_BLOCK_FORCED_LATTICE) {
+        launchColumns(k.rec, 22, 0, 19, k.tmp, 19, 0, cells, c->stream);
+        nl = L.insert(d->view(), d->odd, b, k.tmp, c->stream);
+        launchColumns(k.rec, 22, 19, 3, k.tmp, 3, 0, cells, c->stream);
+        if (d->precision == PLBGPU_FP64)
+            boxPlanesKernel<double, double><<<g, 128, 0, c->stream>>>(static_cast<double*>(d->force), d->n, d->ny,
+                                                                      d->nz, b, k.tmp, 3, 0);
+        else
+            boxPlanesKernel<float, double><<<g, 128, 0, c->stream>>>(static_cast<float*>(d->force), d->n, d->ny,
+                                                                     d->nz, b, k.tmp, 3, 0);
+        nl += 3;
+    } else {
+        const long long off = what == PLBGPU_BLOCK_RHOBAR ? 0 : d->n;
+        if (d->precision == PLBGPU_FP64)
+            boxPlanesKernel<double, double><<<g, 128, 0, c->stream>>>(static_cast<double*>(d->ext) + off, d->n, d->ny,
+                                                                      d->nz, b, k.rec, w, 0);
+        else
+            boxPlanesKernel<float, double><<<g, 128, 0, c->stream>>>(static_cast<float*>(d->ext) + off, d->n, d->ny,
+                                                                     d->nz, b, k.rec, w, 0);
+    }
+    c->launches += nl - 1;
+    return launchBox(c);
+}
+
+// What a load into `what` needs allocated, after the pending faces are done.
+int prepareLoad(plbgpu_ctx* c, Domain* d, int what) {
+    int rc;
+    if ((rc = materialize(c, d))) return rc;
+    if (what == PLBGPU_BLOCK_FORCED_LATTICE && (rc = ensureAux(c, d, false, true, false))) return rc;
+    if ((what == PLBGPU_BLOCK_RHOBAR || what == PLBGPU_BLOCK_J) && (rc = ensureExt(c, d))) return rc;
+    return PLBGPU_OK;
+}
+
 }  // namespace
 
 int plbgpu_save_binary_block(plbgpu_ctx* c, int h, int what, const char* path, int enforce_uint) {
@@ -1297,40 +1374,12 @@ int plbgpu_save_binary_block(plbgpu_ctx* c, int h, int what, const char* path, i
     Ckpt k;
     if ((rc = ckptAlloc(c, k, (long long)planes * d->ny * d->nz, w))) return rc;
     std::vector<char> text;
-    const Launchers& L = launchers(d->precision);
-    const int pending = d->pending && d->bc ? 1 : 0;
     int headLen = 0;
     for (int x0 = 0; x0 < d->nx; x0 += planes) {
         const int x1 = x0 + planes - 1 < d->nx - 1 ? x0 + planes - 1 : d->nx - 1;
         Box b{x0, x1, 0, d->ny - 1, 0, d->nz - 1};
         const long long cells = boxCells(b);
-        int nl = 1;
-        if (what == PLBGPU_BLOCK_LATTICE) {
-            nl = L.extract(d->view(), d->odd, b, pending, k.rec, c->stream);
-        } else if (what == PLBGPU_BLOCK_FORCED_LATTICE) {
-            nl = L.extract(d->view(), d->odd, b, pending, k.tmp, c->stream);
-            launchColumns(k.tmp, 19, 0, 19, k.rec, 22, 0, cells, c->stream);
-            dim3 g = rowGrid(d->nz, d->ny, x1 - x0 + 1, 128);
-            if (!d->force)
-                CUDA_TRY(c, cudaMemsetAsync(k.tmp, 0, sizeof(double) * 3 * cells, c->stream));
-            else if (d->precision == PLBGPU_FP64)
-                boxPlanesKernel<double, double><<<g, 128, 0, c->stream>>>(static_cast<double*>(d->force), d->n, d->ny,
-                                                                          d->nz, b, k.tmp, 3, 1);
-            else
-                boxPlanesKernel<float, double><<<g, 128, 0, c->stream>>>(static_cast<float*>(d->force), d->n, d->ny,
-                                                                         d->nz, b, k.tmp, 3, 1);
-            launchColumns(k.tmp, 3, 0, 3, k.rec, 22, 19, cells, c->stream);
-            nl = 4;
-        } else if (what == PLBGPU_BLOCK_DENSITY || what == PLBGPU_BLOCK_VELOCITY) {
-            nl = L.field(d->view(), d->odd, b, pending, (double)1 / d->rho0, d->bbRho,
-                         what == PLBGPU_BLOCK_DENSITY ? 1 : 0, k.rec, c->stream);
-        } else {
-            if ((rc = extBox(c, d, b, k.tmp, 1))) return rc;
-            launchColumns(k.tmp, 4, what == PLBGPU_BLOCK_RHOBAR ? 0 : 1, w, k.rec, w, 0, cells, c->stream);
-            nl = 1;
-        }
-        c->launches += nl - 1;
-        if ((rc = launchBox(c))) return rc;
+        if ((rc = buildRecords(c, d, what, b, k))) return rc;
         const size_t bodyLen = (size_t)cells * w * sizeof(double);
         const size_t total = (size_t)headLen + bodyLen;
         const bool last = x1 == d->nx - 1;
@@ -1394,13 +1443,10 @@ int plbgpu_load_binary_block(plbgpu_ctx* c, int h, int what, const char* path, i
     if (size != want)
         return fail(c, PLBGPU_ERR_ARG, "%s holds %llu bytes, the %dx%dx%d domain needs %llu", path, size, d->nx, d->ny,
                     d->nz, want);
-    if ((rc = materialize(c, d))) return rc;
-    if (what == PLBGPU_BLOCK_FORCED_LATTICE && (rc = ensureAux(c, d, false, true, false))) return rc;
-    if ((what == PLBGPU_BLOCK_RHOBAR || what == PLBGPU_BLOCK_J) && (rc = ensureExt(c, d))) return rc;
+    if ((rc = prepareLoad(c, d, what))) return rc;
     const int planes = slabPlanes(d, w);
     Ckpt k;
     if ((rc = ckptAlloc(c, k, (long long)planes * d->ny * d->nz, w))) return rc;
-    const Launchers& L = launchers(d->precision);
     const unsigned long long totalQuads = (size + 2) / 3;
     std::vector<char> text;
     for (int x0 = 0; x0 < d->nx; x0 += planes) {
@@ -1424,34 +1470,213 @@ int plbgpu_load_binary_block(plbgpu_ctx* c, int h, int what, const char* path, i
         CUDA_TRY(c, cudaMemcpyAsync(&bad, k.bad, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
         CUDA_TRY(c, cudaStreamSynchronize(c->stream));
         if (bad) return fail(c, PLBGPU_ERR_ARG, "%s: not base64 data", path);
-        int nl = 1;
-        dim3 g = rowGrid(d->nz, d->ny, x1 - x0 + 1, 128);
-        if (what == PLBGPU_BLOCK_LATTICE) {
-            nl = L.insert(d->view(), d->odd, b, k.rec, c->stream);
-        } else if (what == PLBGPU_BLOCK_FORCED_LATTICE) {
-            launchColumns(k.rec, 22, 0, 19, k.tmp, 19, 0, cells, c->stream);
-            nl = L.insert(d->view(), d->odd, b, k.tmp, c->stream);
-            launchColumns(k.rec, 22, 19, 3, k.tmp, 3, 0, cells, c->stream);
-            if (d->precision == PLBGPU_FP64)
-                boxPlanesKernel<double, double><<<g, 128, 0, c->stream>>>(static_cast<double*>(d->force), d->n, d->ny,
-                                                                          d->nz, b, k.tmp, 3, 0);
-            else
-                boxPlanesKernel<float, double><<<g, 128, 0, c->stream>>>(static_cast<float*>(d->force), d->n, d->ny,
-                                                                         d->nz, b, k.tmp, 3, 0);
-            nl += 3;
-        } else {
-            const long long off = what == PLBGPU_BLOCK_RHOBAR ? 0 : d->n;
-            if (d->precision == PLBGPU_FP64)
-                boxPlanesKernel<double, double><<<g, 128, 0, c->stream>>>(static_cast<double*>(d->ext) + off, d->n,
-                                                                          d->ny, d->nz, b, k.rec, w, 0);
-            else
-                boxPlanesKernel<float, double><<<g, 128, 0, c->stream>>>(static_cast<float*>(d->ext) + off, d->n,
-                                                                         d->ny, d->nz, b, k.rec, w, 0);
-        }
-        c->launches += nl - 1;
-        if ((rc = launchBox(c))) return rc;
+        if ((rc = applyRecords(c, d, what, b, k))) return rc;
     }
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if (what == PLBGPU_BLOCK_LATTICE || what == PLBGPU_BLOCK_FORCED_LATTICE) d->statsValid = false;
+    return PLBGPU_OK;
+}
+
+// ------------------------------------------------------------ parallel-I/O states
+
+namespace {
+
+// Family, descriptor and cell size of a block kind as parallelIO::save
+// describes it (io/multiBlockWriter3D.cpp:53-137).
+void stateTypeInfo(int what, const char** family, const char** descriptor) {
+    switch (what) {
+    case PLBGPU_BLOCK_LATTICE: *family = "BlockLattice3D"; *descriptor = "D3Q19"; return;
+    case PLBGPU_BLOCK_FORCED_LATTICE: *family = "BlockLattice3D"; *descriptor = "ForcedD3Q19"; return;
+    case PLBGPU_BLOCK_DENSITY: case PLBGPU_BLOCK_RHOBAR: *family = "ScalarField3D"; *descriptor = nullptr; return;
+    default: *family = "TensorField3D"; *descriptor = nullptr; return;
+    }
+}
+
+// Text of the first <tag ...> ... </tag> element at or after `from` (attributes
+// allowed); npos when absent.  `next` receives the position after it.
+size_t xmlElement(const std::string& doc, const std::string& tag, size_t from, std::string& text, size_t* next) {
+    size_t a = from;
+    while ((a = doc.find("<" + tag, a)) != std::string::npos) {
+        const char after = a + 1 + tag.size() < doc.size() ? doc[a + 1 + tag.size()] : '\0';
+        if (after == '>' || after == ' ') break;
+        a += 1;
+    }
+    if (a == std::string::npos) return a;
+    const size_t open = doc.find('>', a);
+    const size_t close = doc.find("</" + tag + ">", open);
+    if (open == std::string::npos || close == std::string::npos) return std::string::npos;
+    text = doc.substr(open + 1, close - open - 1);
+    if (next) *next = close + tag.size() + 3;
+    return a;
+}
+
+bool parseLongs(const std::string& text, std::vector<long long>& out) {
+    out.clear();
+    const char* p = text.c_str();
+    while (*p) {
+        while (*p == ' ' || *p == '\n' || *p == '\t' || *p == '\r') ++p;
+        if (!*p) break;
+        char* e = nullptr;
+        long long v = strtoll(p, &e, 10);
+        if (e == p) return false;
+        out.push_back(v);
+        p = e;
+    }
+    return true;
+}
+
+}  // namespace
+
+int plbgpu_save_state(plbgpu_ctx* c, int h, int what, const char* base) {
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    const int w = blockWidth(what);
+    if (!w) return fail(c, PLBGPU_ERR_ARG, "unknown block kind %d", what);
+    if (!base) return fail(c, PLBGPU_ERR_ARG, "null path");
+    if ((what == PLBGPU_BLOCK_RHOBAR || what == PLBGPU_BLOCK_J) && !d->ext)
+        return fail(c, PLBGPU_ERR_STATE, "no rho-bar/j fields to save");
+    if ((rc = checkStatus(c, d))) return rc;
+    const std::string datName = std::string(base) + ".dat", plbName = std::string(base) + ".plb";
+    // Raw records of the one component, the whole bounding box
+    // (writeRawData, io/mpiParallelIO.cpp:92-150).
+    {
+        FileCloser fc{fopen(datName.c_str(), "wb")};
+        if (!fc.f) return fail(c, PLBGPU_ERR_ARG, "cannot open %s for writing", datName.c_str());
+        const int planes = slabPlanes(d, w);
+        Ckpt k;
+        if ((rc = ckptAlloc(c, k, (long long)planes * d->ny * d->nz, w))) return rc;
+        std::vector<char> host;
+        for (int x0 = 0; x0 < d->nx; x0 += planes) {
+            const int x1 = x0 + planes - 1 < d->nx - 1 ? x0 + planes - 1 : d->nx - 1;
+            Box b{x0, x1, 0, d->ny - 1, 0, d->nz - 1};
+            if ((rc = buildRecords(c, d, what, b, k))) return rc;
+            host.resize((size_t)boxCells(b) * w * sizeof(double));
+            CUDA_TRY(c, cudaMemcpyAsync(host.data(), k.rec, host.size(), cudaMemcpyDeviceToHost, c->stream));
+            CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+            if (fwrite(host.data(), 1, host.size(), fc.f) != host.size())
+                return fail(c, PLBGPU_ERR_ARG, "write to %s failed", datName.c_str());
+        }
+        if (fflush(fc.f) != 0) return fail(c, PLBGPU_ERR_ARG, "write to %s failed", datName.c_str());
+    }
+    // The description, in the layout of the reference's XML writer
+    // (io/multiBlockWriter3D.cpp:53-137, libraryInterfaces/TINYXML_xmlIO.hh:229-272).
+    const char *family, *descriptor;
+    stateTypeInfo(what, &family, &descriptor);
+    char buf[512];
+    std::string x = "<?xml version=\"1.0\" ?>\n<Block3D>\n    <General>\n";
+    x += std::string("        <Family> ") + family + " </Family>\n        <Datatype> double </Datatype>\n";
+    if (descriptor) x += std::string("        <Descriptor> ") + descriptor + " </Descriptor>\n";
+    snprintf(buf, sizeof(buf),
+             "        <cellDim> %d </cellDim>\n        <dynamicContent> False </dynamicContent>\n"
+             "        <globalId> 0 </globalId>\n    </General>\n    <Structure>\n"
+             "        <BoundingBox> 0 %d 0 %d 0 %d </BoundingBox>\n        <EnvelopeWidth> 1 </EnvelopeWidth>\n"
+             "        <GridLevel> 0 </GridLevel>\n        <NumComponents> 1 </NumComponents>\n    </Structure>\n"
+             "    <Data>\n",
+             w, d->nx - 1, d->ny - 1, d->nz - 1);
+    x += buf;
+    x += "        <File> " + datName + " </File>\n";
+    snprintf(buf, sizeof(buf),
+             "        <Component> 0 %d 0 %d 0 %d </Component>\n        <Offsets> %llu </Offsets>\n    </Data>\n"
+             "</Block3D>\n",
+             d->nx - 1, d->ny - 1, d->nz - 1, (unsigned long long)d->n * w * sizeof(double));
+    x += buf;
+    FileCloser fp{fopen(plbName.c_str(), "wb")};
+    if (!fp.f) return fail(c, PLBGPU_ERR_ARG, "cannot open %s for writing", plbName.c_str());
+    if (fwrite(x.data(), 1, x.size(), fp.f) != x.size() || fflush(fp.f) != 0)
+        return fail(c, PLBGPU_ERR_ARG, "write to %s failed", plbName.c_str());
+    return PLBGPU_OK;
+}
+
+int plbgpu_load_state(plbgpu_ctx* c, int h, int what, const char* plb) {
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    const int w = blockWidth(what);
+    if (!w) return fail(c, PLBGPU_ERR_ARG, "unknown block kind %d", what);
+    if (what == PLBGPU_BLOCK_DENSITY || what == PLBGPU_BLOCK_VELOCITY)
+        return fail(c, PLBGPU_ERR_ARG, "density and velocity blocks are derived data and cannot be loaded");
+    if (!plb) return fail(c, PLBGPU_ERR_ARG, "null path");
+    std::string doc;
+    {
+        FileCloser fc{fopen(plb, "rb")};
+        if (!fc.f) return fail(c, PLBGPU_ERR_ARG, "cannot open %s", plb);
+        char chunk[4096];
+        size_t got;
+        while ((got = fread(chunk, 1, sizeof(chunk), fc.f)) > 0) doc.append(chunk, got);
+    }
+    // readXmlSpec (io/multiBlockReader3D.cpp:135-212)
+    std::string t;
+    std::vector<long long> v;
+    if (xmlElement(doc, "cellDim", 0, t, nullptr) == std::string::npos || !parseLongs(t, v) || v.size() != 1)
+        return fail(c, PLBGPU_ERR_ARG, "%s: no cellDim", plb);
+    if (v[0] != w) return fail(c, PLBGPU_ERR_ARG, "%s: cells of %lld values, this block kind has %d", plb, v[0], w);
+    if (xmlElement(doc, "dynamicContent", 0, t, nullptr) == std::string::npos ||
+        t.find("False") == std::string::npos)
+        return fail(c, PLBGPU_ERR_ARG, "%s: states with dynamic content are not supported", plb);
+    std::vector<long long> bb, offsets;
+    if (xmlElement(doc, "BoundingBox", 0, t, nullptr) == std::string::npos || !parseLongs(t, bb) || bb.size() != 6)
+        return fail(c, PLBGPU_ERR_ARG, "%s: no bounding box", plb);
+    if (bb[1] - bb[0] + 1 != d->nx || bb[3] - bb[2] + 1 != d->ny || bb[5] - bb[4] + 1 != d->nz)
+        return fail(c, PLBGPU_ERR_ARG, "%s: a %lldx%lldx%lld block, the domain is %dx%dx%d", plb, bb[1] - bb[0] + 1,
+                    bb[3] - bb[2] + 1, bb[5] - bb[4] + 1, d->nx, d->ny, d->nz);
+    if (xmlElement(doc, "Offsets", 0, t, nullptr) == std::string::npos || !parseLongs(t, offsets))
+        return fail(c, PLBGPU_ERR_ARG, "%s: no offsets", plb);
+    std::string datName;
+    if (xmlElement(doc, "File", 0, datName, nullptr) == std::string::npos)
+        return fail(c, PLBGPU_ERR_ARG, "%s: no data file", plb);
+    const size_t s0 = datName.find_first_not_of(" \n\t\r"), s1 = datName.find_last_not_of(" \n\t\r");
+    datName = s0 == std::string::npos ? std::string() : datName.substr(s0, s1 - s0 + 1);
+    if (datName.find('/') == std::string::npos) {   // next to the description
+        const std::string p(plb);
+        const size_t slash = p.rfind('/');
+        if (slash != std::string::npos) datName = p.substr(0, slash + 1) + datName;
+    }
+    if (datName.size() < 4 || datName.compare(datName.size() - 4, 4, ".dat") != 0) datName += ".dat";
+    std::vector<Box> comps;
+    size_t pos = 0, next = 0;
+    while (xmlElement(doc, "Component", pos, t, &next) != std::string::npos) {
+        if (!parseLongs(t, v) || v.size() != 6) return fail(c, PLBGPU_ERR_ARG, "%s: bad component", plb);
+        Box b{(int)(v[0] - bb[0]), (int)(v[1] - bb[0]), (int)(v[2] - bb[2]), (int)(v[3] - bb[2]),
+              (int)(v[4] - bb[4]), (int)(v[5] - bb[4])};
+        if (b.x0 < 0 || b.y0 < 0 || b.z0 < 0 || b.x1 >= d->nx || b.y1 >= d->ny || b.z1 >= d->nz || b.x0 > b.x1 ||
+            b.y0 > b.y1 || b.z0 > b.z1)
+            return fail(c, PLBGPU_ERR_ARG, "%s: component outside the bounding box", plb);
+        comps.push_back(b);
+        pos = next;
+    }
+    if (comps.size() != offsets.size() || comps.empty())
+        return fail(c, PLBGPU_ERR_ARG, "%s: %zu components, %zu offsets", plb, comps.size(), offsets.size());
+    FileCloser fd{fopen(datName.c_str(), "rb")};
+    if (!fd.f) return fail(c, PLBGPU_ERR_ARG, "cannot open %s", datName.c_str());
+    if ((rc = prepareLoad(c, d, what))) return rc;
+    std::vector<char> host;
+    long long begin = 0;
+    for (size_t i = 0; i < comps.size(); ++i) {
+        const Box& cb = comps[i];
+        const long long bytes = offsets[i] - begin;
+        if (bytes != boxCells(cb) * w * (long long)sizeof(double))
+            return fail(c, PLBGPU_ERR_ARG, "%s: component %zu holds %lld bytes, its box needs %lld", plb, i, bytes,
+                        boxCells(cb) * w * (long long)sizeof(double));
+        if (fseek(fd.f, (long)begin, SEEK_SET) != 0) return fail(c, PLBGPU_ERR_ARG, "%s: truncated", datName.c_str());
+        // whole x-planes of the component at a time
+        const long long plane = (long long)(cb.y1 - cb.y0 + 1) * (cb.z1 - cb.z0 + 1) * w * sizeof(double);
+        long long per = (32ll << 20) / (plane > 0 ? plane : 1);
+        const int planes = (int)(per < 1 ? 1 : (per > cb.x1 - cb.x0 + 1 ? cb.x1 - cb.x0 + 1 : per));
+        Ckpt k;
+        if ((rc = ckptAlloc(c, k, (long long)planes * (cb.y1 - cb.y0 + 1) * (cb.z1 - cb.z0 + 1), w))) return rc;
+        for (int x0 = cb.x0; x0 <= cb.x1; x0 += planes) {
+            const int x1 = x0 + planes - 1 < cb.x1 ? x0 + planes - 1 : cb.x1;
+            Box b{x0, x1, cb.y0, cb.y1, cb.z0, cb.z1};
+            host.resize((size_t)boxCells(b) * w * sizeof(double));
+            if (fread(host.data(), 1, host.size(), fd.f) != host.size())
+                return fail(c, PLBGPU_ERR_ARG, "%s: truncated data", datName.c_str());
+            CUDA_TRY(c, cudaMemcpyAsync(k.rec, host.data(), host.size(), cudaMemcpyHostToDevice, c->stream));
+            if ((rc = applyRecords(c, d, what, b, k))) return rc;
+            CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+        }
+        begin = offsets[i];
+    }
     if (what == PLBGPU_BLOCK_LATTICE || what == PLBGPU_BLOCK_FORCED_LATTICE) d->statsValid = false;
     return PLBGPU_OK;
 }

@@ -262,6 +262,14 @@ class DeviceLattice3D:
         self._check(self.lib.plbgpu_load_binary_block(self.ctx.h, self.handle, N.BLOCKS[what],
                                                       os.fsencode(path), int(bool(enforce_uint))))
 
+    def save_state(self, base, what="lattice"):
+        """parallelIO::save: <base>.plb and <base>.dat (static content)."""
+        self._check(self.lib.plbgpu_save_state(self.ctx.h, self.handle, N.BLOCKS[what], os.fsencode(base)))
+
+    def load_state(self, plb_path, what="lattice"):
+        """parallelIO::load of a state with static content."""
+        self._check(self.lib.plbgpu_load_state(self.ctx.h, self.handle, N.BLOCKS[what], os.fsencode(plb_path)))
+
     def time_steps(self, nsteps, stats=False) -> float:
         ms = ctypes.c_float()
         self._check(self.lib.plbgpu_time_steps(self.ctx.h, self.handle, int(nsteps), int(bool(stats)),

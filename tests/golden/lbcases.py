@@ -20,6 +20,7 @@ driver (oracle/ref_drivers/common.h), the oracle and the CUDA library:
 from __future__ import annotations
 
 import dataclasses
+import os
 import struct
 
 import numpy as np
@@ -41,6 +42,7 @@ OPT_NO_INITIALIZE = 1
 OPT_EXTERNAL_RHOJ = 2
 OPT_SAVE_BINARY = 4
 OPT_SPARSE = 8
+OPT_SAVE_STATE = 16
 NONE = 255   # not part of the lattice (outside every kept block)
 
 
@@ -479,6 +481,24 @@ def case_sparse_sealed_channel():
     return spec
 
 
+def case_state_periodic_multiblock():
+    """parallelIO::save of a 2 x 2 x 2-block lattice: eight components."""
+    s = case_periodic_bgk_multiblock()
+    s.name = "state_periodic_bgk_multiblock"
+    s.nsteps = 7
+    s.options |= OPT_SAVE_STATE
+    return s
+
+
+def case_state_guo_multiblock():
+    """parallelIO::save of a forced lattice: 22 values per cell, four components."""
+    s = case_guo_periodic_multiblock()
+    s.name = "state_guo_periodic_multiblock"
+    s.nsteps = 5
+    s.options |= OPT_SAVE_STATE
+    return s
+
+
 def case_doctest_cavity20():
     return doctest_cavity(20, 20, 20, name="doctest_cavity20")
 
@@ -502,7 +522,7 @@ CASES = [
     case_velocity_box_multiblock, case_velocity_box_noinit, case_doctest_cavity20,
     case_external_periodic_bgk, case_external_incbgk_nodyn, case_external_guo_periodic,
     case_external_mebb_periodic, case_binary_channel_sphere, case_binary_guo_periodic,
-    case_sparse_sealed_channel,
+    case_sparse_sealed_channel, case_state_periodic_multiblock, case_state_guo_multiblock,
 ]
 
 
@@ -578,6 +598,12 @@ def read_result_file(path: str, spec: CaseSpec):
         out["rho_bar_final"] = np.frombuffer(data, np.float64, m, off).reshape(nx, ny, nz).copy()
         off += 8 * m
         out["j_final"] = np.frombuffer(data, np.float64, 3 * m, off).reshape(nx, ny, nz, 3).copy()
+    if spec.options & OPT_SAVE_STATE:
+        base = os.path.splitext(path)[0] + "_state"
+        with open(base + ".plb") as f:
+            out["state_plb"] = f.read()
+        with open(base + ".dat", "rb") as f:
+            out["state_dat"] = np.frombuffer(f.read(), np.uint8).copy()
     if spec.options & OPT_SAVE_BINARY:
         for what in ("lattice", "density", "velocity"):
             with open(path + "." + what, "rb") as f:

@@ -70,6 +70,8 @@ def main(argv):
             for what in ("lattice", "density", "velocity"):
                 if "binary_" + what in res:
                     extra["binary_" + what] = res["binary_" + what]
+            if "state_plb" in res:
+                extra.update(state_plb=res["state_plb"], state_dat=res["state_dat"])
             if spec.sparse is not None:
                 extra.update(sparse=spec.sparse, in_lattice=res["in_lattice"], compare=spec.compare)
             np.savez_compressed(

@@ -33,3 +33,76 @@ def test_header_forms():
     a = O.binary_block(np.zeros((2, 19)))
     b = O.binary_block(np.zeros((2, 19)), enforce_uint=True)
     assert a[:12].endswith(b"=") and b[:8].endswith(b"==") and a[12:] == b[8:]
+
+
+# ---------------------------------------------------------------- saveState / parallelIO
+
+import os
+import re
+import subprocess
+import tempfile
+
+import lbcases
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+DRIVER = os.path.join(ROOT, "oracle", "_ref", "plb_case")
+STATES = ["state_periodic_bgk_multiblock", "state_guo_periodic_multiblock"]
+
+
+def state_components(plb):
+    boxes = [tuple(map(int, m.split())) for m in re.findall(r"<Component[^>]*>([^<]*)</Component>", plb)]
+    offsets = list(map(int, re.search(r"<Offsets>([^<]*)</Offsets>", plb).group(1).split()))
+    return boxes, offsets
+
+
+def records(g, meta):
+    recs = g["f_final"]
+    if meta["forced"]:
+        recs = np.concatenate([recs, g["force"]], axis=-1)
+    return recs
+
+
+@pytest.mark.parametrize("name", STATES)
+def test_reference_state_layout(name):
+    """The reference's .dat is each component's records, x-major, in
+    component order, at the offsets its description gives."""
+    g, meta = goldens.load(name)
+    plb = str(g["state_plb"])
+    dat = bytes(g["state_dat"])
+    boxes, offsets = state_components(plb)
+    recs = records(g, meta)
+    start = 0
+    for (x0, x1, y0, y1, z0, z1), end in zip(boxes, offsets):
+        part = np.ascontiguousarray(recs[x0:x1 + 1, y0:y1 + 1, z0:z1 + 1]).tobytes()
+        assert dat[start:end] == part
+        start = end
+    assert start == len(dat)
+    assert f"<cellDim> {recs.shape[-1]} </cellDim>" in plb
+
+
+@pytest.mark.skipif(not os.path.exists(DRIVER), reason="reference driver not built (needs the reference sources)")
+@pytest.mark.parametrize("name", STATES)
+def test_reference_loads_single_component_state(name):
+    """A state written the way plbgpu_save_state writes it (one component,
+    oracle.state_files) is loaded by the reference's own parallelIO::load and
+    continues the reference's trajectory bit for bit."""
+    spec = lbcases.case_by_name(name)
+    g, meta = goldens.load(name)
+    f_init = g["f_init"]
+    recs = f_init if not meta["forced"] else np.concatenate([f_init, g["force"]], axis=-1)
+    with tempfile.TemporaryDirectory() as tmp:
+        plb, dat = O.state_files(recs.reshape(-1, recs.shape[-1]), f_init.shape[:3], recs.shape[-1],
+                                 "BlockLattice3D", "ForcedD3Q19" if meta["forced"] else "D3Q19",
+                                 os.path.join(tmp, "s.dat"))
+        with open(os.path.join(tmp, "s.plb"), "w") as f:
+            f.write(plb)
+        with open(os.path.join(tmp, "s.dat"), "wb") as f:
+            f.write(dat)
+        spec.options &= ~lbcases.OPT_SAVE_STATE
+        cpath, rpath = os.path.join(tmp, "c"), os.path.join(tmp, "r")
+        lbcases.write_case_file(spec, cpath)
+        subprocess.run([DRIVER, cpath, rpath], check=True,
+                       env=dict(os.environ, PLB_LOAD_STATE=os.path.join(tmp, "s.plb")))
+        res = lbcases.read_result_file(rpath, spec)
+    assert np.array_equal(res["f_init"], f_init)
+    assert np.array_equal(res["f_final"], g["f_final"])
