@@ -107,6 +107,10 @@ __device__ __forceinline__ BgkConst<R> bgkConsts(R omega) {
     return b;
 }
 
+// The force planes are FP64 for FP64 (and dual) arithmetic, FP32 for FP32.
+template <typename R>
+__host__ __device__ constexpr bool forceIsFp64() { return sizeof(R) != sizeof(float); }
+
 // Guo force of a cell: FP64 planes for the FP64 form, FP32 otherwise; `dF`
 // (tangent runs only) gives its direction.
 template <typename R>
@@ -267,30 +271,41 @@ __device__ R adjCell(int k, const R* f, const R* F, R omega, R invRho0, const R*
 
 // ---------------------------------------------------------------- kernels
 
-// Neighbour of a cell along +c_i: rows with 1 <= x <= nx-2, 1 <= y <= ny-2 use
-// the uniform offsets c_i . (ny*nz, nz, 1) and only check the z ends; border
-// rows use the general neighbourhood.  Returns false where a non-periodic
-// domain is left.
-struct CellMoves {
-    bool interior;
-    Neighbourhood nb;
+// Neighbour of a cell along +c_i.  INTERIOR rows (1 <= x <= nx-2,
+// 1 <= y <= ny-2) use the uniform offsets c_i . (ny*nz, nz, 1) and only check
+// the z ends; border rows use the general neighbourhood.  Returns false where
+// a non-periodic domain is left.  A block covers part of one row, so the
+// kernels pick the form once per block.
+template <bool INTERIOR>
+struct CellMoves;
+
+template <>
+struct CellMoves<true> {
     long long wrapM, wrapP;
     bool okM, okP;
-    __device__ __forceinline__ CellMoves(const DevLattice& L, int x, int y, int z) {
-        interior = x > 0 && x < L.nx - 1 && y > 0 && y < L.ny - 1;
-        nb = neighbourhood(L, x, y, z);
+    __device__ __forceinline__ CellMoves(const DevLattice& L, int, int, int z) {
         wrapM = z == 0 ? L.nz : 0;
         wrapP = z == L.nz - 1 ? -L.nz : 0;
         okM = z > 0 || L.per[2];
         okP = z < L.nz - 1 || L.per[2];
     }
     __device__ __forceinline__ bool plus(int i, const int* D, long long& off) const {
-        if (!interior) return nb.move(i, +1, off);
         const int cz = cdir(i, 2);
         off = D[i] + (cz < 0 ? wrapM : cz > 0 ? wrapP : 0);
         return cz < 0 ? okM : cz > 0 ? okP : true;
     }
 };
+
+template <>
+struct CellMoves<false> {
+    Neighbourhood nb;
+    __device__ __forceinline__ CellMoves(const DevLattice& L, int x, int y, int z) : nb(neighbourhood(L, x, y, z)) {}
+    __device__ __forceinline__ bool plus(int i, const int*, long long& off) const { return nb.move(i, +1, off); }
+};
+
+__device__ __forceinline__ bool interiorRow(const DevLattice& L, int x, int y) {
+    return x > 0 && x < L.nx - 1 && y > 0 && y < L.ny - 1;
+}
 
 struct NeighbourDeltas {
     int d[19];
@@ -302,16 +317,38 @@ inline NeighbourDeltas deltasOf(const DevLattice& L) {
     return D;
 }
 
+// Sums of the backward sweep, kept in kAdjSlots copies (one per block index
+// modulo kAdjSlots) and added up on the host: one address taking an atomic
+// from every warp of every step would serialize the sweep.
+constexpr int kAdjSlots = 64;
+
 struct AdjAcc {
-    double objective;
-    double gOmega;
-    double tangent;
-    double pad;
+    double objective[kAdjSlots];
+    double gOmega[kAdjSlots];
+    double tangent[kAdjSlots];
 };
 
+inline double slotSum(const double* v) {
+    double s = 0.;
+    for (int i = 0; i < kAdjSlots; ++i) s += v[i];
+    return s;
+}
+
+// Block-wide sum of v, one atomic per block on its slot of dst.  Every thread
+// of the block calls it.
 __device__ __forceinline__ void blockAdd(double v, double* dst) {
+    __shared__ double part[32];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0 && v != 0.) atomicAdd(dst, v);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();   // part may still be read by a previous call
+    if (lane == 0) part[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = lane < nw ? part[lane] : 0.;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        const unsigned b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+        if (lane == 0 && v != 0.) atomicAdd(dst + (b & (kAdjSlots - 1)), v);
+    }
 }
 
 // Natural-order copy of the domain's state (either AA parity) and back.
@@ -338,31 +375,37 @@ __global__ void stateInKernel(DevLattice L, const R* in) {
 
 // Push step fin -> fout (natural order): collide, then send f*_i to x + c_i
 // or, leaving a non-periodic domain, back into slot opp(i) of x.
-template <typename R>
-__global__ void pushStepKernel(DevLattice L, NeighbourDeltas D, bool fp64Force, const R* fin, R* fout, R omega,
-                               R invRho0, const double* dF) {
-    const int z = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y, x = blockIdx.z;
-    if (z >= L.nz) return;
+template <typename R, bool INTERIOR>
+__device__ __forceinline__ void pushCell(const DevLattice& L, const NeighbourDeltas& D, const R* fin, R* fout,
+                                         R omega, R invRho0, const double* dF, int x, int y, int z) {
     const long long idx = ((long long)x * L.ny + y) * L.nz + z;
     const int k = L.flags[idx];
     R f[19], F[3];
     for (int i = 0; i < 19; ++i) f[i] = fin[i * L.n + idx];
-    cellForce(L, fp64Force, idx, dF, F);
+    cellForce(L, forceIsFp64<R>(), idx, dF, F);
     adjCollide<R>(k, f, F, bgkConsts<R>(omega), invRho0);
-    CellMoves mv(L, x, y, z);
+    CellMoves<INTERIOR> mv(L, x, y, z);
     fout[idx] = f[0];
 #pragma unroll
     for (int i = 1; i < 19; ++i) {
         long long off;
-        if (mv.plus(i, D.d, off)) fout[i * L.n + idx + off] = f[i];
-        else fout[opp(i) * L.n + idx] = f[i];
+        fout[mv.plus(i, D.d, off) ? i * L.n + idx + off : opp(i) * L.n + idx] = f[i];
     }
+}
+
+template <typename R>
+__global__ void pushStepKernel(DevLattice L, NeighbourDeltas D, const R* fin, R* fout, R omega, R invRho0,
+                               const double* dF) {
+    const int z = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, x = blockIdx.z;
+    if (z >= L.nz) return;
+    if (interiorRow(L, x, y)) pushCell<R, true>(L, D, fin, fout, omega, invRho0, dF, x, y, z);
+    else pushCell<R, false>(L, D, fin, fout, omega, invRho0, dF, x, y, z);
 }
 
 // J, lambda^T = dJ/df^T and the explicit dJ/dF of the Guo velocity u = j/rho + F/2.
 template <typename R>
-__global__ void objectiveKernel(DevLattice L, bool fp64Force, const R* f, const double* uTarget, R invRho0, R* lam,
+__global__ void objectiveKernel(DevLattice L, const R* f, const double* uTarget, R invRho0, R* lam,
                                 R* gF, AdjAcc* acc) {
     const int z = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y, x = blockIdx.z;
@@ -372,7 +415,7 @@ __global__ void objectiveKernel(DevLattice L, bool fp64Force, const R* f, const 
         const int k = L.flags[idx];
         R fc[19], F[3], u[3];
         for (int i = 0; i < 19; ++i) fc[i] = f[i * L.n + idx];
-        cellForce(L, fp64Force, idx, nullptr, F);
+        cellForce(L, forceIsFp64<R>(), idx, nullptr, F);
         cellVelocity<R>(k, fc, F, invRho0, u);
         R dv[3];
         for (int d = 0; d < 3; ++d) {
@@ -395,35 +438,43 @@ __global__ void objectiveKernel(DevLattice L, bool fp64Force, const R* f, const 
             for (int i = 0; i < 19; ++i) lam[i * L.n + idx] = R(0);
         }
     }
-    blockAdd(jsum, &acc->objective);
+    blockAdd(jsum, acc->objective);
 }
 
 // One reverse step: lamIn = lambda^{n+1}, f = f^n (pre-collision), lamOut = lambda^n.
+template <typename R, bool INTERIOR>
+__device__ __forceinline__ R adjointCell(const DevLattice& L, const NeighbourDeltas& D, const R* f, const R* lamIn,
+                                         R* lamOut, R* gF, R omega, R invRho0, int x, int y, int z) {
+    const long long idx = ((long long)x * L.ny + y) * L.nz + z;
+    const int k = L.flags[idx];
+    CellMoves<INTERIOR> mv(L, x, y, z);
+    R mu[19], fc[19], F[3], lam[19], g[3] = {R(0), R(0), R(0)};
+    mu[0] = lamIn[idx];
+#pragma unroll
+    for (int i = 1; i < 19; ++i) {
+        long long off;
+        mu[i] = lamIn[mv.plus(i, D.d, off) ? i * L.n + idx + off : opp(i) * L.n + idx];
+    }
+    for (int i = 0; i < 19; ++i) fc[i] = f[i * L.n + idx];
+    cellForce(L, forceIsFp64<R>(), idx, nullptr, F);
+    const R go = adjCell<R>(k, fc, F, omega, invRho0, mu, lam, g);
+    for (int i = 0; i < 19; ++i) lamOut[i * L.n + idx] = lam[i];
+    if (k == K_GUO)
+        for (int d = 0; d < 3; ++d) gF[d * L.n + idx] += g[d];
+    return go;
+}
+
 template <typename R>
-__global__ void adjointStepKernel(DevLattice L, NeighbourDeltas D, bool fp64Force, const R* f, const R* lamIn,
-                                  R* lamOut, R* gF, R omega, R invRho0, AdjAcc* acc) {
+__global__ void adjointStepKernel(DevLattice L, NeighbourDeltas D, const R* f, const R* lamIn, R* lamOut, R* gF,
+                                  R omega, R invRho0, AdjAcc* acc) {
     const int z = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y, x = blockIdx.z;
     double go = 0.;
     if (z < L.nz) {
-        const long long idx = ((long long)x * L.ny + y) * L.nz + z;
-        const int k = L.flags[idx];
-        CellMoves mv(L, x, y, z);
-        R mu[19], fc[19], F[3], lam[19], g[3] = {R(0), R(0), R(0)};
-        mu[0] = lamIn[idx];
-#pragma unroll
-        for (int i = 1; i < 19; ++i) {
-            long long off;
-            mu[i] = mv.plus(i, D.d, off) ? lamIn[i * L.n + idx + off] : lamIn[opp(i) * L.n + idx];
-        }
-        for (int i = 0; i < 19; ++i) fc[i] = f[i * L.n + idx];
-        cellForce(L, fp64Force, idx, nullptr, F);
-        go = (double)adjCell<R>(k, fc, F, omega, invRho0, mu, lam, g);
-        for (int i = 0; i < 19; ++i) lamOut[i * L.n + idx] = lam[i];
-        if (k == K_GUO)
-            for (int d = 0; d < 3; ++d) gF[d * L.n + idx] += g[d];
+        go = interiorRow(L, x, y) ? (double)adjointCell<R, true>(L, D, f, lamIn, lamOut, gF, omega, invRho0, x, y, z)
+                                  : (double)adjointCell<R, false>(L, D, f, lamIn, lamOut, gF, omega, invRho0, x, y, z);
     }
-    blockAdd(go, &acc->gOmega);
+    blockAdd(go, acc->gOmega);
 }
 
 // J and its tangent from a dual state.
@@ -445,8 +496,8 @@ __global__ void dualObjectiveKernel(DevLattice L, const Dual* f, const double* d
             jd += dv.v * dv.d;
         }
     }
-    blockAdd(jv, &acc->objective);
-    blockAdd(jd, &acc->tangent);
+    blockAdd(jv, acc->objective);
+    blockAdd(jd, acc->tangent);
 }
 
 template <typename R>
@@ -477,12 +528,17 @@ struct AdjointState {
 
 void freeAdjoint(void* p) { delete static_cast<AdjointState*>(p); }
 
-dim3 cellGrid(const DevLattice& L) { return rowGrid(L.nz, L.ny, L.nx, 128); }
+// One thread per cell, a block per row segment; short rows get fewer threads.
+int cellBlock(const DevLattice& L) {
+    const int t = (L.nz + 31) / 32 * 32;
+    return t < 128 ? t : 128;
+}
+dim3 cellGrid(const DevLattice& L) { return rowGrid(L.nz, L.ny, L.nx, cellBlock(L)); }
 
 template <typename S, typename R>
 void stateOut(const DevLattice& L, bool odd, R* out, cudaStream_t s) {
-    if (odd) stateOutKernel<S, R, true><<<cellGrid(L), 128, 0, s>>>(L, out);
-    else stateOutKernel<S, R, false><<<cellGrid(L), 128, 0, s>>>(L, out);
+    if (odd) stateOutKernel<S, R, true><<<cellGrid(L), cellBlock(L), 0, s>>>(L, out);
+    else stateOutKernel<S, R, false><<<cellGrid(L), cellBlock(L), 0, s>>>(L, out);
 }
 
 template <typename R>
@@ -500,11 +556,11 @@ template <typename R>
 void stateInAny(int prec, const DevLattice& L, const R* in, cudaStream_t s) {
     dim3 g = cellGrid(L);
     switch (prec) {
-    case PLBGPU_FP64: stateInKernel<double, R><<<g, 128, 0, s>>>(L, in); break;
-    case PLBGPU_FP32: stateInKernel<float, R><<<g, 128, 0, s>>>(L, in); break;
-    case PLBGPU_BF16: stateInKernel<__nv_bfloat16, R><<<g, 128, 0, s>>>(L, in); break;
-    case PLBGPU_FP16: stateInKernel<__half, R><<<g, 128, 0, s>>>(L, in); break;
-    default: stateInKernel<bf16sr, R><<<g, 128, 0, s>>>(L, in); break;
+    case PLBGPU_FP64: stateInKernel<double, R><<<g, cellBlock(L), 0, s>>>(L, in); break;
+    case PLBGPU_FP32: stateInKernel<float, R><<<g, cellBlock(L), 0, s>>>(L, in); break;
+    case PLBGPU_BF16: stateInKernel<__nv_bfloat16, R><<<g, cellBlock(L), 0, s>>>(L, in); break;
+    case PLBGPU_FP16: stateInKernel<__half, R><<<g, cellBlock(L), 0, s>>>(L, in); break;
+    default: stateInKernel<bf16sr, R><<<g, cellBlock(L), 0, s>>>(L, in); break;
     }
 }
 
@@ -533,7 +589,6 @@ int checkKinds(plbgpu_ctx* c, const DomainAccess& a) {
 template <typename R>
 int forwardImpl(plbgpu_ctx* c, int h, DomainAccess& a, AdjointState* st, int T, int K) {
     const long long n = a.L.n, sz = 19 * n;
-    const bool fp64Force = a.precision == PLBGPU_FP64;
     R* ck = static_cast<R*>(st->ckpt);
     R* sg = static_cast<R*>(st->seg);
     stateOutAny<R>(a.precision, a.L, a.odd, ck, a.stream);
@@ -544,7 +599,7 @@ int forwardImpl(plbgpu_ctx* c, int h, DomainAccess& a, AdjointState* st, int T, 
     const NeighbourDeltas D = deltasOf(a.L);
     for (int t = 0; t < T; ++t) {
         R* out = ((t + 1) % K == 0) ? ck + ((t + 1) / K) * sz : bufs[t & 1];
-        pushStepKernel<R><<<cellGrid(a.L), 128, 0, a.stream>>>(a.L, D, fp64Force, cur, out, omega, invRho0, nullptr);
+        pushStepKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, D, cur, out, omega, invRho0, nullptr);
         *a.launches += 1;
         cur = out;
     }
@@ -561,7 +616,6 @@ int forwardImpl(plbgpu_ctx* c, int h, DomainAccess& a, AdjointState* st, int T, 
 template <typename R>
 int backwardImpl(DomainAccess& a, AdjointState* st, double* objective, double* gOmega, float* ms) {
     const long long n = a.L.n, sz = 19 * n;
-    const bool fp64Force = a.precision == PLBGPU_FP64;
     R* ck = static_cast<R*>(st->ckpt);
     R* sg = static_cast<R*>(st->seg);
     R* lam = static_cast<R*>(st->lam);
@@ -575,22 +629,22 @@ int backwardImpl(DomainAccess& a, AdjointState* st, double* objective, double* g
     cudaMemsetAsync(gF, 0, sizeof(R) * 3 * n, a.stream);
     cudaMemsetAsync(st->acc, 0, sizeof(AdjAcc), a.stream);
     const int T = st->T, K = st->K;
-    objectiveKernel<R><<<cellGrid(a.L), 128, 0, a.stream>>>(a.L, fp64Force, ck + (long long)(T / K) * sz, st->uT,
-                                                            invRho0, lam, gF, st->acc);
+    objectiveKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, ck + (long long)(T / K) * sz,
+                                                                       st->uT, invRho0, lam, gF, st->acc);
     *a.launches += 1;
     int cur = 0;   // lam + cur * sz holds lambda^{t+1}
     for (int s = T / K - 1; s >= 0; --s) {
-        // recompute f^{sK} .. f^{sK+K-1} into seg
-        cudaMemcpyAsync(sg, ck + (long long)s * sz, sizeof(R) * sz, cudaMemcpyDeviceToDevice, a.stream);
+        // f^{sK} is checkpoint s; recompute f^{sK+1} .. f^{sK+K-1} into seg
+        auto state = [&](int k) { return k == 0 ? ck + (long long)s * sz : sg + k * sz; };
         for (int k = 0; k + 1 < K; ++k) {
-            pushStepKernel<R><<<cellGrid(a.L), 128, 0, a.stream>>>(a.L, D, fp64Force, sg + k * sz,
-                                                                   sg + (k + 1) * sz, omega, invRho0, nullptr);
+            pushStepKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, D, state(k),
+                                                                              state(k + 1), omega, invRho0, nullptr);
             *a.launches += 1;
         }
         for (int k = K - 1; k >= 0; --k) {
-            adjointStepKernel<R><<<cellGrid(a.L), 128, 0, a.stream>>>(a.L, D, fp64Force, sg + k * sz,
-                                                                      lam + cur * sz, lam + (1 - cur) * sz, gF, omega,
-                                                                      invRho0, st->acc);
+            adjointStepKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, D, state(k),
+                                                                                 lam + cur * sz, lam + (1 - cur) * sz,
+                                                                                 gF, omega, invRho0, st->acc);
             *a.launches += 1;
             cur = 1 - cur;
         }
@@ -603,8 +657,8 @@ int backwardImpl(DomainAccess& a, AdjointState* st, double* objective, double* g
     AdjAcc h;
     cudaMemcpyAsync(&h, st->acc, sizeof(AdjAcc), cudaMemcpyDeviceToHost, a.stream);
     cudaStreamSynchronize(a.stream);
-    *objective = h.objective;
-    *gOmega = h.gOmega;
+    *objective = slotSum(h.objective);
+    *gOmega = slotSum(h.gOmega);
     return cudaGetLastError() == cudaSuccess ? PLBGPU_OK : PLBGPU_ERR_CUDA;
 }
 
@@ -719,19 +773,19 @@ int plbgpu_tangent_linear(plbgpu_ctx* c, int h, int T, const double* dforce, siz
         const Dual om(a.omega, domega), inv0(1.0 / a.rho0);
         const NeighbourDeltas D = deltasOf(a.L);
         for (int t = 0; t < T; ++t) {
-            pushStepKernel<Dual><<<cellGrid(a.L), 128, 0, a.stream>>>(a.L, D, true, cur, nxt, om, inv0, dF);
+            pushStepKernel<Dual><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, D, cur, nxt, om, inv0, dF);
             *a.launches += 1;
             std::swap(cur, nxt);
         }
-        dualObjectiveKernel<<<cellGrid(a.L), 128, 0, a.stream>>>(a.L, cur, dF, uT, 1.0 / a.rho0, acc);
+        dualObjectiveKernel<<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, cur, dF, uT, 1.0 / a.rho0, acc);
         *a.launches += 1;
         e = cudaGetLastError();
         AdjAcc hacc;
         if (e == cudaSuccess) e = cudaMemcpyAsync(&hacc, acc, sizeof(AdjAcc), cudaMemcpyDeviceToHost, a.stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(a.stream);
         if (e == cudaSuccess) {
-            *objective = hacc.objective;
-            *directional = hacc.tangent;
+            *objective = slotSum(hacc.objective);
+            *directional = slotSum(hacc.tangent);
         }
     }
     cudaFree(f0); cudaFree(buf); cudaFree(dF); cudaFree(uT); cudaFree(acc);
