@@ -227,7 +227,9 @@ def adjoint_cost(ctx, T=2000, K=100, precisions=("fp64", "fp32")):
     from a forward run with a second force field (seed 5678); objective
     1/2 sum |u(T) - u*|^2, checkpoint every K steps.  Reports the device time
     per time step of the forward recording and of the backward sweep
-    (recomputation included) against one fused forward step."""
+    (recomputation included) against one fused forward step; "all_states"
+    repeats the sweep with the interval the library picks from free device
+    memory (K = 1 keeps every state: no recomputation)."""
     from palabos_gb300 import workloads
     out = {"workload": "forced_channel_128x64x64_guo", "T": T, "K": K}
     for prec in precisions:
@@ -249,6 +251,12 @@ def adjoint_cost(ctx, T=2000, K=100, precisions=("fp64", "fp32")):
                      "backward_ms_per_step": round(back_ms / T, 5),
                      "adjoint_step_over_forward_step": round(back_ms / T / fwd_ms, 3),
                      "objective": J, "grad_omega": gO, "grad_force_l2": float(np.sqrt(np.sum(gF * gF)))}
+        lat.send(f0)
+        used = lat.adjoint_forward(T, 0)
+        J1, gF1, gO1, back1 = lat.adjoint_backward(u_target, want_force=False)
+        out[prec]["all_states"] = {"K": used, "backward_ms_per_step": round(back1 / T, 5),
+                                   "adjoint_step_over_forward_step": round(back1 / T / fwd_ms, 3),
+                                   "grad_omega": gO1}
         lat.close()
     return out
 

@@ -296,7 +296,10 @@ int plbgpu_load_state(plbgpu_ctx* ctx, int handle, int what, const char* plb_pat
  * dataProcessors/dataAnalysisWrapper3D.h:127-132).
  *
  * plbgpu_adjoint_forward: run T steps from the current state, keeping a
- * checkpoint every K steps (K divides T); the domain ends at step T.
+ * checkpoint every K steps (K divides T); the domain ends at step T.  K = 0
+ * picks the smallest divisor of T whose checkpoints fit in 80% of the free
+ * device memory (K = 1 keeps every state and the backward sweep recomputes
+ * nothing); plbgpu_adjoint_interval reports the K of the recorded run.
  * plbgpu_adjoint_backward: J, dJ/dF per cell (3 doubles per cell, transfer
  * order; may be NULL) and dJ/domega for that run, recomputing each segment
  * of K steps from its checkpoint; `ms` (may be NULL) receives the device time
@@ -305,6 +308,7 @@ int plbgpu_load_state(plbgpu_ctx* ctx, int handle, int what, const char* plb_pat
  * dJ = grad J . (dforce, domega) from a dual-number run of T steps from the
  * current state, which it leaves unchanged. */
 int plbgpu_adjoint_forward(plbgpu_ctx* ctx, int handle, int T, int K);
+int plbgpu_adjoint_interval(plbgpu_ctx* ctx, int handle, int* K);
 int plbgpu_adjoint_backward(plbgpu_ctx* ctx, int handle, const double* u_target, size_t n_target,
                             double* objective, double* grad_force, size_t n_grad, double* grad_omega,
                             float* ms);

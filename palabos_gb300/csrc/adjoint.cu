@@ -673,12 +673,30 @@ int plbgpu_adjoint_forward(plbgpu_ctx* c, int h, int T, int K) {
     DomainAccess a;
     int rc = domainAccess(c, h, &a);
     if (rc) return rc;
-    if (T < 1 || K < 1 || T % K != 0) return domainFail(c, PLBGPU_ERR_ARG, "adjoint: need T >= 1, K >= 1, K divides T");
+    if (T < 1 || K < 0 || (K > 0 && T % K != 0))
+        return domainFail(c, PLBGPU_ERR_ARG, "adjoint: need T >= 1 and K = 0 or a divisor of T");
     if ((rc = checkKinds(c, a))) return rc;
     if (a.pending) return domainFail(c, PLBGPU_ERR_STATE, "adjoint: boundary faces are not supported");
     AdjointState* st = static_cast<AdjointState*>(*a.adjointSlot);
     const size_t rs = a.precision == PLBGPU_FP64 ? sizeof(double) : sizeof(float);
     const long long n = a.L.n, sz = 19 * n;
+    // states held: T/K + 1 checkpoints, a segment of K recomputed states
+    // (none when every step is a checkpoint) and two adjoint states
+    auto states = [&](int k) { return (long long)(T / k + 1) + (k > 1 ? std::max(k, 2) : 0) + 2; };
+    if (K == 0) {
+        // the smallest interval whose states fit in 80% of the free memory
+        if (st) {
+            freeAdjoint(st);
+            *a.adjointSlot = nullptr;
+            st = nullptr;
+        }
+        size_t freeB = 0, totalB = 0;
+        ADJ_TRY(cudaMemGetInfo(&freeB, &totalB));
+        const double budget = 0.8 * (double)freeB - (double)(rs * 3 + sizeof(double) * 3) * n;
+        for (int k = 1; k <= T && K == 0; ++k)
+            if (T % k == 0 && (double)states(k) * rs * sz <= budget) K = k;
+        if (K == 0) return domainFail(c, PLBGPU_ERR_NOMEM, "adjoint: no checkpoint interval fits in device memory");
+    }
     const int nckpt = T / K + 1;
     if (!st || st->precision != a.precision || st->n != n || st->nckpt != nckpt || st->K != K) {
         if (st) freeAdjoint(st);
@@ -692,7 +710,7 @@ int plbgpu_adjoint_forward(plbgpu_ctx* c, int h, int T, int K) {
         st->nckpt = nckpt;
         st->K = K;
         ADJ_TRY(cudaMalloc(&st->ckpt, rs * sz * nckpt));
-        ADJ_TRY(cudaMalloc(&st->seg, rs * sz * std::max(K, 2)));
+        if (K > 1) ADJ_TRY(cudaMalloc(&st->seg, rs * sz * std::max(K, 2)));
         ADJ_TRY(cudaMalloc(&st->lam, rs * sz * 2));
         ADJ_TRY(cudaMalloc(&st->gF, rs * 3 * n));
         ADJ_TRY(cudaMalloc(&st->uT, sizeof(double) * 3 * n));
@@ -703,6 +721,17 @@ int plbgpu_adjoint_forward(plbgpu_ctx* c, int h, int T, int K) {
     rc = a.precision == PLBGPU_FP64 ? forwardImpl<double>(c, h, a, st, T, K) : forwardImpl<float>(c, h, a, st, T, K);
     if (rc == PLBGPU_OK) st->ready = true;
     return rc;
+}
+
+int plbgpu_adjoint_interval(plbgpu_ctx* c, int h, int* K) {
+    DomainAccess a;
+    int rc = domainAccess(c, h, &a);
+    if (rc) return rc;
+    const AdjointState* st = static_cast<const AdjointState*>(*a.adjointSlot);
+    if (!K) return domainFail(c, PLBGPU_ERR_ARG, "adjoint: K is NULL");
+    if (!st || !st->ready) return domainFail(c, PLBGPU_ERR_STATE, "adjoint: no recorded forward run");
+    *K = st->K;
+    return PLBGPU_OK;
 }
 
 int plbgpu_adjoint_backward(plbgpu_ctx* c, int h, const double* u_target, size_t n3, double* objective,

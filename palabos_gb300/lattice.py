@@ -304,9 +304,14 @@ class DeviceLattice3D:
         return out.reshape(box[1] - box[0] + 1, box[3] - box[2] + 1, box[5] - box[4] + 1)
 
     # ----------------------------------------------------------------- adjoint
-    def adjoint_forward(self, T, K):
-        """Run T steps keeping a checkpoint every K steps (discrete adjoint)."""
+    def adjoint_forward(self, T, K=0):
+        """Run T steps keeping a checkpoint every K steps (discrete adjoint);
+        K = 0 picks the smallest interval that fits in device memory.
+        Returns the interval used."""
         self._check(self.lib.plbgpu_adjoint_forward(self.ctx.h, self.handle, int(T), int(K)))
+        k = ctypes.c_int()
+        self._check(self.lib.plbgpu_adjoint_interval(self.ctx.h, self.handle, ctypes.byref(k)))
+        return k.value
 
     def adjoint_backward(self, u_target, want_force=True):
         """J = 1/2 sum |u(T) - u*|^2, dJ/dF (nx,ny,nz,3) and dJ/domega of the

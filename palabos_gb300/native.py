@@ -108,6 +108,7 @@ SIGNATURES = {
     "plbgpu_cp_receive": [_vp, _i, *LBOX, ctypes.c_char_p, _sz],
     "plbgpu_cp_collide_and_stream": [_vp, _i],
     "plbgpu_adjoint_forward": [_vp, _i, _i, _i],
+    "plbgpu_adjoint_interval": [_vp, _i, _c_int_p],
     "plbgpu_adjoint_backward": [_vp, _i, _c_dbl_p, _sz, _c_dbl_p, _c_dbl_p, _sz, _c_dbl_p,
                                 ctypes.POINTER(ctypes.c_float)],
     "plbgpu_tangent_linear": [_vp, _i, _i, _c_dbl_p, _sz, _d, _c_dbl_p, _sz, _c_dbl_p, _c_dbl_p],

@@ -30,7 +30,7 @@ def _oracle_objective(wl, f0, force, omega, T, u_target):
     return 0.5 * float(np.sum((u - u_target) ** 2))
 
 
-@pytest.mark.parametrize("K", [1, 4, 24])
+@pytest.mark.parametrize("K", [0, 1, 4, 24])
 def test_adjoint_matches_tangent_linear(K):
     wl, u_target, T = _case()
     lat = wl.lattice("fp64")
@@ -40,7 +40,8 @@ def test_adjoint_matches_tangent_linear(K):
     dF[wl.kinds != 1] = 0.0
     domega = 0.7
     J_t, dJ = lat.tangent_linear(T, dF, domega, u_target)
-    lat.adjoint_forward(T, K)
+    used = lat.adjoint_forward(T, K)
+    assert used == (K if K else 1)     # K = 0: a small domain keeps every state
     J, gF, gO, _ = lat.adjoint_backward(u_target)
     assert J == pytest.approx(J_t, rel=1e-13)
     adj = float(np.sum(gF * dF)) + gO * domega
@@ -102,7 +103,13 @@ def test_adjoint_rejects_unsupported_cells():
     with pytest.raises(PlbGpuError):
         lat2.adjoint_forward(5, 2)      # K must divide T
     with pytest.raises(PlbGpuError):
+        lat2.adjoint_forward(4, -1)
+    with pytest.raises(PlbGpuError):
         lat2.adjoint_backward(np.zeros((6, 6, 6, 3)))   # no forward run yet
+    import ctypes
+    from palabos_gb300 import native as N
+    k = ctypes.c_int()
+    assert N.ERRORS[lat2.lib.plbgpu_adjoint_interval(lat2.ctx.h, lat2.handle, ctypes.byref(k))] == "PLBGPU_ERR_STATE"
 
 
 @pytest.mark.slow
