@@ -392,6 +392,11 @@ def main():
                     help="run only the Taylor-Green accuracy study (512^3, 5000 steps) and print its JSON")
     ap.add_argument("--accuracy-n", type=int, default=512)
     ap.add_argument("--accuracy-steps", type=int, default=5000)
+    ap.add_argument("--permeability", action="store_true",
+                    help="run only the sphere-packing permeability study (384^3, 20000 steps) and print its JSON")
+    ap.add_argument("--permeability-n", type=int, default=384)
+    ap.add_argument("--permeability-steps", type=int, default=20000)
+    ap.add_argument("--permeability-adjoint", type=int, nargs="+", default=[3000])
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -401,6 +406,14 @@ def main():
         ctx = Context(dist_env()[2])
         r = taylor_green_study(n=args.accuracy_n, steps=args.accuracy_steps, every=500, slab=8, ctx=ctx)
         print(json.dumps({"study": "taylor_green_storage_forms", **r}))
+        return
+    if args.permeability:
+        from palabos_gb300 import Context
+        from palabos_gb300.accuracy import permeability_study
+        ctx = Context(dist_env()[2])
+        r = permeability_study(n=args.permeability_n, steps=args.permeability_steps,
+                               adjoint_iterations=tuple(args.permeability_adjoint), ctx=ctx)
+        print(json.dumps({"study": "sphere_packing_permeability", **r}))
         return
     if args.impl == "reference":
         run_reference(args)

@@ -306,7 +306,15 @@ int plbgpu_load_state(plbgpu_ctx* ctx, int handle, int what, const char* plb_pat
  * of the backward sweep, recomputation included.
  * plbgpu_tangent_linear (FP64 domains): J and the directional derivative
  * dJ = grad J . (dforce, domega) from a dual-number run of T steps from the
- * current state, which it leaves unchanged. */
+ * current state, which it leaves unchanged.
+ *
+ * The _weighted forms take the objective J = sum over cells w . u(T) instead
+ * (w: 3 doubles per cell, transfer order), e.g. the mean flux
+ * w = (1/n, 0, 0) from which a permeability follows.
+ * plbgpu_adjoint_steady_weighted: the same gradients at a steady state (the
+ * domain's current state, taken as converged): `iterations` reverse steps
+ * linearised around that one state, no recorded run and no checkpoints
+ * (three states of memory); the gradient converges as the flow would relax. */
 int plbgpu_adjoint_forward(plbgpu_ctx* ctx, int handle, int T, int K);
 int plbgpu_adjoint_interval(plbgpu_ctx* ctx, int handle, int* K);
 int plbgpu_adjoint_backward(plbgpu_ctx* ctx, int handle, const double* u_target, size_t n_target,
@@ -315,6 +323,15 @@ int plbgpu_adjoint_backward(plbgpu_ctx* ctx, int handle, const double* u_target,
 int plbgpu_tangent_linear(plbgpu_ctx* ctx, int handle, int T, const double* dforce, size_t n_dforce,
                           double domega, const double* u_target, size_t n_target, double* objective,
                           double* directional);
+int plbgpu_adjoint_backward_weighted(plbgpu_ctx* ctx, int handle, const double* weights, size_t n_weights,
+                                     double* objective, double* grad_force, size_t n_grad, double* grad_omega,
+                                     float* ms);
+int plbgpu_tangent_linear_weighted(plbgpu_ctx* ctx, int handle, int T, const double* dforce, size_t n_dforce,
+                                   double domega, const double* weights, size_t n_weights, double* objective,
+                                   double* directional);
+int plbgpu_adjoint_steady_weighted(plbgpu_ctx* ctx, int handle, int iterations, const double* weights,
+                                   size_t n_weights, double* objective, double* grad_force, size_t n_grad,
+                                   double* grad_omega, float* ms);
 
 /* ------------------------------------------------------------ co-processor form */
 

@@ -74,3 +74,56 @@ def taylor_green_study(n=512, steps=5000, forms=("fp32", "bf16", "fp16", "bf16sr
     for lat in lats.values():
         lat.close()
     return out
+
+
+def _mean_flux(lat, n, slab=16):
+    """Mean x-velocity over all cells (walls count as 0): the superficial velocity."""
+    s = 0.0
+    for x0 in range(0, n, slab):
+        s += float(np.sum(lat.compute_velocity((x0, min(n, x0 + slab) - 1, 0, n - 1, 0, n - 1))[..., 0]))
+    return s / n ** 3
+
+
+def permeability_study(n=384, steps=20000, forms=("fp32", "bf16"), every=1000, adjoint_iterations=(3000,),
+                       force=1e-6, seed=77, ctx=None):
+    """Permeability of the sphere packing (periodic n^3 box, Guo force along
+    x, bounce-back spheres) in the FP64 form and the reduced-precision forms:
+    k = nu <u_x> / F after `steps` steps, with the flux history every `every`
+    steps, the MLUPS of each form, and dk/domega from the steady adjoint of
+    the converged state (FP64 and FP32; one entry per iteration count, so the
+    convergence of the adjoint sum shows)."""
+    wl = workloads.sphere_packing(n=n, seed=seed, force=force)
+    blocks = n // 32
+    fluid = wl.kinds != 3
+    kept = int(fluid[:blocks * 32, :blocks * 32, :blocks * 32]
+               .reshape(blocks, 32, blocks, 32, blocks, 32).any(axis=(1, 3, 5)).sum()) if blocks else 0
+    out = {"n": n, "steps": steps, "omega": wl.omega, "force": force, "porosity": float(fluid.mean()),
+           "blocks_32": blocks ** 3, "blocks_32_with_fluid": kept, "forms": {}}
+    w = None
+    for p in ("fp64",) + tuple(forms):
+        lat = wl.lattice(p, ctx)
+        seconds, history, done = 0.0, [], 0
+        while done < steps:
+            k = min(every, steps - done)
+            seconds += lat.time_steps(k) / 1e3
+            done += k
+            history.append(_mean_flux(lat, n))
+        flux = history[-1]
+        r = {"mean_ux": flux, "k": workloads.permeability(flux, force, wl.omega),
+             "flux_history": history, "mlups": round(n ** 3 * steps / seconds / 1e6, 1)}
+        if p in ("fp64", "fp32"):
+            if w is None:
+                w = np.zeros((n, n, n, 3))
+                w[..., 0] = 1.0 / n ** 3
+            r["adjoint"] = []
+            for it in adjoint_iterations:
+                J, _, g, ms = lat.adjoint_steady(w, it, want_force=False)
+                r["adjoint"].append({"iterations": it, "mean_ux": J, "d_mean_ux_domega": g,
+                                     "dk_domega": workloads.permeability_derivative(J, g, force, wl.omega),
+                                     "ms_per_iteration": round(ms / max(it, 1), 4)})
+        out["forms"][p] = r
+        lat.close()
+    k64 = out["forms"]["fp64"]["k"]
+    for p in forms:
+        out["forms"][p]["k_rel_err"] = abs(out["forms"][p]["k"] - k64) / abs(k64)
+    return out

@@ -404,8 +404,10 @@ __global__ void pushStepKernel(DevLattice L, NeighbourDeltas D, const R* fin, R*
 }
 
 // J, lambda^T = dJ/df^T and the explicit dJ/dF of the Guo velocity u = j/rho + F/2.
+// Two objectives: the mismatch J = 1/2 sum |u - u*|^2 (v = u*), and the
+// weighted velocity J = sum w . u (v = w, `weighted`), e.g. the mean flux.
 template <typename R>
-__global__ void objectiveKernel(DevLattice L, const R* f, const double* uTarget, R invRho0, R* lam,
+__global__ void objectiveKernel(DevLattice L, const R* f, const double* v, bool weighted, R invRho0, R* lam,
                                 R* gF, AdjAcc* acc) {
     const int z = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y, x = blockIdx.z;
@@ -417,10 +419,15 @@ __global__ void objectiveKernel(DevLattice L, const R* f, const double* uTarget,
         for (int i = 0; i < 19; ++i) fc[i] = f[i * L.n + idx];
         cellForce(L, forceIsFp64<R>(), idx, nullptr, F);
         cellVelocity<R>(k, fc, F, invRho0, u);
-        R dv[3];
+        R dv[3];   // dJ/du
         for (int d = 0; d < 3; ++d) {
-            dv[d] = u[d] - (R)uTarget[3 * idx + d];
-            jsum += 0.5 * (double)dv[d] * (double)dv[d];
+            if (weighted) {
+                dv[d] = (R)v[3 * idx + d];
+                jsum += v[3 * idx + d] * (double)u[d];
+            } else {
+                dv[d] = u[d] - (R)v[3 * idx + d];
+                jsum += 0.5 * (double)dv[d] * (double)dv[d];
+            }
         }
         if (k == K_BGK || k == K_GUO || k == K_INCBGK) {
             R rho = R(1), jv[3] = {R(0), R(0), R(0)};
@@ -478,7 +485,7 @@ __global__ void adjointStepKernel(DevLattice L, NeighbourDeltas D, const R* f, c
 }
 
 // J and its tangent from a dual state.
-__global__ void dualObjectiveKernel(DevLattice L, const Dual* f, const double* dF, const double* uTarget,
+__global__ void dualObjectiveKernel(DevLattice L, const Dual* f, const double* dF, const double* v, bool weighted,
                                     double invRho0, AdjAcc* acc) {
     const int z = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y, x = blockIdx.z;
@@ -491,9 +498,14 @@ __global__ void dualObjectiveKernel(DevLattice L, const Dual* f, const double* d
         cellForce(L, true, idx, dF, F);
         cellVelocity<Dual>(k, fc, F, Dual(invRho0), u);
         for (int d = 0; d < 3; ++d) {
-            const Dual dv = u[d] - Dual(uTarget[3 * idx + d]);
-            jv += 0.5 * dv.v * dv.v;
-            jd += dv.v * dv.d;
+            if (weighted) {
+                jv += v[3 * idx + d] * u[d].v;
+                jd += v[3 * idx + d] * u[d].d;
+            } else {
+                const Dual dv = u[d] - Dual(v[3 * idx + d]);
+                jv += 0.5 * dv.v * dv.v;
+                jd += dv.v * dv.d;
+            }
         }
     }
     blockAdd(jv, acc->objective);
@@ -614,7 +626,7 @@ int forwardImpl(plbgpu_ctx* c, int h, DomainAccess& a, AdjointState* st, int T, 
 }
 
 template <typename R>
-int backwardImpl(DomainAccess& a, AdjointState* st, double* objective, double* gOmega, float* ms) {
+int backwardImpl(DomainAccess& a, AdjointState* st, bool weighted, double* objective, double* gOmega, float* ms) {
     const long long n = a.L.n, sz = 19 * n;
     R* ck = static_cast<R*>(st->ckpt);
     R* sg = static_cast<R*>(st->seg);
@@ -630,7 +642,7 @@ int backwardImpl(DomainAccess& a, AdjointState* st, double* objective, double* g
     cudaMemsetAsync(st->acc, 0, sizeof(AdjAcc), a.stream);
     const int T = st->T, K = st->K;
     objectiveKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, ck + (long long)(T / K) * sz,
-                                                                       st->uT, invRho0, lam, gF, st->acc);
+                                                                       st->uT, weighted, invRho0, lam, gF, st->acc);
     *a.launches += 1;
     int cur = 0;   // lam + cur * sz holds lambda^{t+1}
     for (int s = T / K - 1; s >= 0; --s) {
@@ -660,6 +672,163 @@ int backwardImpl(DomainAccess& a, AdjointState* st, double* objective, double* g
     *objective = slotSum(h.objective);
     *gOmega = slotSum(h.gOmega);
     return cudaGetLastError() == cudaSuccess ? PLBGPU_OK : PLBGPU_ERR_CUDA;
+}
+
+// dJ/dF planes [3][n] on the device -> grad_force [cell][3] in transfer order.
+template <typename R>
+int forceGradientOut(plbgpu_ctx* c, const DomainAccess& a, const R* gF, double* grad_force) {
+    const long long n = a.L.n;
+    std::vector<R> planes((size_t)3 * n);
+    ADJ_TRY(cudaMemcpyAsync(planes.data(), gF, sizeof(R) * 3 * n, cudaMemcpyDeviceToHost, a.stream));
+    ADJ_TRY(cudaStreamSynchronize(a.stream));
+    for (long long i = 0; i < n; ++i)
+        for (int d = 0; d < 3; ++d) grad_force[3 * i + d] = (double)planes[d * n + i];
+    return PLBGPU_OK;
+}
+
+int adjointBackward(plbgpu_ctx* c, int h, const double* v, size_t n3, bool weighted, double* objective,
+                    double* grad_force, size_t ng, double* grad_omega, float* ms) {
+    DomainAccess a;
+    int rc = domainAccess(c, h, &a);
+    if (rc) return rc;
+    AdjointState* st = static_cast<AdjointState*>(*a.adjointSlot);
+    if (!st || !st->ready) return domainFail(c, PLBGPU_ERR_STATE, "adjoint: no recorded forward run");
+    const long long n = a.L.n;
+    if (!v || (long long)n3 != 3 * n || !objective || !grad_omega)
+        return domainFail(c, PLBGPU_ERR_ARG, "adjoint: the objective needs 3 values per cell");
+    if (grad_force && (long long)ng != 3 * n)
+        return domainFail(c, PLBGPU_ERR_ARG, "adjoint: grad_force needs 3 values per cell");
+    ADJ_TRY(cudaMemcpyAsync(st->uT, v, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, a.stream));
+    rc = a.precision == PLBGPU_FP64 ? backwardImpl<double>(a, st, weighted, objective, grad_omega, ms)
+                                    : backwardImpl<float>(a, st, weighted, objective, grad_omega, ms);
+    if (rc) return domainFail(c, rc, "adjoint: backward sweep failed");
+    if (!grad_force) return PLBGPU_OK;
+    return a.precision == PLBGPU_FP64 ? forceGradientOut(c, a, static_cast<const double*>(st->gF), grad_force)
+                                      : forceGradientOut(c, a, static_cast<const float*>(st->gF), grad_force);
+}
+
+// Adjoint of a steady state: the domain's state f is a fixed point of the
+// step, so every reverse step linearises around the same f.  The sweep sums
+// (d out / d theta)^T lambda over `iterations` reverse steps from
+// lambda = dJ/df; the sum converges to the derivative of J at the steady
+// state (lambda decays at the rate the flow relaxes; the one mode it keeps,
+// total mass, adds nothing because the collision conserves mass for every
+// omega and force).  Three states of memory whatever the number of steps.
+template <typename R>
+int steadyImpl(plbgpu_ctx* c, DomainAccess& a, int iterations, const double* weights, double* objective,
+               double* grad_force, double* grad_omega, float* ms) {
+    const long long n = a.L.n, sz = 19 * n;
+    struct Buffers {
+        R* f = nullptr;
+        R* lam = nullptr;
+        R* gF = nullptr;
+        double* w = nullptr;
+        AdjAcc* acc = nullptr;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        ~Buffers() {
+            cudaFree(f);
+            cudaFree(lam);
+            cudaFree(gF);
+            cudaFree(w);
+            cudaFree(acc);
+            if (e0) cudaEventDestroy(e0);
+            if (e1) cudaEventDestroy(e1);
+        }
+    } b;
+    ADJ_TRY(cudaMalloc(&b.f, sizeof(R) * sz));
+    ADJ_TRY(cudaMalloc(&b.lam, sizeof(R) * sz * 2));
+    ADJ_TRY(cudaMalloc(&b.gF, sizeof(R) * 3 * n));
+    ADJ_TRY(cudaMalloc(&b.w, sizeof(double) * 3 * n));
+    ADJ_TRY(cudaMalloc(&b.acc, sizeof(AdjAcc)));
+    ADJ_TRY(cudaEventCreate(&b.e0));
+    ADJ_TRY(cudaEventCreate(&b.e1));
+    ADJ_TRY(cudaMemcpyAsync(b.w, weights, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, a.stream));
+    ADJ_TRY(cudaMemsetAsync(b.gF, 0, sizeof(R) * 3 * n, a.stream));
+    ADJ_TRY(cudaMemsetAsync(b.acc, 0, sizeof(AdjAcc), a.stream));
+    const R omega = (R)a.omega, invRho0 = (R)(1.0 / a.rho0);
+    const NeighbourDeltas D = deltasOf(a.L);
+    ADJ_TRY(cudaEventRecord(b.e0, a.stream));
+    stateOutAny<R>(a.precision, a.L, a.odd, b.f, a.stream);
+    objectiveKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, b.f, b.w, true, invRho0, b.lam, b.gF,
+                                                                       b.acc);
+    *a.launches += 2;
+    int cur = 0;
+    for (int t = 0; t < iterations; ++t) {
+        adjointStepKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, D, b.f, b.lam + cur * sz,
+                                                                             b.lam + (1 - cur) * sz, b.gF, omega,
+                                                                             invRho0, b.acc);
+        *a.launches += 1;
+        cur = 1 - cur;
+    }
+    ADJ_TRY(cudaGetLastError());
+    ADJ_TRY(cudaEventRecord(b.e1, a.stream));
+    ADJ_TRY(cudaEventSynchronize(b.e1));
+    if (ms) ADJ_TRY(cudaEventElapsedTime(ms, b.e0, b.e1));
+    AdjAcc h;
+    ADJ_TRY(cudaMemcpyAsync(&h, b.acc, sizeof(AdjAcc), cudaMemcpyDeviceToHost, a.stream));
+    ADJ_TRY(cudaStreamSynchronize(a.stream));
+    *objective = slotSum(h.objective);
+    *grad_omega = slotSum(h.gOmega);
+    return grad_force ? forceGradientOut(c, a, b.gF, grad_force) : PLBGPU_OK;
+}
+
+int tangentLinear(plbgpu_ctx* c, int h, int T, const double* dforce, size_t ndf, double domega,
+                  const double* u_target, size_t n3, bool weighted, double* objective, double* directional) {
+    DomainAccess a;
+    int rc = domainAccess(c, h, &a);
+    if (rc) return rc;
+    if (a.precision != PLBGPU_FP64) return domainFail(c, PLBGPU_ERR_ARG, "tangent: FP64 domains only");
+    const long long n = a.L.n, sz = 19 * n;
+    if (T < 0 || !u_target || (long long)n3 != 3 * n || !objective || !directional || (dforce && (long long)ndf != 3 * n))
+        return domainFail(c, PLBGPU_ERR_ARG, "tangent: bad arguments");
+    if ((rc = checkKinds(c, a))) return rc;
+    if (a.pending) return domainFail(c, PLBGPU_ERR_STATE, "tangent: boundary faces are not supported");
+    double *f0 = nullptr, *dF = nullptr, *uT = nullptr;
+    Dual* buf = nullptr;
+    AdjAcc* acc = nullptr;
+    std::vector<double> planes((size_t)3 * n, 0.);
+    if (dforce)
+        for (long long i = 0; i < n; ++i)
+            for (int d = 0; d < 3; ++d) planes[d * n + i] = dforce[3 * i + d];
+    cudaError_t e = cudaMalloc(&f0, sizeof(double) * sz);
+    if (e == cudaSuccess) e = cudaMalloc(&buf, sizeof(Dual) * sz * 2);
+    if (e == cudaSuccess) e = cudaMalloc(&dF, sizeof(double) * 3 * n);
+    if (e == cudaSuccess) e = cudaMalloc(&uT, sizeof(double) * 3 * n);
+    if (e == cudaSuccess) e = cudaMalloc(&acc, sizeof(AdjAcc));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dF, planes.data(), sizeof(double) * 3 * n, cudaMemcpyHostToDevice, a.stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(uT, u_target, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, a.stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(acc, 0, sizeof(AdjAcc), a.stream);
+    if (e == cudaSuccess) {
+        stateOutAny<double>(a.precision, a.L, a.odd, f0, a.stream);
+        toDualKernel<double><<<(unsigned)((sz + 255) / 256), 256, 0, a.stream>>>(sz, f0, buf);
+        *a.launches += 2;
+        Dual* cur = buf;
+        Dual* nxt = buf + sz;
+        const Dual om(a.omega, domega), inv0(1.0 / a.rho0);
+        const NeighbourDeltas D = deltasOf(a.L);
+        for (int t = 0; t < T; ++t) {
+            pushStepKernel<Dual><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, D, cur, nxt, om, inv0, dF);
+            *a.launches += 1;
+            std::swap(cur, nxt);
+        }
+        dualObjectiveKernel<<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, cur, dF, uT, weighted, 1.0 / a.rho0, acc);
+        *a.launches += 1;
+        e = cudaGetLastError();
+        AdjAcc hacc;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&hacc, acc, sizeof(AdjAcc), cudaMemcpyDeviceToHost, a.stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(a.stream);
+        if (e == cudaSuccess) {
+            *objective = slotSum(hacc.objective);
+            *directional = slotSum(hacc.tangent);
+        }
+    }
+    cudaFree(f0); cudaFree(buf); cudaFree(dF); cudaFree(uT); cudaFree(acc);
+    if (e != cudaSuccess) {
+        char m[256];
+        snprintf(m, sizeof(m), "tangent: %s", cudaGetErrorString(e));
+        return domainFail(c, e == cudaErrorMemoryAllocation ? PLBGPU_ERR_NOMEM : PLBGPU_ERR_CUDA, m);
+    }
+    return PLBGPU_OK;
 }
 
 }  // namespace
@@ -736,94 +905,38 @@ int plbgpu_adjoint_interval(plbgpu_ctx* c, int h, int* K) {
 
 int plbgpu_adjoint_backward(plbgpu_ctx* c, int h, const double* u_target, size_t n3, double* objective,
                             double* grad_force, size_t ng, double* grad_omega, float* ms) {
+    return adjointBackward(c, h, u_target, n3, false, objective, grad_force, ng, grad_omega, ms);
+}
+
+int plbgpu_adjoint_backward_weighted(plbgpu_ctx* c, int h, const double* weights, size_t n3, double* objective,
+                                     double* grad_force, size_t ng, double* grad_omega, float* ms) {
+    return adjointBackward(c, h, weights, n3, true, objective, grad_force, ng, grad_omega, ms);
+}
+
+int plbgpu_adjoint_steady_weighted(plbgpu_ctx* c, int h, int iterations, const double* weights, size_t n3,
+                                   double* objective, double* grad_force, size_t ng, double* grad_omega, float* ms) {
     DomainAccess a;
     int rc = domainAccess(c, h, &a);
     if (rc) return rc;
-    AdjointState* st = static_cast<AdjointState*>(*a.adjointSlot);
-    if (!st || !st->ready) return domainFail(c, PLBGPU_ERR_STATE, "adjoint: no recorded forward run");
     const long long n = a.L.n;
-    if (!u_target || (long long)n3 != 3 * n || !objective || !grad_omega)
-        return domainFail(c, PLBGPU_ERR_ARG, "adjoint: u_target needs 3 values per cell");
-    if (grad_force && (long long)ng != 3 * n) return domainFail(c, PLBGPU_ERR_ARG, "adjoint: grad_force needs 3 values per cell");
-    ADJ_TRY(cudaMemcpyAsync(st->uT, u_target, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, a.stream));
-    rc = a.precision == PLBGPU_FP64 ? backwardImpl<double>(a, st, objective, grad_omega, ms)
-                                    : backwardImpl<float>(a, st, objective, grad_omega, ms);
-    if (rc) return domainFail(c, rc, "adjoint: backward sweep failed");
-    if (grad_force) {
-        // planes [3][n] -> [cell][3]
-        std::vector<double> planes((size_t)3 * n);
-        if (a.precision == PLBGPU_FP64) {
-            ADJ_TRY(cudaMemcpyAsync(planes.data(), st->gF, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, a.stream));
-            ADJ_TRY(cudaStreamSynchronize(a.stream));
-        } else {
-            std::vector<float> pf((size_t)3 * n);
-            ADJ_TRY(cudaMemcpyAsync(pf.data(), st->gF, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, a.stream));
-            ADJ_TRY(cudaStreamSynchronize(a.stream));
-            for (size_t i = 0; i < pf.size(); ++i) planes[i] = pf[i];
-        }
-        for (long long i = 0; i < n; ++i)
-            for (int d = 0; d < 3; ++d) grad_force[3 * i + d] = planes[d * n + i];
-    }
-    return PLBGPU_OK;
+    if (iterations < 0 || !weights || (long long)n3 != 3 * n || !objective || !grad_omega ||
+        (grad_force && (long long)ng != 3 * n))
+        return domainFail(c, PLBGPU_ERR_ARG, "steady adjoint: weights (and grad_force) need 3 values per cell");
+    if ((rc = checkKinds(c, a))) return rc;
+    if (a.pending) return domainFail(c, PLBGPU_ERR_STATE, "steady adjoint: boundary faces are not supported");
+    return a.precision == PLBGPU_FP64
+               ? steadyImpl<double>(c, a, iterations, weights, objective, grad_force, grad_omega, ms)
+               : steadyImpl<float>(c, a, iterations, weights, objective, grad_force, grad_omega, ms);
 }
 
 int plbgpu_tangent_linear(plbgpu_ctx* c, int h, int T, const double* dforce, size_t ndf, double domega,
                           const double* u_target, size_t n3, double* objective, double* directional) {
-    DomainAccess a;
-    int rc = domainAccess(c, h, &a);
-    if (rc) return rc;
-    if (a.precision != PLBGPU_FP64) return domainFail(c, PLBGPU_ERR_ARG, "tangent: FP64 domains only");
-    const long long n = a.L.n, sz = 19 * n;
-    if (T < 0 || !u_target || (long long)n3 != 3 * n || !objective || !directional || (dforce && (long long)ndf != 3 * n))
-        return domainFail(c, PLBGPU_ERR_ARG, "tangent: bad arguments");
-    if ((rc = checkKinds(c, a))) return rc;
-    if (a.pending) return domainFail(c, PLBGPU_ERR_STATE, "tangent: boundary faces are not supported");
-    double *f0 = nullptr, *dF = nullptr, *uT = nullptr;
-    Dual* buf = nullptr;
-    AdjAcc* acc = nullptr;
-    std::vector<double> planes((size_t)3 * n, 0.);
-    if (dforce)
-        for (long long i = 0; i < n; ++i)
-            for (int d = 0; d < 3; ++d) planes[d * n + i] = dforce[3 * i + d];
-    cudaError_t e = cudaMalloc(&f0, sizeof(double) * sz);
-    if (e == cudaSuccess) e = cudaMalloc(&buf, sizeof(Dual) * sz * 2);
-    if (e == cudaSuccess) e = cudaMalloc(&dF, sizeof(double) * 3 * n);
-    if (e == cudaSuccess) e = cudaMalloc(&uT, sizeof(double) * 3 * n);
-    if (e == cudaSuccess) e = cudaMalloc(&acc, sizeof(AdjAcc));
-    if (e == cudaSuccess) e = cudaMemcpyAsync(dF, planes.data(), sizeof(double) * 3 * n, cudaMemcpyHostToDevice, a.stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(uT, u_target, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, a.stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(acc, 0, sizeof(AdjAcc), a.stream);
-    if (e == cudaSuccess) {
-        stateOutAny<double>(a.precision, a.L, a.odd, f0, a.stream);
-        toDualKernel<double><<<(unsigned)((sz + 255) / 256), 256, 0, a.stream>>>(sz, f0, buf);
-        *a.launches += 2;
-        Dual* cur = buf;
-        Dual* nxt = buf + sz;
-        const Dual om(a.omega, domega), inv0(1.0 / a.rho0);
-        const NeighbourDeltas D = deltasOf(a.L);
-        for (int t = 0; t < T; ++t) {
-            pushStepKernel<Dual><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, D, cur, nxt, om, inv0, dF);
-            *a.launches += 1;
-            std::swap(cur, nxt);
-        }
-        dualObjectiveKernel<<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, cur, dF, uT, 1.0 / a.rho0, acc);
-        *a.launches += 1;
-        e = cudaGetLastError();
-        AdjAcc hacc;
-        if (e == cudaSuccess) e = cudaMemcpyAsync(&hacc, acc, sizeof(AdjAcc), cudaMemcpyDeviceToHost, a.stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(a.stream);
-        if (e == cudaSuccess) {
-            *objective = slotSum(hacc.objective);
-            *directional = slotSum(hacc.tangent);
-        }
-    }
-    cudaFree(f0); cudaFree(buf); cudaFree(dF); cudaFree(uT); cudaFree(acc);
-    if (e != cudaSuccess) {
-        char m[256];
-        snprintf(m, sizeof(m), "tangent: %s", cudaGetErrorString(e));
-        return domainFail(c, e == cudaErrorMemoryAllocation ? PLBGPU_ERR_NOMEM : PLBGPU_ERR_CUDA, m);
-    }
-    return PLBGPU_OK;
+    return tangentLinear(c, h, T, dforce, ndf, domega, u_target, n3, false, objective, directional);
+}
+
+int plbgpu_tangent_linear_weighted(plbgpu_ctx* c, int h, int T, const double* dforce, size_t ndf, double domega,
+                                   const double* weights, size_t n3, double* objective, double* directional) {
+    return tangentLinear(c, h, T, dforce, ndf, domega, weights, n3, true, objective, directional);
 }
 
 }  // extern "C"

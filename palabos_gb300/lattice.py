@@ -313,30 +313,53 @@ class DeviceLattice3D:
         self._check(self.lib.plbgpu_adjoint_interval(self.ctx.h, self.handle, ctypes.byref(k)))
         return k.value
 
-    def adjoint_backward(self, u_target, want_force=True):
-        """J = 1/2 sum |u(T) - u*|^2, dJ/dF (nx,ny,nz,3) and dJ/domega of the
-        last adjoint_forward run; also the device time of the sweep in ms."""
-        ut = np.ascontiguousarray(u_target, np.float64).reshape(-1)
-        n3 = 3 * self._cells(self.bounding_box)
+    def _objective(self, u_target, weights):
+        if (u_target is None) == (weights is None):
+            raise ValueError("give exactly one of u_target (mismatch objective) and weights (weighted velocity)")
+        v = u_target if weights is None else weights
+        return np.ascontiguousarray(v, np.float64).reshape(-1), weights is not None
+
+    def adjoint_backward(self, u_target=None, want_force=True, weights=None):
+        """Gradients of the last adjoint_forward run.  Objective J = 1/2 sum
+        |u(T) - u*|^2 (u_target = u*), or J = sum w . u(T) (weights = w, e.g.
+        the mean flux).  Returns J, dJ/dF (nx,ny,nz,3), dJ/domega and the
+        device time of the sweep in ms."""
+        v, weighted = self._objective(u_target, weights)
+        fn = self.lib.plbgpu_adjoint_backward_weighted if weighted else self.lib.plbgpu_adjoint_backward
         J = ctypes.c_double()
         go = ctypes.c_double()
         ms = ctypes.c_float()
-        g = np.empty(n3 if want_force else 0, np.float64)
-        self._check(self.lib.plbgpu_adjoint_backward(self.ctx.h, self.handle, _dp(ut), ut.size, ctypes.byref(J),
-                                                     _dp(g) if want_force else None, g.size, ctypes.byref(go),
-                                                     ctypes.byref(ms)))
+        g = np.empty(v.size if want_force else 0, np.float64)
+        self._check(fn(self.ctx.h, self.handle, _dp(v), v.size, ctypes.byref(J), _dp(g) if want_force else None,
+                       g.size, ctypes.byref(go), ctypes.byref(ms)))
         grad = g.reshape(self.shape + (3,)) if want_force else None
         return J.value, grad, go.value, ms.value
 
-    def tangent_linear(self, T, dforce, domega, u_target):
-        """(J, grad J . (dforce, domega)) from a dual-number run of T steps."""
-        ut = np.ascontiguousarray(u_target, np.float64).reshape(-1)
+    def adjoint_steady(self, weights, iterations, want_force=True):
+        """Gradients of J = sum w . u at the current (converged) state from
+        `iterations` reverse steps around it.  Returns J, dJ/dF, dJ/domega
+        and the device time in ms."""
+        v = np.ascontiguousarray(weights, np.float64).reshape(-1)
+        J = ctypes.c_double()
+        go = ctypes.c_double()
+        ms = ctypes.c_float()
+        g = np.empty(v.size if want_force else 0, np.float64)
+        self._check(self.lib.plbgpu_adjoint_steady_weighted(self.ctx.h, self.handle, int(iterations), _dp(v), v.size,
+                                                            ctypes.byref(J), _dp(g) if want_force else None, g.size,
+                                                            ctypes.byref(go), ctypes.byref(ms)))
+        grad = g.reshape(self.shape + (3,)) if want_force else None
+        return J.value, grad, go.value, ms.value
+
+    def tangent_linear(self, T, dforce, domega, u_target=None, weights=None):
+        """(J, grad J . (dforce, domega)) from a dual-number run of T steps;
+        the objective as in adjoint_backward."""
+        v, weighted = self._objective(u_target, weights)
+        fn = self.lib.plbgpu_tangent_linear_weighted if weighted else self.lib.plbgpu_tangent_linear
         df = None if dforce is None else np.ascontiguousarray(dforce, np.float64).reshape(-1)
         J = ctypes.c_double()
         dj = ctypes.c_double()
-        self._check(self.lib.plbgpu_tangent_linear(self.ctx.h, self.handle, int(T), None if df is None else _dp(df),
-                                                   0 if df is None else df.size, float(domega), _dp(ut), ut.size,
-                                                   ctypes.byref(J), ctypes.byref(dj)))
+        self._check(fn(self.ctx.h, self.handle, int(T), None if df is None else _dp(df), 0 if df is None else df.size,
+                       float(domega), _dp(v), v.size, ctypes.byref(J), ctypes.byref(dj)))
         return J.value, dj.value
 
     def compute_average_energy(self, box=None):

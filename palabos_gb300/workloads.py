@@ -120,41 +120,72 @@ def forced_channel(shape=(128, 64, 64), omega=1.6, seed=1234, sigma=1e-6, drive=
     return Workload("forced_channel", shape, omega, (1, 0, 0), kinds, force=force)
 
 
-def sphere_packing(n=384, porosity=0.4, rmin=6.0, rmax=12.0, seed=77, force=1e-6):
+def sphere_packing(n=384, porosity=0.68, rmin=6.0, rmax=12.0, seed=77, force=1e-6, omega=1.0,
+                   max_attempts=400000):
     """Sphere packing: periodic box, seeded non-overlapping spheres with radius
-    U[rmin, rmax] placed by rejection sampling until the porosity reaches the
-    target, as bounce-back cells; Guo force along x in the fluid."""
+    U[rmin, rmax] placed by random sequential addition until the porosity
+    (fluid fraction) falls to the target or the attempts run out, as
+    bounce-back cells; Guo force along x in every cell (only the fluid uses
+    it).  Non-overlapping random addition jams near a solid fraction of 0.38,
+    and the rejections multiply well before that: at n = 384 the default
+    0.68 takes a little over 3 x 10^5 attempts (porosity 0.72 after 10^5),
+    and 0.65 is not reached in 4 x 10^5.  Overlap tests use a grid of
+    buckets of side 2 rmax."""
     rng = np.random.default_rng(seed)
     solid = np.zeros((n, n, n), bool)
-    centers, radii = [], []
+    nb = max(1, int(n // (2 * rmax)))
+    side = n / nb
+    buckets = {}
     target = (1.0 - porosity) * n ** 3
     filled = 0
     attempts = 0
-    while filled < target and attempts < 200000:
+    while filled < target and attempts < max_attempts:
         attempts += 1
         r = rng.uniform(rmin, rmax)
         c = rng.uniform(0, n, size=3)
+        b = (c // side).astype(int) % nb
         ok = True
-        for c2, r2 in zip(centers, radii):
-            d = np.abs(c - c2)
-            d = np.minimum(d, n - d)
-            if np.dot(d, d) < (r + r2) ** 2:
-                ok = False
+        for dx in (-1, 0, 1):
+            for dy in (-1, 0, 1):
+                for dz in (-1, 0, 1):
+                    for c2, r2 in buckets.get(((b[0] + dx) % nb, (b[1] + dy) % nb, (b[2] + dz) % nb), ()):
+                        d = np.abs(c - c2)
+                        d = np.minimum(d, n - d)
+                        if d[0] * d[0] + d[1] * d[1] + d[2] * d[2] < (r + r2) ** 2:
+                            ok = False
+                            break
+                    if not ok:
+                        break
+                if not ok:
+                    break
+            if not ok:
                 break
         if not ok:
             continue
-        centers.append(c)
-        radii.append(r)
+        buckets.setdefault(tuple(b), []).append((c, r))
         lo = np.floor(c - r).astype(int)
         hi = np.ceil(c + r).astype(int)
         ax = [np.arange(lo[a], hi[a] + 1) for a in range(3)]
         X, Y, Z = np.meshgrid(*ax, indexing="ij")
         m = (X - c[0]) ** 2 + (Y - c[1]) ** 2 + (Z - c[2]) ** 2 <= r * r
-        sl = solid[np.mod(X[m], n), np.mod(Y[m], n), np.mod(Z[m], n)]
-        filled += int((~sl).sum())
-        solid[np.mod(X[m], n), np.mod(Y[m], n), np.mod(Z[m], n)] = True
+        ix, iy, iz = np.mod(X[m], n), np.mod(Y[m], n), np.mod(Z[m], n)
+        filled += int((~solid[ix, iy, iz]).sum())
+        solid[ix, iy, iz] = True
     kinds = np.where(solid, N.BOUNCEBACK, N.GUO).astype(np.uint8)
     f = np.zeros((n, n, n, 3))
     f[..., 0] = force
-    # omega = 1 (nu = 1/6): the configuration fixes the force, not the viscosity
-    return Workload("sphere_packing", (n, n, n), 1.0, (1, 1, 1), kinds, force=f)
+    # omega = 1 (nu = 1/6) by default: the configuration fixes the force, not the viscosity
+    return Workload("sphere_packing", (n, n, n), omega, (1, 1, 1), kinds, force=f)
+
+
+def permeability(mean_ux, force, omega):
+    """Darcy permeability k = nu <u_x> / F of a body-forced periodic medium:
+    <u_x> the superficial velocity (mean over all cells, walls counted as 0),
+    F the force density, nu = (1/omega - 1/2) / 3."""
+    return (1.0 / omega - 0.5) / 3.0 * mean_ux / force
+
+
+def permeability_derivative(mean_ux, d_mean_ux_domega, force, omega):
+    """dk/domega from <u_x> and its derivative d<u_x>/domega."""
+    nu = (1.0 / omega - 0.5) / 3.0
+    return (-1.0 / (3.0 * omega * omega) * mean_ux + nu * d_mean_ux_domega) / force

@@ -144,3 +144,127 @@ def test_forced_channel_gradient_full_size():
         fd = (_oracle_objective(wl, f0, fp, wl.omega, T, u_target) -
               _oracle_objective(wl, f0, fm, wl.omega, T, u_target)) / (2 * hF)
         assert gF[x, y, z, 0] == pytest.approx(fd, rel=1e-5), (gF[x, y, z, 0], fd)
+
+
+def _flux_weights(shape):
+    """J = mean x-velocity over all cells (the superficial velocity)."""
+    w = np.zeros(shape + (3,))
+    w[..., 0] = 1.0 / np.prod(shape)
+    return w
+
+
+@pytest.mark.parametrize("K", [1, 6])
+def test_weighted_adjoint_matches_tangent_linear(K):
+    wl, _, T = _case()
+    rng = np.random.default_rng(21)
+    w = rng.standard_normal(wl.shape + (3,))
+    lat = wl.lattice("fp64")
+    dF = rng.standard_normal(wl.shape + (3,))
+    dF[wl.kinds != 1] = 0.0
+    J_t, dJ = lat.tangent_linear(T, dF, -0.4, weights=w)
+    lat.adjoint_forward(T, K)
+    J, gF, gO, _ = lat.adjoint_backward(weights=w)
+    assert J == pytest.approx(J_t, rel=1e-13)
+    adj = float(np.sum(gF * dF)) + gO * -0.4
+    assert adj == pytest.approx(dJ, rel=1e-9), (adj, dJ)
+
+
+def test_weighted_adjoint_matches_reference_finite_differences():
+    """Mean-flux objective against central differences of the CPU oracle."""
+    wl, _, T = _case()
+    w = _flux_weights(wl.shape)
+    lat = wl.lattice("fp64")
+    f0 = lat.receive()
+    lat.adjoint_forward(T, 4)
+    J, gF, gO, _ = lat.adjoint_backward(weights=w)
+
+    def objective(force, omega):
+        ol = O.OracleLattice(*wl.shape, wl.periodic, omega, wl.kinds, None, force)
+        f, _ = ol.run(f0, T, with_stats=False)
+        return float(np.sum(ol.velocity(f) * w))
+
+    assert J == pytest.approx(objective(wl.force, wl.omega), rel=1e-12)
+    h = 1e-6
+    fd = (objective(wl.force, wl.omega + h) - objective(wl.force, wl.omega - h)) / (2 * h)
+    assert gO == pytest.approx(fd, rel=1e-5), (gO, fd)
+    rng = np.random.default_rng(8)
+    fluid = np.argwhere(wl.kinds == 1)
+    for _ in range(3):
+        x, y, z = fluid[rng.integers(len(fluid))]
+        fp = wl.force.copy()
+        fm = wl.force.copy()
+        fp[x, y, z, 0] += h
+        fm[x, y, z, 0] -= h
+        fd = (objective(fp, wl.omega) - objective(fm, wl.omega)) / (2 * h)
+        assert gF[x, y, z, 0] == pytest.approx(fd, rel=1e-5), (gF[x, y, z, 0], fd)
+
+
+def _converged_packing(omega, force=None, steps=6000, prec="fp64"):
+    wl = workloads.sphere_packing(n=20, porosity=0.6, rmin=2.5, rmax=4.5, seed=5, force=1e-5, omega=omega)
+    if force is not None:
+        wl.force = force
+    lat = wl.lattice(prec)
+    lat.collide_and_stream(steps)
+    return wl, lat
+
+
+def test_steady_adjoint_permeability_gradient():
+    """dk/domega and dk/dF of a converged sphere packing from the steady
+    adjoint, against central differences of converged forward runs."""
+    omega = 1.2
+    wl, lat = _converged_packing(omega)
+    w = _flux_weights(wl.shape)
+    u = lat.compute_velocity()
+    J, gF, gO, _ = lat.adjoint_steady(w, 3000)
+    assert J == pytest.approx(float(np.mean(u[..., 0])), rel=1e-12)
+    J2, _, gO2, _ = lat.adjoint_steady(w, 6000, want_force=False)
+    assert gO2 == pytest.approx(gO, rel=1e-9)       # the sum has converged
+
+    def flux(om, force=None):
+        _, l2 = _converged_packing(om, force)
+        return float(np.mean(l2.compute_velocity()[..., 0]))
+
+    h = 1e-5
+    fd = (flux(omega + h) - flux(omega - h)) / (2 * h)
+    assert gO == pytest.approx(fd, rel=1e-5), (gO, fd)
+    k = workloads.permeability(J, 1e-5, omega)
+    dk = workloads.permeability_derivative(J, gO, 1e-5, omega)
+    k_p = workloads.permeability(flux(omega + h), 1e-5, omega + h)
+    k_m = workloads.permeability(flux(omega - h), 1e-5, omega - h)
+    assert dk == pytest.approx((k_p - k_m) / (2 * h), rel=1e-5)
+    assert k > 0
+    rng = np.random.default_rng(4)
+    fluid = np.argwhere(wl.kinds == 1)
+    hF = 1e-8
+    for _ in range(2):
+        x, y, z = fluid[rng.integers(len(fluid))]
+        fp = wl.force.copy()
+        fm = wl.force.copy()
+        fp[x, y, z, 0] += hF
+        fm[x, y, z, 0] -= hF
+        fd = (flux(omega, fp) - flux(omega, fm)) / (2 * hF)
+        assert gF[x, y, z, 0] == pytest.approx(fd, rel=1e-5), (gF[x, y, z, 0], fd)
+
+
+def test_steady_adjoint_fp32_tracks_fp64():
+    g = {}
+    for prec in ("fp64", "fp32"):
+        wl, lat = _converged_packing(1.2, prec=prec)
+        J, gF, gO, _ = lat.adjoint_steady(_flux_weights(wl.shape), 3000)
+        g[prec] = (J, gF, gO)
+    assert g["fp32"][0] == pytest.approx(g["fp64"][0], rel=1e-4)
+    assert g["fp32"][2] == pytest.approx(g["fp64"][2], rel=1e-3)
+    assert np.abs(g["fp32"][1] - g["fp64"][1]).max() <= 1e-3 * np.abs(g["fp64"][1]).max()
+
+
+def test_adjoint_objective_arguments():
+    from palabos_gb300 import DeviceLattice3D, PlbGpuError
+    lat = DeviceLattice3D(6, 6, 6, 1.2)
+    with pytest.raises(ValueError):
+        lat.adjoint_backward()                       # neither objective
+    with pytest.raises(ValueError):
+        lat.tangent_linear(2, None, 0.1, np.zeros((6, 6, 6, 3)), np.zeros((6, 6, 6, 3)))
+    with pytest.raises(PlbGpuError):
+        lat.adjoint_steady(np.zeros((6, 6, 3)), 4)   # wrong size
+    with pytest.raises(PlbGpuError):
+        lat.adjoint_steady(np.zeros((6, 6, 6, 3)), -1)
