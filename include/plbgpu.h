@@ -290,8 +290,8 @@ int plbgpu_load_state(plbgpu_ctx* ctx, int handle, int what, const char* plb_pat
 /* ------------------------------------------------------------ adjoint */
 
 /* Discrete adjoint of the collide-and-stream step (no counterpart in the
- * reference), for domains of BGK, Guo, incompressible BGK, bounce-back and
- * no-dynamics cells.  The objective is J = 1/2 sum over cells |u(T) - u*|^2
+ * reference), for domains of BGK, Guo, incompressible BGK, bounce-back,
+ * momentum-exchange bounce-back and no-dynamics cells.  The objective is J = 1/2 sum over cells |u(T) - u*|^2
  * with u the velocity each cell's dynamics reports (computeVelocity,
  * dataProcessors/dataAnalysisWrapper3D.h:127-132).
  *
@@ -314,7 +314,11 @@ int plbgpu_load_state(plbgpu_ctx* ctx, int handle, int what, const char* plb_pat
  * plbgpu_adjoint_steady_weighted: the same gradients at a steady state (the
  * domain's current state, taken as converged): `iterations` reverse steps
  * linearised around that one state, no recorded run and no checkpoints
- * (three states of memory); the gradient converges as the flow would relax. */
+ * (three states of memory); the gradient converges as the flow would relax.
+ *
+ * The _drag forms take J = direction . D with D the momentum-exchange drag
+ * of the state (what the next collision records on MomentumExchangeBounceBack
+ * cells, bounceBackModels.hh:100-136; needs plbgpu_initialize_momentum_exchange). */
 int plbgpu_adjoint_forward(plbgpu_ctx* ctx, int handle, int T, int K);
 int plbgpu_adjoint_interval(plbgpu_ctx* ctx, int handle, int* K);
 int plbgpu_adjoint_backward(plbgpu_ctx* ctx, int handle, const double* u_target, size_t n_target,
@@ -332,6 +336,12 @@ int plbgpu_tangent_linear_weighted(plbgpu_ctx* ctx, int handle, int T, const dou
 int plbgpu_adjoint_steady_weighted(plbgpu_ctx* ctx, int handle, int iterations, const double* weights,
                                    size_t n_weights, double* objective, double* grad_force, size_t n_grad,
                                    double* grad_omega, float* ms);
+int plbgpu_adjoint_backward_drag(plbgpu_ctx* ctx, int handle, const double* direction, double* objective,
+                                 double* grad_force, size_t n_grad, double* grad_omega, float* ms);
+int plbgpu_tangent_linear_drag(plbgpu_ctx* ctx, int handle, int T, const double* dforce, size_t n_dforce,
+                               double domega, const double* direction, double* objective, double* directional);
+int plbgpu_adjoint_steady_drag(plbgpu_ctx* ctx, int handle, int iterations, const double* direction,
+                               double* objective, double* grad_force, size_t n_grad, double* grad_omega, float* ms);
 
 /* ------------------------------------------------------------ co-processor form */
 

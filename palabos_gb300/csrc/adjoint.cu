@@ -87,6 +87,7 @@ __device__ __forceinline__ void adjCollide(int k, R* f, const R* F, const BgkCon
         bgkCollide<R>(f, rhoBar, j, bc, invRho0);
         break;
     case K_BB:
+    case K_MEBB:   // bounce-back; the momentum it records is a side reduction
         for (int i = 1; i <= 9; ++i) {
             R t = f[i]; f[i] = f[i + 9]; f[i + 9] = t;
         }
@@ -169,7 +170,7 @@ __device__ __forceinline__ void cellVelocity(int k, const R* f, const R* F, R in
 // forward collision.
 template <typename R>
 __device__ R adjCell(int k, const R* f, const R* F, R omega, R invRho0, const R* mu, R* lam, R* gF) {
-    if (k == K_BB) {
+    if (k == K_BB || k == K_MEBB) {
         lam[0] = mu[0];
 #pragma unroll
         for (int i = 1; i < 19; ++i) lam[i] = mu[opp(i)];
@@ -448,6 +449,53 @@ __global__ void objectiveKernel(DevLattice L, const R* f, const double* v, bool 
     blockAdd(jsum, acc->objective);
 }
 
+// Drag objective J = w . D(f) with D the momentum-exchange drag the next
+// collision records (bounceBackModels.hh:100-136): over the fluid directions i
+// of each momentum-exchange cell, D -= 2 c_i f_opp(i).  Linear in f, so
+// lambda is -2 w . c_i on population opp(i) of those cells and zero elsewhere;
+// no explicit force term.
+template <typename R>
+__global__ void dragObjectiveKernel(DevLattice L, const R* f, double w0, double w1, double w2, R* lam, AdjAcc* acc) {
+    const int z = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, x = blockIdx.z;
+    double jsum = 0.;
+    if (z < L.nz) {
+        const long long idx = ((long long)x * L.ny + y) * L.nz + z;
+        const uint32_t mask = L.flags[idx] == K_MEBB ? L.mebb[idx] : 0u;
+        R l[19];
+        for (int i = 0; i < 19; ++i) l[i] = R(0);
+#pragma unroll
+        for (int i = 1; i < 19; ++i) {
+            if (!(mask & (1u << i))) continue;
+            const double c = -2. * (w0 * cdir(i, 0) + w1 * cdir(i, 1) + w2 * cdir(i, 2));
+            l[opp(i)] += (R)c;
+            jsum += c * (double)f[opp(i) * L.n + idx];
+        }
+        for (int i = 0; i < 19; ++i) lam[i * L.n + idx] = l[i];
+    }
+    blockAdd(jsum, acc->objective);
+}
+
+__global__ void dualDragObjectiveKernel(DevLattice L, const Dual* f, double w0, double w1, double w2,
+                                        AdjAcc* acc) {
+    const int z = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, x = blockIdx.z;
+    double jv = 0., jd = 0.;
+    if (z < L.nz) {
+        const long long idx = ((long long)x * L.ny + y) * L.nz + z;
+        const uint32_t mask = L.flags[idx] == K_MEBB ? L.mebb[idx] : 0u;
+        for (int i = 1; i < 19; ++i) {
+            if (!(mask & (1u << i))) continue;
+            const double c = -2. * (w0 * cdir(i, 0) + w1 * cdir(i, 1) + w2 * cdir(i, 2));
+            const Dual fo = f[opp(i) * L.n + idx];
+            jv += c * fo.v;
+            jd += c * fo.d;
+        }
+    }
+    blockAdd(jv, acc->objective);
+    blockAdd(jd, acc->tangent);
+}
+
 // One reverse step: lamIn = lambda^{n+1}, f = f^n (pre-collision), lamOut = lambda^n.
 template <typename R, bool INTERIOR>
 __device__ __forceinline__ R adjointCell(const DevLattice& L, const NeighbourDeltas& D, const R* f, const R* lamIn,
@@ -576,13 +624,48 @@ void stateInAny(int prec, const DevLattice& L, const R* in, cudaStream_t s) {
     }
 }
 
+// Objective of a sweep: the velocity mismatch (v = u*), a weighted velocity
+// (v = w), or the momentum-exchange drag along dir.
+enum { kMismatch = 0, kWeighted = 1, kDrag = 2 };
+struct Objective {
+    int kind = kMismatch;
+    const double* v = nullptr;   // host, 3 values per cell (velocity objectives)
+    size_t nv = 0;
+    double dir[3] = {0., 0., 0.};
+};
+
+int checkObjective(plbgpu_ctx* c, const DomainAccess& a, const Objective& o) {
+    if (o.kind == kDrag) {
+        if (!a.L.mebb)
+            return domainFail(c, PLBGPU_ERR_STATE, "adjoint: the drag objective needs initialize_momentum_exchange");
+        return PLBGPU_OK;
+    }
+    if (!o.v || (long long)o.nv != 3 * a.L.n)
+        return domainFail(c, PLBGPU_ERR_ARG, "adjoint: the objective needs 3 values per cell");
+    return PLBGPU_OK;
+}
+
+// J, lambda = dJ/df and the explicit dJ/dF for state f; vDev holds the
+// objective's per-cell values on the device (velocity objectives).
+template <typename R>
+void launchObjective(const DomainAccess& a, const Objective& o, const R* f, const double* vDev, R* lam, R* gF,
+                     AdjAcc* acc) {
+    if (o.kind == kDrag)
+        dragObjectiveKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, f, o.dir[0], o.dir[1], o.dir[2],
+                                                                               lam, acc);
+    else
+        objectiveKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, f, vDev, o.kind == kWeighted,
+                                                                           (R)(1.0 / a.rho0), lam, gF, acc);
+    *a.launches += 1;
+}
+
 int checkKinds(plbgpu_ctx* c, const DomainAccess& a) {
     std::vector<uint8_t> k((size_t)a.L.n);
     if (cudaMemcpyAsync(k.data(), a.L.flags, k.size(), cudaMemcpyDeviceToHost, a.stream) != cudaSuccess ||
         cudaStreamSynchronize(a.stream) != cudaSuccess)
         return domainFail(c, PLBGPU_ERR_CUDA, "reading cell kinds failed");
     for (uint8_t v : k)
-        if (v != K_BGK && v != K_GUO && v != K_INCBGK && v != K_BB && v != K_NODYN)
+        if (v != K_BGK && v != K_GUO && v != K_INCBGK && v != K_BB && v != K_MEBB && v != K_NODYN)
             return domainFail(c, PLBGPU_ERR_ARG,
                               "the adjoint supports BGK, Guo, incompressible BGK, bounce-back and no-dynamics cells");
     return PLBGPU_OK;
@@ -626,7 +709,8 @@ int forwardImpl(plbgpu_ctx* c, int h, DomainAccess& a, AdjointState* st, int T, 
 }
 
 template <typename R>
-int backwardImpl(DomainAccess& a, AdjointState* st, bool weighted, double* objective, double* gOmega, float* ms) {
+int backwardImpl(DomainAccess& a, AdjointState* st, const Objective& o, double* objective, double* gOmega,
+                 float* ms) {
     const long long n = a.L.n, sz = 19 * n;
     R* ck = static_cast<R*>(st->ckpt);
     R* sg = static_cast<R*>(st->seg);
@@ -641,9 +725,7 @@ int backwardImpl(DomainAccess& a, AdjointState* st, bool weighted, double* objec
     cudaMemsetAsync(gF, 0, sizeof(R) * 3 * n, a.stream);
     cudaMemsetAsync(st->acc, 0, sizeof(AdjAcc), a.stream);
     const int T = st->T, K = st->K;
-    objectiveKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, ck + (long long)(T / K) * sz,
-                                                                       st->uT, weighted, invRho0, lam, gF, st->acc);
-    *a.launches += 1;
+    launchObjective<R>(a, o, ck + (long long)(T / K) * sz, st->uT, lam, gF, st->acc);
     int cur = 0;   // lam + cur * sz holds lambda^{t+1}
     for (int s = T / K - 1; s >= 0; --s) {
         // f^{sK} is checkpoint s; recompute f^{sK+1} .. f^{sK+K-1} into seg
@@ -686,21 +768,22 @@ int forceGradientOut(plbgpu_ctx* c, const DomainAccess& a, const R* gF, double* 
     return PLBGPU_OK;
 }
 
-int adjointBackward(plbgpu_ctx* c, int h, const double* v, size_t n3, bool weighted, double* objective,
-                    double* grad_force, size_t ng, double* grad_omega, float* ms) {
+int adjointBackward(plbgpu_ctx* c, int h, const Objective& o, double* objective, double* grad_force, size_t ng,
+                    double* grad_omega, float* ms) {
     DomainAccess a;
     int rc = domainAccess(c, h, &a);
     if (rc) return rc;
     AdjointState* st = static_cast<AdjointState*>(*a.adjointSlot);
     if (!st || !st->ready) return domainFail(c, PLBGPU_ERR_STATE, "adjoint: no recorded forward run");
     const long long n = a.L.n;
-    if (!v || (long long)n3 != 3 * n || !objective || !grad_omega)
-        return domainFail(c, PLBGPU_ERR_ARG, "adjoint: the objective needs 3 values per cell");
+    if (!objective || !grad_omega) return domainFail(c, PLBGPU_ERR_ARG, "adjoint: objective and grad_omega are NULL");
+    if ((rc = checkObjective(c, a, o))) return rc;
     if (grad_force && (long long)ng != 3 * n)
         return domainFail(c, PLBGPU_ERR_ARG, "adjoint: grad_force needs 3 values per cell");
-    ADJ_TRY(cudaMemcpyAsync(st->uT, v, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, a.stream));
-    rc = a.precision == PLBGPU_FP64 ? backwardImpl<double>(a, st, weighted, objective, grad_omega, ms)
-                                    : backwardImpl<float>(a, st, weighted, objective, grad_omega, ms);
+    if (o.kind != kDrag)
+        ADJ_TRY(cudaMemcpyAsync(st->uT, o.v, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, a.stream));
+    rc = a.precision == PLBGPU_FP64 ? backwardImpl<double>(a, st, o, objective, grad_omega, ms)
+                                    : backwardImpl<float>(a, st, o, objective, grad_omega, ms);
     if (rc) return domainFail(c, rc, "adjoint: backward sweep failed");
     if (!grad_force) return PLBGPU_OK;
     return a.precision == PLBGPU_FP64 ? forceGradientOut(c, a, static_cast<const double*>(st->gF), grad_force)
@@ -715,7 +798,7 @@ int adjointBackward(plbgpu_ctx* c, int h, const double* v, size_t n3, bool weigh
 // total mass, adds nothing because the collision conserves mass for every
 // omega and force).  Three states of memory whatever the number of steps.
 template <typename R>
-int steadyImpl(plbgpu_ctx* c, DomainAccess& a, int iterations, const double* weights, double* objective,
+int steadyImpl(plbgpu_ctx* c, DomainAccess& a, int iterations, const Objective& o, double* objective,
                double* grad_force, double* grad_omega, float* ms) {
     const long long n = a.L.n, sz = 19 * n;
     struct Buffers {
@@ -742,16 +825,16 @@ int steadyImpl(plbgpu_ctx* c, DomainAccess& a, int iterations, const double* wei
     ADJ_TRY(cudaMalloc(&b.acc, sizeof(AdjAcc)));
     ADJ_TRY(cudaEventCreate(&b.e0));
     ADJ_TRY(cudaEventCreate(&b.e1));
-    ADJ_TRY(cudaMemcpyAsync(b.w, weights, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, a.stream));
+    if (o.kind != kDrag)
+        ADJ_TRY(cudaMemcpyAsync(b.w, o.v, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, a.stream));
     ADJ_TRY(cudaMemsetAsync(b.gF, 0, sizeof(R) * 3 * n, a.stream));
     ADJ_TRY(cudaMemsetAsync(b.acc, 0, sizeof(AdjAcc), a.stream));
     const R omega = (R)a.omega, invRho0 = (R)(1.0 / a.rho0);
     const NeighbourDeltas D = deltasOf(a.L);
     ADJ_TRY(cudaEventRecord(b.e0, a.stream));
     stateOutAny<R>(a.precision, a.L, a.odd, b.f, a.stream);
-    objectiveKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, b.f, b.w, true, invRho0, b.lam, b.gF,
-                                                                       b.acc);
-    *a.launches += 2;
+    *a.launches += 1;
+    launchObjective<R>(a, o, b.f, b.w, b.lam, b.gF, b.acc);
     int cur = 0;
     for (int t = 0; t < iterations; ++t) {
         adjointStepKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, D, b.f, b.lam + cur * sz,
@@ -772,15 +855,16 @@ int steadyImpl(plbgpu_ctx* c, DomainAccess& a, int iterations, const double* wei
     return grad_force ? forceGradientOut(c, a, b.gF, grad_force) : PLBGPU_OK;
 }
 
-int tangentLinear(plbgpu_ctx* c, int h, int T, const double* dforce, size_t ndf, double domega,
-                  const double* u_target, size_t n3, bool weighted, double* objective, double* directional) {
+int tangentLinear(plbgpu_ctx* c, int h, int T, const double* dforce, size_t ndf, double domega, const Objective& o,
+                  double* objective, double* directional) {
     DomainAccess a;
     int rc = domainAccess(c, h, &a);
     if (rc) return rc;
     if (a.precision != PLBGPU_FP64) return domainFail(c, PLBGPU_ERR_ARG, "tangent: FP64 domains only");
     const long long n = a.L.n, sz = 19 * n;
-    if (T < 0 || !u_target || (long long)n3 != 3 * n || !objective || !directional || (dforce && (long long)ndf != 3 * n))
+    if (T < 0 || !objective || !directional || (dforce && (long long)ndf != 3 * n))
         return domainFail(c, PLBGPU_ERR_ARG, "tangent: bad arguments");
+    if ((rc = checkObjective(c, a, o))) return rc;
     if ((rc = checkKinds(c, a))) return rc;
     if (a.pending) return domainFail(c, PLBGPU_ERR_STATE, "tangent: boundary faces are not supported");
     double *f0 = nullptr, *dF = nullptr, *uT = nullptr;
@@ -796,7 +880,8 @@ int tangentLinear(plbgpu_ctx* c, int h, int T, const double* dforce, size_t ndf,
     if (e == cudaSuccess) e = cudaMalloc(&uT, sizeof(double) * 3 * n);
     if (e == cudaSuccess) e = cudaMalloc(&acc, sizeof(AdjAcc));
     if (e == cudaSuccess) e = cudaMemcpyAsync(dF, planes.data(), sizeof(double) * 3 * n, cudaMemcpyHostToDevice, a.stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(uT, u_target, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, a.stream);
+    if (e == cudaSuccess && o.kind != kDrag)
+        e = cudaMemcpyAsync(uT, o.v, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, a.stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(acc, 0, sizeof(AdjAcc), a.stream);
     if (e == cudaSuccess) {
         stateOutAny<double>(a.precision, a.L, a.odd, f0, a.stream);
@@ -811,7 +896,12 @@ int tangentLinear(plbgpu_ctx* c, int h, int T, const double* dforce, size_t ndf,
             *a.launches += 1;
             std::swap(cur, nxt);
         }
-        dualObjectiveKernel<<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, cur, dF, uT, weighted, 1.0 / a.rho0, acc);
+        if (o.kind == kDrag)
+            dualDragObjectiveKernel<<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, cur, o.dir[0], o.dir[1],
+                                                                                    o.dir[2], acc);
+        else
+            dualObjectiveKernel<<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, cur, dF, uT, o.kind == kWeighted,
+                                                                                1.0 / a.rho0, acc);
         *a.launches += 1;
         e = cudaGetLastError();
         AdjAcc hacc;
@@ -905,38 +995,87 @@ int plbgpu_adjoint_interval(plbgpu_ctx* c, int h, int* K) {
 
 int plbgpu_adjoint_backward(plbgpu_ctx* c, int h, const double* u_target, size_t n3, double* objective,
                             double* grad_force, size_t ng, double* grad_omega, float* ms) {
-    return adjointBackward(c, h, u_target, n3, false, objective, grad_force, ng, grad_omega, ms);
+    Objective o;
+    o.v = u_target;
+    o.nv = n3;
+    return adjointBackward(c, h, o, objective, grad_force, ng, grad_omega, ms);
 }
 
 int plbgpu_adjoint_backward_weighted(plbgpu_ctx* c, int h, const double* weights, size_t n3, double* objective,
                                      double* grad_force, size_t ng, double* grad_omega, float* ms) {
-    return adjointBackward(c, h, weights, n3, true, objective, grad_force, ng, grad_omega, ms);
+    Objective o;
+    o.kind = kWeighted;
+    o.v = weights;
+    o.nv = n3;
+    return adjointBackward(c, h, o, objective, grad_force, ng, grad_omega, ms);
 }
 
-int plbgpu_adjoint_steady_weighted(plbgpu_ctx* c, int h, int iterations, const double* weights, size_t n3,
-                                   double* objective, double* grad_force, size_t ng, double* grad_omega, float* ms) {
+int plbgpu_adjoint_backward_drag(plbgpu_ctx* c, int h, const double* direction, double* objective, double* grad_force,
+                                 size_t ng, double* grad_omega, float* ms) {
+    if (!direction) return domainFail(c, PLBGPU_ERR_ARG, "adjoint: direction is NULL");
+    Objective o;
+    o.kind = kDrag;
+    for (int d = 0; d < 3; ++d) o.dir[d] = direction[d];
+    return adjointBackward(c, h, o, objective, grad_force, ng, grad_omega, ms);
+}
+
+static int adjointSteady(plbgpu_ctx* c, int h, int iterations, const Objective& o, double* objective,
+                         double* grad_force, size_t ng, double* grad_omega, float* ms) {
     DomainAccess a;
     int rc = domainAccess(c, h, &a);
     if (rc) return rc;
     const long long n = a.L.n;
-    if (iterations < 0 || !weights || (long long)n3 != 3 * n || !objective || !grad_omega ||
-        (grad_force && (long long)ng != 3 * n))
-        return domainFail(c, PLBGPU_ERR_ARG, "steady adjoint: weights (and grad_force) need 3 values per cell");
+    if (iterations < 0 || !objective || !grad_omega || (grad_force && (long long)ng != 3 * n))
+        return domainFail(c, PLBGPU_ERR_ARG, "steady adjoint: bad arguments");
+    if ((rc = checkObjective(c, a, o))) return rc;
     if ((rc = checkKinds(c, a))) return rc;
     if (a.pending) return domainFail(c, PLBGPU_ERR_STATE, "steady adjoint: boundary faces are not supported");
-    return a.precision == PLBGPU_FP64
-               ? steadyImpl<double>(c, a, iterations, weights, objective, grad_force, grad_omega, ms)
-               : steadyImpl<float>(c, a, iterations, weights, objective, grad_force, grad_omega, ms);
+    return a.precision == PLBGPU_FP64 ? steadyImpl<double>(c, a, iterations, o, objective, grad_force, grad_omega, ms)
+                                      : steadyImpl<float>(c, a, iterations, o, objective, grad_force, grad_omega, ms);
+}
+
+int plbgpu_adjoint_steady_weighted(plbgpu_ctx* c, int h, int iterations, const double* weights, size_t n3,
+                                   double* objective, double* grad_force, size_t ng, double* grad_omega, float* ms) {
+    Objective o;
+    o.kind = kWeighted;
+    o.v = weights;
+    o.nv = n3;
+    return adjointSteady(c, h, iterations, o, objective, grad_force, ng, grad_omega, ms);
+}
+
+int plbgpu_adjoint_steady_drag(plbgpu_ctx* c, int h, int iterations, const double* direction, double* objective,
+                               double* grad_force, size_t ng, double* grad_omega, float* ms) {
+    if (!direction) return domainFail(c, PLBGPU_ERR_ARG, "steady adjoint: direction is NULL");
+    Objective o;
+    o.kind = kDrag;
+    for (int d = 0; d < 3; ++d) o.dir[d] = direction[d];
+    return adjointSteady(c, h, iterations, o, objective, grad_force, ng, grad_omega, ms);
 }
 
 int plbgpu_tangent_linear(plbgpu_ctx* c, int h, int T, const double* dforce, size_t ndf, double domega,
                           const double* u_target, size_t n3, double* objective, double* directional) {
-    return tangentLinear(c, h, T, dforce, ndf, domega, u_target, n3, false, objective, directional);
+    Objective o;
+    o.v = u_target;
+    o.nv = n3;
+    return tangentLinear(c, h, T, dforce, ndf, domega, o, objective, directional);
 }
 
 int plbgpu_tangent_linear_weighted(plbgpu_ctx* c, int h, int T, const double* dforce, size_t ndf, double domega,
                                    const double* weights, size_t n3, double* objective, double* directional) {
-    return tangentLinear(c, h, T, dforce, ndf, domega, weights, n3, true, objective, directional);
+    Objective o;
+    o.kind = kWeighted;
+    o.v = weights;
+    o.nv = n3;
+    return tangentLinear(c, h, T, dforce, ndf, domega, o, objective, directional);
+}
+
+int plbgpu_tangent_linear_drag(plbgpu_ctx* c, int h, int T, const double* dforce, size_t ndf, double domega,
+                               const double* direction, double* objective, double* directional) {
+    if (!direction) return domainFail(c, PLBGPU_ERR_ARG, "tangent: direction is NULL");
+    Objective o;
+    o.kind = kDrag;
+    for (int d = 0; d < 3; ++d) o.dir[d] = direction[d];
+    return tangentLinear(c, h, T, dforce, ndf, domega, o, objective, directional);
 }
 
 }  // extern "C"

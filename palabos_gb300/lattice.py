@@ -313,53 +313,79 @@ class DeviceLattice3D:
         self._check(self.lib.plbgpu_adjoint_interval(self.ctx.h, self.handle, ctypes.byref(k)))
         return k.value
 
-    def _objective(self, u_target, weights):
-        if (u_target is None) == (weights is None):
-            raise ValueError("give exactly one of u_target (mismatch objective) and weights (weighted velocity)")
-        v = u_target if weights is None else weights
-        return np.ascontiguousarray(v, np.float64).reshape(-1), weights is not None
+    def _objective(self, u_target, weights, drag):
+        """(kind, values) of the one objective given: "mismatch" (u_target),
+        "weighted" (weights) or "drag" (a direction)."""
+        given = [(k, v) for k, v in (("mismatch", u_target), ("weighted", weights), ("drag", drag)) if v is not None]
+        if len(given) != 1:
+            raise ValueError("give exactly one objective: u_target (mismatch), weights (weighted velocity) "
+                             "or drag (a direction)")
+        kind, v = given[0]
+        v = np.ascontiguousarray(v, np.float64).reshape(-1)
+        if kind == "drag" and v.size != 3:
+            raise ValueError("drag needs a direction of 3 components")
+        return kind, v
 
-    def adjoint_backward(self, u_target=None, want_force=True, weights=None):
+    def adjoint_backward(self, u_target=None, want_force=True, weights=None, drag=None):
         """Gradients of the last adjoint_forward run.  Objective J = 1/2 sum
-        |u(T) - u*|^2 (u_target = u*), or J = sum w . u(T) (weights = w, e.g.
-        the mean flux).  Returns J, dJ/dF (nx,ny,nz,3), dJ/domega and the
-        device time of the sweep in ms."""
-        v, weighted = self._objective(u_target, weights)
-        fn = self.lib.plbgpu_adjoint_backward_weighted if weighted else self.lib.plbgpu_adjoint_backward
+        |u(T) - u*|^2 (u_target = u*), J = sum w . u(T) (weights = w, e.g.
+        the mean flux), or J = drag . D(T) with D the momentum-exchange drag
+        (drag = direction).  Returns J, dJ/dF (nx,ny,nz,3), dJ/domega and
+        the device time of the sweep in ms."""
+        kind, v = self._objective(u_target, weights, drag)
         J = ctypes.c_double()
         go = ctypes.c_double()
         ms = ctypes.c_float()
-        g = np.empty(v.size if want_force else 0, np.float64)
-        self._check(fn(self.ctx.h, self.handle, _dp(v), v.size, ctypes.byref(J), _dp(g) if want_force else None,
-                       g.size, ctypes.byref(go), ctypes.byref(ms)))
+        g = np.empty(3 * self._cells(self.bounding_box) if want_force else 0, np.float64)
+        gp = _dp(g) if want_force else None
+        if kind == "drag":
+            rc = self.lib.plbgpu_adjoint_backward_drag(self.ctx.h, self.handle, _dp(v), ctypes.byref(J), gp, g.size,
+                                                       ctypes.byref(go), ctypes.byref(ms))
+        else:
+            fn = self.lib.plbgpu_adjoint_backward_weighted if kind == "weighted" else self.lib.plbgpu_adjoint_backward
+            rc = fn(self.ctx.h, self.handle, _dp(v), v.size, ctypes.byref(J), gp, g.size, ctypes.byref(go),
+                    ctypes.byref(ms))
+        self._check(rc)
         grad = g.reshape(self.shape + (3,)) if want_force else None
         return J.value, grad, go.value, ms.value
 
-    def adjoint_steady(self, weights, iterations, want_force=True):
-        """Gradients of J = sum w . u at the current (converged) state from
-        `iterations` reverse steps around it.  Returns J, dJ/dF, dJ/domega
-        and the device time in ms."""
-        v = np.ascontiguousarray(weights, np.float64).reshape(-1)
+    def adjoint_steady(self, weights=None, iterations=1000, want_force=True, drag=None):
+        """Gradients of J = sum w . u (weights) or J = drag . D (drag) at the
+        current (converged) state from `iterations` reverse steps around it.
+        Returns J, dJ/dF, dJ/domega and the device time in ms."""
+        kind, v = self._objective(None, weights, drag)
         J = ctypes.c_double()
         go = ctypes.c_double()
         ms = ctypes.c_float()
-        g = np.empty(v.size if want_force else 0, np.float64)
-        self._check(self.lib.plbgpu_adjoint_steady_weighted(self.ctx.h, self.handle, int(iterations), _dp(v), v.size,
-                                                            ctypes.byref(J), _dp(g) if want_force else None, g.size,
-                                                            ctypes.byref(go), ctypes.byref(ms)))
+        g = np.empty(3 * self._cells(self.bounding_box) if want_force else 0, np.float64)
+        gp = _dp(g) if want_force else None
+        if kind == "drag":
+            rc = self.lib.plbgpu_adjoint_steady_drag(self.ctx.h, self.handle, int(iterations), _dp(v),
+                                                     ctypes.byref(J), gp, g.size, ctypes.byref(go), ctypes.byref(ms))
+        else:
+            rc = self.lib.plbgpu_adjoint_steady_weighted(self.ctx.h, self.handle, int(iterations), _dp(v), v.size,
+                                                         ctypes.byref(J), gp, g.size, ctypes.byref(go),
+                                                         ctypes.byref(ms))
+        self._check(rc)
         grad = g.reshape(self.shape + (3,)) if want_force else None
         return J.value, grad, go.value, ms.value
 
-    def tangent_linear(self, T, dforce, domega, u_target=None, weights=None):
+    def tangent_linear(self, T, dforce, domega, u_target=None, weights=None, drag=None):
         """(J, grad J . (dforce, domega)) from a dual-number run of T steps;
         the objective as in adjoint_backward."""
-        v, weighted = self._objective(u_target, weights)
-        fn = self.lib.plbgpu_tangent_linear_weighted if weighted else self.lib.plbgpu_tangent_linear
+        kind, v = self._objective(u_target, weights, drag)
         df = None if dforce is None else np.ascontiguousarray(dforce, np.float64).reshape(-1)
+        dfp, dfn = (None, 0) if df is None else (_dp(df), df.size)
         J = ctypes.c_double()
         dj = ctypes.c_double()
-        self._check(fn(self.ctx.h, self.handle, int(T), None if df is None else _dp(df), 0 if df is None else df.size,
-                       float(domega), _dp(v), v.size, ctypes.byref(J), ctypes.byref(dj)))
+        if kind == "drag":
+            rc = self.lib.plbgpu_tangent_linear_drag(self.ctx.h, self.handle, int(T), dfp, dfn, float(domega), _dp(v),
+                                                     ctypes.byref(J), ctypes.byref(dj))
+        else:
+            fn = self.lib.plbgpu_tangent_linear_weighted if kind == "weighted" else self.lib.plbgpu_tangent_linear
+            rc = fn(self.ctx.h, self.handle, int(T), dfp, dfn, float(domega), _dp(v), v.size, ctypes.byref(J),
+                    ctypes.byref(dj))
+        self._check(rc)
         return J.value, dj.value
 
     def compute_average_energy(self, box=None):

@@ -117,6 +117,11 @@ SIGNATURES = {
     "plbgpu_tangent_linear_weighted": [_vp, _i, _i, _c_dbl_p, _sz, _d, _c_dbl_p, _sz, _c_dbl_p, _c_dbl_p],
     "plbgpu_adjoint_steady_weighted": [_vp, _i, _i, _c_dbl_p, _sz, _c_dbl_p, _c_dbl_p, _sz, _c_dbl_p,
                                        ctypes.POINTER(ctypes.c_float)],
+    "plbgpu_adjoint_backward_drag": [_vp, _i, _c_dbl_p, _c_dbl_p, _c_dbl_p, _sz, _c_dbl_p,
+                                     ctypes.POINTER(ctypes.c_float)],
+    "plbgpu_tangent_linear_drag": [_vp, _i, _i, _c_dbl_p, _sz, _d, _c_dbl_p, _c_dbl_p, _c_dbl_p],
+    "plbgpu_adjoint_steady_drag": [_vp, _i, _i, _c_dbl_p, _c_dbl_p, _c_dbl_p, _sz, _c_dbl_p,
+                                   ctypes.POINTER(ctypes.c_float)],
     "plbgpu_reduce_noalloc": [_vp, ctypes.c_longlong, _vp, _i, _i, _i, _d, _d, _vp, _vp],
 }
 

@@ -1,16 +1,20 @@
 """Discrete adjoint of the collide-and-stream step.
 
-The gradient of J = 1/2 sum |u(T) - u*|^2 with respect to the per-cell Guo
-force and omega, from the checkpointed reverse sweep, is checked against
+The gradients of J = 1/2 sum |u(T) - u*|^2, of a weighted velocity (the mean
+flux) and of the momentum-exchange drag with respect to the per-cell Guo
+force and omega, from the checkpointed reverse sweep and from the steady
+adjoint, are checked against
   - a forward-mode dual-number directional derivative of the same GPU FP64
     path (plbgpu_tangent_linear): agreement to 1e-9 relative;
   - central finite differences of the CPU oracle (the reference's FP64 step,
-    bit for bit): agreement to 1e-5 relative.
+    bit for bit), or of converged FP64 runs for the steady adjoint:
+    agreement to 1e-5 relative.
 """
 import numpy as np
 import pytest
 
 import oracle as O
+from palabos_gb300 import native as N
 from palabos_gb300 import workloads
 
 pytestmark = pytest.mark.gpu
@@ -107,7 +111,6 @@ def test_adjoint_rejects_unsupported_cells():
     with pytest.raises(PlbGpuError):
         lat2.adjoint_backward(np.zeros((6, 6, 6, 3)))   # no forward run yet
     import ctypes
-    from palabos_gb300 import native as N
     k = ctypes.c_int()
     assert N.ERRORS[lat2.lib.plbgpu_adjoint_interval(lat2.ctx.h, lat2.handle, ctypes.byref(k))] == "PLBGPU_ERR_STATE"
 
@@ -257,6 +260,114 @@ def test_steady_adjoint_fp32_tracks_fp64():
     assert np.abs(g["fp32"][1] - g["fp64"][1]).max() <= 1e-3 * np.abs(g["fp64"][1]).max()
 
 
+def _obstacle_channel(shape=(12, 10, 8), T=24, seed=3):
+    """The forced channel with a 2x2x2 momentum-exchange block in its middle."""
+    wl, _, T = _case(shape, T, seed)
+    kinds = wl.kinds.copy()
+    cx, cy, cz = (s // 2 for s in shape)
+    kinds[cx - 1:cx + 1, cy - 1:cy + 1, cz - 1:cz + 1] = N.MOMENTUM_EXCHANGE
+    wl.kinds = kinds
+    return wl, T
+
+
+DRAG_DIR = np.array([1.0, 0.3, -0.2])
+
+
+def _oracle_drag(wl, f0, force, omega, T):
+    """direction . drag of the state after T steps (the drag step T + 1 records)."""
+    ol = O.OracleLattice(*wl.shape, wl.periodic, omega, wl.kinds, None, force)
+    f, _ = ol.run(f0, T, with_stats=False)
+    _, st = ol.run(f, 1, with_stats=True)
+    return float(np.dot(DRAG_DIR, st[0, 3:6]))
+
+
+@pytest.mark.parametrize("K", [1, 4])
+def test_drag_adjoint_matches_tangent_linear(K):
+    wl, T = _obstacle_channel()
+    lat = wl.lattice("fp64")
+    rng = np.random.default_rng(31)
+    dF = rng.standard_normal(wl.shape + (3,))
+    dF[wl.kinds != N.GUO] = 0.0
+    J_t, dJ = lat.tangent_linear(T, dF, 0.3, drag=DRAG_DIR)
+    lat.adjoint_forward(T, K)
+    J, gF, gO, _ = lat.adjoint_backward(drag=DRAG_DIR)
+    assert J == pytest.approx(J_t, rel=1e-13)
+    assert J != 0.0
+    adj = float(np.sum(gF * dF)) + gO * 0.3
+    assert adj == pytest.approx(dJ, rel=1e-9), (adj, dJ)
+
+
+def test_drag_adjoint_matches_reference_finite_differences():
+    wl, T = _obstacle_channel()
+    lat = wl.lattice("fp64")
+    f0 = lat.receive()
+    lat.adjoint_forward(T, 6)
+    J, gF, gO, _ = lat.adjoint_backward(drag=DRAG_DIR)
+    assert J == pytest.approx(_oracle_drag(wl, f0, wl.force, wl.omega, T), rel=1e-12)
+    h = 1e-6
+    fd = (_oracle_drag(wl, f0, wl.force, wl.omega + h, T) - _oracle_drag(wl, f0, wl.force, wl.omega - h, T)) / (2 * h)
+    assert gO == pytest.approx(fd, rel=1e-5), (gO, fd)
+    rng = np.random.default_rng(9)
+    fluid = np.argwhere(wl.kinds == N.GUO)
+    for _ in range(3):
+        x, y, z = fluid[rng.integers(len(fluid))]
+        fp = wl.force.copy()
+        fm = wl.force.copy()
+        fp[x, y, z, 0] += h
+        fm[x, y, z, 0] -= h
+        fd = (_oracle_drag(wl, f0, fp, wl.omega, T) - _oracle_drag(wl, f0, fm, wl.omega, T)) / (2 * h)
+        assert gF[x, y, z, 0] == pytest.approx(fd, rel=1e-5, abs=1e-9 * abs(gF).max()), (gF[x, y, z, 0], fd)
+
+
+def _converged_sphere_drag(omega, force=None, steps=8000):
+    """Channel 16^3, periodic x, bounce-back walls at the y and z ends, Guo
+    force 1e-5 along x, momentum-exchange sphere of radius 3 in the middle:
+    the sphere takes a share of the applied force that depends on the flow
+    (in a fully periodic box it would take all of it, whatever omega)."""
+    n = 16
+    X, Y, Z = np.meshgrid(*(np.arange(n),) * 3, indexing="ij")
+    kinds = np.full((n, n, n), N.GUO, np.uint8)
+    kinds[:, 0, :] = kinds[:, -1, :] = kinds[:, :, 0] = kinds[:, :, -1] = N.BOUNCEBACK
+    kinds[(X - 7.5) ** 2 + (Y - 7.5) ** 2 + (Z - 7.5) ** 2 <= 9.0] = N.MOMENTUM_EXCHANGE
+    F = np.zeros((n, n, n, 3))
+    F[..., 0] = 1e-5
+    wl = workloads.Workload("sphere_in_channel", (n, n, n), omega, (1, 0, 0), kinds,
+                            force=F if force is None else force)
+    lat = wl.lattice("fp64")
+    lat.collide_and_stream(steps)
+    return wl, lat
+
+
+def test_steady_drag_adjoint():
+    omega = 1.0
+    wl, lat = _converged_sphere_drag(omega)
+    J, gF, gO, _ = lat.adjoint_steady(iterations=4000, drag=DRAG_DIR)
+    _, _, gO2, _ = lat.adjoint_steady(iterations=8000, want_force=False, drag=DRAG_DIR)
+    assert gO2 == pytest.approx(gO, rel=1e-9, abs=1e-15)
+
+    def drag(om, force=None):
+        _, l2 = _converged_sphere_drag(om, force)
+        J2, _, _, _ = l2.adjoint_steady(iterations=0, want_force=False, drag=DRAG_DIR)
+        return J2
+
+    assert J == pytest.approx(drag(omega), rel=1e-13)
+    assert 0 < J < 1e-5 * 14 * 14 * 16      # a share of the applied force
+    h = 1e-5
+    fd = (drag(omega + h) - drag(omega - h)) / (2 * h)
+    assert gO == pytest.approx(fd, rel=1e-5, abs=1e-9 * J), (gO, fd)
+    rng = np.random.default_rng(12)
+    fluid = np.argwhere(wl.kinds == N.GUO)
+    hF = 1e-8
+    for _ in range(2):
+        x, y, z = fluid[rng.integers(len(fluid))]
+        fp = wl.force.copy()
+        fm = wl.force.copy()
+        fp[x, y, z, 0] += hF
+        fm[x, y, z, 0] -= hF
+        fd = (drag(omega, fp) - drag(omega, fm)) / (2 * hF)
+        assert gF[x, y, z, 0] == pytest.approx(fd, rel=1e-5), (gF[x, y, z, 0], fd)
+
+
 def test_adjoint_objective_arguments():
     from palabos_gb300 import DeviceLattice3D, PlbGpuError
     lat = DeviceLattice3D(6, 6, 6, 1.2)
@@ -268,3 +379,7 @@ def test_adjoint_objective_arguments():
         lat.adjoint_steady(np.zeros((6, 6, 3)), 4)   # wrong size
     with pytest.raises(PlbGpuError):
         lat.adjoint_steady(np.zeros((6, 6, 6, 3)), -1)
+    with pytest.raises(ValueError):
+        lat.adjoint_backward(drag=(1.0, 0.0))            # a direction has 3 components
+    with pytest.raises(PlbGpuError):
+        lat.adjoint_steady(iterations=2, drag=(1.0, 0.0, 0.0))   # no momentum-exchange masks
