@@ -398,6 +398,12 @@ int buildSurface(plbgpu_ctx* c, Domain* d) {
     return PLBGPU_OK;
 }
 
+// Steps per CUDA graph of a long collide_and_stream call (even: the graph
+// ends on the parity it started on), and the replays that make capturing it
+// worth while.
+constexpr int kGraphSteps = 16;
+constexpr int kGraphMinReplays = 2;
+
 StepConsts consts(const Domain* d) {
     StepConsts s;
     // bgk_ma2_collision_base (dynamicsTemplates3D.h:2290-2293) with
@@ -989,20 +995,68 @@ int plbgpu_collide_and_stream(plbgpu_ctx* c, int h, int nsteps, int collect_stat
     if (nsteps < 0) return fail(c, PLBGPU_ERR_ARG, "nsteps %d", nsteps);
     if (nsteps == 0) return PLBGPU_OK;
     const Launchers& L = launchers(d->precision);
-    bool hasFaces = d->bc != nullptr;
+    const bool hasFaces = d->bc != nullptr;
     if (d->surfDirty && (rc = buildSurface(c, d))) return rc;
-    for (int s = 0; s < nsteps; ++s) {
-        bool stats = collect_stats && s == nsteps - 1;
+    auto stepOnce = [&](bool stats) -> int {
         if (stats) CUDA_TRY(c, cudaMemsetAsync(d->stats, 0, sizeof(StatsAcc) * kStatsSlots, c->stream));
         StepConsts k = consts(d);
         int nl = L.step(d->view(), d->odd, stats, k, d->stats, c->stream, &c->side);
         c->launches += nl - 1;
-        if ((rc = launchBox(c))) return rc;
+        int r = launchBox(c);
+        if (r) return r;
         d->odd = !d->odd;
         d->pending = hasFaces;
         d->steps += 1;
-        if ((rc = finishSurface(c, d))) return rc;
+        return finishSurface(c, d);
+    };
+    int s = 0;
+    // The first step may complete faces lazily and the last may gather
+    // statistics; the steps between repeat the same launches every two steps,
+    // so a long run replays them from a CUDA graph of kGraphSteps steps
+    // (fewer host launches and no stream-event round trips between the
+    // interior and border kernels).  Stochastic rounding draws a new seed
+    // every step and keeps the plain launches.
+    if ((rc = stepOnce(collect_stats && nsteps == 1))) return rc;
+    ++s;
+    const int last = nsteps - (collect_stats ? 1 : 0);   // steps [s, last) gather nothing
+    const int reps = (last - s) / kGraphSteps;
+    if (reps >= kGraphMinReplays && d->precision != PLBGPU_BF16_SR) {
+        const long long launches0 = c->launches;
+        const bool odd0 = d->odd, pending0 = d->pending;
+        const long long steps0 = d->steps;
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        bool captured = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        if (captured) {
+            for (int g = 0; g < kGraphSteps && rc == PLBGPU_OK; ++g) rc = stepOnce(false);
+            captured = cudaStreamEndCapture(c->stream, &graph) == cudaSuccess && rc == PLBGPU_OK &&
+                       cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+        }
+        const long long perGraph = c->launches - launches0;
+        // the capture only recorded the launches: the domain is where it was
+        d->odd = odd0;
+        d->pending = pending0;
+        d->steps = steps0;
+        c->launches = launches0;
+        rc = PLBGPU_OK;
+        (void)cudaGetLastError();
+        if (captured) {
+            for (int r = 0; r < reps && rc == PLBGPU_OK; ++r)
+                if (cudaGraphLaunch(exec, c->stream) != cudaSuccess) rc = fail(c, PLBGPU_ERR_CUDA, "graph launch failed");
+            if (rc == PLBGPU_OK) {
+                s += reps * kGraphSteps;
+                d->steps += (long long)reps * kGraphSteps;
+                d->odd = (kGraphSteps % 2) ? !odd0 : odd0;
+                d->pending = hasFaces;
+                c->launches += perGraph * reps;
+            }
+        }
+        if (exec) cudaGraphExecDestroy(exec);   // freed when the launches finish
+        if (graph) cudaGraphDestroy(graph);
+        if (rc) return rc;
     }
+    for (; s < nsteps; ++s)
+        if ((rc = stepOnce(collect_stats && s == nsteps - 1))) return rc;
     if (collect_stats) d->statsValid = true;
     return PLBGPU_OK;
 }

@@ -127,6 +127,26 @@ def test_multistep_calls_and_odd_parity_transfers(name):
     assert np.array_equal(lat.receive(), g["f_final"])
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32", "bf16", "bf16sr"])
+@pytest.mark.parametrize("name", ["velocity_box", "channel_sphere", "guo_channel", "zhpress_faces"])
+def test_long_call_replays_steps_like_single_steps(name, precision):
+    """A long collide_and_stream call replays its middle steps from a CUDA
+    graph; the result, the statistics of its last step and the parity equal
+    those of one call per step."""
+    g, meta = goldens.load(name)
+    n = 1 + 16 * 3 + 5
+    runs = []
+    for per_call in (n, 1):
+        lat = _lat(g, meta, precision)
+        lat.send(g["f_init"])
+        for _ in range(n // per_call):
+            lat.collide_and_stream(per_call, stats=True)
+        runs.append((lat.receive(), lat.internal_statistics()["raw"]))
+        lat.close()
+    assert np.array_equal(runs[0][0], runs[1][0])
+    assert np.array_equal(runs[0][1], runs[1][1])
+
+
 def test_velocity_condition_on_block_boundaries_sets_faces_edges_corners():
     """setVelocityConditionOnBlockBoundaries over a box: the kinds of the
     reference's instantiation, interior kinds left alone."""
