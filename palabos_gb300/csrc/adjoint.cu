@@ -708,6 +708,24 @@ int forwardImpl(plbgpu_ctx* c, int h, DomainAccess& a, AdjointState* st, int T, 
     return PLBGPU_OK;
 }
 
+// Capture the launches `enqueue` makes on stream s into an executable graph;
+// nullptr when the capture or instantiation fails (nothing was launched then).
+template <class F>
+cudaGraphExec_t captureGraph(cudaStream_t s, F&& enqueue) {
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    enqueue();
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    if (cudaStreamEndCapture(s, &g) != cudaSuccess || cudaGraphInstantiate(&exec, g, 0) != cudaSuccess)
+        exec = nullptr;
+    if (g) cudaGraphDestroy(g);
+    (void)cudaGetLastError();
+    return exec;
+}
+
 template <typename R>
 int backwardImpl(DomainAccess& a, AdjointState* st, const Objective& o, double* objective, double* gOmega,
                  float* ms) {
@@ -718,36 +736,46 @@ int backwardImpl(DomainAccess& a, AdjointState* st, const Objective& o, double* 
     R* gF = static_cast<R*>(st->gF);
     const R omega = (R)a.omega, invRho0 = (R)(1.0 / a.rho0);
     const NeighbourDeltas D = deltasOf(a.L);
+    const int T = st->T, K = st->K;
+    auto sweep = [&]() {
+        cudaMemsetAsync(gF, 0, sizeof(R) * 3 * n, a.stream);
+        cudaMemsetAsync(st->acc, 0, sizeof(AdjAcc), a.stream);
+        launchObjective<R>(a, o, ck + (long long)(T / K) * sz, st->uT, lam, gF, st->acc);
+        int cur = 0;   // lam + cur * sz holds lambda^{t+1}
+        for (int s = T / K - 1; s >= 0; --s) {
+            // f^{sK} is checkpoint s; recompute f^{sK+1} .. f^{sK+K-1} into seg
+            auto state = [&](int k) { return k == 0 ? ck + (long long)s * sz : sg + k * sz; };
+            for (int k = 0; k + 1 < K; ++k) {
+                pushStepKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, D, state(k), state(k + 1),
+                                                                                  omega, invRho0, nullptr);
+                *a.launches += 1;
+            }
+            for (int k = K - 1; k >= 0; --k) {
+                adjointStepKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(
+                    a.L, D, state(k), lam + cur * sz, lam + (1 - cur) * sz, gF, omega, invRho0, st->acc);
+                *a.launches += 1;
+                cur = 1 - cur;
+            }
+        }
+    };
+    // The sweep is captured once into a CUDA graph and launched as one unit
+    // (no host launch gaps between its 2T kernels); without a graph it is
+    // launched directly.
+    const long long launches0 = *a.launches;
+    cudaGraphExec_t exec = captureGraph(a.stream, sweep);
+    if (!exec) *a.launches = launches0;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, a.stream);
-    cudaMemsetAsync(gF, 0, sizeof(R) * 3 * n, a.stream);
-    cudaMemsetAsync(st->acc, 0, sizeof(AdjAcc), a.stream);
-    const int T = st->T, K = st->K;
-    launchObjective<R>(a, o, ck + (long long)(T / K) * sz, st->uT, lam, gF, st->acc);
-    int cur = 0;   // lam + cur * sz holds lambda^{t+1}
-    for (int s = T / K - 1; s >= 0; --s) {
-        // f^{sK} is checkpoint s; recompute f^{sK+1} .. f^{sK+K-1} into seg
-        auto state = [&](int k) { return k == 0 ? ck + (long long)s * sz : sg + k * sz; };
-        for (int k = 0; k + 1 < K; ++k) {
-            pushStepKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, D, state(k),
-                                                                              state(k + 1), omega, invRho0, nullptr);
-            *a.launches += 1;
-        }
-        for (int k = K - 1; k >= 0; --k) {
-            adjointStepKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, D, state(k),
-                                                                                 lam + cur * sz, lam + (1 - cur) * sz,
-                                                                                 gF, omega, invRho0, st->acc);
-            *a.launches += 1;
-            cur = 1 - cur;
-        }
-    }
+    if (exec) cudaGraphLaunch(exec, a.stream);
+    else sweep();
     cudaEventRecord(e1, a.stream);
     cudaEventSynchronize(e1);
     if (ms) cudaEventElapsedTime(ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (exec) cudaGraphExecDestroy(exec);
     AdjAcc h;
     cudaMemcpyAsync(&h, st->acc, sizeof(AdjAcc), cudaMemcpyDeviceToHost, a.stream);
     cudaStreamSynchronize(a.stream);
