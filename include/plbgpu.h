@@ -287,6 +287,22 @@ int plbgpu_load_binary_block(plbgpu_ctx* ctx, int handle, int what, const char* 
 int plbgpu_save_state(plbgpu_ctx* ctx, int handle, int what, const char* base);
 int plbgpu_load_state(plbgpu_ctx* ctx, int handle, int what, const char* plb_path);
 
+/* ------------------------------------------------------------ voxelizer */
+
+/* Voxel flags of a closed triangle mesh on the box [0, nx-1] x [0, ny-1] x
+ * [0, nz-1], as voxelize(mesh, domain, borderWidth) gives them
+ * (offLattice/voxelizer.hh:106-141, DetectBorderLineFunctional3D :653-685):
+ * 1 outside, 2 outerBorder (outside with an inside cell within border_width),
+ * 3 inside, 4 innerBorder.  The box's outer layer is outside.  triangles:
+ * n_triangles x 3 vertices x (x, y, z) in lattice units, each triangle's
+ * normal (v1 - v0) x (v2 - v0) pointing out of the body (a cell centre on the
+ * surface counts as inside).  flags: n = nx*ny*nz int32, z fastest.  A lattice
+ * line crossing the surface more than 64 times is refused (PLBGPU_ERR_ARG).
+ * The surface must lie inside the box's outer layer, which the reference
+ * seeds as outside: a body cut by that layer has no path-independent answer. */
+int plbgpu_voxelize(plbgpu_ctx* ctx, const double* triangles, size_t n_triangles, int nx, int ny, int nz,
+                    int border_width, int32_t* flags, size_t n);
+
 /* ------------------------------------------------------------ adjoint */
 
 /* Discrete adjoint of the collide-and-stream step (no counterpart in the

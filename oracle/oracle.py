@@ -53,6 +53,9 @@ def lib():
                                            ctypes.POINTER(ctypes.c_int32), ctypes.c_int, ctypes.c_int,
                                            ctypes.c_int, ctypes.POINTER(ctypes.c_uint8)]
         _lib.orc_sparse_blocks.restype = ctypes.c_int
+        _lib.orc_voxelize.argtypes = [dp, ctypes.c_long, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      ctypes.POINTER(ctypes.c_int32)]
+        _lib.orc_voxelize.restype = ctypes.c_int
         _lib.orc_set_threads.argtypes = [ctypes.c_int]
         _lib.orc_max_threads.restype = ctypes.c_int
     return _lib
@@ -179,6 +182,20 @@ def sparse_blocks(field, blocks):
     lib().orc_sparse_blocks(nx, ny, nz, field.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), bx, by, bz,
                             keep.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)))
     return keep.reshape(bx, by, bz)
+
+
+def voxelize(triangles, shape, border_width=1):
+    """voxelize(mesh, Box3D(0..nx-1, ...), borderWidth) restated: voxel flags
+    (1 outside, 2 outerBorder, 3 inside, 4 innerBorder) of the closed mesh
+    given as triangles (t, 3, 3) in lattice coordinates."""
+    tri = np.ascontiguousarray(triangles, np.float64).reshape(-1, 9)
+    nx, ny, nz = shape
+    flags = np.zeros(nx * ny * nz, np.int32)
+    rc = lib().orc_voxelize(_dp(tri), tri.shape[0], nx, ny, nz, int(border_width),
+                            flags.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+    if rc != 0:
+        raise MemoryError("oracle allocation failed")
+    return flags.reshape(nx, ny, nz)
 
 
 def regular_ranges(n, b):

@@ -1043,3 +1043,171 @@ int orc_sparse_blocks(int nx, int ny, int nz, const int32_t* field, int bx, int 
     return kept;
 }
 
+
+/* ------------------------------------------------------------ mesh voxelizer
+ *
+ * voxelize(mesh, domain, borderWidth) (offLattice/voxelizer.hh:106-141): the
+ * outer layer of the box is seeded "outside", every other cell starts
+ * undetermined; sweeps of VoxelizeMeshFunctional3D give an undetermined cell
+ * the flag of a determined neighbour (any of the 26), inverted when the
+ * segment between their centres crosses the surface an odd number of times
+ * (voxelizer.hh:330-380, checkIfFacetsCrossed :259-310), until no cell is
+ * undetermined; DetectBorderLineFunctional3D (:653-685) then marks outside
+ * cells with an inside cell within borderWidth as outerBorder and inside
+ * cells with an outside one as innerBorder.
+ *
+ * The segment test restates TriangularSurfaceMesh::pointOnTriangle with
+ * flag 0 (triangularSurfaceMesh.hh:1022-1120): tolerance eps1 = 100 DBL_EPSILON;
+ * an end point on the triangle's plane shifts the triangle by 2 eps1 along
+ * its unit normal (so a cell centre on the surface lies behind it); a
+ * segment parallel to the plane does not cross.  The crossings of a segment
+ * are counted as distinct distances (equal within 1e4 DBL_EPSILON, the
+ * reference's merge tolerance), after sorting them; the reference compares
+ * them in the order its triangle hash lists them.
+ *
+ * Flags: 1 outside, 2 outerBorder, 3 inside, 4 innerBorder.  The check of a
+ * whole mesh against every segment is brute force (with a bounding-box
+ * rejection): test infrastructure for boxes of some 10^5 cells. */
+
+enum { VX_UNDET = 0, VX_OUT = 1, VX_OUTB = 2, VX_IN = 3, VX_INB = 4 };
+
+static int vx_inside(int f) { return f == VX_IN || f == VX_INB; }
+static int vx_outside(int f) { return f == VX_OUT || f == VX_OUTB; }
+
+static double vx_dot(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+/* pointOnTriangle(p1, p2, flag 0): 1 and the distance from p1 when the
+ * segment p1-p2 meets the triangle (boundary included), else 0. */
+static int vx_segment_hits(const double* tri, const double* p1, const double* p2, double* dist) {
+    const double eps1 = 100.0 * 2.220446049250313e-16;
+    double v0[3] = {tri[0], tri[1], tri[2]};
+    double e0[3], e1[3], n[3], dir[3];
+    for (int d = 0; d < 3; ++d) {
+        e0[d] = tri[3 + d] - tri[d];
+        e1[d] = tri[6 + d] - tri[d];
+        dir[d] = p2[d] - p1[d];
+    }
+    n[0] = e0[1] * e1[2] - e0[2] * e1[1];
+    n[1] = e0[2] * e1[0] - e0[0] * e1[2];
+    n[2] = e0[0] * e1[1] - e0[1] * e1[0];
+    const double nn = sqrt(vx_dot(n, n));
+    for (int d = 0; d < 3; ++d) n[d] /= nn;
+    double num = vx_dot(v0, n) - vx_dot(p1, n);
+    const double denom = vx_dot(dir, n);
+    double t = num / denom;
+    if (fabs(t) <= eps1 || fabs(t - 1.0) <= eps1) {
+        for (int d = 0; d < 3; ++d) v0[d] += 2.0 * eps1 * n[d];
+        num = vx_dot(v0, n) - vx_dot(p1, n);
+        t = num / denom;
+    }
+    if (fabs(denom) <= eps1) return 0;   /* parallel (or in the plane): no crossing counted */
+    if ((t < 0.0 && fabs(t) > eps1) || (t > 1.0 && fabs(t - 1.0) > eps1)) return 0;
+    double x[3], tmp[3];
+    for (int d = 0; d < 3; ++d) {
+        x[d] = p1[d] + dir[d] * t;
+        tmp[d] = x[d] - v0[d];
+    }
+    const double a00 = vx_dot(e0, e0), a01 = vx_dot(e0, e1), a11 = vx_dot(e1, e1);
+    const double b0 = vx_dot(tmp, e0), b1 = vx_dot(tmp, e1);
+    const double det = a00 * a11 - a01 * a01;
+    const double u = (a11 * b0 - a01 * b1) / det;
+    const double v = (a00 * b1 - a01 * b0) / det;
+    const double upv = u + v;
+    if ((u < 0.0 && fabs(u) > eps1) || (u > 1.0 && fabs(u - 1.0) > eps1) || (v < 0.0 && fabs(v) > eps1) ||
+        (v > 1.0 && fabs(v - 1.0) > eps1) || (upv > 1.0 && fabs(upv - 1.0) > eps1))
+        return 0;
+    *dist = fabs(t) * sqrt(vx_dot(dir, dir));
+    return 1;
+}
+
+static int vx_cmp(const void* a, const void* b) {
+    const double x = *(const double*)a, y = *(const double*)b;
+    return x < y ? -1 : (x > y ? 1 : 0);
+}
+
+/* checkIfFacetsCrossed: an odd number of distinct crossings. */
+static int vx_crossed(const double* tri, long ntri, const double* lo, const double* hi, const double* p1,
+                      const double* p2, double* buf) {
+    int m = 0;
+    for (long k = 0; k < ntri; ++k) {
+        const double* T = tri + 9 * k;
+        int skip = 0;
+        for (int d = 0; d < 3 && !skip; ++d) {
+            const double smin = p1[d] < p2[d] ? p1[d] : p2[d], smax = p1[d] < p2[d] ? p2[d] : p1[d];
+            if (hi[3 * k + d] < smin - 1e-9 || lo[3 * k + d] > smax + 1e-9) skip = 1;
+        }
+        double dist;
+        if (!skip && vx_segment_hits(T, p1, p2, &dist) && m < 256) buf[m++] = dist;
+    }
+    if (m == 0) return 0;
+    qsort(buf, (size_t)m, sizeof(double), vx_cmp);
+    int distinct = 1;
+    for (int i = 1; i < m; ++i)
+        if (fabs(buf[i] - buf[i - 1]) > 1e4 * 2.220446049250313e-16) ++distinct;
+    return distinct & 1;
+}
+
+int orc_voxelize(const double* tri, long ntri, int nx, int ny, int nz, int borderWidth, int32_t* flags) {
+    const long n = (long)nx * ny * nz;
+    double* lo = (double*)malloc(sizeof(double) * 3 * (size_t)(ntri > 0 ? ntri : 1));
+    double* hi = (double*)malloc(sizeof(double) * 3 * (size_t)(ntri > 0 ? ntri : 1));
+    int32_t* bulk = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+    double buf[256];
+    if (!lo || !hi || !bulk) {
+        free(lo); free(hi); free(bulk);
+        return -1;
+    }
+    for (long k = 0; k < ntri; ++k)
+        for (int d = 0; d < 3; ++d) {
+            double a = tri[9 * k + d], b = tri[9 * k + 3 + d], c = tri[9 * k + 6 + d];
+            lo[3 * k + d] = fmin(a, fmin(b, c));
+            hi[3 * k + d] = fmax(a, fmax(b, c));
+        }
+    for (int x = 0; x < nx; ++x)
+        for (int y = 0; y < ny; ++y)
+            for (int z = 0; z < nz; ++z) {
+                const int edge = x == 0 || y == 0 || z == 0 || x == nx - 1 || y == ny - 1 || z == nz - 1;
+                bulk[((long)x * ny + y) * nz + z] = edge ? VX_OUT : VX_UNDET;
+            }
+    int changed = 1;
+    while (changed) {
+        changed = 0;
+        for (int x = 1; x < nx - 1; ++x)
+            for (int y = 1; y < ny - 1; ++y)
+                for (int z = 1; z < nz - 1; ++z) {
+                    const long id = ((long)x * ny + y) * nz + z;
+                    if (bulk[id] != VX_UNDET) continue;
+                    for (int k = 0; k < 27 && bulk[id] == VX_UNDET; ++k) {
+                        const int dx = k / 9 - 1, dy = (k / 3) % 3 - 1, dz = k % 3 - 1;
+                        if (!dx && !dy && !dz) continue;
+                        const int nb = bulk[((long)(x + dx) * ny + (y + dy)) * nz + (z + dz)];
+                        if (nb == VX_UNDET) continue;
+                        const double p1[3] = {x, y, z}, p2[3] = {x + dx, y + dy, z + dz};
+                        const int c = vx_crossed(tri, ntri, lo, hi, p1, p2, buf);
+                        bulk[id] = c ? (nb == VX_IN ? VX_OUT : VX_IN) : nb;
+                        changed = 1;
+                    }
+                }
+    }
+    for (int x = 0; x < nx; ++x)
+        for (int y = 0; y < ny; ++y)
+            for (int z = 0; z < nz; ++z) {
+                const long id = ((long)x * ny + y) * nz + z;
+                int f = bulk[id];
+                for (int dx = -borderWidth; dx <= borderWidth; ++dx)
+                    for (int dy = -borderWidth; dy <= borderWidth; ++dy)
+                        for (int dz = -borderWidth; dz <= borderWidth; ++dz) {
+                            if (!dx && !dy && !dz) continue;
+                            const int X = x + dx, Y = y + dy, Z = z + dz;
+                            if (X < 0 || Y < 0 || Z < 0 || X >= nx || Y >= ny || Z >= nz) continue;
+                            const int g = bulk[((long)X * ny + Y) * nz + Z];
+                            if (vx_outside(bulk[id]) && vx_inside(g)) f = VX_OUTB;
+                            if (vx_inside(bulk[id]) && vx_outside(g)) f = VX_INB;
+                        }
+                flags[id] = f;
+            }
+    free(lo);
+    free(hi);
+    free(bulk);
+    return 0;
+}

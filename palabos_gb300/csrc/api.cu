@@ -520,6 +520,8 @@ int domainAccess(plbgpu_ctx* c, int h, DomainAccess* out) {
 
 int domainFail(plbgpu_ctx* c, int code, const char* msg) { return fail(c, code, "%s", msg); }
 
+cudaStream_t contextStream(plbgpu_ctx* c) { return c ? c->stream : nullptr; }
+
 void domainSetState(plbgpu_ctx* c, int h, bool odd, bool pending) {
     Domain* d;
     if (lookup(c, h, &d)) return;

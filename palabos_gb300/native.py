@@ -107,6 +107,7 @@ SIGNATURES = {
     "plbgpu_cp_send": [_vp, _i, *LBOX, ctypes.c_char_p, _sz],
     "plbgpu_cp_receive": [_vp, _i, *LBOX, ctypes.c_char_p, _sz],
     "plbgpu_cp_collide_and_stream": [_vp, _i],
+    "plbgpu_voxelize": [_vp, _c_dbl_p, _sz, _i, _i, _i, _i, ctypes.POINTER(ctypes.c_int32), _sz],
     "plbgpu_adjoint_forward": [_vp, _i, _i, _i],
     "plbgpu_adjoint_interval": [_vp, _i, _c_int_p],
     "plbgpu_adjoint_backward": [_vp, _i, _c_dbl_p, _sz, _c_dbl_p, _c_dbl_p, _sz, _c_dbl_p,

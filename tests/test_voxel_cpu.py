@@ -1,0 +1,102 @@
+"""Mesh generators and the oracle's restatement of the reference voxelizer,
+against geometry whose answer is known: analytic spheres and boxes.
+
+The reference's own voxelizer (offLattice/voxelizer.hh) does not compile from
+this snapshot, so its restatement is pinned by these known answers instead
+of golden files.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from palabos_gb300 import meshes, voxel
+from palabos_gb300 import native as N
+
+
+def _signed_volume(tri):
+    return float(np.sum(np.einsum("ij,ij->i", tri[:, 0], np.cross(tri[:, 1], tri[:, 2])))) / 6.0
+
+
+def _closed(tri):
+    """Every edge is shared by exactly two triangles, in opposite directions."""
+    edges = {}
+    for t in np.round(tri, 12):
+        for a, b in ((0, 1), (1, 2), (2, 0)):
+            key = (tuple(t[a]), tuple(t[b]))
+            edges[key] = edges.get(key, 0) + 1
+    return all(edges.get((b, a), 0) == n for (a, b), n in edges.items())
+
+
+def test_meshes_are_closed_and_point_outwards():
+    s = meshes.sphere((10.3, 11.1, 9.7), 6.4, 500)
+    assert len(s) >= 500 and _closed(s)
+    assert _signed_volume(s) == pytest.approx(4 / 3 * np.pi * 6.4 ** 3, rel=0.02)
+    c = meshes.cuboid((1.5, 2.0, 3.25), (9.5, 7.0, 8.25), (2, 3, 1))
+    assert _closed(c)
+    assert _signed_volume(c) == pytest.approx(8.0 * 5.0 * 5.0, rel=1e-12)
+    assert _signed_volume(meshes.merge(s, c)) == pytest.approx(_signed_volume(s) + _signed_volume(c))
+
+
+def _grid(shape):
+    return np.meshgrid(*(np.arange(n, dtype=float) for n in shape), indexing="ij")
+
+
+def test_oracle_voxelizer_sphere_matches_geometry():
+    shape, c, r = (32, 34, 30), (15.3, 16.7, 14.1), 9.2
+    flags = O.voxelize(meshes.sphere(c, r, 320), shape)
+    X, Y, Z = _grid(shape)
+    d = np.sqrt((X - c[0]) ** 2 + (Y - c[1]) ** 2 + (Z - c[2]) ** 2)
+    inside = np.isin(flags, (voxel.INSIDE, voxel.INNER_BORDER))
+    # the facets stay within 0.5 cell of the sphere of this size and resolution
+    far = np.abs(d - r) > 0.5
+    assert np.array_equal(inside[far], (d < r)[far])
+    assert set(np.unique(flags)) == {voxel.OUTSIDE, voxel.OUTER_BORDER, voxel.INSIDE, voxel.INNER_BORDER}
+
+
+@pytest.mark.parametrize("lo,hi", [((5.5, 6.25, 4.75), (20.5, 18.25, 22.75)), ((5, 6, 4), (20, 18, 22))])
+def test_oracle_voxelizer_box_is_exact(lo, hi):
+    """Fractional faces, and faces through cell centres (which count as
+    inside: the reference shifts the surface outward along its normal)."""
+    shape = (28, 26, 30)
+    flags = O.voxelize(meshes.cuboid(lo, hi, (3, 2, 4)), shape)
+    X, Y, Z = _grid(shape)
+    inside = ((X >= lo[0]) & (X <= hi[0]) & (Y >= lo[1]) & (Y <= hi[1]) & (Z >= lo[2]) & (Z <= hi[2]))
+    assert np.array_equal(np.isin(flags, (voxel.INSIDE, voxel.INNER_BORDER)), inside)
+
+
+@pytest.mark.parametrize("width", [0, 1, 2])
+def test_oracle_border_layers(width):
+    """DetectBorderLineFunctional3D: a border cell has a cell of the other
+    side within `width` (box neighbourhood), a bulk cell has none."""
+    shape = (20, 21, 19)
+    flags = O.voxelize(meshes.cuboid((5.5, 6.5, 4.5), (13.5, 14.5, 12.5)), shape, width)
+    inside = np.isin(flags, (voxel.INSIDE, voxel.INNER_BORDER))
+    padded = np.pad(inside, width, constant_values=False)
+    padded_out = np.pad(~inside, width, constant_values=False)
+    near_in = np.zeros(shape, bool)
+    near_out = np.zeros(shape, bool)
+    for dx in range(-width, width + 1):
+        for dy in range(-width, width + 1):
+            for dz in range(-width, width + 1):
+                sl = tuple(slice(width + d, width + d + n) for d, n in zip((dx, dy, dz), shape))
+                near_in |= padded[sl]
+                near_out |= padded_out[sl]
+    assert np.array_equal(flags == voxel.OUTER_BORDER, ~inside & near_in)
+    assert np.array_equal(flags == voxel.INNER_BORDER, inside & near_out)
+
+
+def test_oracle_voxelizer_two_bodies():
+    shape = (40, 30, 30)
+    flags = O.voxelize(meshes.merge(meshes.sphere((11.2, 15.3, 14.6), 6.1, 320),
+                                    meshes.cuboid((23.5, 8.5, 9.5), (33.5, 21.5, 19.5))), shape)
+    assert not np.isin(flags[:, :, :2], (voxel.INSIDE, voxel.INNER_BORDER)).any()
+    assert np.isin(flags[11, 15, 14], (voxel.INSIDE,)) and flags[28, 15, 14] == voxel.INSIDE
+    assert flags[20, 15, 14] == voxel.OUTSIDE and flags[18, 15, 14] == voxel.OUTER_BORDER
+
+
+def test_kinds_from_flags():
+    flags = np.array([voxel.OUTSIDE, voxel.OUTER_BORDER, voxel.INNER_BORDER, voxel.INSIDE])
+    assert list(voxel.kinds_from_flags(flags, "outside")) == [N.BGK, N.BGK, N.BOUNCEBACK, N.NODYNAMICS]
+    assert list(voxel.kinds_from_flags(flags, "inside", N.GUO)) == [N.NODYNAMICS, N.BOUNCEBACK, N.GUO, N.GUO]
+    with pytest.raises(ValueError):
+        voxel.kinds_from_flags(flags, "around")
