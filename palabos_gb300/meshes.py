@@ -83,3 +83,58 @@ def cuboid(lower, upper, segments=(1, 1, 1)):
 def merge(*meshes):
     """One mesh from several (the reference's TriangleSet::append)."""
     return np.concatenate([np.asarray(m, np.float64).reshape(-1, 3, 3) for m in meshes])
+
+
+def read_stl(path):
+    """Triangles (t, 3, 3) of an ASCII or binary STL file (what the reference's
+    TriangleSet reads, offLattice/triangleSet.hh), vertices in file order."""
+    with open(path, "rb") as f:
+        data = f.read()
+    if len(data) >= 84:
+        count = int(np.frombuffer(data, "<u4", 1, 80)[0])
+        if 84 + 50 * count == len(data):
+            rec = np.dtype([("n", "<f4", 3), ("v", "<f4", (3, 3)), ("attr", "<u2")])
+            return np.frombuffer(data, rec, count, 84)["v"].astype(np.float64)
+    text = data.decode("ascii", errors="replace").split()
+    verts = [text[i + 1:i + 4] for i, w in enumerate(text) if w == "vertex"]
+    if not verts or len(verts) % 3:
+        raise ValueError(f"{path}: not an STL file")
+    return np.array(verts, np.float64).reshape(-1, 3, 3)
+
+
+def write_stl(path, triangles, binary=True):
+    """Write triangles (t, 3, 3) as a binary (or ASCII) STL file."""
+    tri = np.asarray(triangles, np.float64).reshape(-1, 3, 3)
+    n = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+    n /= np.maximum(np.linalg.norm(n, axis=1, keepdims=True), 1e-300)
+    if binary:
+        rec = np.zeros(len(tri), np.dtype([("n", "<f4", 3), ("v", "<f4", (3, 3)), ("attr", "<u2")]))
+        rec["n"], rec["v"] = n, tri
+        with open(path, "wb") as f:
+            f.write(b"\0" * 80 + np.uint32(len(tri)).tobytes() + rec.tobytes())
+        return
+    with open(path, "w") as f:
+        f.write("solid mesh\n")
+        for t, nn in zip(tri, n):
+            f.write(f"facet normal {nn[0]:.9e} {nn[1]:.9e} {nn[2]:.9e}\n outer loop\n")
+            for v in t:
+                f.write(f"  vertex {v[0]:.17e} {v[1]:.17e} {v[2]:.17e}\n")
+            f.write(" endloop\nendfacet\n")
+        f.write("endsolid mesh\n")
+
+
+def to_lattice_units(triangles, resolution, reference_direction=0, layer=0):
+    """The reference's DEFscaledMesh(set, resolution, referenceDirection,
+    margin, extraLayer) scaling (toLatticeUnits,
+    offLattice/triangularSurfaceMesh.hh:1552-1575; triangleBoundary3D.hh:
+    272-300): the bounding box's low corner moves to the origin, the extent
+    along reference_direction becomes `resolution` cells, then everything
+    shifts by `layer` (margin + extraLayer) cells on every axis.  Returns the
+    mesh, the physical position of the lattice origin and dx."""
+    tri = np.asarray(triangles, np.float64).reshape(-1, 3, 3)
+    lo = tri.reshape(-1, 3).min(axis=0)
+    hi = tri.reshape(-1, 3).max(axis=0)
+    scale = float(resolution) / (hi[reference_direction] - lo[reference_direction])
+    dx = 1.0 / scale
+    out = (tri - lo) * scale + float(layer)
+    return out, lo - float(layer) * dx, dx

@@ -100,3 +100,19 @@ def test_kinds_from_flags():
     assert list(voxel.kinds_from_flags(flags, "inside", N.GUO)) == [N.NODYNAMICS, N.BOUNCEBACK, N.GUO, N.GUO]
     with pytest.raises(ValueError):
         voxel.kinds_from_flags(flags, "around")
+
+
+@pytest.mark.parametrize("binary", [True, False])
+def test_stl_round_trip_and_lattice_units(tmp_path, binary):
+    tri = meshes.sphere((0.1, -0.2, 0.05), 0.4, 80)
+    path = tmp_path / "s.stl"
+    meshes.write_stl(path, tri, binary=binary)
+    back = meshes.read_stl(path)
+    assert back.shape == tri.shape
+    assert np.allclose(back, tri, atol=1e-6 if binary else 0.0)
+    lu, origin, dx = meshes.to_lattice_units(back, 40, 0, layer=3)
+    assert lu[..., 0].min() == pytest.approx(3.0) and lu[..., 0].max() == pytest.approx(43.0)
+    assert dx == pytest.approx(np.ptp(back[..., 0]) / 40)
+    assert np.allclose(origin + dx * lu.reshape(-1, 3), back.reshape(-1, 3))
+    flags = O.voxelize(lu, (50, 50, 50))
+    assert np.isin(flags[23, 23, 23], (voxel.INSIDE,))
