@@ -550,7 +550,12 @@ int plbgpu_create(int device, plbgpu_ctx** out) {
         delete c;
         return PLBGPU_ERR_CUDA;
     }
-    if (cudaStreamCreateWithFlags(&c->side.stream, cudaStreamNonBlocking) != cudaSuccess ||
+    // The border rows' stream has the highest priority: submitted after the
+    // interior kernel, its blocks take the first SM slots that free up
+    // instead of waiting for the interior kernel's last wave.
+    int leastPriority = 0, greatestPriority = 0;
+    cudaDeviceGetStreamPriorityRange(&leastPriority, &greatestPriority);
+    if (cudaStreamCreateWithPriority(&c->side.stream, cudaStreamNonBlocking, greatestPriority) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->side.fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->side.join, cudaEventDisableTiming) != cudaSuccess) {
         if (c->side.stream) cudaStreamDestroy(c->side.stream);

@@ -682,7 +682,7 @@ __global__ void __launch_bounds__(128, 8)
 // x = nx-1 (all y), then y = 0, y = ny-1 (1 <= x <= nx-2); when nx < 3 or
 // ny < 3, or on a sparse domain, every row is a border row.
 template <typename S, bool ODD, bool STATS, bool EXT, bool SPARSE>
-__global__ void __launch_bounds__(128) edgeRowStepKernel(DevLattice L, StepParams<typename StoreT<S>::R> P,
+__global__ void __launch_bounds__(128, sizeof(S) <= 4 ? 6 : 1) edgeRowStepKernel(DevLattice L, StepParams<typename StoreT<S>::R> P,
                                                           StatsAcc* acc, int rows) {
     using R = typename StoreT<S>::R;
     const int z = blockIdx.x * blockDim.x + threadIdx.x;

@@ -25,11 +25,12 @@ struct StepLaunch {
         // which checks each neighbour's kind.
         const bool general = L.sparse || L.nx < 3 || L.ny < 3;
         const int edgeRows = general ? L.nx * L.ny : 2 * L.ny + 2 * (L.nx - 2);
-        // The border rows run on the side stream, beside the interior kernel.
-        // Submission order decides whose blocks take the SMs first: for the
-        // 2-byte forms the interior kernel goes first and the border blocks
-        // fill its last wave (3% faster); for FP32 the border kernel goes
-        // first (2% faster); FP64 is bound by its FP64 pipe either way.
+        // The border rows run on the side stream (the context's highest
+        // priority), beside the interior kernel.  Submission order decides
+        // whose blocks take the SMs first: the 2-byte forms submit the
+        // interior kernel first and the border blocks take the first slots
+        // that free up (2-4% faster); FP32 submits the border kernel first
+        // (2% faster); FP64 is bound by its FP64 pipe either way.
         constexpr bool interiorFirst = sizeof(S) == 2;
         cudaStream_t es = s;
         if (side && !general && cudaEventRecord(side->fork, s) == cudaSuccess &&
