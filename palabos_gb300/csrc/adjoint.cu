@@ -65,11 +65,12 @@ template <> __device__ inline double tangentOf<Dual>(const Dual& x) { return x.d
 template <typename R>
 __device__ __forceinline__ void adjCollide(int k, R* f, const R* F, const BgkConst<R>& bc, R invRho0) {
     R rhoBar, j[3];
-    switch (k) {
-    case K_BGK:
+    if (bgkBase(k)) {   // BGK, and the BGK base of the face conditions
         rhoBarJ<R>(f, rhoBar, j);
         bgkCollide<R>(f, rhoBar, j, bc, invRhoOf(rhoBar));
-        break;
+        return;
+    }
+    switch (k) {
     case K_GUO: {
         R rb = rhoBarSeq<R>(f);
         R rb2, jj[3], u[3];
@@ -378,11 +379,14 @@ __global__ void stateInKernel(DevLattice L, const R* in) {
 // or, leaving a non-periodic domain, back into slot opp(i) of x.
 template <typename R, bool INTERIOR>
 __device__ __forceinline__ void pushCell(const DevLattice& L, const NeighbourDeltas& D, const R* fin, R* fout,
-                                         R omega, R invRho0, const double* dF, int x, int y, int z) {
+                                         R omega, R invRho0, const double* dF, bool pending, int x, int y, int z) {
     const long long idx = ((long long)x * L.ny + y) * L.nz + z;
     const int k = L.flags[idx];
     R f[19], F[3];
     for (int i = 0; i < 19; ++i) f[i] = fin[i * L.n + idx];
+    // a face cell's missing populations are completed before it collides
+    // when the state comes from a streaming step, as in the fused step
+    if (pending && isFace(k)) completeIfFace<R>(L, idx, k, f);
     cellForce(L, forceIsFp64<R>(), idx, dF, F);
     adjCollide<R>(k, f, F, bgkConsts<R>(omega), invRho0);
     CellMoves<INTERIOR> mv(L, x, y, z);
@@ -396,12 +400,12 @@ __device__ __forceinline__ void pushCell(const DevLattice& L, const NeighbourDel
 
 template <typename R>
 __global__ void pushStepKernel(DevLattice L, NeighbourDeltas D, const R* fin, R* fout, R omega, R invRho0,
-                               const double* dF) {
+                               const double* dF, bool pending) {
     const int z = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y, x = blockIdx.z;
     if (z >= L.nz) return;
-    if (interiorRow(L, x, y)) pushCell<R, true>(L, D, fin, fout, omega, invRho0, dF, x, y, z);
-    else pushCell<R, false>(L, D, fin, fout, omega, invRho0, dF, x, y, z);
+    if (interiorRow(L, x, y)) pushCell<R, true>(L, D, fin, fout, omega, invRho0, dF, pending, x, y, z);
+    else pushCell<R, false>(L, D, fin, fout, omega, invRho0, dF, pending, x, y, z);
 }
 
 // J, lambda^T = dJ/df^T and the explicit dJ/dF of the Guo velocity u = j/rho + F/2.
@@ -447,6 +451,43 @@ __global__ void objectiveKernel(DevLattice L, const R* f, const double* v, bool 
         }
     }
     blockAdd(jsum, acc->objective);
+}
+
+// Reverse step of the face cells (regularized and Zou/He velocity and
+// pressure faces), one thread per cell of `faces`: the cell's local map
+// out = collide(complete(f)) (completion only when `pending`) is
+// differentiated in forward mode, one dual pass per input population and one
+// for omega, giving lambda^n = J^T mu and (d out / d omega)^T mu.  Face cells
+// are a thin layer, so twenty passes over them cost little next to the bulk.
+template <typename R>
+__global__ void faceAdjointKernel(DevLattice L, const R* f, const R* lamIn, R* lamOut, double omega, bool pending,
+                                  const long long* faces, int nFaces, AdjAcc* acc) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double go = 0.;
+    if (t < nFaces) {
+        const long long idx = faces[t];
+        const int z = (int)(idx % L.nz), y = (int)((idx / L.nz) % L.ny), x = (int)(idx / ((long long)L.ny * L.nz));
+        const int k = L.flags[idx];
+        const Neighbourhood nb = neighbourhood(L, x, y, z);
+        double mu[19], fc[19];
+        mu[0] = (double)lamIn[idx];
+        for (int i = 1; i < 19; ++i) {
+            long long off;
+            mu[i] = (double)(nb.move(i, +1, off) ? lamIn[i * L.n + idx + off] : lamIn[opp(i) * L.n + idx]);
+        }
+        for (int i = 0; i < 19; ++i) fc[i] = (double)f[i * L.n + idx];
+        for (int dir = 0; dir <= 19; ++dir) {   // 0..18: population dir; 19: omega
+            Dual g[19], F[3];
+            for (int i = 0; i < 19; ++i) g[i] = Dual(fc[i], i == dir ? 1. : 0.);
+            if (pending) completeIfFace<Dual>(L, idx, k, g);
+            adjCollide<Dual>(k, g, F, bgkConsts<Dual>(Dual(omega, dir == 19 ? 1. : 0.)), Dual(0.));
+            double s = 0.;
+            for (int i = 0; i < 19; ++i) s += mu[i] * g[i].d;
+            if (dir < 19) lamOut[dir * L.n + idx] = (R)s;
+            else go = s;
+        }
+    }
+    blockAdd(go, acc->gOmega);
 }
 
 // Drag objective J = w . D(f) with D the momentum-exchange drag the next
@@ -502,6 +543,7 @@ __device__ __forceinline__ R adjointCell(const DevLattice& L, const NeighbourDel
                                          R* lamOut, R* gF, R omega, R invRho0, int x, int y, int z) {
     const long long idx = ((long long)x * L.ny + y) * L.nz + z;
     const int k = L.flags[idx];
+    if (isFace(k)) return R(0);   // faceAdjointKernel reverses the face cells
     CellMoves<INTERIOR> mv(L, x, y, z);
     R mu[19], fc[19], F[3], lam[19], g[3] = {R(0), R(0), R(0)};
     mu[0] = lamIn[idx];
@@ -580,10 +622,16 @@ struct AdjointState {
     void* gF = nullptr;        // 3 planes
     double* uT = nullptr;      // target velocity, n * 3
     AdjAcc* acc = nullptr;
+    long long* faces = nullptr;   // face cells (cell indices), nFaces of them
+    int nFaces = 0;
+    bool pending0 = false;     // the recorded run's first step completes its faces
     bool ready = false;        // a forward run is recorded
     ~AdjointState() {
-        cudaFree(ckpt); cudaFree(seg); cudaFree(lam); cudaFree(gF); cudaFree(uT); cudaFree(acc);
+        cudaFree(ckpt); cudaFree(seg); cudaFree(lam); cudaFree(gF); cudaFree(uT); cudaFree(acc); cudaFree(faces);
     }
+    // Steps after the first collide states that came from a streaming step:
+    // their faces are completed first.
+    bool pendingAt(long long t) const { return t == 0 ? pending0 : nFaces > 0; }
 };
 
 void freeAdjoint(void* p) { delete static_cast<AdjointState*>(p); }
@@ -659,16 +707,37 @@ void launchObjective(const DomainAccess& a, const Objective& o, const R* f, cons
     *a.launches += 1;
 }
 
-int checkKinds(plbgpu_ctx* c, const DomainAccess& a) {
+// The adjoint covers BGK, Guo, incompressible BGK, bounce-back,
+// momentum-exchange bounce-back, no-dynamics and the regularized and Zou/He
+// face cells; `faces` (optional) receives the face cells' indices.  Edges and
+// corners (finite differences over neighbours) are refused.
+int checkKinds(plbgpu_ctx* c, const DomainAccess& a, std::vector<long long>* faces = nullptr) {
     std::vector<uint8_t> k((size_t)a.L.n);
     if (cudaMemcpyAsync(k.data(), a.L.flags, k.size(), cudaMemcpyDeviceToHost, a.stream) != cudaSuccess ||
         cudaStreamSynchronize(a.stream) != cudaSuccess)
         return domainFail(c, PLBGPU_ERR_CUDA, "reading cell kinds failed");
-    for (uint8_t v : k)
+    for (size_t i = 0; i < k.size(); ++i) {
+        const int v = k[i];
+        if (isFace(v)) {
+            if (faces) faces->push_back((long long)i);
+            continue;
+        }
         if (v != K_BGK && v != K_GUO && v != K_INCBGK && v != K_BB && v != K_MEBB && v != K_NODYN)
             return domainFail(c, PLBGPU_ERR_ARG,
-                              "the adjoint supports BGK, Guo, incompressible BGK, bounce-back and no-dynamics cells");
+                              "the adjoint supports BGK, Guo, incompressible BGK, bounce-back, momentum-exchange, "
+                              "no-dynamics and face cells (no edges or corners)");
+    }
     return PLBGPU_OK;
+}
+
+// The face cells' reverse step beside the bulk's (disjoint writes).
+template <typename R>
+void launchFaceAdjoint(const DomainAccess& a, const long long* faces, int nFaces, const R* f, const R* lamIn,
+                       R* lamOut, bool pending, AdjAcc* acc) {
+    if (nFaces == 0) return;
+    faceAdjointKernel<R><<<(nFaces + 127) / 128, 128, 0, a.stream>>>(a.L, f, lamIn, lamOut, a.omega, pending, faces,
+                                                                       nFaces, acc);
+    *a.launches += 1;
 }
 
 #define ADJ_TRY(call)                                                                          \
@@ -694,7 +763,8 @@ int forwardImpl(plbgpu_ctx* c, int h, DomainAccess& a, AdjointState* st, int T, 
     const NeighbourDeltas D = deltasOf(a.L);
     for (int t = 0; t < T; ++t) {
         R* out = ((t + 1) % K == 0) ? ck + ((t + 1) / K) * sz : bufs[t & 1];
-        pushStepKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, D, cur, out, omega, invRho0, nullptr);
+        pushStepKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, D, cur, out, omega, invRho0, nullptr,
+                                                                          st->pendingAt(t));
         *a.launches += 1;
         cur = out;
     }
@@ -704,7 +774,8 @@ int forwardImpl(plbgpu_ctx* c, int h, DomainAccess& a, AdjointState* st, int T, 
     *a.launches += 1;
     ADJ_TRY(cudaGetLastError());
     ADJ_TRY(cudaStreamSynchronize(a.stream));
-    domainSetState(c, h, false, false);
+    // the last push streamed: face cells are completed at the next collision
+    domainSetState(c, h, false, st->nFaces > 0);
     return PLBGPU_OK;
 }
 
@@ -746,14 +817,16 @@ int backwardImpl(DomainAccess& a, AdjointState* st, const Objective& o, double* 
             // f^{sK} is checkpoint s; recompute f^{sK+1} .. f^{sK+K-1} into seg
             auto state = [&](int k) { return k == 0 ? ck + (long long)s * sz : sg + k * sz; };
             for (int k = 0; k + 1 < K; ++k) {
-                pushStepKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, D, state(k), state(k + 1),
-                                                                                  omega, invRho0, nullptr);
+                pushStepKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(
+                    a.L, D, state(k), state(k + 1), omega, invRho0, nullptr, st->pendingAt((long long)s * K + k));
                 *a.launches += 1;
             }
             for (int k = K - 1; k >= 0; --k) {
                 adjointStepKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(
                     a.L, D, state(k), lam + cur * sz, lam + (1 - cur) * sz, gF, omega, invRho0, st->acc);
                 *a.launches += 1;
+                launchFaceAdjoint<R>(a, st->faces, st->nFaces, state(k), lam + cur * sz, lam + (1 - cur) * sz,
+                                     st->pendingAt((long long)s * K + k), st->acc);
                 cur = 1 - cur;
             }
         }
@@ -826,8 +899,9 @@ int adjointBackward(plbgpu_ctx* c, int h, const Objective& o, double* objective,
 // total mass, adds nothing because the collision conserves mass for every
 // omega and force).  Three states of memory whatever the number of steps.
 template <typename R>
-int steadyImpl(plbgpu_ctx* c, DomainAccess& a, int iterations, const Objective& o, double* objective,
-               double* grad_force, double* grad_omega, float* ms) {
+int steadyImpl(plbgpu_ctx* c, DomainAccess& a, int iterations, const Objective& o,
+               const std::vector<long long>& faceList, double* objective, double* grad_force, double* grad_omega,
+               float* ms) {
     const long long n = a.L.n, sz = 19 * n;
     struct Buffers {
         R* f = nullptr;
@@ -835,8 +909,10 @@ int steadyImpl(plbgpu_ctx* c, DomainAccess& a, int iterations, const Objective& 
         R* gF = nullptr;
         double* w = nullptr;
         AdjAcc* acc = nullptr;
+        long long* faces = nullptr;
         cudaEvent_t e0 = nullptr, e1 = nullptr;
         ~Buffers() {
+            cudaFree(faces);
             cudaFree(f);
             cudaFree(lam);
             cudaFree(gF);
@@ -853,6 +929,12 @@ int steadyImpl(plbgpu_ctx* c, DomainAccess& a, int iterations, const Objective& 
     ADJ_TRY(cudaMalloc(&b.acc, sizeof(AdjAcc)));
     ADJ_TRY(cudaEventCreate(&b.e0));
     ADJ_TRY(cudaEventCreate(&b.e1));
+    const int nFaces = (int)faceList.size();
+    if (nFaces) {
+        ADJ_TRY(cudaMalloc(&b.faces, sizeof(long long) * faceList.size()));
+        ADJ_TRY(cudaMemcpyAsync(b.faces, faceList.data(), sizeof(long long) * faceList.size(), cudaMemcpyHostToDevice,
+                                a.stream));
+    }
     if (o.kind != kDrag)
         ADJ_TRY(cudaMemcpyAsync(b.w, o.v, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, a.stream));
     ADJ_TRY(cudaMemsetAsync(b.gF, 0, sizeof(R) * 3 * n, a.stream));
@@ -869,6 +951,8 @@ int steadyImpl(plbgpu_ctx* c, DomainAccess& a, int iterations, const Objective& 
                                                                              b.lam + (1 - cur) * sz, b.gF, omega,
                                                                              invRho0, b.acc);
         *a.launches += 1;
+        // the steady state is a streamed state: its faces complete at each step
+        launchFaceAdjoint<R>(a, b.faces, nFaces, b.f, b.lam + cur * sz, b.lam + (1 - cur) * sz, nFaces > 0, b.acc);
         cur = 1 - cur;
     }
     ADJ_TRY(cudaGetLastError());
@@ -893,8 +977,9 @@ int tangentLinear(plbgpu_ctx* c, int h, int T, const double* dforce, size_t ndf,
     if (T < 0 || !objective || !directional || (dforce && (long long)ndf != 3 * n))
         return domainFail(c, PLBGPU_ERR_ARG, "tangent: bad arguments");
     if ((rc = checkObjective(c, a, o))) return rc;
-    if ((rc = checkKinds(c, a))) return rc;
-    if (a.pending) return domainFail(c, PLBGPU_ERR_STATE, "tangent: boundary faces are not supported");
+    std::vector<long long> faceList;
+    if ((rc = checkKinds(c, a, &faceList))) return rc;
+    const bool hasFaces = !faceList.empty();
     double *f0 = nullptr, *dF = nullptr, *uT = nullptr;
     Dual* buf = nullptr;
     AdjAcc* acc = nullptr;
@@ -920,7 +1005,8 @@ int tangentLinear(plbgpu_ctx* c, int h, int T, const double* dforce, size_t ndf,
         const Dual om(a.omega, domega), inv0(1.0 / a.rho0);
         const NeighbourDeltas D = deltasOf(a.L);
         for (int t = 0; t < T; ++t) {
-            pushStepKernel<Dual><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, D, cur, nxt, om, inv0, dF);
+            pushStepKernel<Dual><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, D, cur, nxt, om, inv0, dF,
+                                                                                 t == 0 ? a.pending : hasFaces);
             *a.launches += 1;
             std::swap(cur, nxt);
         }
@@ -962,8 +1048,8 @@ int plbgpu_adjoint_forward(plbgpu_ctx* c, int h, int T, int K) {
     if (rc) return rc;
     if (T < 1 || K < 0 || (K > 0 && T % K != 0))
         return domainFail(c, PLBGPU_ERR_ARG, "adjoint: need T >= 1 and K = 0 or a divisor of T");
-    if ((rc = checkKinds(c, a))) return rc;
-    if (a.pending) return domainFail(c, PLBGPU_ERR_STATE, "adjoint: boundary faces are not supported");
+    std::vector<long long> faces;
+    if ((rc = checkKinds(c, a, &faces))) return rc;
     AdjointState* st = static_cast<AdjointState*>(*a.adjointSlot);
     const size_t rs = a.precision == PLBGPU_FP64 ? sizeof(double) : sizeof(float);
     const long long n = a.L.n, sz = 19 * n;
@@ -1005,6 +1091,15 @@ int plbgpu_adjoint_forward(plbgpu_ctx* c, int h, int T, int K) {
     }
     st->T = T;
     st->ready = false;
+    cudaFree(st->faces);
+    st->faces = nullptr;
+    st->nFaces = (int)faces.size();
+    st->pending0 = a.pending;
+    if (!faces.empty()) {
+        ADJ_TRY(cudaMalloc(&st->faces, sizeof(long long) * faces.size()));
+        ADJ_TRY(cudaMemcpyAsync(st->faces, faces.data(), sizeof(long long) * faces.size(), cudaMemcpyHostToDevice,
+                                a.stream));
+    }
     rc = a.precision == PLBGPU_FP64 ? forwardImpl<double>(c, h, a, st, T, K) : forwardImpl<float>(c, h, a, st, T, K);
     if (rc == PLBGPU_OK) st->ready = true;
     return rc;
@@ -1056,10 +1151,11 @@ static int adjointSteady(plbgpu_ctx* c, int h, int iterations, const Objective& 
     if (iterations < 0 || !objective || !grad_omega || (grad_force && (long long)ng != 3 * n))
         return domainFail(c, PLBGPU_ERR_ARG, "steady adjoint: bad arguments");
     if ((rc = checkObjective(c, a, o))) return rc;
-    if ((rc = checkKinds(c, a))) return rc;
-    if (a.pending) return domainFail(c, PLBGPU_ERR_STATE, "steady adjoint: boundary faces are not supported");
-    return a.precision == PLBGPU_FP64 ? steadyImpl<double>(c, a, iterations, o, objective, grad_force, grad_omega, ms)
-                                      : steadyImpl<float>(c, a, iterations, o, objective, grad_force, grad_omega, ms);
+    std::vector<long long> faces;
+    if ((rc = checkKinds(c, a, &faces))) return rc;
+    return a.precision == PLBGPU_FP64
+               ? steadyImpl<double>(c, a, iterations, o, faces, objective, grad_force, grad_omega, ms)
+               : steadyImpl<float>(c, a, iterations, o, faces, objective, grad_force, grad_omega, ms);
 }
 
 int plbgpu_adjoint_steady_weighted(plbgpu_ctx* c, int h, int iterations, const double* weights, size_t n3,

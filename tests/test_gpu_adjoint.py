@@ -98,9 +98,9 @@ def test_fp32_adjoint_tracks_fp64():
 
 
 def test_adjoint_rejects_unsupported_cells():
-    from palabos_gb300 import DeviceLattice3D, PlbGpuError, face_kind, REG_VELOCITY
+    from palabos_gb300 import DeviceLattice3D, PlbGpuError
     lat = DeviceLattice3D(6, 6, 6, 1.2)
-    lat.define_dynamics((0, 0, 1, 4, 1, 4), face_kind(REG_VELOCITY, 0, -1))
+    lat.define_dynamics((0, 0, 0, 0, 1, 4), N.VELOCITY_EDGE)   # edges and corners have no reverse step
     with pytest.raises(PlbGpuError):
         lat.adjoint_forward(4, 2)
     lat2 = DeviceLattice3D(6, 6, 6, 1.2)
@@ -383,3 +383,90 @@ def test_adjoint_objective_arguments():
         lat.adjoint_backward(drag=(1.0, 0.0))            # a direction has 3 components
     with pytest.raises(PlbGpuError):
         lat.adjoint_steady(iterations=2, drag=(1.0, 0.0, 0.0))   # no momentum-exchange masks
+
+
+def _face_channel(faces="regularized", omega=1.8, shape=(24, 12, 12)):
+    """Channel past a momentum-exchange sphere with a velocity inlet and a
+    pressure outlet, regularized or Zou/He."""
+    wl = workloads.channel_sphere(shape, (8.2, 5.6, 6.3), 2.5, 0.05, omega)
+    if faces == "zouhe":
+        k = wl.kinds.copy()
+        k[k == N.face_kind(N.REG_VELOCITY, 0, -1)] = N.face_kind(N.ZOUHE_VELOCITY, 0, -1)
+        k[k == N.face_kind(N.REG_PRESSURE, 0, +1)] = N.face_kind(N.ZOUHE_PRESSURE, 0, +1)
+        wl.kinds = k
+    return wl
+
+
+@pytest.mark.parametrize("warm", [0, 3])
+@pytest.mark.parametrize("faces", ["regularized", "zouhe"])
+@pytest.mark.parametrize("K", [1, 5])
+def test_face_adjoint_drag_matches_tangent_linear(faces, K, warm):
+    """Velocity inlet, pressure outlet: the face cells' reverse step (dual
+    passes over their completion and collision) against the dual-number run,
+    from a freshly initialized state and from one whose faces are pending."""
+    wl = _face_channel(faces)
+    T = 20
+    lat = wl.lattice("fp64")
+    lat.collide_and_stream(warm)
+    J_t, dJ = lat.tangent_linear(T, None, 0.37, drag=DRAG_DIR)
+    lat.adjoint_forward(T, K)
+    J, _, gO, _ = lat.adjoint_backward(drag=DRAG_DIR, want_force=False)
+    assert J == pytest.approx(J_t, rel=1e-13) and J != 0.0
+    assert gO * 0.37 == pytest.approx(dJ, rel=1e-9), (gO * 0.37, dJ)
+
+
+def test_face_adjoint_weighted_matches_tangent_linear():
+    wl = _face_channel("regularized")
+    lat = wl.lattice("fp64")
+    lat.collide_and_stream(2)
+    w = np.random.default_rng(17).standard_normal(wl.shape + (3,))
+    J_t, dJ = lat.tangent_linear(16, None, -0.8, weights=w)
+    lat.adjoint_forward(16, 4)
+    J, _, gO, _ = lat.adjoint_backward(weights=w, want_force=False)
+    assert J == pytest.approx(J_t, rel=1e-13)
+    assert gO * -0.8 == pytest.approx(dJ, rel=1e-9)
+
+
+def test_face_adjoint_drag_matches_reference_finite_differences():
+    wl = _face_channel("regularized")
+    T = 20
+    lat = wl.lattice("fp64")
+    lat.collide_and_stream(3)
+    f0 = lat.receive()   # faces completed, as the reference holds them after a step
+    lat.adjoint_forward(T, 5)
+    J, _, gO, _ = lat.adjoint_backward(drag=DRAG_DIR, want_force=False)
+
+    def drag(omega):
+        ol = O.OracleLattice(*wl.shape, wl.periodic, omega, wl.kinds, wl.bcval, None)
+        f, _ = ol.run(f0, T, with_stats=False)
+        _, st = ol.run(f, 1, with_stats=True)
+        return float(np.dot(DRAG_DIR, st[0, 3:6]))
+
+    assert J == pytest.approx(drag(wl.omega), rel=1e-12)
+    h = 1e-6
+    fd = (drag(wl.omega + h) - drag(wl.omega - h)) / (2 * h)
+    assert gO == pytest.approx(fd, rel=1e-5), (gO, fd)
+
+
+def test_face_steady_drag_adjoint():
+    """dDrag/domega of the converged channel past a sphere (velocity inlet,
+    pressure outlet) from the steady adjoint, against central differences of
+    converged FP64 runs."""
+    def converged(omega):
+        lat = _face_channel("regularized", omega=omega, shape=(20, 10, 10)).lattice("fp64")
+        lat.collide_and_stream(12000)
+        return lat
+
+    omega = 1.2
+    lat = converged(omega)
+    J, _, gO, _ = lat.adjoint_steady(iterations=6000, want_force=False, drag=DRAG_DIR)
+    _, _, gO2, _ = lat.adjoint_steady(iterations=12000, want_force=False, drag=DRAG_DIR)
+    assert gO2 == pytest.approx(gO, rel=1e-8)
+
+    def drag(om):
+        J2, _, _, _ = converged(om).adjoint_steady(iterations=0, want_force=False, drag=DRAG_DIR)
+        return J2
+
+    h = 1e-5
+    fd = (drag(omega + h) - drag(omega - h)) / (2 * h)
+    assert gO == pytest.approx(fd, rel=1e-5), (gO, fd)
