@@ -397,6 +397,9 @@ def main():
     ap.add_argument("--permeability-n", type=int, default=384)
     ap.add_argument("--permeability-steps", type=int, default=20000)
     ap.add_argument("--permeability-adjoint", type=int, nargs="+", default=[3000])
+    ap.add_argument("--drag-gradient", action="store_true",
+                    help="run only the channel-past-a-sphere drag-gradient study (256x128x128, 10000 steps)")
+    ap.add_argument("--drag-gradient-steps", type=int, default=10000)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -406,6 +409,13 @@ def main():
         ctx = Context(dist_env()[2])
         r = taylor_green_study(n=args.accuracy_n, steps=args.accuracy_steps, every=500, slab=8, ctx=ctx)
         print(json.dumps({"study": "taylor_green_storage_forms", **r}))
+        return
+    if args.drag_gradient:
+        from palabos_gb300 import Context
+        from palabos_gb300.accuracy import drag_gradient_study
+        ctx = Context(dist_env()[2])
+        r = drag_gradient_study(steps=args.drag_gradient_steps, ctx=ctx)
+        print(json.dumps({"study": "channel_sphere_drag_gradient", **r}))
         return
     if args.permeability:
         from palabos_gb300 import Context

@@ -127,3 +127,46 @@ def permeability_study(n=384, steps=20000, forms=("fp32", "bf16"), every=1000, a
     for p in forms:
         out["forms"][p]["k_rel_err"] = abs(out["forms"][p]["k"] - k64) / abs(k64)
     return out
+
+
+def drag_gradient_study(shape=(256, 128, 128), steps=10000, precisions=("fp64", "fp32"), fd_h=1e-4, ctx=None):
+    """dD_x/domega of the channel past a sphere (regularized parabolic inlet,
+    regularized pressure outlet, bounce-back walls, momentum-exchange sphere
+    r = shape[1] / 8, omega 1.8): D the momentum-exchange drag of the state
+    after `steps` steps from rest, through the checkpointed adjoint (the
+    checkpoint interval the library picks from free memory), against a
+    central difference of two FP64 runs.  Reports the cost of the recording
+    and of the backward sweep per step against a plain step."""
+    from . import workloads
+    nx, ny, nz = shape
+    wl = workloads.channel_sphere(shape, (nx / 4, ny / 2, nz / 2), ny / 8, 0.05, 1.8)
+    e = np.array([1.0, 0.0, 0.0])
+    out = {"shape": list(shape), "steps": steps, "omega": wl.omega, "forms": {}}
+    for p in precisions:
+        lat = wl.lattice(p, ctx)
+        f0 = lat.receive()
+        fwd_ms = lat.time_steps(100) / 100
+        lat.send(f0)
+        t0 = time.perf_counter()
+        K = lat.adjoint_forward(steps, 0)
+        rec_s = time.perf_counter() - t0
+        J, _, g, ms = lat.adjoint_backward(drag=e, want_force=False)
+        out["forms"][p] = {"drag_x": J, "d_drag_x_domega": g, "K": K,
+                           "forward_step_ms": round(fwd_ms, 4), "record_ms_per_step": round(rec_s * 1e3 / steps, 4),
+                           "backward_ms_per_step": round(ms / steps, 4),
+                           "backward_over_forward": round(ms / steps / fwd_ms, 3)}
+        lat.close()
+    if fd_h:
+        vals = []
+        for om in (wl.omega + fd_h, wl.omega - fd_h):
+            w2 = workloads.channel_sphere(shape, (nx / 4, ny / 2, nz / 2), ny / 8, 0.05, om)
+            lat = w2.lattice("fp64", ctx)
+            lat.collide_and_stream(steps)
+            J2, _, _, _ = lat.adjoint_steady(iterations=0, want_force=False, drag=e)
+            vals.append(J2)
+            lat.close()
+        fd = (vals[0] - vals[1]) / (2 * fd_h)
+        out["fd_fp64"] = {"h": fd_h, "d_drag_x_domega": fd}
+        for p in precisions:
+            out["forms"][p]["rel_err_vs_fd"] = abs(out["forms"][p]["d_drag_x_domega"] - fd) / abs(fd)
+    return out

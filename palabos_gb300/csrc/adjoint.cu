@@ -33,27 +33,44 @@ namespace plbgpu {
 
 // ---------------------------------------------------------------- dual numbers
 
-struct Dual {
-    double v, d;
-    __host__ __device__ Dual() : v(0.), d(0.) {}
-    __host__ __device__ Dual(double x) : v(x), d(0.) {}
-    __host__ __device__ Dual(double x, double y) : v(x), d(y) {}
-    __host__ __device__ Dual& operator+=(const Dual& o) { v += o.v; d += o.d; return *this; }
-    __host__ __device__ Dual& operator-=(const Dual& o) { v -= o.v; d -= o.d; return *this; }
-    __host__ __device__ Dual& operator*=(const Dual& o) { d = d * o.v + v * o.d; v *= o.v; return *this; }
+template <typename T>
+struct DualT {
+    T v, d;
+    __host__ __device__ DualT() : v(0), d(0) {}
+    __host__ __device__ DualT(double x) : v((T)x), d(0) {}
+    __host__ __device__ DualT(double x, double y) : v((T)x), d((T)y) {}
+    __host__ __device__ DualT& operator+=(const DualT& o) { v += o.v; d += o.d; return *this; }
+    __host__ __device__ DualT& operator-=(const DualT& o) { v -= o.v; d -= o.d; return *this; }
+    __host__ __device__ DualT& operator*=(const DualT& o) { d = d * o.v + v * o.d; v *= o.v; return *this; }
 };
-__host__ __device__ inline Dual operator+(Dual a, const Dual& b) { return a += b; }
-__host__ __device__ inline Dual operator-(Dual a, const Dual& b) { return a -= b; }
-__host__ __device__ inline Dual operator*(Dual a, const Dual& b) { return a *= b; }
-__host__ __device__ inline Dual operator-(const Dual& a) { return Dual(-a.v, -a.d); }
-__host__ __device__ inline Dual operator/(const Dual& a, const Dual& b) {
-    const double q = a.v / b.v;
-    return Dual(q, (a.d - q * b.d) / b.v);
+template <typename T>
+__host__ __device__ inline DualT<T> operator+(DualT<T> a, const DualT<T>& b) { return a += b; }
+template <typename T>
+__host__ __device__ inline DualT<T> operator-(DualT<T> a, const DualT<T>& b) { return a -= b; }
+template <typename T>
+__host__ __device__ inline DualT<T> operator*(DualT<T> a, const DualT<T>& b) { return a *= b; }
+template <typename T>
+__host__ __device__ inline DualT<T> operator-(const DualT<T>& a) { return DualT<T>(-a.v, -a.d); }
+template <typename T>
+__host__ __device__ inline DualT<T> operator/(const DualT<T>& a, const DualT<T>& b) {
+    const T q = a.v / b.v;
+    DualT<T> r;
+    r.v = q;
+    r.d = (a.d - q * b.d) / b.v;
+    return r;
 }
-__device__ inline Dual invRhoOf(Dual rhoBar) {
-    const double r = 1.0 / (rhoBar.v + 1.0);
-    return Dual(r, -rhoBar.d * r * r);
+template <typename T>
+__device__ inline DualT<T> invRhoOf(DualT<T> rhoBar) {
+    const T r = (T)1 / (rhoBar.v + (T)1);
+    DualT<T> out;
+    out.v = r;
+    out.d = -rhoBar.d * r * r;
+    return out;
 }
+// FP64 duals (the tangent run, the FP64 adjoint) and FP32 duals (the FP32
+// adjoint's face cells, on the FP32 pipe).
+using Dual = DualT<double>;
+using DualF = DualT<float>;
 
 template <typename R> __device__ inline double valueOf(const R& x) { return (double)x; }
 template <> __device__ inline double valueOf<Dual>(const Dual& x) { return x.v; }
@@ -469,22 +486,30 @@ __global__ void faceAdjointKernel(DevLattice L, const R* f, const R* lamIn, R* l
         const int z = (int)(idx % L.nz), y = (int)((idx / L.nz) % L.ny), x = (int)(idx / ((long long)L.ny * L.nz));
         const int k = L.flags[idx];
         const Neighbourhood nb = neighbourhood(L, x, y, z);
-        double mu[19], fc[19];
-        mu[0] = (double)lamIn[idx];
+        using FD = DualT<R>;   // the form's own arithmetic
+        R mu[19], fc[19];
+        mu[0] = lamIn[idx];
         for (int i = 1; i < 19; ++i) {
             long long off;
-            mu[i] = (double)(nb.move(i, +1, off) ? lamIn[i * L.n + idx + off] : lamIn[opp(i) * L.n + idx]);
+            mu[i] = nb.move(i, +1, off) ? lamIn[i * L.n + idx + off] : lamIn[opp(i) * L.n + idx];
         }
-        for (int i = 0; i < 19; ++i) fc[i] = (double)f[i * L.n + idx];
+        for (int i = 0; i < 19; ++i) fc[i] = f[i * L.n + idx];
+        // the completion overwrites the populations that entered from outside
+        // (c[DIR] = -ORI) without reading them: their rows of J^T are zero
+        const int sub = (k - K_REGVEL) % 6, fdir = sub >> 1, fori = (sub & 1) ? 1 : -1;
         for (int dir = 0; dir <= 19; ++dir) {   // 0..18: population dir; 19: omega
-            Dual g[19], F[3];
-            for (int i = 0; i < 19; ++i) g[i] = Dual(fc[i], i == dir ? 1. : 0.);
-            if (pending) completeIfFace<Dual>(L, idx, k, g);
-            adjCollide<Dual>(k, g, F, bgkConsts<Dual>(Dual(omega, dir == 19 ? 1. : 0.)), Dual(0.));
-            double s = 0.;
+            if (dir < 19 && pending && cdir(dir, fdir) == -fori) {
+                lamOut[dir * L.n + idx] = R(0);
+                continue;
+            }
+            FD g[19], F[3];
+            for (int i = 0; i < 19; ++i) g[i] = FD(fc[i], i == dir ? 1. : 0.);
+            if (pending) completeIfFace<FD>(L, idx, k, g);
+            adjCollide<FD>(k, g, F, bgkConsts<FD>(FD(omega, dir == 19 ? 1. : 0.)), FD(0.));
+            R s = R(0);
             for (int i = 0; i < 19; ++i) s += mu[i] * g[i].d;
-            if (dir < 19) lamOut[dir * L.n + idx] = (R)s;
-            else go = s;
+            if (dir < 19) lamOut[dir * L.n + idx] = s;
+            else go = (double)s;
         }
     }
     blockAdd(go, acc->gOmega);

@@ -470,3 +470,16 @@ def test_face_steady_drag_adjoint():
     h = 1e-5
     fd = (drag(omega + h) - drag(omega - h)) / (2 * h)
     assert gO == pytest.approx(fd, rel=1e-5), (gO, fd)
+
+
+def test_face_adjoint_fp32_tracks_fp64():
+    wl = _face_channel("regularized")
+    g = {}
+    for prec in ("fp64", "fp32"):
+        lat = wl.lattice(prec)
+        lat.collide_and_stream(3)
+        lat.adjoint_forward(30, 6)
+        J, _, gO, _ = lat.adjoint_backward(drag=DRAG_DIR, want_force=False)
+        g[prec] = (J, gO)
+    assert g["fp32"][0] == pytest.approx(g["fp64"][0], rel=1e-4)
+    assert g["fp32"][1] == pytest.approx(g["fp64"][1], rel=1e-3)
