@@ -282,10 +282,32 @@ int plbgpu_load_binary_block(plbgpu_ctx* ctx, int handle, int what, const char* 
  * descriptor, cell size, bounding box, components, byte offsets, data file).
  * Save writes one component, the whole domain; load accepts any number of
  * components (the reference writes one per block) with a bounding box of the
- * domain's size.  Static content only: a state saved with dynamic content
- * (dynamics objects) is refused. */
+ * domain's size.  Loading a lattice state saved with dynamic content takes its
+ * populations (and force) only, as load(plb, block, false) does; a field's
+ * records are the same with or without dynamic content. */
 int plbgpu_save_state(plbgpu_ctx* ctx, int handle, int what, const char* base);
 int plbgpu_load_state(plbgpu_ctx* ctx, int handle, int what, const char* plb_path);
+
+/* parallelIO::save(lattice, base, true) / parallelIO::load(plb, lattice, true)
+ * -- the states with dynamic content, parallelIO::save's default
+ * (io/multiBlockWriter3D.h:42-43, atomicBlock/blockLattice3D.hh:703-722,
+ * 812-845): in front of every cell's static values, its serialized dynamics
+ * chain (class id, then the parameters: omega, 1/rho0 of incompressible BGK,
+ * the wall density, the momentum-exchange fluid directions, a face's stored
+ * velocity or rho-bar around its BGK base), and in <base>.plb a DynamicsDict
+ * mapping the ids to the dynamics names.  what: PLBGPU_BLOCK_LATTICE or
+ * PLBGPU_BLOCK_FORCED_LATTICE.  Save writes one component; it refuses sparse
+ * domains (PLBGPU_ERR_STATE).  Load reads any number of components that cover
+ * the domain, then sets the cell kinds, the boundary values, the
+ * momentum-exchange directions, omega / rho0 / the wall density, and the
+ * populations, as the reference regenerates the dynamics objects.  A state
+ * whose cells need more than the domain holds -- dynamics without a GPU kind,
+ * several omegas, rho0s or wall densities, a stored-velocity cell off the
+ * domain's edges and corners -- is refused (PLBGPU_ERR_ARG) before anything
+ * changes.  Data processors listed in the description are neither written
+ * nor read: the domain's own boundary handling follows its kinds. */
+int plbgpu_save_state_dynamic(plbgpu_ctx* ctx, int handle, int what, const char* base);
+int plbgpu_load_state_dynamic(plbgpu_ctx* ctx, int handle, int what, const char* plb_path);
 
 /* ------------------------------------------------------------ voxelizer */
 

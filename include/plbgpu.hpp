@@ -197,6 +197,25 @@ public:
         return u;
     }
 
+    // Checkpoints in the reference's formats: saveBinaryBlock / loadBinaryBlock
+    // (io/serializerIO_3D.cpp:37-60) and parallelIO::save / load, with or
+    // without dynamic content (io/multiBlockWriter3D.cpp:201-213,
+    // io/multiBlockReader3D.cpp:261-270).  `what` is a PLBGPU_BLOCK_* kind.
+    void saveBinaryBlock(const std::string& path, int what = PLBGPU_BLOCK_LATTICE, bool enforceUint = false) {
+        ctx_.check(plbgpu_save_binary_block(ctx_.get(), h_, what, path.c_str(), enforceUint));
+    }
+    void loadBinaryBlock(const std::string& path, int what = PLBGPU_BLOCK_LATTICE, bool enforceUint = false) {
+        ctx_.check(plbgpu_load_binary_block(ctx_.get(), h_, what, path.c_str(), enforceUint));
+    }
+    void saveState(const std::string& base, bool dynamicContent = true, int what = PLBGPU_BLOCK_LATTICE) {
+        ctx_.check(dynamicContent ? plbgpu_save_state_dynamic(ctx_.get(), h_, what, base.c_str())
+                                  : plbgpu_save_state(ctx_.get(), h_, what, base.c_str()));
+    }
+    void loadState(const std::string& plb, bool dynamicContent = true, int what = PLBGPU_BLOCK_LATTICE) {
+        ctx_.check(dynamicContent ? plbgpu_load_state_dynamic(ctx_.get(), h_, what, plb.c_str())
+                                  : plbgpu_load_state(ctx_.get(), h_, what, plb.c_str()));
+    }
+
 private:
     Context& ctx_;
     int nx_, ny_, nz_;

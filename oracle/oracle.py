@@ -8,6 +8,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import struct
 import subprocess
 
 import numpy as np
@@ -240,3 +241,191 @@ def state_files(records, shape, cell_dim, family, descriptor, dat_name):
               f"        <Offsets> {len(data)} </Offsets>", "    </Data>", "</Block3D>", ""]
     return "\n".join(lines), data
 
+
+
+# ---------------------------------------------------------------- states with dynamic content
+
+_BASIC_DYNAMICS = ["BGK", "BGK_ExternalForce_Guo", "BGK_Incompressible", "BounceBack", "MomentumExchangeBounceBack",
+                   "NoDynamics"]
+_FACE_FAMILIES = ["Boundary_RegularizedVelocity", "Boundary_RegularizedDensity", "Boundary_ZouHeVelocity",
+                  "Boundary_ZouHePressure"]
+_K_FACE, _K_EDGE, _K_END = 6, 30, 50
+_K_INCBGK, _K_BB, _K_MEBB, _K_NODYN = 2, 3, 4, 5
+
+
+def dynamics_name(kind):
+    """Registry name of the dynamics class of a cell kind (the names of
+    meta::dynamicsRegistration, e.g. regularizedBoundaryDynamics.hh:44-47)."""
+    if kind < _K_FACE:
+        return _BASIC_DYNAMICS[kind]
+    if kind < _K_EDGE:
+        r = kind - _K_FACE
+        face = r % 6
+        return f"{_FACE_FAMILIES[r // 6]}_{face // 2}_{1 if face % 2 else -1}"
+    return "Boundary_StoreVelocity"
+
+
+def _is_density_kind(kind):
+    return 12 <= kind < 18 or 24 <= kind < 30
+
+
+def _d(v):
+    return (8, struct.pack("<d", v))
+
+
+def _cell_values(kind, bc, mask, omega, rho0, bb_rho):
+    """What each dynamics of the cell's chain serializes, outermost first
+    (core/dynamics.hh:119-122, 445-450, 770-773, 955-958;
+    boundaryCondition/bounceBackModels.hh:75-84; boundaryDynamics.hh:238-242,
+    315-321): a list of (value size, bytes) per dynamics."""
+    if kind in (0, 1):
+        return [[_d(omega)]]
+    if kind == _K_INCBGK:
+        return [[_d(omega), _d(1.0 / rho0)]]
+    if kind in (_K_BB, _K_NODYN):
+        return [[_d(bb_rho)]]
+    if kind == _K_MEBB:
+        dirs = [i for i in range(19) if (int(mask) >> i) & 1]
+        return [[_d(bb_rho), (4, struct.pack("<i", len(dirs)))] + [(8, struct.pack("<q", i)) for i in dirs]
+                + [(8, struct.pack("<q", a)) for a in range(3)]]
+    if _is_density_kind(kind):
+        stored = [_d(float(bc[0]) - 1.0)]
+    else:
+        stored = [_d(float(bc[a])) for a in range(3)]
+    return [stored + [(1, bytes([1 if kind >= _K_EDGE else 0]))], [_d(omega)]]
+
+
+def _chain_bytes(ids, values):
+    """HierarchicSerializer (core/hierarchicSerializer.h:152-230): numDynamics,
+    then per dynamics its id, its number of values and runs of values of one
+    size (size, count, values)."""
+    out = bytearray(struct.pack("<i", len(ids)))
+    for did, vals in zip(ids, values):
+        out += struct.pack("<ii", did, len(vals))
+        i = 0
+        while i < len(vals):
+            j = i
+            while j < len(vals) and vals[j][0] == vals[i][0]:
+                j += 1
+            out += struct.pack("<ii", vals[i][0], j - i)
+            for _, b in vals[i:j]:
+                out += b
+            i = j
+    return bytes(out)
+
+
+def _own_ids(kind):
+    return 31 if kind >= _K_EDGE else kind + 1
+
+
+def dynamic_state_files(kinds, bcval, masks, records, cell_dim, descriptor, dat_name, omega, rho0, bb_rho,
+                        ids=None):
+    """parallelIO::save(lattice, base, true) of a lattice as one component:
+    every cell's dynamics chain, then its `cell_dim` static values
+    (atomicBlock/blockLattice3D.hh:703-722), and a description whose
+    DynamicsDict maps the ids to names (io/multiBlockWriter3D.cpp:92-110).
+    ids: name -> id (default: the library's own ids, kind + 1 and 31 for
+    stored-velocity cells).  Returns (plb text, dat bytes)."""
+    shape = kinds.shape
+    recs = np.ascontiguousarray(records, dtype="<f8").reshape(-1, cell_dim)
+    kf = kinds.reshape(-1)
+    bf = np.asarray(bcval, dtype=np.float64).reshape(-1, 3)
+    mf = np.asarray(masks).reshape(-1) if masks is not None else np.zeros(kf.size, np.uint32)
+    idof = (lambda name, k: ids[name]) if ids else (lambda name, k: 1 if name == "BGK" else _own_ids(k))
+    out = bytearray()
+    dict_ = {}
+    for c in range(kf.size):
+        k = int(kf[c])
+        names = [dynamics_name(k)] + (["BGK"] if k >= _K_FACE else [])
+        chain_ids = [idof(names[0], k)] + ([idof("BGK", 0)] if k >= _K_FACE else [])
+        for nm, i in zip(names, chain_ids):
+            dict_[nm] = i
+        out += _chain_bytes(chain_ids, _cell_values(k, bf[c], mf[c], omega, rho0, bb_rho))
+        out += recs[c].tobytes()
+    plb, _ = state_files(np.zeros((0, cell_dim)), shape, cell_dim, "BlockLattice3D", descriptor, dat_name)
+    plb = plb.replace("<dynamicContent> False </dynamicContent>", "<dynamicContent> True </dynamicContent>")
+    plb = plb.replace("<Offsets> 0 </Offsets>", f"<Offsets> {len(out)} </Offsets>")
+    block = ["        <DynamicsDict>"] + [f"            <{n}> {dict_[n]} </{n}>" for n in sorted(dict_)] + \
+            ["        </DynamicsDict>"]
+    plb = plb.replace("    </Data>", "\n".join(block) + "\n    </Data>")
+    return plb, bytes(out)
+
+
+def _surface_kind(x, y, z, shape):
+    side = [(-1 if q == 0 else (1 if q == n - 1 else 0)) for q, n in zip((x, y, z), shape)]
+    count = sum(s != 0 for s in side)
+    if count == 3:
+        return 42 + 4 * (side[0] > 0) + 2 * (side[1] > 0) + (side[2] > 0)
+    if count == 2:
+        plane = [i for i in range(3) if side[i] == 0][0]
+        return _K_EDGE + 4 * plane + 2 * (side[(plane + 1) % 3] > 0) + (side[(plane + 2) % 3] > 0)
+    raise ValueError("a stored-velocity cell that is not on an edge or corner of the lattice")
+
+
+def read_dynamic_state(plb, dat, shape):
+    """Decode a lattice state with dynamic content (any number of components):
+    kinds, boundary values (velocity, or the density rho-bar + 1 in [..., 0]),
+    momentum-exchange fluid-direction masks, static records, and the sets of
+    omegas, 1/rho0s and wall densities the cells hold
+    (blockLattice3D.hh:812-845, hierarchicSerializer.h)."""
+    import re
+    cell_dim = int(re.search(r"<cellDim>([^<]*)</cellDim>", plb).group(1))
+    boxes = [tuple(map(int, m.split())) for m in re.findall(r"<Component[^>]*>([^<]*)</Component>", plb)]
+    offsets = list(map(int, re.search(r"<Offsets>([^<]*)</Offsets>", plb).group(1).split()))
+    dd = re.search(r"<DynamicsDict>(.*?)</DynamicsDict>", plb, re.S).group(1)
+    names = {int(v): n for n, v in re.findall(r"<([^/>]+)>\s*(-?\d+)\s*</\1>", dd)}
+    name_kind = {dynamics_name(k): k for k in range(_K_EDGE)}
+    nx, ny, nz = shape
+    kinds = np.full(shape, 255, np.uint8)
+    bc = np.zeros(shape + (3,))
+    masks = np.zeros(shape, np.uint32)
+    recs = np.zeros(shape + (cell_dim,))
+    omegas, inv_rho0s, rhos = set(), set(), set()
+    pos, start = 0, 0
+    for (x0, x1, y0, y1, z0, z1), end in zip(boxes, offsets):
+        for x in range(x0, x1 + 1):
+            for y in range(y0, y1 + 1):
+                for z in range(z0, z1 + 1):
+                    (nd,) = struct.unpack_from("<i", dat, pos)
+                    pos += 4
+                    chain = []
+                    for _ in range(nd):
+                        did, nv = struct.unpack_from("<ii", dat, pos)
+                        pos += 8
+                        vals = []
+                        while len(vals) < nv:
+                            size, count = struct.unpack_from("<ii", dat, pos)
+                            pos += 8
+                            vals += [dat[pos + r * size:pos + (r + 1) * size] for r in range(count)]
+                            pos += size * count
+                        chain.append((names[did], vals))
+                    top, v = chain[0]
+                    if top == "Boundary_StoreVelocity" or name_kind.get(top, -1) >= _K_FACE:
+                        k = _surface_kind(x, y, z, shape) if top == "Boundary_StoreVelocity" else name_kind[top]
+                        if _is_density_kind(k):
+                            bc[x, y, z, 0] = struct.unpack("<d", v[0])[0] + 1.0
+                        else:
+                            bc[x, y, z] = [struct.unpack("<d", v[a])[0] for a in range(3)]
+                        assert chain[1][0] == "BGK"
+                        omegas.add(struct.unpack("<d", chain[1][1][0])[0])
+                    else:
+                        k = name_kind[top]
+                        first = struct.unpack("<d", v[0])[0]
+                        if k in (0, 1):
+                            omegas.add(first)
+                        elif k == _K_INCBGK:
+                            omegas.add(first)
+                            inv_rho0s.add(struct.unpack("<d", v[1])[0])
+                        else:
+                            rhos.add(first)
+                        if k == _K_MEBB:
+                            (n,) = struct.unpack("<i", v[1])
+                            for b in v[2:2 + n]:
+                                masks[x, y, z] |= np.uint32(1 << struct.unpack("<q", b)[0])
+                    kinds[x, y, z] = k
+                    recs[x, y, z] = np.frombuffer(dat, "<f8", cell_dim, pos)
+                    pos += 8 * cell_dim
+        assert pos == end, (pos, end)
+        start = end
+    return dict(kinds=kinds, bc=bc, masks=masks, records=recs, omegas=omegas, inv_rho0s=inv_rho0s, rhos=rhos,
+                names=names)

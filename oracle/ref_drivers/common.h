@@ -67,8 +67,10 @@ enum {
                              // <result>.lattice / .density / .velocity
     OPT_SPARSE = 8,          // build the lattice on computeSparseManagement of the
                              // given int field over the regular block distribution
-    OPT_SAVE_STATE = 16      // after the run, parallelIO::save(lattice, <base>_state, false)
+    OPT_SAVE_STATE = 16,     // after the run, parallelIO::save(lattice, <base>_state, false)
                              // with <base> the result path without its extension
+    OPT_SAVE_DYNAMIC_STATE = 32  // after the run, parallelIO::save(lattice, <base>_dstate, true):
+                                 // the state with dynamic content (serialized dynamics)
 };
 
 struct Case {

@@ -292,6 +292,9 @@ int run(const Case& c, const char* outPath) {
     // With PLB_LOAD_STATE=<base>: the populations come from a saved state
     // (parallelIO::load of <base>.plb / <base>.dat, static content).
     if (const char* lpath = std::getenv("PLB_LOAD_STATE")) parallelIO::load(lpath, lat, false);
+    // With PLB_LOAD_DYNAMIC_STATE=<plb>: parallelIO::load(plb, lattice, true) --
+    // the dynamics objects are regenerated from the state, then the populations.
+    if (const char* lpath = std::getenv("PLB_LOAD_DYNAMIC_STATE")) parallelIO::load(lpath, lat, true);
 
     std::vector<double> fInit, fFinal;
     dumpPopulations(lat, c, fInit);
@@ -373,6 +376,12 @@ int run(const Case& c, const char* outPath) {
         const size_t slash = base.rfind('/'), dot = base.rfind('.');
         if (dot != std::string::npos && (slash == std::string::npos || dot > slash)) base.erase(dot);
         parallelIO::save(lat, base + "_state", false);
+    }
+    if (c.options & OPT_SAVE_DYNAMIC_STATE) {   // <result without extension>_dstate.plb / .dat
+        std::string base(outPath);
+        const size_t slash = base.rfind('/'), dot = base.rfind('.');
+        if (dot != std::string::npos && (slash == std::string::npos || dot > slash)) base.erase(dot);
+        parallelIO::save(lat, base + "_dstate", true);
     }
     if (c.options & OPT_SAVE_BINARY) {
         std::string base(outPath);

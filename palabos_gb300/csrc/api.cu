@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "../../include/plbgpu.h"
+#include "dynstate.h"
 #include "launch.h"
 
 using namespace plbgpu;
@@ -1586,6 +1587,41 @@ bool parseLongs(const std::string& text, std::vector<long long>& out) {
     return true;
 }
 
+// The description <base>.plb of a one-component state, in the layout of the
+// reference's XML writer (io/multiBlockWriter3D.cpp:53-137,
+// libraryInterfaces/TINYXML_xmlIO.hh:229-272).  dict: the DynamicsDict of a
+// state with dynamic content (name -> id, in name order), null for static
+// content.
+std::string stateDescription(const Domain* d, int what, const std::string& datName, unsigned long long bytes,
+                             const std::map<std::string, int>* dict) {
+    const int w = blockWidth(what);
+    const char *family, *descriptor;
+    stateTypeInfo(what, &family, &descriptor);
+    char buf[512];
+    std::string x = "<?xml version=\"1.0\" ?>\n<Block3D>\n    <General>\n";
+    x += std::string("        <Family> ") + family + " </Family>\n        <Datatype> double </Datatype>\n";
+    if (descriptor) x += std::string("        <Descriptor> ") + descriptor + " </Descriptor>\n";
+    snprintf(buf, sizeof(buf),
+             "        <cellDim> %d </cellDim>\n        <dynamicContent> %s </dynamicContent>\n"
+             "        <globalId> 0 </globalId>\n    </General>\n    <Structure>\n"
+             "        <BoundingBox> 0 %d 0 %d 0 %d </BoundingBox>\n        <EnvelopeWidth> 1 </EnvelopeWidth>\n"
+             "        <GridLevel> 0 </GridLevel>\n        <NumComponents> 1 </NumComponents>\n    </Structure>\n"
+             "    <Data>\n",
+             w, dict ? "True" : "False", d->nx - 1, d->ny - 1, d->nz - 1);
+    x += buf;
+    x += "        <File> " + datName + " </File>\n";
+    snprintf(buf, sizeof(buf), "        <Component> 0 %d 0 %d 0 %d </Component>\n        <Offsets> %llu </Offsets>\n",
+             d->nx - 1, d->ny - 1, d->nz - 1, bytes);
+    x += buf;
+    if (dict && !dict->empty()) {
+        x += "        <DynamicsDict>\n";
+        for (const auto& e : *dict) x += "            <" + e.first + "> " + std::to_string(e.second) + " </" + e.first + ">\n";
+        x += "        </DynamicsDict>\n";
+    }
+    x += "    </Data>\n</Block3D>\n";
+    return x;
+}
+
 }  // namespace
 
 int plbgpu_save_state(plbgpu_ctx* c, int h, int what, const char* base) {
@@ -1620,28 +1656,7 @@ int plbgpu_save_state(plbgpu_ctx* c, int h, int what, const char* base) {
         }
         if (fflush(fc.f) != 0) return fail(c, PLBGPU_ERR_ARG, "write to %s failed", datName.c_str());
     }
-    // The description, in the layout of the reference's XML writer
-    // (io/multiBlockWriter3D.cpp:53-137, libraryInterfaces/TINYXML_xmlIO.hh:229-272).
-    const char *family, *descriptor;
-    stateTypeInfo(what, &family, &descriptor);
-    char buf[512];
-    std::string x = "<?xml version=\"1.0\" ?>\n<Block3D>\n    <General>\n";
-    x += std::string("        <Family> ") + family + " </Family>\n        <Datatype> double </Datatype>\n";
-    if (descriptor) x += std::string("        <Descriptor> ") + descriptor + " </Descriptor>\n";
-    snprintf(buf, sizeof(buf),
-             "        <cellDim> %d </cellDim>\n        <dynamicContent> False </dynamicContent>\n"
-             "        <globalId> 0 </globalId>\n    </General>\n    <Structure>\n"
-             "        <BoundingBox> 0 %d 0 %d 0 %d </BoundingBox>\n        <EnvelopeWidth> 1 </EnvelopeWidth>\n"
-             "        <GridLevel> 0 </GridLevel>\n        <NumComponents> 1 </NumComponents>\n    </Structure>\n"
-             "    <Data>\n",
-             w, d->nx - 1, d->ny - 1, d->nz - 1);
-    x += buf;
-    x += "        <File> " + datName + " </File>\n";
-    snprintf(buf, sizeof(buf),
-             "        <Component> 0 %d 0 %d 0 %d </Component>\n        <Offsets> %llu </Offsets>\n    </Data>\n"
-             "</Block3D>\n",
-             d->nx - 1, d->ny - 1, d->nz - 1, (unsigned long long)d->n * w * sizeof(double));
-    x += buf;
+    const std::string x = stateDescription(d, what, datName, (unsigned long long)d->n * w * sizeof(double), nullptr);
     FileCloser fp{fopen(plbName.c_str(), "wb")};
     if (!fp.f) return fail(c, PLBGPU_ERR_ARG, "cannot open %s for writing", plbName.c_str());
     if (fwrite(x.data(), 1, x.size(), fp.f) != x.size() || fflush(fp.f) != 0)
@@ -1649,15 +1664,20 @@ int plbgpu_save_state(plbgpu_ctx* c, int h, int what, const char* base) {
     return PLBGPU_OK;
 }
 
-int plbgpu_load_state(plbgpu_ctx* c, int h, int what, const char* plb) {
-    Domain* d;
-    int rc = lookup(c, h, &d);
-    if (rc) return rc;
-    const int w = blockWidth(what);
-    if (!w) return fail(c, PLBGPU_ERR_ARG, "unknown block kind %d", what);
-    if (what == PLBGPU_BLOCK_DENSITY || what == PLBGPU_BLOCK_VELOCITY)
-        return fail(c, PLBGPU_ERR_ARG, "density and velocity blocks are derived data and cannot be loaded");
-    if (!plb) return fail(c, PLBGPU_ERR_ARG, "null path");
+namespace {
+
+// What <base>.plb says (readXmlSpec, io/multiBlockReader3D.cpp:135-212, and
+// createDynamicsForeignIds3D, :67-90); component boxes relative to the
+// bounding box, whose size must be the domain's.
+struct StateSpec {
+    bool dynamic = false;
+    std::vector<Box> comps;
+    std::vector<long long> offsets;
+    std::string datName;
+    std::map<int, std::string> names;   // DynamicsDict: id -> dynamics name
+};
+
+int parseStateSpec(plbgpu_ctx* c, const Domain* d, const char* plb, int w, StateSpec& s) {
     std::string doc;
     {
         FileCloser fc{fopen(plb, "rb")};
@@ -1666,22 +1686,21 @@ int plbgpu_load_state(plbgpu_ctx* c, int h, int what, const char* plb) {
         size_t got;
         while ((got = fread(chunk, 1, sizeof(chunk), fc.f)) > 0) doc.append(chunk, got);
     }
-    // readXmlSpec (io/multiBlockReader3D.cpp:135-212)
     std::string t;
     std::vector<long long> v;
     if (xmlElement(doc, "cellDim", 0, t, nullptr) == std::string::npos || !parseLongs(t, v) || v.size() != 1)
         return fail(c, PLBGPU_ERR_ARG, "%s: no cellDim", plb);
     if (v[0] != w) return fail(c, PLBGPU_ERR_ARG, "%s: cells of %lld values, this block kind has %d", plb, v[0], w);
-    if (xmlElement(doc, "dynamicContent", 0, t, nullptr) == std::string::npos ||
-        t.find("False") == std::string::npos)
-        return fail(c, PLBGPU_ERR_ARG, "%s: states with dynamic content are not supported", plb);
-    std::vector<long long> bb, offsets;
+    if (xmlElement(doc, "dynamicContent", 0, t, nullptr) == std::string::npos)
+        return fail(c, PLBGPU_ERR_ARG, "%s: no dynamicContent", plb);
+    s.dynamic = t.find("True") != std::string::npos;
+    std::vector<long long> bb;
     if (xmlElement(doc, "BoundingBox", 0, t, nullptr) == std::string::npos || !parseLongs(t, bb) || bb.size() != 6)
         return fail(c, PLBGPU_ERR_ARG, "%s: no bounding box", plb);
     if (bb[1] - bb[0] + 1 != d->nx || bb[3] - bb[2] + 1 != d->ny || bb[5] - bb[4] + 1 != d->nz)
         return fail(c, PLBGPU_ERR_ARG, "%s: a %lldx%lldx%lld block, the domain is %dx%dx%d", plb, bb[1] - bb[0] + 1,
                     bb[3] - bb[2] + 1, bb[5] - bb[4] + 1, d->nx, d->ny, d->nz);
-    if (xmlElement(doc, "Offsets", 0, t, nullptr) == std::string::npos || !parseLongs(t, offsets))
+    if (xmlElement(doc, "Offsets", 0, t, nullptr) == std::string::npos || !parseLongs(t, s.offsets))
         return fail(c, PLBGPU_ERR_ARG, "%s: no offsets", plb);
     std::string datName;
     if (xmlElement(doc, "File", 0, datName, nullptr) == std::string::npos)
@@ -1694,7 +1713,7 @@ int plbgpu_load_state(plbgpu_ctx* c, int h, int what, const char* plb) {
         if (slash != std::string::npos) datName = p.substr(0, slash + 1) + datName;
     }
     if (datName.size() < 4 || datName.compare(datName.size() - 4, 4, ".dat") != 0) datName += ".dat";
-    std::vector<Box> comps;
+    s.datName = datName;
     size_t pos = 0, next = 0;
     while (xmlElement(doc, "Component", pos, t, &next) != std::string::npos) {
         if (!parseLongs(t, v) || v.size() != 6) return fail(c, PLBGPU_ERR_ARG, "%s: bad component", plb);
@@ -1703,23 +1722,134 @@ int plbgpu_load_state(plbgpu_ctx* c, int h, int what, const char* plb) {
         if (b.x0 < 0 || b.y0 < 0 || b.z0 < 0 || b.x1 >= d->nx || b.y1 >= d->ny || b.z1 >= d->nz || b.x0 > b.x1 ||
             b.y0 > b.y1 || b.z0 > b.z1)
             return fail(c, PLBGPU_ERR_ARG, "%s: component outside the bounding box", plb);
-        comps.push_back(b);
+        s.comps.push_back(b);
         pos = next;
     }
-    if (comps.size() != offsets.size() || comps.empty())
-        return fail(c, PLBGPU_ERR_ARG, "%s: %zu components, %zu offsets", plb, comps.size(), offsets.size());
-    FileCloser fd{fopen(datName.c_str(), "rb")};
-    if (!fd.f) return fail(c, PLBGPU_ERR_ARG, "cannot open %s", datName.c_str());
+    if (s.comps.size() != s.offsets.size() || s.comps.empty())
+        return fail(c, PLBGPU_ERR_ARG, "%s: %zu components, %zu offsets", plb, s.comps.size(), s.offsets.size());
+    // <DynamicsDict> <name> id </name> ... </DynamicsDict>
+    if (xmlElement(doc, "DynamicsDict", 0, t, nullptr) != std::string::npos) {
+        size_t p = 0;
+        while ((p = t.find('<', p)) != std::string::npos) {
+            const size_t gt = t.find('>', p);
+            if (gt == std::string::npos) return fail(c, PLBGPU_ERR_ARG, "%s: bad DynamicsDict", plb);
+            const std::string name = t.substr(p + 1, gt - p - 1);
+            const size_t close = t.find("</" + name + ">", gt);
+            if (close == std::string::npos || !parseLongs(t.substr(gt + 1, close - gt - 1), v) || v.size() != 1)
+                return fail(c, PLBGPU_ERR_ARG, "%s: bad DynamicsDict entry %s", plb, name.c_str());
+            s.names[(int)v[0]] = name;
+            p = close + name.size() + 3;
+        }
+    }
+    return PLBGPU_OK;
+}
+
+// The cells of a lattice state with dynamic content: per component, its cells
+// x-major, each one's dynamics chain then its w static values
+// (blockLattice3D.hh:703-722).  rec receives the static values over the whole
+// domain (x-major, w per cell); cells, when given, each cell's dynamics.
+int readDynamicCells(plbgpu_ctx* c, const Domain* d, const StateSpec& s, int w, std::vector<double>& rec,
+                     std::vector<plbgpu_dyn::Cell>* cells) {
+    FileCloser fd{fopen(s.datName.c_str(), "rb")};
+    if (!fd.f) return fail(c, PLBGPU_ERR_ARG, "cannot open %s", s.datName.c_str());
+    rec.assign((size_t)d->n * w, 0.0);
+    std::vector<uint8_t> seen((size_t)d->n, 0);
+    if (cells) cells->assign((size_t)d->n, plbgpu_dyn::Cell());
+    std::vector<char> buf;
+    long long begin = 0;
+    for (size_t i = 0; i < s.comps.size(); ++i) {
+        const Box& cb = s.comps[i];
+        if (s.offsets[i] < begin) return fail(c, PLBGPU_ERR_ARG, "%s: offsets out of order", s.datName.c_str());
+        buf.resize((size_t)(s.offsets[i] - begin));
+        if (fseek(fd.f, (long)begin, SEEK_SET) != 0 || fread(buf.data(), 1, buf.size(), fd.f) != buf.size())
+            return fail(c, PLBGPU_ERR_ARG, "%s: truncated data", s.datName.c_str());
+        size_t pos = 0;
+        for (int x = cb.x0; x <= cb.x1; ++x)
+            for (int y = cb.y0; y <= cb.y1; ++y)
+                for (int z = cb.z0; z <= cb.z1; ++z) {
+                    const size_t idx = ((size_t)x * d->ny + y) * d->nz + z;
+                    plbgpu_dyn::Cell cell;
+                    const std::string err =
+                        plbgpu_dyn::readCell(buf.data(), buf.size(), pos, s.names, x, y, z, d->nx, d->ny, d->nz, cell);
+                    if (!err.empty())
+                        return fail(c, PLBGPU_ERR_ARG, "%s: cell (%d, %d, %d): %s", s.datName.c_str(), x, y, z,
+                                    err.c_str());
+                    if (pos + w * sizeof(double) > buf.size())
+                        return fail(c, PLBGPU_ERR_ARG, "%s: truncated data", s.datName.c_str());
+                    memcpy(&rec[idx * w], buf.data() + pos, w * sizeof(double));
+                    pos += w * sizeof(double);
+                    seen[idx] = 1;
+                    if (cells) (*cells)[idx] = cell;
+                }
+        if (pos != buf.size())
+            return fail(c, PLBGPU_ERR_ARG, "%s: component %zu has %zu bytes beyond its cells", s.datName.c_str(), i,
+                        buf.size() - pos);
+        begin = s.offsets[i];
+    }
+    for (size_t idx = 0; idx < seen.size(); ++idx)
+        if (!seen[idx]) return fail(c, PLBGPU_ERR_ARG, "%s: the components do not cover the domain", s.datName.c_str());
+    return PLBGPU_OK;
+}
+
+// Host records of the whole domain (x-major, blockWidth(what) per cell) into
+// the domain, slab by slab.
+int uploadRecords(plbgpu_ctx* c, Domain* d, int what, const std::vector<double>& rec) {
+    const int w = blockWidth(what);
+    const int planes = slabPlanes(d, w);
+    Ckpt k;
+    int rc;
+    if ((rc = ckptAlloc(c, k, (long long)planes * d->ny * d->nz, w))) return rc;
+    for (int x0 = 0; x0 < d->nx; x0 += planes) {
+        const int x1 = x0 + planes - 1 < d->nx - 1 ? x0 + planes - 1 : d->nx - 1;
+        Box b{x0, x1, 0, d->ny - 1, 0, d->nz - 1};
+        const size_t first = (size_t)x0 * d->ny * d->nz * w;
+        CUDA_TRY(c, cudaMemcpyAsync(k.rec, rec.data() + first, (size_t)boxCells(b) * w * sizeof(double),
+                                    cudaMemcpyHostToDevice, c->stream));
+        if ((rc = applyRecords(c, d, what, b, k))) return rc;
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    }
+    return PLBGPU_OK;
+}
+
+bool isLatticeBlock(int what) { return what == PLBGPU_BLOCK_LATTICE || what == PLBGPU_BLOCK_FORCED_LATTICE; }
+
+}  // namespace
+
+int plbgpu_load_state(plbgpu_ctx* c, int h, int what, const char* plb) {
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    const int w = blockWidth(what);
+    if (!w) return fail(c, PLBGPU_ERR_ARG, "unknown block kind %d", what);
+    if (what == PLBGPU_BLOCK_DENSITY || what == PLBGPU_BLOCK_VELOCITY)
+        return fail(c, PLBGPU_ERR_ARG, "density and velocity blocks are derived data and cannot be loaded");
+    if (!plb) return fail(c, PLBGPU_ERR_ARG, "null path");
+    StateSpec s;
+    if ((rc = parseStateSpec(c, d, plb, w, s))) return rc;
+    if (s.dynamic && isLatticeBlock(what)) {
+        // load(plb, lattice, false) of a state with dynamic content: the
+        // populations (and force) only, the dynamics chains are skipped.
+        std::vector<double> rec;
+        if ((rc = readDynamicCells(c, d, s, w, rec, nullptr))) return rc;
+        if ((rc = prepareLoad(c, d, what))) return rc;
+        if ((rc = uploadRecords(c, d, what, rec))) return rc;
+        d->statsValid = false;
+        return PLBGPU_OK;
+    }
+    // Static content (a field's records are the same with or without it:
+    // ScalarFieldDataTransfer3D ignores the kind, dataField3D.hh:133-150).
+    FileCloser fd{fopen(s.datName.c_str(), "rb")};
+    if (!fd.f) return fail(c, PLBGPU_ERR_ARG, "cannot open %s", s.datName.c_str());
     if ((rc = prepareLoad(c, d, what))) return rc;
     std::vector<char> host;
     long long begin = 0;
-    for (size_t i = 0; i < comps.size(); ++i) {
-        const Box& cb = comps[i];
-        const long long bytes = offsets[i] - begin;
+    for (size_t i = 0; i < s.comps.size(); ++i) {
+        const Box& cb = s.comps[i];
+        const long long bytes = s.offsets[i] - begin;
         if (bytes != boxCells(cb) * w * (long long)sizeof(double))
             return fail(c, PLBGPU_ERR_ARG, "%s: component %zu holds %lld bytes, its box needs %lld", plb, i, bytes,
                         boxCells(cb) * w * (long long)sizeof(double));
-        if (fseek(fd.f, (long)begin, SEEK_SET) != 0) return fail(c, PLBGPU_ERR_ARG, "%s: truncated", datName.c_str());
+        if (fseek(fd.f, (long)begin, SEEK_SET) != 0) return fail(c, PLBGPU_ERR_ARG, "%s: truncated", s.datName.c_str());
         // whole x-planes of the component at a time
         const long long plane = (long long)(cb.y1 - cb.y0 + 1) * (cb.z1 - cb.z0 + 1) * w * sizeof(double);
         long long per = (32ll << 20) / (plane > 0 ? plane : 1);
@@ -1731,14 +1861,161 @@ int plbgpu_load_state(plbgpu_ctx* c, int h, int what, const char* plb) {
             Box b{x0, x1, cb.y0, cb.y1, cb.z0, cb.z1};
             host.resize((size_t)boxCells(b) * w * sizeof(double));
             if (fread(host.data(), 1, host.size(), fd.f) != host.size())
-                return fail(c, PLBGPU_ERR_ARG, "%s: truncated data", datName.c_str());
+                return fail(c, PLBGPU_ERR_ARG, "%s: truncated data", s.datName.c_str());
             CUDA_TRY(c, cudaMemcpyAsync(k.rec, host.data(), host.size(), cudaMemcpyHostToDevice, c->stream));
             if ((rc = applyRecords(c, d, what, b, k))) return rc;
             CUDA_TRY(c, cudaStreamSynchronize(c->stream));
         }
-        begin = offsets[i];
+        begin = s.offsets[i];
     }
-    if (what == PLBGPU_BLOCK_LATTICE || what == PLBGPU_BLOCK_FORCED_LATTICE) d->statsValid = false;
+    if (isLatticeBlock(what)) d->statsValid = false;
+    return PLBGPU_OK;
+}
+
+int plbgpu_save_state_dynamic(plbgpu_ctx* c, int h, int what, const char* base) {
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if (!isLatticeBlock(what)) return fail(c, PLBGPU_ERR_ARG, "dynamic content: block kind %d is not a lattice", what);
+    if (!base) return fail(c, PLBGPU_ERR_ARG, "null path");
+    if (d->sparse)
+        return fail(c, PLBGPU_ERR_STATE, "dynamic content of a sparse domain is not supported (its cells outside "
+                                         "the lattice have no dynamics)");
+    if ((rc = checkStatus(c, d))) return rc;
+    const int w = blockWidth(what);
+    const size_t n = (size_t)d->n;
+    // Cell kinds, boundary values and momentum-exchange directions, host side.
+    std::vector<uint8_t> kinds(n);
+    std::vector<double> bc(d->bc ? 3 * n : 0);
+    std::vector<uint32_t> mask(d->mebb ? n : 0);
+    CUDA_TRY(c, cudaMemcpyAsync(kinds.data(), d->flags, n, cudaMemcpyDeviceToHost, c->stream));
+    if (d->bc) CUDA_TRY(c, cudaMemcpyAsync(bc.data(), d->bc, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if (d->mebb)
+        CUDA_TRY(c, cudaMemcpyAsync(mask.data(), d->mebb, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    std::map<std::string, int> dict;   // uniqueDynamicsIds over the chains (metaStuffWrapper3D.hh:167-179)
+    {
+        bool present[K_NKINDS] = {false};
+        for (size_t i = 0; i < n; ++i)
+            if (kinds[i] < K_NKINDS) present[kinds[i]] = true;
+        for (int k = 0; k < K_NKINDS; ++k)
+            if (present[k]) {
+                dict[plbgpu_dyn::kindName(k)] = plbgpu_dyn::kindId(k);
+                if (plbgpu_dyn::isComposite(k)) dict["BGK"] = plbgpu_dyn::kBgkId;
+            }
+    }
+    plbgpu_dyn::Params p;
+    p.omega = d->omega;
+    p.rho0 = d->rho0;
+    p.bbRho = d->bbRho;
+    const std::string datName = std::string(base) + ".dat", plbName = std::string(base) + ".plb";
+    unsigned long long total = 0;
+    {
+        FileCloser fc{fopen(datName.c_str(), "wb")};
+        if (!fc.f) return fail(c, PLBGPU_ERR_ARG, "cannot open %s for writing", datName.c_str());
+        const int planes = slabPlanes(d, w);
+        Ckpt k;
+        if ((rc = ckptAlloc(c, k, (long long)planes * d->ny * d->nz, w))) return rc;
+        std::vector<double> host;
+        std::vector<char> out;
+        for (int x0 = 0; x0 < d->nx; x0 += planes) {
+            const int x1 = x0 + planes - 1 < d->nx - 1 ? x0 + planes - 1 : d->nx - 1;
+            Box b{x0, x1, 0, d->ny - 1, 0, d->nz - 1};
+            if ((rc = buildRecords(c, d, what, b, k))) return rc;
+            const size_t cells = (size_t)boxCells(b);
+            host.resize(cells * w);
+            CUDA_TRY(c, cudaMemcpyAsync(host.data(), k.rec, host.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                        c->stream));
+            CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+            out.clear();
+            const size_t first = (size_t)x0 * d->ny * d->nz;
+            for (size_t j = 0; j < cells; ++j) {
+                const size_t idx = first + j;
+                const double v[3] = {bc.empty() ? 0. : bc[idx], bc.empty() ? 0. : bc[n + idx],
+                                     bc.empty() ? 0. : bc[2 * n + idx]};
+                plbgpu_dyn::appendCell(out, kinds[idx], v, mask.empty() ? 0u : mask[idx], p);
+                const size_t at = out.size();
+                out.resize(at + w * sizeof(double));
+                memcpy(&out[at], &host[j * w], w * sizeof(double));
+            }
+            if (fwrite(out.data(), 1, out.size(), fc.f) != out.size())
+                return fail(c, PLBGPU_ERR_ARG, "write to %s failed", datName.c_str());
+            total += out.size();
+        }
+        if (fflush(fc.f) != 0) return fail(c, PLBGPU_ERR_ARG, "write to %s failed", datName.c_str());
+    }
+    const std::string x = stateDescription(d, what, datName, total, &dict);
+    FileCloser fp{fopen(plbName.c_str(), "wb")};
+    if (!fp.f) return fail(c, PLBGPU_ERR_ARG, "cannot open %s for writing", plbName.c_str());
+    if (fwrite(x.data(), 1, x.size(), fp.f) != x.size() || fflush(fp.f) != 0)
+        return fail(c, PLBGPU_ERR_ARG, "write to %s failed", plbName.c_str());
+    return PLBGPU_OK;
+}
+
+int plbgpu_load_state_dynamic(plbgpu_ctx* c, int h, int what, const char* plb) {
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if (!isLatticeBlock(what)) return fail(c, PLBGPU_ERR_ARG, "dynamic content: block kind %d is not a lattice", what);
+    if (!plb) return fail(c, PLBGPU_ERR_ARG, "null path");
+    const int w = blockWidth(what);
+    StateSpec s;
+    if ((rc = parseStateSpec(c, d, plb, w, s))) return rc;
+    if (!s.dynamic) return fail(c, PLBGPU_ERR_ARG, "%s: the state has no dynamic content", plb);
+    std::vector<double> rec;
+    std::vector<plbgpu_dyn::Cell> cells;
+    if ((rc = readDynamicCells(c, d, s, w, rec, &cells))) return rc;
+    // The GPU lattice holds one omega, one rho0 and one wall density.
+    const size_t n = cells.size();
+    bool haveOmega = false, haveInv = false, haveRho = false, composite = false, mebb = false;
+    double omega = d->omega, invRho0 = 0, rho = d->bbRho;
+    std::vector<uint8_t> kinds(n);
+    for (size_t i = 0; i < n; ++i) {
+        const plbgpu_dyn::Cell& cl = cells[i];
+        kinds[i] = (uint8_t)cl.kind;
+        composite |= plbgpu_dyn::isComposite(cl.kind);
+        mebb |= cl.kind == PLBGPU_MOMENTUM_EXCHANGE;
+        if (cl.hasOmega) {
+            if (haveOmega && cl.omega != omega) return fail(c, PLBGPU_ERR_ARG, "%s: cells with different omega", plb);
+            omega = cl.omega;
+            haveOmega = true;
+        }
+        if (cl.hasInvRho0) {
+            if (haveInv && cl.invRho0 != invRho0) return fail(c, PLBGPU_ERR_ARG, "%s: cells with different rho0", plb);
+            invRho0 = cl.invRho0;
+            haveInv = true;
+        }
+        if (cl.hasRho) {
+            if (haveRho && cl.rho != rho)
+                return fail(c, PLBGPU_ERR_ARG, "%s: wall cells (bounce-back, no-dynamics) with different densities",
+                            plb);
+            rho = cl.rho;
+            haveRho = true;
+        }
+    }
+    double rho0 = d->rho0;
+    if (haveInv && !plbgpu_dyn::rho0FromInverse(invRho0, rho0))
+        return fail(c, PLBGPU_ERR_ARG, "%s: no rho0 has the stored 1/rho0 as its reciprocal", plb);
+    if ((rc = plbgpu_set_params(c, h, omega, rho0, rho))) return rc;
+    if ((rc = plbgpu_set_kinds(c, h, 0, d->nx - 1, 0, d->ny - 1, 0, d->nz - 1, kinds.data(), n))) return rc;
+    if (composite) {
+        std::vector<double> bc(3 * n);
+        for (size_t i = 0; i < n; ++i)
+            for (int a = 0; a < 3; ++a) bc[a * n + i] = cells[i].bc[a];
+        if ((rc = ensureAux(c, d, true, false, false))) return rc;
+        CUDA_TRY(c, cudaMemcpyAsync(d->bc, bc.data(), 3 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    }
+    if (mebb) {
+        std::vector<uint32_t> mask(n);
+        for (size_t i = 0; i < n; ++i) mask[i] = cells[i].mask;
+        if ((rc = ensureAux(c, d, false, false, true))) return rc;
+        CUDA_TRY(c, cudaMemcpyAsync(d->mebb, mask.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream));
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    }
+    if ((rc = prepareLoad(c, d, what))) return rc;
+    if ((rc = uploadRecords(c, d, what, rec))) return rc;
+    d->statsValid = false;
     return PLBGPU_OK;
 }
 

@@ -267,8 +267,22 @@ class DeviceLattice3D:
         self._check(self.lib.plbgpu_save_state(self.ctx.h, self.handle, N.BLOCKS[what], os.fsencode(base)))
 
     def load_state(self, plb_path, what="lattice"):
-        """parallelIO::load of a state with static content."""
+        """parallelIO::load(plb, block, false): the populations (and force) of a
+        state, with or without dynamic content."""
         self._check(self.lib.plbgpu_load_state(self.ctx.h, self.handle, N.BLOCKS[what], os.fsencode(plb_path)))
+
+    def save_state_dynamic(self, base, what="lattice"):
+        """parallelIO::save(lattice, base, true): each cell's dynamics chain
+        before its populations."""
+        self._check(self.lib.plbgpu_save_state_dynamic(self.ctx.h, self.handle, N.BLOCKS[what],
+                                                       os.fsencode(base)))
+
+    def load_state_dynamic(self, plb_path, what="lattice"):
+        """parallelIO::load(plb, lattice, true): cell kinds, boundary values,
+        momentum-exchange directions, parameters and populations from the
+        state."""
+        self._check(self.lib.plbgpu_load_state_dynamic(self.ctx.h, self.handle, N.BLOCKS[what],
+                                                       os.fsencode(plb_path)))
 
     def time_steps(self, nsteps, stats=False) -> float:
         ms = ctypes.c_float()

@@ -85,6 +85,8 @@ SIGNATURES = {
     "plbgpu_load_binary_block": [_vp, _i, _i, ctypes.c_char_p, _i],
     "plbgpu_save_state": [_vp, _i, _i, ctypes.c_char_p],
     "plbgpu_load_state": [_vp, _i, _i, ctypes.c_char_p],
+    "plbgpu_save_state_dynamic": [_vp, _i, _i, ctypes.c_char_p],
+    "plbgpu_load_state_dynamic": [_vp, _i, _i, ctypes.c_char_p],
     "plbgpu_set_boundary_velocity": [_vp, _i, *BOX, _d, _d, _d],
     "plbgpu_set_boundary_velocity_field": [_vp, _i, *BOX, _c_dbl_p, _sz],
     "plbgpu_set_boundary_density": [_vp, _i, *BOX, _d],

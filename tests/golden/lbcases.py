@@ -43,6 +43,7 @@ OPT_EXTERNAL_RHOJ = 2
 OPT_SAVE_BINARY = 4
 OPT_SPARSE = 8
 OPT_SAVE_STATE = 16
+OPT_SAVE_DYNAMIC_STATE = 32
 NONE = 255   # not part of the lattice (outside every kept block)
 
 
@@ -499,6 +500,43 @@ def case_state_guo_multiblock():
     return s
 
 
+def _dynamic_state(builder, name, nsteps):
+    s = builder()
+    s.name = name
+    s.nsteps = nsteps
+    s.options |= OPT_SAVE_DYNAMIC_STATE
+    return s
+
+
+def case_dstate_channel_sphere_multiblock():
+    """parallelIO::save(lattice, base, true) of six blocks holding a
+    regularized velocity inlet, a regularized pressure outlet, bounce-back
+    walls and a momentum-exchange obstacle: each cell's dynamics chain before
+    its populations."""
+    return _dynamic_state(case_channel_sphere_multiblock, "dstate_channel_sphere_multiblock", 6)
+
+
+def case_dstate_velocity_box():
+    """Dynamic content of regularized velocity faces, edges and corners
+    (stored-velocity dynamics around BGK)."""
+    return _dynamic_state(case_velocity_box, "dstate_velocity_box", 4)
+
+
+def case_dstate_zhpress_faces():
+    """Dynamic content of Zou/He pressure faces on all six sides."""
+    return _dynamic_state(case_zhpress_faces, "dstate_zhpress_faces", 4)
+
+
+def case_dstate_guo_channel():
+    """Forced descriptor: Guo dynamics and bounce-back, 22 static values."""
+    return _dynamic_state(case_guo_channel, "dstate_guo_channel", 4)
+
+
+def case_dstate_incbgk_nodyn():
+    """Incompressible BGK, no-dynamics and bounce-back cells."""
+    return _dynamic_state(case_incbgk_nodyn, "dstate_incbgk_nodyn", 4)
+
+
 def case_doctest_cavity20():
     return doctest_cavity(20, 20, 20, name="doctest_cavity20")
 
@@ -523,6 +561,8 @@ CASES = [
     case_external_periodic_bgk, case_external_incbgk_nodyn, case_external_guo_periodic,
     case_external_mebb_periodic, case_binary_channel_sphere, case_binary_guo_periodic,
     case_sparse_sealed_channel, case_state_periodic_multiblock, case_state_guo_multiblock,
+    case_dstate_channel_sphere_multiblock, case_dstate_velocity_box, case_dstate_zhpress_faces,
+    case_dstate_guo_channel, case_dstate_incbgk_nodyn,
 ]
 
 
@@ -604,6 +644,12 @@ def read_result_file(path: str, spec: CaseSpec):
             out["state_plb"] = f.read()
         with open(base + ".dat", "rb") as f:
             out["state_dat"] = np.frombuffer(f.read(), np.uint8).copy()
+    if spec.options & OPT_SAVE_DYNAMIC_STATE:
+        base = os.path.splitext(path)[0] + "_dstate"
+        with open(base + ".plb") as f:
+            out["dstate_plb"] = f.read()
+        with open(base + ".dat", "rb") as f:
+            out["dstate_dat"] = np.frombuffer(f.read(), np.uint8).copy()
     if spec.options & OPT_SAVE_BINARY:
         for what in ("lattice", "density", "velocity"):
             with open(path + "." + what, "rb") as f:

@@ -72,6 +72,8 @@ def main(argv):
                     extra["binary_" + what] = res["binary_" + what]
             if "state_plb" in res:
                 extra.update(state_plb=res["state_plb"], state_dat=res["state_dat"])
+            if "dstate_plb" in res:
+                extra.update(dstate_plb=res["dstate_plb"], dstate_dat=res["dstate_dat"])
             if spec.sparse is not None:
                 extra.update(sparse=spec.sparse, in_lattice=res["in_lattice"], compare=spec.compare)
             np.savez_compressed(

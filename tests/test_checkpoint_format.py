@@ -106,3 +106,100 @@ def test_reference_loads_single_component_state(name):
         res = lbcases.read_result_file(rpath, spec)
     assert np.array_equal(res["f_init"], f_init)
     assert np.array_equal(res["f_final"], g["f_final"])
+
+
+# ---------------------------------------------------------------- states with dynamic content
+
+DSTATES = ["dstate_channel_sphere_multiblock", "dstate_velocity_box", "dstate_zhpress_faces",
+           "dstate_guo_channel", "dstate_incbgk_nodyn"]
+SINGLE_COMPONENT = DSTATES[1:]
+
+
+def _shape(meta):
+    return (meta["nx"], meta["ny"], meta["nz"])
+
+
+def _velocity_kind(k):
+    return 6 <= k < 12 or 18 <= k < 24 or k >= 30
+
+
+def _density_kind(k):
+    return 12 <= k < 18 or 24 <= k < 30
+
+
+def _masks(g, meta):
+    return O.OracleLattice.from_golden(g, meta).mebb_masks().reshape(_shape(meta))
+
+
+@pytest.mark.parametrize("name", DSTATES)
+def test_reference_dynamic_state_decodes(name):
+    """parallelIO::save(lattice, base, true) as the reference wrote it: every
+    cell's dynamics chain decodes to the case's kind, wall values and
+    parameters, and its static values are the final populations."""
+    g, meta = goldens.load(name)
+    st = O.read_dynamic_state(str(g["dstate_plb"]), bytes(g["dstate_dat"]), _shape(meta))
+    kinds = g["flags"]
+    assert np.array_equal(st["kinds"], kinds)
+    vel = np.vectorize(_velocity_kind)(kinds)
+    den = np.vectorize(_density_kind)(kinds)
+    assert np.array_equal(st["bc"][vel], g["bcval"][vel])
+    assert np.array_equal(st["bc"][den][:, 0], g["bcval"][den][:, 0])
+    assert np.array_equal(st["records"], records(g, meta).reshape(st["records"].shape))
+    assert st["omegas"] == {meta["omega"]}
+    if (kinds == 2).any():
+        assert st["inv_rho0s"] == {1.0 / meta["rho0"]}
+    if np.isin(kinds, (3, 4, 5)).any():
+        assert st["rhos"] == {meta["bb_rho"]}
+    mebb = kinds == 4
+    if mebb.any():
+        assert np.array_equal(st["masks"][mebb], _masks(g, meta)[mebb])
+
+
+@pytest.mark.parametrize("name", SINGLE_COMPONENT)
+def test_dynamic_state_writer_reproduces_reference_bytes(name):
+    """With the reference's own dynamics ids, the restated writer gives the
+    reference's data file byte for byte and its DynamicsDict."""
+    g, meta = goldens.load(name)
+    ref_plb, ref_dat = str(g["dstate_plb"]), bytes(g["dstate_dat"])
+    ids = {n: i for i, n in O.read_dynamic_state(ref_plb, ref_dat, _shape(meta))["names"].items()}
+    plb, dat = O.dynamic_state_files(g["flags"], g["bcval"], _masks(g, meta), records(g, meta), 22 if meta["forced"] else 19,
+                                     "ForcedD3Q19" if meta["forced"] else "D3Q19", "x.dat", meta["omega"],
+                                     meta["rho0"], meta["bb_rho"], ids=ids)
+    assert dat == ref_dat
+    dd = re.search(r"<DynamicsDict>.*?</DynamicsDict>", plb, re.S).group(0)
+    assert dd == re.search(r"<DynamicsDict>.*?</DynamicsDict>", ref_plb, re.S).group(0)
+
+
+@pytest.mark.skipif(not os.path.exists(DRIVER), reason="reference driver not built (needs the reference sources)")
+@pytest.mark.parametrize("name", ["dstate_channel_sphere_multiblock", "dstate_velocity_box", "dstate_zhpress_faces",
+                                  "dstate_incbgk_nodyn"])
+def test_reference_loads_dynamic_state(name):
+    """A state written the way plbgpu_save_state_dynamic writes it (one
+    component, the library's own ids) is loaded by the reference's
+    parallelIO::load(plb, lattice, true) into a lattice built with other
+    parameters (omega, wall velocities and densities, rho0); the regenerated
+    dynamics carry the state's and the run continues the reference's
+    trajectory bit for bit."""
+    spec = lbcases.case_by_name(name)
+    g, meta = goldens.load(name)
+    cd = 22 if meta["forced"] else 19
+    recs = g["f_init"] if not meta["forced"] else np.concatenate([g["f_init"], g["force"]], axis=-1)
+    with tempfile.TemporaryDirectory() as tmp:
+        plb, dat = O.dynamic_state_files(g["flags"], g["bcval"], _masks(g, meta), recs, cd,
+                                         "ForcedD3Q19" if meta["forced"] else "D3Q19", os.path.join(tmp, "s.dat"),
+                                         meta["omega"], meta["rho0"], meta["bb_rho"])
+        with open(os.path.join(tmp, "s.plb"), "w") as f:
+            f.write(plb)
+        with open(os.path.join(tmp, "s.dat"), "wb") as f:
+            f.write(dat)
+        spec.options &= ~lbcases.OPT_SAVE_DYNAMIC_STATE
+        spec.omega = 1.1
+        spec.bcval = np.where(spec.bcval != 0, 0.5 * spec.bcval + 0.25, 0.0)
+        spec.rho0 = 1.07
+        cpath, rpath = os.path.join(tmp, "c"), os.path.join(tmp, "r")
+        lbcases.write_case_file(spec, cpath)
+        subprocess.run([DRIVER, cpath, rpath], check=True,
+                       env=dict(os.environ, PLB_LOAD_DYNAMIC_STATE=os.path.join(tmp, "s.plb")))
+        res = lbcases.read_result_file(rpath, spec)
+    assert np.array_equal(res["f_init"], g["f_init"])
+    assert np.array_equal(res["f_final"], g["f_final"])

@@ -76,3 +76,110 @@ def test_state_round_trip_and_refusals(tmp_path):
         fh.write(text)
     with pytest.raises(PlbGpuError):
         other.load_state(str(tmp_path / "b.plb"))                               # dynamic content
+
+
+# ---------------------------------------------------------------- dynamic content
+
+import re
+
+DSTATES = ["dstate_channel_sphere_multiblock", "dstate_velocity_box", "dstate_zhpress_faces",
+           "dstate_guo_channel", "dstate_incbgk_nodyn"]
+
+
+def _what(meta):
+    return "forced_lattice" if meta["forced"] else "lattice"
+
+
+def _recs(g, meta, key):
+    return g[key] if not meta["forced"] else np.concatenate([g[key], g["force"]], axis=-1)
+
+
+def _masks(g, meta):
+    return O.OracleLattice.from_golden(g, meta).mebb_masks().reshape(meta["nx"], meta["ny"], meta["nz"])
+
+
+def _reference_files(g, tmp_path):
+    dat_path = str(tmp_path / "ref.dat")
+    with open(dat_path, "wb") as f:
+        f.write(bytes(g["dstate_dat"]))
+    plb = re.sub(r"<File>[^<]*</File>", f"<File> {dat_path} </File>", str(g["dstate_plb"]))
+    with open(tmp_path / "ref.plb", "w") as f:
+        f.write(plb)
+    return str(tmp_path / "ref.plb")
+
+
+@pytest.mark.parametrize("name", DSTATES)
+def test_save_state_dynamic_matches_format(name, tmp_path):
+    """plbgpu_save_state_dynamic writes exactly the restated format (which the
+    reference loads and continues bit for bit, tests/test_checkpoint_format.py)."""
+    g, meta = goldens.load(name)
+    lat = _lat(g, meta)
+    lat.send(g["f_init"])
+    lat.collide_and_stream(meta["nsteps"])
+    base = str(tmp_path / "s")
+    lat.save_state_dynamic(base, _what(meta))
+    recs = _recs(g, meta, "f_final")
+    plb, dat = O.dynamic_state_files(g["flags"], g["bcval"], _masks(g, meta), recs, recs.shape[-1],
+                                     "ForcedD3Q19" if meta["forced"] else "D3Q19", base + ".dat", meta["omega"],
+                                     meta.get("rho0", 1.0), meta.get("bb_rho", 0.0))
+    assert open(base + ".plb").read() == plb
+    assert open(base + ".dat", "rb").read() == dat
+
+
+@pytest.mark.parametrize("name", DSTATES)
+def test_load_reference_dynamic_state(name, tmp_path):
+    """The reference's state (one component per block) into a blank lattice
+    of the same size: kinds, wall values, parameters and populations come
+    from the file, and the next steps equal the oracle's."""
+    g, meta = goldens.load(name)
+    lat = DeviceLattice3D(meta["nx"], meta["ny"], meta["nz"], 1.0)
+    lat.periodicity(*meta["periodic"])
+    lat.load_state_dynamic(_reference_files(g, tmp_path), _what(meta))
+    assert np.array_equal(lat.get_kinds(), g["flags"])
+    assert np.array_equal(lat.receive(), g["f_final"])
+    lat.collide_and_stream(3)
+    ol = O.OracleLattice.from_golden(g, meta)
+    ref, _ = ol.run(np.ascontiguousarray(g["f_final"]).copy(), 3)
+    assert np.array_equal(lat.receive(), ref.reshape(g["f_final"].shape))
+
+
+def test_static_load_of_dynamic_state_takes_populations_only(tmp_path):
+    name = "dstate_channel_sphere_multiblock"
+    g, meta = goldens.load(name)
+    lat = DeviceLattice3D(meta["nx"], meta["ny"], meta["nz"], 1.0)
+    before = lat.get_kinds()
+    lat.load_state(_reference_files(g, tmp_path))
+    assert np.array_equal(lat.get_kinds(), before)
+    lat2 = _lat(g, meta)
+    lat2.load_state(str(tmp_path / "ref.plb"))
+    assert np.array_equal(lat2.receive(), g["f_final"])
+
+
+def test_dynamic_state_round_trip_and_refusals(tmp_path):
+    g, meta = goldens.load("dstate_velocity_box")
+    lat = _lat(g, meta)
+    lat.send(g["f_init"])
+    lat.collide_and_stream(5)
+    ref = lat.receive()
+    lat.save_state_dynamic(str(tmp_path / "a"))
+    other = DeviceLattice3D(meta["nx"], meta["ny"], meta["nz"], 1.7)
+    other.load_state_dynamic(str(tmp_path / "a.plb"))
+    assert np.array_equal(other.get_kinds(), g["flags"])
+    assert np.array_equal(other.receive(), ref)
+    lat.collide_and_stream(4)
+    other.collide_and_stream(4)
+    assert np.array_equal(other.receive(), lat.receive())
+    with pytest.raises(PlbGpuError):
+        DeviceLattice3D(meta["nx"], meta["ny"], meta["nz"] + 1, 1.0).load_state_dynamic(str(tmp_path / "a.plb"))
+    lat.save_state(str(tmp_path / "s"))
+    with pytest.raises(PlbGpuError):
+        other.load_state_dynamic(str(tmp_path / "s.plb"))                   # static content
+    # two omegas: the GPU lattice holds one
+    dat = open(tmp_path / "a.dat", "rb").read()
+    om = np.float64(meta["omega"]).tobytes()
+    bad = dat.replace(om, np.float64(1.2345).tobytes(), 1)
+    with open(tmp_path / "a.dat", "wb") as f:
+        f.write(bad)
+    with pytest.raises(PlbGpuError):
+        other.load_state_dynamic(str(tmp_path / "a.plb"))
+    assert np.array_equal(other.get_kinds(), g["flags"])                     # nothing changed
