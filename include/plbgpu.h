@@ -296,9 +296,12 @@ int plbgpu_load_state(plbgpu_ctx* ctx, int handle, int what, const char* plb_pat
  * the wall density, the momentum-exchange fluid directions, a face's stored
  * velocity or rho-bar around its BGK base), and in <base>.plb a DynamicsDict
  * mapping the ids to the dynamics names.  what: PLBGPU_BLOCK_LATTICE or
- * PLBGPU_BLOCK_FORCED_LATTICE.  Save writes one component; it refuses sparse
- * domains (PLBGPU_ERR_STATE).  Load reads any number of components that cover
- * the domain, then sets the cell kinds, the boundary values, the
+ * PLBGPU_BLOCK_FORCED_LATTICE.  Save writes one component (cells outside the
+ * lattice of a sparse domain as NoDynamics with zero populations, which a
+ * reference lattice on the same sparse blocks does not have and skips).  Load
+ * reads any number of components that cover every cell of the lattice (cells
+ * outside it stay outside, as the reference's load fills only the blocks that
+ * exist), then sets the cell kinds, the boundary values, the
  * momentum-exchange directions, omega / rho0 / the wall density, and the
  * populations, as the reference regenerates the dynamics objects.  A state
  * whose cells need more than the domain holds -- dynamics without a GPU kind,

@@ -336,6 +336,8 @@ def dynamic_state_files(kinds, bcval, masks, records, cell_dim, descriptor, dat_
     dict_ = {}
     for c in range(kf.size):
         k = int(kf[c])
+        if k == 255:   # outside the lattice of a sparse domain: NoDynamics, zero populations
+            k = _K_NODYN
         names = [dynamics_name(k)] + (["BGK"] if k >= _K_FACE else [])
         chain_ids = [idof(names[0], k)] + ([idof("BGK", 0)] if k >= _K_FACE else [])
         for nm, i in zip(names, chain_ids):

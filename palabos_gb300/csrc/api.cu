@@ -1746,15 +1746,17 @@ int parseStateSpec(plbgpu_ctx* c, const Domain* d, const char* plb, int w, State
 
 // The cells of a lattice state with dynamic content: per component, its cells
 // x-major, each one's dynamics chain then its w static values
-// (blockLattice3D.hh:703-722).  rec receives the static values over the whole
-// domain (x-major, w per cell); cells, when given, each cell's dynamics.
-int readDynamicCells(plbgpu_ctx* c, const Domain* d, const StateSpec& s, int w, std::vector<double>& rec,
-                     std::vector<plbgpu_dyn::Cell>* cells) {
+// (blockLattice3D.hh:703-722).  recs receives each component's static values
+// (x-major over its box, w per cell); cells, when given, each covered cell's
+// dynamics (domain-indexed) and seen which cells the components cover.
+int readDynamicCells(plbgpu_ctx* c, const Domain* d, const StateSpec& s, int w,
+                     std::vector<std::vector<double>>& recs, std::vector<plbgpu_dyn::Cell>* cells,
+                     std::vector<uint8_t>* seen) {
     FileCloser fd{fopen(s.datName.c_str(), "rb")};
     if (!fd.f) return fail(c, PLBGPU_ERR_ARG, "cannot open %s", s.datName.c_str());
-    rec.assign((size_t)d->n * w, 0.0);
-    std::vector<uint8_t> seen((size_t)d->n, 0);
+    recs.assign(s.comps.size(), std::vector<double>());
     if (cells) cells->assign((size_t)d->n, plbgpu_dyn::Cell());
+    if (seen) seen->assign((size_t)d->n, 0);
     std::vector<char> buf;
     long long begin = 0;
     for (size_t i = 0; i < s.comps.size(); ++i) {
@@ -1763,10 +1765,12 @@ int readDynamicCells(plbgpu_ctx* c, const Domain* d, const StateSpec& s, int w, 
         buf.resize((size_t)(s.offsets[i] - begin));
         if (fseek(fd.f, (long)begin, SEEK_SET) != 0 || fread(buf.data(), 1, buf.size(), fd.f) != buf.size())
             return fail(c, PLBGPU_ERR_ARG, "%s: truncated data", s.datName.c_str());
-        size_t pos = 0;
+        std::vector<double>& rec = recs[i];
+        rec.resize((size_t)boxCells(cb) * w);
+        size_t pos = 0, j = 0;
         for (int x = cb.x0; x <= cb.x1; ++x)
             for (int y = cb.y0; y <= cb.y1; ++y)
-                for (int z = cb.z0; z <= cb.z1; ++z) {
+                for (int z = cb.z0; z <= cb.z1; ++z, ++j) {
                     const size_t idx = ((size_t)x * d->ny + y) * d->nz + z;
                     plbgpu_dyn::Cell cell;
                     const std::string err =
@@ -1776,9 +1780,9 @@ int readDynamicCells(plbgpu_ctx* c, const Domain* d, const StateSpec& s, int w, 
                                     err.c_str());
                     if (pos + w * sizeof(double) > buf.size())
                         return fail(c, PLBGPU_ERR_ARG, "%s: truncated data", s.datName.c_str());
-                    memcpy(&rec[idx * w], buf.data() + pos, w * sizeof(double));
+                    memcpy(&rec[j * w], buf.data() + pos, w * sizeof(double));
                     pos += w * sizeof(double);
-                    seen[idx] = 1;
+                    if (seen) (*seen)[idx] = 1;
                     if (cells) (*cells)[idx] = cell;
                 }
         if (pos != buf.size())
@@ -1786,23 +1790,23 @@ int readDynamicCells(plbgpu_ctx* c, const Domain* d, const StateSpec& s, int w, 
                         buf.size() - pos);
         begin = s.offsets[i];
     }
-    for (size_t idx = 0; idx < seen.size(); ++idx)
-        if (!seen[idx]) return fail(c, PLBGPU_ERR_ARG, "%s: the components do not cover the domain", s.datName.c_str());
     return PLBGPU_OK;
 }
 
-// Host records of the whole domain (x-major, blockWidth(what) per cell) into
-// the domain, slab by slab.
-int uploadRecords(plbgpu_ctx* c, Domain* d, int what, const std::vector<double>& rec) {
+// Host records of box cb (x-major, blockWidth(what) per cell) into the domain,
+// slab by slab.
+int uploadRecords(plbgpu_ctx* c, Domain* d, int what, const Box& cb, const std::vector<double>& rec) {
     const int w = blockWidth(what);
-    const int planes = slabPlanes(d, w);
+    const long long plane = (long long)(cb.y1 - cb.y0 + 1) * (cb.z1 - cb.z0 + 1);
+    long long per = (32ll << 20) / (plane * w * (long long)sizeof(double));
+    const int planes = (int)(per < 1 ? 1 : (per > cb.x1 - cb.x0 + 1 ? cb.x1 - cb.x0 + 1 : per));
     Ckpt k;
     int rc;
-    if ((rc = ckptAlloc(c, k, (long long)planes * d->ny * d->nz, w))) return rc;
-    for (int x0 = 0; x0 < d->nx; x0 += planes) {
-        const int x1 = x0 + planes - 1 < d->nx - 1 ? x0 + planes - 1 : d->nx - 1;
-        Box b{x0, x1, 0, d->ny - 1, 0, d->nz - 1};
-        const size_t first = (size_t)x0 * d->ny * d->nz * w;
+    if ((rc = ckptAlloc(c, k, (long long)planes * plane, w))) return rc;
+    for (int x0 = cb.x0; x0 <= cb.x1; x0 += planes) {
+        const int x1 = x0 + planes - 1 < cb.x1 ? x0 + planes - 1 : cb.x1;
+        Box b{x0, x1, cb.y0, cb.y1, cb.z0, cb.z1};
+        const size_t first = (size_t)(x0 - cb.x0) * plane * w;
         CUDA_TRY(c, cudaMemcpyAsync(k.rec, rec.data() + first, (size_t)boxCells(b) * w * sizeof(double),
                                     cudaMemcpyHostToDevice, c->stream));
         if ((rc = applyRecords(c, d, what, b, k))) return rc;
@@ -1829,10 +1833,11 @@ int plbgpu_load_state(plbgpu_ctx* c, int h, int what, const char* plb) {
     if (s.dynamic && isLatticeBlock(what)) {
         // load(plb, lattice, false) of a state with dynamic content: the
         // populations (and force) only, the dynamics chains are skipped.
-        std::vector<double> rec;
-        if ((rc = readDynamicCells(c, d, s, w, rec, nullptr))) return rc;
+        std::vector<std::vector<double>> recs;
+        if ((rc = readDynamicCells(c, d, s, w, recs, nullptr, nullptr))) return rc;
         if ((rc = prepareLoad(c, d, what))) return rc;
-        if ((rc = uploadRecords(c, d, what, rec))) return rc;
+        for (size_t i = 0; i < s.comps.size(); ++i)
+            if ((rc = uploadRecords(c, d, what, s.comps[i], recs[i]))) return rc;
         d->statsValid = false;
         return PLBGPU_OK;
     }
@@ -1878,9 +1883,6 @@ int plbgpu_save_state_dynamic(plbgpu_ctx* c, int h, int what, const char* base) 
     if (rc) return rc;
     if (!isLatticeBlock(what)) return fail(c, PLBGPU_ERR_ARG, "dynamic content: block kind %d is not a lattice", what);
     if (!base) return fail(c, PLBGPU_ERR_ARG, "null path");
-    if (d->sparse)
-        return fail(c, PLBGPU_ERR_STATE, "dynamic content of a sparse domain is not supported (its cells outside "
-                                         "the lattice have no dynamics)");
     if ((rc = checkStatus(c, d))) return rc;
     const int w = blockWidth(what);
     const size_t n = (size_t)d->n;
@@ -1897,7 +1899,7 @@ int plbgpu_save_state_dynamic(plbgpu_ctx* c, int h, int what, const char* base) 
     {
         bool present[K_NKINDS] = {false};
         for (size_t i = 0; i < n; ++i)
-            if (kinds[i] < K_NKINDS) present[kinds[i]] = true;
+            present[kinds[i] < K_NKINDS ? kinds[i] : K_NODYN] = true;   // outside the lattice: NoDynamics
         for (int k = 0; k < K_NKINDS; ++k)
             if (present[k]) {
                 dict[plbgpu_dyn::kindName(k)] = plbgpu_dyn::kindId(k);
@@ -1962,15 +1964,24 @@ int plbgpu_load_state_dynamic(plbgpu_ctx* c, int h, int what, const char* plb) {
     StateSpec s;
     if ((rc = parseStateSpec(c, d, plb, w, s))) return rc;
     if (!s.dynamic) return fail(c, PLBGPU_ERR_ARG, "%s: the state has no dynamic content", plb);
-    std::vector<double> rec;
+    std::vector<std::vector<double>> recs;
     std::vector<plbgpu_dyn::Cell> cells;
-    if ((rc = readDynamicCells(c, d, s, w, rec, &cells))) return rc;
-    // The GPU lattice holds one omega, one rho0 and one wall density.
+    std::vector<uint8_t> seen;
+    if ((rc = readDynamicCells(c, d, s, w, recs, &cells, &seen))) return rc;
+    // Cells outside the lattice of a sparse domain stay outside (the
+    // reference copies a loaded state into the blocks that exist); every
+    // other cell must be in the state.
     const size_t n = cells.size();
+    std::vector<uint8_t> kinds(n);
+    CUDA_TRY(c, cudaMemcpyAsync(kinds.data(), d->flags, n, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    // The GPU lattice holds one omega, one rho0 and one wall density.
     bool haveOmega = false, haveInv = false, haveRho = false, composite = false, mebb = false;
     double omega = d->omega, invRho0 = 0, rho = d->bbRho;
-    std::vector<uint8_t> kinds(n);
     for (size_t i = 0; i < n; ++i) {
+        if (kinds[i] == K_NONE) continue;
+        if (!seen[i])
+            return fail(c, PLBGPU_ERR_ARG, "%s: the components do not cover the lattice (cell %zu)", plb, i);
         const plbgpu_dyn::Cell& cl = cells[i];
         kinds[i] = (uint8_t)cl.kind;
         composite |= plbgpu_dyn::isComposite(cl.kind);
@@ -2014,7 +2025,8 @@ int plbgpu_load_state_dynamic(plbgpu_ctx* c, int h, int what, const char* plb) {
         CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     }
     if ((rc = prepareLoad(c, d, what))) return rc;
-    if ((rc = uploadRecords(c, d, what, rec))) return rc;
+    for (size_t i = 0; i < s.comps.size(); ++i)
+        if ((rc = uploadRecords(c, d, what, s.comps[i], recs[i]))) return rc;
     d->statsValid = false;
     return PLBGPU_OK;
 }

@@ -20,8 +20,7 @@
 //   Boundary_*Density_d_o,          rhoBar, bool, then the base (boundaryDynamics.hh:238-242)
 //   Boundary_ZouHePressure_d_o
 //
-// Host-only C++ (no CUDA): the library's state reader and writer use it, and a
-// CPU test driver checks it against states the reference wrote.
+// Host-only C++ (no CUDA), used by the library's state reader and writer.
 #pragma once
 
 #include <cmath>
@@ -36,8 +35,7 @@
 
 namespace plbgpu_dyn {
 
-// Name of the dynamics class (its registry name) of a GPU kind, and of the base
-// dynamics a composite kind wraps ("" for none).
+// Name of the dynamics class (its registry name) of a GPU kind ("" for none).
 inline std::string kindName(int k) {
     static const char* basic[6] = {"BGK", "BGK_ExternalForce_Guo", "BGK_Incompressible", "BounceBack",
                                    "MomentumExchangeBounceBack", "NoDynamics"};
@@ -116,10 +114,16 @@ struct Params {
     double omega = 1.0, rho0 = 1.0, bbRho = 0.0;
 };
 
+// Kind byte of a cell outside the lattice of a sparse domain.
+constexpr int kOutside = 255;
+
 // Append the dynamics chain of one cell of kind k.  bc: the cell's three
 // boundary values (velocity, or density in bc[0]); mask: its momentum-exchange
-// fluid directions (bit i for direction i).
+// fluid directions (bit i for direction i).  A cell outside the lattice is
+// written as NoDynamics (its populations are zero): a reference lattice built
+// on the same sparse blocks has no cell there and ignores it on loading.
 inline void appendCell(std::vector<char>& out, int k, const double* bc, uint32_t mask, const Params& p) {
+    if (k == kOutside) k = PLBGPU_NODYNAMICS;
     ChainWriter w(out, kindId(k));
     if (k == PLBGPU_BGK || k == PLBGPU_GUO) {
         w.value(p.omega);

@@ -537,6 +537,11 @@ def case_dstate_incbgk_nodyn():
     return _dynamic_state(case_incbgk_nodyn, "dstate_incbgk_nodyn", 4)
 
 
+def case_sparse_dstate_sealed_channel():
+    """Dynamic content of a sparse lattice: one component per kept block."""
+    return _dynamic_state(case_sparse_sealed_channel, "sparse_dstate_sealed_channel", 4)
+
+
 def case_doctest_cavity20():
     return doctest_cavity(20, 20, 20, name="doctest_cavity20")
 
@@ -562,7 +567,7 @@ CASES = [
     case_external_mebb_periodic, case_binary_channel_sphere, case_binary_guo_periodic,
     case_sparse_sealed_channel, case_state_periodic_multiblock, case_state_guo_multiblock,
     case_dstate_channel_sphere_multiblock, case_dstate_velocity_box, case_dstate_zhpress_faces,
-    case_dstate_guo_channel, case_dstate_incbgk_nodyn,
+    case_dstate_guo_channel, case_dstate_incbgk_nodyn, case_sparse_dstate_sealed_channel,
 ]
 
 

@@ -111,8 +111,16 @@ def test_reference_loads_single_component_state(name):
 # ---------------------------------------------------------------- states with dynamic content
 
 DSTATES = ["dstate_channel_sphere_multiblock", "dstate_velocity_box", "dstate_zhpress_faces",
-           "dstate_guo_channel", "dstate_incbgk_nodyn"]
-SINGLE_COMPONENT = DSTATES[1:]
+           "dstate_guo_channel", "dstate_incbgk_nodyn", "sparse_dstate_sealed_channel"]
+SINGLE_COMPONENT = DSTATES[1:5]
+
+
+def _kinds(g):
+    """The case's kinds, 255 outside the lattice of a sparse case."""
+    kinds = g["flags"].copy()
+    if "in_lattice" in g:
+        kinds[~g["in_lattice"].astype(bool)] = 255
+    return kinds
 
 
 def _shape(meta):
@@ -127,8 +135,12 @@ def _density_kind(k):
     return 12 <= k < 18 or 24 <= k < 30
 
 
-def _masks(g, meta):
-    return O.OracleLattice.from_golden(g, meta).mebb_masks().reshape(_shape(meta))
+def _masks(g, meta, kinds=None):
+    if kinds is None:
+        return O.OracleLattice.from_golden(g, meta).mebb_masks().reshape(_shape(meta))
+    ol = O.OracleLattice(meta["nx"], meta["ny"], meta["nz"], meta["periodic"], meta["omega"], kinds, g["bcval"],
+                         g["force"], meta["rho0"], meta["bb_rho"])
+    return ol.mebb_masks().reshape(_shape(meta))
 
 
 @pytest.mark.parametrize("name", DSTATES)
@@ -138,13 +150,14 @@ def test_reference_dynamic_state_decodes(name):
     parameters, and its static values are the final populations."""
     g, meta = goldens.load(name)
     st = O.read_dynamic_state(str(g["dstate_plb"]), bytes(g["dstate_dat"]), _shape(meta))
-    kinds = g["flags"]
-    assert np.array_equal(st["kinds"], kinds)
+    kinds = _kinds(g)
+    assert np.array_equal(st["kinds"], kinds)   # a sparse state holds the kept blocks only
     vel = np.vectorize(_velocity_kind)(kinds)
     den = np.vectorize(_density_kind)(kinds)
     assert np.array_equal(st["bc"][vel], g["bcval"][vel])
     assert np.array_equal(st["bc"][den][:, 0], g["bcval"][den][:, 0])
-    assert np.array_equal(st["records"], records(g, meta).reshape(st["records"].shape))
+    inside = kinds != 255
+    assert np.array_equal(st["records"][inside], records(g, meta).reshape(st["records"].shape)[inside])
     assert st["omegas"] == {meta["omega"]}
     if (kinds == 2).any():
         assert st["inv_rho0s"] == {1.0 / meta["rho0"]}
@@ -152,7 +165,7 @@ def test_reference_dynamic_state_decodes(name):
         assert st["rhos"] == {meta["bb_rho"]}
     mebb = kinds == 4
     if mebb.any():
-        assert np.array_equal(st["masks"][mebb], _masks(g, meta)[mebb])
+        assert np.array_equal(st["masks"][mebb], _masks(g, meta, kinds)[mebb])
 
 
 @pytest.mark.parametrize("name", SINGLE_COMPONENT)
@@ -172,7 +185,7 @@ def test_dynamic_state_writer_reproduces_reference_bytes(name):
 
 @pytest.mark.skipif(not os.path.exists(DRIVER), reason="reference driver not built (needs the reference sources)")
 @pytest.mark.parametrize("name", ["dstate_channel_sphere_multiblock", "dstate_velocity_box", "dstate_zhpress_faces",
-                                  "dstate_incbgk_nodyn"])
+                                  "dstate_incbgk_nodyn", "sparse_dstate_sealed_channel"])
 def test_reference_loads_dynamic_state(name):
     """A state written the way plbgpu_save_state_dynamic writes it (one
     component, the library's own ids) is loaded by the reference's
@@ -185,7 +198,8 @@ def test_reference_loads_dynamic_state(name):
     cd = 22 if meta["forced"] else 19
     recs = g["f_init"] if not meta["forced"] else np.concatenate([g["f_init"], g["force"]], axis=-1)
     with tempfile.TemporaryDirectory() as tmp:
-        plb, dat = O.dynamic_state_files(g["flags"], g["bcval"], _masks(g, meta), recs, cd,
+        kinds = _kinds(g)
+        plb, dat = O.dynamic_state_files(kinds, g["bcval"], _masks(g, meta, kinds), recs, cd,
                                          "ForcedD3Q19" if meta["forced"] else "D3Q19", os.path.join(tmp, "s.dat"),
                                          meta["omega"], meta["rho0"], meta["bb_rho"])
         with open(os.path.join(tmp, "s.plb"), "w") as f:
@@ -202,4 +216,8 @@ def test_reference_loads_dynamic_state(name):
                        env=dict(os.environ, PLB_LOAD_DYNAMIC_STATE=os.path.join(tmp, "s.plb")))
         res = lbcases.read_result_file(rpath, spec)
     assert np.array_equal(res["f_init"], g["f_init"])
-    assert np.array_equal(res["f_final"], g["f_final"])
+    # A sparse lattice's blocks keep envelope cells facing the dropped blocks,
+    # which are in no state and collide with the lattice's own background
+    # dynamics: the fluid sealed off from them is compared.
+    cmp = g["compare"].astype(bool) if "compare" in g else np.ones(g["flags"].shape, bool)
+    assert np.array_equal(res["f_final"][cmp], g["f_final"][cmp])

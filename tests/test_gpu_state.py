@@ -183,3 +183,31 @@ def test_dynamic_state_round_trip_and_refusals(tmp_path):
     with pytest.raises(PlbGpuError):
         other.load_state_dynamic(str(tmp_path / "a.plb"))
     assert np.array_equal(other.get_kinds(), g["flags"])                     # nothing changed
+
+
+def test_sparse_dynamic_state(tmp_path):
+    """The reference's state of a sparse lattice (one component per kept
+    block) loads into the GPU's sparse domain on the same blocks; the GPU's
+    save writes the cells outside the lattice as NoDynamics with zero
+    populations, as restated (the reference skips them when loading)."""
+    g, meta = goldens.load("sparse_dstate_sealed_channel")
+    shape = (meta["nx"], meta["ny"], meta["nz"])
+    lat = lattice_from_description(*shape, meta["periodic"], meta["omega"], g["flags"], g["bcval"], g["force"],
+                                   sparse=(g["sparse"], meta["blocks"]))
+    ref_plb = _reference_files(g, tmp_path)
+    lat.load_state_dynamic(ref_plb)
+    inside = g["in_lattice"].astype(bool)
+    kinds = lat.get_kinds()
+    assert np.array_equal(kinds[inside], g["flags"][inside]) and (kinds[~inside] == 255).all()
+    f = lat.receive()
+    assert np.array_equal(f[inside], g["f_final"][inside]) and not f[~inside].any()
+    base = str(tmp_path / "s")
+    lat.save_state_dynamic(base)
+    ol = O.OracleLattice(*shape, meta["periodic"], meta["omega"], kinds, g["bcval"], g["force"], meta["rho0"],
+                         meta["bb_rho"])
+    plb, dat = O.dynamic_state_files(kinds, g["bcval"], ol.mebb_masks().reshape(shape), f, 19, "D3Q19",
+                                     base + ".dat", meta["omega"], meta["rho0"], meta["bb_rho"])
+    assert open(base + ".plb").read() == plb
+    assert open(base + ".dat", "rb").read() == dat
+    with pytest.raises(PlbGpuError):   # a dense lattice: the kept blocks do not cover it
+        DeviceLattice3D(*shape, 1.0).load_state_dynamic(ref_plb)
