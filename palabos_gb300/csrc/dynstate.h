@@ -20,7 +20,8 @@
 //   Boundary_*Density_d_o,          rhoBar, bool, then the base (boundaryDynamics.hh:238-242)
 //   Boundary_ZouHePressure_d_o
 //
-// Host-only C++ (no CUDA), used by the library's state reader and writer.
+// Host-only C++ (no CUDA), used by the library's state reader and writer;
+// tests/cpp/dynstate_check.cpp re-encodes states the reference wrote with it.
 #pragma once
 
 #include <cmath>
@@ -122,9 +123,18 @@ constexpr int kOutside = 255;
 // fluid directions (bit i for direction i).  A cell outside the lattice is
 // written as NoDynamics (its populations are zero): a reference lattice built
 // on the same sparse blocks has no cell there and ignores it on loading.
-inline void appendCell(std::vector<char>& out, int k, const double* bc, uint32_t mask, const Params& p) {
+// ids: the registry ids to write by dynamics name (default: kindId / kBgkId).
+inline void appendCell(std::vector<char>& out, int k, const double* bc, uint32_t mask, const Params& p,
+                       const std::map<std::string, int>* ids = nullptr) {
     if (k == kOutside) k = PLBGPU_NODYNAMICS;
-    ChainWriter w(out, kindId(k));
+    auto idOf = [ids](const std::string& name, int dflt) {
+        if (ids) {
+            auto it = ids->find(name);
+            if (it != ids->end()) return it->second;
+        }
+        return dflt;
+    };
+    ChainWriter w(out, idOf(kindName(k), kindId(k)));
     if (k == PLBGPU_BGK || k == PLBGPU_GUO) {
         w.value(p.omega);
     } else if (k == PLBGPU_INCBGK) {
@@ -149,7 +159,7 @@ inline void appendCell(std::vector<char>& out, int k, const double* bc, uint32_t
             w.value(bc[2]);
         }
         w.value((bool)(k >= PLBGPU_VELOCITY_EDGE));   // edges and corners prepare themselves
-        w.next(kBgkId);
+        w.next(idOf("BGK", kBgkId));
         w.value(p.omega);
     }
 }

@@ -221,3 +221,30 @@ def test_reference_loads_dynamic_state(name):
     # dynamics: the fluid sealed off from them is compared.
     cmp = g["compare"].astype(bool) if "compare" in g else np.ones(g["flags"].shape, bool)
     assert np.array_equal(res["f_final"][cmp], g["f_final"][cmp])
+
+
+@pytest.fixture(scope="module")
+def dynstate_check(tmp_path_factory):
+    """tests/cpp/dynstate_check.cpp built with the host compiler."""
+    import shutil
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    exe = str(tmp_path_factory.mktemp("cpp") / "dynstate_check")
+    subprocess.run([cxx, "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "dynstate_check.cpp"), "-o", exe], check=True)
+    return exe
+
+
+@pytest.mark.parametrize("name", DSTATES)
+def test_library_state_codec_reencodes_reference_bytes(name, dynstate_check, tmp_path):
+    """The library's own C++ codec (palabos_gb300/csrc/dynstate.h) decodes
+    every cell of the reference's state and, under the state's ids, encodes
+    it back to the same bytes."""
+    g, meta = goldens.load(name)
+    plb, dat = tmp_path / "s.plb", tmp_path / "s.dat"
+    plb.write_text(str(g["dstate_plb"]))
+    dat.write_bytes(bytes(g["dstate_dat"]))
+    out = subprocess.run([dynstate_check, str(plb), str(dat), str(meta["nx"]), str(meta["ny"]), str(meta["nz"])],
+                         capture_output=True, text=True)
+    assert out.returncode == 0 and out.stdout.startswith("ok "), out.stdout
