@@ -1,32 +1,37 @@
-"""GPU voxelizer against the oracle's restatement of the reference's
+"""GPU voxelizer against the reference's own voxel flags
+(tests/golden/voxel_reference.npz) and the oracle's restatement of its
 voxelize() (flood fill with segment crossings), and the voxelized-domain
 pipeline (kinds, sparse blocks) against the oracle's block selection."""
+import os
+
 import numpy as np
 import pytest
 
 import oracle as O
 from palabos_gb300 import DeviceLattice3D, PlbGpuError, meshes, voxel
 from palabos_gb300 import native as N
+from voxcases import CASES, WIDTHS
 
 pytestmark = pytest.mark.gpu
 
-CASES = {
-    "sphere": (lambda: meshes.sphere((15.3, 16.7, 14.1), 9.2, 1280), (32, 34, 30)),
-    "sphere_integer_centre": (lambda: meshes.sphere((16.0, 15.0, 17.0), 8.0, 320), (33, 31, 35)),
-    "box_fractional": (lambda: meshes.cuboid((5.5, 6.25, 4.75), (20.5, 18.25, 22.75), (3, 2, 4)), (28, 26, 30)),
-    "box_on_cell_centres": (lambda: meshes.cuboid((5, 6, 4), (20, 18, 22), (3, 2, 4)), (28, 26, 30)),
-    "two_bodies": (lambda: meshes.merge(meshes.sphere((11.2, 15.3, 14.6), 6.1, 320),
-                                        meshes.cuboid((23.31, 8.62, 9.41), (33.57, 21.38, 19.66))), (40, 30, 30)),
-    "thin_box": (lambda: meshes.cuboid((3.37, 4.21, 5.62), (30.41, 5.83, 22.29), (5, 1, 3)), (34, 12, 28)),
-}
+VOXEL_GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "voxel_reference.npz")
 
 
-@pytest.mark.parametrize("width", [0, 1, 2])
+@pytest.mark.parametrize("width", WIDTHS)
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_gpu_voxelizer_matches_oracle(name, width):
     make, shape = CASES[name]
     tri = make()
     assert np.array_equal(voxel.voxelize(tri, shape, width), O.voxelize(tri, shape, width))
+
+
+@pytest.mark.parametrize("width", WIDTHS)
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_gpu_voxelizer_matches_reference(name, width):
+    """The reference's own voxel flags of the same meshes."""
+    g = np.load(VOXEL_GOLDEN)
+    tri, shape = g[f"{name}__tri"], tuple(g[f"{name}__shape"])
+    assert np.array_equal(voxel.voxelize(tri, shape, width), g[f"{name}__w{width}"])
 
 
 def test_gpu_voxelizer_counts_edge_touches_as_touches():

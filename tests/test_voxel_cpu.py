@@ -1,12 +1,14 @@
 """Mesh generators and the oracle's restatement of the reference voxelizer,
+against the reference's own voxel flags (tests/golden/voxel_reference.npz,
+made by tests/golden/make_voxel_golden.py from oracle/_ref/plb_voxel) and
 against geometry whose answer is known: analytic spheres and boxes.
-
-The reference's own voxelizer (offLattice/voxelizer.hh) does not compile from
-this snapshot, so its restatement is pinned by these known answers instead
-of golden files.
 """
+import os
+
 import numpy as np
 import pytest
+
+import voxcases
 
 import oracle as O
 from palabos_gb300 import meshes, voxel
@@ -116,3 +118,31 @@ def test_stl_round_trip_and_lattice_units(tmp_path, binary):
     assert np.allclose(origin + dx * lu.reshape(-1, 3), back.reshape(-1, 3))
     flags = O.voxelize(lu, (50, 50, 50))
     assert np.isin(flags[23, 23, 23], (voxel.INSIDE,))
+
+
+VOXEL_GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "voxel_reference.npz")
+
+
+@pytest.mark.parametrize("width", voxcases.WIDTHS)
+@pytest.mark.parametrize("name", sorted(voxcases.CASES))
+def test_oracle_voxelizer_matches_reference(name, width):
+    """The restated flood gives the reference's voxel flags cell for cell:
+    spheres (generic and integer centres, vertices on cell centres), boxes
+    with fractional and integer faces, two bodies, a thin slab."""
+    g = np.load(VOXEL_GOLDEN)
+    tri, shape = g[f"{name}__tri"], tuple(g[f"{name}__shape"])
+    assert np.array_equal(O.voxelize(tri, shape, width), g[f"{name}__w{width}"])
+
+
+def test_reference_flood_misreads_edge_touches():
+    """The reference on a thin box whose edges lie exactly on the flood's
+    diagonal neighbour segments: it merges the two equal-distance crossings
+    of such a touch into one, flips the flag and marks cells wrongly, so its
+    inside set is not the box (the GPU counts the touch as no crossing and
+    gives the box, tests/test_gpu_voxel.py)."""
+    g = np.load(VOXEL_GOLDEN)
+    lo, hi, _, shape = voxcases.EDGE_TOUCH
+    X, Y, Z = np.meshgrid(*(np.arange(n) for n in shape), indexing="ij")
+    box = (X > lo[0]) & (X < hi[0]) & (Y > lo[1]) & (Y < hi[1]) & (Z > lo[2]) & (Z < hi[2])
+    inside = np.isin(g["edge_touch__w1"], (3, 4))
+    assert (inside != box).sum() > 0
