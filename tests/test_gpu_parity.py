@@ -131,8 +131,10 @@ def test_multistep_calls_and_odd_parity_transfers(name):
 @pytest.mark.parametrize("name", ["velocity_box", "channel_sphere", "guo_channel", "zhpress_faces"])
 def test_long_call_replays_steps_like_single_steps(name, precision):
     """A long collide_and_stream call replays its middle steps from a CUDA
-    graph; the result, the statistics of its last step and the parity equal
-    those of one call per step."""
+    graph; the result and the parity equal those of one call per step, the
+    statistics of its last step agree to the rounding of their summation (the
+    per-block partial sums of the interior and border rows, which run on two
+    streams, meet in FP64 atomic adds whose order varies from run to run)."""
     g, meta = goldens.load(name)
     n = 1 + 16 * 3 + 5
     runs = []
@@ -144,7 +146,8 @@ def test_long_call_replays_steps_like_single_steps(name, precision):
         runs.append((lat.receive(), lat.internal_statistics()["raw"]))
         lat.close()
     assert np.array_equal(runs[0][0], runs[1][0])
-    assert np.array_equal(runs[0][1], runs[1][1])
+    ok, worst = goldens.stats_close(runs[0][1], runs[1][1])
+    assert ok, worst
 
 
 def test_velocity_condition_on_block_boundaries_sets_faces_edges_corners():
