@@ -248,3 +248,25 @@ def test_library_state_codec_reencodes_reference_bytes(name, dynstate_check, tmp
     out = subprocess.run([dynstate_check, str(plb), str(dat), str(meta["nx"]), str(meta["ny"]), str(meta["nz"])],
                          capture_output=True, text=True)
     assert out.returncode == 0 and out.stdout.startswith("ok "), out.stdout
+
+
+@pytest.mark.parametrize("damage", ["truncated", "unknown_id", "bad_run", "extra_bytes"])
+def test_library_state_codec_rejects_damaged_states(damage, dynstate_check, tmp_path):
+    """A damaged state is reported as an error, not read past its end: a
+    truncated data file, a dynamics id missing from the DynamicsDict, a run
+    whose count exceeds the dynamics' values, bytes beyond the last cell."""
+    g, meta = goldens.load("dstate_velocity_box")
+    plb, dat = str(g["dstate_plb"]), bytearray(bytes(g["dstate_dat"]))
+    if damage == "truncated":
+        dat = dat[:len(dat) // 2]
+    elif damage == "unknown_id":
+        dat[4:8] = (9999).to_bytes(4, "little")          # id of the first cell's outer dynamics
+    elif damage == "bad_run":
+        dat[16:20] = (1000).to_bytes(4, "little")        # count of its first run of values
+    else:
+        dat += b"\0" * 8
+    (tmp_path / "s.plb").write_text(plb)
+    (tmp_path / "s.dat").write_bytes(bytes(dat))
+    out = subprocess.run([dynstate_check, str(tmp_path / "s.plb"), str(tmp_path / "s.dat"), str(meta["nx"]),
+                          str(meta["ny"]), str(meta["nz"])], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 1 and out.stdout.startswith("FAIL"), (out.returncode, out.stdout)
