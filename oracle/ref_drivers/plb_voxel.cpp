@@ -2,6 +2,10 @@
 // voxelize(mesh, domain, borderWidth) (offLattice/voxelizer.hh:106-141) on a
 // triangle set given in lattice units.
 //
+//   plb_voxel --stl <file.stl> <flt|dbl> <result>
+//   result: "PLBTRI01", int32 n, float64 triangles[n][3][3] -- what
+//           TriangleSet<double>(file, precision) read (offLattice/triangleSet.hh:70-345)
+//
 //   plb_voxel <case> <result>
 //   case:   "PLBVOX01", int32 nx, ny, nz, borderWidth, nTriangles,
 //           float64 triangles[nTriangles][3][3] (vertex, then x, y, z)
@@ -51,7 +55,21 @@ static void die(const char* m) {
 
 int main(int argc, char** argv) {
     plbInit(&argc, &argv);
-    if (argc != 3) die("usage: plb_voxel <case> <result>");
+    if (argc == 5 && std::strcmp(argv[1], "--stl") == 0) {
+        TriangleSet<double> set(argv[2], std::strcmp(argv[3], "dbl") == 0 ? DBL : FLT);
+        std::vector<TriangleSet<double>::Triangle> const& t = set.getTriangles();
+        FILE* o = std::fopen(argv[4], "wb");
+        if (!o) die("cannot open result");
+        const int32_t n = (int32_t)t.size();
+        std::fwrite("PLBTRI01", 1, 8, o);
+        std::fwrite(&n, sizeof(n), 1, o);
+        for (int32_t i = 0; i < n; ++i)
+            for (int k = 0; k < 3; ++k)
+                for (int a = 0; a < 3; ++a) std::fwrite(&t[i][k][a], sizeof(double), 1, o);
+        std::fclose(o);
+        return 0;
+    }
+    if (argc != 3) die("usage: plb_voxel <case> <result> | plb_voxel --stl <file> <flt|dbl> <result>");
     FILE* f = std::fopen(argv[1], "rb");
     if (!f) die("cannot open case");
     char magic[8];

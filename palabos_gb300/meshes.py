@@ -85,21 +85,45 @@ def merge(*meshes):
     return np.concatenate([np.asarray(m, np.float64).reshape(-1, 3, 3) for m in meshes])
 
 
-def read_stl(path):
-    """Triangles (t, 3, 3) of an ASCII or binary STL file (what the reference's
-    TriangleSet reads, offLattice/triangleSet.hh), vertices in file order."""
+def read_stl(path, precision="flt"):
+    """Triangles (t, 3, 3) of an ASCII or binary STL file as the reference's
+    TriangleSet(fname, precision) reads them (offLattice/triangleSet.hh:70-345):
+    vertices in file order, except that a facet whose vertex order disagrees
+    with its stored normal gets its last two vertices swapped, and a facet
+    with an edge or an area within 2 eps of zero is dropped
+    (checkForDegenerateTrianglesAndFixOrientationNoAbort, :498-548), eps = 10x
+    the machine epsilon of `precision`, "flt" (the constructor's default) or
+    "dbl" (core/globalDefs.h:104-126)."""
     with open(path, "rb") as f:
         data = f.read()
+    tri = nrm = None
     if len(data) >= 84:
         count = int(np.frombuffer(data, "<u4", 1, 80)[0])
         if 84 + 50 * count == len(data):
-            rec = np.dtype([("n", "<f4", 3), ("v", "<f4", (3, 3)), ("attr", "<u2")])
-            return np.frombuffer(data, rec, count, 84)["v"].astype(np.float64)
-    text = data.decode("ascii", errors="replace").split()
-    verts = [text[i + 1:i + 4] for i, w in enumerate(text) if w == "vertex"]
-    if not verts or len(verts) % 3:
-        raise ValueError(f"{path}: not an STL file")
-    return np.array(verts, np.float64).reshape(-1, 3, 3)
+            rec = np.frombuffer(data, np.dtype([("n", "<f4", 3), ("v", "<f4", (3, 3)), ("attr", "<u2")]), count, 84)
+            tri, nrm = rec["v"].astype(np.float64), rec["n"].astype(np.float64)
+    if tri is None:
+        text = data.decode("ascii", errors="replace").split()
+        verts = [text[i + 1:i + 4] for i, w in enumerate(text) if w == "vertex"]
+        norms = [text[i + 1:i + 4] for i, w in enumerate(text) if w == "normal"]
+        if not verts or len(verts) % 3 or len(norms) * 3 != len(verts):
+            raise ValueError(f"{path}: not an STL file")
+        tri = np.array(verts, np.float64).reshape(-1, 3, 3)
+        nrm = np.array(norms, np.float64).reshape(-1, 3)
+    eps = 10.0 * float(np.finfo(np.float32 if precision == "flt" else np.float64).eps)
+
+    def norm(v):
+        return np.sqrt((v[:, 0] * v[:, 0] + v[:, 1] * v[:, 1]) + v[:, 2] * v[:, 2])
+
+    v01, v02, v12 = tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0], tri[:, 2] - tri[:, 1]
+    cn = np.stack([v01[:, 1] * v02[:, 2] - v01[:, 2] * v02[:, 1],
+                   v01[:, 2] * v02[:, 0] - v01[:, 0] * v02[:, 2],
+                   v01[:, 0] * v02[:, 1] - v01[:, 1] * v02[:, 0]], axis=1)
+    keep = (norm(v01) > 2 * eps) & (norm(v02) > 2 * eps) & (norm(v12) > 2 * eps) & (norm(cn) > 2 * eps)
+    dot = (cn[:, 0] * nrm[:, 0] + cn[:, 1] * nrm[:, 1]) + cn[:, 2] * nrm[:, 2]
+    tri = tri.copy()
+    tri[dot < 0] = tri[dot < 0][:, [0, 2, 1]]
+    return tri[keep]
 
 
 def write_stl(path, triangles, binary=True):

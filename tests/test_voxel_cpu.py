@@ -146,3 +146,57 @@ def test_reference_flood_misreads_edge_touches():
     box = (X > lo[0]) & (X < hi[0]) & (Y > lo[1]) & (Y < hi[1]) & (Z > lo[2]) & (Z < hi[2])
     inside = np.isin(g["edge_touch__w1"], (3, 4))
     assert (inside != box).sum() > 0
+
+
+PLB_VOXEL = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref", "plb_voxel")
+
+
+def _awkward_facets():
+    """A sphere plus facets the reference's reader treats specially: stored
+    normals opposite to the vertex order, a repeated vertex, collinear
+    vertices, and a 1e-6 edge (dropped at FLT precision, kept at DBL)."""
+    tri = meshes.sphere((4.1, 3.7, 5.2), 2.5, 80)
+    extra = np.array([[[3.0, 3.0, 3.0], [3.0, 3.0, 3.0], [4.0, 3.0, 3.0]],
+                      [[1.0, 1.0, 1.0], [2.0, 2.0, 2.0], [3.0, 3.0, 3.0]],
+                      [[3.0, 4.0, 5.0], [3.000001, 4.0, 5.0], [3.0, 5.0, 5.0]]])
+    tri = np.concatenate([tri, extra])
+    cn = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+    nrm = cn / np.maximum(np.linalg.norm(cn, axis=1, keepdims=True), 1e-300)
+    nrm[::7] *= -1.0
+    return tri, nrm
+
+
+def _write(path, tri, nrm, binary):
+    if binary:
+        rec = np.zeros(len(tri), np.dtype([("n", "<f4", 3), ("v", "<f4", (3, 3)), ("attr", "<u2")]))
+        rec["n"], rec["v"] = nrm, tri
+        with open(path, "wb") as f:
+            f.write(b"binary".ljust(80, b" ") + np.uint32(len(tri)).tobytes() + rec.tobytes())
+    else:
+        lines = ["solid awkward"]
+        for t, n in zip(tri, nrm):
+            lines += ["  facet normal " + " ".join(repr(float(x)) for x in n), "    outer loop"]
+            lines += ["      vertex " + " ".join(repr(float(x)) for x in v) for v in t]
+            lines += ["    endloop", "  endfacet"]
+        with open(path, "w") as f:
+            f.write("\n".join(lines + ["endsolid awkward", ""]))
+
+
+@pytest.mark.skipif(not os.path.exists(PLB_VOXEL), reason="reference driver not built (needs the reference sources)")
+@pytest.mark.parametrize("precision", ["flt", "dbl"])
+@pytest.mark.parametrize("binary", [True, False])
+def test_read_stl_matches_reference_reader(binary, precision, tmp_path):
+    """read_stl gives the triangles the reference's TriangleSet(fname,
+    precision) reads from the same file: same order and values, facets with
+    reversed normals reoriented, degenerate facets dropped."""
+    import subprocess
+    tri, nrm = _awkward_facets()
+    path, out = str(tmp_path / "m.stl"), str(tmp_path / "r")
+    _write(path, tri, nrm, binary)
+    subprocess.run([PLB_VOXEL, "--stl", path, precision, out], check=True, capture_output=True)
+    data = open(out, "rb").read()
+    assert data[:8] == b"PLBTRI01"
+    n = int(np.frombuffer(data, "<i4", 1, 8)[0])
+    ref = np.frombuffer(data, "<f8", n * 9, 12).reshape(n, 3, 3)
+    got = meshes.read_stl(path, precision)
+    assert got.shape == ref.shape and np.array_equal(got, ref)
