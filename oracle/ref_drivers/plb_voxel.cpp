@@ -6,6 +6,11 @@
 //   result: "PLBTRI01", int32 n, float64 triangles[n][3][3] -- what
 //           TriangleSet<double>(file, precision) read (offLattice/triangleSet.hh:70-345)
 //
+//   plb_voxel --scale <file.stl> <resolution> <referenceDirection> <margin> <extraLayer> <result>
+//   result: "PLBTRI01", as above -- the triangles of DEFscaledMesh(TriangleSet<double>(file, DBL),
+//           resolution, referenceDirection, margin, extraLayer) in lattice units
+//           (offLattice/triangleBoundary3D.hh:255-300, triangularSurfaceMesh.hh:1552-1575)
+//
 //   plb_voxel <case> <result>
 //   case:   "PLBVOX01", int32 nx, ny, nz, borderWidth, nTriangles,
 //           float64 triangles[nTriangles][3][3] (vertex, then x, y, z)
@@ -66,6 +71,25 @@ int main(int argc, char** argv) {
         for (int32_t i = 0; i < n; ++i)
             for (int k = 0; k < 3; ++k)
                 for (int a = 0; a < 3; ++a) std::fwrite(&t[i][k][a], sizeof(double), 1, o);
+        std::fclose(o);
+        return 0;
+    }
+    if (argc == 8 && std::strcmp(argv[1], "--scale") == 0) {
+        TriangleSet<double> set(argv[2], DBL);
+        DEFscaledMesh<double> scaled(set, std::atol(argv[3]), std::atol(argv[4]), std::atol(argv[5]),
+                                     (plint)std::atol(argv[6]));
+        TriangularSurfaceMesh<double> const& mesh = scaled.getMesh();
+        FILE* o = std::fopen(argv[7], "wb");
+        if (!o) die("cannot open result");
+        const int32_t n = (int32_t)mesh.getNumTriangles();
+        std::fwrite("PLBTRI01", 1, 8, o);
+        std::fwrite(&n, sizeof(n), 1, o);
+        for (int32_t i = 0; i < n; ++i)
+            for (int k = 0; k < 3; ++k)
+                for (int a = 0; a < 3; ++a) {
+                    const double v = mesh.getVertex(i, k)[a];
+                    std::fwrite(&v, sizeof(double), 1, o);
+                }
         std::fclose(o);
         return 0;
     }

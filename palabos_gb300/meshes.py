@@ -127,7 +127,11 @@ def read_stl(path, precision="flt"):
 
 
 def write_stl(path, triangles, binary=True):
-    """Write triangles (t, 3, 3) as a binary (or ASCII) STL file."""
+    """Write triangles (t, 3, 3) as a binary (or ASCII) STL file.  ASCII
+    vertices are written in the shortest text that reads back to the same
+    double, and the first facet is kept short: the reference's reader takes a
+    file for ASCII only if "endfacet" appears within the 256 bytes after byte
+    80 (offLattice/triangleSet.hh:120-160, PLB_CBUFSIZ)."""
     tri = np.asarray(triangles, np.float64).reshape(-1, 3, 3)
     n = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
     n /= np.maximum(np.linalg.norm(n, axis=1, keepdims=True), 1e-300)
@@ -140,10 +144,10 @@ def write_stl(path, triangles, binary=True):
     with open(path, "w") as f:
         f.write("solid mesh\n")
         for t, nn in zip(tri, n):
-            f.write(f"facet normal {nn[0]:.9e} {nn[1]:.9e} {nn[2]:.9e}\n outer loop\n")
+            f.write(f"facet normal {nn[0]:.6e} {nn[1]:.6e} {nn[2]:.6e}\nouter loop\n")
             for v in t:
-                f.write(f"  vertex {v[0]:.17e} {v[1]:.17e} {v[2]:.17e}\n")
-            f.write(" endloop\nendfacet\n")
+                f.write("vertex " + " ".join(repr(float(x)) for x in v) + "\n")
+            f.write("endloop\nendfacet\n")
         f.write("endsolid mesh\n")
 
 

@@ -200,3 +200,25 @@ def test_read_stl_matches_reference_reader(binary, precision, tmp_path):
     ref = np.frombuffer(data, "<f8", n * 9, 12).reshape(n, 3, 3)
     got = meshes.read_stl(path, precision)
     assert got.shape == ref.shape and np.array_equal(got, ref)
+
+
+@pytest.mark.skipif(not os.path.exists(PLB_VOXEL), reason="reference driver not built (needs the reference sources)")
+@pytest.mark.parametrize("binary", [True, False])
+def test_written_stl_scales_like_reference(binary, tmp_path):
+    """Files written by write_stl are read by the reference (ASCII included:
+    its reader's ASCII test looks for the first "endfacet" in a fixed window),
+    and to_lattice_units gives the triangles of the reference's
+    DEFscaledMesh(set, resolution, referenceDirection, margin, extraLayer)
+    bit for bit."""
+    import subprocess
+    tri = meshes.merge(meshes.sphere((4.1, 3.7, 5.2), 2.5, 320), meshes.cuboid((7.3, 1.2, 2.2), (9.9, 4.4, 8.1)))
+    path, out = str(tmp_path / "m.stl"), str(tmp_path / "r")
+    meshes.write_stl(path, tri, binary=binary)
+    for res, direction, margin, extra in [(40, 0, 0, 0), (64, 1, 2, 1), (33, 2, 3, 0)]:
+        subprocess.run([PLB_VOXEL, "--scale", path, str(res), str(direction), str(margin), str(extra), out],
+                       check=True, capture_output=True)
+        data = open(out, "rb").read()
+        n = int(np.frombuffer(data, "<i4", 1, 8)[0])
+        ref = np.frombuffer(data, "<f8", n * 9, 12).reshape(n, 3, 3)
+        got = meshes.to_lattice_units(meshes.read_stl(path, "dbl"), res, direction, margin + extra)[0]
+        assert got.shape == ref.shape and np.array_equal(got, ref)
