@@ -14,8 +14,13 @@ no explicit flush is needed between steps.
 
 Prints one JSON line (rank 0).  `value` = MLUPS of the FP64 form with the
 state resident in HBM; `e2e` = the same metric through the C ABI with host
-buffers (state sent from pinned host memory at the start, drag read back every
-100 steps, state received at the end, all inside the timed region).
+buffers (the FP64 state in an ordinary, pageable host array -- sent at the
+start, drag read back every 100 steps, state received at the end into the same
+array, all inside the timed region; on a GB300 the transfer kernels read and
+write the host array directly over NVLink-C2C).  The FP64 form is bound by the
+FP64 pipe, not by HBM: its `roofline` compares the algorithmic FP64 adds and
+multiplies per second with the pipe rate the library measures in the same run
+(plbgpu_measure_fp64_rate), and carries the HBM fraction beside it.
 """
 from __future__ import annotations
 
@@ -41,6 +46,10 @@ FALLBACK_HBM_GBS = 6800.0
 # Algorithmic bytes per cell and step (AA pattern: every population read once
 # and written once, plus the one-byte cell kind).
 B_CELL = {"fp64": 305, "fp32": 153, "bf16": 77, "fp16": 77, "bf16sr": 77}
+# Algorithmic FP64 adds and multiplies of one BGK collision in the reference's
+# operand order (dynamicsTemplates3D.h:2289-2366, momentTemplates3D.h:351-365):
+# moments 37 adds, 1 / (rho-bar + 1) one add and one division, collision 137.
+FP64_OPS_BGK = 176
 
 
 def workload_geometry():
@@ -61,8 +70,11 @@ def algorithmic_bytes(kinds, precision):
     cells = kinds.size
     faces = int(((kinds >= N.REG_VELOCITY) & (kinds < N.VELOCITY_EDGE)).sum())
     mebb = int((kinds == N.MOMENTUM_EXCHANGE).sum())
+    # cells that run a BGK collision (bulk, faces, edges, corners)
+    colliding = int(((kinds == N.BGK) | (kinds == N.GUO) | (kinds == N.INCBGK)
+                     | ((kinds >= N.REG_VELOCITY) & (kinds < N.NKINDS))).sum())
     # faces also read their 3 FP64 boundary values
-    return cells * B_CELL[precision] + faces * 24, dict(cells=cells, faces=faces, mebb=mebb)
+    return cells * B_CELL[precision] + faces * 24, dict(cells=cells, faces=faces, mebb=mebb, colliding=colliding)
 
 
 def load_peaks():
@@ -304,27 +316,38 @@ def run_gpu(args):
     k_ms = time_form(lat, min(K, 400), 10) / min(K, 400)
     achieved = bytes_step / (k_ms * 1e-3) / 1e9
     traffic = load_traffic(f"stepKernel_{head}_channel_sphere")
+    fp64_rate = ctx.fp64_rate() if head == "fp64" else None
 
-    # e2e through the C ABI with host buffers
-    f_host = lat.receive()
+    # e2e through the C ABI with host buffers: an ordinary (pageable) host
+    # array holding the FP64 state, allocated and touched before the timed
+    # region, sent at the start and received into at the end
+    f_host = np.empty(SHAPE + (19,))
+    lat.receive(out=f_host)
     e2e_steps = K
     barrier(dist)
     t0 = time.perf_counter()
     lat.send(f_host)
+    t_sent = time.perf_counter()
     done = 0
     while done < e2e_steps:
         chunk = min(STATS_EVERY, e2e_steps - done)
         lat.collide_and_stream(chunk, stats=True)
         lat.internal_statistics()      # drag to the host (synchronizes)
         done += chunk
-    f_host = lat.receive()
-    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+    t_recv = time.perf_counter()
+    lat.receive(out=f_host)
+    t1 = time.perf_counter()
+    e2e_s = max_over_ranks(dist, t1 - t0)
     state_bytes = cells * 19 * 8   # the ABI exchanges FP64 f-bar
     nread = (e2e_steps + STATS_EVERY - 1) // STATS_EVERY
     e2e = {"value": round(ws * cells * e2e_steps / e2e_s / 1e6, 2), "unit": "MLUPS",
            "h2d_bytes_per_step": round(state_bytes / e2e_steps, 1),
            "d2h_bytes_per_step": round((state_bytes + 56 * nread) / e2e_steps, 1),
-           "note": "state sent once and received once per run of K steps; drag read every 100 steps"}
+           "h2d_gbs": round(state_bytes / (t_sent - t0) / 1e9, 1),
+           "d2h_gbs": round(state_bytes / (t1 - t_recv) / 1e9, 1),
+           "note": "FP64 state in a pageable host array, sent once and received once per run of K steps "
+                   "(read and written by the transfer kernels directly where the GPU uses the host's page "
+                   "tables, else staged in 64 MiB chunks); drag read every 100 steps"}
     lat.close()
 
     # the other storage forms on the same workload (kernel-only rate)
@@ -347,6 +370,31 @@ def run_gpu(args):
 
     adjoint = None if args.skip_adjoint else adjoint_cost(ctx)
 
+    kernel_name = (f"rowStepKernel+edgeRowStepKernel<{head}>: one fused collide+stream+faces step, AA pattern"
+                   if head in ("fp64", "fp32") else
+                   f"pairRowStepKernel+edgeRowStepKernel<{head}>: one fused collide+stream+faces step, AA pattern")
+    hbm = {"achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+           "traffic": traffic, "traffic_source": "committed ncu capture (profiles/ncu_traffic.json), "
+                                                 "scaled from the row kernel by cells; not measured in this run",
+           "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)", "bytes_per_launch": bytes_step}
+    if head == "fp64":
+        ops_step = FP64_OPS_BGK * counts["colliding"]
+        fp64_achieved = ops_step / (k_ms * 1e-3) / 1e12
+        fp64_peak = fp64_rate / 1e12
+        roofline = {"bound": "fp64", "achieved": round(fp64_achieved, 4), "peak": round(fp64_peak, 4),
+                    "unit": "TFLOP/s", "frac": round(fp64_achieved / fp64_peak, 4), "traffic": traffic,
+                    "kernel": kernel_name,
+                    "ops_per_launch": ops_step,
+                    "ops_per_cell": f"{FP64_OPS_BGK} FP64 adds and multiplies per colliding cell "
+                                    f"({counts['colliding']} of {cells} cells collide)",
+                    "peak_source": "measured in this run: plbgpu_measure_fp64_rate (independent DMUL/DADD chains, "
+                                   "every SM, CUDA events)",
+                    "hbm": hbm}
+    else:
+        roofline = {"bound": "hbm", **{k: hbm[k] for k in ("achieved", "peak", "unit", "frac", "traffic")},
+                    "kernel": kernel_name, **{k: hbm[k] for k in ("traffic_source", "peak_source",
+                                                                   "bytes_per_launch")}}
+
     if rank == 0:
         clocks = clk.summary()
         line = {
@@ -360,11 +408,7 @@ def run_gpu(args):
                        "drag_every": STATS_EVERY, "cells": cells, "faces": counts["faces"],
                        "mebb_cells": counts["mebb"], "l2": "state (637 MB) larger than L2, no flush",
                        "parallelism": f"replicas{ws}"},
-            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                         "frac": round(achieved / peak, 4), "traffic": traffic,
-                         "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
-                         "kernel": f"rowStepKernel+edgeRowStepKernel<{head}>: one fused collide+stream+faces step, AA pattern; traffic scaled from the row kernel by cells",
-                         "bytes_per_launch": bytes_step},
+            "roofline": roofline,
             "forms": forms,
             "adjoint": adjoint,
             "e2e": e2e,

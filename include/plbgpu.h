@@ -77,7 +77,12 @@ typedef struct plbgpu_ctx plbgpu_ctx;
 /* ------------------------------------------------------------ context */
 
 /* Create a context on CUDA device `device`.  Replaces the singleton
- * global::defaultCoProcessor3D<T>() (coProcessors/coProcessor3D.h:178-186). */
+ * global::defaultCoProcessor3D<T>() (coProcessors/coProcessor3D.h:178-186).
+ * Environment variables read here: PLBGPU_STAGED_TRANSFERS=1 (see
+ * plbgpu_send) and PLBGPU_ROW_KERNEL=cell, which makes the interior rows of
+ * every storage type run the one-cell-per-thread kernel instead of the
+ * paired or 128-bit vector kernels of the 2-byte forms (same results; a
+ * cross-check of the faster kernels). */
 int plbgpu_create(int device, plbgpu_ctx** out);
 int plbgpu_destroy(plbgpu_ctx* ctx);
 /* Message of the last failing call on this context ("" if none). */
@@ -86,6 +91,17 @@ const char* plbgpu_last_error(const plbgpu_ctx* ctx);
 int plbgpu_launch_count(const plbgpu_ctx* ctx, unsigned long long* count);
 /* The CUDA stream (cudaStream_t) all work of the context is issued on. */
 int plbgpu_get_stream(const plbgpu_ctx* ctx, void** stream);
+/* Measured rate of the GPU's FP64 pipe in adds + multiplies per second
+ * (independent DMUL/DADD chains on every SM, fastest of three launches).
+ * The FP64 step rounds every add and multiply of the reference's collision
+ * separately, so this rate, not HBM bandwidth, bounds it.  A measurement
+ * aid with no counterpart in the reference. */
+int plbgpu_measure_fp64_rate(plbgpu_ctx* ctx, double* ops_per_second);
+/* Wait for the context's work.  Also reports (once, then clears) a diverged
+ * state of any domain: PLBGPU_ERR_STATE when a step that gathered statistics
+ * met a NaN or an infinity in a cell's density or kinetic energy.
+ * plbgpu_receive and plbgpu_get_stats report it the same way; the domain stays
+ * usable (send a new state to continue). */
 int plbgpu_synchronize(plbgpu_ctx* ctx);
 
 /* ------------------------------------------------------------ domains */
@@ -182,7 +198,14 @@ int plbgpu_initialize(plbgpu_ctx* ctx, int handle);
 
 /* Host -> device / device -> host of the populations of a sub-box, FP64
  * f-bar, transfer layout above; n = number of doubles in buf (19 per cell).
- * CoProcessor3D::send / receive (coProcessors/coProcessor3D.h:80-96). */
+ * CoProcessor3D::send / receive (coProcessors/coProcessor3D.h:80-96).
+ * buf may be host memory (pageable or pinned) or device memory.  When the GPU
+ * can address buf -- device, managed or pinned memory, or pageable memory on
+ * a GPU that uses the host's page tables (GB300 with its Grace CPU) -- one
+ * kernel reads or writes it directly, coalesced; otherwise the records go
+ * through a device staging buffer of at most 64 MiB, chunk by chunk
+ * (environment variable PLBGPU_STAGED_TRANSFERS=1 at plbgpu_create forces
+ * this path).  Both calls return once buf may be reused. */
 int plbgpu_send(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1, int z0, int z1,
                 const double* buf, size_t n);
 int plbgpu_receive(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1, int z0, int z1,
@@ -407,9 +430,9 @@ int plbgpu_cp_collide_and_stream(plbgpu_ctx* ctx, int handle);
 
 /* Average energy and density of a lattice held in caller-owned device memory,
  * computed without allocating any device memory.  No counterpart in the
- * reference: it serves callers that cannot call cudaMalloc (work recorded into
- * a CUDA graph under capture, applications with their own device-memory pool
- * or a fixed budget).
+ * reference: it serves callers that cannot call cudaMalloc (applications with
+ * their own device-memory pool or a fixed budget, hosts where the runtime
+ * allocator is off limits).
  *
  * populations: 19 planes of FP64 f-bar, plane i at populations + i * stride,
  *              cell (x, y, z) at index (x * ny + y) * nz + z, post-stream
@@ -425,7 +448,9 @@ int plbgpu_cp_collide_and_stream(plbgpu_ctx* ctx, int handle);
  * process exits.  Sizes with nx * ny > PLBGPU_NOALLOC_MAX_ROWS are rejected
  * with PLBGPU_ERR_ARG.  All calls share the array; calls whose kernels overlap
  * on the GPU race on it.  The first call on a device looks up the array's
- * address with that device current: make it before any stream capture.
+ * address with that device current: make it before any stream capture.  The
+ * address is kept for the life of the process, so after a cudaDeviceReset of
+ * that device this entry point must not be called again.
  * Asynchronous: returns once both kernels are queued. */
 int plbgpu_reduce_noalloc(const double* populations, long long stride, const uint8_t* kinds, int nx, int ny,
                           int nz, double bb_rho, double rho0, double* result, void* stream);

@@ -76,10 +76,16 @@ class OracleLattice:
         self.p = _Params(nx, ny, nz, (ctypes.c_int * 3)(*[int(v) for v in periodic]),
                          float(omega), float(rho0), float(bb_rho))
         self.flags = np.ascontiguousarray(flags, np.uint8).reshape(n)
+        # the C code reads the face values of face / edge / corner cells and
+        # the force of Guo cells only: a lattice without such cells gets a
+        # three-value stand-in instead of n * 3 zeros (large lattices)
+        kinds = np.unique(self.flags)
+        needs_bc = bool(np.any((kinds >= 6) & (kinds < 50)))
+        needs_force = bool(np.any(kinds == 1))
         self.bcval = np.ascontiguousarray(
-            np.zeros((n, 3)) if bcval is None else bcval, np.float64).reshape(n * 3)
+            (np.zeros((n, 3)) if needs_bc else np.zeros(3)) if bcval is None else bcval, np.float64).reshape(-1)
         self.force = np.ascontiguousarray(
-            np.zeros((n, 3)) if force is None else force, np.float64).reshape(n * 3)
+            (np.zeros((n, 3)) if needs_force else np.zeros(3)) if force is None else force, np.float64).reshape(-1)
 
     @classmethod
     def from_golden(cls, g, meta):
@@ -96,9 +102,14 @@ class OracleLattice:
                              _dp(f))
         return f
 
-    def run(self, f, nsteps, with_stats=True):
-        """Advance f ([x][y][z][19] f-bar) by nsteps; returns (f, stats[nsteps, 7])."""
-        f = np.ascontiguousarray(f, np.float64).copy()
+    def run(self, f, nsteps, with_stats=True, inplace=False):
+        """Advance f ([x][y][z][19] f-bar) by nsteps; returns (f, stats[nsteps, 7]).
+        inplace: advance the caller's C-contiguous float64 array itself."""
+        if inplace:
+            if f.dtype != np.float64 or not f.flags["C_CONTIGUOUS"]:
+                raise ValueError("run(inplace=True) needs a C-contiguous float64 array")
+        else:
+            f = np.ascontiguousarray(f, np.float64).copy()
         stats = np.zeros((max(nsteps, 1), 7)) if with_stats else None
         rc = lib().orc_run(ctypes.byref(self.p), self._u8(), _dp(self.bcval), _dp(self.force),
                            _dp(f), int(nsteps), _dp(stats) if with_stats else None)

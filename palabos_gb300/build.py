@@ -32,7 +32,8 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
 FORMS = [("fp64", False), ("fp32", True), ("bf16", True), ("fp16", True), ("bf16sr", True)]
 UNITS = ([(f"step_{f}_{p}.cu", fm) for f, fm in FORMS for p in ("even", "odd")]
          + [(f"step_{f}.cu", fm) for f, fm in FORMS]
-         + [("adjoint.cu", False), ("api.cu", False), ("noalloc.cu", False), ("checkpoint.cu", False), ("voxelizer.cu", False)])
+         + [("adjoint.cu", False), ("api.cu", False), ("noalloc.cu", False), ("checkpoint.cu", False), ("voxelizer.cu", False),
+            ("pipe_rate.cu", False)])
 
 
 def nvcc() -> str:

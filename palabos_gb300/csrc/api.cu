@@ -9,7 +9,9 @@
 // cells.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdarg>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -18,6 +20,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/plbgpu.h"
 #include "dynstate.h"
 #include "launch.h"
@@ -25,6 +29,31 @@
 using namespace plbgpu;
 
 namespace {
+
+// NVTX ranges named like the reference profiler's timers
+// (core/plbProfiler.h:44-56): "cycle" around a collide-and-stream call
+// (MultiBlockLattice3D::collideAndStream, multiBlock/multiBlockLattice3D.hh:319),
+// "collStream" around the launches of one time step, with the number of cells
+// as payload (the "collStreamCells" counter, atomicBlock/blockLattice3D.hh:
+// 257-258), "dataProcessor" around the edge and corner processors
+// (multiBlock/multiBlock3D.cpp:487), "io" around transfers and checkpoints.
+// The ranges mark host-side submission; without an attached tool they cost
+// one branch each.
+struct ProfRange {
+    explicit ProfRange(const char* name, unsigned long long payload = 0) {
+        nvtxEventAttributes_t a = {};
+        a.version = NVTX_VERSION;
+        a.size = NVTX_EVENT_ATTRIB_STRUCT_SIZE;
+        a.messageType = NVTX_MESSAGE_TYPE_ASCII;
+        a.message.ascii = name;
+        a.payloadType = NVTX_PAYLOAD_TYPE_UNSIGNED_INT64;
+        a.payload.ullValue = payload;
+        nvtxRangePushEx(&a);
+    }
+    ~ProfRange() { nvtxRangePop(); }
+    ProfRange(const ProfRange&) = delete;
+    ProfRange& operator=(const ProfRange&) = delete;
+};
 
 struct Domain {
     int nx = 0, ny = 0, nz = 0;
@@ -70,6 +99,7 @@ struct Domain {
         L.per[0] = per[0]; L.per[1] = per[1]; L.per[2] = per[2];
         L.n = n;
         L.status = status;
+        L.rowForm = 0;
         return L;
     }
 };
@@ -86,6 +116,9 @@ struct plbgpu_ctx {
     unsigned long long launches = 0;
     void* staging = nullptr;     // device staging buffer for transfers
     size_t stagingBytes = 0;
+    bool pageableAccess = false; // kernels may dereference pageable host memory (host page tables)
+    bool forceStaged = false;    // PLBGPU_STAGED_TRANSFERS=1: always go through the staging buffer
+    int rowForm = 0;             // PLBGPU_ROW_KERNEL=cell: one-cell interior-row kernels (DevLattice::rowForm)
 };
 
 namespace {
@@ -153,6 +186,62 @@ int ensureStaging(plbgpu_ctx* c, size_t bytes) {
     }
     CUDA_TRY(c, cudaMalloc(&c->staging, bytes));
     c->stagingBytes = bytes;
+    return PLBGPU_OK;
+}
+
+// How the transfer kernels reach a caller's buffer of populations: directly
+// when the GPU can address it -- device or managed memory, pinned host memory,
+// or, on a GPU that walks the host's page tables (a GB300 next to its Grace
+// CPU over NVLink-C2C), plain pageable host memory -- otherwise (nullptr)
+// through the bounded staging buffer, chunk by chunk.
+const void* directPointer(plbgpu_ctx* c, const void* p) {
+    if (c->forceStaged) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    switch (a.type) {
+    case cudaMemoryTypeDevice: return a.device == c->device ? a.devicePointer : nullptr;
+    case cudaMemoryTypeManaged:
+    case cudaMemoryTypeHost: return a.devicePointer;
+    default: return c->pageableAccess ? p : nullptr;
+    }
+}
+
+// Staged transfers move at most this many bytes per copy.
+constexpr size_t kStageChunk = size_t(64) << 20;
+
+// The sub-boxes of b (whole x-planes, or rows of one plane when a plane is
+// larger than a chunk) whose transfer records fit in one staging chunk, with
+// their offset (in doubles) in the box's buffer.  Returns the staging bytes.
+template <class Fn>
+int forEachChunk(const Box& b, Fn fn, size_t* stageBytes) {
+    const long long bny = b.y1 - b.y0 + 1, bnz = b.z1 - b.z0 + 1;
+    const size_t rowB = (size_t)bnz * 19 * sizeof(double), planeB = rowB * (size_t)bny;
+    if (planeB <= kStageChunk) {
+        const int xs = (int)(kStageChunk / planeB);
+        *stageBytes = planeB * (size_t)std::min<long long>(xs, b.x1 - b.x0 + 1);
+        for (int x = b.x0; x <= b.x1; x += xs) {
+            Box s = b;
+            s.x0 = x;
+            s.x1 = std::min(x + xs - 1, b.x1);
+            int rc = fn(s, (size_t)(x - b.x0) * bny * bnz * 19);
+            if (rc) return rc;
+        }
+    } else {
+        const int ys = (int)std::max<size_t>(1, kStageChunk / rowB);
+        *stageBytes = rowB * (size_t)std::min<long long>(ys, bny);
+        for (int x = b.x0; x <= b.x1; ++x)
+            for (int y = b.y0; y <= b.y1; y += ys) {
+                Box s = b;
+                s.x0 = s.x1 = x;
+                s.y0 = y;
+                s.y1 = std::min(y + ys - 1, b.y1);
+                int rc = fn(s, ((size_t)(x - b.x0) * bny + (y - b.y0)) * bnz * 19);
+                if (rc) return rc;
+            }
+    }
     return PLBGPU_OK;
 }
 
@@ -421,15 +510,20 @@ StepConsts consts(const Domain* d) {
     return s;
 }
 
-// The kernels record failures (a bulk-copy wait that gave up) in a device
-// status word; report and clear it.
+// The step kernels record a diverged state (a NaN or an infinity met by a
+// statistics step) in the domain's device status word; report it once and
+// clear it, so that the context stays usable (a new state can be sent).
 int checkStatus(plbgpu_ctx* c, Domain* d) {
     unsigned st = 0;
     CUDA_TRY(c, cudaMemcpyAsync(&st, d->status, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     if (st) {
         CUDA_TRY(c, cudaMemsetAsync(d->status, 0, sizeof(unsigned), c->stream));
-        return fail(c, PLBGPU_ERR_CUDA, "device status 0x%x: a staged-copy wait timed out, results are invalid", st);
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+        if (st & kStatusNonFinite)
+            return fail(c, PLBGPU_ERR_STATE,
+                        "non-finite populations (NaN or infinity) met by a statistics step: the run has diverged");
+        return fail(c, PLBGPU_ERR_CUDA, "device status 0x%x", st);
     }
     return PLBGPU_OK;
 }
@@ -456,6 +550,7 @@ int finishSurface(plbgpu_ctx* c, Domain* d) {
     int rc;
     if (d->surfDirty && (rc = buildSurface(c, d))) return rc;
     if (d->nEdges + d->nCorners == 0) return PLBGPU_OK;
+    ProfRange prof("dataProcessor", (unsigned long long)(d->nEdges + d->nCorners));
     const Launchers& L = launchers(d->precision);
     const int pending = d->pending && d->bc ? 1 : 0;
     const double invRho0 = (double)1 / d->rho0;
@@ -523,6 +618,10 @@ int domainFail(plbgpu_ctx* c, int code, const char* msg) { return fail(c, code, 
 
 cudaStream_t contextStream(plbgpu_ctx* c) { return c ? c->stream : nullptr; }
 
+void countLaunches(plbgpu_ctx* c, int n) {
+    if (c) c->launches += (unsigned long long)n;
+}
+
 void domainSetState(plbgpu_ctx* c, int h, bool odd, bool pending) {
     Domain* d;
     if (lookup(c, h, &d)) return;
@@ -547,6 +646,13 @@ int plbgpu_create(int device, plbgpu_ctx** out) {
     plbgpu_ctx* c = new (std::nothrow) plbgpu_ctx();
     if (!c) return PLBGPU_ERR_NOMEM;
     c->device = device;
+    int pageable = 0;
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) == cudaSuccess)
+        c->pageableAccess = pageable != 0;
+    const char* staged = getenv("PLBGPU_STAGED_TRANSFERS");
+    c->forceStaged = staged && staged[0] == '1';
+    const char* rowKernel = getenv("PLBGPU_ROW_KERNEL");
+    c->rowForm = rowKernel && strcmp(rowKernel, "cell") == 0 ? 1 : 0;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete c;
         return PLBGPU_ERR_CUDA;
@@ -959,6 +1065,7 @@ int plbgpu_initialize(plbgpu_ctx* c, int h) {
 }
 
 int plbgpu_send(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, const double* buf, size_t n) {
+    ProfRange prof("io");
     Domain* d;
     Box b;
     int rc = lookup(c, h, &d);
@@ -967,17 +1074,32 @@ int plbgpu_send(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, in
     long long cells = boxCells(b);
     if (!buf || (long long)n != 19 * cells) return fail(c, PLBGPU_ERR_ARG, "send: %zu doubles for %lld cells", n, cells);
     if ((rc = materialize(c, d))) return rc;
-    if ((rc = ensureStaging(c, sizeof(double) * n))) return rc;
-    CUDA_TRY(c, cudaMemcpyAsync(c->staging, buf, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
-    int k = launchers(d->precision).insert(d->view(), d->odd, b, static_cast<const double*>(c->staging), c->stream);
-    c->launches += k - 1;
-    if ((rc = launchBox(c))) return rc;
+    const Launchers& L = launchers(d->precision);
+    if (const void* dp = directPointer(c, buf)) {
+        // one pass: the insert kernel reads the caller's buffer itself
+        int k = L.insert(d->view(), d->odd, b, static_cast<const double*>(dp), c->stream);
+        c->launches += k - 1;
+        if ((rc = launchBox(c))) return rc;
+    } else {
+        size_t stage = 0;
+        forEachChunk(b, [](const Box&, size_t) { return PLBGPU_OK; }, &stage);
+        if ((rc = ensureStaging(c, stage))) return rc;
+        rc = forEachChunk(b, [&](const Box& s, size_t off) -> int {
+            CUDA_TRY(c, cudaMemcpyAsync(c->staging, buf + off, sizeof(double) * 19 * (size_t)boxCells(s),
+                                        cudaMemcpyHostToDevice, c->stream));
+            int k = L.insert(d->view(), d->odd, s, static_cast<const double*>(c->staging), c->stream);
+            c->launches += k - 1;
+            return launchBox(c);
+        }, &stage);
+        if (rc) return rc;
+    }
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     d->statsValid = false;
     return PLBGPU_OK;
 }
 
 int plbgpu_receive(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, double* buf, size_t n) {
+    ProfRange prof("io");
     Domain* d;
     Box b;
     int rc = lookup(c, h, &d);
@@ -986,12 +1108,28 @@ int plbgpu_receive(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0,
     long long cells = boxCells(b);
     if (!buf || (long long)n != 19 * cells) return fail(c, PLBGPU_ERR_ARG, "receive: %zu doubles for %lld cells", n, cells);
     if ((rc = checkStatus(c, d))) return rc;
-    if ((rc = ensureStaging(c, sizeof(double) * n))) return rc;
-    int k = launchers(d->precision).extract(d->view(), d->odd, b, d->pending && d->bc ? 1 : 0,
-                                            static_cast<double*>(c->staging), c->stream);
-    c->launches += k - 1;
-    if ((rc = launchBox(c))) return rc;
-    CUDA_TRY(c, cudaMemcpyAsync(buf, c->staging, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    const Launchers& L = launchers(d->precision);
+    const int pending = d->pending && d->bc ? 1 : 0;
+    if (const void* dp = directPointer(c, buf)) {
+        // one pass: the extract kernel writes the caller's buffer itself
+        int k = L.extract(d->view(), d->odd, b, pending, static_cast<double*>(const_cast<void*>(dp)), c->stream);
+        c->launches += k - 1;
+        if ((rc = launchBox(c))) return rc;
+    } else {
+        size_t stage = 0;
+        forEachChunk(b, [](const Box&, size_t) { return PLBGPU_OK; }, &stage);
+        if ((rc = ensureStaging(c, stage))) return rc;
+        rc = forEachChunk(b, [&](const Box& s, size_t off) -> int {
+            int k = L.extract(d->view(), d->odd, s, pending, static_cast<double*>(c->staging), c->stream);
+            c->launches += k - 1;
+            int r = launchBox(c);
+            if (r) return r;
+            CUDA_TRY(c, cudaMemcpyAsync(buf + off, c->staging, sizeof(double) * 19 * (size_t)boxCells(s),
+                                        cudaMemcpyDeviceToHost, c->stream));
+            return PLBGPU_OK;
+        }, &stage);
+        if (rc) return rc;
+    }
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     return PLBGPU_OK;
 }
@@ -1002,13 +1140,17 @@ int plbgpu_collide_and_stream(plbgpu_ctx* c, int h, int nsteps, int collect_stat
     if (rc) return rc;
     if (nsteps < 0) return fail(c, PLBGPU_ERR_ARG, "nsteps %d", nsteps);
     if (nsteps == 0) return PLBGPU_OK;
+    ProfRange prof("cycle", (unsigned long long)nsteps);
     const Launchers& L = launchers(d->precision);
     const bool hasFaces = d->bc != nullptr;
     if (d->surfDirty && (rc = buildSurface(c, d))) return rc;
     auto stepOnce = [&](bool stats) -> int {
+        ProfRange step("collStream", (unsigned long long)d->n);
         if (stats) CUDA_TRY(c, cudaMemsetAsync(d->stats, 0, sizeof(StatsAcc) * kStatsSlots, c->stream));
         StepConsts k = consts(d);
-        int nl = L.step(d->view(), d->odd, stats, k, d->stats, c->stream, &c->side);
+        DevLattice v = d->view();
+        v.rowForm = c->rowForm;
+        int nl = L.step(v, d->odd, stats, k, d->stats, c->stream, &c->side);
         c->launches += nl - 1;
         int r = launchBox(c);
         if (r) return r;
@@ -1224,7 +1366,9 @@ int plbgpu_collide_and_stream_external(plbgpu_ctx* c, int h, int nsteps, int rec
         if (stats) CUDA_TRY(c, cudaMemsetAsync(d->stats, 0, sizeof(StatsAcc) * kStatsSlots, c->stream));
         StepConsts k = consts(d);
         k.external = 1;
-        int nl = L.step(d->view(), d->odd, stats, k, d->stats, c->stream, &c->side);
+        DevLattice v = d->view();
+        v.rowForm = c->rowForm;
+        int nl = L.step(v, d->odd, stats, k, d->stats, c->stream, &c->side);
         c->launches += nl - 1;
         if ((rc = launchBox(c))) return rc;
         d->odd = !d->odd;
@@ -1410,6 +1554,7 @@ int prepareLoad(plbgpu_ctx* c, Domain* d, int what) {
 }  // namespace
 
 int plbgpu_save_binary_block(plbgpu_ctx* c, int h, int what, const char* path, int enforce_uint) {
+    ProfRange prof("io");
     Domain* d;
     int rc = lookup(c, h, &d);
     if (rc) return rc;
@@ -1465,6 +1610,7 @@ int plbgpu_save_binary_block(plbgpu_ctx* c, int h, int what, const char* path, i
 }
 
 int plbgpu_load_binary_block(plbgpu_ctx* c, int h, int what, const char* path, int enforce_uint) {
+    ProfRange prof("io");
     Domain* d;
     int rc = lookup(c, h, &d);
     if (rc) return rc;
@@ -1625,6 +1771,7 @@ std::string stateDescription(const Domain* d, int what, const std::string& datNa
 }  // namespace
 
 int plbgpu_save_state(plbgpu_ctx* c, int h, int what, const char* base) {
+    ProfRange prof("io");
     Domain* d;
     int rc = lookup(c, h, &d);
     if (rc) return rc;
@@ -1820,6 +1967,7 @@ bool isLatticeBlock(int what) { return what == PLBGPU_BLOCK_LATTICE || what == P
 }  // namespace
 
 int plbgpu_load_state(plbgpu_ctx* c, int h, int what, const char* plb) {
+    ProfRange prof("io");
     Domain* d;
     int rc = lookup(c, h, &d);
     if (rc) return rc;
@@ -1878,6 +2026,7 @@ int plbgpu_load_state(plbgpu_ctx* c, int h, int what, const char* plb) {
 }
 
 int plbgpu_save_state_dynamic(plbgpu_ctx* c, int h, int what, const char* base) {
+    ProfRange prof("io");
     Domain* d;
     int rc = lookup(c, h, &d);
     if (rc) return rc;
@@ -1955,6 +2104,7 @@ int plbgpu_save_state_dynamic(plbgpu_ctx* c, int h, int what, const char* base) 
 }
 
 int plbgpu_load_state_dynamic(plbgpu_ctx* c, int h, int what, const char* plb) {
+    ProfRange prof("io");
     Domain* d;
     int rc = lookup(c, h, &d);
     if (rc) return rc;

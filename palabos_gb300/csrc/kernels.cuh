@@ -151,8 +151,15 @@ struct DevLattice {
     int nx, ny, nz;
     int per[3];
     long long n;
-    unsigned* status;       // device error word (bit 0: a bulk-copy wait timed out)
+    unsigned* status;       // device error word (kStatusNonFinite)
+    int rowForm;            // interior-row kernel: 0 the fastest for the storage type, 1 one cell per thread
 };
+
+// Bits of DevLattice::status.  A statistics step that meets a NaN or an
+// infinity in the density or kinetic-energy sums of a block (a population of
+// one of its cells is not finite: the run has diverged) sets kStatusNonFinite;
+// the host reports it as PLBGPU_ERR_STATE at the next synchronization.
+constexpr unsigned kStatusNonFinite = 1u;
 
 template <typename R>
 struct StepParams {
@@ -427,7 +434,7 @@ __device__ __forceinline__ bool collideCell(const DevLattice& L, const StepParam
 // Block-wide sum of the per-thread statistics, one set of atomics per block
 // on the block's slot.  Every thread of the block must call it.
 __device__ __forceinline__ void flushStats(double sR, double sU, unsigned long long cnt, unsigned long long mx,
-                                           StatsAcc* acc) {
+                                           StatsAcc* acc, unsigned* status) {
     __shared__ double shR[32], shU[32];
     __shared__ unsigned long long shC[32], shM[32];
     sR = warpSum(sR);
@@ -452,6 +459,8 @@ __device__ __forceinline__ void flushStats(double sR, double sU, unsigned long l
         cnt = warpSumU(cnt);
         mx = warpMaxU(mx);
         if (lane == 0 && cnt > 0) {
+            // one test per block: a NaN or infinity of any cell reaches the sums
+            if (!isfinite(sR) || !isfinite(sU)) atomicOr(status, kStatusNonFinite);
             StatsAcc* a = statsSlot(acc);
             atomicAdd(&a->sumRhoBar, sR);
             atomicAdd(&a->sumUSqr, sU);
@@ -462,10 +471,11 @@ __device__ __forceinline__ void flushStats(double sR, double sU, unsigned long l
 }
 
 template <bool STATS>
-__device__ __forceinline__ void accumulateStats(bool gathers, double rhoBar, double uSqr, StatsAcc* acc) {
+__device__ __forceinline__ void accumulateStats(bool gathers, double rhoBar, double uSqr, StatsAcc* acc,
+                                                unsigned* status) {
     if (!STATS) return;
     flushStats(gathers ? rhoBar : 0., gathers ? uSqr : 0., gathers ? 1ull : 0ull,
-               gathers ? (unsigned long long)__double_as_longlong(uSqr) : 0ull, acc);
+               gathers ? (unsigned long long)__double_as_longlong(uSqr) : 0ull, acc, status);
 }
 
 // General cell update: any position, periodic wrap and the domain-edge rule.
@@ -602,7 +612,7 @@ __global__ void __launch_bounds__(128, RowShape<S>::blocks)
             mx = b > mx ? b : mx;
         }
     }
-    if (STATS) flushStats(sR, sU, cnt, mx, acc);
+    if (STATS) flushStats(sR, sU, cnt, mx, acc, L.status);
 }
 
 // ---------------------------------------------------------------- paired row kernel
@@ -696,7 +706,7 @@ __global__ void __launch_bounds__(128, 8)
             }
         }
     }
-    if (STATS) flushStats(sR, sU, cnt, mx, acc);
+    if (STATS) flushStats(sR, sU, cnt, mx, acc, L.status);
 }
 
 // Rows on the x or y border of the domain, with the general addressing
@@ -728,7 +738,7 @@ __global__ void __launch_bounds__(128, sizeof(S) <= 4 ? 6 : 1) edgeRowStepKernel
     R rhoBar = R(0), uSqr = R(0);
     bool g = false;
     if (z < L.nz) g = processCellGeneral<S, ODD, STATS, EXT, SPARSE>(L, P, x, y, z, acc, rhoBar, uSqr);
-    accumulateStats<STATS>(g, (double)rhoBar, (double)uSqr, acc);
+    accumulateStats<STATS>(g, (double)rhoBar, (double)uSqr, acc, L.status);
 }
 
 // Complete the boundary faces in place (used before a transfer into a state
@@ -755,45 +765,63 @@ __global__ void completeFacesKernel(DevLattice L) {
 struct Box { int x0, x1, y0, y1, z0, z1; };
 
 // Canonical transfer layout: [x][y][z][19] over the box, z fastest, FP64.
+// The buffer may be device memory or, over NVLink-C2C, the caller's host
+// memory (pinned or pageable), so a block stages its run of up to kXferCells
+// cells of one box row in shared memory and reads or writes the run as one
+// contiguous, coalesced stretch of 19 * cells doubles; the slots in the
+// population planes are then written or read one cell per thread.
+constexpr int kXferCells = 128;
+
 template <typename S, bool ODD>
-__global__ void extractKernel(DevLattice L, Box b, int pending, double* out) {
+__global__ void __launch_bounds__(kXferCells) extractKernel(DevLattice L, Box b, int pending, double* out) {
     using R = typename StoreT<S>::R;
+    __shared__ double sh[kXferCells * 19];
     const int bnz = b.z1 - b.z0 + 1, bny = b.y1 - b.y0 + 1;
-    const int dz = blockIdx.x * blockDim.x + threadIdx.x;
-    if (dz >= bnz) return;
-    const int z = b.z0 + dz, y = b.y0 + blockIdx.y, x = b.x0 + blockIdx.z;
-    const long long idx = ((long long)x * L.ny + y) * L.nz + z;
-    const long long o = (((long long)blockIdx.z * bny + blockIdx.y) * bnz + dz) * 19;
-    const int k = L.flags[idx];
-    if (k == K_NONE) {   // not part of the lattice: reads as zeros
+    const int dz0 = blockIdx.x * kXferCells;
+    const int cnt = min(kXferCells, bnz - dz0);
+    const int t = threadIdx.x;
+    if (t < cnt) {
+        const int z = b.z0 + dz0 + t, y = b.y0 + blockIdx.y, x = b.x0 + blockIdx.z;
+        const long long idx = ((long long)x * L.ny + y) * L.nz + z;
+        const int k = L.flags[idx];
+        R f[19];
+        if (k == K_NONE) {   // not part of the lattice: reads as zeros
 #pragma unroll
-        for (int i = 0; i < 19; ++i) out[o + i] = 0.;
-        return;
+            for (int i = 0; i < 19; ++i) f[i] = R(0);
+        } else {
+            Neighbourhood nb = neighbourhood(L, x, y, z);
+            const S* Pp = static_cast<const S*>(L.pop);
+#pragma unroll
+            for (int i = 0; i < 19; ++i) f[i] = StoreT<S>::ld(Pp + slotOf<ODD>(L, nb, idx, i));
+            if (pending && isFace(k)) completeIfFace<R>(L, idx, k, f);
+        }
+#pragma unroll
+        for (int i = 0; i < 19; ++i) sh[t * 19 + i] = (double)f[i];
     }
-    Neighbourhood nb = neighbourhood(L, x, y, z);
-    const S* Pp = static_cast<const S*>(L.pop);
-    R f[19];
-#pragma unroll
-    for (int i = 0; i < 19; ++i) f[i] = StoreT<S>::ld(Pp + slotOf<ODD>(L, nb, idx, i));
-    if (pending && isFace(k)) completeIfFace<R>(L, idx, k, f);
-#pragma unroll
-    for (int i = 0; i < 19; ++i) out[o + i] = (double)f[i];
+    __syncthreads();
+    const long long o0 = (((long long)blockIdx.z * bny + blockIdx.y) * bnz + dz0) * 19;
+    for (int q = t; q < cnt * 19; q += kXferCells) out[o0 + q] = sh[q];
 }
 
 template <typename S, bool ODD>
-__global__ void insertKernel(DevLattice L, Box b, const double* in) {
+__global__ void __launch_bounds__(kXferCells) insertKernel(DevLattice L, Box b, const double* in) {
+    __shared__ double sh[kXferCells * 19];
     const int bnz = b.z1 - b.z0 + 1, bny = b.y1 - b.y0 + 1;
-    const int dz = blockIdx.x * blockDim.x + threadIdx.x;
-    if (dz >= bnz) return;
-    const int z = b.z0 + dz, y = b.y0 + blockIdx.y, x = b.x0 + blockIdx.z;
+    const int dz0 = blockIdx.x * kXferCells;
+    const int cnt = min(kXferCells, bnz - dz0);
+    const int t = threadIdx.x;
+    const long long o0 = (((long long)blockIdx.z * bny + blockIdx.y) * bnz + dz0) * 19;
+    for (int q = t; q < cnt * 19; q += kXferCells) sh[q] = in[o0 + q];
+    __syncthreads();
+    if (t >= cnt) return;
+    const int z = b.z0 + dz0 + t, y = b.y0 + blockIdx.y, x = b.x0 + blockIdx.z;
     const long long idx = ((long long)x * L.ny + y) * L.nz + z;
-    const long long o = (((long long)blockIdx.z * bny + blockIdx.y) * bnz + dz) * 19;
     if (L.flags[idx] == K_NONE) return;
     Neighbourhood nb = neighbourhood(L, x, y, z);
     S* Pp = static_cast<S*>(L.pop);
 #pragma unroll
     for (int i = 0; i < 19; ++i)
-        StoreT<S>::st(Pp + slotOf<ODD>(L, nb, idx, i), (typename StoreT<S>::R)in[o + i]);
+        StoreT<S>::st(Pp + slotOf<ODD>(L, nb, idx, i), (typename StoreT<S>::R)sh[t * 19 + i]);
 }
 
 // Macroscopic values of one cell the way each dynamics reports them

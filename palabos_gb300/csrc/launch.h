@@ -73,6 +73,8 @@ int domainAccess(plbgpu_ctx* c, int handle, DomainAccess* out);
 int domainFail(plbgpu_ctx* c, int code, const char* msg);
 // The context's stream (kernels that belong to no domain, e.g. the voxelizer).
 cudaStream_t contextStream(plbgpu_ctx* c);
+// Add n kernel launches to the context's counter.
+void countLaunches(plbgpu_ctx* c, int n);
 // After the adjoint module rewrote the populations in natural order.
 void domainSetState(plbgpu_ctx* c, int handle, bool odd, bool pending);
 

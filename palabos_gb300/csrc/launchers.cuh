@@ -74,15 +74,15 @@ struct LaunchImpl {
         return 1;
     }
     static int extract(const DevLattice& L, bool odd, Box b, int pending, double* out, cudaStream_t s) {
-        dim3 g = rowGrid(b.z1 - b.z0 + 1, b.y1 - b.y0 + 1, b.x1 - b.x0 + 1, kBlock);
-        if (odd) extractKernel<S, true><<<g, kBlock, 0, s>>>(L, b, pending, out);
-        else extractKernel<S, false><<<g, kBlock, 0, s>>>(L, b, pending, out);
+        dim3 g = rowGrid(b.z1 - b.z0 + 1, b.y1 - b.y0 + 1, b.x1 - b.x0 + 1, kXferCells);
+        if (odd) extractKernel<S, true><<<g, kXferCells, 0, s>>>(L, b, pending, out);
+        else extractKernel<S, false><<<g, kXferCells, 0, s>>>(L, b, pending, out);
         return 1;
     }
     static int insert(const DevLattice& L, bool odd, Box b, const double* in, cudaStream_t s) {
-        dim3 g = rowGrid(b.z1 - b.z0 + 1, b.y1 - b.y0 + 1, b.x1 - b.x0 + 1, kBlock);
-        if (odd) insertKernel<S, true><<<g, kBlock, 0, s>>>(L, b, in);
-        else insertKernel<S, false><<<g, kBlock, 0, s>>>(L, b, in);
+        dim3 g = rowGrid(b.z1 - b.z0 + 1, b.y1 - b.y0 + 1, b.x1 - b.x0 + 1, kXferCells);
+        if (odd) insertKernel<S, true><<<g, kXferCells, 0, s>>>(L, b, in);
+        else insertKernel<S, false><<<g, kXferCells, 0, s>>>(L, b, in);
         return 1;
     }
     static int reduce(const DevLattice& L, bool odd, Box b, int pending, double invRho0, double bbRho,

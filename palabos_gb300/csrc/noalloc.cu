@@ -1,12 +1,11 @@
 // Allocation-free variant of the average energy / density reduction.
 //
 // Who needs it: callers that own all device memory themselves and may not
-// call cudaMalloc -- code issuing work into a CUDA graph that is being
-// captured (allocation calls are not allowed during capture), applications
-// with their own pooled allocator or a fixed device-memory budget, and hosts
-// that drive the GPU from a context where the runtime allocator is off
-// limits.  They pass the lattice (FP64 f-bar planes and cell kinds) and the
-// result buffer; this entry point adds nothing to the device heap.
+// call cudaMalloc -- applications with their own pooled allocator or a fixed
+// device-memory budget, and hosts that drive the GPU from a context where
+// the runtime allocator is off limits.  They pass the lattice (FP64 f-bar
+// planes and cell kinds) and the result buffer; this entry point adds
+// nothing to the device heap.
 //
 // Scratch: one row-sum pair per (x, y) row lives in a file-scope device array
 // of NOALLOC_MAX_ROWS entries (4 MiB).  Every GPU that loads this library
@@ -18,7 +17,8 @@
 // Set-up: the device address of the array is looked up once per device, on
 // the first call made with that device current (cudaGetSymbolAddress, which
 // may also load the module).  Make that first call before any stream capture
-// begins.
+// begins.  The address is kept for the life of the process: after a
+// cudaDeviceReset of that device the entry point must not be called again.
 #include <cuda_runtime.h>
 
 #include <mutex>

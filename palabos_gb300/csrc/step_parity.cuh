@@ -5,6 +5,7 @@
 #pragma once
 
 #include "launchers.cuh"
+#include "vecrow.cuh"
 
 namespace plbgpu {
 
@@ -15,7 +16,10 @@ struct StepLaunch {
 
     // Row kernel of this storage type: the paired kernel for the 2-byte forms
     // when rows have an even length, the one-cell register kernel otherwise.
-    static bool pairedRows(const DevLattice& L) { return sizeof(S) == 2 && L.nz % 2 == 0; }
+    static bool pairedRows(const DevLattice& L) { return sizeof(S) == 2 && L.nz % 2 == 0 && L.rowForm == 0; }
+    // Eight cells per thread, 128-bit population vectors (vecrow.cuh): rows of
+    // a multiple of eight cells.
+    static bool vectorRows(const DevLattice& L) { return sizeof(S) == 2 && L.nz % 8 == 0 && L.rowForm == 0; }
 
     template <bool ODD, bool STATS, bool EXT>
     static int stepSplit(const DevLattice& L, const StepParams<R>& p, StatsAcc* acc, cudaStream_t s,
@@ -37,7 +41,20 @@ struct StepLaunch {
             cudaStreamWaitEvent(side->stream, side->fork, 0) == cudaSuccess)
             es = side->stream;
         auto interior = [&]() {
-            if (!general && pairedRows(L)) {
+            if (!general && vectorRows(L)) {
+                if constexpr (sizeof(S) == 2) {
+                    Planes<S> pl;
+                    RowDeltas d;
+                    for (int i = 0; i < 19; ++i) {
+                        pl.p[i] = static_cast<S*>(L.pop) + (long long)i * L.stride;
+                        d.d[i] = cdir(i, 0) * L.ny * L.nz + cdir(i, 1) * L.nz;
+                    }
+                    const long long segs = (long long)(L.nx - 2) * (L.ny - 2) * (L.nz / 8);
+                    const unsigned blocks = (unsigned)((segs + kBlock - 1) / kBlock);
+                    vecRowStepKernel<S, ODD, STATS, EXT><<<blocks, kBlock, 0, s>>>(L, pl, d, p, acc, segs);
+                    ++launched;
+                }
+            } else if (!general && pairedRows(L)) {
                 Planes<S> pl;
                 Deltas d;
                 for (int i = 0; i < 19; ++i) {

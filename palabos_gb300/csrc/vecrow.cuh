@@ -1,0 +1,247 @@
+// Interior-row step kernel of the 2-byte storage forms (BF16, BF16 with
+// stochastic rounding, FP16): eight consecutive cells of a row per thread,
+// every population read and written as one aligned 128-bit vector.
+//
+// Rows with 1 <= x <= nx-2 and 1 <= y <= ny-2 of a dense domain whose rows
+// hold a multiple of eight cells (nz % 8 == 0; planes start on 256-byte
+// boundaries, so every eight-cell segment of a plane row is one aligned
+// 16-byte vector).  Thread g owns segment g % (nz/8) of interior row
+// g / (nz/8): cells z0..z0+7, z0 = 8 * segment.
+//
+// Even AA step: the 19 vectors of the thread's own cells are loaded, each
+// cell collides, and population i goes back into slot opp(i) of the same
+// cells -- 19 vector loads and 19 vector stores per eight cells.
+//
+// Odd AA step: slot opp(i) of x - c_i is read and population i written to slot
+// i of x + c_i.  Moves along x and y are a uniform row offset (interior rows);
+// the nine populations with c_z = 0 stay aligned.  For the ten that move along
+// z the thread's window is its aligned vector shifted by one cell: the missing
+// element is the neighbouring lane's edge element, passed by one warp shuffle
+// and merged with four byte permutes.  Where the neighbour is not in the same
+// row and warp the element is read with a 16-bit load: at a warp boundary
+// inside a row, the plain neighbour; at the row ends, the periodic wrap or --
+// on a non-periodic z axis -- the reference's domain-edge rule (a population
+// that would leave the domain stays in its cell, reversed: slot i of the own
+// cell).  Stores mirror this: a lane whose vector needs an element from a lane
+// it cannot shuffle with writes the other seven elements with 16-, 32- and
+// 64-bit stores, and the element's owner writes it with a 16-bit store.
+//
+// Every slot is still read and written by one thread only: an element a
+// thread hands to its neighbour through a shuffle is one the thread itself
+// read, and an element it receives is one it writes.  This is the same
+// ownership as the one-cell kernels, so the results are bit-identical to them.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace plbgpu {
+
+// Unpack one 16-bit value (low or high half of a 32-bit word) to FP32 and pack
+// an FP32 value into one half of a word, per storage type.
+template <typename S> struct Half16;
+template <> struct Half16<__nv_bfloat16> {
+    static __device__ __forceinline__ float get(unsigned w, bool hi) {
+        return __uint_as_float(hi ? (w & 0xffff0000u) : (w << 16));
+    }
+    static __device__ __forceinline__ unsigned put(unsigned w, bool hi, float v, const void*, unsigned) {
+        const unsigned b = __bfloat16_as_ushort(__float2bfloat16_rn(v));
+        return hi ? __byte_perm(w, b, 0x5410) : __byte_perm(w, b, 0x3254);
+    }
+};
+template <> struct Half16<__half> {
+    static __device__ __forceinline__ float get(unsigned w, bool hi) {
+        return __half2float(__ushort_as_half((unsigned short)(hi ? (w >> 16) : (w & 0xffffu))));
+    }
+    static __device__ __forceinline__ unsigned put(unsigned w, bool hi, float v, const void*, unsigned) {
+        const unsigned b = __half_as_ushort(__float2half_rn(v));
+        return hi ? __byte_perm(w, b, 0x5410) : __byte_perm(w, b, 0x3254);
+    }
+};
+template <> struct Half16<bf16sr> {
+    static __device__ __forceinline__ float get(unsigned w, bool hi) {
+        return __uint_as_float(hi ? (w & 0xffff0000u) : (w << 16));
+    }
+    // random bits from the cell's own slot address and the step's salt
+    static __device__ __forceinline__ unsigned put(unsigned w, bool hi, float v, const void* cellSlot, unsigned salt) {
+        const unsigned b = bf16Stochastic(v, srBits(cellSlot, salt));
+        return hi ? __byte_perm(w, b, 0x5410) : __byte_perm(w, b, 0x3254);
+    }
+};
+
+__device__ __forceinline__ uint4 ldVec(const void* p) {
+    uint4 v;
+    asm volatile("ld.global.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ void stVec(void* p, uint4 v) {
+    asm volatile("st.global.v4.u32 [%0], {%1, %2, %3, %4};" ::"l"(p), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w)
+                 : "memory");
+}
+__device__ __forceinline__ unsigned ld16(const void* p) {
+    unsigned short u;
+    asm volatile("ld.global.u16 %0, [%1];" : "=h"(u) : "l"(p));
+    return u;
+}
+__device__ __forceinline__ void st16(void* p, unsigned v) {
+    asm volatile("st.global.u16 [%0], %1;" ::"l"(p), "h"((unsigned short)v) : "memory");
+}
+__device__ __forceinline__ void st32(void* p, unsigned v) {
+    asm volatile("st.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void st64(void* p, unsigned a, unsigned b) {
+    asm volatile("st.global.v2.u32 [%0], {%1, %2};" ::"l"(p), "r"(a), "r"(b) : "memory");
+}
+
+// Elements e0..e7 of a vector; word k holds e(2k) in its low half.
+// (p, e0, ..., e6): p in the high half of `prev`.
+__device__ __forceinline__ uint4 shiftUp(uint4 v, unsigned prev) {
+    return make_uint4(__byte_perm(prev, v.x, 0x5432), __byte_perm(v.x, v.y, 0x5432), __byte_perm(v.y, v.z, 0x5432),
+                      __byte_perm(v.z, v.w, 0x5432));
+}
+// (e1, ..., e7, n): n in the low half of `next`.
+__device__ __forceinline__ uint4 shiftDown(uint4 v, unsigned next) {
+    return make_uint4(__byte_perm(v.x, v.y, 0x5432), __byte_perm(v.y, v.z, 0x5432), __byte_perm(v.z, v.w, 0x5432),
+                      __byte_perm(v.w, next, 0x5432));
+}
+
+__device__ __forceinline__ unsigned& word(uint4& v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); }
+
+// Uniform row offsets c_x * ny * nz + c_y * nz of the 19 populations.
+struct RowDeltas {
+    int d[19];
+};
+
+template <typename S>
+struct VecShape { static constexpr int blocks = 3; };
+
+template <typename S, bool ODD, bool STATS, bool EXT>
+__global__ void __launch_bounds__(128, VecShape<S>::blocks)
+    vecRowStepKernel(DevLattice L, Planes<S> Pl, RowDeltas D, StepParams<typename StoreT<S>::R> P, StatsAcc* acc,
+                     long long segments) {
+    using R = typename StoreT<S>::R;
+    const int R8 = L.nz >> 3;                       // segments per row
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = g < segments;
+    // Threads past the last segment mirror it (the warp's shuffles need every
+    // lane); they store nothing and gather no statistics.
+    const long long gg = live ? g : segments - 1;
+    const int row = (int)(gg / R8), seg = (int)(gg - (long long)row * R8);
+    const int x = 1 + row / (L.ny - 2), y = 1 + row % (L.ny - 2);
+    const int lane = threadIdx.x & 31;
+    const bool first = seg == 0, last = seg == R8 - 1;
+    const bool upOk = !first && lane > 0;           // lane - 1 holds cells z0-8..z0-1 of this row
+    const bool downOk = !last && lane < 31;         // lane + 1 holds cells z0+8..z0+15 of this row
+    const bool perZ = L.per[2] != 0;
+    const int rowIdx = (x * L.ny + y) * L.nz;
+    const int z0 = seg << 3;
+    const int idx0 = rowIdx + z0;
+    const int nz = L.nz;
+
+    uint4 v[19];
+    // ---- load
+#pragma unroll
+    for (int i = 0; i < 19; ++i) {
+        if (!ODD) {
+            v[i] = ldVec(Pl.p[i] + idx0);
+        } else {
+            const S* src = Pl.p[opp(i)];
+            const int srow = rowIdx - D.d[i];       // source row x - c_i (x and y part)
+            const int cz = cdir(i, 2);
+            const uint4 a = ldVec(src + (srow + z0));
+            if (cz == 0) {
+                v[i] = a;
+            } else if (cz > 0) {                    // window z0-1 .. z0+6
+                unsigned prev = __shfl_up_sync(0xffffffffu, a.w, 1);
+                if (!upOk) {
+                    const S* p = !first ? src + (srow + z0 - 1) : (perZ ? src + (srow + nz - 1) : Pl.p[i] + rowIdx);
+                    prev = ld16(p) << 16;
+                }
+                v[i] = shiftUp(a, prev);
+            } else {                                // window z0+1 .. z0+8
+                unsigned next = __shfl_down_sync(0xffffffffu, a.x, 1);
+                if (!downOk) {
+                    const S* p = !last ? src + (srow + z0 + 8) : (perZ ? src + srow : Pl.p[i] + (rowIdx + nz - 1));
+                    next = ld16(p);
+                }
+                v[i] = shiftDown(a, next);
+            }
+        }
+    }
+    const uint2 kk = *reinterpret_cast<const uint2*>(L.flags + idx0);
+
+    // ---- collide, one cell at a time; results go back into the same halves
+    double sR = 0., sU = 0.;
+    unsigned long long cnt = 0, mx = 0;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const int w = c >> 1;
+        const bool hi = c & 1;
+        const int k = (int)(((c < 4 ? kk.x : kk.y) >> (8 * (c & 3))) & 0xffu);
+        R f[19];
+#pragma unroll
+        for (int i = 0; i < 19; ++i) f[i] = Half16<S>::get(word(v[i], w), hi);
+        const int idx = idx0 + c;
+        R rhoBar = R(0), uSqr = R(0);
+        if (P.pending && isFace(k)) completeIfFace<R>(L, idx, k, f);
+        const bool gathers = collideCell<S, EXT>(L, P, idx, k, f, rhoBar, uSqr, acc, STATS && live);
+#pragma unroll
+        for (int i = 0; i < 19; ++i) word(v[i], w) = Half16<S>::put(word(v[i], w), hi, f[i], Pl.p[i] + idx, P.seed);
+        if (STATS && live && gathers) {
+            sR += (double)rhoBar;
+            sU += (double)uSqr;
+            cnt += 1;
+            const unsigned long long b = (unsigned long long)__double_as_longlong((double)uSqr);
+            mx = b > mx ? b : mx;
+        }
+    }
+
+    // ---- store
+#pragma unroll
+    for (int i = 0; i < 19; ++i) {
+        if (!ODD) {
+            if (live) stVec(Pl.p[opp(i)] + idx0, v[i]);
+        } else {
+            S* dst = Pl.p[i];
+            const int drow = rowIdx + D.d[i];       // destination row x + c_i (x and y part)
+            const int d0 = drow + z0;
+            const int cz = cdir(i, 2);
+            const uint4 a = v[i];
+            if (cz == 0) {
+                if (live) stVec(dst + d0, a);
+            } else if (cz > 0) {                    // cells z0..z0+7 -> positions z0+1..z0+8
+                const unsigned prev = __shfl_up_sync(0xffffffffu, a.w, 1);
+                if (live) {
+                    if (upOk) {
+                        stVec(dst + d0, shiftUp(a, prev));
+                    } else {                        // position z0 is written by its owner
+                        st16(dst + (d0 + 1), a.x);
+                        st32(dst + (d0 + 2), __byte_perm(a.x, a.y, 0x5432));
+                        st64(dst + (d0 + 4), __byte_perm(a.y, a.z, 0x5432), __byte_perm(a.z, a.w, 0x5432));
+                    }
+                    if (!downOk) {                  // e7: no lane of this warp takes it
+                        S* p = !last ? dst + (d0 + 8) : (perZ ? dst + drow : Pl.p[opp(i)] + (rowIdx + nz - 1));
+                        st16(p, a.w >> 16);
+                    }
+                }
+            } else {                                // cells z0..z0+7 -> positions z0-1..z0+6
+                const unsigned next = __shfl_down_sync(0xffffffffu, a.x, 1);
+                if (live) {
+                    if (downOk) {
+                        stVec(dst + d0, shiftDown(a, next));
+                    } else {                        // position z0+7 is written by its owner
+                        st64(dst + d0, __byte_perm(a.x, a.y, 0x5432), __byte_perm(a.y, a.z, 0x5432));
+                        st32(dst + (d0 + 4), __byte_perm(a.z, a.w, 0x5432));
+                        st16(dst + (d0 + 6), a.w >> 16);
+                    }
+                    if (!upOk) {                    // e0: no lane of this warp takes it
+                        S* p = !first ? dst + (d0 - 1) : (perZ ? dst + (drow + nz - 1) : Pl.p[opp(i)] + rowIdx);
+                        st16(p, a.x);
+                    }
+                }
+            }
+        }
+    }
+    if (STATS) flushStats(sR, sU, cnt, mx, acc, L.status);
+}
+
+}  // namespace plbgpu

@@ -39,8 +39,32 @@ namespace plbgpu {
 namespace {
 
 constexpr int kMaxCrossings = 64;   // per column; more is reported as an error
-constexpr int kMaxIntervals = 32;   // facets parallel to x holding a column's line
+constexpr int kMaxRuns = 32;        // disjoint runs of on-surface cells per column; more is an error
 constexpr int kVxOutside = 1, kVxOuterBorder = 2, kVxInside = 3, kVxInnerBorder = 4;
+constexpr unsigned kTooManyCrossings = 1u, kTooManyRuns = 2u;   // status bits
+
+// The cells x = lo..hi of a column lie on the surface (hence inside).  Runs
+// are kept disjoint and merged as they arrive -- overlapping or touching runs
+// become one -- so a finely meshed face that many facets cover counts once.
+// Returns false when a new disjoint run does not fit.
+__device__ bool addRun(int* runLo, int* runHi, int& m, int lo, int hi) {
+    for (int k = 0; k < m;) {
+        if (lo <= runHi[k] + 1 && runLo[k] <= hi + 1) {   // overlap or touch: absorb run k
+            lo = min(lo, runLo[k]);
+            hi = max(hi, runHi[k]);
+            --m;
+            runLo[k] = runLo[m];
+            runHi[k] = runHi[m];
+        } else {
+            ++k;
+        }
+    }
+    if (m == kMaxRuns) return false;
+    runLo[m] = lo;
+    runHi[m] = hi;
+    ++m;
+    return true;
+}
 
 // Sign of the orientation of p against the edge u -> v in the (y, z) plane,
 // never zero: the edge is evaluated from its lexicographically smaller end
@@ -111,8 +135,13 @@ __global__ void columnKernel(int nx, int ny, int nz, const double* tri, const in
     const double py = y, pz = z;
     int seg[kMaxCrossings];   // the crossing lies in the unit segment (seg - 1, seg]
     int m = 0;
-    double ilo[kMaxIntervals], ihi[kMaxIntervals];   // x-ranges of the line on facets parallel to x
+    int runLo[kMaxRuns], runHi[kMaxRuns];   // disjoint runs of cells on the surface
     int m2 = 0;
+    // cells x (1 <= x <= nx-2, the flooded interior) with lo - 1e-12 <= x <= hi + 1e-12
+    auto onSurface = [&](double lo, double hi) {
+        const double a = fmax(1., ceil(lo - 1e-12)), b = fmin((double)(nx - 2), floor(hi + 1e-12));
+        if (a <= b && !addRun(runLo, runHi, m2, (int)a, (int)b)) atomicOr(status, kTooManyRuns);
+    };
     const int c = y * nz + z;
     for (int k = start[c]; k < start[c + 1]; ++k) {
         const double* T = tri + 9 * (long long)list[k];
@@ -125,13 +154,7 @@ __global__ void columnKernel(int nx, int ny, int nz, const double* tri, const in
             // a facet parallel to x: the cells of the line that lie on it are
             // on the surface, hence inside
             double lo, hi;
-            if (m2 < kMaxIntervals && facetSpan(T, py, pz, scale, lo, hi)) {
-                ilo[m2] = lo;
-                ihi[m2] = hi;
-                ++m2;
-            } else if (m2 == kMaxIntervals) {
-                atomicOr(status, 1u);
-            }
+            if (facetSpan(T, py, pz, scale, lo, hi)) onSurface(lo, hi);
             continue;
         }
         const double wa = (cy - by) * (pz - bz) - (cz - bz) * (py - by);
@@ -143,15 +166,7 @@ __global__ void columnKernel(int nx, int ny, int nz, const double* tri, const in
         // a cell centre on the closed facet (edges and vertices too, where the
         // line may only touch the surface) is on the surface, hence inside
         const bool closed = area > 0. ? (wa >= -tol && wb >= -tol && wc >= -tol) : (wa <= tol && wb <= tol && wc <= tol);
-        if (closed && centre && r >= 0. && r <= (double)nx) {
-            if (m2 < kMaxIntervals) {
-                ilo[m2] = r;
-                ihi[m2] = r;
-                ++m2;
-            } else {
-                atomicOr(status, 1u);
-            }
-        }
+        if (closed && centre && r >= 0. && r <= (double)nx) onSurface(r, r);
         const int s1 = edgeSide(ay, az, by, bz, py, pz);
         const int s2 = edgeSide(by, bz, cy, cz, py, pz);
         const int s3 = edgeSide(cy, cz, ay, az, py, pz);
@@ -162,7 +177,7 @@ __global__ void columnKernel(int nx, int ny, int nz, const double* tri, const in
         else s = (int)ceil(xi);
         if (s < 1 || s > nx - 2) continue;   // segments outside the flooded interior
         if (m == kMaxCrossings) {
-            atomicOr(status, 1u);
+            atomicOr(status, kTooManyCrossings);
             break;
         }
         seg[m++] = s;
@@ -186,7 +201,7 @@ __global__ void columnKernel(int nx, int ny, int nz, const double* tri, const in
             ++next;
         }
         bool on = false;
-        for (int k = 0; k < m2; ++k) on |= x >= ilo[k] - 1e-12 && x <= ihi[k] + 1e-12;
+        for (int k = 0; k < m2; ++k) on |= x >= runLo[k] && x <= runHi[k];
         flags[x * plane + col] = (inside || on) ? kVxInside : kVxOutside;
     }
     if (nx > 1) flags[(nx - 1) * plane + col] = kVxOutside;
@@ -226,8 +241,10 @@ extern "C" int plbgpu_voxelize(plbgpu_ctx* c, const double* triangles, size_t n_
     for (size_t i = 0; i < 9 * n_triangles; ++i)
         if (!std::isfinite(triangles[i])) return domainFail(c, PLBGPU_ERR_ARG, "voxelize: a vertex is not finite");
     // bin the triangles to the (y, z) lattice columns their projection covers
+    // (counted in 64 bits; the device lists take at most INT32_MAX entries)
     const int ncol = ny * nz;
-    std::vector<int> start((size_t)ncol + 1, 0), list;
+    std::vector<long long> count((size_t)ncol + 1, 0);
+    std::vector<int> start, list;
     auto span = [&](int t, int a, int dim, int& lo, int& hi) {
         const double* T = triangles + 9 * (size_t)t;
         const double mn = std::min(T[a], std::min(T[3 + a], T[6 + a])), mx = std::max(T[a], std::max(T[3 + a], T[6 + a]));
@@ -235,11 +252,15 @@ extern "C" int plbgpu_voxelize(plbgpu_ctx* c, const double* triangles, size_t n_
         hi = (int)std::min((double)dim - 1., std::max(-1., std::floor(mx + 1e-9)));
     };
     for (int pass = 0; pass < 2; ++pass) {
-        std::vector<int> fill;
+        std::vector<long long> fill;
         if (pass == 1) {
-            for (int k = 0; k < ncol; ++k) start[k + 1] += start[k];
-            list.resize((size_t)start[ncol]);
-            fill.assign(start.begin(), start.end() - 1);
+            for (int k = 0; k < ncol; ++k) count[k + 1] += count[k];
+            if (count[ncol] > (long long)INT32_MAX)
+                return domainFail(c, PLBGPU_ERR_ARG,
+                                  "voxelize: the triangles cover more than 2^31-1 (triangle, lattice line) pairs");
+            start.assign(count.begin(), count.end());
+            list.resize((size_t)count[ncol]);
+            fill.assign(count.begin(), count.end() - 1);
         }
         for (int t = 0; t < (int)n_triangles; ++t) {
             int y0, y1, z0, z1;
@@ -247,7 +268,7 @@ extern "C" int plbgpu_voxelize(plbgpu_ctx* c, const double* triangles, size_t n_
             span(t, 2, nz, z0, z1);
             for (int y = y0; y <= y1; ++y)
                 for (int z = z0; z <= z1; ++z) {
-                    if (pass == 0) ++start[(size_t)y * nz + z + 1];
+                    if (pass == 0) ++count[(size_t)y * nz + z + 1];
                     else list[(size_t)fill[(size_t)y * nz + z]++] = t;
                 }
         }
@@ -292,6 +313,10 @@ extern "C" int plbgpu_voxelize(plbgpu_ctx* c, const double* triangles, size_t n_
         snprintf(m, sizeof(m), "voxelize: %s", cudaGetErrorString(e));
         return domainFail(c, e == cudaErrorMemoryAllocation ? PLBGPU_ERR_NOMEM : PLBGPU_ERR_CUDA, m);
     }
-    if (status) return domainFail(c, PLBGPU_ERR_ARG, "voxelize: a lattice line crosses the surface more than 64 times");
+    if (status & kTooManyCrossings)
+        return domainFail(c, PLBGPU_ERR_ARG, "voxelize: a lattice line crosses the surface more than 64 times");
+    if (status & kTooManyRuns)
+        return domainFail(c, PLBGPU_ERR_ARG,
+                          "voxelize: a lattice line lies on the surface in more than 32 separate runs of cells");
     return PLBGPU_OK;
 }

@@ -47,6 +47,12 @@ class Context:
     def synchronize(self):
         N.check(self.h, self.lib.plbgpu_synchronize(self.h))
 
+    def fp64_rate(self) -> float:
+        """Measured FP64 pipe rate, adds + multiplies per second."""
+        v = ctypes.c_double()
+        N.check(self.h, self.lib.plbgpu_measure_fp64_rate(self.h, ctypes.byref(v)))
+        return float(v.value)
+
     def close(self):
         if self.h:
             self.lib.plbgpu_destroy(self.h)
@@ -201,11 +207,19 @@ class DeviceLattice3D:
         a = np.ascontiguousarray(f, np.float64).reshape(-1)
         self._check(self.lib.plbgpu_send(self.ctx.h, self.handle, *box, _dp(a), a.size))
 
-    def receive(self, box=None):
+    def receive(self, box=None, out=None):
+        """Populations of a box as [x][y][z][19] FP64 f-bar; `out` (a
+        C-contiguous float64 array of that many values) is filled and
+        returned instead of a new array."""
         box = self._box(box)
-        out = np.empty(self._cells(box) * 19, np.float64)
-        self._check(self.lib.plbgpu_receive(self.ctx.h, self.handle, *box, _dp(out), out.size))
-        return out.reshape(box[1] - box[0] + 1, box[3] - box[2] + 1, box[5] - box[4] + 1, 19)
+        shape = (box[1] - box[0] + 1, box[3] - box[2] + 1, box[5] - box[4] + 1, 19)
+        if out is None:
+            out = np.empty(shape, np.float64)
+        elif (out.dtype != np.float64 or not out.flags["C_CONTIGUOUS"] or out.size != self._cells(box) * 19):
+            raise ValueError(f"receive: out must be a C-contiguous float64 array of {self._cells(box) * 19} values")
+        flat = out.reshape(-1)
+        self._check(self.lib.plbgpu_receive(self.ctx.h, self.handle, *box, _dp(flat), flat.size))
+        return out.reshape(shape)
 
     # ----------------------------------------------------------------- stepping
     def collide_and_stream(self, nsteps=1, stats=False):

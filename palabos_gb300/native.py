@@ -66,6 +66,7 @@ SIGNATURES = {
     "plbgpu_destroy": [_vp],
     "plbgpu_launch_count": [_vp, ctypes.POINTER(ctypes.c_ulonglong)],
     "plbgpu_get_stream": [_vp, ctypes.POINTER(_vp)],
+    "plbgpu_measure_fp64_rate": [_vp, _c_dbl_p],
     "plbgpu_synchronize": [_vp],
     "plbgpu_add_domain": [_vp, _i, _i, _i, _i, _c_int_p],
     "plbgpu_remove_domain": [_vp, _i],

@@ -12,7 +12,7 @@ import lbcases
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 DRIVER = os.path.join(ROOT, "tests", "cpp", "_build", "plb_case_gpu")
-REFERENCE = "/root/reference"
+REFERENCE = os.environ.get("PALABOS_REFERENCE", "/root/reference")
 
 
 @pytest.mark.gpu

@@ -261,6 +261,36 @@ def test_error_paths_leave_context_usable():
     assert lat.internal_statistics()["count"] == 64
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32", "bf16"])
+def test_diverged_state_is_reported_and_cleared(precision):
+    """A NaN planted on the host in one fluid cell's populations (sent through
+    plbgpu_send) reaches the next statistics step's block sums: synchronize
+    reports PLBGPU_ERR_STATE once, and the domain keeps working once a finite
+    state is sent again."""
+    from palabos_gb300 import DeviceLattice3D, PlbGpuError
+    from palabos_gb300 import native as N
+    lat = DeviceLattice3D(12, 10, 16, 1.2, precision)
+    lat.periodicity(1, 1, 1)
+    f = np.zeros((12, 10, 16, 19))
+    lat.send(f)
+    lat.collide_and_stream(2, stats=True)
+    lat.ctx.synchronize()                       # finite state: nothing reported
+    bad = f.copy()
+    bad[5, 4, 7, 3] = np.nan
+    lat.send(bad)
+    lat.collide_and_stream(1, stats=False)      # no statistics: not looked at yet
+    lat.ctx.synchronize()
+    lat.collide_and_stream(1, stats=True)
+    with pytest.raises(PlbGpuError) as e:
+        lat.ctx.synchronize()
+    assert e.value.code == -5 and "non-finite" in str(e.value)
+    lat.ctx.synchronize()                       # reported once, then cleared
+    lat.send(f)
+    lat.collide_and_stream(3, stats=True)
+    st = lat.internal_statistics()
+    assert st["count"] == 12 * 10 * 16 and np.isfinite(st["avRhoBar"])
+
+
 def test_sparse_lattice_matches_reference_and_oracle():
     """A sparse lattice (computeSparseManagement over a 4x3x3 regular
     distribution): the kept blocks are the reference's; the fluid sealed off

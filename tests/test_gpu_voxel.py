@@ -47,6 +47,17 @@ def test_gpu_voxelizer_counts_edge_touches_as_touches():
     assert np.array_equal(np.isin(flags, (voxel.INSIDE, voxel.INNER_BORDER)), box)
 
 
+@pytest.mark.parametrize("width", (0, 1))
+def test_gpu_voxelizer_finely_meshed_faces_on_lattice_planes(width):
+    """A cuboid whose faces lie on lattice planes, every face cut into 20x20
+    squares: each lattice line in its y and z faces runs along some forty
+    facets parallel to x, whose on-surface cells form one run however many
+    facets cover them.  The GPU equals the oracle (the reference's flood)."""
+    shape = (26, 24, 28)
+    tri = meshes.cuboid((5, 6, 4), (20, 18, 22), (20, 20, 20))
+    assert np.array_equal(voxel.voxelize(tri, shape, width), O.voxelize(tri, shape, width))
+
+
 def test_gpu_voxelizer_large_sphere_matches_geometry():
     """256^3 box, 20480 facets: the inside set equals the analytic sphere
     away from the surface, and the border layers are one cell thick."""

@@ -1,8 +1,8 @@
 """The allocation-free reduction entry point, checked against plbgpu_reduce.
 
 plbgpu_reduce_noalloc is for callers that cannot call cudaMalloc themselves
-(for example work recorded into a CUDA graph under capture, or applications
-that manage a fixed device-memory budget): they pass their own device arrays
+(for example applications with their own device-memory pool or a fixed
+device-memory budget): they pass their own device arrays
 and result buffer, and the entry point keeps its scratch in a static device
 array instead of allocating.  Here the caller-owned device memory comes from
 torch; the lattice itself is built with the regular C ABI, and both entry
