@@ -210,6 +210,12 @@ int plbgpu_send(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1, int
                 const double* buf, size_t n);
 int plbgpu_receive(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1, int z0, int z1,
                    double* buf, size_t n);
+/* The same with FP32 records (19 floats per cell): the transfer of a
+ * single-precision lattice, CoProcessor3D<float>::send / receive. */
+int plbgpu_send_f32(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1, int z0, int z1,
+                    const float* buf, size_t n);
+int plbgpu_receive_f32(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1, int z0, int z1,
+                       float* buf, size_t n);
 
 /* ------------------------------------------------------------ time stepping */
 
@@ -422,6 +428,15 @@ int plbgpu_cp_send(plbgpu_ctx* ctx, int handle, long x0, long x1, long y0, long 
 int plbgpu_cp_receive(plbgpu_ctx* ctx, int handle, long x0, long x1, long y0, long y1, long z0, long z1,
                       char* data, size_t nbytes);
 int plbgpu_cp_collide_and_stream(plbgpu_ctx* ctx, int handle);
+/* plb::CoProcessor3D<float> (the reference's single-precision lattice,
+ * e.g. jlabos/src/testing/test_cylinder.py:96-97): an FP32 domain (FP32
+ * arithmetic and storage) whose `data` holds 19 floats per cell, nbytes =
+ * 76 * cells.  collideAndStream is plbgpu_cp_collide_and_stream. */
+int plbgpu_cp_add_domain_f32(plbgpu_ctx* ctx, long nx, long ny, long nz, double omega, int* handle);
+int plbgpu_cp_send_f32(plbgpu_ctx* ctx, int handle, long x0, long x1, long y0, long y1, long z0, long z1,
+                       const char* data, size_t nbytes);
+int plbgpu_cp_receive_f32(plbgpu_ctx* ctx, int handle, long x0, long x1, long y0, long y1, long z0, long z1,
+                          char* data, size_t nbytes);
 
 /* ------------------------------------------------------------ allocation-free form */
 

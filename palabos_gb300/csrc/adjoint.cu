@@ -470,12 +470,187 @@ __global__ void objectiveKernel(DevLattice L, const R* f, const double* v, bool 
     blockAdd(jsum, acc->objective);
 }
 
+// Reverse of a face cell's completion: lam = (d complete / d f)^T nu for the
+// wrapped regularized or Zou/He velocity or pressure condition of direction
+// DIR and orientation ORI (the forward map is completeFaceT of d3q19.cuh:
+// velFaceRhoBar / pressFaceJ, then regularizedComplete or zouHeComplete), in
+// exact arithmetic.  f is the streamed state before completion, v the face's
+// stored velocity (or density in v[0]).  The populations that enter from
+// outside (c[DIR] = -ORI) are overwritten unread: their entries of lam are 0.
+//
+// Forward, with w_i = 1 on c[DIR] = 0 and 2 on c[DIR] = ORI (the known
+// populations), e_i = c_i.j:
+//   velocity face: rhoBar = (sum_i w_i f_i - u_n) / (1 + u_n), j = (rhoBar + 1) u;
+//   pressure face: rhoBar = rho - 1,  j_DIR = ORI (sum_i w_i f_i - rhoBar);
+//   feq_i = t_i (rhoBar + 3 e_i + (4.5 e_i^2 - 1.5 j.j) / (rhoBar + 1));
+//   regularized: Pi = sum_known w_i c_i c_i^T (f_i - feq_i),
+//                out_i = feq_i + 4.5 t_i (c_i c_i^T - I/3) : Pi;
+//   Zou/He: f'_p = f_opp(p) - feq_opp(p) + feq_p on the incoming p, then the
+//           incoming diagonals p get c_p,d (j_d - sum_i c_i,d f'_i) / nd along
+//           the two tangential axes d.
+template <typename R, int FAM, int DIR, int ORI>
+__device__ __forceinline__ void completeFaceAdjT(const R* f, const double* v, const R* nu, R* lam) {
+    // the forward quantities the reverse needs
+    R rhoBar, j[3];
+    const R vel[3] = {(R)v[0], (R)v[1], (R)v[2]};
+    const R velNormal = (R)ORI * vel[DIR];
+    if (FAM == 0 || FAM == 2) {
+        rhoBar = velFaceRhoBar<R, DIR, ORI>(f, vel[DIR]);
+        const R rho = rhoBar + (R)1;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) j[d] = rho * vel[d];
+    } else {
+        rhoBar = (R)v[0] - (R)1;
+        pressFaceJ<R, DIR, ORI>(f, rhoBar, j);
+    }
+    const R invRho = (R)1 / (rhoBar + (R)1);
+    const R jSqr = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
+    R feqW[19];   // adjoint weight of each feq_i
+#pragma unroll
+    for (int i = 0; i < 19; ++i) {
+        lam[i] = R(0);
+        feqW[i] = R(0);
+    }
+    if (FAM < 2) {   // regularized
+        R nuPi[6];
+        int iPi = 0;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = a; b < 3; ++b) {
+                R s = R(0);
+#pragma unroll
+                for (int i = 0; i < 19; ++i) {
+                    const R q = a == b ? (R)(cdir(i, a) * cdir(i, a)) - (R)1 / (R)3 : (R)2 * (R)(cdir(i, a) * cdir(i, b));
+                    s += nu[i] * tw<R>(i) * q;
+                }
+                nuPi[iPi++] = (R)4.5 * s;
+            }
+#pragma unroll
+        for (int i = 0; i < 19; ++i) {
+            const int c = cdir(i, DIR);
+            R nuFneq = R(0);
+            if (c == 0 || c == ORI) {
+                iPi = 0;
+#pragma unroll
+                for (int a = 0; a < 3; ++a)
+#pragma unroll
+                    for (int b = a; b < 3; ++b) nuFneq += (R)(cdir(i, a) * cdir(i, b)) * nuPi[iPi++];
+                nuFneq *= (c == 0) ? (R)1 : (R)2;
+                lam[i] += nuFneq;
+            }
+            feqW[i] = nu[i] - nuFneq;
+        }
+    } else {         // Zou/He
+        constexpr int nd = subIndexCount<DIR, ORI>() - 1;
+        R nuP[19];
+#pragma unroll
+        for (int i = 0; i < 19; ++i) nuP[i] = nu[i];
+        R nuDiff[3] = {R(0), R(0), R(0)};
+        forEachZh<DIR, ORI, true>([&](auto p) {
+#pragma unroll
+            for (int s2 = 1; s2 < 3; ++s2) {
+                const int d = (DIR + s2) % 3;
+                nuDiff[d] += (R)cdir(p, d) * nu[p];
+            }
+        });
+        R jBarT[3] = {R(0), R(0), R(0)};
+#pragma unroll
+        for (int s2 = 1; s2 < 3; ++s2) {
+            const int d = (DIR + s2) % 3;
+            jBarT[d] = nuDiff[d] / (R)nd;
+#pragma unroll
+            for (int i = 0; i < 19; ++i) nuP[i] -= (R)cdir(i, d) * jBarT[d];
+        }
+        bool missing[19];
+#pragma unroll
+        for (int i = 0; i < 19; ++i) missing[i] = false;
+        forEachZh<DIR, ORI, false>([&](auto p) {
+            missing[p] = true;
+            const int o = opp(p);
+            lam[o] += nuP[p];
+            feqW[o] -= nuP[p];
+            feqW[p] += nuP[p];
+        });
+#pragma unroll
+        for (int i = 0; i < 19; ++i)
+            if (!missing[i]) lam[i] += nuP[i];
+        // the face's own j enters the tangential correction directly
+        if (FAM == 2) {
+            R rbT = R(0);
+#pragma unroll
+            for (int d = 0; d < 3; ++d) rbT += jBarT[d] * vel[d];
+            const R s = rbT / ((R)1 + velNormal);
+#pragma unroll
+            for (int i = 0; i < 19; ++i) {
+                const int c = cdir(i, DIR);
+                if (c == 0) lam[i] += s;
+                else if (c == ORI) lam[i] += (R)2 * s;
+            }
+        }
+    }
+    // through feq_i(rhoBar, j)
+    R rbBar = R(0), jBar[3] = {R(0), R(0), R(0)};
+#pragma unroll
+    for (int i = 0; i < 19; ++i) {
+        const R e = (R)cdir(i, 0) * j[0] + (R)cdir(i, 1) * j[1] + (R)cdir(i, 2) * j[2];
+        const R w = feqW[i] * tw<R>(i);
+        rbBar += w * ((R)1 - invRho * invRho * ((R)4.5 * e * e - (R)1.5 * jSqr));
+#pragma unroll
+        for (int d = 0; d < 3; ++d) jBar[d] += w * ((R)3 * (R)cdir(i, d) + invRho * ((R)9 * e * (R)cdir(i, d) - (R)3 * j[d]));
+    }
+    // through (rhoBar, j) to the known populations
+    if (FAM == 0 || FAM == 2) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) rbBar += jBar[d] * vel[d];
+        const R s = rbBar / ((R)1 + velNormal);
+#pragma unroll
+        for (int i = 0; i < 19; ++i) {
+            const int c = cdir(i, DIR);
+            if (c == 0) lam[i] += s;
+            else if (c == ORI) lam[i] += (R)2 * s;
+        }
+    } else {
+        const R s = (R)ORI * jBar[DIR];
+#pragma unroll
+        for (int i = 0; i < 19; ++i) {
+            const int c = cdir(i, DIR);
+            if (c == 0) lam[i] += s;
+            else if (c == ORI) lam[i] += (R)2 * s;
+        }
+    }
+}
+
+template <typename R, int FAM>
+__device__ __forceinline__ void completeFaceAdjFam(int sub, const R* f, const double* v, const R* nu, R* lam) {
+    switch (sub) {
+    case 0: completeFaceAdjT<R, FAM, 0, -1>(f, v, nu, lam); break;
+    case 1: completeFaceAdjT<R, FAM, 0, 1>(f, v, nu, lam); break;
+    case 2: completeFaceAdjT<R, FAM, 1, -1>(f, v, nu, lam); break;
+    case 3: completeFaceAdjT<R, FAM, 1, 1>(f, v, nu, lam); break;
+    case 4: completeFaceAdjT<R, FAM, 2, -1>(f, v, nu, lam); break;
+    default: completeFaceAdjT<R, FAM, 2, 1>(f, v, nu, lam); break;
+    }
+}
+
+template <typename R>
+__device__ __noinline__ void completeFaceAdj(int kind, const R* f, const double* v, const R* nu, R* lam) {
+    const int fam = (kind - K_REGVEL) / 6, sub = (kind - K_REGVEL) % 6;
+    switch (fam) {
+    case 0: completeFaceAdjFam<R, 0>(sub, f, v, nu, lam); break;
+    case 1: completeFaceAdjFam<R, 1>(sub, f, v, nu, lam); break;
+    case 2: completeFaceAdjFam<R, 2>(sub, f, v, nu, lam); break;
+    default: completeFaceAdjFam<R, 3>(sub, f, v, nu, lam); break;
+    }
+}
+
 // Reverse step of the face cells (regularized and Zou/He velocity and
-// pressure faces), one thread per cell of `faces`: the cell's local map
-// out = collide(complete(f)) (completion only when `pending`) is
-// differentiated in forward mode, one dual pass per input population and one
-// for omega, giving lambda^n = J^T mu and (d out / d omega)^T mu.  Face cells
-// are a thin layer, so twenty passes over them cost little next to the bulk.
+// pressure faces), one thread per cell of `faces`: the cell's local map is
+// out = collide(complete(f)) (completion only when `pending`, collision with
+// the BGK base), so lambda^n = (d complete / d f)^T (d collide / d g)^T mu
+// with g = complete(f): the BGK reverse of adjCell on the completed state,
+// then the closed-form reverse of the completion.  The omega derivative is
+// the collision's.
 template <typename R>
 __global__ void faceAdjointKernel(DevLattice L, const R* f, const R* lamIn, R* lamOut, double omega, bool pending,
                                   const long long* faces, int nFaces, AdjAcc* acc) {
@@ -486,30 +661,22 @@ __global__ void faceAdjointKernel(DevLattice L, const R* f, const R* lamIn, R* l
         const int z = (int)(idx % L.nz), y = (int)((idx / L.nz) % L.ny), x = (int)(idx / ((long long)L.ny * L.nz));
         const int k = L.flags[idx];
         const Neighbourhood nb = neighbourhood(L, x, y, z);
-        using FD = DualT<R>;   // the form's own arithmetic
-        R mu[19], fc[19];
+        R mu[19], fc[19], g[19], nu[19], F[3] = {R(0), R(0), R(0)}, gF[3] = {R(0), R(0), R(0)};
         mu[0] = lamIn[idx];
         for (int i = 1; i < 19; ++i) {
             long long off;
             mu[i] = nb.move(i, +1, off) ? lamIn[i * L.n + idx + off] : lamIn[opp(i) * L.n + idx];
         }
-        for (int i = 0; i < 19; ++i) fc[i] = f[i * L.n + idx];
-        // the completion overwrites the populations that entered from outside
-        // (c[DIR] = -ORI) without reading them: their rows of J^T are zero
-        const int sub = (k - K_REGVEL) % 6, fdir = sub >> 1, fori = (sub & 1) ? 1 : -1;
-        for (int dir = 0; dir <= 19; ++dir) {   // 0..18: population dir; 19: omega
-            if (dir < 19 && pending && cdir(dir, fdir) == -fori) {
-                lamOut[dir * L.n + idx] = R(0);
-                continue;
-            }
-            FD g[19], F[3];
-            for (int i = 0; i < 19; ++i) g[i] = FD(fc[i], i == dir ? 1. : 0.);
-            if (pending) completeIfFace<FD>(L, idx, k, g);
-            adjCollide<FD>(k, g, F, bgkConsts<FD>(FD(omega, dir == 19 ? 1. : 0.)), FD(0.));
-            R s = R(0);
-            for (int i = 0; i < 19; ++i) s += mu[i] * g[i].d;
-            if (dir < 19) lamOut[dir * L.n + idx] = s;
-            else go = (double)s;
+        for (int i = 0; i < 19; ++i) fc[i] = g[i] = f[i * L.n + idx];
+        if (pending) completeIfFace<R>(L, idx, k, g);
+        go = (double)adjCell<R>(K_BGK, g, F, (R)omega, R(0), mu, nu, gF);
+        if (pending) {
+            const double v[3] = {L.bc[idx], L.bc[L.n + idx], L.bc[2 * L.n + idx]};
+            R lam[19];
+            completeFaceAdj<R>(k, fc, v, nu, lam);
+            for (int i = 0; i < 19; ++i) lamOut[i * L.n + idx] = lam[i];
+        } else {
+            for (int i = 0; i < 19; ++i) lamOut[i * L.n + idx] = nu[i];
         }
     }
     blockAdd(go, acc->gOmega);

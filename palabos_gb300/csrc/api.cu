@@ -1064,7 +1064,26 @@ int plbgpu_initialize(plbgpu_ctx* c, int h) {
     return finishSurface(c, d);
 }
 
-int plbgpu_send(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, const double* buf, size_t n) {
+}  // extern "C"
+
+namespace {
+
+// plbgpu_send / plbgpu_receive for transfer records of B (double, or float
+// for the single-precision co-processor form).
+template <typename B>
+int insertRecords(const Launchers& L, const DevLattice& v, bool odd, const Box& b, const B* in, cudaStream_t s) {
+    if constexpr (sizeof(B) == sizeof(double)) return L.insert(v, odd, b, in, s);
+    else return L.insertF32(v, odd, b, in, s);
+}
+template <typename B>
+int extractRecords(const Launchers& L, const DevLattice& v, bool odd, const Box& b, int pending, B* out,
+                   cudaStream_t s) {
+    if constexpr (sizeof(B) == sizeof(double)) return L.extract(v, odd, b, pending, out, s);
+    else return L.extractF32(v, odd, b, pending, out, s);
+}
+
+template <typename B>
+int sendRecords(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, const B* buf, size_t n) {
     ProfRange prof("io");
     Domain* d;
     Box b;
@@ -1072,22 +1091,23 @@ int plbgpu_send(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, in
     if (rc) return rc;
     if ((rc = checkBox(c, d, x0, x1, y0, y1, z0, z1, &b))) return rc;
     long long cells = boxCells(b);
-    if (!buf || (long long)n != 19 * cells) return fail(c, PLBGPU_ERR_ARG, "send: %zu doubles for %lld cells", n, cells);
+    if (!buf || (long long)n != 19 * cells) return fail(c, PLBGPU_ERR_ARG, "send: %zu values for %lld cells", n, cells);
     if ((rc = materialize(c, d))) return rc;
     const Launchers& L = launchers(d->precision);
     if (const void* dp = directPointer(c, buf)) {
         // one pass: the insert kernel reads the caller's buffer itself
-        int k = L.insert(d->view(), d->odd, b, static_cast<const double*>(dp), c->stream);
+        int k = insertRecords<B>(L, d->view(), d->odd, b, static_cast<const B*>(dp), c->stream);
         c->launches += k - 1;
         if ((rc = launchBox(c))) return rc;
     } else {
         size_t stage = 0;
         forEachChunk(b, [](const Box&, size_t) { return PLBGPU_OK; }, &stage);
+        stage = stage / sizeof(double) * sizeof(B);
         if ((rc = ensureStaging(c, stage))) return rc;
         rc = forEachChunk(b, [&](const Box& s, size_t off) -> int {
-            CUDA_TRY(c, cudaMemcpyAsync(c->staging, buf + off, sizeof(double) * 19 * (size_t)boxCells(s),
+            CUDA_TRY(c, cudaMemcpyAsync(c->staging, buf + off, sizeof(B) * 19 * (size_t)boxCells(s),
                                         cudaMemcpyHostToDevice, c->stream));
-            int k = L.insert(d->view(), d->odd, s, static_cast<const double*>(c->staging), c->stream);
+            int k = insertRecords<B>(L, d->view(), d->odd, s, static_cast<const B*>(c->staging), c->stream);
             c->launches += k - 1;
             return launchBox(c);
         }, &stage);
@@ -1098,7 +1118,8 @@ int plbgpu_send(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, in
     return PLBGPU_OK;
 }
 
-int plbgpu_receive(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, double* buf, size_t n) {
+template <typename B>
+int receiveRecords(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, B* buf, size_t n) {
     ProfRange prof("io");
     Domain* d;
     Box b;
@@ -1106,25 +1127,26 @@ int plbgpu_receive(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0,
     if (rc) return rc;
     if ((rc = checkBox(c, d, x0, x1, y0, y1, z0, z1, &b))) return rc;
     long long cells = boxCells(b);
-    if (!buf || (long long)n != 19 * cells) return fail(c, PLBGPU_ERR_ARG, "receive: %zu doubles for %lld cells", n, cells);
+    if (!buf || (long long)n != 19 * cells) return fail(c, PLBGPU_ERR_ARG, "receive: %zu values for %lld cells", n, cells);
     if ((rc = checkStatus(c, d))) return rc;
     const Launchers& L = launchers(d->precision);
     const int pending = d->pending && d->bc ? 1 : 0;
     if (const void* dp = directPointer(c, buf)) {
         // one pass: the extract kernel writes the caller's buffer itself
-        int k = L.extract(d->view(), d->odd, b, pending, static_cast<double*>(const_cast<void*>(dp)), c->stream);
+        int k = extractRecords<B>(L, d->view(), d->odd, b, pending, static_cast<B*>(const_cast<void*>(dp)), c->stream);
         c->launches += k - 1;
         if ((rc = launchBox(c))) return rc;
     } else {
         size_t stage = 0;
         forEachChunk(b, [](const Box&, size_t) { return PLBGPU_OK; }, &stage);
+        stage = stage / sizeof(double) * sizeof(B);
         if ((rc = ensureStaging(c, stage))) return rc;
         rc = forEachChunk(b, [&](const Box& s, size_t off) -> int {
-            int k = L.extract(d->view(), d->odd, s, pending, static_cast<double*>(c->staging), c->stream);
+            int k = extractRecords<B>(L, d->view(), d->odd, s, pending, static_cast<B*>(c->staging), c->stream);
             c->launches += k - 1;
             int r = launchBox(c);
             if (r) return r;
-            CUDA_TRY(c, cudaMemcpyAsync(buf + off, c->staging, sizeof(double) * 19 * (size_t)boxCells(s),
+            CUDA_TRY(c, cudaMemcpyAsync(buf + off, c->staging, sizeof(B) * 19 * (size_t)boxCells(s),
                                         cudaMemcpyDeviceToHost, c->stream));
             return PLBGPU_OK;
         }, &stage);
@@ -1132,6 +1154,23 @@ int plbgpu_receive(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0,
     }
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     return PLBGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int plbgpu_send(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, const double* buf, size_t n) {
+    return sendRecords<double>(c, h, x0, x1, y0, y1, z0, z1, buf, n);
+}
+int plbgpu_receive(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, double* buf, size_t n) {
+    return receiveRecords<double>(c, h, x0, x1, y0, y1, z0, z1, buf, n);
+}
+int plbgpu_send_f32(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, const float* buf, size_t n) {
+    return sendRecords<float>(c, h, x0, x1, y0, y1, z0, z1, buf, n);
+}
+int plbgpu_receive_f32(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, float* buf, size_t n) {
+    return receiveRecords<float>(c, h, x0, x1, y0, y1, z0, z1, buf, n);
 }
 
 int plbgpu_collide_and_stream(plbgpu_ctx* c, int h, int nsteps, int collect_stats) {
@@ -2210,6 +2249,35 @@ int plbgpu_cp_receive(plbgpu_ctx* c, int handle, long x0, long x1, long y0, long
     }
     return plbgpu_receive(c, handle, (int)x0, (int)x1, (int)y0, (int)y1, (int)z0, (int)z1,
                           reinterpret_cast<double*>(data), nbytes / sizeof(double)) == PLBGPU_OK;
+}
+
+int plbgpu_cp_add_domain_f32(plbgpu_ctx* c, long nx, long ny, long nz, double omega, int* handle) {
+    if (!c || !handle || nx < 1 || ny < 1 || nz < 1 || nx > (1 << 30) || ny > (1 << 30) || nz > (1 << 30)) return 0;
+    int h;
+    if (plbgpu_add_domain(c, (int)nx, (int)ny, (int)nz, PLBGPU_FP32, &h) != PLBGPU_OK) return 0;
+    if (plbgpu_set_params(c, h, omega, 1.0, 0.0) != PLBGPU_OK) return 0;
+    *handle = h;
+    return 1;
+}
+
+int plbgpu_cp_send_f32(plbgpu_ctx* c, int handle, long x0, long x1, long y0, long y1, long z0, long z1,
+                       const char* data, size_t nbytes) {
+    if (nbytes % (19 * sizeof(float))) {
+        fail(c, PLBGPU_ERR_ARG, "co-processor send: %zu bytes is not a whole number of D3Q19 cells", nbytes);
+        return 0;
+    }
+    return plbgpu_send_f32(c, handle, (int)x0, (int)x1, (int)y0, (int)y1, (int)z0, (int)z1,
+                           reinterpret_cast<const float*>(data), nbytes / sizeof(float)) == PLBGPU_OK;
+}
+
+int plbgpu_cp_receive_f32(plbgpu_ctx* c, int handle, long x0, long x1, long y0, long y1, long z0, long z1,
+                          char* data, size_t nbytes) {
+    if (nbytes % (19 * sizeof(float))) {
+        fail(c, PLBGPU_ERR_ARG, "co-processor receive: %zu bytes is not a whole number of D3Q19 cells", nbytes);
+        return 0;
+    }
+    return plbgpu_receive_f32(c, handle, (int)x0, (int)x1, (int)y0, (int)y1, (int)z0, (int)z1,
+                              reinterpret_cast<float*>(data), nbytes / sizeof(float)) == PLBGPU_OK;
 }
 
 int plbgpu_cp_collide_and_stream(plbgpu_ctx* c, int handle) {

@@ -772,8 +772,10 @@ struct Box { int x0, x1, y0, y1, z0, z1; };
 // population planes are then written or read one cell per thread.
 constexpr int kXferCells = 128;
 
-template <typename S, bool ODD>
-__global__ void __launch_bounds__(kXferCells) extractKernel(DevLattice L, Box b, int pending, double* out) {
+// B: the element type of the transfer buffer (double, or float for the
+// single-precision co-processor form).
+template <typename S, bool ODD, typename B>
+__global__ void __launch_bounds__(kXferCells) extractKernel(DevLattice L, Box b, int pending, B* out) {
     using R = typename StoreT<S>::R;
     __shared__ double sh[kXferCells * 19];
     const int bnz = b.z1 - b.z0 + 1, bny = b.y1 - b.y0 + 1;
@@ -800,18 +802,18 @@ __global__ void __launch_bounds__(kXferCells) extractKernel(DevLattice L, Box b,
     }
     __syncthreads();
     const long long o0 = (((long long)blockIdx.z * bny + blockIdx.y) * bnz + dz0) * 19;
-    for (int q = t; q < cnt * 19; q += kXferCells) out[o0 + q] = sh[q];
+    for (int q = t; q < cnt * 19; q += kXferCells) out[o0 + q] = (B)sh[q];
 }
 
-template <typename S, bool ODD>
-__global__ void __launch_bounds__(kXferCells) insertKernel(DevLattice L, Box b, const double* in) {
+template <typename S, bool ODD, typename B>
+__global__ void __launch_bounds__(kXferCells) insertKernel(DevLattice L, Box b, const B* in) {
     __shared__ double sh[kXferCells * 19];
     const int bnz = b.z1 - b.z0 + 1, bny = b.y1 - b.y0 + 1;
     const int dz0 = blockIdx.x * kXferCells;
     const int cnt = min(kXferCells, bnz - dz0);
     const int t = threadIdx.x;
     const long long o0 = (((long long)blockIdx.z * bny + blockIdx.y) * bnz + dz0) * 19;
-    for (int q = t; q < cnt * 19; q += kXferCells) sh[q] = in[o0 + q];
+    for (int q = t; q < cnt * 19; q += kXferCells) sh[q] = (double)in[o0 + q];
     __syncthreads();
     if (t >= cnt) return;
     const int z = b.z0 + dz0 + t, y = b.y0 + blockIdx.y, x = b.x0 + blockIdx.z;

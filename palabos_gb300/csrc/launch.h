@@ -44,6 +44,9 @@ struct Launchers {
     // Edge or corner cells (x, y, z, kind) finished after a step.
     int (*surface)(const DevLattice&, bool odd, const int4* cells, int count, int pending, double invRho0,
                    double bbRho, double omega, cudaStream_t);
+    // The transfer layout with FP32 records (the single-precision co-processor form).
+    int (*extractF32)(const DevLattice&, bool odd, Box, int pending, float* out, cudaStream_t);
+    int (*insertF32)(const DevLattice&, bool odd, Box, const float* in, cudaStream_t);
 };
 
 const Launchers& launchersFp64();

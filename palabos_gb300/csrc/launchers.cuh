@@ -73,17 +73,31 @@ struct LaunchImpl {
         else completeFacesKernel<S, false><<<g, kBlock, 0, s>>>(L);
         return 1;
     }
-    static int extract(const DevLattice& L, bool odd, Box b, int pending, double* out, cudaStream_t s) {
+    template <typename B>
+    static int extractT(const DevLattice& L, bool odd, Box b, int pending, B* out, cudaStream_t s) {
         dim3 g = rowGrid(b.z1 - b.z0 + 1, b.y1 - b.y0 + 1, b.x1 - b.x0 + 1, kXferCells);
-        if (odd) extractKernel<S, true><<<g, kXferCells, 0, s>>>(L, b, pending, out);
-        else extractKernel<S, false><<<g, kXferCells, 0, s>>>(L, b, pending, out);
+        if (odd) extractKernel<S, true, B><<<g, kXferCells, 0, s>>>(L, b, pending, out);
+        else extractKernel<S, false, B><<<g, kXferCells, 0, s>>>(L, b, pending, out);
         return 1;
     }
-    static int insert(const DevLattice& L, bool odd, Box b, const double* in, cudaStream_t s) {
+    template <typename B>
+    static int insertT(const DevLattice& L, bool odd, Box b, const B* in, cudaStream_t s) {
         dim3 g = rowGrid(b.z1 - b.z0 + 1, b.y1 - b.y0 + 1, b.x1 - b.x0 + 1, kXferCells);
-        if (odd) insertKernel<S, true><<<g, kXferCells, 0, s>>>(L, b, in);
-        else insertKernel<S, false><<<g, kXferCells, 0, s>>>(L, b, in);
+        if (odd) insertKernel<S, true, B><<<g, kXferCells, 0, s>>>(L, b, in);
+        else insertKernel<S, false, B><<<g, kXferCells, 0, s>>>(L, b, in);
         return 1;
+    }
+    static int extract(const DevLattice& L, bool odd, Box b, int pending, double* out, cudaStream_t s) {
+        return extractT<double>(L, odd, b, pending, out, s);
+    }
+    static int insert(const DevLattice& L, bool odd, Box b, const double* in, cudaStream_t s) {
+        return insertT<double>(L, odd, b, in, s);
+    }
+    static int extractF32(const DevLattice& L, bool odd, Box b, int pending, float* out, cudaStream_t s) {
+        return extractT<float>(L, odd, b, pending, out, s);
+    }
+    static int insertF32(const DevLattice& L, bool odd, Box b, const float* in, cudaStream_t s) {
+        return insertT<float>(L, odd, b, in, s);
     }
     static int reduce(const DevLattice& L, bool odd, Box b, int pending, double invRho0, double bbRho,
                       ReduceAcc* acc, cudaStream_t s) {
@@ -128,7 +142,7 @@ struct LaunchImpl {
     }
     static const Launchers& table() {
         static const Launchers t = {step,  completeFaces, extract, insert, reduce,
-                                    equilibrium, field, rhoBarJ, surface};
+                                    equilibrium, field, rhoBarJ, surface, extractF32, insertF32};
         return t;
     }
 };

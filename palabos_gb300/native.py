@@ -100,6 +100,8 @@ SIGNATURES = {
     "plbgpu_initialize": [_vp, _i],
     "plbgpu_send": [_vp, _i, *BOX, _c_dbl_p, _sz],
     "plbgpu_receive": [_vp, _i, *BOX, _c_dbl_p, _sz],
+    "plbgpu_send_f32": [_vp, _i, *BOX, ctypes.POINTER(ctypes.c_float), _sz],
+    "plbgpu_receive_f32": [_vp, _i, *BOX, ctypes.POINTER(ctypes.c_float), _sz],
     "plbgpu_collide_and_stream": [_vp, _i, _i, _i],
     "plbgpu_get_stats": [_vp, _i, _c_dbl_p],
     "plbgpu_reduce": [_vp, _i, *BOX, _c_dbl_p, _c_dbl_p],
@@ -110,6 +112,9 @@ SIGNATURES = {
     "plbgpu_cp_send": [_vp, _i, *LBOX, ctypes.c_char_p, _sz],
     "plbgpu_cp_receive": [_vp, _i, *LBOX, ctypes.c_char_p, _sz],
     "plbgpu_cp_collide_and_stream": [_vp, _i],
+    "plbgpu_cp_add_domain_f32": [_vp, _l, _l, _l, _d, _c_int_p],
+    "plbgpu_cp_send_f32": [_vp, _i, *LBOX, ctypes.c_char_p, _sz],
+    "plbgpu_cp_receive_f32": [_vp, _i, *LBOX, ctypes.c_char_p, _sz],
     "plbgpu_voxelize": [_vp, _c_dbl_p, _sz, _i, _i, _i, _i, ctypes.POINTER(ctypes.c_int32), _sz],
     "plbgpu_adjoint_forward": [_vp, _i, _i, _i],
     "plbgpu_adjoint_interval": [_vp, _i, _c_int_p],

@@ -39,20 +39,41 @@ def test_cpp_driver_reproduces_reference_golden(name):
 
 
 @pytest.mark.slow
-def test_coprocessor_adapter_compiles_against_reference():
-    """plbgpu::GpuD3Q19CoProcessor3D<double> derives from the reference's
-    plb::CoProcessor3D<double> and links with the reference library."""
+def test_coprocessor_adapter_runs_reference_coprocessor_path():
+    """plbgpu::GpuD3Q19CoProcessor3D<T> (include/plbgpu_coprocessor3d.hh)
+    registered as the reference's default co-processor and driven through the
+    reference's own wiring -- initiateCoProcessors, transferToCoProcessors,
+    MultiBlockLattice3D::collideAndStream, transferFromCoProcessors
+    (coProcessors/coProcessorCommunication3D.hh:34-125) -- on a 2x2x1-block
+    BGK lattice, against the reference's example co-processor
+    (D3Q19ExampleCoProcessor3D).  The device calls go to a CPU stand-in built
+    on the oracle (tests/cpp/fake_plbgpu_cp.cpp); the GPU's co-processor calls
+    are checked against the same oracle on the GPU.  T = double is bit for
+    bit, T = float (FP32 records) to FP32 rounding."""
     lib = os.path.join(ROOT, "oracle", "_ref", "libplb.a")
+    orc = os.path.join(ROOT, "oracle", "_build")
     if not os.path.isdir(os.path.join(REFERENCE, "src")) or not os.path.exists(lib):
         pytest.skip("reference sources / library not present")
-    gpu_lib = os.path.join(ROOT, "palabos_gb300", "_lib")
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
     src = os.path.join(REFERENCE, "src")
+    inc = ["-I", src, "-I", os.path.join(src, "externalLibraries"), "-I",
+           os.path.join(src, "externalLibraries", "tinyxml"), "-I", os.path.join(ROOT, "include")]
     with tempfile.TemporaryDirectory() as tmp:
-        exe = os.path.join(tmp, "adapter")
-        subprocess.run(["g++", "-std=c++11", "-O1", "-w", "-I", src, "-I", os.path.join(src, "externalLibraries"),
-                        "-I", os.path.join(src, "externalLibraries", "tinyxml"), "-I", os.path.join(ROOT, "include"),
-                        os.path.join(ROOT, "tests", "cpp", "coprocessor_adapter_check.cpp"), lib,
-                        "-L", gpu_lib, "-lplbgpu", f"-Wl,-rpath,{gpu_lib}", "-o", exe], check=True)
+        fake = os.path.join(tmp, "fake.o")
+        drv = os.path.join(tmp, "e2e.o")
+        exe = os.path.join(tmp, "e2e")
+        subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), "-c",
+                        os.path.join(ROOT, "tests", "cpp", "fake_plbgpu_cp.cpp"), "-o", fake], check=True)
+        subprocess.run(["g++", "-std=c++11", "-O1", "-w", *inc, "-c",
+                        os.path.join(ROOT, "tests", "cpp", "coprocessor_e2e.cpp"), "-o", drv], check=True)
+        subprocess.run(["g++", drv, fake, lib, "-L", orc, "-lplboracle", f"-Wl,-rpath,{orc}", "-o", exe],
+                       check=True)
         out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
-    assert "addDomain=0 context=no" in out or "addDomain=1 context=yes" in out
-    assert "energy=" in out
+    rows = {}
+    for line in out.splitlines():
+        kv = dict(t.split("=") for t in line.split()[1:])
+        rows[line.split()[0]] = kv
+    assert rows["double"]["domains"] == "4/4" and rows["float"]["domains"] == "4/4", out
+    assert float(rows["double"]["maxabs"]) > 1e-3, out          # the flow is not trivial
+    assert float(rows["double"]["maxdiff"]) == 0.0, out
+    assert float(rows["float"]["maxdiff"]) <= 1e-6 * float(rows["float"]["maxabs"]), out

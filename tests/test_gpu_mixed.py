@@ -3,8 +3,12 @@ storage) against the reference's FP64 golden results.
 
 These forms do not reproduce the reference bit for bit; the bound is on the
 largest population error relative to the largest |f-bar| of the case, with
-the tolerance of each storage type written here.  They run through the same
-C ABI, including the staged (bulk-copy) row kernel of the 2- and 4-byte forms.
+the tolerance of each storage type written here (about twice the largest
+error measured on a GB300 over these cases: FP32 6.1e-6, FP16 8.9e-4, BF16
+8.5e-3, BF16 with stochastic rounding 1.2e-2).  They run through the same C
+ABI and the same interior-row kernels as production runs: the 128-bit
+eight-cell kernel of the 2-byte forms where rows hold a multiple of eight
+cells, the one-cell kernel otherwise.
 """
 import numpy as np
 import pytest
@@ -15,7 +19,7 @@ from palabos_gb300 import lattice_from_description
 pytestmark = pytest.mark.gpu
 
 # max |f - f_ref| / max |f_ref| after the case's steps
-TOL = {"fp32": 2e-5, "fp16": 1e-2, "bf16": 6e-2, "bf16sr": 6e-2}
+TOL = {"fp32": 1.5e-5, "fp16": 2e-3, "bf16": 1.5e-2, "bf16sr": 2.5e-2}
 CASES = ["periodic_bgk", "cavity_bb_lid", "channel_sphere", "guo_channel", "regvel_faces",
          "zhpress_faces", "incbgk_nodyn", "mebb_walls", "velocity_box"]
 
@@ -59,9 +63,10 @@ def test_reduced_precision_external_form(name, precision):
 
 
 @pytest.mark.parametrize("precision", ["fp32", "bf16"])
-def test_staged_rows_match_unstaged_geometry(precision):
-    """nz a multiple of the 16-byte copy granule (staged row kernel) and nz odd
-    (register row kernel) must give the same physics on the same flow."""
+def test_row_kernels_agree_across_row_lengths(precision):
+    """nz = 32 (the 128-bit eight-cell kernel for BF16, the one-cell kernel for
+    FP32) and nz = 33 (the one-cell kernel) give the same physics on a flow
+    that depends only on y."""
     from palabos_gb300 import DeviceLattice3D
     out = []
     for nz in (32, 33):

@@ -230,6 +230,32 @@ def test_coprocessor_form_matches_block_lattice():
     assert lib.plbgpu_cp_collide_and_stream(ctx.h, 12345) == 0
 
 
+def test_coprocessor_form_single_precision():
+    """plbgpu_cp_*_f32: CoProcessor3D<float> -- an FP32 domain exchanging 19
+    floats per cell -- against the oracle's FP64 BlockLattice3D run of the same
+    block, to FP32 rounding."""
+    import ctypes
+    from palabos_gb300 import default_context
+    ctx = default_context()
+    lib = ctx.lib
+    nx, ny, nz, omega = 9, 7, 16, 1.3
+    h = ctypes.c_int()
+    assert lib.plbgpu_cp_add_domain_f32(ctx.h, nx, ny, nz, omega, ctypes.byref(h)) == 1
+    f0 = lbcases.initial_state((nx, ny, nz), np.random.default_rng(6)).astype(np.float32)
+    data = np.ascontiguousarray(f0).tobytes()
+    assert lib.plbgpu_cp_send_f32(ctx.h, h.value, 0, nx - 1, 0, ny - 1, 0, nz - 1, data, len(data)) == 1
+    for _ in range(5):
+        assert lib.plbgpu_cp_collide_and_stream(ctx.h, h.value) == 1
+    out = ctypes.create_string_buffer(len(data))
+    assert lib.plbgpu_cp_receive_f32(ctx.h, h.value, 0, nx - 1, 0, ny - 1, 0, nz - 1, out, len(data)) == 1
+    got = np.frombuffer(out.raw, np.float32).reshape(nx, ny, nz, 19)
+    ol = O.OracleLattice(nx, ny, nz, (0, 0, 0), omega, np.zeros((nx, ny, nz), np.uint8))
+    ref, _ = ol.run(f0.astype(np.float64), 5)
+    assert np.abs(got - ref).max() <= 2e-5 * np.abs(ref).max()
+    # FP32 records: a byte count of doubles is not a whole number of cells here
+    assert lib.plbgpu_cp_send_f32(ctx.h, h.value, 0, nx - 1, 0, ny - 1, 0, nz - 1, data, len(data) - 4) == 0
+
+
 def test_equilibrium_initialization_matches_oracle_formula():
     """initializeAtEquilibrium: f-bar = t_i (rhoBar + 3 c.j + invRho(4.5 (c.j)^2 - 1.5 j^2)), 0 on walls."""
     nx, ny, nz = 6, 5, 4

@@ -52,10 +52,17 @@ def test_gpu_voxelizer_finely_meshed_faces_on_lattice_planes(width):
     """A cuboid whose faces lie on lattice planes, every face cut into 20x20
     squares: each lattice line in its y and z faces runs along some forty
     facets parallel to x, whose on-surface cells form one run however many
-    facets cover them.  The GPU equals the oracle (the reference's flood)."""
+    facets cover them.  The GPU gives exactly the flags of the same box meshed
+    with two triangles per face, on which it equals the oracle (the
+    reference's flood).  On the subdivided mesh the oracle itself does not: its
+    flood meets facet edges head-on along many diagonal neighbour segments and
+    merges the equal-distance crossings there (the edge-touch defect of the
+    reference's flood), misplacing some 700 cells."""
     shape = (26, 24, 28)
-    tri = meshes.cuboid((5, 6, 4), (20, 18, 22), (20, 20, 20))
-    assert np.array_equal(voxel.voxelize(tri, shape, width), O.voxelize(tri, shape, width))
+    fine = voxel.voxelize(meshes.cuboid((5, 6, 4), (20, 18, 22), (20, 20, 20)), shape, width)
+    coarse_tri = meshes.cuboid((5, 6, 4), (20, 18, 22), (1, 1, 1))
+    assert np.array_equal(fine, voxel.voxelize(coarse_tri, shape, width))
+    assert np.array_equal(fine, O.voxelize(coarse_tri, shape, width))
 
 
 def test_gpu_voxelizer_large_sphere_matches_geometry():
