@@ -279,6 +279,42 @@ def time_form(lat, steps, warmup):
     return lat.time_steps(steps, stats=False)
 
 
+def sparse_throughput(n=256, radius=110.0, block=16, steps=200, precisions=("fp64", "fp32", "bf16"), ctx=None):
+    """Flow outside a voxelized sphere in a periodic n^3 box (Guo force along
+    x), blocks of block^3 cells: the blocks deep inside the sphere hold
+    neither fluid nor wall and leave the lattice (computeSparseManagement).
+    MLUPS over the cells of the kept blocks, against the same geometry with
+    every block kept (the sphere's interior as no-dynamics cells)."""
+    from palabos_gb300 import DeviceLattice3D, meshes, voxel
+    from palabos_gb300 import native as N
+    shape = (n, n, n)
+    c = (n / 2 - 0.37, n / 2 + 0.21, n / 2 - 0.13)
+    flags = voxel.voxelize(meshes.sphere(c, radius, 20000), shape, ctx=ctx)
+    kinds = voxel.kinds_from_flags(flags, "outside", fluid=N.GUO)
+    blocks = (n // block,) * 3
+    out = {"workload": f"sphere_exterior_{n}^3_r{radius:g}_blocks{block}^3", "steps": steps}
+    for prec in precisions:
+        res = {}
+        for sparse in (False, True):
+            lat = DeviceLattice3D(n, n, n, 1.7, prec, ctx)
+            lat.periodicity(1, 1, 1)
+            lat.set_kinds(kinds)
+            kept = n ** 3
+            if sparse:
+                keep = lat.select_sparse_blocks((kinds != N.NODYNAMICS).astype(np.int32), blocks)
+                kept = int(keep.sum()) * block ** 3
+                res["kept_blocks"] = f"{int(keep.sum())}/{keep.size}"
+            lat.set_external_vector(None, np.array([1e-6, 0.0, 0.0]))
+            lat.initialize_at_equilibrium(None, 1.0, (0.0, 0.0, 0.0))
+            lat.collide_and_stream(10)
+            ms = lat.time_steps(steps) / steps
+            res["sparse_mlups_kept" if sparse else "dense_mlups"] = round(kept / (ms * 1e-3) / 1e6, 1)
+            res["sparse_ms" if sparse else "dense_ms"] = round(ms, 4)
+            lat.close()
+        out[prec] = res
+    return out
+
+
 def run_gpu(args):
     ws, rank, local = dist_env()
     dist = init_dist(ws)
@@ -318,36 +354,52 @@ def run_gpu(args):
     traffic = load_traffic(f"stepKernel_{head}_channel_sphere")
     fp64_rate = ctx.fp64_rate() if head == "fp64" else None
 
-    # e2e through the C ABI with host buffers: an ordinary (pageable) host
-    # array holding the FP64 state, allocated and touched before the timed
-    # region, sent at the start and received into at the end
-    f_host = np.empty(SHAPE + (19,))
-    lat.receive(out=f_host)
+    # e2e through the C ABI with host buffers: the FP64 state in pinned host
+    # memory (allocated and touched before the timed region), sent at the
+    # start, drag read every 100 steps, state received into the same buffer at
+    # the end; then the same with an ordinary pageable array
     e2e_steps = K
-    barrier(dist)
-    t0 = time.perf_counter()
-    lat.send(f_host)
-    t_sent = time.perf_counter()
-    done = 0
-    while done < e2e_steps:
-        chunk = min(STATS_EVERY, e2e_steps - done)
-        lat.collide_and_stream(chunk, stats=True)
-        lat.internal_statistics()      # drag to the host (synchronizes)
-        done += chunk
-    t_recv = time.perf_counter()
-    lat.receive(out=f_host)
-    t1 = time.perf_counter()
-    e2e_s = max_over_ranks(dist, t1 - t0)
     state_bytes = cells * 19 * 8   # the ABI exchanges FP64 f-bar
     nread = (e2e_steps + STATS_EVERY - 1) // STATS_EVERY
-    e2e = {"value": round(ws * cells * e2e_steps / e2e_s / 1e6, 2), "unit": "MLUPS",
+
+    def e2e_run(f_host):
+        lat.receive(out=f_host)
+        barrier(dist)
+        t0 = time.perf_counter()
+        lat.send(f_host)
+        t_sent = time.perf_counter()
+        done = 0
+        while done < e2e_steps:
+            chunk = min(STATS_EVERY, e2e_steps - done)
+            lat.collide_and_stream(chunk, stats=True)
+            lat.internal_statistics()      # drag to the host (synchronizes)
+            done += chunk
+        t_recv = time.perf_counter()
+        lat.receive(out=f_host)
+        t1 = time.perf_counter()
+        e2e_s = max_over_ranks(dist, t1 - t0)
+        return (round(ws * cells * e2e_steps / e2e_s / 1e6, 2), round(state_bytes / (t_sent - t0) / 1e9, 1),
+                round(state_bytes / (t1 - t_recv) / 1e9, 1))
+
+    try:
+        import torch
+        pinned = torch.empty(SHAPE + (19,), dtype=torch.float64, pin_memory=True).numpy()
+        pinned[...] = 0.0
+        host_kind = "pinned"
+    except Exception:   # no torch or no pinned allocation: pageable only
+        pinned, host_kind = np.zeros(SHAPE + (19,)), "pageable"
+    v_e2e, h2d, d2h = e2e_run(pinned)
+    pageable = np.zeros(SHAPE + (19,))
+    v_pg, h2d_pg, d2h_pg = e2e_run(pageable)
+    e2e = {"value": v_e2e, "unit": "MLUPS",
            "h2d_bytes_per_step": round(state_bytes / e2e_steps, 1),
            "d2h_bytes_per_step": round((state_bytes + 56 * nread) / e2e_steps, 1),
-           "h2d_gbs": round(state_bytes / (t_sent - t0) / 1e9, 1),
-           "d2h_gbs": round(state_bytes / (t1 - t_recv) / 1e9, 1),
-           "note": "FP64 state in a pageable host array, sent once and received once per run of K steps "
-                   "(read and written by the transfer kernels directly where the GPU uses the host's page "
-                   "tables, else staged in 64 MiB chunks); drag read every 100 steps"}
+           "h2d_gbs": h2d, "d2h_gbs": d2h, "host_memory": host_kind,
+           "pageable": {"value": v_pg, "h2d_gbs": h2d_pg, "d2h_gbs": d2h_pg},
+           "note": f"FP64 state in {host_kind} host memory, sent once and received once per run of K steps "
+                   "(the transfer kernels read and write the host buffer directly over NVLink-C2C); drag read "
+                   "every 100 steps; 'pageable' repeats it with an ordinary numpy array"}
+    del pinned, pageable
     lat.close()
 
     # the other storage forms on the same workload (kernel-only rate)
@@ -444,6 +496,8 @@ def main():
     ap.add_argument("--drag-gradient", action="store_true",
                     help="run only the channel-past-a-sphere drag-gradient study (256x128x128, 10000 steps)")
     ap.add_argument("--drag-gradient-steps", type=int, default=10000)
+    ap.add_argument("--sparse", action="store_true",
+                    help="run only the sparse-domain throughput study (voxelized sphere exterior, 256^3)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -460,6 +514,11 @@ def main():
         ctx = Context(dist_env()[2])
         r = drag_gradient_study(steps=args.drag_gradient_steps, ctx=ctx)
         print(json.dumps({"study": "channel_sphere_drag_gradient", **r}))
+        return
+    if args.sparse:
+        from palabos_gb300 import Context
+        ctx = Context(dist_env()[2])
+        print(json.dumps({"study": "sparse_sphere_exterior", **sparse_throughput(ctx=ctx)}))
         return
     if args.permeability:
         from palabos_gb300 import Context

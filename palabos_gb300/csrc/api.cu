@@ -69,6 +69,8 @@ struct Domain {
     void* ext = nullptr;         // 4 * n of FP64 or FP32: external rho-bar, jx, jy, jz
     uint32_t* mebb = nullptr;    // n
     int4* surf = nullptr;        // edge cells, then corner cells: (x, y, z, kind)
+    int2* rowLists = nullptr;    // sparse domains: dense rows, then general rows (x, y)
+    int nDense = 0, nGeneral = 0, rowListCap = 0;
     int surfCap = 0, nEdges = 0, nCorners = 0;
     bool hasSurface = false;     // any edge or corner kind
     bool sparse = false;         // any cell outside the lattice (K_NONE)
@@ -100,6 +102,11 @@ struct Domain {
         L.n = n;
         L.status = status;
         L.rowForm = 0;
+        const bool lists = sparse && rowLists;
+        L.denseRows = lists && nDense ? rowLists : nullptr;
+        L.nDense = lists ? nDense : 0;
+        L.generalRows = lists && nGeneral ? rowLists + nDense : nullptr;
+        L.nGeneral = lists ? nGeneral : 0;
         return L;
     }
 };
@@ -303,6 +310,20 @@ __global__ void mebbMaskKernel(DevLattice L, uint32_t* out) {
     out[idx] = m;
 }
 
+// Per row (x, y): bit 0 some cell is part of the lattice, bit 1 every cell is.
+__global__ void rowLiveKernel(const uint8_t* flags, int rows, int nz, uint8_t* live) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    bool any = false, all = true;
+    const uint8_t* f = flags + (long long)r * nz;
+    for (int z = 0; z < nz; ++z) {
+        const bool in = f[z] != K_NONE;
+        any |= in;
+        all &= in;
+    }
+    live[r] = (uint8_t)((any ? 1 : 0) | (all ? 2 : 0));
+}
+
 __global__ void kindMaskKernel(const uint8_t* flags, long long n, unsigned long long* mask) {
     unsigned long long m = 0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
@@ -427,6 +448,54 @@ int kindMask(plbgpu_ctx* c, Domain* d, unsigned long long* mask) {
     return PLBGPU_OK;
 }
 
+// The row lists of a sparse domain: rows whose 3x3 neighbourhood of rows is
+// entirely part of the lattice ("dense": the interior-row kernels step them,
+// their neighbours never fall outside), then the other rows with a live cell
+// (the general kernel, which treats a neighbour outside the lattice like the
+// domain edge).  Rows without live cells are left out.
+int buildRowLists(plbgpu_ctx* c, Domain* d) {
+    const int rows = d->nx * d->ny;
+    int rc = ensureStaging(c, (size_t)rows);
+    if (rc) return rc;
+    uint8_t* dl = static_cast<uint8_t*>(c->staging);
+    rowLiveKernel<<<(rows + 255) / 256, 256, 0, c->stream>>>(d->flags, rows, d->nz, dl);
+    if ((rc = launchBox(c))) return rc;
+    std::vector<uint8_t> live((size_t)rows);
+    CUDA_TRY(c, cudaMemcpyAsync(live.data(), dl, (size_t)rows, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    std::vector<int2> dense, general;
+    for (int x = 0; x < d->nx; ++x)
+        for (int y = 0; y < d->ny; ++y) {
+            const uint8_t l = live[(size_t)x * d->ny + y];
+            if (!(l & 1)) continue;
+            bool full = x >= 1 && x <= d->nx - 2 && y >= 1 && y <= d->ny - 2;
+            for (int dx = -1; dx <= 1 && full; ++dx)
+                for (int dy = -1; dy <= 1 && full; ++dy) full = (live[(size_t)(x + dx) * d->ny + (y + dy)] & 2) != 0;
+            (full ? dense : general).push_back(make_int2(x, y));
+        }
+    const int total = (int)(dense.size() + general.size());
+    if (total > d->rowListCap) {
+        if (d->rowLists) {
+            CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+            cudaFree(d->rowLists);
+            d->deviceBytes -= sizeof(int2) * (size_t)d->rowListCap;
+            d->rowLists = nullptr;
+            d->rowListCap = 0;
+        }
+        CUDA_TRY(c, cudaMalloc(&d->rowLists, sizeof(int2) * (size_t)(total > 0 ? total : 1)));
+        d->rowListCap = total > 0 ? total : 1;
+        d->deviceBytes += sizeof(int2) * (size_t)d->rowListCap;
+    }
+    dense.insert(dense.end(), general.begin(), general.end());
+    if (total)
+        CUDA_TRY(c, cudaMemcpyAsync(d->rowLists, dense.data(), sizeof(int2) * (size_t)total, cudaMemcpyHostToDevice,
+                                    c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    d->nDense = total - (int)general.size();
+    d->nGeneral = (int)general.size();
+    return PLBGPU_OK;
+}
+
 int syncKinds(plbgpu_ctx* c, Domain* d) {
     unsigned long long m = 0;
     int rc = kindMask(c, d, &m);
@@ -437,6 +506,7 @@ int syncKinds(plbgpu_ctx* c, Domain* d) {
     d->hasSurface = surface;
     d->surfDirty = true;
     d->sparse = (m >> 63) & 1;   // kinds >= 63: only K_NONE
+    if (d->sparse && (rc = buildRowLists(c, d))) return rc;
     return ensureAux(c, d, faces, (m >> K_GUO) & 1, (m >> K_MEBB) & 1);
 }
 
@@ -652,7 +722,11 @@ int plbgpu_create(int device, plbgpu_ctx** out) {
     const char* staged = getenv("PLBGPU_STAGED_TRANSFERS");
     c->forceStaged = staged && staged[0] == '1';
     const char* rowKernel = getenv("PLBGPU_ROW_KERNEL");
-    c->rowForm = rowKernel && strcmp(rowKernel, "cell") == 0 ? 1 : 0;
+    c->rowForm = !rowKernel                           ? 0
+                 : strcmp(rowKernel, "cell") == 0     ? 1
+                 : strcmp(rowKernel, "vec4") == 0     ? 2
+                 : strcmp(rowKernel, "pair") == 0     ? 3
+                                                      : 0;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete c;
         return PLBGPU_ERR_CUDA;
@@ -760,6 +834,7 @@ int plbgpu_remove_domain(plbgpu_ctx* c, int h) {
     if (d->ext) cudaFree(d->ext);
     if (d->mebb) cudaFree(d->mebb);
     if (d->surf) cudaFree(d->surf);
+    if (d->rowLists) cudaFree(d->rowLists);
     cudaFree(d->stats);
     cudaFree(d->status);
     cudaFree(d->red);

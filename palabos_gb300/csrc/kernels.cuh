@@ -152,7 +152,15 @@ struct DevLattice {
     int per[3];
     long long n;
     unsigned* status;       // device error word (kStatusNonFinite)
-    int rowForm;            // interior-row kernel: 0 the fastest for the storage type, 1 one cell per thread
+    int rowForm;            // interior-row kernel of the 2-byte forms: 0 eight cells per thread (128-bit
+                            // vectors), 1 one cell per thread (every form), 2 four cells (64-bit), 3 two cells
+    // Sparse domains: the rows (x, y) the interior-row kernels may take -- the
+    // 3x3 rows around them hold no cell outside the lattice -- and the other
+    // rows with live cells, which take the general kernel (null: no lists).
+    const int2* denseRows;
+    int nDense;
+    const int2* generalRows;
+    int nGeneral;
 };
 
 // Bits of DevLattice::status.  A statistics step that meets a NaN or an
@@ -580,7 +588,13 @@ __global__ void __launch_bounds__(128, RowShape<S>::blocks)
     rowStepKernel(DevLattice L, Planes<S> Pl, Deltas D, StepParams<typename StoreT<S>::R> P, StatsAcc* acc) {
     using R = typename StoreT<S>::R;
     constexpr int NC = RowShape<S>::cells;
-    const int x = blockIdx.z + 1, y = blockIdx.y + 1;
+    int x = blockIdx.z + 1, y = blockIdx.y + 1;
+    if (L.denseRows) {   // whole blocks leave: the row is the block's
+        const int r = blockIdx.y + gridDim.y * blockIdx.z;
+        if (r >= L.nDense) return;
+        x = L.denseRows[r].x;
+        y = L.denseRows[r].y;
+    }
     const int z0 = blockIdx.x * blockDim.x * NC + threadIdx.x;
     R f[NC][19];
     int kind[NC];
@@ -628,7 +642,13 @@ template <typename S, bool ODD, bool STATS, bool EXT>
 __global__ void __launch_bounds__(128, 8)
     pairRowStepKernel(DevLattice L, Planes<S> Pl, Deltas D, StepParams<typename StoreT<S>::R> P, StatsAcc* acc) {
     using R = typename StoreT<S>::R;
-    const int x = blockIdx.z + 1, y = blockIdx.y + 1;
+    int x = blockIdx.z + 1, y = blockIdx.y + 1;
+    if (L.denseRows) {   // whole blocks leave: the row is the block's
+        const int r = blockIdx.y + gridDim.y * blockIdx.z;
+        if (r >= L.nDense) return;
+        x = L.denseRows[r].x;
+        y = L.denseRows[r].y;
+    }
     const int zA = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     double sR = 0., sU = 0.;
     unsigned long long cnt = 0, mx = 0;
@@ -713,7 +733,8 @@ __global__ void __launch_bounds__(128, 8)
 // (periodic wrap and the domain-edge rule on every axis).  Row
 // blockIdx.y + gridDim.y * blockIdx.z enumerates the border rows: x = 0,
 // x = nx-1 (all y), then y = 0, y = ny-1 (1 <= x <= nx-2); when nx < 3 or
-// ny < 3, or on a sparse domain, every row is a border row.
+// ny < 3 every row is a border row; on a sparse domain the rows are its
+// list of general rows (or every row when it has no lists).
 template <typename S, bool ODD, bool STATS, bool EXT, bool SPARSE>
 __global__ void __launch_bounds__(128, sizeof(S) <= 4 ? 6 : 1) edgeRowStepKernel(DevLattice L, StepParams<typename StoreT<S>::R> P,
                                                           StatsAcc* acc, int rows) {
@@ -723,7 +744,10 @@ __global__ void __launch_bounds__(128, sizeof(S) <= 4 ? 6 : 1) edgeRowStepKernel
     if (row >= rows) return;   // whole blocks
     const int nx = L.nx, ny = L.ny;
     int x, y;
-    if (SPARSE || nx < 3 || ny < 3) {
+    if (SPARSE && L.generalRows) {
+        x = L.generalRows[row].x;
+        y = L.generalRows[row].y;
+    } else if (SPARSE || nx < 3 || ny < 3) {
         x = row / ny;
         y = row - x * ny;
     } else if (row < ny) {

@@ -16,19 +16,34 @@ struct StepLaunch {
 
     // Row kernel of this storage type: the paired kernel for the 2-byte forms
     // when rows have an even length, the one-cell register kernel otherwise.
-    static bool pairedRows(const DevLattice& L) { return sizeof(S) == 2 && L.nz % 2 == 0 && L.rowForm == 0; }
-    // Eight cells per thread, 128-bit population vectors (vecrow.cuh): rows of
-    // a multiple of eight cells.
-    static bool vectorRows(const DevLattice& L) { return sizeof(S) == 2 && L.nz % 8 == 0 && L.rowForm == 0; }
+    static bool pairedRows(const DevLattice& L) { return sizeof(S) == 2 && L.nz % 2 == 0 && L.rowForm != 1; }
+    // Eight (or four) cells per thread, 128-bit (64-bit) population vectors
+    // (vecrow.cuh): rows of a multiple of eight cells.
+    static bool vectorRows(const DevLattice& L) {
+        return sizeof(S) == 2 && L.nz % 8 == 0 && (L.rowForm == 0 || L.rowForm == 2);
+    }
 
     template <bool ODD, bool STATS, bool EXT>
     static int stepSplit(const DevLattice& L, const StepParams<R>& p, StatsAcc* acc, cudaStream_t s,
                          const SideStream* side) {
         int launched = 0;
-        // A sparse domain runs every row through the general addressing,
-        // which checks each neighbour's kind.
-        const bool general = L.sparse || L.nx < 3 || L.ny < 3;
-        const int edgeRows = general ? L.nx * L.ny : 2 * L.ny + 2 * (L.nx - 2);
+        // A sparse domain with row lists runs its dense rows (no cell outside
+        // the lattice in the 3x3 rows around them) through the interior-row
+        // kernels and the other live rows through the general addressing,
+        // which checks each neighbour's kind; without lists every row goes the
+        // general way.
+        const bool lists = L.sparse && (L.denseRows || L.generalRows);
+        const bool general = (L.sparse && !lists) || L.nx < 3 || L.ny < 3;
+        const int edgeRows = lists ? L.nGeneral : general ? L.nx * L.ny : 2 * L.ny + 2 * (L.nx - 2);
+        const long long interiorRows = lists ? L.nDense : (long long)(L.nx - 2) * (L.ny - 2);
+        // grid (blocksPerRow, y, z) over the interior rows: the row is
+        // (blockIdx.z + 1, blockIdx.y + 1), or entry blockIdx.y + gridDim.y *
+        // blockIdx.z of the dense-row list
+        auto interiorGrid = [&](int blocksPerRow) {
+            if (!lists) return dim3((unsigned)blocksPerRow, (unsigned)(L.ny - 2), (unsigned)(L.nx - 2));
+            const unsigned gy = (unsigned)(L.nDense < 65535 ? L.nDense : 65535);
+            return dim3((unsigned)blocksPerRow, gy, (unsigned)((L.nDense + gy - 1) / gy));
+        };
         // The border rows run on the side stream (the context's highest
         // priority), beside the interior kernel.  Submission order decides
         // whose blocks take the SMs first: the 2-byte forms submit the
@@ -41,7 +56,8 @@ struct StepLaunch {
             cudaStreamWaitEvent(side->stream, side->fork, 0) == cudaSuccess)
             es = side->stream;
         auto interior = [&]() {
-            if (!general && vectorRows(L)) {
+            if (general || interiorRows == 0) return;
+            if (vectorRows(L)) {
                 if constexpr (sizeof(S) == 2) {
                     Planes<S> pl;
                     RowDeltas d;
@@ -49,12 +65,18 @@ struct StepLaunch {
                         pl.p[i] = static_cast<S*>(L.pop) + (long long)i * L.stride;
                         d.d[i] = cdir(i, 0) * L.ny * L.nz + cdir(i, 1) * L.nz;
                     }
-                    const long long segs = (long long)(L.nx - 2) * (L.ny - 2) * (L.nz / 8);
-                    const unsigned blocks = (unsigned)((segs + kBlock - 1) / kBlock);
-                    vecRowStepKernel<S, ODD, STATS, EXT><<<blocks, kBlock, 0, s>>>(L, pl, d, p, acc, segs);
+                    if (L.rowForm == 2) {   // four cells per thread, 8-byte vectors
+                        const long long segs = interiorRows * (L.nz / 4);
+                        const unsigned blocks = (unsigned)((segs + kBlock - 1) / kBlock);
+                        vecRowStepKernel<S, ODD, STATS, EXT, 4><<<blocks, kBlock, 0, s>>>(L, pl, d, p, acc, segs);
+                    } else {
+                        const long long segs = interiorRows * (L.nz / 8);
+                        const unsigned blocks = (unsigned)((segs + kBlock - 1) / kBlock);
+                        vecRowStepKernel<S, ODD, STATS, EXT, 8><<<blocks, kBlock, 0, s>>>(L, pl, d, p, acc, segs);
+                    }
                     ++launched;
                 }
-            } else if (!general && pairedRows(L)) {
+            } else if (pairedRows(L)) {
                 Planes<S> pl;
                 Deltas d;
                 for (int i = 0; i < 19; ++i) {
@@ -65,11 +87,11 @@ struct StepLaunch {
                     const int pairs = L.nz / 2;
                     int tpb = (pairs + 31) / 32 * 32;
                     tpb = tpb < kBlock ? tpb : kBlock;
-                    pairRowStepKernel<S, ODD, STATS, EXT><<<rowGrid(pairs, L.ny - 2, L.nx - 2, tpb), tpb, 0, s>>>(L, pl, d, p,
-                                                                                                          acc);
+                    pairRowStepKernel<S, ODD, STATS, EXT><<<interiorGrid((pairs + tpb - 1) / tpb), tpb, 0, s>>>(L, pl, d, p,
+                                                                                                         acc);
                     ++launched;
                 }
-            } else if (!general) {
+            } else {
                 Planes<S> pl;
                 Deltas d;
                 for (int i = 0; i < 19; ++i) {
@@ -81,11 +103,13 @@ struct StepLaunch {
                 constexpr int NC = RowShape<S>::cells;
                 int tpb = ((L.nz + NC - 1) / NC + 31) / 32 * 32;
                 tpb = tpb < kBlock ? tpb : kBlock;
-                rowStepKernel<S, ODD, STATS, EXT><<<rowGrid(L.nz, L.ny - 2, L.nx - 2, tpb * NC), tpb, 0, s>>>(L, pl, d, p, acc);
+                rowStepKernel<S, ODD, STATS, EXT><<<interiorGrid((L.nz + tpb * NC - 1) / (tpb * NC)), tpb, 0, s>>>(L, pl, d, p,
+                                                                                                        acc);
                 ++launched;
             }
         };
         auto border = [&]() {
+            if (edgeRows == 0) return;
             const int gy = edgeRows < 65535 ? edgeRows : 65535;
             dim3 g((unsigned)((L.nz + kBlock - 1) / kBlock), (unsigned)gy, (unsigned)((edgeRows + gy - 1) / gy));
             if (L.sparse)

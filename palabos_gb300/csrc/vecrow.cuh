@@ -68,14 +68,32 @@ template <> struct Half16<bf16sr> {
     }
 };
 
-__device__ __forceinline__ uint4 ldVec(const void* p) {
-    uint4 v;
-    asm volatile("ld.global.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p));
+// NW 32-bit words of 16-bit values (NW = 2: eight bytes, NW = 4: sixteen),
+// element e in word e / 2, low half first.
+template <int NW>
+struct Words {
+    unsigned w[NW];
+};
+
+template <int NW>
+__device__ __forceinline__ Words<NW> ldWords(const void* p) {
+    Words<NW> v;
+    if constexpr (NW == 4)
+        asm volatile("ld.global.v4.u32 {%0, %1, %2, %3}, [%4];"
+                     : "=r"(v.w[0]), "=r"(v.w[1]), "=r"(v.w[2]), "=r"(v.w[3])
+                     : "l"(p));
+    else
+        asm volatile("ld.global.v2.u32 {%0, %1}, [%2];" : "=r"(v.w[0]), "=r"(v.w[1]) : "l"(p));
     return v;
 }
-__device__ __forceinline__ void stVec(void* p, uint4 v) {
-    asm volatile("st.global.v4.u32 [%0], {%1, %2, %3, %4};" ::"l"(p), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w)
-                 : "memory");
+template <int NW>
+__device__ __forceinline__ void stWords(void* p, const Words<NW>& v) {
+    if constexpr (NW == 4)
+        asm volatile("st.global.v4.u32 [%0], {%1, %2, %3, %4};" ::"l"(p), "r"(v.w[0]), "r"(v.w[1]), "r"(v.w[2]),
+                     "r"(v.w[3])
+                     : "memory");
+    else
+        asm volatile("st.global.v2.u32 [%0], {%1, %2};" ::"l"(p), "r"(v.w[0]), "r"(v.w[1]) : "memory");
 }
 __device__ __forceinline__ unsigned ld16(const void* p) {
     unsigned short u;
@@ -92,100 +110,120 @@ __device__ __forceinline__ void st64(void* p, unsigned a, unsigned b) {
     asm volatile("st.global.v2.u32 [%0], {%1, %2};" ::"l"(p), "r"(a), "r"(b) : "memory");
 }
 
-// Elements e0..e7 of a vector; word k holds e(2k) in its low half.
-// (p, e0, ..., e6): p in the high half of `prev`.
-__device__ __forceinline__ uint4 shiftUp(uint4 v, unsigned prev) {
-    return make_uint4(__byte_perm(prev, v.x, 0x5432), __byte_perm(v.x, v.y, 0x5432), __byte_perm(v.y, v.z, 0x5432),
-                      __byte_perm(v.z, v.w, 0x5432));
+// (p, e0, ..., e_{n-2}): p in the high half of `prev`.
+template <int NW>
+__device__ __forceinline__ Words<NW> shiftUp(const Words<NW>& v, unsigned prev) {
+    Words<NW> r;
+    r.w[0] = __byte_perm(prev, v.w[0], 0x5432);
+#pragma unroll
+    for (int k = 1; k < NW; ++k) r.w[k] = __byte_perm(v.w[k - 1], v.w[k], 0x5432);
+    return r;
 }
-// (e1, ..., e7, n): n in the low half of `next`.
-__device__ __forceinline__ uint4 shiftDown(uint4 v, unsigned next) {
-    return make_uint4(__byte_perm(v.x, v.y, 0x5432), __byte_perm(v.y, v.z, 0x5432), __byte_perm(v.z, v.w, 0x5432),
-                      __byte_perm(v.w, next, 0x5432));
+// (e1, ..., e_{n-1}, n): n in the low half of `next`.
+template <int NW>
+__device__ __forceinline__ Words<NW> shiftDown(const Words<NW>& v, unsigned next) {
+    Words<NW> r;
+#pragma unroll
+    for (int k = 0; k + 1 < NW; ++k) r.w[k] = __byte_perm(v.w[k], v.w[k + 1], 0x5432);
+    r.w[NW - 1] = __byte_perm(v.w[NW - 1], next, 0x5432);
+    return r;
 }
-
-__device__ __forceinline__ unsigned& word(uint4& v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); }
 
 // Uniform row offsets c_x * ny * nz + c_y * nz of the 19 populations.
 struct RowDeltas {
     int d[19];
 };
 
-template <typename S>
-struct VecShape { static constexpr int blocks = 3; };
+// Cells per thread and residency of the vector kernel: CPT = 8 moves 16-byte
+// vectors (19 of them held as 76 registers of packed values), CPT = 4 moves
+// 8-byte vectors with half the registers and more resident warps.
+template <int CPT>
+struct VecShape {
+    static constexpr int blocks = CPT == 8 ? 3 : 5;
+};
 
-template <typename S, bool ODD, bool STATS, bool EXT>
-__global__ void __launch_bounds__(128, VecShape<S>::blocks)
+template <typename S, bool ODD, bool STATS, bool EXT, int CPT>
+__global__ void __launch_bounds__(128, VecShape<CPT>::blocks)
     vecRowStepKernel(DevLattice L, Planes<S> Pl, RowDeltas D, StepParams<typename StoreT<S>::R> P, StatsAcc* acc,
                      long long segments) {
     using R = typename StoreT<S>::R;
-    const int R8 = L.nz >> 3;                       // segments per row
+    constexpr int NW = CPT / 2;
+    const int RS = L.nz / CPT;                      // segments per row
     const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = g < segments;
     // Threads past the last segment mirror it (the warp's shuffles need every
     // lane); they store nothing and gather no statistics.
     const long long gg = live ? g : segments - 1;
-    const int row = (int)(gg / R8), seg = (int)(gg - (long long)row * R8);
-    const int x = 1 + row / (L.ny - 2), y = 1 + row % (L.ny - 2);
+    const int row = (int)(gg / RS), seg = (int)(gg - (long long)row * RS);
+    const int x = L.denseRows ? L.denseRows[row].x : 1 + row / (L.ny - 2);
+    const int y = L.denseRows ? L.denseRows[row].y : 1 + row % (L.ny - 2);
     const int lane = threadIdx.x & 31;
-    const bool first = seg == 0, last = seg == R8 - 1;
-    const bool upOk = !first && lane > 0;           // lane - 1 holds cells z0-8..z0-1 of this row
-    const bool downOk = !last && lane < 31;         // lane + 1 holds cells z0+8..z0+15 of this row
+    const bool first = seg == 0, last = seg == RS - 1;
+    const bool upOk = !first && lane > 0;           // lane - 1 holds the CPT cells below z0 in this row
+    const bool downOk = !last && lane < 31;         // lane + 1 holds the CPT cells from z0 + CPT on
     const bool perZ = L.per[2] != 0;
-    const int rowIdx = (x * L.ny + y) * L.nz;
-    const int z0 = seg << 3;
-    const int idx0 = rowIdx + z0;
     const int nz = L.nz;
+    const int rowIdx = (x * L.ny + y) * nz;
+    const int z0 = seg * CPT;
+    const int idx0 = rowIdx + z0;
 
-    uint4 v[19];
+    Words<NW> v[19];
     // ---- load
 #pragma unroll
     for (int i = 0; i < 19; ++i) {
         if (!ODD) {
-            v[i] = ldVec(Pl.p[i] + idx0);
+            v[i] = ldWords<NW>(Pl.p[i] + idx0);
         } else {
             const S* src = Pl.p[opp(i)];
             const int srow = rowIdx - D.d[i];       // source row x - c_i (x and y part)
             const int cz = cdir(i, 2);
-            const uint4 a = ldVec(src + (srow + z0));
+            const Words<NW> a = ldWords<NW>(src + (srow + z0));
             if (cz == 0) {
                 v[i] = a;
-            } else if (cz > 0) {                    // window z0-1 .. z0+6
-                unsigned prev = __shfl_up_sync(0xffffffffu, a.w, 1);
+            } else if (cz > 0) {                    // window z0-1 .. z0+CPT-2
+                unsigned prev = __shfl_up_sync(0xffffffffu, a.w[NW - 1], 1);
                 if (!upOk) {
                     const S* p = !first ? src + (srow + z0 - 1) : (perZ ? src + (srow + nz - 1) : Pl.p[i] + rowIdx);
                     prev = ld16(p) << 16;
                 }
-                v[i] = shiftUp(a, prev);
-            } else {                                // window z0+1 .. z0+8
-                unsigned next = __shfl_down_sync(0xffffffffu, a.x, 1);
+                v[i] = shiftUp<NW>(a, prev);
+            } else {                                // window z0+1 .. z0+CPT
+                unsigned next = __shfl_down_sync(0xffffffffu, a.w[0], 1);
                 if (!downOk) {
-                    const S* p = !last ? src + (srow + z0 + 8) : (perZ ? src + srow : Pl.p[i] + (rowIdx + nz - 1));
+                    const S* p = !last ? src + (srow + z0 + CPT) : (perZ ? src + srow : Pl.p[i] + (rowIdx + nz - 1));
                     next = ld16(p);
                 }
-                v[i] = shiftDown(a, next);
+                v[i] = shiftDown<NW>(a, next);
             }
         }
     }
-    const uint2 kk = *reinterpret_cast<const uint2*>(L.flags + idx0);
+    unsigned kk[2];   // the cells' kinds, four per word
+    if constexpr (NW == 4) {
+        const uint2 t = *reinterpret_cast<const uint2*>(L.flags + idx0);
+        kk[0] = t.x;
+        kk[1] = t.y;
+    } else {
+        kk[0] = *reinterpret_cast<const unsigned*>(L.flags + idx0);
+        kk[1] = 0u;
+    }
 
     // ---- collide, one cell at a time; results go back into the same halves
     double sR = 0., sU = 0.;
     unsigned long long cnt = 0, mx = 0;
 #pragma unroll
-    for (int c = 0; c < 8; ++c) {
+    for (int c = 0; c < CPT; ++c) {
         const int w = c >> 1;
         const bool hi = c & 1;
-        const int k = (int)(((c < 4 ? kk.x : kk.y) >> (8 * (c & 3))) & 0xffu);
+        const int k = (int)((kk[c >> 2] >> (8 * (c & 3))) & 0xffu);
         R f[19];
 #pragma unroll
-        for (int i = 0; i < 19; ++i) f[i] = Half16<S>::get(word(v[i], w), hi);
+        for (int i = 0; i < 19; ++i) f[i] = Half16<S>::get(v[i].w[w], hi);
         const int idx = idx0 + c;
         R rhoBar = R(0), uSqr = R(0);
         if (P.pending && isFace(k)) completeIfFace<R>(L, idx, k, f);
         const bool gathers = collideCell<S, EXT>(L, P, idx, k, f, rhoBar, uSqr, acc, STATS && live);
 #pragma unroll
-        for (int i = 0; i < 19; ++i) word(v[i], w) = Half16<S>::put(word(v[i], w), hi, f[i], Pl.p[i] + idx, P.seed);
+        for (int i = 0; i < 19; ++i) v[i].w[w] = Half16<S>::put(v[i].w[w], hi, f[i], Pl.p[i] + idx, P.seed);
         if (STATS && live && gathers) {
             sR += (double)rhoBar;
             sU += (double)uSqr;
@@ -199,43 +237,49 @@ __global__ void __launch_bounds__(128, VecShape<S>::blocks)
 #pragma unroll
     for (int i = 0; i < 19; ++i) {
         if (!ODD) {
-            if (live) stVec(Pl.p[opp(i)] + idx0, v[i]);
+            if (live) stWords<NW>(Pl.p[opp(i)] + idx0, v[i]);
         } else {
             S* dst = Pl.p[i];
             const int drow = rowIdx + D.d[i];       // destination row x + c_i (x and y part)
             const int d0 = drow + z0;
             const int cz = cdir(i, 2);
-            const uint4 a = v[i];
+            const Words<NW>& a = v[i];
             if (cz == 0) {
-                if (live) stVec(dst + d0, a);
-            } else if (cz > 0) {                    // cells z0..z0+7 -> positions z0+1..z0+8
-                const unsigned prev = __shfl_up_sync(0xffffffffu, a.w, 1);
+                if (live) stWords<NW>(dst + d0, a);
+            } else if (cz > 0) {                    // cells z0.. -> positions z0+1 .. z0+CPT
+                const unsigned prev = __shfl_up_sync(0xffffffffu, a.w[NW - 1], 1);
                 if (live) {
                     if (upOk) {
-                        stVec(dst + d0, shiftUp(a, prev));
+                        stWords<NW>(dst + d0, shiftUp<NW>(a, prev));
                     } else {                        // position z0 is written by its owner
-                        st16(dst + (d0 + 1), a.x);
-                        st32(dst + (d0 + 2), __byte_perm(a.x, a.y, 0x5432));
-                        st64(dst + (d0 + 4), __byte_perm(a.y, a.z, 0x5432), __byte_perm(a.z, a.w, 0x5432));
+                        st16(dst + (d0 + 1), a.w[0]);
+                        st32(dst + (d0 + 2), __byte_perm(a.w[0], a.w[1], 0x5432));
+                        if constexpr (NW == 4)
+                            st64(dst + (d0 + 4), __byte_perm(a.w[1], a.w[2], 0x5432),
+                                 __byte_perm(a.w[2], a.w[3], 0x5432));
                     }
-                    if (!downOk) {                  // e7: no lane of this warp takes it
-                        S* p = !last ? dst + (d0 + 8) : (perZ ? dst + drow : Pl.p[opp(i)] + (rowIdx + nz - 1));
-                        st16(p, a.w >> 16);
+                    if (!downOk) {                  // the last cell's value: no lane of this warp takes it
+                        S* p = !last ? dst + (d0 + CPT) : (perZ ? dst + drow : Pl.p[opp(i)] + (rowIdx + nz - 1));
+                        st16(p, a.w[NW - 1] >> 16);
                     }
                 }
-            } else {                                // cells z0..z0+7 -> positions z0-1..z0+6
-                const unsigned next = __shfl_down_sync(0xffffffffu, a.x, 1);
+            } else {                                // cells z0.. -> positions z0-1 .. z0+CPT-2
+                const unsigned next = __shfl_down_sync(0xffffffffu, a.w[0], 1);
                 if (live) {
                     if (downOk) {
-                        stVec(dst + d0, shiftDown(a, next));
-                    } else {                        // position z0+7 is written by its owner
-                        st64(dst + d0, __byte_perm(a.x, a.y, 0x5432), __byte_perm(a.y, a.z, 0x5432));
-                        st32(dst + (d0 + 4), __byte_perm(a.z, a.w, 0x5432));
-                        st16(dst + (d0 + 6), a.w >> 16);
+                        stWords<NW>(dst + d0, shiftDown<NW>(a, next));
+                    } else {                        // position z0+CPT-1 is written by its owner
+                        if constexpr (NW == 4) {
+                            st64(dst + d0, __byte_perm(a.w[0], a.w[1], 0x5432), __byte_perm(a.w[1], a.w[2], 0x5432));
+                            st32(dst + (d0 + 4), __byte_perm(a.w[2], a.w[3], 0x5432));
+                        } else {
+                            st32(dst + d0, __byte_perm(a.w[0], a.w[1], 0x5432));
+                        }
+                        st16(dst + (d0 + CPT - 2), a.w[NW - 1] >> 16);
                     }
-                    if (!upOk) {                    // e0: no lane of this warp takes it
+                    if (!upOk) {                    // the first cell's value: no lane of this warp takes it
                         S* p = !first ? dst + (d0 - 1) : (perZ ? dst + (drow + nz - 1) : Pl.p[opp(i)] + rowIdx);
-                        st16(p, a.x);
+                        st16(p, a.w[0]);
                     }
                 }
             }

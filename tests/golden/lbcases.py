@@ -482,6 +482,41 @@ def case_sparse_sealed_channel():
     return spec
 
 
+def case_sparse_unsealed_channel():
+    """A sparse lattice whose fluid touches the dropped blocks directly: the
+    same 4 x 3 x 3 distribution of 24 x 18 x 18 and block selection as
+    sparse_sealed_channel, but no bounce-back seal -- every kept cell is BGK
+    fluid (with a momentum-exchange obstacle).  The reference keeps, per kept
+    block, an envelope layer facing the dropped blocks whose cells collide and
+    stream within that block; the GPU treats a neighbour in a dropped block
+    like the domain edge.  Compared bit for bit: the kept cells more than one
+    cell per step (chessboard distance) away from every dropped cell."""
+    shape = (24, 18, 18)
+    rng = np.random.default_rng(114)
+    flags, bcval, force, _ = empty(shape)
+    x0, x1, y0, y1, z0, z1 = 1, 14, 1, 10, 1, 10
+    seal = np.zeros(shape, bool)
+    seal[x0:x1 + 1, y0:y1 + 1, z0:z1 + 1] = True
+    flags[5:7, 4:6, 5:8] = MEBB
+    field = seal.astype(np.int32)
+    f0 = initial_state(shape, rng, u_amp=0.03, rho_amp=0.003)
+    spec = _spec("sparse_unsealed_channel", shape, (0, 0, 0), 1.7, 6, flags, bcval, force, f0,
+                 blocks=(4, 3, 3), options=OPT_SPARSE)
+    spec.sparse = field
+    from scipy.ndimage import distance_transform_cdt
+    kept = np.zeros(shape, bool)
+    edges = [np.linspace(0, n, b + 1).round().astype(int) for n, b in zip(shape, spec.blocks)]
+    for ix in range(spec.blocks[0]):
+        for iy in range(spec.blocks[1]):
+            for iz in range(spec.blocks[2]):
+                sl = (slice(edges[0][ix], edges[0][ix + 1]), slice(edges[1][iy], edges[1][iy + 1]),
+                      slice(edges[2][iz], edges[2][iz + 1]))
+                if field[sl].any():
+                    kept[sl] = True
+    spec.compare = kept & (distance_transform_cdt(kept, metric="chessboard") > spec.nsteps)
+    return spec
+
+
 def case_state_periodic_multiblock():
     """parallelIO::save of a 2 x 2 x 2-block lattice: eight components."""
     s = case_periodic_bgk_multiblock()
@@ -565,7 +600,7 @@ CASES = [
     case_velocity_box_multiblock, case_velocity_box_noinit, case_doctest_cavity20,
     case_external_periodic_bgk, case_external_incbgk_nodyn, case_external_guo_periodic,
     case_external_mebb_periodic, case_binary_channel_sphere, case_binary_guo_periodic,
-    case_sparse_sealed_channel, case_state_periodic_multiblock, case_state_guo_multiblock,
+    case_sparse_sealed_channel, case_sparse_unsealed_channel, case_state_periodic_multiblock, case_state_guo_multiblock,
     case_dstate_channel_sphere_multiblock, case_dstate_velocity_box, case_dstate_zhpress_faces,
     case_dstate_guo_channel, case_dstate_incbgk_nodyn, case_sparse_dstate_sealed_channel,
 ]

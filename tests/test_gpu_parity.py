@@ -351,3 +351,36 @@ def test_sparse_lattice_matches_reference_and_oracle():
     e, rho = lat.reduce()
     oe, orho = ol.reduce(ref)
     assert e == pytest.approx(oe, rel=1e-12) and rho == pytest.approx(orho, rel=1e-12)
+
+
+def test_sparse_lattice_without_seal_counts_the_band_next_to_dropped_blocks():
+    """Fluid touching dropped blocks directly (no bounce-back seal).  The
+    reference gives each kept block an envelope layer facing the dropped
+    blocks whose cells collide and stream within that block; the GPU treats
+    a neighbour in a dropped block like the domain edge.  After n steps the two
+    differ exactly in the kept cells within n cells (chessboard distance) of a
+    dropped block -- every one of them differs, none beyond -- and the GPU
+    equals the oracle (the same domain-edge rule) on every cell."""
+    from scipy.ndimage import distance_transform_cdt
+    g, meta = goldens.load("sparse_unsealed_channel")
+    lat = lattice_from_description(meta["nx"], meta["ny"], meta["nz"], meta["periodic"], meta["omega"],
+                                   g["flags"], g["bcval"], g["force"], sparse=(g["sparse"], meta["blocks"]))
+    kinds = lat.get_kinds()
+    inl = g["in_lattice"].astype(bool)
+    assert np.array_equal(kinds != 255, inl)
+    lat.send(g["f_init"])
+    lat.collide_and_stream(meta["nsteps"], stats=True)
+    f = lat.receive()
+    dist = distance_transform_cdt(inl, metric="chessboard")
+    far = inl & (dist > meta["nsteps"])
+    band = inl & (dist <= meta["nsteps"])
+    assert far.sum() > 0
+    assert np.array_equal(f[far], g["f_final"][far])
+    differ = np.any(f != g["f_final"], axis=-1) & inl
+    assert not (differ & far).any()
+    assert differ.sum() == band.sum() == 2160      # 2592 kept cells, 432 beyond the band
+    ol = O.OracleLattice(meta["nx"], meta["ny"], meta["nz"], meta["periodic"], meta["omega"], kinds, g["bcval"],
+                         g["force"])
+    ref, _ = ol.run(g["f_init"], meta["nsteps"])
+    assert np.array_equal(f, ref.reshape(f.shape))
+

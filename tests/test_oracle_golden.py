@@ -18,7 +18,7 @@ import oracle as O
 def test_oracle_matches_reference(name):
     g, meta = goldens.load(name)
     if meta.get("options", 0) & lbcases.OPT_SPARSE:
-        return _check_sparse(g, meta)
+        return _check_sparse(g, meta, with_drag=name != "sparse_unsealed_channel")
     lat = O.OracleLattice.from_golden(g, meta)
     if meta.get("options", 0) & lbcases.OPT_EXTERNAL_RHOJ:
         f, rb, j, stats = lat.run_external(g["f_init"], g["rho_bar0"], g["j0"], meta["nsteps"])
@@ -46,17 +46,21 @@ def sparse_flags(g, meta):
     return flags, mask
 
 
-def _check_sparse(g, meta):
+def _check_sparse(g, meta, with_drag=True):
+    """Populations of the compared cells bit for bit (the fluid a bounce-back
+    seal keeps away from the dropped blocks, or the cells further from them
+    than one cell per step); the drag where the obstacle is among them."""
     flags, mask = sparse_flags(g, meta)
     assert np.array_equal(mask, g["in_lattice"].astype(bool))   # the reference's block selection
     lat = O.OracleLattice(meta["nx"], meta["ny"], meta["nz"], meta["periodic"], meta["omega"], flags,
                           g["bcval"], g["force"], meta.get("rho0", 1.0), meta.get("bb_rho", 0.0))
     f, stats = lat.run(g["f_init"], meta["nsteps"])
     cmp = g["compare"].astype(bool)
-    assert np.array_equal(f[cmp], g["f_final"][cmp])
-    gs = g["stats"]
-    ok, worst = goldens.stats_close(stats[gs[:, 0].astype(int) - 1, 3:6], gs[:, 4:7])   # drag
-    assert ok, worst
+    assert cmp.any() and np.array_equal(f[cmp], g["f_final"][cmp])
+    if with_drag:
+        gs = g["stats"]
+        ok, worst = goldens.stats_close(stats[gs[:, 0].astype(int) - 1, 3:6], gs[:, 4:7])   # drag
+        assert ok, worst
 
 
 @pytest.mark.parametrize("name", goldens.case_names())
