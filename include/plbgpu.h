@@ -79,10 +79,11 @@ typedef struct plbgpu_ctx plbgpu_ctx;
 /* Create a context on CUDA device `device`.  Replaces the singleton
  * global::defaultCoProcessor3D<T>() (coProcessors/coProcessor3D.h:178-186).
  * Environment variables read here: PLBGPU_STAGED_TRANSFERS=1 (see
- * plbgpu_send) and PLBGPU_ROW_KERNEL=cell, which makes the interior rows of
- * every storage type run the one-cell-per-thread kernel instead of the
- * paired or 128-bit vector kernels of the 2-byte forms (same results; a
- * cross-check of the faster kernels). */
+ * plbgpu_send) and PLBGPU_ROW_KERNEL, the interior-row kernel: "cell" runs
+ * one cell per thread for every storage type instead of the paired kernel of
+ * the 2-byte forms; "vec8" / "vec4" run eight / four cells per thread with
+ * 128- / 64-bit population vectors (2-byte forms, rows of a multiple of eight
+ * cells).  All give the same results; the default is the fastest on GB300. */
 int plbgpu_create(int device, plbgpu_ctx** out);
 int plbgpu_destroy(plbgpu_ctx* ctx);
 /* Message of the last failing call on this context ("" if none). */

@@ -69,8 +69,8 @@ struct Domain {
     void* ext = nullptr;         // 4 * n of FP64 or FP32: external rho-bar, jx, jy, jz
     uint32_t* mebb = nullptr;    // n
     int4* surf = nullptr;        // edge cells, then corner cells: (x, y, z, kind)
-    int2* rowLists = nullptr;    // sparse domains: dense rows, then general rows (x, y)
-    int nDense = 0, nGeneral = 0, rowListCap = 0;
+    int4* tileLists = nullptr;   // sparse domains: dense tiles, then general tiles (x, y, z0, z1)
+    int nDense = 0, nGeneral = 0, tileListCap = 0;
     int surfCap = 0, nEdges = 0, nCorners = 0;
     bool hasSurface = false;     // any edge or corner kind
     bool sparse = false;         // any cell outside the lattice (K_NONE)
@@ -102,10 +102,10 @@ struct Domain {
         L.n = n;
         L.status = status;
         L.rowForm = 0;
-        const bool lists = sparse && rowLists;
-        L.denseRows = lists && nDense ? rowLists : nullptr;
+        const bool lists = sparse && tileLists;
+        L.denseTiles = lists && nDense ? tileLists : nullptr;
         L.nDense = lists ? nDense : 0;
-        L.generalRows = lists && nGeneral ? rowLists + nDense : nullptr;
+        L.generalTiles = lists && nGeneral ? tileLists + nDense : nullptr;
         L.nGeneral = lists ? nGeneral : 0;
         return L;
     }
@@ -310,18 +310,28 @@ __global__ void mebbMaskKernel(DevLattice L, uint32_t* out) {
     out[idx] = m;
 }
 
-// Per row (x, y): bit 0 some cell is part of the lattice, bit 1 every cell is.
-__global__ void rowLiveKernel(const uint8_t* flags, int rows, int nz, uint8_t* live) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= rows) return;
-    bool any = false, all = true;
+// Per tile (row r, cells z0 .. z1-1 with z0 = t * kTileCells): bit 0 some
+// cell of the tile is part of the lattice, bit 1 every cell from z0 - 1 to z1
+// is (wrapping around a periodic z axis; beyond a non-periodic one nothing
+// needs to be).
+__global__ void tileLiveKernel(const uint8_t* flags, int rows, int nz, int tiles, int perZ, uint8_t* live) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= (long long)rows * tiles) return;
+    const int r = (int)(i / tiles), t = (int)(i - (long long)r * tiles);
+    const int z0 = t * kTileCells, z1 = min(z0 + kTileCells, nz);
     const uint8_t* f = flags + (long long)r * nz;
-    for (int z = 0; z < nz; ++z) {
-        const bool in = f[z] != K_NONE;
-        any |= in;
+    bool any = false, all = true;
+    for (int z = z0 - 1; z <= z1; ++z) {
+        int zz = z;
+        if (zz < 0 || zz >= nz) {
+            if (!perZ) continue;
+            zz = zz < 0 ? zz + nz : zz - nz;
+        }
+        const bool in = f[zz] != K_NONE;
         all &= in;
+        if (z >= z0 && z < z1) any |= in;
     }
-    live[r] = (uint8_t)((any ? 1 : 0) | (all ? 2 : 0));
+    live[i] = (uint8_t)((any ? 1 : 0) | (all ? 2 : 0));
 }
 
 __global__ void kindMaskKernel(const uint8_t* flags, long long n, unsigned long long* mask) {
@@ -448,47 +458,53 @@ int kindMask(plbgpu_ctx* c, Domain* d, unsigned long long* mask) {
     return PLBGPU_OK;
 }
 
-// The row lists of a sparse domain: rows whose 3x3 neighbourhood of rows is
-// entirely part of the lattice ("dense": the interior-row kernels step them,
-// their neighbours never fall outside), then the other rows with a live cell
-// (the general kernel, which treats a neighbour outside the lattice like the
-// domain edge).  Rows without live cells are left out.
-int buildRowLists(plbgpu_ctx* c, Domain* d) {
+// The tile lists of a sparse domain: tiles of up to kTileCells cells of a row
+// whose 3x3 neighbourhood of rows is part of the lattice from one cell before
+// the tile to one cell after it ("dense": the interior-row kernels step them,
+// no neighbour falls outside), then the other tiles with a live cell (the
+// general kernel, which treats a neighbour outside the lattice like the domain
+// edge).  Tiles without live cells are left out.  Rebuilt when the kinds or
+// the periodicity change.
+int buildTileLists(plbgpu_ctx* c, Domain* d) {
     const int rows = d->nx * d->ny;
-    int rc = ensureStaging(c, (size_t)rows);
+    const int tiles = (d->nz + kTileCells - 1) / kTileCells;
+    const size_t nt = (size_t)rows * tiles;
+    int rc = ensureStaging(c, nt);
     if (rc) return rc;
     uint8_t* dl = static_cast<uint8_t*>(c->staging);
-    rowLiveKernel<<<(rows + 255) / 256, 256, 0, c->stream>>>(d->flags, rows, d->nz, dl);
+    tileLiveKernel<<<(unsigned)((nt + 255) / 256), 256, 0, c->stream>>>(d->flags, rows, d->nz, tiles, d->per[2], dl);
     if ((rc = launchBox(c))) return rc;
-    std::vector<uint8_t> live((size_t)rows);
-    CUDA_TRY(c, cudaMemcpyAsync(live.data(), dl, (size_t)rows, cudaMemcpyDeviceToHost, c->stream));
+    std::vector<uint8_t> live(nt);
+    CUDA_TRY(c, cudaMemcpyAsync(live.data(), dl, nt, cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-    std::vector<int2> dense, general;
+    auto at = [&](int x, int y, int t) { return live[((size_t)x * d->ny + y) * tiles + t]; };
+    std::vector<int4> dense, general;
     for (int x = 0; x < d->nx; ++x)
-        for (int y = 0; y < d->ny; ++y) {
-            const uint8_t l = live[(size_t)x * d->ny + y];
-            if (!(l & 1)) continue;
-            bool full = x >= 1 && x <= d->nx - 2 && y >= 1 && y <= d->ny - 2;
-            for (int dx = -1; dx <= 1 && full; ++dx)
-                for (int dy = -1; dy <= 1 && full; ++dy) full = (live[(size_t)(x + dx) * d->ny + (y + dy)] & 2) != 0;
-            (full ? dense : general).push_back(make_int2(x, y));
-        }
+        for (int y = 0; y < d->ny; ++y)
+            for (int t = 0; t < tiles; ++t) {
+                if (!(at(x, y, t) & 1)) continue;
+                bool full = x >= 1 && x <= d->nx - 2 && y >= 1 && y <= d->ny - 2;
+                for (int dx = -1; dx <= 1 && full; ++dx)
+                    for (int dy = -1; dy <= 1 && full; ++dy) full = (at(x + dx, y + dy, t) & 2) != 0;
+                const int z0 = t * kTileCells, z1 = std::min(z0 + kTileCells, d->nz);
+                (full ? dense : general).push_back(make_int4(x, y, z0, z1));
+            }
     const int total = (int)(dense.size() + general.size());
-    if (total > d->rowListCap) {
-        if (d->rowLists) {
+    if (total > d->tileListCap) {
+        if (d->tileLists) {
             CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-            cudaFree(d->rowLists);
-            d->deviceBytes -= sizeof(int2) * (size_t)d->rowListCap;
-            d->rowLists = nullptr;
-            d->rowListCap = 0;
+            cudaFree(d->tileLists);
+            d->deviceBytes -= sizeof(int4) * (size_t)d->tileListCap;
+            d->tileLists = nullptr;
+            d->tileListCap = 0;
         }
-        CUDA_TRY(c, cudaMalloc(&d->rowLists, sizeof(int2) * (size_t)(total > 0 ? total : 1)));
-        d->rowListCap = total > 0 ? total : 1;
-        d->deviceBytes += sizeof(int2) * (size_t)d->rowListCap;
+        CUDA_TRY(c, cudaMalloc(&d->tileLists, sizeof(int4) * (size_t)(total > 0 ? total : 1)));
+        d->tileListCap = total > 0 ? total : 1;
+        d->deviceBytes += sizeof(int4) * (size_t)d->tileListCap;
     }
     dense.insert(dense.end(), general.begin(), general.end());
     if (total)
-        CUDA_TRY(c, cudaMemcpyAsync(d->rowLists, dense.data(), sizeof(int2) * (size_t)total, cudaMemcpyHostToDevice,
+        CUDA_TRY(c, cudaMemcpyAsync(d->tileLists, dense.data(), sizeof(int4) * (size_t)total, cudaMemcpyHostToDevice,
                                     c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     d->nDense = total - (int)general.size();
@@ -506,7 +522,7 @@ int syncKinds(plbgpu_ctx* c, Domain* d) {
     d->hasSurface = surface;
     d->surfDirty = true;
     d->sparse = (m >> 63) & 1;   // kinds >= 63: only K_NONE
-    if (d->sparse && (rc = buildRowLists(c, d))) return rc;
+    if (d->sparse && (rc = buildTileLists(c, d))) return rc;
     return ensureAux(c, d, faces, (m >> K_GUO) & 1, (m >> K_MEBB) & 1);
 }
 
@@ -725,7 +741,7 @@ int plbgpu_create(int device, plbgpu_ctx** out) {
     c->rowForm = !rowKernel                           ? 0
                  : strcmp(rowKernel, "cell") == 0     ? 1
                  : strcmp(rowKernel, "vec4") == 0     ? 2
-                 : strcmp(rowKernel, "pair") == 0     ? 3
+                 : strcmp(rowKernel, "vec8") == 0     ? 4
                                                       : 0;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete c;
@@ -834,7 +850,7 @@ int plbgpu_remove_domain(plbgpu_ctx* c, int h) {
     if (d->ext) cudaFree(d->ext);
     if (d->mebb) cudaFree(d->mebb);
     if (d->surf) cudaFree(d->surf);
-    if (d->rowLists) cudaFree(d->rowLists);
+    if (d->tileLists) cudaFree(d->tileLists);
     cudaFree(d->stats);
     cudaFree(d->status);
     cudaFree(d->red);
@@ -868,10 +884,12 @@ int plbgpu_set_periodicity(plbgpu_ctx* c, int h, int px, int py, int pz) {
         d->per[0] = px != 0; d->per[1] = py != 0; d->per[2] = pz != 0;
         d->odd = false;
         d->surfDirty = d->hasSurface;
+        if (d->sparse && (rc = buildTileLists(c, d))) return rc;
         return plbgpu_send(c, h, 0, d->nx - 1, 0, d->ny - 1, 0, d->nz - 1, tmp.data(), tmp.size());
     }
     d->per[0] = px != 0; d->per[1] = py != 0; d->per[2] = pz != 0;
     d->surfDirty = d->hasSurface;
+    if (d->sparse) return buildTileLists(c, d);   // the tiles at the z ends depend on the z periodicity
     return PLBGPU_OK;
 }
 

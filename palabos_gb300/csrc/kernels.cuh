@@ -152,16 +152,22 @@ struct DevLattice {
     int per[3];
     long long n;
     unsigned* status;       // device error word (kStatusNonFinite)
-    int rowForm;            // interior-row kernel of the 2-byte forms: 0 eight cells per thread (128-bit
-                            // vectors), 1 one cell per thread (every form), 2 four cells (64-bit), 3 two cells
-    // Sparse domains: the rows (x, y) the interior-row kernels may take -- the
-    // 3x3 rows around them hold no cell outside the lattice -- and the other
-    // rows with live cells, which take the general kernel (null: no lists).
-    const int2* denseRows;
+    int rowForm;            // interior-row kernel: 0 the default (two cells per thread for the 2-byte
+                            // forms), 1 one cell per thread (every form), 2 / 4 four / eight cells per
+                            // thread with 64- / 128-bit vectors (2-byte forms, rows of 8k cells)
+    // Sparse domains: tiles (x, y, z0, z1) of at most kTileCells cells of a
+    // row.  Dense tiles -- the 3x3 rows around them hold no cell outside the
+    // lattice from z0 - 1 to z1 -- take the interior-row kernels, one block per
+    // tile; the other tiles with live cells take the general kernel (null:
+    // no lists, every row general).
+    const int4* denseTiles;
     int nDense;
-    const int2* generalRows;
+    const int4* generalTiles;
     int nGeneral;
 };
+
+// Cells of a row tile of a sparse domain's step lists.
+constexpr int kTileCells = 64;
 
 // Bits of DevLattice::status.  A statistics step that meets a NaN or an
 // infinity in the density or kinetic-energy sums of a block (a population of
@@ -589,20 +595,23 @@ __global__ void __launch_bounds__(128, RowShape<S>::blocks)
     using R = typename StoreT<S>::R;
     constexpr int NC = RowShape<S>::cells;
     int x = blockIdx.z + 1, y = blockIdx.y + 1;
-    if (L.denseRows) {   // whole blocks leave: the row is the block's
+    int z0 = blockIdx.x * blockDim.x * NC + threadIdx.x, zEnd = L.nz;
+    if (L.denseTiles) {   // one block per tile: whole blocks leave
         const int r = blockIdx.y + gridDim.y * blockIdx.z;
         if (r >= L.nDense) return;
-        x = L.denseRows[r].x;
-        y = L.denseRows[r].y;
+        const int4 t = L.denseTiles[r];
+        x = t.x;
+        y = t.y;
+        z0 = t.z + threadIdx.x;
+        zEnd = t.w;
     }
-    const int z0 = blockIdx.x * blockDim.x * NC + threadIdx.x;
     R f[NC][19];
     int kind[NC];
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
         const int z = z0 + c * blockDim.x;
         kind[c] = K_NONE;
-        if (z < L.nz) {
+        if (z < zEnd) {
             RowCell<S, ODD> rc(L, x, y, z);
             kind[c] = L.flags[rc.idx];
             if (kind[c] != K_NONE) rc.load(Pl, D, f[c]);
@@ -643,16 +652,19 @@ __global__ void __launch_bounds__(128, 8)
     pairRowStepKernel(DevLattice L, Planes<S> Pl, Deltas D, StepParams<typename StoreT<S>::R> P, StatsAcc* acc) {
     using R = typename StoreT<S>::R;
     int x = blockIdx.z + 1, y = blockIdx.y + 1;
-    if (L.denseRows) {   // whole blocks leave: the row is the block's
+    int zA = 2 * (blockIdx.x * blockDim.x + threadIdx.x), zEnd = L.nz;
+    if (L.denseTiles) {   // one block per tile: whole blocks leave
         const int r = blockIdx.y + gridDim.y * blockIdx.z;
         if (r >= L.nDense) return;
-        x = L.denseRows[r].x;
-        y = L.denseRows[r].y;
+        const int4 t = L.denseTiles[r];
+        x = t.x;
+        y = t.y;
+        zA = t.z + 2 * threadIdx.x;
+        zEnd = t.w;
     }
-    const int zA = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     double sR = 0., sU = 0.;
     unsigned long long cnt = 0, mx = 0;
-    if (zA < L.nz) {
+    if (zA < zEnd) {
         RowCell<S, ODD> ca(L, x, y, zA), cb(L, x, y, zA + 1);
         const int kA = L.flags[ca.idx], kB = L.flags[cb.idx];
         R fa[19], fb[19];
@@ -733,20 +745,23 @@ __global__ void __launch_bounds__(128, 8)
 // (periodic wrap and the domain-edge rule on every axis).  Row
 // blockIdx.y + gridDim.y * blockIdx.z enumerates the border rows: x = 0,
 // x = nx-1 (all y), then y = 0, y = ny-1 (1 <= x <= nx-2); when nx < 3 or
-// ny < 3 every row is a border row; on a sparse domain the rows are its
-// list of general rows (or every row when it has no lists).
+// ny < 3 every row is a border row; on a sparse domain the blocks are its
+// general tiles (or every row when it has no lists).
 template <typename S, bool ODD, bool STATS, bool EXT, bool SPARSE>
 __global__ void __launch_bounds__(128, sizeof(S) <= 4 ? 6 : 1) edgeRowStepKernel(DevLattice L, StepParams<typename StoreT<S>::R> P,
                                                           StatsAcc* acc, int rows) {
     using R = typename StoreT<S>::R;
-    const int z = blockIdx.x * blockDim.x + threadIdx.x;
+    int z = blockIdx.x * blockDim.x + threadIdx.x, zEnd = L.nz;
     const int row = blockIdx.y + gridDim.y * blockIdx.z;
     if (row >= rows) return;   // whole blocks
     const int nx = L.nx, ny = L.ny;
     int x, y;
-    if (SPARSE && L.generalRows) {
-        x = L.generalRows[row].x;
-        y = L.generalRows[row].y;
+    if (SPARSE && L.generalTiles) {   // one block per tile
+        const int4 t = L.generalTiles[row];
+        x = t.x;
+        y = t.y;
+        z = t.z + threadIdx.x;
+        zEnd = t.w;
     } else if (SPARSE || nx < 3 || ny < 3) {
         x = row / ny;
         y = row - x * ny;
@@ -761,7 +776,7 @@ __global__ void __launch_bounds__(128, sizeof(S) <= 4 ? 6 : 1) edgeRowStepKernel
     }
     R rhoBar = R(0), uSqr = R(0);
     bool g = false;
-    if (z < L.nz) g = processCellGeneral<S, ODD, STATS, EXT, SPARSE>(L, P, x, y, z, acc, rhoBar, uSqr);
+    if (z < zEnd) g = processCellGeneral<S, ODD, STATS, EXT, SPARSE>(L, P, x, y, z, acc, rhoBar, uSqr);
     accumulateStats<STATS>(g, (double)rhoBar, (double)uSqr, acc, L.status);
 }
 

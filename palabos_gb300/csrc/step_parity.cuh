@@ -16,33 +16,37 @@ struct StepLaunch {
 
     // Row kernel of this storage type: the paired kernel for the 2-byte forms
     // when rows have an even length, the one-cell register kernel otherwise.
+    // Two cells per thread: the fastest form of the 2-byte storage types on
+    // GB300 (rows of even length).
     static bool pairedRows(const DevLattice& L) { return sizeof(S) == 2 && L.nz % 2 == 0 && L.rowForm != 1; }
     // Eight (or four) cells per thread, 128-bit (64-bit) population vectors
-    // (vecrow.cuh): rows of a multiple of eight cells.
+    // (vecrow.cuh), on request: bit-identical, but 34-43% slower than the
+    // paired kernel on GB300 (the packed state of eight cells holds 168
+    // registers, 12 resident warps per SM, too few to keep HBM busy).
     static bool vectorRows(const DevLattice& L) {
-        return sizeof(S) == 2 && L.nz % 8 == 0 && (L.rowForm == 0 || L.rowForm == 2);
+        return sizeof(S) == 2 && L.nz % 8 == 0 && (L.rowForm == 4 || L.rowForm == 2);
     }
 
     template <bool ODD, bool STATS, bool EXT>
     static int stepSplit(const DevLattice& L, const StepParams<R>& p, StatsAcc* acc, cudaStream_t s,
                          const SideStream* side) {
         int launched = 0;
-        // A sparse domain with row lists runs its dense rows (no cell outside
-        // the lattice in the 3x3 rows around them) through the interior-row
-        // kernels and the other live rows through the general addressing,
-        // which checks each neighbour's kind; without lists every row goes the
-        // general way.
-        const bool lists = L.sparse && (L.denseRows || L.generalRows);
+        // A sparse domain with tile lists runs its dense tiles (no cell outside
+        // the lattice in the 3x3 rows around them, one cell beyond each end)
+        // through the interior-row kernels, one block per tile, and its other
+        // live tiles through the general addressing, which checks each
+        // neighbour's kind; without lists every row goes the general way.
+        const bool lists = L.sparse && (L.denseTiles || L.generalTiles);
         const bool general = (L.sparse && !lists) || L.nx < 3 || L.ny < 3;
         const int edgeRows = lists ? L.nGeneral : general ? L.nx * L.ny : 2 * L.ny + 2 * (L.nx - 2);
         const long long interiorRows = lists ? L.nDense : (long long)(L.nx - 2) * (L.ny - 2);
-        // grid (blocksPerRow, y, z) over the interior rows: the row is
-        // (blockIdx.z + 1, blockIdx.y + 1), or entry blockIdx.y + gridDim.y *
-        // blockIdx.z of the dense-row list
+        // grid over the interior rows: (blocksPerRow, ny-2, nx-2), the row
+        // being (blockIdx.z + 1, blockIdx.y + 1); or one block per dense tile,
+        // entry blockIdx.y + gridDim.y * blockIdx.z of the list
         auto interiorGrid = [&](int blocksPerRow) {
             if (!lists) return dim3((unsigned)blocksPerRow, (unsigned)(L.ny - 2), (unsigned)(L.nx - 2));
             const unsigned gy = (unsigned)(L.nDense < 65535 ? L.nDense : 65535);
-            return dim3((unsigned)blocksPerRow, gy, (unsigned)((L.nDense + gy - 1) / gy));
+            return dim3(1u, gy, (unsigned)((L.nDense + gy - 1) / gy));
         };
         // The border rows run on the side stream (the context's highest
         // priority), beside the interior kernel.  Submission order decides
@@ -66,11 +70,11 @@ struct StepLaunch {
                         d.d[i] = cdir(i, 0) * L.ny * L.nz + cdir(i, 1) * L.nz;
                     }
                     if (L.rowForm == 2) {   // four cells per thread, 8-byte vectors
-                        const long long segs = interiorRows * (L.nz / 4);
+                        const long long segs = interiorRows * (lists ? kTileCells / 4 : L.nz / 4);
                         const unsigned blocks = (unsigned)((segs + kBlock - 1) / kBlock);
                         vecRowStepKernel<S, ODD, STATS, EXT, 4><<<blocks, kBlock, 0, s>>>(L, pl, d, p, acc, segs);
                     } else {
-                        const long long segs = interiorRows * (L.nz / 8);
+                        const long long segs = interiorRows * (lists ? kTileCells / 8 : L.nz / 8);
                         const unsigned blocks = (unsigned)((segs + kBlock - 1) / kBlock);
                         vecRowStepKernel<S, ODD, STATS, EXT, 8><<<blocks, kBlock, 0, s>>>(L, pl, d, p, acc, segs);
                     }
@@ -87,6 +91,7 @@ struct StepLaunch {
                     const int pairs = L.nz / 2;
                     int tpb = (pairs + 31) / 32 * 32;
                     tpb = tpb < kBlock ? tpb : kBlock;
+                    if (lists) tpb = kTileCells / 2;
                     pairRowStepKernel<S, ODD, STATS, EXT><<<interiorGrid((pairs + tpb - 1) / tpb), tpb, 0, s>>>(L, pl, d, p,
                                                                                                          acc);
                     ++launched;
@@ -103,6 +108,7 @@ struct StepLaunch {
                 constexpr int NC = RowShape<S>::cells;
                 int tpb = ((L.nz + NC - 1) / NC + 31) / 32 * 32;
                 tpb = tpb < kBlock ? tpb : kBlock;
+                if (lists) tpb = (kTileCells + NC - 1) / NC;
                 rowStepKernel<S, ODD, STATS, EXT><<<interiorGrid((L.nz + tpb * NC - 1) / (tpb * NC)), tpb, 0, s>>>(L, pl, d, p,
                                                                                                         acc);
                 ++launched;
@@ -111,9 +117,9 @@ struct StepLaunch {
         auto border = [&]() {
             if (edgeRows == 0) return;
             const int gy = edgeRows < 65535 ? edgeRows : 65535;
-            dim3 g((unsigned)((L.nz + kBlock - 1) / kBlock), (unsigned)gy, (unsigned)((edgeRows + gy - 1) / gy));
+            dim3 g(lists ? 1u : (unsigned)((L.nz + kBlock - 1) / kBlock), (unsigned)gy, (unsigned)((edgeRows + gy - 1) / gy));
             if (L.sparse)
-                edgeRowStepKernel<S, ODD, STATS, EXT, true><<<g, kBlock, 0, es>>>(L, p, acc, edgeRows);
+                edgeRowStepKernel<S, ODD, STATS, EXT, true><<<g, lists ? kTileCells : kBlock, 0, es>>>(L, p, acc, edgeRows);
             else
                 edgeRowStepKernel<S, ODD, STATS, EXT, false><<<g, kBlock, 0, es>>>(L, p, acc, edgeRows);
             ++launched;

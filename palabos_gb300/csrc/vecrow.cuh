@@ -154,17 +154,34 @@ __global__ void __launch_bounds__(128, VecShape<CPT>::blocks)
     // Threads past the last segment mirror it (the warp's shuffles need every
     // lane); they store nothing and gather no statistics.
     const long long gg = live ? g : segments - 1;
-    const int row = (int)(gg / RS), seg = (int)(gg - (long long)row * RS);
-    const int x = L.denseRows ? L.denseRows[row].x : 1 + row / (L.ny - 2);
-    const int y = L.denseRows ? L.denseRows[row].y : 1 + row % (L.ny - 2);
+    int x, y, z0;
+    bool live2 = live, upOk, downOk;
     const int lane = threadIdx.x & 31;
-    const bool first = seg == 0, last = seg == RS - 1;
-    const bool upOk = !first && lane > 0;           // lane - 1 holds the CPT cells below z0 in this row
-    const bool downOk = !last && lane < 31;         // lane + 1 holds the CPT cells from z0 + CPT on
-    const bool perZ = L.per[2] != 0;
+    if (L.denseTiles) {   // sparse domain: segments of the dense tiles
+        constexpr int TS = kTileCells / CPT;
+        const int r = (int)(gg / TS), s = (int)(gg - (long long)r * TS);
+        const int4 t = L.denseTiles[r];
+        x = t.x;
+        y = t.y;
+        z0 = t.z + s * CPT;
+        if (z0 >= t.w) {  // past a short tile's end: mirror its first segment
+            z0 = t.z;
+            live2 = false;
+        }
+        upOk = s > 0 && lane > 0;
+        downOk = s + 1 < TS && z0 + CPT < t.w && lane < 31;
+    } else {
+        const int row = (int)(gg / RS), seg = (int)(gg - (long long)row * RS);
+        x = 1 + row / (L.ny - 2);
+        y = 1 + row % (L.ny - 2);
+        z0 = seg * CPT;
+        upOk = seg > 0 && lane > 0;                 // lane - 1 holds the CPT cells below z0 in this row
+        downOk = seg < RS - 1 && lane < 31;         // lane + 1 holds the CPT cells from z0 + CPT on
+    }
     const int nz = L.nz;
+    const bool first = z0 == 0, last = z0 + CPT == nz;
+    const bool perZ = L.per[2] != 0;
     const int rowIdx = (x * L.ny + y) * nz;
-    const int z0 = seg * CPT;
     const int idx0 = rowIdx + z0;
 
     Words<NW> v[19];
@@ -221,10 +238,10 @@ __global__ void __launch_bounds__(128, VecShape<CPT>::blocks)
         const int idx = idx0 + c;
         R rhoBar = R(0), uSqr = R(0);
         if (P.pending && isFace(k)) completeIfFace<R>(L, idx, k, f);
-        const bool gathers = collideCell<S, EXT>(L, P, idx, k, f, rhoBar, uSqr, acc, STATS && live);
+        const bool gathers = collideCell<S, EXT>(L, P, idx, k, f, rhoBar, uSqr, acc, STATS && live2);
 #pragma unroll
         for (int i = 0; i < 19; ++i) v[i].w[w] = Half16<S>::put(v[i].w[w], hi, f[i], Pl.p[i] + idx, P.seed);
-        if (STATS && live && gathers) {
+        if (STATS && live2 && gathers) {
             sR += (double)rhoBar;
             sU += (double)uSqr;
             cnt += 1;
@@ -237,7 +254,7 @@ __global__ void __launch_bounds__(128, VecShape<CPT>::blocks)
 #pragma unroll
     for (int i = 0; i < 19; ++i) {
         if (!ODD) {
-            if (live) stWords<NW>(Pl.p[opp(i)] + idx0, v[i]);
+            if (live2) stWords<NW>(Pl.p[opp(i)] + idx0, v[i]);
         } else {
             S* dst = Pl.p[i];
             const int drow = rowIdx + D.d[i];       // destination row x + c_i (x and y part)
@@ -245,10 +262,10 @@ __global__ void __launch_bounds__(128, VecShape<CPT>::blocks)
             const int cz = cdir(i, 2);
             const Words<NW>& a = v[i];
             if (cz == 0) {
-                if (live) stWords<NW>(dst + d0, a);
+                if (live2) stWords<NW>(dst + d0, a);
             } else if (cz > 0) {                    // cells z0.. -> positions z0+1 .. z0+CPT
                 const unsigned prev = __shfl_up_sync(0xffffffffu, a.w[NW - 1], 1);
-                if (live) {
+                if (live2) {
                     if (upOk) {
                         stWords<NW>(dst + d0, shiftUp<NW>(a, prev));
                     } else {                        // position z0 is written by its owner
@@ -265,7 +282,7 @@ __global__ void __launch_bounds__(128, VecShape<CPT>::blocks)
                 }
             } else {                                // cells z0.. -> positions z0-1 .. z0+CPT-2
                 const unsigned next = __shfl_down_sync(0xffffffffu, a.w[0], 1);
-                if (live) {
+                if (live2) {
                     if (downOk) {
                         stWords<NW>(dst + d0, shiftDown<NW>(a, next));
                     } else {                        // position z0+CPT-1 is written by its owner

@@ -6,9 +6,9 @@ largest population error relative to the largest |f-bar| of the case, with
 the tolerance of each storage type written here (about twice the largest
 error measured on a GB300 over these cases: FP32 6.1e-6, FP16 8.9e-4, BF16
 8.5e-3, BF16 with stochastic rounding 1.2e-2).  They run through the same C
-ABI and the same interior-row kernels as production runs: the 128-bit
-eight-cell kernel of the 2-byte forms where rows hold a multiple of eight
-cells, the one-cell kernel otherwise.
+ABI and the same interior-row kernels as production runs: the paired
+(two-cell) kernel of the 2-byte forms where rows have an even length, the
+one-cell kernel otherwise.
 """
 import numpy as np
 import pytest
@@ -64,9 +64,9 @@ def test_reduced_precision_external_form(name, precision):
 
 @pytest.mark.parametrize("precision", ["fp32", "bf16"])
 def test_row_kernels_agree_across_row_lengths(precision):
-    """nz = 32 (the 128-bit eight-cell kernel for BF16, the one-cell kernel for
-    FP32) and nz = 33 (the one-cell kernel) give the same physics on a flow
-    that depends only on y."""
+    """nz = 32 (the paired kernel for BF16, the one-cell kernel for FP32) and
+    nz = 33 (the one-cell kernel) give the same physics on a flow that
+    depends only on y."""
     from palabos_gb300 import DeviceLattice3D
     out = []
     for nz in (32, 33):

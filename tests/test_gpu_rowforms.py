@@ -1,10 +1,11 @@
-"""The 128-bit interior-row kernel of the 2-byte storage forms (eight cells per
-thread, palabos_gb300/csrc/vecrow.cuh) against the one-cell kernel
-(PLBGPU_ROW_KERNEL=cell), bit for bit.
+"""The interior-row kernels of the 2-byte storage forms against the one-cell
+kernel (PLBGPU_ROW_KERNEL=cell), bit for bit: the default paired kernel (two
+cells per thread) and the vector kernels (palabos_gb300/csrc/vecrow.cuh:
+eight or four cells per thread, 128- or 64-bit population vectors).
 
-Both run the same FP32 collision on the same stored values, so every stored
+All run the same FP32 collision on the same stored values, so every stored
 population must be identical; the cases reach every path of the vector
-kernel's streaming:
+kernels' streaming:
 
   rows of 1, 2, 12 and 64 eight-cell segments (a whole row in one lane, rows
   inside a warp, rows straddling warp boundaries, rows spanning two warps);
@@ -26,10 +27,11 @@ pytestmark = pytest.mark.gpu
 
 
 def _context(form):
-    """A context whose interior rows run `form` ("cell" or the default)."""
+    """A context whose interior rows run `form` ("cell", "vec8", "vec4" or
+    "default")."""
     old = os.environ.get("PLBGPU_ROW_KERNEL")
-    if form == "cell":
-        os.environ["PLBGPU_ROW_KERNEL"] = "cell"
+    if form != "default":
+        os.environ["PLBGPU_ROW_KERNEL"] = form
     else:
         os.environ.pop("PLBGPU_ROW_KERNEL", None)
     try:
@@ -128,11 +130,12 @@ def _run(case, precision, form, steps, external=False):
 
 
 @pytest.mark.parametrize("precision", ["bf16", "fp16"])
-@pytest.mark.parametrize("steps", [6, 9])
+@pytest.mark.parametrize("form", ["default", "vec8", "vec4"])
 @pytest.mark.parametrize("name", sorted(CASES))
-def test_vector_rows_equal_one_cell_rows(name, steps, precision):
+def test_row_kernels_equal_one_cell_rows(name, form, precision):
     case = CASES[name]()
-    f_vec, st_vec = _run(case, precision, "vector", steps)
+    steps = 9   # both AA parities, ending on an odd step
+    f_vec, st_vec = _run(case, precision, form, steps)
     f_cell, st_cell = _run(case, precision, "cell", steps)
     assert np.isfinite(f_vec).all()
     if not np.array_equal(f_vec, f_cell):
@@ -144,18 +147,20 @@ def test_vector_rows_equal_one_cell_rows(name, steps, precision):
 
 
 @pytest.mark.parametrize("precision", ["bf16", "fp16"])
-def test_vector_rows_external_form_equal_one_cell_rows(precision):
+@pytest.mark.parametrize("form", ["default", "vec8", "vec4"])
+def test_row_kernels_external_form_equal_one_cell_rows(form, precision):
     case = _periodic((8, 6, 64), 19)
-    f_vec, _ = _run(case, precision, "vector", 7, external=True)
+    f_vec, _ = _run(case, precision, form, 7, external=True)
     f_cell, _ = _run(case, precision, "cell", 7, external=True)
     assert np.array_equal(f_vec, f_cell)
 
 
-def test_vector_rows_stochastic_rounding_tracks_one_cell_rows():
+@pytest.mark.parametrize("form", ["default", "vec8"])
+def test_row_kernels_stochastic_rounding_track_one_cell_rows(form):
     """BF16 with stochastic rounding draws its random bits from different
-    addresses in the two kernels, so the states agree only to the rounding."""
+    addresses in the kernels, so the states agree only to the rounding."""
     case = _periodic((7, 6, 96), 20)
-    f_vec, _ = _run(case, "bf16sr", "vector", 9)
+    f_vec, _ = _run(case, "bf16sr", form, 9)
     f_cell, _ = _run(case, "bf16sr", "cell", 9)
     scale = np.abs(f_cell).max()
     assert np.abs(f_vec - f_cell).max() <= 0.03 * scale
