@@ -157,17 +157,18 @@ struct DevLattice {
                             // thread with 64- / 128-bit vectors (2-byte forms, rows of 8k cells)
     // Sparse domains: tiles (x, y, z0, z1) of at most kTileCells cells of a
     // row.  Dense tiles -- the 3x3 rows around them hold no cell outside the
-    // lattice from z0 - 1 to z1 -- take the interior-row kernels, one block per
-    // tile; the other tiles with live cells take the general kernel (null:
-    // no lists, every row general).
+    // lattice from z0 - 1 to z1 -- take the interior-row kernels; the other
+    // tiles with live cells take the general kernel (null: no lists, every
+    // row general).
     const int4* denseTiles;
     int nDense;
     const int4* generalTiles;
     int nGeneral;
 };
 
-// Cells of a row tile of a sparse domain's step lists.
-constexpr int kTileCells = 64;
+// Cells of a row tile of a sparse domain's step lists; the kernels run several
+// tiles per block (blockDim / threads per tile).
+constexpr int kTileCells = 32;
 
 // Bits of DevLattice::status.  A statistics step that meets a NaN or an
 // infinity in the density or kinetic-energy sums of a block (a population of
@@ -596,14 +597,16 @@ __global__ void __launch_bounds__(128, RowShape<S>::blocks)
     constexpr int NC = RowShape<S>::cells;
     int x = blockIdx.z + 1, y = blockIdx.y + 1;
     int z0 = blockIdx.x * blockDim.x * NC + threadIdx.x, zEnd = L.nz;
-    if (L.denseTiles) {   // one block per tile: whole blocks leave
-        const int r = blockIdx.y + gridDim.y * blockIdx.z;
-        if (r >= L.nDense) return;
-        const int4 t = L.denseTiles[r];
-        x = t.x;
-        y = t.y;
-        z0 = t.z + threadIdx.x;
-        zEnd = t.w;
+    if (L.denseTiles) {   // blockDim / kTileCells tiles per block (NC = 1)
+        const int r = (blockIdx.y + gridDim.y * blockIdx.z) * (blockDim.x / kTileCells) + threadIdx.x / kTileCells;
+        zEnd = -1;        // no cells past the list's end
+        if (r < L.nDense) {
+            const int4 t = L.denseTiles[r];
+            x = t.x;
+            y = t.y;
+            z0 = t.z + threadIdx.x % kTileCells;
+            zEnd = t.w;
+        }
     }
     R f[NC][19];
     int kind[NC];
@@ -653,14 +656,17 @@ __global__ void __launch_bounds__(128, 8)
     using R = typename StoreT<S>::R;
     int x = blockIdx.z + 1, y = blockIdx.y + 1;
     int zA = 2 * (blockIdx.x * blockDim.x + threadIdx.x), zEnd = L.nz;
-    if (L.denseTiles) {   // one block per tile: whole blocks leave
-        const int r = blockIdx.y + gridDim.y * blockIdx.z;
-        if (r >= L.nDense) return;
-        const int4 t = L.denseTiles[r];
-        x = t.x;
-        y = t.y;
-        zA = t.z + 2 * threadIdx.x;
-        zEnd = t.w;
+    if (L.denseTiles) {   // blockDim / (kTileCells / 2) tiles per block
+        constexpr int TT = kTileCells / 2;
+        const int r = (blockIdx.y + gridDim.y * blockIdx.z) * (blockDim.x / TT) + threadIdx.x / TT;
+        zEnd = -1;        // no cells past the list's end
+        if (r < L.nDense) {
+            const int4 t = L.denseTiles[r];
+            x = t.x;
+            y = t.y;
+            zA = t.z + 2 * (threadIdx.x % TT);
+            zEnd = t.w;
+        }
     }
     double sR = 0., sU = 0.;
     unsigned long long cnt = 0, mx = 0;
@@ -752,16 +758,21 @@ __global__ void __launch_bounds__(128, sizeof(S) <= 4 ? 6 : 1) edgeRowStepKernel
                                                           StatsAcc* acc, int rows) {
     using R = typename StoreT<S>::R;
     int z = blockIdx.x * blockDim.x + threadIdx.x, zEnd = L.nz;
-    const int row = blockIdx.y + gridDim.y * blockIdx.z;
-    if (row >= rows) return;   // whole blocks
+    int row = blockIdx.y + gridDim.y * blockIdx.z;
+    const bool tiles = SPARSE && L.generalTiles;
+    if (tiles) row = row * (blockDim.x / kTileCells) + threadIdx.x / kTileCells;   // several tiles per block
+    else if (row >= rows) return;   // whole blocks
     const int nx = L.nx, ny = L.ny;
-    int x, y;
-    if (SPARSE && L.generalTiles) {   // one block per tile
-        const int4 t = L.generalTiles[row];
-        x = t.x;
-        y = t.y;
-        z = t.z + threadIdx.x;
-        zEnd = t.w;
+    int x = 0, y = 0;
+    if (tiles) {
+        zEnd = -1;                  // no cells past the list's end
+        if (row < rows) {
+            const int4 t = L.generalTiles[row];
+            x = t.x;
+            y = t.y;
+            z = t.z + threadIdx.x % kTileCells;
+            zEnd = t.w;
+        }
     } else if (SPARSE || nx < 3 || ny < 3) {
         x = row / ny;
         y = row - x * ny;

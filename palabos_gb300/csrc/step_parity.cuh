@@ -43,10 +43,12 @@ struct StepLaunch {
         // grid over the interior rows: (blocksPerRow, ny-2, nx-2), the row
         // being (blockIdx.z + 1, blockIdx.y + 1); or one block per dense tile,
         // entry blockIdx.y + gridDim.y * blockIdx.z of the list
-        auto interiorGrid = [&](int blocksPerRow) {
+        // tilesPerBlock: the tiles one block of the list steps
+        auto interiorGrid = [&](int blocksPerRow, int tilesPerBlock) {
             if (!lists) return dim3((unsigned)blocksPerRow, (unsigned)(L.ny - 2), (unsigned)(L.nx - 2));
-            const unsigned gy = (unsigned)(L.nDense < 65535 ? L.nDense : 65535);
-            return dim3(1u, gy, (unsigned)((L.nDense + gy - 1) / gy));
+            const int blocks = (L.nDense + tilesPerBlock - 1) / tilesPerBlock;
+            const unsigned gy = (unsigned)(blocks < 65535 ? blocks : 65535);
+            return dim3(1u, gy, (unsigned)((blocks + gy - 1) / gy));
         };
         // The border rows run on the side stream (the context's highest
         // priority), beside the interior kernel.  Submission order decides
@@ -91,9 +93,9 @@ struct StepLaunch {
                     const int pairs = L.nz / 2;
                     int tpb = (pairs + 31) / 32 * 32;
                     tpb = tpb < kBlock ? tpb : kBlock;
-                    if (lists) tpb = kTileCells / 2;
-                    pairRowStepKernel<S, ODD, STATS, EXT><<<interiorGrid((pairs + tpb - 1) / tpb), tpb, 0, s>>>(L, pl, d, p,
-                                                                                                         acc);
+                    if (lists) tpb = kBlock;
+                    const dim3 g = interiorGrid((pairs + tpb - 1) / tpb, kBlock / (kTileCells / 2));
+                    pairRowStepKernel<S, ODD, STATS, EXT><<<g, tpb, 0, s>>>(L, pl, d, p, acc);
                     ++launched;
                 }
             } else {
@@ -108,18 +110,20 @@ struct StepLaunch {
                 constexpr int NC = RowShape<S>::cells;
                 int tpb = ((L.nz + NC - 1) / NC + 31) / 32 * 32;
                 tpb = tpb < kBlock ? tpb : kBlock;
-                if (lists) tpb = (kTileCells + NC - 1) / NC;
-                rowStepKernel<S, ODD, STATS, EXT><<<interiorGrid((L.nz + tpb * NC - 1) / (tpb * NC)), tpb, 0, s>>>(L, pl, d, p,
+                if (lists) tpb = kBlock;
+                rowStepKernel<S, ODD, STATS, EXT><<<interiorGrid((L.nz + tpb * NC - 1) / (tpb * NC), kBlock / kTileCells), tpb, 0, s>>>(L, pl, d, p,
                                                                                                         acc);
                 ++launched;
             }
         };
         auto border = [&]() {
             if (edgeRows == 0) return;
-            const int gy = edgeRows < 65535 ? edgeRows : 65535;
-            dim3 g(lists ? 1u : (unsigned)((L.nz + kBlock - 1) / kBlock), (unsigned)gy, (unsigned)((edgeRows + gy - 1) / gy));
+            // rows, or blocks of kBlock / kTileCells tiles of the general-tile list
+            const int blocks = lists ? (edgeRows + kBlock / kTileCells - 1) / (kBlock / kTileCells) : edgeRows;
+            const int gy = blocks < 65535 ? blocks : 65535;
+            dim3 g(lists ? 1u : (unsigned)((L.nz + kBlock - 1) / kBlock), (unsigned)gy, (unsigned)((blocks + gy - 1) / gy));
             if (L.sparse)
-                edgeRowStepKernel<S, ODD, STATS, EXT, true><<<g, lists ? kTileCells : kBlock, 0, es>>>(L, p, acc, edgeRows);
+                edgeRowStepKernel<S, ODD, STATS, EXT, true><<<g, kBlock, 0, es>>>(L, p, acc, edgeRows);
             else
                 edgeRowStepKernel<S, ODD, STATS, EXT, false><<<g, kBlock, 0, es>>>(L, p, acc, edgeRows);
             ++launched;
