@@ -69,8 +69,10 @@ struct Domain {
     void* ext = nullptr;         // 4 * n of FP64 or FP32: external rho-bar, jx, jy, jz
     uint32_t* mebb = nullptr;    // n
     int4* surf = nullptr;        // edge cells, then corner cells: (x, y, z, kind)
-    int4* tileLists = nullptr;   // sparse domains: dense tiles, then general tiles (x, y, z0, z1)
-    int nDense = 0, nGeneral = 0, tileListCap = 0;
+    int4* tileLists = nullptr;   // sparse domains: dense, masked, then general tiles (x, y, z0, z1)
+    int nDense = 0, nMasked = 0, nGeneral = 0, tileListCap = 0;
+    uint32_t* tileMasks = nullptr;   // per cell of the masked tiles: neighbours outside the lattice
+    int tileMaskCap = 0;
     int surfCap = 0, nEdges = 0, nCorners = 0;
     bool hasSurface = false;     // any edge or corner kind
     bool sparse = false;         // any cell outside the lattice (K_NONE)
@@ -105,7 +107,10 @@ struct Domain {
         const bool lists = sparse && tileLists;
         L.denseTiles = lists && nDense ? tileLists : nullptr;
         L.nDense = lists ? nDense : 0;
-        L.generalTiles = lists && nGeneral ? tileLists + nDense : nullptr;
+        L.maskedTiles = lists && nMasked ? tileLists + nDense : nullptr;
+        L.nMasked = lists ? nMasked : 0;
+        L.tileMasks = lists && nMasked ? tileMasks : nullptr;
+        L.generalTiles = lists && nGeneral ? tileLists + nDense + nMasked : nullptr;
         L.nGeneral = lists ? nGeneral : 0;
         return L;
     }
@@ -334,6 +339,31 @@ __global__ void tileLiveKernel(const uint8_t* flags, int rows, int nz, int tiles
     live[i] = (uint8_t)((any ? 1 : 0) | (all ? 2 : 0));
 }
 
+// Per cell of the masked tiles: bit k set when the neighbour x + c_k is
+// outside the lattice (its rows are interior rows: x and y moves stay inside;
+// along z a periodic axis wraps and a non-periodic one's edge is the kernels'
+// own domain-edge rule).
+__global__ void tileMaskKernel(const uint8_t* flags, int ny, int nz, int perZ, const int4* tiles, int nTiles,
+                               uint32_t* masks) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= (long long)nTiles * kTileCells) return;
+    const int4 t = tiles[i / kTileCells];
+    const int z = t.z + (int)(i % kTileCells);
+    uint32_t m = 0;
+    if (z < t.w) {
+        for (int k = 1; k < 19; ++k) {
+            int zz = z + cdir(k, 2);
+            if (zz < 0 || zz >= nz) {
+                if (!perZ) continue;
+                zz = zz < 0 ? zz + nz : zz - nz;
+            }
+            const long long nb = ((long long)(t.x + cdir(k, 0)) * ny + (t.y + cdir(k, 1))) * nz + zz;
+            if (flags[nb] == K_NONE) m |= 1u << k;
+        }
+    }
+    masks[i] = m;
+}
+
 __global__ void kindMaskKernel(const uint8_t* flags, long long n, unsigned long long* mask) {
     unsigned long long m = 0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
@@ -461,10 +491,11 @@ int kindMask(plbgpu_ctx* c, Domain* d, unsigned long long* mask) {
 // The tile lists of a sparse domain: tiles of up to kTileCells cells of a row
 // whose 3x3 neighbourhood of rows is part of the lattice from one cell before
 // the tile to one cell after it ("dense": the interior-row kernels step them,
-// no neighbour falls outside), then the other tiles with a live cell (the
-// general kernel, which treats a neighbour outside the lattice like the domain
-// edge).  Tiles without live cells are left out.  Rebuilt when the kinds or
-// the periodicity change.
+// no neighbour falls outside); the other tiles of interior rows with a live
+// cell ("masked": the one-cell row kernel, with each cell's mask of neighbours
+// outside the lattice, which follow the domain-edge rule); the tiles of the
+// domain's border rows with a live cell (the general kernel).  Tiles without
+// live cells are left out.  Rebuilt when the kinds or the periodicity change.
 int buildTileLists(plbgpu_ctx* c, Domain* d) {
     const int rows = d->nx * d->ny;
     const int tiles = (d->nz + kTileCells - 1) / kTileCells;
@@ -478,18 +509,19 @@ int buildTileLists(plbgpu_ctx* c, Domain* d) {
     CUDA_TRY(c, cudaMemcpyAsync(live.data(), dl, nt, cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     auto at = [&](int x, int y, int t) { return live[((size_t)x * d->ny + y) * tiles + t]; };
-    std::vector<int4> dense, general;
+    std::vector<int4> dense, masked, general;
     for (int x = 0; x < d->nx; ++x)
         for (int y = 0; y < d->ny; ++y)
             for (int t = 0; t < tiles; ++t) {
                 if (!(at(x, y, t) & 1)) continue;
-                bool full = x >= 1 && x <= d->nx - 2 && y >= 1 && y <= d->ny - 2;
+                const bool interiorRow = x >= 1 && x <= d->nx - 2 && y >= 1 && y <= d->ny - 2;
+                bool full = interiorRow;
                 for (int dx = -1; dx <= 1 && full; ++dx)
                     for (int dy = -1; dy <= 1 && full; ++dy) full = (at(x + dx, y + dy, t) & 2) != 0;
                 const int z0 = t * kTileCells, z1 = std::min(z0 + kTileCells, d->nz);
-                (full ? dense : general).push_back(make_int4(x, y, z0, z1));
+                (full ? dense : interiorRow ? masked : general).push_back(make_int4(x, y, z0, z1));
             }
-    const int total = (int)(dense.size() + general.size());
+    const int total = (int)(dense.size() + masked.size() + general.size());
     if (total > d->tileListCap) {
         if (d->tileLists) {
             CUDA_TRY(c, cudaStreamSynchronize(c->stream));
@@ -502,12 +534,33 @@ int buildTileLists(plbgpu_ctx* c, Domain* d) {
         d->tileListCap = total > 0 ? total : 1;
         d->deviceBytes += sizeof(int4) * (size_t)d->tileListCap;
     }
+    const int nd = (int)dense.size(), nm = (int)masked.size();
+    dense.insert(dense.end(), masked.begin(), masked.end());
     dense.insert(dense.end(), general.begin(), general.end());
     if (total)
         CUDA_TRY(c, cudaMemcpyAsync(d->tileLists, dense.data(), sizeof(int4) * (size_t)total, cudaMemcpyHostToDevice,
                                     c->stream));
+    if (nm > d->tileMaskCap) {
+        if (d->tileMasks) {
+            CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+            cudaFree(d->tileMasks);
+            d->deviceBytes -= sizeof(uint32_t) * kTileCells * (size_t)d->tileMaskCap;
+            d->tileMasks = nullptr;
+            d->tileMaskCap = 0;
+        }
+        CUDA_TRY(c, cudaMalloc(&d->tileMasks, sizeof(uint32_t) * kTileCells * (size_t)nm));
+        d->tileMaskCap = nm;
+        d->deviceBytes += sizeof(uint32_t) * kTileCells * (size_t)nm;
+    }
+    if (nm) {
+        const long long cells = (long long)nm * kTileCells;
+        tileMaskKernel<<<(unsigned)((cells + 255) / 256), 256, 0, c->stream>>>(d->flags, d->ny, d->nz, d->per[2],
+                                                                            d->tileLists + nd, nm, d->tileMasks);
+        if ((rc = launchBox(c))) return rc;
+    }
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-    d->nDense = total - (int)general.size();
+    d->nDense = nd;
+    d->nMasked = nm;
     d->nGeneral = (int)general.size();
     return PLBGPU_OK;
 }
@@ -851,6 +904,7 @@ int plbgpu_remove_domain(plbgpu_ctx* c, int h) {
     if (d->mebb) cudaFree(d->mebb);
     if (d->surf) cudaFree(d->surf);
     if (d->tileLists) cudaFree(d->tileLists);
+    if (d->tileMasks) cudaFree(d->tileMasks);
     cudaFree(d->stats);
     cudaFree(d->status);
     cudaFree(d->red);

@@ -164,6 +164,12 @@ struct DevLattice {
     int nDense;
     const int4* generalTiles;
     int nGeneral;
+    // Interior-row tiles next to dropped blocks: the one-cell row kernel with
+    // a per-cell mask of the neighbours outside the lattice (tileMasks, one
+    // 32-bit word per cell, kTileCells per tile).
+    const int4* maskedTiles;
+    int nMasked;
+    const uint32_t* tileMasks;
 };
 
 // Cells of a row tile of a sparse domain's step lists; the kernels run several
@@ -526,10 +532,14 @@ struct Deltas {
 // plane_i + idx +- delta_i with uniform deltas and a 32-bit cell index; only
 // the ten populations that move along z carry a per-thread wrap / reflection
 // select.
-template <typename S, bool ODD>
+template <typename S, bool ODD, bool MASKED = false>
 struct RowCell {
     int idx, wrapM, wrapP;
     bool okM, okP;
+    // MASKED: bit k set when the neighbour x + c_k is outside the lattice (a
+    // sparse domain's dropped block): that population follows the
+    // domain-edge rule, like one leaving a non-periodic box
+    unsigned gone = 0;
 
     __device__ __forceinline__ RowCell(const DevLattice& L, int x, int y, int z) {
         idx = (x * L.ny + y) * L.nz + z;
@@ -547,12 +557,13 @@ struct RowCell {
             if (!ODD) {
                 f[i] = StoreT<S>::ld(Pl.p[i] + idx);
             } else {
-                const int mz = -cdir(i, 2);   // the source is x - c_i
-                if (mz == 0) {
+                const int mz = -cdir(i, 2);   // the source is x - c_i = x + c_opp(i)
+                if (mz == 0 && !MASKED) {
                     f[i] = StoreT<S>::ld(Pl.p[opp(i)] + (idx - D.d[i]));
                 } else {
-                    const bool ok = mz < 0 ? okM : okP;
-                    const int off = -D.d[i] + (mz < 0 ? wrapM : wrapP);
+                    bool ok = mz == 0 ? true : (mz < 0 ? okM : okP);
+                    if (MASKED) ok = ok && !((gone >> opp(i)) & 1u);
+                    const int off = -D.d[i] + (mz == 0 ? 0 : (mz < 0 ? wrapM : wrapP));
                     const S* a = ok ? Pl.p[opp(i)] + (idx + off) : Pl.p[i] + idx;
                     f[i] = StoreT<S>::ld(a);
                 }
@@ -569,11 +580,12 @@ struct RowCell {
                 StoreT<S>::st(Pl.p[opp(i)] + idx, f[i], salt);
             } else {
                 const int cz = cdir(i, 2);    // the destination is x + c_i
-                if (cz == 0) {
+                if (cz == 0 && !MASKED) {
                     StoreT<S>::st(Pl.p[i] + (idx + D.d[i]), f[i], salt);
                 } else {
-                    const bool ok = cz < 0 ? okM : okP;
-                    const int off = D.d[i] + (cz < 0 ? wrapM : wrapP);
+                    bool ok = cz == 0 ? true : (cz < 0 ? okM : okP);
+                    if (MASKED) ok = ok && !((gone >> i) & 1u);
+                    const int off = D.d[i] + (cz == 0 ? 0 : (cz < 0 ? wrapM : wrapP));
                     S* a = ok ? Pl.p[i] + (idx + off) : Pl.p[opp(i)] + idx;
                     StoreT<S>::st(a, f[i], salt);
                 }
@@ -590,22 +602,26 @@ template <> struct RowShape<double> { static constexpr int cells = 1, blocks = 5
 // Rows with 1 <= x <= nx-2 and 1 <= y <= ny-2 (all z): nearly all of the time
 // step.  A block covers RowShape::cells * blockDim.x consecutive cells of one
 // row; thread t owns cells t, t + blockDim.x, ... (coalesced planes).
-template <typename S, bool ODD, bool STATS, bool EXT>
+template <typename S, bool ODD, bool STATS, bool EXT, bool MASKED = false>
 __global__ void __launch_bounds__(128, RowShape<S>::blocks)
     rowStepKernel(DevLattice L, Planes<S> Pl, Deltas D, StepParams<typename StoreT<S>::R> P, StatsAcc* acc) {
     using R = typename StoreT<S>::R;
     constexpr int NC = RowShape<S>::cells;
+    static_assert(!MASKED || NC == 1, "masked tiles: one cell per thread");
     int x = blockIdx.z + 1, y = blockIdx.y + 1;
     int z0 = blockIdx.x * blockDim.x * NC + threadIdx.x, zEnd = L.nz;
-    if (L.denseTiles) {   // blockDim / kTileCells tiles per block (NC = 1)
+    unsigned gone = 0;
+    const int4* tiles = MASKED ? L.maskedTiles : L.denseTiles;
+    if (tiles) {          // blockDim / kTileCells tiles per block (NC = 1)
         const int r = (blockIdx.y + gridDim.y * blockIdx.z) * (blockDim.x / kTileCells) + threadIdx.x / kTileCells;
         zEnd = -1;        // no cells past the list's end
-        if (r < L.nDense) {
-            const int4 t = L.denseTiles[r];
+        if (r < (MASKED ? L.nMasked : L.nDense)) {
+            const int4 t = tiles[r];
             x = t.x;
             y = t.y;
             z0 = t.z + threadIdx.x % kTileCells;
             zEnd = t.w;
+            if (MASKED) gone = L.tileMasks[(long long)r * kTileCells + threadIdx.x % kTileCells];
         }
     }
     R f[NC][19];
@@ -615,7 +631,8 @@ __global__ void __launch_bounds__(128, RowShape<S>::blocks)
         const int z = z0 + c * blockDim.x;
         kind[c] = K_NONE;
         if (z < zEnd) {
-            RowCell<S, ODD> rc(L, x, y, z);
+            RowCell<S, ODD, MASKED> rc(L, x, y, z);
+            rc.gone = gone;
             kind[c] = L.flags[rc.idx];
             if (kind[c] != K_NONE) rc.load(Pl, D, f[c]);
         }
@@ -625,7 +642,8 @@ __global__ void __launch_bounds__(128, RowShape<S>::blocks)
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
         if (kind[c] == K_NONE) continue;
-        RowCell<S, ODD> rc(L, x, y, z0 + c * blockDim.x);
+        RowCell<S, ODD, MASKED> rc(L, x, y, z0 + c * blockDim.x);
+        rc.gone = gone;
         R rhoBar = R(0), uSqr = R(0);
         if (P.pending && isFace(kind[c])) completeIfFace<R>(L, rc.idx, kind[c], f[c]);
         bool g = collideCell<S, EXT>(L, P, rc.idx, kind[c], f[c], rhoBar, uSqr, acc, STATS);

@@ -36,7 +36,7 @@ struct StepLaunch {
         // through the interior-row kernels, one block per tile, and its other
         // live tiles through the general addressing, which checks each
         // neighbour's kind; without lists every row goes the general way.
-        const bool lists = L.sparse && (L.denseTiles || L.generalTiles);
+        const bool lists = L.sparse && (L.denseTiles || L.generalTiles || L.maskedTiles);
         const bool general = (L.sparse && !lists) || L.nx < 3 || L.ny < 3;
         const int edgeRows = lists ? L.nGeneral : general ? L.nx * L.ny : 2 * L.ny + 2 * (L.nx - 2);
         const long long interiorRows = lists ? L.nDense : (long long)(L.nx - 2) * (L.ny - 2);
@@ -116,6 +116,22 @@ struct StepLaunch {
                 ++launched;
             }
         };
+        // interior-row tiles next to dropped blocks: the one-cell row kernel
+        // with each cell's mask of neighbours outside the lattice
+        auto masked = [&]() {
+            if (!lists || L.nMasked == 0) return;
+            Planes<S> pl;
+            Deltas d;
+            for (int i = 0; i < 19; ++i) {
+                pl.p[i] = static_cast<S*>(L.pop) + (long long)i * L.stride;
+                d.d[i] = cdir(i, 0) * L.ny * L.nz + cdir(i, 1) * L.nz + cdir(i, 2);
+            }
+            const int blocks = (L.nMasked + kBlock / kTileCells - 1) / (kBlock / kTileCells);
+            const unsigned gy = (unsigned)(blocks < 65535 ? blocks : 65535);
+            rowStepKernel<S, ODD, STATS, EXT, true><<<dim3(1u, gy, (unsigned)((blocks + gy - 1) / gy)), kBlock, 0, s>>>(
+                L, pl, d, p, acc);
+            ++launched;
+        };
         auto border = [&]() {
             if (edgeRows == 0) return;
             // rows, or blocks of kBlock / kTileCells tiles of the general-tile list
@@ -130,10 +146,12 @@ struct StepLaunch {
         };
         if (interiorFirst) {
             interior();
+            masked();
             border();
         } else {
             border();
             interior();
+            masked();
         }
         if (es != s) {   // join: the next step waits for both kernels
             if (cudaEventRecord(side->join, es) != cudaSuccess || cudaStreamWaitEvent(s, side->join, 0) != cudaSuccess)

@@ -1,8 +1,9 @@
-"""Sparse domains stepped through tile lists: the tiles (up to 64 cells of a
+"""Sparse domains stepped through tile lists: the tiles (up to 32 cells of a
 row) whose 3x3 neighbourhood of rows lies entirely in kept blocks, one cell
 beyond each end included, take the interior-row kernels (uniform neighbour
-offsets), the other live tiles the general kernel, and cells of dropped blocks
-nothing.
+offsets); the other live tiles of interior rows take the one-cell row kernel
+with each cell's mask of neighbours in dropped blocks; the live tiles of the
+domain's border rows the general kernel; cells of dropped blocks nothing.
 
 The geometry is a voxelized sphere in a box with a body force, flow outside
 the sphere: the blocks deep inside the sphere hold neither fluid nor wall and
