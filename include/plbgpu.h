@@ -83,7 +83,8 @@ typedef struct plbgpu_ctx plbgpu_ctx;
  * one cell per thread for every storage type instead of the paired kernel of
  * the 2-byte forms; "vec8" / "vec4" run eight / four cells per thread with
  * 128- / 64-bit population vectors (2-byte forms, rows of a multiple of eight
- * cells).  All give the same results; the default is the fastest on GB300. */
+ * cells); "vec2" two cells per thread with packed 32-bit population words
+ * (2-byte forms, rows of even length).  All give the same results. */
 int plbgpu_create(int device, plbgpu_ctx** out);
 int plbgpu_destroy(plbgpu_ctx* ctx);
 /* Message of the last failing call on this context ("" if none). */
@@ -145,6 +146,37 @@ int plbgpu_get_kinds(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1
  * next plbgpu_initialize / plbgpu_collide_and_stream as PLBGPU_ERR_ARG. */
 int plbgpu_set_velocity_condition_on_block_boundaries(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0,
                                                       int y1, int z0, int z1);
+
+/* bc->addVelocityBoundary{d}{N|P}(box, lattice), addPressureBoundary{d}{N|P},
+ * addExternalVelocityEdge{plane}{N|P}{N|P} and addExternalVelocityCorner
+ * {N|P}{N|P}{N|P} of the local regularized and Zou/He conditions
+ * (boundaryCondition/boundaryCondition3D.h:58-140, boundaryInstantiator3D.h):
+ * the face, edge or corner `kind` over the box, as plbgpu_define_dynamics,
+ * plus the data-processor record the reference integrates with it (see
+ * plbgpu_add_processor).  plbgpu_set_velocity_condition_on_block_boundaries
+ * records its 26 processors the same way, in the reference's order. */
+int plbgpu_add_boundary(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int y1, int z0, int z1, int kind);
+
+/* The lattice's data-processor list, which every saved lattice state's
+ * description carries (io/multiBlockWriter3D.cpp:113-136: name, domain,
+ * serialized data, level, block ids, indexed by place in the list).  The
+ * GPU's own boundary handling follows the cell kinds; the list is what the
+ * reference lattice built by the same calls would hold.  In `name`, "%TD"
+ * stands for "double_<Descriptor>" of the saved lattice, as the reference
+ * names generators after their template arguments
+ * ("OuterVelocityEdge_%TD_0_-1_1").  plbgpu_load_processors appends the
+ * processors listed in a description that meet the domain, clipped to it,
+ * as readXmlProcessors does for a loaded block
+ * (io/multiBlockReader3D.cpp:91-133).  plbgpu_get_processor fails when a
+ * buffer is too small; nblocks receives the block count either way. */
+int plbgpu_add_processor(plbgpu_ctx* ctx, int handle, const char* name, const long long* domain6,
+                         const char* data, long long level, const long long* blocks, int nblocks);
+int plbgpu_clear_processors(plbgpu_ctx* ctx, int handle);
+int plbgpu_processor_count(plbgpu_ctx* ctx, int handle, int* count);
+int plbgpu_get_processor(plbgpu_ctx* ctx, int handle, int index, char* name, size_t name_cap, long long* domain6,
+                         char* data, size_t data_cap, long long* level, long long* blocks, int blocks_cap,
+                         int* nblocks);
+int plbgpu_load_processors(plbgpu_ctx* ctx, int handle, const char* plb_path);
 
 /* Sparse domain: computeSparseManagement(field) (offLattice/makeSparse3D.hh:
  * 107-160) over the regular distribution createRegularDistribution3D(nx, ny,
@@ -337,8 +369,10 @@ int plbgpu_load_state(plbgpu_ctx* ctx, int handle, int what, const char* plb_pat
  * whose cells need more than the domain holds -- dynamics without a GPU kind,
  * several omegas, rho0s or wall densities, a stored-velocity cell off the
  * domain's edges and corners -- is refused (PLBGPU_ERR_ARG) before anything
- * changes.  Data processors listed in the description are neither written
- * nor read: the domain's own boundary handling follows its kinds. */
+ * changes.  Both lattice saves write the domain's data-processor list
+ * (plbgpu_add_processor) into the description; the loads leave the domain's
+ * list as it is, as the reference's load copies cells only
+ * (io/multiBlockReader3D.cpp:261-268) -- plbgpu_load_processors reads it. */
 int plbgpu_save_state_dynamic(plbgpu_ctx* ctx, int handle, int what, const char* base);
 int plbgpu_load_state_dynamic(plbgpu_ctx* ctx, int handle, int what, const char* plb_path);
 

@@ -97,16 +97,16 @@ public:
     }
     // Wrapped regularized (or Zou/He) face conditions: direction 0/1/2, orientation -1/+1.
     void addVelocityBoundary(const Box& b, int direction, int orientation, bool zouHe = false) {
-        defineDynamics(b, (zouHe ? PLBGPU_ZOUHE_VELOCITY : PLBGPU_REG_VELOCITY) + 2 * direction + (orientation > 0));
+        addBoundary(b, (zouHe ? PLBGPU_ZOUHE_VELOCITY : PLBGPU_REG_VELOCITY) + 2 * direction + (orientation > 0));
     }
     // addExternalVelocityEdge{plane}{N|P}{N|P}: normal1 along (plane+1)%3, normal2 along (plane+2)%3.
     void addExternalVelocityEdge(const Box& b, int plane, int normal1, int normal2) {
-        defineDynamics(b, PLBGPU_VELOCITY_EDGE + 4 * plane + 2 * (normal1 > 0) + (normal2 > 0));
+        addBoundary(b, PLBGPU_VELOCITY_EDGE + 4 * plane + 2 * (normal1 > 0) + (normal2 > 0));
     }
     // addExternalVelocityCorner{N|P}{N|P}{N|P}(x, y, z, lattice).
     void addExternalVelocityCorner(int x, int y, int z, int xNormal, int yNormal, int zNormal) {
-        defineDynamics(Box{x, x, y, y, z, z},
-                       PLBGPU_VELOCITY_CORNER + 4 * (xNormal > 0) + 2 * (yNormal > 0) + (zNormal > 0));
+        addBoundary(Box{x, x, y, y, z, z},
+                    PLBGPU_VELOCITY_CORNER + 4 * (xNormal > 0) + 2 * (yNormal > 0) + (zNormal > 0));
     }
     // bc->setVelocityConditionOnBlockBoundaries(lattice, box): faces, edges and corners.
     void setVelocityConditionOnBlockBoundaries(const Box& b) {
@@ -115,7 +115,18 @@ public:
     }
     void setVelocityConditionOnBlockBoundaries() { setVelocityConditionOnBlockBoundaries(boundingBox()); }
     void addPressureBoundary(const Box& b, int direction, int orientation, bool zouHe = false) {
-        defineDynamics(b, (zouHe ? PLBGPU_ZOUHE_PRESSURE : PLBGPU_REG_PRESSURE) + 2 * direction + (orientation > 0));
+        addBoundary(b, (zouHe ? PLBGPU_ZOUHE_PRESSURE : PLBGPU_REG_PRESSURE) + 2 * direction + (orientation > 0));
+    }
+    // A face, edge or corner kind plus the data-processor record the
+    // reference's boundary instantiator adds with it.
+    void addBoundary(const Box& b, int kind) {
+        ctx_.check(plbgpu_add_boundary(ctx_.get(), h_, b.x0, b.x1, b.y0, b.y1, b.z0, b.z1, kind));
+    }
+    // The lattice's data-processor list as saved states describe it.
+    int processorCount() const {
+        int n = 0;
+        ctx_.check(plbgpu_processor_count(ctx_.get(), h_, &n));
+        return n;
     }
     void setBoundaryVelocity(const Box& b, double ux, double uy, double uz) {
         ctx_.check(plbgpu_set_boundary_velocity(ctx_.get(), h_, b.x0, b.x1, b.y0, b.y1, b.z0, b.z1, ux, uy, uz));

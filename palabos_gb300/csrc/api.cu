@@ -55,6 +55,19 @@ struct ProfRange {
     ProfRange& operator=(const ProfRange&) = delete;
 };
 
+// One entry of the data-processor list a lattice state's description carries
+// (io/multiBlockWriter3D.cpp:113-136): the processor's registered name, its
+// domain, its serialized data, its level and the ids of the blocks it acts
+// on.  In the name, "%TD" stands for "double_<Descriptor>" of the saved
+// lattice (the reference names its generators after their template
+// arguments, e.g. OuterVelocityEdge_double_D3Q19_0_-1_1).
+struct ProcessorRecord {
+    std::string name, data;
+    long long domain[6] = {0, 0, 0, 0, 0, 0};
+    long long level = 0;
+    std::vector<long long> blocks;
+};
+
 struct Domain {
     int nx = 0, ny = 0, nz = 0;
     int precision = PLBGPU_FP64;
@@ -88,6 +101,7 @@ struct Domain {
     unsigned long long deviceBytes = 0;
     void* adjoint = nullptr;              // adjoint checkpoints and buffers (adjoint.cu)
     void (*adjointFree)(void*) = nullptr;
+    std::vector<ProcessorRecord> processors;   // the lattice's data-processor list, in order
 
     DevLattice view() const {
         DevLattice L;
@@ -794,6 +808,7 @@ int plbgpu_create(int device, plbgpu_ctx** out) {
     c->rowForm = !rowKernel                           ? 0
                  : strcmp(rowKernel, "cell") == 0     ? 1
                  : strcmp(rowKernel, "vec4") == 0     ? 2
+                 : strcmp(rowKernel, "vec2") == 0     ? 3
                  : strcmp(rowKernel, "vec8") == 0     ? 4
                                                       : 0;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -958,6 +973,115 @@ int plbgpu_set_params(plbgpu_ctx* c, int h, double omega, double rho0, double bb
     return PLBGPU_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// The data-processor record that the reference's boundary-condition
+// instantiator integrates beside a face, edge or corner kind over a box
+// (boundaryCondition/boundaryInstantiator3D.h): the wrapped local boundary
+// functional of a face (regularized and Zou/He alike), the finite-difference
+// processor of an external velocity edge or corner; data "dxScale dtScale "
+// of a functional with the default scales (atomicBlock/
+// dataProcessingFunctional3D.cpp:62-65), level 0, acting on block 0 (the
+// lattice's global id in the saved description).
+ProcessorRecord boundaryRecord(int kind, const Box& b) {
+    ProcessorRecord r;
+    if (isFace(kind)) {
+        r.name = "WrappedLocalBoundary3D_%TD";
+    } else if (kind >= K_EDGE && kind < K_CORNER) {
+        const int e = kind - K_EDGE, plane = e / 4, n1 = (e & 2) ? 1 : -1, n2 = (e & 1) ? 1 : -1;
+        r.name = "OuterVelocityEdge_%TD_" + std::to_string(plane) + "_" + std::to_string(n1) + "_" + std::to_string(n2);
+    } else {
+        const int e = kind - K_CORNER;
+        r.name = std::string("OuterVelocityCorner3D_%TD_") + ((e & 4) ? "1" : "-1") + "_" + ((e & 2) ? "1" : "-1") +
+                 "_" + ((e & 1) ? "1" : "-1");
+    }
+    r.data = "0 0 ";
+    const long long dom[6] = {b.x0, b.x1, b.y0, b.y1, b.z0, b.z1};
+    std::copy(dom, dom + 6, r.domain);
+    r.blocks = {0};
+    return r;
+}
+
+}  // namespace
+
+extern "C" {
+
+int plbgpu_add_boundary(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, int kind) {
+    Domain* d;
+    Box b;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if ((rc = checkBox(c, d, x0, x1, y0, y1, z0, z1, &b))) return rc;
+    if (!isFace(kind) && !isSurface(kind))
+        return fail(c, PLBGPU_ERR_ARG, "kind %d is not a face, edge or corner kind", kind);
+    if ((rc = plbgpu_define_dynamics(c, h, x0, x1, y0, y1, z0, z1, kind))) return rc;
+    d->processors.push_back(boundaryRecord(kind, b));
+    return PLBGPU_OK;
+}
+
+int plbgpu_add_processor(plbgpu_ctx* c, int h, const char* name, const long long* domain, const char* data,
+                         long long level, const long long* blocks, int nblocks) {
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if (!name || !*name || !domain || !data || nblocks < 0 || (nblocks > 0 && !blocks))
+        return fail(c, PLBGPU_ERR_ARG, "processor record: null name, domain, data or blocks");
+    for (const char* p = name; *p; ++p)
+        if (*p == '<' || *p == '>' || *p == ' ' || *p == '\n')
+            return fail(c, PLBGPU_ERR_ARG, "processor name '%s' is not an XML tag text", name);
+    if (strchr(data, '<') || strchr(data, '>'))
+        return fail(c, PLBGPU_ERR_ARG, "processor data may not hold '<' or '>'");
+    ProcessorRecord r;
+    r.name = name;
+    r.data = data;
+    std::copy(domain, domain + 6, r.domain);
+    r.level = level;
+    r.blocks.assign(blocks, blocks + nblocks);
+    d->processors.push_back(r);
+    return PLBGPU_OK;
+}
+
+int plbgpu_clear_processors(plbgpu_ctx* c, int h) {
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    d->processors.clear();
+    return PLBGPU_OK;
+}
+
+int plbgpu_processor_count(plbgpu_ctx* c, int h, int* count) {
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if (!count) return fail(c, PLBGPU_ERR_ARG, "null count");
+    *count = (int)d->processors.size();
+    return PLBGPU_OK;
+}
+
+int plbgpu_get_processor(plbgpu_ctx* c, int h, int i, char* name, size_t nameCap, long long* domain, char* data,
+                         size_t dataCap, long long* level, long long* blocks, int blocksCap, int* nblocks) {
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if (i < 0 || i >= (int)d->processors.size())
+        return fail(c, PLBGPU_ERR_ARG, "processor %d of %zu", i, d->processors.size());
+    const ProcessorRecord& r = d->processors[(size_t)i];
+    if (!name || nameCap <= r.name.size() || !data || dataCap <= r.data.size())
+        return fail(c, PLBGPU_ERR_ARG, "processor %d: name needs %zu bytes, data %zu", i, r.name.size() + 1,
+                    r.data.size() + 1);
+    if (nblocks) *nblocks = (int)r.blocks.size();
+    if ((int)r.blocks.size() > blocksCap || (!blocks && !r.blocks.empty()))
+        return fail(c, PLBGPU_ERR_ARG, "processor %d acts on %zu blocks", i, r.blocks.size());
+    memcpy(name, r.name.c_str(), r.name.size() + 1);
+    memcpy(data, r.data.c_str(), r.data.size() + 1);
+    if (domain) std::copy(r.domain, r.domain + 6, domain);
+    if (level) *level = r.level;
+    if (!r.blocks.empty()) std::copy(r.blocks.begin(), r.blocks.end(), blocks);
+    return PLBGPU_OK;
+}
+
 int plbgpu_define_dynamics(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, int kind) {
     Domain* d;
     Box b;
@@ -1030,7 +1154,37 @@ int plbgpu_set_velocity_condition_on_block_boundaries(plbgpu_ctx* c, int h, int 
                 }
                 kinds[o] = (uint8_t)k;
             }
-    return plbgpu_set_kinds(c, h, x0, x1, y0, y1, z0, z1, kinds.data(), kinds.size());
+    if ((rc = plbgpu_set_kinds(c, h, x0, x1, y0, y1, z0, z1, kinds.data(), kinds.size()))) return rc;
+    // the processors the reference integrates, in its order: six faces, twelve
+    // edges (plane 0, 1, 2; normals NN, NP, PN, PP), eight corners (x, y, z
+    // sides N before P, x slowest) (boundaryCondition/boundaryCondition3D.hh:65-163)
+    auto piece = [&](int kind, const int (&side)[3]) {   // side: -1 low, +1 high, 0 the inner extent
+        int l[3], u[3];
+        for (int a = 0; a < 3; ++a) {
+            l[a] = side[a] < 0 ? lo[a] : side[a] > 0 ? hi[a] : lo[a] + 1;
+            u[a] = side[a] < 0 ? lo[a] : side[a] > 0 ? hi[a] : hi[a] - 1;
+        }
+        d->processors.push_back(boundaryRecord(kind, Box{l[0], u[0], l[1], u[1], l[2], u[2]}));
+    };
+    for (int a = 0; a < 3; ++a)
+        for (int o = -1; o <= 1; o += 2) {
+            int side[3] = {0, 0, 0};
+            side[a] = o;
+            piece(K_REGVEL + 2 * a + (o > 0), side);
+        }
+    for (int plane = 0; plane < 3; ++plane)
+        for (int n1 = -1; n1 <= 1; n1 += 2)
+            for (int n2 = -1; n2 <= 1; n2 += 2) {
+                int side[3] = {0, 0, 0};
+                side[(plane + 1) % 3] = n1;
+                side[(plane + 2) % 3] = n2;
+                piece(K_EDGE + 4 * plane + 2 * (n1 > 0) + (n2 > 0), side);
+            }
+    for (int e = 0; e < 8; ++e) {
+        const int side[3] = {(e & 4) ? 1 : -1, (e & 2) ? 1 : -1, (e & 1) ? 1 : -1};
+        piece(K_CORNER + e, side);
+    }
+    return PLBGPU_OK;
 }
 
 int plbgpu_select_sparse_blocks(plbgpu_ctx* c, int h, const int32_t* field, size_t n, int bx, int by, int bz,
@@ -1877,6 +2031,8 @@ namespace {
 
 // Family, descriptor and cell size of a block kind as parallelIO::save
 // describes it (io/multiBlockWriter3D.cpp:53-137).
+bool isLatticeBlock(int what) { return what == PLBGPU_BLOCK_LATTICE || what == PLBGPU_BLOCK_FORCED_LATTICE; }
+
 void stateTypeInfo(int what, const char** family, const char** descriptor) {
     switch (what) {
     case PLBGPU_BLOCK_LATTICE: *family = "BlockLattice3D"; *descriptor = "D3Q19"; return;
@@ -1924,6 +2080,8 @@ bool parseLongs(const std::string& text, std::vector<long long>& out) {
 // libraryInterfaces/TINYXML_xmlIO.hh:229-272).  dict: the DynamicsDict of a
 // state with dynamic content (name -> id, in name order), null for static
 // content.
+std::string processorList(const Domain* d, const char* descriptor);
+
 std::string stateDescription(const Domain* d, int what, const std::string& datName, unsigned long long bytes,
                              const std::map<std::string, int>* dict) {
     const int w = blockWidth(what);
@@ -1950,7 +2108,38 @@ std::string stateDescription(const Domain* d, int what, const std::string& datNa
         for (const auto& e : *dict) x += "            <" + e.first + "> " + std::to_string(e.second) + " </" + e.first + ">\n";
         x += "        </DynamicsDict>\n";
     }
+    if (isLatticeBlock(what)) x += processorList(d, descriptor);
     x += "    </Data>\n</Block3D>\n";
+    return x;
+}
+
+// The <Processor> entries of a lattice description, indexed by their place
+// in the list (io/multiBlockWriter3D.cpp:113-136), as the reference's XML
+// writer prints an indexed element (libraryInterfaces/TINYXML_xmlIO.hh:
+// 229-272): the id attribute unless the list is one entry, and each value
+// between single spaces.
+std::string processorList(const Domain* d, const char* descriptor) {
+    // a leaf element: the text between single spaces, nothing when empty
+    auto leaf = [](const char* tag, const std::string& text) {
+        return std::string("            <") + tag + ">" + (text.empty() ? "" : " " + text + " ") + "</" + tag + ">\n";
+    };
+    auto joined = [](const long long* v, size_t n) {
+        std::string t;
+        for (size_t i = 0; i < n; ++i) t += (i ? " " : "") + std::to_string(v[i]);
+        return t;
+    };
+    std::string x;
+    const bool ids = d->processors.size() > 1;
+    const std::string td = std::string("double_") + descriptor;
+    for (size_t i = 0; i < d->processors.size(); ++i) {
+        const ProcessorRecord& r = d->processors[i];
+        std::string name = r.name;
+        for (size_t p; (p = name.find("%TD")) != std::string::npos;) name.replace(p, 3, td);
+        x += ids ? "        <Processor id=\"" + std::to_string(i) + "\">\n" : std::string("        <Processor>\n");
+        x += leaf("Name", name) + leaf("Domain", joined(r.domain, 6)) + leaf("Data", r.data) +
+             leaf("Level", std::to_string(r.level)) + leaf("Blocks", joined(r.blocks.data(), r.blocks.size()));
+        x += "        </Processor>\n";
+    }
     return x;
 }
 
@@ -2148,7 +2337,6 @@ int uploadRecords(plbgpu_ctx* c, Domain* d, int what, const Box& cb, const std::
     return PLBGPU_OK;
 }
 
-bool isLatticeBlock(int what) { return what == PLBGPU_BLOCK_LATTICE || what == PLBGPU_BLOCK_FORCED_LATTICE; }
 
 }  // namespace
 
@@ -2286,6 +2474,80 @@ int plbgpu_save_state_dynamic(plbgpu_ctx* c, int h, int what, const char* base) 
     if (!fp.f) return fail(c, PLBGPU_ERR_ARG, "cannot open %s for writing", plbName.c_str());
     if (fwrite(x.data(), 1, x.size(), fp.f) != x.size() || fflush(fp.f) != 0)
         return fail(c, PLBGPU_ERR_ARG, "write to %s failed", plbName.c_str());
+    return PLBGPU_OK;
+}
+
+int plbgpu_load_processors(plbgpu_ctx* c, int h, const char* plb) {
+    ProfRange prof("io");
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if (!plb) return fail(c, PLBGPU_ERR_ARG, "null path");
+    std::string doc;
+    {
+        FileCloser fc{fopen(plb, "rb")};
+        if (!fc.f) return fail(c, PLBGPU_ERR_ARG, "cannot open %s", plb);
+        char chunk[4096];
+        size_t got;
+        while ((got = fread(chunk, 1, sizeof(chunk), fc.f)) > 0) doc.append(chunk, got);
+    }
+    auto trim = [](const std::string& t) {
+        const size_t a = t.find_first_not_of(" \n\t\r"), b = t.find_last_not_of(" \n\t\r");
+        return a == std::string::npos ? std::string() : t.substr(a, b - a + 1);
+    };
+    std::string t;
+    std::vector<long long> bb, v;
+    if (xmlElement(doc, "BoundingBox", 0, t, nullptr) == std::string::npos || !parseLongs(t, bb) || bb.size() != 6)
+        return fail(c, PLBGPU_ERR_ARG, "%s: no bounding box", plb);
+    std::string descriptor;
+    if (xmlElement(doc, "Descriptor", 0, t, nullptr) != std::string::npos) descriptor = trim(t);
+    const std::string td = "double_" + descriptor;
+    std::vector<ProcessorRecord> add;
+    size_t pos = 0, next = 0;
+    while (xmlElement(doc, "Processor", pos, t, &next) != std::string::npos) {
+        pos = next;
+        ProcessorRecord r;
+        std::string f;
+        if (xmlElement(t, "Name", 0, f, nullptr) == std::string::npos || trim(f).empty())
+            return fail(c, PLBGPU_ERR_ARG, "%s: processor without a name", plb);
+        r.name = trim(f);
+        if (!descriptor.empty())
+            for (size_t p = 0; (p = r.name.find(td, p)) != std::string::npos;) {
+                const size_t e = p + td.size();
+                if (p > 0 && r.name[p - 1] == '_' && (e == r.name.size() || r.name[e] == '_')) {
+                    r.name.replace(p, td.size(), "%TD");
+                    p += 3;
+                } else {
+                    p = e;
+                }
+            }
+        // the writer puts one space on either side of a non-empty text
+        if (xmlElement(t, "Data", 0, f, nullptr) == std::string::npos)
+            return fail(c, PLBGPU_ERR_ARG, "%s: processor %s without data", plb, r.name.c_str());
+        r.data = f.size() >= 2 && f.front() == ' ' && f.back() == ' ' ? f.substr(1, f.size() - 2) : f;
+        if (xmlElement(t, "Domain", 0, f, nullptr) == std::string::npos || !parseLongs(f, v) || v.size() != 6)
+            return fail(c, PLBGPU_ERR_ARG, "%s: processor %s without a domain", plb, r.name.c_str());
+        // readXmlProcessors keeps the processors that meet the block, clipped
+        // to it (io/multiBlockReader3D.cpp:91-133); coordinates relative to
+        // the bounding box, whose origin is the domain's
+        const int ext[3] = {d->nx, d->ny, d->nz};
+        bool meets = true;
+        for (int a = 0; a < 3; ++a) {
+            long long l = v[2 * a] - bb[2 * a], u = v[2 * a + 1] - bb[2 * a];
+            l = l < 0 ? 0 : l;
+            u = u > ext[a] - 1 ? ext[a] - 1 : u;
+            meets = meets && l <= u;
+            r.domain[2 * a] = l;
+            r.domain[2 * a + 1] = u;
+        }
+        if (xmlElement(t, "Level", 0, f, nullptr) == std::string::npos || !parseLongs(f, v) || v.size() != 1)
+            return fail(c, PLBGPU_ERR_ARG, "%s: processor %s without a level", plb, r.name.c_str());
+        r.level = v[0];
+        if (xmlElement(t, "Blocks", 0, f, nullptr) == std::string::npos || !parseLongs(f, r.blocks))
+            return fail(c, PLBGPU_ERR_ARG, "%s: processor %s without blocks", plb, r.name.c_str());
+        if (meets) add.push_back(r);
+    }
+    d->processors.insert(d->processors.end(), add.begin(), add.end());
     return PLBGPU_OK;
 }
 

@@ -154,7 +154,8 @@ struct DevLattice {
     unsigned* status;       // device error word (kStatusNonFinite)
     int rowForm;            // interior-row kernel: 0 the default (two cells per thread for the 2-byte
                             // forms), 1 one cell per thread (every form), 2 / 4 four / eight cells per
-                            // thread with 64- / 128-bit vectors (2-byte forms, rows of 8k cells)
+                            // thread with 64- / 128-bit vectors (2-byte forms, rows of 8k cells), 3 two
+                            // cells per thread with packed 32-bit words (2-byte forms, rows of 2k cells)
     // Sparse domains: tiles (x, y, z0, z1) of at most kTileCells cells of a
     // row.  Dense tiles -- the 3x3 rows around them hold no cell outside the
     // lattice from z0 - 1 to z1 -- take the interior-row kernels; the other

@@ -19,12 +19,17 @@ struct StepLaunch {
     // Two cells per thread: the fastest form of the 2-byte storage types on
     // GB300 (rows of even length).
     static bool pairedRows(const DevLattice& L) { return sizeof(S) == 2 && L.nz % 2 == 0 && L.rowForm != 1; }
-    // Eight (or four) cells per thread, 128-bit (64-bit) population vectors
-    // (vecrow.cuh), on request: bit-identical, but 34-43% slower than the
-    // paired kernel on GB300 (the packed state of eight cells holds 168
-    // registers, 12 resident warps per SM, too few to keep HBM busy).
-    static bool vectorRows(const DevLattice& L) {
-        return sizeof(S) == 2 && L.nz % 8 == 0 && (L.rowForm == 4 || L.rowForm == 2);
+    // Eight, four or two cells per thread with packed 128-, 64- or 32-bit
+    // population words (vecrow.cuh), on request: bit-identical.  Eight and
+    // four cells are 34-43% slower than the paired kernel on GB300 (the packed
+    // state of eight cells holds 168 registers, 12 resident warps per SM, too
+    // few to keep HBM busy).
+    static int vectorCells(const DevLattice& L) {
+        if (sizeof(S) != 2) return 0;
+        if (L.rowForm == 4 && L.nz % 8 == 0) return 8;
+        if (L.rowForm == 2 && L.nz % 8 == 0) return 4;
+        if (L.rowForm == 3 && L.nz % 2 == 0) return 2;
+        return 0;
     }
 
     template <bool ODD, bool STATS, bool EXT>
@@ -63,7 +68,7 @@ struct StepLaunch {
             es = side->stream;
         auto interior = [&]() {
             if (general || interiorRows == 0) return;
-            if (vectorRows(L)) {
+            if (const int cpt = vectorCells(L)) {
                 if constexpr (sizeof(S) == 2) {
                     Planes<S> pl;
                     RowDeltas d;
@@ -71,7 +76,11 @@ struct StepLaunch {
                         pl.p[i] = static_cast<S*>(L.pop) + (long long)i * L.stride;
                         d.d[i] = cdir(i, 0) * L.ny * L.nz + cdir(i, 1) * L.nz;
                     }
-                    if (L.rowForm == 2) {   // four cells per thread, 8-byte vectors
+                    if (cpt == 2) {         // two cells per thread, 4-byte words
+                        const long long segs = interiorRows * (lists ? kTileCells / 2 : L.nz / 2);
+                        const unsigned blocks = (unsigned)((segs + kBlock - 1) / kBlock);
+                        vecRowStepKernel<S, ODD, STATS, EXT, 2><<<blocks, kBlock, 0, s>>>(L, pl, d, p, acc, segs);
+                    } else if (cpt == 4) {  // four cells per thread, 8-byte vectors
                         const long long segs = interiorRows * (lists ? kTileCells / 4 : L.nz / 4);
                         const unsigned blocks = (unsigned)((segs + kBlock - 1) / kBlock);
                         vecRowStepKernel<S, ODD, STATS, EXT, 4><<<blocks, kBlock, 0, s>>>(L, pl, d, p, acc, segs);
@@ -117,7 +126,8 @@ struct StepLaunch {
             }
         };
         // interior-row tiles next to dropped blocks: the one-cell row kernel
-        // with each cell's mask of neighbours outside the lattice
+        // with each cell's mask of neighbours outside the lattice, on the
+        // border stream beside the interior kernel
         auto masked = [&]() {
             if (!lists || L.nMasked == 0) return;
             Planes<S> pl;
@@ -128,7 +138,7 @@ struct StepLaunch {
             }
             const int blocks = (L.nMasked + kBlock / kTileCells - 1) / (kBlock / kTileCells);
             const unsigned gy = (unsigned)(blocks < 65535 ? blocks : 65535);
-            rowStepKernel<S, ODD, STATS, EXT, true><<<dim3(1u, gy, (unsigned)((blocks + gy - 1) / gy)), kBlock, 0, s>>>(
+            rowStepKernel<S, ODD, STATS, EXT, true><<<dim3(1u, gy, (unsigned)((blocks + gy - 1) / gy)), kBlock, 0, es>>>(
                 L, pl, d, p, acc);
             ++launched;
         };

@@ -1,12 +1,14 @@
 // Interior-row step kernel of the 2-byte storage forms (BF16, BF16 with
-// stochastic rounding, FP16): eight consecutive cells of a row per thread,
-// every population read and written as one aligned 128-bit vector.
+// stochastic rounding, FP16): CPT = 2, 4 or 8 consecutive cells of a row per
+// thread, every population read and written as one aligned 32-, 64- or
+// 128-bit word, the populations of all CPT cells held packed (one register
+// per two cells and population) while the cells collide one after another.
 //
 // Rows with 1 <= x <= nx-2 and 1 <= y <= ny-2 of a dense domain whose rows
-// hold a multiple of eight cells (nz % 8 == 0; planes start on 256-byte
-// boundaries, so every eight-cell segment of a plane row is one aligned
-// 16-byte vector).  Thread g owns segment g % (nz/8) of interior row
-// g / (nz/8): cells z0..z0+7, z0 = 8 * segment.
+// hold a multiple of CPT cells (planes start on 256-byte boundaries, so every
+// CPT-cell segment of a plane row is one aligned vector).  Thread g owns
+// segment g % (nz/CPT) of interior row g / (nz/CPT): cells z0..z0+CPT-1,
+// z0 = CPT * segment.
 //
 // Even AA step: the 19 vectors of the thread's own cells are loaded, each
 // cell collides, and population i goes back into slot opp(i) of the same
@@ -23,7 +25,7 @@
 // on a non-periodic z axis -- the reference's domain-edge rule (a population
 // that would leave the domain stays in its cell, reversed: slot i of the own
 // cell).  Stores mirror this: a lane whose vector needs an element from a lane
-// it cannot shuffle with writes the other seven elements with 16-, 32- and
+// it cannot shuffle with writes its other CPT - 1 elements with 16-, 32- and
 // 64-bit stores, and the element's owner writes it with a 16-bit store.
 //
 // Every slot is still read and written by one thread only: an element a
@@ -68,8 +70,8 @@ template <> struct Half16<bf16sr> {
     }
 };
 
-// NW 32-bit words of 16-bit values (NW = 2: eight bytes, NW = 4: sixteen),
-// element e in word e / 2, low half first.
+// NW 32-bit words of 16-bit values (NW = 1, 2 or 4: four, eight or sixteen
+// bytes), element e in word e / 2, low half first.
 template <int NW>
 struct Words {
     unsigned w[NW];
@@ -82,8 +84,10 @@ __device__ __forceinline__ Words<NW> ldWords(const void* p) {
         asm volatile("ld.global.v4.u32 {%0, %1, %2, %3}, [%4];"
                      : "=r"(v.w[0]), "=r"(v.w[1]), "=r"(v.w[2]), "=r"(v.w[3])
                      : "l"(p));
-    else
+    else if constexpr (NW == 2)
         asm volatile("ld.global.v2.u32 {%0, %1}, [%2];" : "=r"(v.w[0]), "=r"(v.w[1]) : "l"(p));
+    else   // a warp reads 128 bytes of a plane: the L2 prefetches the 256-byte segment
+        v.w[0] = ldPair256(p);
     return v;
 }
 template <int NW>
@@ -92,8 +96,10 @@ __device__ __forceinline__ void stWords(void* p, const Words<NW>& v) {
         asm volatile("st.global.v4.u32 [%0], {%1, %2, %3, %4};" ::"l"(p), "r"(v.w[0]), "r"(v.w[1]), "r"(v.w[2]),
                      "r"(v.w[3])
                      : "memory");
-    else
+    else if constexpr (NW == 2)
         asm volatile("st.global.v2.u32 [%0], {%1, %2};" ::"l"(p), "r"(v.w[0]), "r"(v.w[1]) : "memory");
+    else
+        asm volatile("st.global.u32 [%0], %1;" ::"l"(p), "r"(v.w[0]) : "memory");
 }
 __device__ __forceinline__ unsigned ld16(const void* p) {
     unsigned short u;
@@ -136,10 +142,11 @@ struct RowDeltas {
 
 // Cells per thread and residency of the vector kernel: CPT = 8 moves 16-byte
 // vectors (19 of them held as 76 registers of packed values), CPT = 4 moves
-// 8-byte vectors with half the registers and more resident warps.
+// 8-byte vectors with half the registers and more resident warps, CPT = 2
+// 4-byte words (19 registers of packed values, 64 registers a thread).
 template <int CPT>
 struct VecShape {
-    static constexpr int blocks = CPT == 8 ? 3 : 5;
+    static constexpr int blocks = CPT == 8 ? 3 : CPT == 4 ? 5 : 8;
 };
 
 template <typename S, bool ODD, bool STATS, bool EXT, int CPT>
@@ -219,8 +226,11 @@ __global__ void __launch_bounds__(128, VecShape<CPT>::blocks)
         const uint2 t = *reinterpret_cast<const uint2*>(L.flags + idx0);
         kk[0] = t.x;
         kk[1] = t.y;
-    } else {
+    } else if constexpr (NW == 2) {
         kk[0] = *reinterpret_cast<const unsigned*>(L.flags + idx0);
+        kk[1] = 0u;
+    } else {
+        kk[0] = *reinterpret_cast<const unsigned short*>(L.flags + idx0);
         kk[1] = 0u;
     }
 
@@ -270,7 +280,7 @@ __global__ void __launch_bounds__(128, VecShape<CPT>::blocks)
                         stWords<NW>(dst + d0, shiftUp<NW>(a, prev));
                     } else {                        // position z0 is written by its owner
                         st16(dst + (d0 + 1), a.w[0]);
-                        st32(dst + (d0 + 2), __byte_perm(a.w[0], a.w[1], 0x5432));
+                        if constexpr (NW >= 2) st32(dst + (d0 + 2), __byte_perm(a.w[0], a.w[1], 0x5432));
                         if constexpr (NW == 4)
                             st64(dst + (d0 + 4), __byte_perm(a.w[1], a.w[2], 0x5432),
                                  __byte_perm(a.w[2], a.w[3], 0x5432));
@@ -289,7 +299,7 @@ __global__ void __launch_bounds__(128, VecShape<CPT>::blocks)
                         if constexpr (NW == 4) {
                             st64(dst + d0, __byte_perm(a.w[0], a.w[1], 0x5432), __byte_perm(a.w[1], a.w[2], 0x5432));
                             st32(dst + (d0 + 4), __byte_perm(a.w[2], a.w[3], 0x5432));
-                        } else {
+                        } else if constexpr (NW == 2) {
                             st32(dst + d0, __byte_perm(a.w[0], a.w[1], 0x5432));
                         }
                         st16(dst + (d0 + CPT - 2), a.w[NW - 1] >> 16);

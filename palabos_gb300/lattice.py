@@ -132,19 +132,24 @@ class DeviceLattice3D:
                                               out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), out.size))
         return out.reshape(box[1] - box[0] + 1, box[3] - box[2] + 1, box[5] - box[4] + 1)
 
+    def add_boundary(self, box, kind):
+        """A face, edge or corner kind over the box plus the data-processor
+        record the reference's boundary instantiator integrates with it."""
+        self._check(self.lib.plbgpu_add_boundary(self.ctx.h, self.handle, *self._box(box), int(kind)))
+
     def add_velocity_boundary(self, box, direction, orientation, zou_he=False):
         fam = N.ZOUHE_VELOCITY if zou_he else N.REG_VELOCITY
-        self.define_dynamics(box, N.face_kind(fam, direction, orientation))
+        self.add_boundary(box, N.face_kind(fam, direction, orientation))
 
     def add_external_velocity_edge(self, box, plane, normal1, normal2):
         """addExternalVelocityEdge{plane}{N|P}{N|P}(box, lattice) of the local
         regularized condition: finished after every step (and by
         initialize()) by the finite-difference edge processor."""
-        self.define_dynamics(box, N.edge_kind(plane, normal1, normal2))
+        self.add_boundary(box, N.edge_kind(plane, normal1, normal2))
 
     def add_external_velocity_corner(self, x, y, z, x_normal, y_normal, z_normal):
         """addExternalVelocityCorner{N|P}{N|P}{N|P}(x, y, z, lattice)."""
-        self.define_dynamics((x, x, y, y, z, z), N.corner_kind(x_normal, y_normal, z_normal))
+        self.add_boundary((x, x, y, y, z, z), N.corner_kind(x_normal, y_normal, z_normal))
 
     def set_velocity_condition_on_block_boundaries(self, box=None):
         """setVelocityConditionOnBlockBoundaries(lattice, box): regularized
@@ -154,7 +159,36 @@ class DeviceLattice3D:
 
     def add_pressure_boundary(self, box, direction, orientation, zou_he=False):
         fam = N.ZOUHE_PRESSURE if zou_he else N.REG_PRESSURE
-        self.define_dynamics(box, N.face_kind(fam, direction, orientation))
+        self.add_boundary(box, N.face_kind(fam, direction, orientation))
+
+    def processors(self):
+        """The data-processor list saved lattice states describe: dicts of
+        name ("%TD" for double_<Descriptor>), domain, data, level, blocks."""
+        n = ctypes.c_int(0)
+        self._check(self.lib.plbgpu_processor_count(self.ctx.h, self.handle, ctypes.byref(n)))
+        out = []
+        for i in range(n.value):
+            name, data = ctypes.create_string_buffer(1024), ctypes.create_string_buffer(4096)
+            dom, level, nb = (ctypes.c_longlong * 6)(), ctypes.c_longlong(0), ctypes.c_int(0)
+            blocks = (ctypes.c_longlong * 64)()
+            self._check(self.lib.plbgpu_get_processor(self.ctx.h, self.handle, i, name, 1024, dom, data, 4096,
+                                                      ctypes.byref(level), blocks, 64, ctypes.byref(nb)))
+            out.append({"name": name.value.decode(), "domain": tuple(dom), "data": data.value.decode(),
+                        "level": level.value, "blocks": tuple(blocks[:nb.value])})
+        return out
+
+    def add_processor(self, name, domain, data="0 0 ", level=0, blocks=(0,)):
+        dom = (ctypes.c_longlong * 6)(*[int(v) for v in domain])
+        bl = (ctypes.c_longlong * max(1, len(blocks)))(*[int(v) for v in blocks])
+        self._check(self.lib.plbgpu_add_processor(self.ctx.h, self.handle, name.encode(), dom, data.encode(),
+                                                  int(level), bl, len(blocks)))
+
+    def clear_processors(self):
+        self._check(self.lib.plbgpu_clear_processors(self.ctx.h, self.handle))
+
+    def load_processors(self, plb_path):
+        """readXmlProcessors: append the processors a saved description lists."""
+        self._check(self.lib.plbgpu_load_processors(self.ctx.h, self.handle, str(plb_path).encode()))
 
     def set_boundary_velocity(self, box, u):
         box = self._box(box)

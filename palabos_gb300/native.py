@@ -77,6 +77,14 @@ SIGNATURES = {
     "plbgpu_set_kinds": [_vp, _i, *BOX, _c_u8_p, _sz],
     "plbgpu_get_kinds": [_vp, _i, *BOX, _c_u8_p, _sz],
     "plbgpu_set_velocity_condition_on_block_boundaries": [_vp, _i, *BOX],
+    "plbgpu_add_boundary": [_vp, _i, *BOX, _i],
+    "plbgpu_add_processor": [_vp, _i, ctypes.c_char_p, ctypes.POINTER(_l), ctypes.c_char_p, _l,
+                             ctypes.POINTER(_l), _i],
+    "plbgpu_clear_processors": [_vp, _i],
+    "plbgpu_processor_count": [_vp, _i, _c_int_p],
+    "plbgpu_get_processor": [_vp, _i, _i, ctypes.c_char_p, _sz, ctypes.POINTER(_l), ctypes.c_char_p, _sz,
+                             ctypes.POINTER(_l), ctypes.POINTER(_l), _i, _c_int_p],
+    "plbgpu_load_processors": [_vp, _i, ctypes.c_char_p],
     "plbgpu_compute_rhobar_j": [_vp, _i],
     "plbgpu_set_rhobar_j": [_vp, _i, *BOX, _c_dbl_p, _sz],
     "plbgpu_get_rhobar_j": [_vp, _i, *BOX, _c_dbl_p, _sz],

@@ -1,14 +1,16 @@
 """The interior-row kernels of the 2-byte storage forms against the one-cell
 kernel (PLBGPU_ROW_KERNEL=cell), bit for bit: the default paired kernel (two
 cells per thread) and the vector kernels (palabos_gb300/csrc/vecrow.cuh:
-eight or four cells per thread, 128- or 64-bit population vectors).
+eight, four or two cells per thread, 128-, 64- or 32-bit population words).
 
 All run the same FP32 collision on the same stored values, so every stored
 population must be identical; the cases reach every path of the vector
 kernels' streaming:
 
   rows of 1, 2, 12 and 64 eight-cell segments (a whole row in one lane, rows
-  inside a warp, rows straddling warp boundaries, rows spanning two warps);
+  inside a warp, rows straddling warp boundaries, rows spanning two warps) and
+  of 1 and 33 two-cell segments (rows whose length is no multiple of eight,
+  which only the two-cell vector kernel and the paired kernel take);
   periodic and non-periodic z (the wrap and the domain-edge reflection at the
   row ends); bounce-back, momentum exchange, Guo force, regularized and
   Zou/He faces inside interior rows (pending face completion); both AA
@@ -27,8 +29,8 @@ pytestmark = pytest.mark.gpu
 
 
 def _context(form):
-    """A context whose interior rows run `form` ("cell", "vec8", "vec4" or
-    "default")."""
+    """A context whose interior rows run `form` ("cell", "vec8", "vec4",
+    "vec2" or "default")."""
     old = os.environ.get("PLBGPU_ROW_KERNEL")
     if form != "default":
         os.environ["PLBGPU_ROW_KERNEL"] = form
@@ -102,6 +104,8 @@ CASES = {
     "periodic_rows_of_12_segments": lambda: _periodic((7, 6, 96), 12),
     "walled_z_rows_of_1_segment": lambda: _walled_z((9, 7, 8), 13),
     "walled_z_rows_of_12_segments": lambda: _walled_z((6, 7, 96), 14),
+    "periodic_rows_of_1_pair": lambda: _periodic((6, 5, 2), 21),
+    "walled_z_rows_of_33_pairs": lambda: _walled_z((6, 7, 66), 22),
     "regularized_velocity_faces_in_rows": lambda: _faces_z((8, 7, 24), 15, N.REG_VELOCITY),
     "zouhe_pressure_faces_in_rows": lambda: _faces_z((8, 7, 40), 16, N.ZOUHE_PRESSURE),
     "cavity_lid_in_rows": lambda: _cavity((10, 9, 96), 17),
@@ -130,7 +134,7 @@ def _run(case, precision, form, steps, external=False):
 
 
 @pytest.mark.parametrize("precision", ["bf16", "fp16"])
-@pytest.mark.parametrize("form", ["default", "vec8", "vec4"])
+@pytest.mark.parametrize("form", ["default", "vec8", "vec4", "vec2"])
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_row_kernels_equal_one_cell_rows(name, form, precision):
     case = CASES[name]()
@@ -147,7 +151,7 @@ def test_row_kernels_equal_one_cell_rows(name, form, precision):
 
 
 @pytest.mark.parametrize("precision", ["bf16", "fp16"])
-@pytest.mark.parametrize("form", ["default", "vec8", "vec4"])
+@pytest.mark.parametrize("form", ["default", "vec8", "vec4", "vec2"])
 def test_row_kernels_external_form_equal_one_cell_rows(form, precision):
     case = _periodic((8, 6, 64), 19)
     f_vec, _ = _run(case, precision, form, 7, external=True)
@@ -155,7 +159,7 @@ def test_row_kernels_external_form_equal_one_cell_rows(form, precision):
     assert np.array_equal(f_vec, f_cell)
 
 
-@pytest.mark.parametrize("form", ["default", "vec8"])
+@pytest.mark.parametrize("form", ["default", "vec8", "vec2"])
 def test_row_kernels_stochastic_rounding_track_one_cell_rows(form):
     """BF16 with stochastic rounding draws its random bits from different
     addresses in the kernels, so the states agree only to the rounding."""

@@ -106,7 +106,7 @@ def _run_form(box, kinds, live, precision, form):
     return f
 
 
-@pytest.mark.parametrize("form", [None, "vec8", "vec4"])
+@pytest.mark.parametrize("form", [None, "vec8", "vec4", "vec2"])
 @pytest.mark.parametrize("precision", ["bf16", "fp16", "fp32"])
 @pytest.mark.parametrize("box", sorted(BOXES))
 def test_sparse_tile_lists_reduced_forms_match_one_cell_kernel(box, precision, form):

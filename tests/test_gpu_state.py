@@ -211,3 +211,116 @@ def test_sparse_dynamic_state(tmp_path):
     assert open(base + ".dat", "rb").read() == dat
     with pytest.raises(PlbGpuError):   # a dense lattice: the kept blocks do not cover it
         DeviceLattice3D(*shape, 1.0).load_state_dynamic(ref_plb)
+
+
+# ---------------------------------------------------------------- data-processor list
+
+def _processor_section(plb_text):
+    a, b = plb_text.find("        <Processor"), plb_text.rfind("</Processor>\n")
+    return "" if a < 0 else plb_text[a:b + len("</Processor>\n")]
+
+
+def _planar_runs(flags, kind, direction):
+    """The case builder's maximal one-kind runs: along z for x and y faces,
+    along x for z faces (the wrapped boundary processors need a planar box)."""
+    nx, ny, nz = flags.shape
+    runs = []
+    if direction != 2:
+        for x in range(nx):
+            for y in range(ny):
+                z = 0
+                while z < nz:
+                    if flags[x, y, z] != kind:
+                        z += 1
+                        continue
+                    z1 = z
+                    while z1 + 1 < nz and flags[x, y, z1 + 1] == kind:
+                        z1 += 1
+                    runs.append((x, x, y, y, z, z1))
+                    z = z1 + 1
+    else:
+        for y in range(ny):
+            for z in range(nz):
+                x = 0
+                while x < nx:
+                    if flags[x, y, z] != kind:
+                        x += 1
+                        continue
+                    x1 = x
+                    while x1 + 1 < nx and flags[x1 + 1, y, z] == kind:
+                        x1 += 1
+                    runs.append((x, x1, y, y, z, z))
+                    x = x1 + 1
+    return runs
+
+
+def _replay_boundary_calls(lat, flags):
+    """The boundary-condition calls that built the case in the reference:
+    faces kind by kind over their planar runs, then every edge and corner
+    cell on its own."""
+    from palabos_gb300 import native as N
+    for k in range(N.REG_VELOCITY, N.VELOCITY_EDGE):
+        for run in _planar_runs(flags, k, ((k - N.REG_VELOCITY) % 6) // 2):
+            lat.add_boundary(run, k)
+    for k in range(N.VELOCITY_EDGE, N.NKINDS):
+        for x, y, z in np.argwhere(flags == k):
+            lat.add_boundary((x, x, y, y, z, z), k)
+
+
+@pytest.mark.parametrize("name", DSTATES)
+def test_saved_description_carries_the_reference_processor_list(name, tmp_path):
+    """The lattice built by the same boundary-condition calls as the
+    reference's case saves the reference's <Processor> list byte for byte
+    (names, domains, data, levels, block ids, ids), static and dynamic."""
+    g, meta = goldens.load(name)
+    ref = _processor_section(str(g["dstate_plb"]))
+    lat = _lat(g, meta)
+    _replay_boundary_calls(lat, g["flags"])
+    assert len(lat.processors()) == ref.count("<Processor")
+    lat.save_state_dynamic(str(tmp_path / "d"), _what(meta))
+    assert _processor_section(open(tmp_path / "d.plb").read()) == ref
+    lat.save_state(str(tmp_path / "s"), _what(meta))
+    assert _processor_section(open(tmp_path / "s.plb").read()) == ref
+
+
+@pytest.mark.parametrize("name", ["dstate_velocity_box", "dstate_zhpress_faces"])
+def test_processor_list_read_from_a_reference_description(name, tmp_path):
+    """readXmlProcessors: the list read from the reference's description is
+    saved again unchanged; a load of the state leaves the list alone."""
+    g, meta = goldens.load(name)
+    ref_plb = _reference_files(g, tmp_path)
+    lat = _lat(g, meta)
+    lat.load_state_dynamic(ref_plb, _what(meta))
+    assert lat.processors() == []
+    lat.load_processors(ref_plb)
+    lat.save_state_dynamic(str(tmp_path / "d"), _what(meta))
+    assert _processor_section(open(tmp_path / "d.plb").read()) == _processor_section(str(g["dstate_plb"]))
+    first = lat.processors()[0]
+    assert first["name"] == "WrappedLocalBoundary3D_%TD" and first["data"] == "0 0 " and first["blocks"] == (0,)
+
+
+def test_block_boundaries_record_the_reference_processors(tmp_path):
+    """setVelocityConditionOnBlockBoundaries over a 6x5x4 box: six faces,
+    twelve edges, eight corners, in the reference's order and boxes."""
+    lat = DeviceLattice3D(6, 5, 4, 1.2)
+    lat.set_velocity_condition_on_block_boundaries()
+    p = lat.processors()
+    assert [r["name"] for r in p[:6]] == ["WrappedLocalBoundary3D_%TD"] * 6
+    assert p[0]["domain"] == (0, 0, 1, 3, 1, 2) and p[5]["domain"] == (1, 4, 1, 3, 3, 3)
+    assert [r["name"] for r in p[6:10]] == [f"OuterVelocityEdge_%TD_0_{a}_{b}" for a in (-1, 1) for b in (-1, 1)]
+    assert p[6]["domain"] == (1, 4, 0, 0, 0, 0) and p[9]["domain"] == (1, 4, 4, 4, 3, 3)
+    assert p[11]["domain"] == (5, 5, 1, 3, 0, 0)          # plane y: z negative, x positive
+    assert p[14]["domain"] == (0, 0, 0, 0, 1, 2) and p[16]["domain"] == (5, 5, 0, 0, 1, 2)   # plane z: x, y sides
+    assert [r["name"] for r in p[18:]] == [f"OuterVelocityCorner3D_%TD_{x}_{y}_{z}"
+                                           for x in (-1, 1) for y in (-1, 1) for z in (-1, 1)]
+    assert p[25]["domain"] == (5, 5, 4, 4, 3, 3)
+    lat.save_state(str(tmp_path / "s"))
+    text = open(tmp_path / "s.plb").read()
+    assert text.count("<Processor id=") == 26 and "OuterVelocityCorner3D_double_D3Q19_1_1_1" in text
+    lat.clear_processors()
+    lat.add_processor("Custom_%TD", (0, 1, 0, 1, 0, 1), data="", level=1, blocks=())
+    lat.save_state(str(tmp_path / "t"), "forced_lattice")
+    assert _processor_section(open(tmp_path / "t.plb").read()) == (
+        "        <Processor>\n            <Name> Custom_double_ForcedD3Q19 </Name>\n"
+        "            <Domain> 0 1 0 1 0 1 </Domain>\n            <Data></Data>\n            <Level> 1 </Level>\n"
+        "            <Blocks></Blocks>\n        </Processor>\n")
