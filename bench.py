@@ -14,10 +14,11 @@ no explicit flush is needed between steps.
 
 Prints one JSON line (rank 0).  `value` = MLUPS of the FP64 form with the
 state resident in HBM; `e2e` = the same metric through the C ABI with host
-buffers (the FP64 state in an ordinary, pageable host array -- sent at the
-start, drag read back every 100 steps, state received at the end into the same
-array, all inside the timed region; on a GB300 the transfer kernels read and
-write the host array directly over NVLink-C2C).  The FP64 form is bound by the
+buffers (the FP64 state in pinned host memory allocated before the timed
+region -- sent at the start, drag read back every 100 steps, state received at
+the end into the same buffer, all inside the timed region; on a GB300 the
+transfer kernels read and write the host buffer directly over NVLink-C2C;
+`e2e.pageable` repeats the run with an ordinary numpy array).  The FP64 form is bound by the
 FP64 pipe, not by HBM: its `roofline` compares the algorithmic FP64 adds and
 multiplies per second with the pipe rate the library measures in the same run
 (plbgpu_measure_fp64_rate), and carries the HBM fraction beside it.
@@ -498,6 +499,9 @@ def main():
     ap.add_argument("--drag-gradient-steps", type=int, default=10000)
     ap.add_argument("--sparse", action="store_true",
                     help="run only the sparse-domain throughput study (voxelized sphere exterior, 256^3)")
+    ap.add_argument("--sparse-steps", type=int, default=200)
+    ap.add_argument("--sparse-precisions", nargs="+", default=["fp64", "fp32", "bf16"],
+                    choices=["fp64", "fp32", "bf16", "fp16", "bf16sr"])
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -518,7 +522,8 @@ def main():
     if args.sparse:
         from palabos_gb300 import Context
         ctx = Context(dist_env()[2])
-        print(json.dumps({"study": "sparse_sphere_exterior", **sparse_throughput(ctx=ctx)}))
+        r = sparse_throughput(steps=args.sparse_steps, precisions=tuple(args.sparse_precisions), ctx=ctx)
+        print(json.dumps({"study": "sparse_sphere_exterior", **r}))
         return
     if args.permeability:
         from palabos_gb300 import Context

@@ -71,6 +71,10 @@ __device__ inline DualT<T> invRhoOf(DualT<T> rhoBar) {
 // adjoint's face cells, on the FP32 pipe).
 using Dual = DualT<double>;
 using DualF = DualT<float>;
+// The density of a dual rho-bar (the edge and corner processors' rounding to
+// R has derivative one).
+template <typename T>
+__device__ inline DualT<T> densityOfRhoBar(DualT<T> rb) { return rb + DualT<T>(1.0); }
 
 template <typename R> __device__ inline double valueOf(const R& x) { return (double)x; }
 template <> __device__ inline double valueOf<Dual>(const Dual& x) { return x.v; }
@@ -746,7 +750,8 @@ __device__ __forceinline__ R adjointCell(const DevLattice& L, const NeighbourDel
     }
     for (int i = 0; i < 19; ++i) fc[i] = f[i * L.n + idx];
     cellForce(L, forceIsFp64<R>(), idx, nullptr, F);
-    const R go = adjCell<R>(k, fc, F, omega, invRho0, mu, lam, g);
+    // an edge or corner cell collides with its BGK base
+    const R go = adjCell<R>(isSurface(k) ? K_BGK : k, fc, F, omega, invRho0, mu, lam, g);
     for (int i = 0; i < 19; ++i) lamOut[i * L.n + idx] = lam[i];
     if (k == K_GUO)
         for (int d = 0; d < 3; ++d) gF[d * L.n + idx] += g[d];
@@ -800,6 +805,131 @@ __global__ void toDualKernel(long long n19, const double* in, Dual* out) {
     if (i < n19) out[i] = Dual(in[i], 0.);
 }
 
+// ---------------------------------------------------------------- edges and corners
+//
+// The external velocity edges and corners (finite-difference processors) run
+// after each push step, edges first, then corners, on the natural-order state:
+// the same arithmetic as the domain's own surfaceKernel (kernels.cuh), in the
+// adjoint's arithmetic T (R, or a dual number for the tangent run).
+
+// Populations of a natural-order state.
+template <typename T>
+struct NatSource {
+    const T* buf;
+    long long n;
+    __device__ __forceinline__ void operator()(long long idx, T* f) const {
+#pragma unroll
+        for (int i = 0; i < 19; ++i) f[i] = buf[i * n + idx];
+    }
+};
+
+template <typename R, typename T>
+__global__ void surfaceNatKernel(DevLattice L, T* buf, const int4* cells, int count, R invRho0, double bbRho,
+                                 T omega) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const int4 c = cells[t];
+    const long long idx = ((long long)c.x * L.ny + c.y) * L.nz + c.z;
+    NatSource<T> src{buf, L.n};
+    T rho, g[3][3], vel[3], f[19];
+    // after a push step the faces are as streamed: their completion is pending
+    surfaceGradients<R, T>(L, c, 1, invRho0, bbRho, src, rho, g);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) vel[d] = T((R)L.bc[d * L.n + idx]);
+    surfaceFromGradients<T>(rho, g, vel, omega, f);
+    for (int i = 0; i < 19; ++i) buf[i * L.n + idx] = f[i];
+}
+
+// Populations of a natural-order state as dual numbers, with the derivative
+// seeded on population `pop` of cell `seed`.
+template <typename R>
+struct SeededSource {
+    const R* buf;
+    long long n, seed;
+    int pop;
+    __device__ __forceinline__ void operator()(long long idx, DualT<R>* f) const {
+#pragma unroll
+        for (int i = 0; i < 19; ++i) f[i] = DualT<R>(buf[i * n + idx], (idx == seed && i == pop) ? 1.0 : 0.0);
+    }
+};
+
+// Reverse of the edge (or corner) processor of one launch's cells on lambda,
+// in place, at the state f it produced: each cell's 19 adjoint values go to
+// the populations of the neighbours it read -- its inward neighbours (density
+// and velocity) and, for an edge, the two along the edge unless they store
+// their velocity -- and its own incoming populations, overwritten unread, get
+// zero.  Each neighbour population is differentiated through the whole
+// processor (finite differences, face completion of a pending neighbour,
+// rebuild) with one dual pass; one more pass gives the omega derivative, which
+// goes to gOmega.  Corners read edges' densities, so the corners' reverse runs
+// first.
+template <typename R>
+__global__ void surfaceAdjointKernel(DevLattice L, const R* f, R* lam, const int4* cells, int count, R invRho0,
+                                         double bbRho, R omega, AdjAcc* acc) {
+    using D = DualT<R>;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double go = 0.;
+    if (t < count) {
+        const int4 c = cells[t];
+        const int p[3] = {c.x, c.y, c.z};
+        const long long idx = ((long long)c.x * L.ny + c.y) * L.nz + c.z;
+        R lo[19];
+        for (int i = 0; i < 19; ++i) {
+            lo[i] = lam[i * L.n + idx];
+            lam[i * L.n + idx] = R(0);
+        }
+        D vel[3];
+        for (int d = 0; d < 3; ++d) vel[d] = D((R)L.bc[d * L.n + idx]);
+        auto pass = [&](long long seed, int pop, bool seedOmega) {
+            SeededSource<R> src{f, L.n, seed, pop};
+            D rho, g[3][3], fo[19];
+            surfaceGradients<R, D>(L, c, 1, invRho0, bbRho, src, rho, g);
+            surfaceFromGradients<D>(rho, g, vel, D(omega, seedOmega ? 1.0 : 0.0), fo);
+            R v = R(0);
+            for (int i = 0; i < 19; ++i) v += lo[i] * fo[i].d;
+            return v;
+        };
+        go = (double)pass(-1, 0, true);
+        // the cells read: the inward neighbours (density and velocity) and, for
+        // an edge, the two along it (velocity only: nothing to differentiate
+        // when they store their velocity)
+        int nrmAxis[3], nrmSide[3], nn = 0;
+        if (c.w < K_CORNER) {
+            const int e = c.w - K_EDGE, plane = e / 4;
+            nrmAxis[0] = (plane + 1) % 3;
+            nrmSide[0] = (e & 2) ? -1 : 1;
+            nrmAxis[1] = (plane + 2) % 3;
+            nrmSide[1] = (e & 1) ? -1 : 1;
+            nrmAxis[2] = plane;
+            nn = 2;
+        } else {
+            const int q = c.w - K_CORNER;
+            for (int a = 0; a < 3; ++a) {
+                nrmAxis[a] = a;
+                nrmSide[a] = (q & (4 >> a)) ? -1 : 1;
+            }
+            nn = 3;
+        }
+        for (int r = 0; r < (c.w < K_CORNER ? 4 : 3); ++r) {
+            int q[3] = {p[0], p[1], p[2]};
+            if (r < nn) q[nrmAxis[r]] += nrmSide[r];
+            else q[nrmAxis[2]] += (r == nn ? 1 : -1);
+            {
+                const long long qi = ((long long)wrapAxis(q[0], L.nx) * L.ny + wrapAxis(q[1], L.ny)) * L.nz +
+                                     wrapAxis(q[2], L.nz);
+                const int k = L.flags[qi];
+                if (k == K_BB || k == K_MEBB || k == K_NODYN || k == K_NONE) continue;
+                if (r >= nn && isSurface(k)) continue;
+                for (int j = 0; j < 19; ++j) {
+                    const R v = pass(qi, j, false);
+                    if (v != R(0)) atomicAdd(&lam[j * L.n + qi], v);
+                }
+            }
+        }
+    }
+    blockAdd(go, acc->gOmega);
+}
+
 // ---------------------------------------------------------------- host side
 
 namespace {
@@ -816,10 +946,13 @@ struct AdjointState {
     AdjAcc* acc = nullptr;
     long long* faces = nullptr;   // face cells (cell indices), nFaces of them
     int nFaces = 0;
+    int4* surf = nullptr;         // edge cells, then corner cells (x, y, z, kind)
+    int nEdges = 0, nCorners = 0;
     bool pending0 = false;     // the recorded run's first step completes its faces
     bool ready = false;        // a forward run is recorded
     ~AdjointState() {
         cudaFree(ckpt); cudaFree(seg); cudaFree(lam); cudaFree(gF); cudaFree(uT); cudaFree(acc); cudaFree(faces);
+        cudaFree(surf);
     }
     // Steps after the first collide states that came from a streaming step:
     // their faces are completed first.
@@ -900,26 +1033,94 @@ void launchObjective(const DomainAccess& a, const Objective& o, const R* f, cons
 }
 
 // The adjoint covers BGK, Guo, incompressible BGK, bounce-back,
-// momentum-exchange bounce-back, no-dynamics and the regularized and Zou/He
-// face cells; `faces` (optional) receives the face cells' indices.  Edges and
-// corners (finite differences over neighbours) are refused.
+// momentum-exchange bounce-back, no-dynamics, the regularized and Zou/He face
+// cells and the external velocity edges and corners; `faces` (optional)
+// receives the face cells' indices.  An edge or corner that reads a
+// Guo-forced cell is refused: its rebuilt populations would depend on that
+// cell's force through the finite differences, a path the force gradient does
+// not follow.
 int checkKinds(plbgpu_ctx* c, const DomainAccess& a, std::vector<long long>* faces = nullptr) {
     std::vector<uint8_t> k((size_t)a.L.n);
     if (cudaMemcpyAsync(k.data(), a.L.flags, k.size(), cudaMemcpyDeviceToHost, a.stream) != cudaSuccess ||
         cudaStreamSynchronize(a.stream) != cudaSuccess)
         return domainFail(c, PLBGPU_ERR_CUDA, "reading cell kinds failed");
+    const int nx = a.L.nx, ny = a.L.ny, nz = a.L.nz;
+    auto kindAt = [&](int x, int y, int z) {
+        x = x < 0 ? x + nx : (x >= nx ? x - nx : x);
+        y = y < 0 ? y + ny : (y >= ny ? y - ny : y);
+        z = z < 0 ? z + nz : (z >= nz ? z - nz : z);
+        return (int)k[((size_t)x * ny + y) * nz + z];
+    };
     for (size_t i = 0; i < k.size(); ++i) {
         const int v = k[i];
         if (isFace(v)) {
             if (faces) faces->push_back((long long)i);
             continue;
         }
+        if (isSurface(v)) {
+            const int p[3] = {(int)(i / ((size_t)ny * nz)), (int)((i / nz) % ny), (int)(i % nz)};
+            for (int ax = 0; ax < 3; ++ax)
+                for (int s = -1; s <= 1; s += 2) {
+                    int q[3] = {p[0], p[1], p[2]};
+                    q[ax] += s;
+                    if (kindAt(q[0], q[1], q[2]) == K_GUO)
+                        return domainFail(c, PLBGPU_ERR_ARG,
+                                          "adjoint: an edge or corner cell next to a Guo-forced cell is not supported");
+                }
+            continue;
+        }
         if (v != K_BGK && v != K_GUO && v != K_INCBGK && v != K_BB && v != K_MEBB && v != K_NODYN)
             return domainFail(c, PLBGPU_ERR_ARG,
                               "the adjoint supports BGK, Guo, incompressible BGK, bounce-back, momentum-exchange, "
-                              "no-dynamics and face cells (no edges or corners)");
+                              "no-dynamics, face, edge and corner cells");
     }
     return PLBGPU_OK;
+}
+
+// The domain's edge and corner list, copied (the adjoint's run outlives later
+// changes of the domain's kinds).
+int copySurface(plbgpu_ctx* c, int h, const DomainAccess& a, int4** dst, int* nEdges, int* nCorners) {
+    const int4* cells = nullptr;
+    int ne = 0, nc = 0;
+    int rc = domainSurface(c, h, &cells, &ne, &nc);
+    if (rc) return rc;
+    cudaFree(*dst);
+    *dst = nullptr;
+    *nEdges = ne;
+    *nCorners = nc;
+    if (ne + nc == 0) return PLBGPU_OK;
+    if (cudaMalloc(dst, sizeof(int4) * (size_t)(ne + nc)) != cudaSuccess ||
+        cudaMemcpyAsync(*dst, cells, sizeof(int4) * (size_t)(ne + nc), cudaMemcpyDeviceToDevice, a.stream) !=
+            cudaSuccess)
+        return domainFail(c, PLBGPU_ERR_NOMEM, "adjoint: copying the edge and corner list failed");
+    return PLBGPU_OK;
+}
+
+// The edge processors, then the corner processors, on a natural-order state
+// just pushed.
+template <typename R, typename T>
+void launchSurfaceNat(const DomainAccess& a, const int4* surf, int nEdges, int nCorners, T* buf, T omega) {
+    const R invRho0 = (R)(1.0 / a.rho0);
+    if (nEdges)
+        surfaceNatKernel<R, T><<<(nEdges + 63) / 64, 64, 0, a.stream>>>(a.L, buf, surf, nEdges, invRho0, a.bbRho, omega);
+    if (nCorners)
+        surfaceNatKernel<R, T><<<(nCorners + 63) / 64, 64, 0, a.stream>>>(a.L, buf, surf + nEdges, nCorners, invRho0,
+                                                                        a.bbRho, omega);
+    *a.launches += (nEdges ? 1 : 0) + (nCorners ? 1 : 0);
+}
+
+// Their reverse on lambda at the state f they produced: corners first.
+template <typename R>
+void launchSurfaceAdjoint(const DomainAccess& a, const int4* surf, int nEdges, int nCorners, const R* f, R* lam,
+                          AdjAcc* acc) {
+    const R invRho0 = (R)(1.0 / a.rho0), omega = (R)a.omega;
+    if (nCorners)
+        surfaceAdjointKernel<R><<<(nCorners + 63) / 64, 64, 0, a.stream>>>(a.L, f, lam, surf + nEdges, nCorners,
+                                                                         invRho0, a.bbRho, omega, acc);
+    if (nEdges)
+        surfaceAdjointKernel<R><<<(nEdges + 63) / 64, 64, 0, a.stream>>>(a.L, f, lam, surf, nEdges, invRho0, a.bbRho,
+                                                                       omega, acc);
+    *a.launches += (nEdges ? 1 : 0) + (nCorners ? 1 : 0);
 }
 
 // The face cells' reverse step beside the bulk's (disjoint writes).
@@ -958,6 +1159,7 @@ int forwardImpl(plbgpu_ctx* c, int h, DomainAccess& a, AdjointState* st, int T, 
         pushStepKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, D, cur, out, omega, invRho0, nullptr,
                                                                           st->pendingAt(t));
         *a.launches += 1;
+        launchSurfaceNat<R, R>(a, st->surf, st->nEdges, st->nCorners, out, omega);
         cur = out;
     }
     ADJ_TRY(cudaGetLastError());
@@ -1007,13 +1209,18 @@ int backwardImpl(DomainAccess& a, AdjointState* st, const Objective& o, double* 
         int cur = 0;   // lam + cur * sz holds lambda^{t+1}
         for (int s = T / K - 1; s >= 0; --s) {
             // f^{sK} is checkpoint s; recompute f^{sK+1} .. f^{sK+K-1} into seg
-            auto state = [&](int k) { return k == 0 ? ck + (long long)s * sz : sg + k * sz; };
+            auto state = [&](int k) {
+                return k == 0 ? ck + (long long)s * sz : (k == K ? ck + (long long)(s + 1) * sz : sg + k * sz);
+            };
             for (int k = 0; k + 1 < K; ++k) {
                 pushStepKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(
                     a.L, D, state(k), state(k + 1), omega, invRho0, nullptr, st->pendingAt((long long)s * K + k));
                 *a.launches += 1;
+                launchSurfaceNat<R, R>(a, st->surf, st->nEdges, st->nCorners, state(k + 1), omega);
             }
             for (int k = K - 1; k >= 0; --k) {
+                // the edge and corner processors that finished step k, reversed at the state they produced
+                launchSurfaceAdjoint<R>(a, st->surf, st->nEdges, st->nCorners, state(k + 1), lam + cur * sz, st->acc);
                 adjointStepKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(
                     a.L, D, state(k), lam + cur * sz, lam + (1 - cur) * sz, gF, omega, invRho0, st->acc);
                 *a.launches += 1;
@@ -1092,8 +1299,8 @@ int adjointBackward(plbgpu_ctx* c, int h, const Objective& o, double* objective,
 // omega and force).  Three states of memory whatever the number of steps.
 template <typename R>
 int steadyImpl(plbgpu_ctx* c, DomainAccess& a, int iterations, const Objective& o,
-               const std::vector<long long>& faceList, double* objective, double* grad_force, double* grad_omega,
-               float* ms) {
+               const std::vector<long long>& faceList, const int4* surf, int nEdges, int nCorners, double* objective,
+               double* grad_force, double* grad_omega, float* ms) {
     const long long n = a.L.n, sz = 19 * n;
     struct Buffers {
         R* f = nullptr;
@@ -1139,6 +1346,7 @@ int steadyImpl(plbgpu_ctx* c, DomainAccess& a, int iterations, const Objective& 
     launchObjective<R>(a, o, b.f, b.w, b.lam, b.gF, b.acc);
     int cur = 0;
     for (int t = 0; t < iterations; ++t) {
+        launchSurfaceAdjoint<R>(a, surf, nEdges, nCorners, b.f, b.lam + cur * sz, b.acc);
         adjointStepKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, D, b.f, b.lam + cur * sz,
                                                                              b.lam + (1 - cur) * sz, b.gF, omega,
                                                                              invRho0, b.acc);
@@ -1172,6 +1380,12 @@ int tangentLinear(plbgpu_ctx* c, int h, int T, const double* dforce, size_t ndf,
     std::vector<long long> faceList;
     if ((rc = checkKinds(c, a, &faceList))) return rc;
     const bool hasFaces = !faceList.empty();
+    struct SurfList {
+        int4* p = nullptr;
+        ~SurfList() { cudaFree(p); }
+    } surf;
+    int ne = 0, nc = 0;
+    if ((rc = copySurface(c, h, a, &surf.p, &ne, &nc))) return rc;
     double *f0 = nullptr, *dF = nullptr, *uT = nullptr;
     Dual* buf = nullptr;
     AdjAcc* acc = nullptr;
@@ -1200,6 +1414,7 @@ int tangentLinear(plbgpu_ctx* c, int h, int T, const double* dforce, size_t ndf,
             pushStepKernel<Dual><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(a.L, D, cur, nxt, om, inv0, dF,
                                                                                  t == 0 ? a.pending : hasFaces);
             *a.launches += 1;
+            launchSurfaceNat<double, Dual>(a, surf.p, ne, nc, nxt, om);
             std::swap(cur, nxt);
         }
         if (o.kind == kDrag)
@@ -1283,6 +1498,7 @@ int plbgpu_adjoint_forward(plbgpu_ctx* c, int h, int T, int K) {
     }
     st->T = T;
     st->ready = false;
+    if ((rc = copySurface(c, h, a, &st->surf, &st->nEdges, &st->nCorners))) return rc;
     cudaFree(st->faces);
     st->faces = nullptr;
     st->nFaces = (int)faces.size();
@@ -1345,9 +1561,15 @@ static int adjointSteady(plbgpu_ctx* c, int h, int iterations, const Objective& 
     if ((rc = checkObjective(c, a, o))) return rc;
     std::vector<long long> faces;
     if ((rc = checkKinds(c, a, &faces))) return rc;
-    return a.precision == PLBGPU_FP64
-               ? steadyImpl<double>(c, a, iterations, o, faces, objective, grad_force, grad_omega, ms)
-               : steadyImpl<float>(c, a, iterations, o, faces, objective, grad_force, grad_omega, ms);
+    int4* surf = nullptr;
+    int ne = 0, nc = 0;
+    if ((rc = copySurface(c, h, a, &surf, &ne, &nc))) return rc;
+    rc = a.precision == PLBGPU_FP64
+             ? steadyImpl<double>(c, a, iterations, o, faces, surf, ne, nc, objective, grad_force, grad_omega, ms)
+             : steadyImpl<float>(c, a, iterations, o, faces, surf, ne, nc, objective, grad_force, grad_omega, ms);
+    cudaStreamSynchronize(a.stream);
+    cudaFree(surf);
+    return rc;
 }
 
 int plbgpu_adjoint_steady_weighted(plbgpu_ctx* c, int h, int iterations, const double* weights, size_t n3,

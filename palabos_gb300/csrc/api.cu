@@ -760,6 +760,7 @@ int domainAccess(plbgpu_ctx* c, int h, DomainAccess* out) {
     out->pending = d->pending;
     out->omega = d->omega;
     out->rho0 = d->rho0;
+    out->bbRho = d->bbRho;
     out->stream = c->stream;
     out->adjointSlot = &d->adjoint;
     out->adjointFree = &d->adjointFree;
@@ -773,6 +774,18 @@ cudaStream_t contextStream(plbgpu_ctx* c) { return c ? c->stream : nullptr; }
 
 void countLaunches(plbgpu_ctx* c, int n) {
     if (c) c->launches += (unsigned long long)n;
+}
+
+int domainSurface(plbgpu_ctx* c, int h, const int4** cells, int* nEdges, int* nCorners) {
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if ((rc = materialize(c, d))) return rc;
+    if (d->surfDirty && (rc = buildSurface(c, d))) return rc;
+    *cells = d->surf;
+    *nEdges = d->nEdges;
+    *nCorners = d->nCorners;
+    return PLBGPU_OK;
 }
 
 void domainSetState(plbgpu_ctx* c, int h, bool odd, bool pending) {

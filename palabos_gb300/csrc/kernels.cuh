@@ -979,79 +979,200 @@ __device__ __forceinline__ bool cellMacroscopic(const DevLattice& L, int x, int 
 // every neighbour read below lies inside the domain (after the periodic wrap),
 // and that an edge reads no edge's or corner's density and a corner no
 // corner's density, so that no thread reads populations another one writes.
+//
+// The processor is written once for any arithmetic type T (the form's R, or
+// a dual number of R in the adjoint module) and any population source: a
+// source `src(idx, f)` loads the raw post-stream populations of cell idx into
+// f[19].
 
 __device__ __forceinline__ int wrapAxis(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
 
-// cellMacroscopic as one out-of-line call: the finite differences read up to
-// five neighbours, and inlining the face completion into each would multiply
-// the kernel's code (and compile time) for no gain on a few thousand cells.
-template <typename S, bool ODD>
-__device__ __noinline__ void surfaceMacro(const DevLattice& L, int x, int y, int z, int pending,
-                                          typename StoreT<S>::R invRho0, double bbRho, typename StoreT<S>::R* u,
-                                          typename StoreT<S>::R& rb, double& rho) {
-    cellMacroscopic<S, ODD>(L, x, y, z, pending, invRho0, bbRho, u, rb, rho);
-}
+// fullRho(rhoBar) as Cell::computeDensity reports it, rounded to R: the
+// density is formed in double ((double)rhoBar + 1) and the finite differences
+// use it in R.
+template <typename R>
+__device__ __forceinline__ R densityOfRhoBar(R rb) { return (R)((double)rb + 1.0); }
 
-// Cell::computeVelocity of the cell at p (faces pending completion included).
-template <typename S, bool ODD>
-__device__ __forceinline__ void surfaceVelocity(const DevLattice& L, const int* p, int pending,
-                                                typename StoreT<S>::R invRho0, double bbRho,
-                                                typename StoreT<S>::R* u) {
-    using R = typename StoreT<S>::R;
-    const int x = wrapAxis(p[0], L.nx), y = wrapAxis(p[1], L.ny), z = wrapAxis(p[2], L.nz);
-    const long long idx = ((long long)x * L.ny + y) * L.nz + z;
-    if (isSurface(L.flags[idx])) {  // stored velocity: no population read
-#pragma unroll
-        for (int d = 0; d < 3; ++d) u[d] = (R)L.bc[d * L.n + idx];
+// Cell::computeVelocity / computeDensity of a cell of kind k from its raw
+// post-stream populations f (completed in place first when the faces are
+// pending), the way each dynamics reports them.  rho is the density in R.
+template <typename R, typename T>
+__device__ __forceinline__ void macroOfPops(const DevLattice& L, long long idx, int k, T* f, int pending, R invRho0,
+                                            double bbRho, T* u, T& rho) {
+    if (pending && isFace(k)) completeIfFace<T>(L, idx, k, f);
+    u[0] = u[1] = u[2] = T(0);
+    if (k == K_BB || k == K_MEBB || k == K_NODYN || k == K_NONE) {  // core/dynamics.hh:814-829, 994-1008
+        rho = T((R)bbRho);
         return;
     }
-    R rb;
-    double rho;
-    surfaceMacro<S, ODD>(L, x, y, z, pending, invRho0, bbRho, u, rb, rho);
+    T rb;
+    if (k == K_BGK) {  // momentTemplates3D.h:402-408 compute_uLb
+        T jj[3], rr;
+        rhoBarJ<T>(f, rr, jj);
+        rb = rhoBarSeq<T>(f);
+        T invRho = invRhoOf(rb);
+        for (int d = 0; d < 3; ++d) u[d] = jj[d] * invRho;
+    } else if (k == K_GUO) {  // externalForceDynamics.hh:58-73
+        const R* fp = static_cast<const R*>(L.force);
+        T jj[3], rr;
+        rhoBarJ<T>(f, rr, jj);
+        T invRho = invRhoOf(rr);
+        T Fv[3] = {T(fp[idx]), T(fp[L.n + idx]), T(fp[2 * L.n + idx])};
+        for (int d = 0; d < 3; ++d) u[d] = jj[d] * invRho + Fv[d] / T(2);
+        rb = rhoBarSeq<T>(f);
+    } else if (k == K_INCBGK) {  // isoThermalDynamics.hh:1388-1395
+        T jj[3], rr;
+        rhoBarJ<T>(f, rr, jj);
+        for (int d = 0; d < 3; ++d) u[d] = jj[d] * T(invRho0);
+        rb = rhoBarSeq<T>(f);
+    } else if (isSurface(k)) {  // StoreVelocityDynamics over BGK: stored u, base density
+        for (int d = 0; d < 3; ++d) u[d] = T((R)L.bc[d * L.n + idx]);
+        rho = rhoBarSeq<T>(f) + T(1);        // BoundaryCompositeDynamics::computeDensity
+        return;
+    } else {  // faces
+        const int fam = faceFamily(k), dir = faceDir(k);
+        const double v[3] = {L.bc[idx], L.bc[L.n + idx], L.bc[2 * L.n + idx]};
+        if (fam == 0 || fam == 2) {  // stored velocity, boundaryDynamics.hh:324-330
+            for (int d = 0; d < 3; ++d) u[d] = T((R)v[d]);
+            rb = velFaceRhoBarAny<T>(f, k, T((R)v[dir]));
+        } else {  // boundaryDynamics.hh:790-812
+            rb = T((R)v[0]) - T(1);
+            pressFaceJAny<T>(f, k, rb, u);
+            T invRho = invRhoOf(rb);
+            for (int d = 0; d < 3; ++d) { u[d] *= invRho; u[d] += T(0.5) * T(0); }
+        }
+    }
+    rho = densityOfRhoBar(rb);
 }
 
-// Cell::computeDensity of the cell at p.
-template <typename S, bool ODD>
-__device__ __forceinline__ typename StoreT<S>::R surfaceDensity(const DevLattice& L, const int* p, int pending,
-                                                               typename StoreT<S>::R invRho0, double bbRho) {
-    using R = typename StoreT<S>::R;
-    R u[3], rb;
-    double rho;
-    surfaceMacro<S, ODD>(L, wrapAxis(p[0], L.nx), wrapAxis(p[1], L.ny), wrapAxis(p[2], L.nz), pending, invRho0,
-                         bbRho, u, rb, rho);
-    return (R)rho;
-}
-
-// fd::DirectedGradients3D (finiteDifference/finiteDifference3D.h:61-190):
-// first-order one-sided difference into the domain along a normal,
-// d_A u = -normal (u(x - normal e_A) - u(x)); centred difference along the
-// boundary, d_A u = (u(x + e_A) - u(x - e_A)) / 2.
-template <typename S, bool ODD>
-__device__ __forceinline__ void normalGradient(const DevLattice& L, const int* p, int axis, int normal, int pending,
-                                               typename StoreT<S>::R invRho0, double bbRho,
-                                               const typename StoreT<S>::R* u0, typename StoreT<S>::R* g) {
-    using R = typename StoreT<S>::R;
-    int q[3] = {p[0], p[1], p[2]};
-    q[axis] -= normal;
-    R u1[3];
-    surfaceVelocity<S, ODD>(L, q, pending, invRho0, bbRho, u1);
+// Velocity of the cell at p (wrapped): the stored velocity of an edge or
+// corner (no population read), else computeVelocity.
+template <typename R, typename T, class Src>
+__device__ __forceinline__ void surfaceVelocityAt(const DevLattice& L, const int* p, int pending, R invRho0,
+                                                  double bbRho, Src& src, T* u) {
+    const long long idx = ((long long)wrapAxis(p[0], L.nx) * L.ny + wrapAxis(p[1], L.ny)) * L.nz + wrapAxis(p[2], L.nz);
+    const int k = L.flags[idx];
+    if (isSurface(k)) {
 #pragma unroll
-    for (int d = 0; d < 3; ++d) g[d] = (R)(-normal) * (-u0[d] + u1[d]);
+        for (int d = 0; d < 3; ++d) u[d] = T((R)L.bc[d * L.n + idx]);
+        return;
+    }
+    T f[19], rho;
+    src(idx, f);
+    macroOfPops<R, T>(L, idx, k, f, pending, invRho0, bbRho, u, rho);
 }
 
+// Density of the cell at p (wrapped).
+template <typename R, typename T, class Src>
+__device__ __forceinline__ T surfaceDensityAt(const DevLattice& L, const int* p, int pending, R invRho0, double bbRho,
+                                              Src& src) {
+    const long long idx = ((long long)wrapAxis(p[0], L.nx) * L.ny + wrapAxis(p[1], L.ny)) * L.nz + wrapAxis(p[2], L.nz);
+    T f[19], u[3], rho;
+    src(idx, f);
+    macroOfPops<R, T>(L, idx, L.flags[idx], f, pending, invRho0, bbRho, u, rho);
+    return rho;
+}
+
+// The finite differences of an edge or corner cell (fd::DirectedGradients3D,
+// finiteDifference/finiteDifference3D.h:61-190: first-order one-sided into the
+// domain along a normal, d_A u = -normal (u(x - normal e_A) - u(x)); centred
+// along an edge, d_A u = (u(x + e_A) - u(x - e_A)) / 2) and its density: the
+// mean of the inward neighbours' densities.  g[A][d] = d_A u_d.
+template <typename R, typename T, class Src>
+__device__ __forceinline__ void surfaceGradients(const DevLattice& L, int4 c, int pending, R invRho0, double bbRho,
+                                                 Src& src, T& rho, T (&g)[3][3]) {
+    const int p[3] = {c.x, c.y, c.z};
+    const long long idx = ((long long)c.x * L.ny + c.y) * L.nz + c.z;
+    T vel[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) vel[d] = T((R)L.bc[d * L.n + idx]);
+    auto normal = [&](int axis, int nrm) {
+        int q[3] = {p[0], p[1], p[2]};
+        q[axis] -= nrm;
+        T u1[3];
+        surfaceVelocityAt<R, T>(L, q, pending, invRho0, bbRho, src, u1);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) g[axis][d] = T(-nrm) * (-vel[d] + u1[d]);
+    };
+    if (c.w < K_CORNER) {
+        const int e = c.w - K_EDGE, plane = e / 4;
+        const int n1 = (e & 2) ? 1 : -1, n2 = (e & 1) ? 1 : -1;
+        const int d1 = (plane + 1) % 3, d2 = (plane + 2) % 3;
+        int a[3] = {p[0], p[1], p[2]}, b[3] = {p[0], p[1], p[2]};
+        a[d1] -= n1;
+        b[d2] -= n2;
+        const T rho10 = surfaceDensityAt<R, T>(L, a, pending, invRho0, bbRho, src);
+        const T rho01 = surfaceDensityAt<R, T>(L, b, pending, invRho0, bbRho, src);
+        rho = T(0.5) * (rho01 + rho10);
+        int up[3] = {p[0], p[1], p[2]}, um[3] = {p[0], p[1], p[2]};
+        up[plane] += 1;
+        um[plane] -= 1;
+        T uu[3], ud[3];
+        surfaceVelocityAt<R, T>(L, up, pending, invRho0, bbRho, src, uu);
+        surfaceVelocityAt<R, T>(L, um, pending, invRho0, bbRho, src, ud);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) g[plane][d] = (uu[d] - ud[d]) / T(2);
+        normal(d1, n1);
+        normal(d2, n2);
+    } else {
+        const int q = c.w - K_CORNER;
+        const int nrm[3] = {(q & 4) ? 1 : -1, (q & 2) ? 1 : -1, (q & 1) ? 1 : -1};
+        T r[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            int nbp[3] = {p[0], p[1], p[2]};
+            nbp[a] -= nrm[a];
+            r[a] = surfaceDensityAt<R, T>(L, nbp, pending, invRho0, bbRho, src);
+        }
+        rho = T(1) / T(3) * (r[2] + r[1] + r[0]);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) normal(a, nrm[a]);
+    }
+}
+
+// The rebuilt populations from (rho, velocity gradients): off-equilibrium
+// stress Pi = -rho / (3 omega) (grad u + grad u^T), then f_eq(rho, rho u) +
+// fNeq(Pi) (finiteDifferenceBoundaryProcessor3D.hh:180-206).
+template <typename T>
+__device__ __forceinline__ void surfaceFromGradients(const T& rho, const T (&g)[3][3], const T* vel, const T& omega,
+                                                     T* f) {
+    const T sToPi = -rho / T(3) / omega;
+    T Pi[6];
+    Pi[0] = T(2) * g[0][0] * sToPi;
+    Pi[1] = (g[0][1] + g[1][0]) * sToPi;
+    Pi[2] = (g[0][2] + g[2][0]) * sToPi;
+    Pi[3] = T(2) * g[1][1] * sToPi;
+    Pi[4] = (g[1][2] + g[2][1]) * sToPi;
+    Pi[5] = T(2) * g[2][2] * sToPi;
+    T j[3] = {rho * vel[0], rho * vel[1], rho * vel[2]};
+    const T jSqr = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
+    regularizeFromPi<T>(f, rho - T(1), j, jSqr, Pi);
+}
+
+// Populations of the AA-ordered state of parity ODD.
 template <typename S, bool ODD>
-__device__ __forceinline__ void centralGradient(const DevLattice& L, const int* p, int axis, int pending,
+struct AASource {
+    const DevLattice& L;
+    __device__ __forceinline__ void operator()(long long idx, typename StoreT<S>::R* f) const {
+        const int z = (int)(idx % L.nz), y = (int)((idx / L.nz) % L.ny), x = (int)(idx / ((long long)L.ny * L.nz));
+        Neighbourhood nb = neighbourhood(L, x, y, z);
+        const S* Pp = static_cast<const S*>(L.pop);
+#pragma unroll
+        for (int i = 0; i < 19; ++i) f[i] = StoreT<S>::ld(Pp + slotOf<ODD>(L, nb, idx, i));
+    }
+};
+
+// Gradients and density of one edge or corner cell of the domain's own state,
+// as one out-of-line call: the finite differences read up to five
+// neighbours, and inlining their macroscopic values into the kernel would
+// multiply its code for no gain on a few thousand cells.
+template <typename S, bool ODD>
+__device__ __noinline__ void surfaceGradientsAA(const DevLattice& L, int4 c, int pending,
                                                 typename StoreT<S>::R invRho0, double bbRho,
-                                                typename StoreT<S>::R* g) {
+                                                typename StoreT<S>::R& rho, typename StoreT<S>::R (&g)[3][3]) {
     using R = typename StoreT<S>::R;
-    int a[3] = {p[0], p[1], p[2]}, b[3] = {p[0], p[1], p[2]};
-    a[axis] += 1;
-    b[axis] -= 1;
-    R up[3], um[3];
-    surfaceVelocity<S, ODD>(L, a, pending, invRho0, bbRho, up);
-    surfaceVelocity<S, ODD>(L, b, pending, invRho0, bbRho, um);
-#pragma unroll
-    for (int d = 0; d < 3; ++d) g[d] = (up[d] - um[d]) / (R)2;
+    AASource<S, ODD> src{L};
+    surfaceGradients<R, R>(L, c, pending, invRho0, bbRho, src, rho, g);
 }
 
 // One launch finishes `count` edge cells or `count` corner cells.
@@ -1062,53 +1183,12 @@ __global__ void surfaceKernel(DevLattice L, const int4* __restrict__ cells, int 
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= count) return;
     const int4 c = cells[t];
-    const int p[3] = {c.x, c.y, c.z};
-    const int k = c.w;
     const long long idx = ((long long)c.x * L.ny + c.y) * L.nz + c.z;
-    R vel[3];
+    R rho, g[3][3], vel[3], f[19];
+    surfaceGradientsAA<S, ODD>(L, c, pending, invRho0, bbRho, rho, g);
 #pragma unroll
     for (int d = 0; d < 3; ++d) vel[d] = (R)L.bc[d * L.n + idx];
-    R rho, g[3][3];
-    if (k < K_CORNER) {
-        const int e = k - K_EDGE, plane = e / 4;
-        const int n1 = (e & 2) ? 1 : -1, n2 = (e & 1) ? 1 : -1;
-        const int d1 = (plane + 1) % 3, d2 = (plane + 2) % 3;
-        int a[3] = {p[0], p[1], p[2]}, b[3] = {p[0], p[1], p[2]};
-        a[d1] -= n1;
-        b[d2] -= n2;
-        const R rho10 = surfaceDensity<S, ODD>(L, a, pending, invRho0, bbRho);
-        const R rho01 = surfaceDensity<S, ODD>(L, b, pending, invRho0, bbRho);
-        rho = (R)0.5 * (rho01 + rho10);
-        centralGradient<S, ODD>(L, p, plane, pending, invRho0, bbRho, g[plane]);
-        normalGradient<S, ODD>(L, p, d1, n1, pending, invRho0, bbRho, vel, g[d1]);
-        normalGradient<S, ODD>(L, p, d2, n2, pending, invRho0, bbRho, vel, g[d2]);
-    } else {
-        const int q = k - K_CORNER;
-        const int nrm[3] = {(q & 4) ? 1 : -1, (q & 2) ? 1 : -1, (q & 1) ? 1 : -1};
-        R r[3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            int nbp[3] = {p[0], p[1], p[2]};
-            nbp[a] -= nrm[a];
-            r[a] = surfaceDensity<S, ODD>(L, nbp, pending, invRho0, bbRho);
-        }
-        rho = (R)1 / (R)3 * (r[2] + r[1] + r[0]);
-#pragma unroll
-        for (int a = 0; a < 3; ++a) normalGradient<S, ODD>(L, p, a, nrm[a], pending, invRho0, bbRho, vel, g[a]);
-    }
-    // finiteDifferenceBoundaryProcessor3D.hh:180-206
-    const R sToPi = -rho / (R)3 / omega;
-    R Pi[6];
-    Pi[0] = (R)2 * g[0][0] * sToPi;
-    Pi[1] = (g[0][1] + g[1][0]) * sToPi;
-    Pi[2] = (g[0][2] + g[2][0]) * sToPi;
-    Pi[3] = (R)2 * g[1][1] * sToPi;
-    Pi[4] = (g[1][2] + g[2][1]) * sToPi;
-    Pi[5] = (R)2 * g[2][2] * sToPi;
-    R j[3] = {rho * vel[0], rho * vel[1], rho * vel[2]};
-    const R jSqr = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
-    R f[19];
-    regularizeFromPi<R>(f, rho - (R)1, j, jSqr, Pi);
+    surfaceFromGradients<R>(rho, g, vel, omega, f);
     Neighbourhood nb = neighbourhood(L, c.x, c.y, c.z);
     S* Pp = static_cast<S*>(L.pop);
 #pragma unroll

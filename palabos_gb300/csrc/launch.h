@@ -66,7 +66,7 @@ struct DomainAccess {
     DevLattice L;
     int precision;
     bool odd, pending;
-    double omega, rho0;
+    double omega, rho0, bbRho;
     cudaStream_t stream;
     void** adjointSlot;            // per-domain storage owned by the adjoint module
     void (**adjointFree)(void*);   // its release function, called when the domain goes away
@@ -80,6 +80,9 @@ cudaStream_t contextStream(plbgpu_ctx* c);
 void countLaunches(plbgpu_ctx* c, int n);
 // After the adjoint module rewrote the populations in natural order.
 void domainSetState(plbgpu_ctx* c, int handle, bool odd, bool pending);
+// The domain's checked list of external velocity edge cells, then corner
+// cells (x, y, z, kind), rebuilt first when the kinds changed.
+int domainSurface(plbgpu_ctx* c, int handle, const int4** cells, int* nEdges, int* nCorners);
 
 // Binary-block checkpoints (checkpoint.cu): base64 of the byte stream
 // head[0..headLen) ++ body[0..bodyLen) as `quads` output quads (the last one

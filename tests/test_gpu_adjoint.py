@@ -100,7 +100,8 @@ def test_fp32_adjoint_tracks_fp64():
 def test_adjoint_rejects_unsupported_cells():
     from palabos_gb300 import DeviceLattice3D, PlbGpuError
     lat = DeviceLattice3D(6, 6, 6, 1.2)
-    lat.define_dynamics((0, 0, 0, 0, 1, 4), N.VELOCITY_EDGE)   # edges and corners have no reverse step
+    lat.define_dynamics((0, 5, 0, 5, 0, 5), N.GUO)
+    lat.define_dynamics((2, 2, 2, 2, 2, 2), N.edge_kind(0, -1, -1))   # an edge reading Guo-forced cells
     with pytest.raises(PlbGpuError):
         lat.adjoint_forward(4, 2)
     lat2 = DeviceLattice3D(6, 6, 6, 1.2)
@@ -397,6 +398,39 @@ def _face_channel(faces="regularized", omega=1.8, shape=(24, 12, 12)):
     return wl
 
 
+def _permuted(wl, perm):
+    """The workload with its axes permuted (new axis a = old axis perm[a]):
+    face kinds turned with it, velocity values rotated, densities kept."""
+    import dataclasses
+    kinds = np.ascontiguousarray(np.transpose(wl.kinds, perm))
+    bc = np.ascontiguousarray(np.transpose(wl.bcval, perm + (3,)))
+    out = kinds.copy()
+    for fam in (N.REG_VELOCITY, N.REG_PRESSURE, N.ZOUHE_VELOCITY, N.ZOUHE_PRESSURE):
+        for d in range(3):
+            for o in (-1, 1):
+                m = kinds == N.face_kind(fam, d, o)
+                out[m] = N.face_kind(fam, perm.index(d), o)
+                if fam in (N.REG_VELOCITY, N.ZOUHE_VELOCITY):
+                    bc[m] = bc[m][:, list(perm)]
+    return dataclasses.replace(wl, shape=tuple(wl.shape[a] for a in perm), kinds=out, bcval=bc,
+                               periodic=tuple(wl.periodic[a] for a in perm))
+
+
+@pytest.mark.parametrize("faces", ["regularized", "zouhe"])
+@pytest.mark.parametrize("perm", [(1, 0, 2), (2, 1, 0)])
+def test_face_adjoint_every_orientation_matches_tangent_linear(faces, perm):
+    """The channel turned to run along y and along z: the closed-form reverse
+    of the face completion for the other four face orientations."""
+    wl = _permuted(_face_channel(faces), perm)
+    lat = wl.lattice("fp64")
+    lat.collide_and_stream(3)
+    J_t, dJ = lat.tangent_linear(12, None, 0.41, drag=DRAG_DIR)
+    lat.adjoint_forward(12, 4)
+    J, _, gO, _ = lat.adjoint_backward(drag=DRAG_DIR, want_force=False)
+    assert J == pytest.approx(J_t, rel=1e-13) and J != 0.0
+    assert gO * 0.41 == pytest.approx(dJ, rel=1e-9), (gO * 0.41, dJ)
+
+
 @pytest.mark.parametrize("warm", [0, 3])
 @pytest.mark.parametrize("faces", ["regularized", "zouhe"])
 @pytest.mark.parametrize("K", [1, 5])
@@ -483,3 +517,136 @@ def test_face_adjoint_fp32_tracks_fp64():
         g[prec] = (J, gO)
     assert g["fp32"][0] == pytest.approx(g["fp64"][0], rel=1e-4)
     assert g["fp32"][1] == pytest.approx(g["fp64"][1], rel=1e-3)
+
+
+# ---------------------------------------------------------------- edges and corners
+
+def _velocity_box(shape=(12, 10, 9), omega=1.7, seed=7, precision="fp64", lid_only=False):
+    """setVelocityConditionOnBlockBoundaries over the whole box (regularized
+    velocity faces, external velocity edges and corners, all with stored
+    wall velocities), BGK next to the walls and a Guo-forced core; or
+    (lid_only) a box driven by its top face's velocity whose x = nx-1 face is
+    a regularized pressure outlet at rho = 1 (which fixes the mass, so that
+    the steady state is unique; the edges around it read the outlet's
+    computed velocity)."""
+    from palabos_gb300 import DeviceLattice3D
+    nx, ny, nz = shape
+    rng = np.random.default_rng(seed)
+    lat = DeviceLattice3D(nx, ny, nz, omega, precision)
+    lat.set_velocity_condition_on_block_boundaries()
+    force = np.zeros(shape + (3,))
+    if not lid_only:
+        lat.define_dynamics((2, nx - 3, 2, ny - 3, 2, nz - 3), N.GUO)
+        force[2:-2, 2:-2, 2:-2] = 1e-5 + 1e-6 * rng.standard_normal((nx - 4, ny - 4, nz - 4, 3))
+        lat.set_external_vector(None, force)
+        u = 0.02 * rng.standard_normal(shape + (3,))
+    else:
+        u = np.zeros(shape + (3,))
+        u[:, :, -1, 0] = 0.04
+    lat.set_boundary_velocity(None, u)
+    if lid_only:
+        outlet = (nx - 1, nx - 1, 1, ny - 2, 1, nz - 2)
+        lat.add_pressure_boundary(outlet, 0, +1)
+        lat.set_boundary_density(outlet, 1.0)      # after the velocities: the density shares their slot
+    if lid_only:
+        lat.initialize_at_equilibrium(None, 1.0, (0.0, 0.0, 0.0))
+    else:
+        rho = 1.0 + 0.01 * rng.standard_normal(shape)
+        lat.initialize_at_equilibrium(None, rho, 0.01 * rng.standard_normal(shape + (3,)))
+    lat.initialize()
+    return lat, force
+
+
+@pytest.mark.parametrize("K", [1, 4])
+def test_edge_corner_adjoint_matches_tangent_linear(K):
+    """Faces, edges and corners of a velocity box: the reverse of the edge and
+    corner processors (finite differences over the neighbours) with the rest
+    of the step, against the dual-number run, for a force direction on the
+    Guo core and omega; the domain continues bit for bit like a plain run."""
+    lat, force = _velocity_box()
+    lat.collide_and_stream(2)
+    f0 = lat.receive()
+    T = 16
+    rng = np.random.default_rng(21)
+    w = rng.standard_normal(lat.shape + (3,))
+    dF = np.zeros_like(force)
+    dF[2:-2, 2:-2, 2:-2] = rng.standard_normal(force[2:-2, 2:-2, 2:-2].shape)
+    J_t, dJ = lat.tangent_linear(T, dF, 0.6, weights=w)
+    lat.adjoint_forward(T, K)
+    J, gF, gO, _ = lat.adjoint_backward(weights=w)
+    assert J == pytest.approx(J_t, rel=1e-13) and J != 0.0
+    adj = float(np.sum(gF * dF)) + gO * 0.6
+    assert adj == pytest.approx(dJ, rel=1e-9), (adj, dJ)
+    plain, _ = _velocity_box()
+    plain.collide_and_stream(2)
+    assert np.array_equal(plain.receive(), f0)
+    plain.collide_and_stream(T)
+    assert np.array_equal(lat.receive(), plain.receive())
+
+
+def test_edge_corner_adjoint_matches_finite_differences():
+    """dJ/domega and dJ/dF against central differences of the domain's own
+    FP64 steps (the fused kernels and the edge and corner processors, bit for
+    bit the reference's arithmetic)."""
+    T = 12
+    w = np.random.default_rng(4).standard_normal((12, 10, 9, 3))
+
+    def objective(omega, force_delta=None):
+        lat, force = _velocity_box()          # the same initial state (initialize() depends on omega)
+        lat.set_params(omega)
+        if force_delta is not None:
+            lat.set_external_vector(None, force + force_delta)
+        lat.collide_and_stream(T)
+        J, _, _, _ = lat.adjoint_steady(weights=w, iterations=0, want_force=False)
+        return J
+
+    lat, force = _velocity_box()
+    lat.adjoint_forward(T, 3)
+    J, gF, gO, _ = lat.adjoint_backward(weights=w)
+    assert J == pytest.approx(objective(1.7), rel=1e-13)
+    h = 1e-6
+    fd = (objective(1.7 + h) - objective(1.7 - h)) / (2 * h)
+    assert gO == pytest.approx(fd, rel=1e-5), (gO, fd)
+    for cell, d in (((3, 4, 4), 0), ((6, 2, 5), 2), ((9, 7, 2), 1)):
+        e = np.zeros_like(force)
+        e[cell + (d,)] = 1e-7
+        fd = (objective(1.7, e) - objective(1.7, -e)) / 2e-7
+        assert gF[cell + (d,)] == pytest.approx(fd, rel=1e-5, abs=1e-9 * abs(gO)), (cell, d, gF[cell + (d,)], fd)
+
+
+def test_edge_corner_steady_adjoint():
+    """Lid-driven box with a pressure outlet at steady state: d(sum w . u)/domega
+    from the steady adjoint against central differences of converged FP64
+    runs.  (In a box closed by velocity conditions alone the mass level is a
+    neutral mode that the transient sets, which a steady adjoint cannot see.)"""
+    w = np.random.default_rng(9).standard_normal((10, 8, 8, 3))
+
+    def converged(omega):
+        lat, _ = _velocity_box((10, 8, 8), omega=omega, lid_only=True)
+        lat.collide_and_stream(8000)
+        return lat
+
+    lat = converged(1.3)
+    J, _, gO, _ = lat.adjoint_steady(weights=w, iterations=4000, want_force=False)
+    _, _, gO2, _ = lat.adjoint_steady(weights=w, iterations=8000, want_force=False)
+    assert gO2 == pytest.approx(gO, rel=1e-8)
+    h = 1e-5
+
+    def J_at(om):
+        return converged(om).adjoint_steady(weights=w, iterations=0, want_force=False)[0]
+
+    fd = (J_at(1.3 + h) - J_at(1.3 - h)) / (2 * h)
+    assert gO == pytest.approx(fd, rel=1e-5), (gO, fd)
+
+
+def test_edge_corner_adjoint_fp32_tracks_fp64():
+    w = np.random.default_rng(3).standard_normal((12, 10, 9, 3))
+    g = {}
+    for prec in ("fp64", "fp32"):
+        lat, _ = _velocity_box(precision=prec)
+        lat.adjoint_forward(20, 5)
+        J, gF, gO, _ = lat.adjoint_backward(weights=w)
+        g[prec] = (J, gF, gO)
+    assert g["fp32"][0] == pytest.approx(g["fp64"][0], rel=1e-4)
+    assert np.abs(g["fp32"][1] - g["fp64"][1]).max() <= 2e-3 * np.abs(g["fp64"][1]).max()
+    assert g["fp32"][2] == pytest.approx(g["fp64"][2], rel=2e-3)
