@@ -853,81 +853,81 @@ struct SeededSource {
     }
 };
 
+// The cells an edge or corner processor reads that carry a derivative:
+// candidate r of cell c (the inward neighbours, then for an edge the two
+// along it).  Returns the cell index, or -1 when candidate r reads nothing
+// differentiable (a wall, a cell outside the lattice, or a stored-velocity
+// cell read for its velocity only).
+__device__ __forceinline__ long long surfaceCandidate(const DevLattice& L, int4 c, int r) {
+    const bool edge = c.w < K_CORNER;
+    int axis, side;
+    bool velocityOnly = false;
+    if (edge) {
+        const int e = c.w - K_EDGE, plane = e / 4;
+        if (r == 0) { axis = (plane + 1) % 3; side = (e & 2) ? -1 : 1; }
+        else if (r == 1) { axis = (plane + 2) % 3; side = (e & 1) ? -1 : 1; }
+        else { axis = plane; side = r == 2 ? 1 : -1; velocityOnly = true; }
+    } else {
+        const int q = c.w - K_CORNER;
+        axis = r;
+        side = (q & (4 >> r)) ? -1 : 1;
+    }
+    int p[3] = {c.x, c.y, c.z};
+    p[axis] += side;
+    const long long qi = ((long long)wrapAxis(p[0], L.nx) * L.ny + wrapAxis(p[1], L.ny)) * L.nz + wrapAxis(p[2], L.nz);
+    const int k = L.flags[qi];
+    if (k == K_BB || k == K_MEBB || k == K_NODYN || k == K_NONE) return -1;
+    if (velocityOnly && isSurface(k)) return -1;
+    return qi;
+}
+
+// Number of dual passes of one edge (corner) cell: omega, then 19 per candidate.
+__host__ __device__ constexpr int surfacePasses(bool edge) { return 1 + 19 * (edge ? 4 : 3); }
+
 // Reverse of the edge (or corner) processor of one launch's cells on lambda,
-// in place, at the state f it produced: each cell's 19 adjoint values go to
-// the populations of the neighbours it read -- its inward neighbours (density
-// and velocity) and, for an edge, the two along the edge unless they store
-// their velocity -- and its own incoming populations, overwritten unread, get
-// zero.  Each neighbour population is differentiated through the whole
+// at the state f it produced, one dual pass per thread: pass 0 of a cell
+// gives the omega derivative (to gOmega), pass 1 + 19 r + j the derivative
+// with respect to population j of the cell's candidate r -- the whole
 // processor (finite differences, face completion of a pending neighbour,
-// rebuild) with one dual pass; one more pass gives the omega derivative, which
-// goes to gOmega.  Corners read edges' densities, so the corners' reverse runs
-// first.
+// rebuild) differentiated at once -- contracted with the cell's 19 adjoint
+// values and added to that population's.  The cell's own incoming
+// populations, overwritten unread, get zero afterwards (surfaceAdjointZero).
+// Corners read edges' densities, so the corners' reverse runs first.
 template <typename R>
-__global__ void surfaceAdjointKernel(DevLattice L, const R* f, R* lam, const int4* cells, int count, R invRho0,
-                                         double bbRho, R omega, AdjAcc* acc) {
+__global__ void surfaceAdjointKernel(DevLattice L, const R* f, R* lam, const int4* cells, int count, int passes,
+                                     R invRho0, double bbRho, R omega, AdjAcc* acc) {
     using D = DualT<R>;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     double go = 0.;
-    if (t < count) {
+    if (g < (long long)count * passes) {
+        const int t = (int)(g / passes), pass = (int)(g - (long long)t * passes);
         const int4 c = cells[t];
-        const int p[3] = {c.x, c.y, c.z};
         const long long idx = ((long long)c.x * L.ny + c.y) * L.nz + c.z;
-        R lo[19];
-        for (int i = 0; i < 19; ++i) {
-            lo[i] = lam[i * L.n + idx];
-            lam[i * L.n + idx] = R(0);
-        }
-        D vel[3];
-        for (int d = 0; d < 3; ++d) vel[d] = D((R)L.bc[d * L.n + idx]);
-        auto pass = [&](long long seed, int pop, bool seedOmega) {
-            SeededSource<R> src{f, L.n, seed, pop};
-            D rho, g[3][3], fo[19];
-            surfaceGradients<R, D>(L, c, 1, invRho0, bbRho, src, rho, g);
-            surfaceFromGradients<D>(rho, g, vel, D(omega, seedOmega ? 1.0 : 0.0), fo);
+        const long long qi = pass == 0 ? -1 : surfaceCandidate(L, c, (pass - 1) / 19);
+        if (pass == 0 || qi >= 0) {
+            const int j = pass == 0 ? 0 : (pass - 1) % 19;
+            SeededSource<R> src{f, L.n, qi, j};
+            D rho, gr[3][3], vel[3], fo[19];
+            surfaceGradients<R, D>(L, c, 1, invRho0, bbRho, src, rho, gr);
+            for (int d = 0; d < 3; ++d) vel[d] = D((R)L.bc[d * L.n + idx]);
+            surfaceFromGradients<D>(rho, gr, vel, D(omega, pass == 0 ? 1.0 : 0.0), fo);
             R v = R(0);
-            for (int i = 0; i < 19; ++i) v += lo[i] * fo[i].d;
-            return v;
-        };
-        go = (double)pass(-1, 0, true);
-        // the cells read: the inward neighbours (density and velocity) and, for
-        // an edge, the two along it (velocity only: nothing to differentiate
-        // when they store their velocity)
-        int nrmAxis[3], nrmSide[3], nn = 0;
-        if (c.w < K_CORNER) {
-            const int e = c.w - K_EDGE, plane = e / 4;
-            nrmAxis[0] = (plane + 1) % 3;
-            nrmSide[0] = (e & 2) ? -1 : 1;
-            nrmAxis[1] = (plane + 2) % 3;
-            nrmSide[1] = (e & 1) ? -1 : 1;
-            nrmAxis[2] = plane;
-            nn = 2;
-        } else {
-            const int q = c.w - K_CORNER;
-            for (int a = 0; a < 3; ++a) {
-                nrmAxis[a] = a;
-                nrmSide[a] = (q & (4 >> a)) ? -1 : 1;
-            }
-            nn = 3;
-        }
-        for (int r = 0; r < (c.w < K_CORNER ? 4 : 3); ++r) {
-            int q[3] = {p[0], p[1], p[2]};
-            if (r < nn) q[nrmAxis[r]] += nrmSide[r];
-            else q[nrmAxis[2]] += (r == nn ? 1 : -1);
-            {
-                const long long qi = ((long long)wrapAxis(q[0], L.nx) * L.ny + wrapAxis(q[1], L.ny)) * L.nz +
-                                     wrapAxis(q[2], L.nz);
-                const int k = L.flags[qi];
-                if (k == K_BB || k == K_MEBB || k == K_NODYN || k == K_NONE) continue;
-                if (r >= nn && isSurface(k)) continue;
-                for (int j = 0; j < 19; ++j) {
-                    const R v = pass(qi, j, false);
-                    if (v != R(0)) atomicAdd(&lam[j * L.n + qi], v);
-                }
-            }
+            for (int i = 0; i < 19; ++i) v += lam[i * L.n + idx] * fo[i].d;
+            if (pass == 0) go = (double)v;
+            else if (v != R(0)) atomicAdd(&lam[j * L.n + qi], v);
         }
     }
     blockAdd(go, acc->gOmega);
+}
+
+// The edge and corner cells' own adjoint values, once their reverse has read them.
+template <typename R>
+__global__ void surfaceAdjointZero(DevLattice L, R* lam, const int4* cells, int count) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const int4 c = cells[t];
+    const long long idx = ((long long)c.x * L.ny + c.y) * L.nz + c.z;
+    for (int i = 0; i < 19; ++i) lam[i * L.n + idx] = R(0);
 }
 
 // ---------------------------------------------------------------- host side
@@ -1114,13 +1114,20 @@ template <typename R>
 void launchSurfaceAdjoint(const DomainAccess& a, const int4* surf, int nEdges, int nCorners, const R* f, R* lam,
                           AdjAcc* acc) {
     const R invRho0 = (R)(1.0 / a.rho0), omega = (R)a.omega;
-    if (nCorners)
-        surfaceAdjointKernel<R><<<(nCorners + 63) / 64, 64, 0, a.stream>>>(a.L, f, lam, surf + nEdges, nCorners,
-                                                                         invRho0, a.bbRho, omega, acc);
-    if (nEdges)
-        surfaceAdjointKernel<R><<<(nEdges + 63) / 64, 64, 0, a.stream>>>(a.L, f, lam, surf, nEdges, invRho0, a.bbRho,
-                                                                       omega, acc);
-    *a.launches += (nEdges ? 1 : 0) + (nCorners ? 1 : 0);
+    auto reverse = [&](const int4* cells, int count, bool edge) {
+        const int passes = surfacePasses(edge);
+        const long long threads = (long long)count * passes;
+        surfaceAdjointKernel<R><<<(unsigned)((threads + 127) / 128), 128, 0, a.stream>>>(
+            a.L, f, lam, cells, count, passes, invRho0, a.bbRho, omega, acc);
+        *a.launches += 1;
+    };
+    if (nCorners) reverse(surf + nEdges, nCorners, false);
+    if (nEdges) reverse(surf, nEdges, true);
+    if (nEdges + nCorners) {
+        surfaceAdjointZero<R><<<(nEdges + nCorners + 127) / 128, 128, 0, a.stream>>>(a.L, lam, surf,
+                                                                                     nEdges + nCorners);
+        *a.launches += 1;
+    }
 }
 
 // The face cells' reverse step beside the bulk's (disjoint writes).
