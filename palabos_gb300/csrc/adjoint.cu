@@ -856,8 +856,8 @@ struct SeededSource {
 // The cells an edge or corner processor reads that carry a derivative:
 // candidate r of cell c (the inward neighbours, then for an edge the two
 // along it).  Returns the cell index, or -1 when candidate r reads nothing
-// differentiable (a wall, a cell outside the lattice, or a stored-velocity
-// cell read for its velocity only).
+// differentiable (a wall, a cell outside the lattice, or a cell that stores
+// its velocity read for its velocity only).
 __device__ __forceinline__ long long surfaceCandidate(const DevLattice& L, int4 c, int r) {
     const bool edge = c.w < K_CORNER;
     int axis, side;
@@ -877,7 +877,7 @@ __device__ __forceinline__ long long surfaceCandidate(const DevLattice& L, int4 
     const long long qi = ((long long)wrapAxis(p[0], L.nx) * L.ny + wrapAxis(p[1], L.ny)) * L.nz + wrapAxis(p[2], L.nz);
     const int k = L.flags[qi];
     if (k == K_BB || k == K_MEBB || k == K_NODYN || k == K_NONE) return -1;
-    if (velocityOnly && isSurface(k)) return -1;
+    if (velocityOnly && (isSurface(k) || (isFace(k) && (faceFamily(k) == 0 || faceFamily(k) == 2)))) return -1;
     return qi;
 }
 

@@ -1045,16 +1045,21 @@ __device__ __forceinline__ void macroOfPops(const DevLattice& L, long long idx, 
     rho = densityOfRhoBar(rb);
 }
 
-// Velocity of the cell at p (wrapped): the stored velocity of an edge or
-// corner (no population read), else computeVelocity.
+// Velocity of the cell at p (wrapped): the stored velocity of an edge, a
+// corner or a velocity face and the zero of a wall, without reading
+// populations (the values macroOfPops gives them), else computeVelocity.
 template <typename R, typename T, class Src>
 __device__ __forceinline__ void surfaceVelocityAt(const DevLattice& L, const int* p, int pending, R invRho0,
                                                   double bbRho, Src& src, T* u) {
     const long long idx = ((long long)wrapAxis(p[0], L.nx) * L.ny + wrapAxis(p[1], L.ny)) * L.nz + wrapAxis(p[2], L.nz);
     const int k = L.flags[idx];
-    if (isSurface(k)) {
+    if (isSurface(k) || (isFace(k) && (faceFamily(k) == 0 || faceFamily(k) == 2))) {
 #pragma unroll
         for (int d = 0; d < 3; ++d) u[d] = T((R)L.bc[d * L.n + idx]);
+        return;
+    }
+    if (k == K_BB || k == K_MEBB || k == K_NODYN || k == K_NONE) {
+        u[0] = u[1] = u[2] = T(0);
         return;
     }
     T f[19], rho;
@@ -1062,14 +1067,16 @@ __device__ __forceinline__ void surfaceVelocityAt(const DevLattice& L, const int
     macroOfPops<R, T>(L, idx, k, f, pending, invRho0, bbRho, u, rho);
 }
 
-// Density of the cell at p (wrapped).
+// Density of the cell at p (wrapped); a wall's without reading populations.
 template <typename R, typename T, class Src>
 __device__ __forceinline__ T surfaceDensityAt(const DevLattice& L, const int* p, int pending, R invRho0, double bbRho,
                                               Src& src) {
     const long long idx = ((long long)wrapAxis(p[0], L.nx) * L.ny + wrapAxis(p[1], L.ny)) * L.nz + wrapAxis(p[2], L.nz);
+    const int k = L.flags[idx];
+    if (k == K_BB || k == K_MEBB || k == K_NODYN || k == K_NONE) return T((R)bbRho);
     T f[19], u[3], rho;
     src(idx, f);
-    macroOfPops<R, T>(L, idx, L.flags[idx], f, pending, invRho0, bbRho, u, rho);
+    macroOfPops<R, T>(L, idx, k, f, pending, invRho0, bbRho, u, rho);
     return rho;
 }
 
