@@ -817,7 +817,7 @@ template <typename T>
 struct NatSource {
     const T* buf;
     long long n;
-    __device__ __forceinline__ void operator()(long long idx, T* f) const {
+    __device__ __forceinline__ void operator()(int, int, int, long long idx, T* f) const {
 #pragma unroll
         for (int i = 0; i < 19; ++i) f[i] = buf[i * n + idx];
     }
@@ -847,7 +847,7 @@ struct SeededSource {
     const R* buf;
     long long n, seed;
     int pop;
-    __device__ __forceinline__ void operator()(long long idx, DualT<R>* f) const {
+    __device__ __forceinline__ void operator()(int, int, int, long long idx, DualT<R>* f) const {
 #pragma unroll
         for (int i = 0; i < 19; ++i) f[i] = DualT<R>(buf[i * n + idx], (idx == seed && i == pop) ? 1.0 : 0.0);
     }

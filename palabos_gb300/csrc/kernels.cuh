@@ -982,7 +982,8 @@ __device__ __forceinline__ bool cellMacroscopic(const DevLattice& L, int x, int 
 //
 // The processor is written once for any arithmetic type T (the form's R, or
 // a dual number of R in the adjoint module) and any population source: a
-// source `src(idx, f)` loads the raw post-stream populations of cell idx into
+// source `src(x, y, z, idx, f)` loads the raw post-stream populations of cell
+// (x, y, z) = idx into
 // f[19].
 
 __device__ __forceinline__ int wrapAxis(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
@@ -1051,7 +1052,8 @@ __device__ __forceinline__ void macroOfPops(const DevLattice& L, long long idx, 
 template <typename R, typename T, class Src>
 __device__ __forceinline__ void surfaceVelocityAt(const DevLattice& L, const int* p, int pending, R invRho0,
                                                   double bbRho, Src& src, T* u) {
-    const long long idx = ((long long)wrapAxis(p[0], L.nx) * L.ny + wrapAxis(p[1], L.ny)) * L.nz + wrapAxis(p[2], L.nz);
+    const int x = wrapAxis(p[0], L.nx), y = wrapAxis(p[1], L.ny), z = wrapAxis(p[2], L.nz);
+    const long long idx = ((long long)x * L.ny + y) * L.nz + z;
     const int k = L.flags[idx];
     if (isSurface(k) || (isFace(k) && (faceFamily(k) == 0 || faceFamily(k) == 2))) {
 #pragma unroll
@@ -1063,7 +1065,7 @@ __device__ __forceinline__ void surfaceVelocityAt(const DevLattice& L, const int
         return;
     }
     T f[19], rho;
-    src(idx, f);
+    src(x, y, z, idx, f);
     macroOfPops<R, T>(L, idx, k, f, pending, invRho0, bbRho, u, rho);
 }
 
@@ -1071,11 +1073,12 @@ __device__ __forceinline__ void surfaceVelocityAt(const DevLattice& L, const int
 template <typename R, typename T, class Src>
 __device__ __forceinline__ T surfaceDensityAt(const DevLattice& L, const int* p, int pending, R invRho0, double bbRho,
                                               Src& src) {
-    const long long idx = ((long long)wrapAxis(p[0], L.nx) * L.ny + wrapAxis(p[1], L.ny)) * L.nz + wrapAxis(p[2], L.nz);
+    const int x = wrapAxis(p[0], L.nx), y = wrapAxis(p[1], L.ny), z = wrapAxis(p[2], L.nz);
+    const long long idx = ((long long)x * L.ny + y) * L.nz + z;
     const int k = L.flags[idx];
     if (k == K_BB || k == K_MEBB || k == K_NODYN || k == K_NONE) return T((R)bbRho);
     T f[19], u[3], rho;
-    src(idx, f);
+    src(x, y, z, idx, f);
     macroOfPops<R, T>(L, idx, k, f, pending, invRho0, bbRho, u, rho);
     return rho;
 }
@@ -1160,8 +1163,7 @@ __device__ __forceinline__ void surfaceFromGradients(const T& rho, const T (&g)[
 template <typename S, bool ODD>
 struct AASource {
     const DevLattice& L;
-    __device__ __forceinline__ void operator()(long long idx, typename StoreT<S>::R* f) const {
-        const int z = (int)(idx % L.nz), y = (int)((idx / L.nz) % L.ny), x = (int)(idx / ((long long)L.ny * L.nz));
+    __device__ __forceinline__ void operator()(int x, int y, int z, long long idx, typename StoreT<S>::R* f) const {
         Neighbourhood nb = neighbourhood(L, x, y, z);
         const S* Pp = static_cast<const S*>(L.pop);
 #pragma unroll
