@@ -415,11 +415,16 @@ def run_gpu(args):
             forms[prec] = {"mlups": round(cells / (ms * 1e-3) / 1e6, 1), "bytes_per_cell": B_CELL[prec],
                            "hbm_frac": round(b / (ms * 1e-3) / 1e9 / peak, 4)}
             l2.close()
-        # accuracy of each storage form against FP64 on a 128^3 Taylor-Green vortex
+        # accuracy of each storage form against FP64 on the Taylor-Green vortex (u0 0.04,
+        # Re 1600) at 256^3 for 2500 steps: with u0 and Re fixed, the viscous time of the
+        # 512^3 x 5000-step configuration
         from palabos_gb300.accuracy import taylor_green_study
-        tg = taylor_green_study(n=128, steps=1000, every=250, slab=32, ctx=ctx)
+        tg = taylor_green_study(n=256, steps=2500, every=500, slab=16, ctx=ctx)
         for prec, acc in tg["forms"].items():
-            forms[prec]["taylor_green_128_1000steps"] = {k: round(v, 9) for k, v in acc.items()}
+            forms[prec]["taylor_green_256_2500steps"] = {k: round(v, 9) for k, v in acc.items()}
+        met = sorted(p for p, a in tg["forms"].items() if a["vel_l2_rel"] <= 1e-3)
+        forms["accuracy_bound"] = {"criterion": "velocity L2 <= 1e-3 relative to FP64, Taylor-Green 256^3 x 2500",
+                                   "meets": met, "fails": sorted(set(tg["forms"]) - set(met))}
 
     adjoint = None if args.skip_adjoint else adjoint_cost(ctx)
 
