@@ -316,6 +316,21 @@ def sparse_throughput(n=256, radius=110.0, block=16, steps=200, precisions=("fp6
     return out
 
 
+def cavity_throughput(n=64, steps=1000, precisions=("fp64", "fp32", "bf16", "fp16"), ctx=None):
+    """The lid-driven cavity (bounce-back on five walls, regularized velocity lid
+    u = (0.02, 0, 0), Re 100, from rest): MLUPS of `steps` steps per storage form."""
+    from palabos_gb300 import workloads
+    wl = workloads.cavity(n)
+    out = {"workload": f"lid_driven_cavity_{n}^3_re100", "steps": steps}
+    for prec in precisions:
+        lat = wl.lattice(prec, ctx)
+        lat.collide_and_stream(10)
+        ms = lat.time_steps(steps) / steps
+        out[prec] = {"mlups": round(n ** 3 / (ms * 1e-3) / 1e6, 1), "ms_per_step": round(ms, 5)}
+        lat.close()
+    return out
+
+
 def run_gpu(args):
     ws, rank, local = dist_env()
     dist = init_dist(ws)
@@ -504,6 +519,9 @@ def main():
     ap.add_argument("--drag-gradient-steps", type=int, default=10000)
     ap.add_argument("--sparse", action="store_true",
                     help="run only the sparse-domain throughput study (voxelized sphere exterior, 256^3)")
+    ap.add_argument("--cavity", action="store_true",
+                    help="run only the lid-driven cavity throughput study (64^3, 1000 steps per storage form)")
+    ap.add_argument("--cavity-n", type=int, default=64)
     ap.add_argument("--sparse-steps", type=int, default=200)
     ap.add_argument("--sparse-precisions", nargs="+", default=["fp64", "fp32", "bf16"],
                     choices=["fp64", "fp32", "bf16", "fp16", "bf16sr"])
@@ -523,6 +541,11 @@ def main():
         ctx = Context(dist_env()[2])
         r = drag_gradient_study(steps=args.drag_gradient_steps, ctx=ctx)
         print(json.dumps({"study": "channel_sphere_drag_gradient", **r}))
+        return
+    if args.cavity:
+        from palabos_gb300 import Context
+        ctx = Context(dist_env()[2])
+        print(json.dumps({"study": "lid_driven_cavity", **cavity_throughput(n=args.cavity_n, ctx=ctx)}))
         return
     if args.sparse:
         from palabos_gb300 import Context

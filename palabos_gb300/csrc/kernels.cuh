@@ -152,6 +152,8 @@ struct DevLattice {
     int per[3];
     long long n;
     unsigned* status;       // device error word (kStatusNonFinite)
+    int rowFacesDone;       // the face cells of interior rows were completed before this launch
+                            // (completeFaceListKernel): the interior-row kernels skip their completion
     int rowForm;            // interior-row kernel: 0 the default (two cells per thread for the 2-byte
                             // forms), 1 one cell per thread (every form), 2 / 4 four / eight cells per
                             // thread with 64- / 128-bit vectors (2-byte forms, rows of 8k cells), 3 two
@@ -646,7 +648,7 @@ __global__ void __launch_bounds__(128, RowShape<S>::blocks)
         RowCell<S, ODD, MASKED> rc(L, x, y, z0 + c * blockDim.x);
         rc.gone = gone;
         R rhoBar = R(0), uSqr = R(0);
-        if (P.pending && isFace(kind[c])) completeIfFace<R>(L, rc.idx, kind[c], f[c]);
+        if (P.pending && !L.rowFacesDone && isFace(kind[c])) completeIfFace<R>(L, rc.idx, kind[c], f[c]);
         bool g = collideCell<S, EXT>(L, P, rc.idx, kind[c], f[c], rhoBar, uSqr, acc, STATS);
         rc.store(Pl, D, f[c], P.seed);
         if (STATS && g) {
@@ -718,11 +720,11 @@ __global__ void __launch_bounds__(128, 8)
         R rbA = R(0), usA = R(0), rbB = R(0), usB = R(0);
         bool gA = false, gB = false;
         if (liveA) {
-            if (P.pending && isFace(kA)) completeIfFace<R>(L, ca.idx, kA, fa);
+            if (P.pending && !L.rowFacesDone && isFace(kA)) completeIfFace<R>(L, ca.idx, kA, fa);
             gA = collideCell<S, EXT>(L, P, ca.idx, kA, fa, rbA, usA, acc, STATS);
         }
         if (liveB) {
-            if (P.pending && isFace(kB)) completeIfFace<R>(L, cb.idx, kB, fb);
+            if (P.pending && !L.rowFacesDone && isFace(kB)) completeIfFace<R>(L, cb.idx, kB, fb);
             gB = collideCell<S, EXT>(L, P, cb.idx, kB, fb, rbB, usB, acc, STATS);
         }
         if (liveA && liveB) {
@@ -827,6 +829,28 @@ __global__ void completeFacesKernel(DevLattice L) {
 #pragma unroll
     for (int i = 0; i < 19; ++i) f[i] = StoreT<S>::ld(Pp + slotOf<ODD>(L, nb, idx, i));
     completeIfFace<R>(L, idx, k, f);
+#pragma unroll
+    for (int i = 0; i < 19; ++i) StoreT<S>::st(Pp + slotOf<ODD>(L, nb, idx, i), f[i]);
+}
+
+// The face cells of a list (x, y, z, kind), completed in place before a step:
+// the interior-row kernels then find them complete.  A face cell inside an
+// interior row (a lid or a face plane across the rows) would otherwise make
+// its warp run the completion for one lane while the others wait; listed, the
+// completions run in full warps.
+template <typename S, bool ODD>
+__global__ void completeFaceListKernel(DevLattice L, const int4* __restrict__ cells, int count) {
+    using R = typename StoreT<S>::R;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const int4 c = cells[t];
+    const long long idx = ((long long)c.x * L.ny + c.y) * L.nz + c.z;
+    Neighbourhood nb = neighbourhood(L, c.x, c.y, c.z);
+    S* Pp = static_cast<S*>(L.pop);
+    R f[19];
+#pragma unroll
+    for (int i = 0; i < 19; ++i) f[i] = StoreT<S>::ld(Pp + slotOf<ODD>(L, nb, idx, i));
+    completeIfFace<R>(L, idx, c.w, f);
 #pragma unroll
     for (int i = 0; i < 19; ++i) StoreT<S>::st(Pp + slotOf<ODD>(L, nb, idx, i), f[i]);
 }

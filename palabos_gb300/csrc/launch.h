@@ -47,6 +47,8 @@ struct Launchers {
     // The transfer layout with FP32 records (the single-precision co-processor form).
     int (*extractF32)(const DevLattice&, bool odd, Box, int pending, float* out, cudaStream_t);
     int (*insertF32)(const DevLattice&, bool odd, Box, const float* in, cudaStream_t);
+    // Face cells (x, y, z, kind) of interior rows completed in place before a step.
+    int (*completeFaceList)(const DevLattice&, bool odd, const int4* cells, int count, cudaStream_t);
 };
 
 const Launchers& launchersFp64();

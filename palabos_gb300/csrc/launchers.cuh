@@ -140,9 +140,17 @@ struct LaunchImpl {
             surfaceKernel<S, false><<<blocks, tpb, 0, s>>>(L, cells, count, pending, (R)invRho0, bbRho, (R)omega);
         return 1;
     }
+    static int completeFaceList(const DevLattice& L, bool odd, const int4* cells, int count, cudaStream_t s) {
+        if (count <= 0) return 0;
+        const unsigned blocks = (unsigned)((count + kBlock - 1) / kBlock);
+        if (odd) completeFaceListKernel<S, true><<<blocks, kBlock, 0, s>>>(L, cells, count);
+        else completeFaceListKernel<S, false><<<blocks, kBlock, 0, s>>>(L, cells, count);
+        return 1;
+    }
     static const Launchers& table() {
         static const Launchers t = {step,  completeFaces, extract, insert, reduce,
-                                    equilibrium, field, rhoBarJ, surface, extractF32, insertF32};
+                                    equilibrium, field, rhoBarJ, surface, extractF32, insertF32,
+                                    completeFaceList};
         return t;
     }
 };

@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(128, VecShape<CPT>::blocks)
         for (int i = 0; i < 19; ++i) f[i] = Half16<S>::get(v[i].w[w], hi);
         const int idx = idx0 + c;
         R rhoBar = R(0), uSqr = R(0);
-        if (P.pending && isFace(k)) completeIfFace<R>(L, idx, k, f);
+        if (P.pending && !L.rowFacesDone && isFace(k)) completeIfFace<R>(L, idx, k, f);
         const bool gathers = collideCell<S, EXT>(L, P, idx, k, f, rhoBar, uSqr, acc, STATS && live2);
 #pragma unroll
         for (int i = 0; i < 19; ++i) v[i].w[w] = Half16<S>::put(v[i].w[w], hi, f[i], Pl.p[i] + idx, P.seed);
