@@ -440,6 +440,19 @@ def run_gpu(args):
         met = sorted(p for p, a in tg["forms"].items() if a["vel_l2_rel"] <= 1e-3)
         forms["accuracy_bound"] = {"criterion": "velocity L2 <= 1e-3 relative to FP64, Taylor-Green 256^3 x 2500",
                                    "meets": met, "fails": sorted(set(tg["forms"]) - set(met))}
+        # the benchmark's own quantity: the momentum-exchange drag after the full
+        # 10000 steps of the channel, FP32 storage against FP64
+        drag = {}
+        for prec in ("fp64", "fp32"):
+            l2, _ = build_lattice(prec, ctx)
+            l2.collide_and_stream(9999)
+            l2.collide_and_stream(1, stats=True)
+            drag[prec] = l2.internal_statistics()["drag"].tolist()
+            l2.close()
+        ref = np.asarray(drag["fp64"])
+        forms["drag_channel_10000_steps"] = {
+            "fp64": drag["fp64"], "fp32": drag["fp32"],
+            "fp32_rel_err": float(np.linalg.norm(np.asarray(drag["fp32"]) - ref) / np.linalg.norm(ref))}
 
     adjoint = None if args.skip_adjoint else adjoint_cost(ctx)
 
