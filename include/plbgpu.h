@@ -186,8 +186,12 @@ int plbgpu_load_processors(plbgpu_ctx* ctx, int handle, const char* plb_path);
  * never updated, read back as zeros, count in no reduction or statistic, and
  * their neighbours treat them like the outside of a non-periodic domain (the
  * domain-edge rule).  keep (optional, bx*by*bz entries, x-major) receives the
- * selection.  Steps on a sparse domain use the general addressing for every
- * row. */
+ * selection.  Steps on a sparse domain go by 32-cell row tiles, rebuilt when
+ * the kinds or the periodicity change: tiles whose neighbourhood lies in the
+ * lattice take the interior-row kernels, the other tiles of interior rows the
+ * one-cell row kernel with per-cell masks of the neighbours outside the
+ * lattice, the tiles of border rows the general addressing; tiles without a
+ * live cell are not stepped. */
 int plbgpu_select_sparse_blocks(plbgpu_ctx* ctx, int handle, const int32_t* field, size_t n, int bx, int by,
                                 int bz, uint8_t* keep, size_t nblocks);
 
