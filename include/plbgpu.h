@@ -400,9 +400,12 @@ int plbgpu_voxelize(plbgpu_ctx* ctx, const double* triangles, size_t n_triangles
 
 /* Discrete adjoint of the collide-and-stream step (no counterpart in the
  * reference), for domains of BGK, Guo, incompressible BGK, bounce-back,
- * momentum-exchange bounce-back, no-dynamics and regularized or Zou/He
- * velocity and pressure face cells (edges and corners are refused; face
- * cells count as zero velocity in the velocity objectives).  The objective is J = 1/2 sum over cells |u(T) - u*|^2
+ * momentum-exchange bounce-back, no-dynamics, regularized or Zou/He velocity
+ * and pressure face cells, and the external velocity edges and corners
+ * (their finite-difference processors replayed after each step and
+ * reversed; an edge or corner next to a Guo-forced cell is refused).  Face,
+ * edge and corner cells count as zero velocity in the velocity objectives.
+ * The objective is J = 1/2 sum over cells |u(T) - u*|^2
  * with u the velocity each cell's dynamics reports (computeVelocity,
  * dataProcessors/dataAnalysisWrapper3D.h:127-132).
  *
