@@ -940,6 +940,9 @@ struct AdjointState {
     int T = 0, K = 0, nckpt = 0;
     void* ckpt = nullptr;      // (nckpt) states
     void* seg = nullptr;       // (K + 1) states
+    void* seg2 = nullptr;      // a second segment, recomputed beside the reverse of the first (or null)
+    cudaStream_t side = nullptr;   // the stream that recomputes the next segment
+    cudaEvent_t fork = nullptr, join = nullptr;
     void* lam = nullptr;       // 2 states
     void* gF = nullptr;        // 3 planes
     double* uT = nullptr;      // target velocity, n * 3
@@ -952,7 +955,10 @@ struct AdjointState {
     bool ready = false;        // a forward run is recorded
     ~AdjointState() {
         cudaFree(ckpt); cudaFree(seg); cudaFree(lam); cudaFree(gF); cudaFree(uT); cudaFree(acc); cudaFree(faces);
-        cudaFree(surf);
+        cudaFree(surf); cudaFree(seg2);
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
+        if (side) cudaStreamDestroy(side);
     }
     // Steps after the first collide states that came from a streaming step:
     // their faces are completed first.
@@ -1099,13 +1105,15 @@ int copySurface(plbgpu_ctx* c, int h, const DomainAccess& a, int4** dst, int* nE
 // The edge processors, then the corner processors, on a natural-order state
 // just pushed.
 template <typename R, typename T>
-void launchSurfaceNat(const DomainAccess& a, const int4* surf, int nEdges, int nCorners, T* buf, T omega) {
+void launchSurfaceNat(const DomainAccess& a, const int4* surf, int nEdges, int nCorners, T* buf, T omega,
+                      cudaStream_t stream = nullptr) {
     const R invRho0 = (R)(1.0 / a.rho0);
+    cudaStream_t s = stream ? stream : a.stream;
     if (nEdges)
-        surfaceNatKernel<R, T><<<(nEdges + 63) / 64, 64, 0, a.stream>>>(a.L, buf, surf, nEdges, invRho0, a.bbRho, omega);
+        surfaceNatKernel<R, T><<<(nEdges + 63) / 64, 64, 0, s>>>(a.L, buf, surf, nEdges, invRho0, a.bbRho, omega);
     if (nCorners)
-        surfaceNatKernel<R, T><<<(nCorners + 63) / 64, 64, 0, a.stream>>>(a.L, buf, surf + nEdges, nCorners, invRho0,
-                                                                        a.bbRho, omega);
+        surfaceNatKernel<R, T><<<(nCorners + 63) / 64, 64, 0, s>>>(a.L, buf, surf + nEdges, nCorners, invRho0,
+                                                                   a.bbRho, omega);
     *a.launches += (nEdges ? 1 : 0) + (nCorners ? 1 : 0);
 }
 
@@ -1209,21 +1217,40 @@ int backwardImpl(DomainAccess& a, AdjointState* st, const Objective& o, double* 
     const R omega = (R)a.omega, invRho0 = (R)(1.0 / a.rho0);
     const NeighbourDeltas D = deltasOf(a.L);
     const int T = st->T, K = st->K;
+    // Segment s holds f^{sK+1} .. f^{sK+K-1}; with a second segment buffer the
+    // side stream recomputes segment s-1 while the main stream reverses
+    // segment s (both kernels are latency-bound at a third of the warp slots,
+    // so they share the SMs), otherwise each segment is recomputed first.
+    R* sg2 = static_cast<R*>(st->seg2);
+    const bool overlap = sg2 && st->side && st->fork && st->join && K > 1;
+    auto segBuf = [&](int s) { return overlap && (s & 1) ? sg2 : sg; };
+    auto stateOf = [&](int s, int k) {
+        return k == 0 ? ck + (long long)s * sz : (k == K ? ck + (long long)(s + 1) * sz : segBuf(s) + k * sz);
+    };
+    auto recompute = [&](int s, cudaStream_t strm) {
+        for (int k = 0; k + 1 < K; ++k) {
+            pushStepKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, strm>>>(
+                a.L, D, stateOf(s, k), stateOf(s, k + 1), omega, invRho0, nullptr, st->pendingAt((long long)s * K + k));
+            *a.launches += 1;
+            launchSurfaceNat<R, R>(a, st->surf, st->nEdges, st->nCorners, stateOf(s, k + 1), omega, strm);
+        }
+    };
     auto sweep = [&]() {
         cudaMemsetAsync(gF, 0, sizeof(R) * 3 * n, a.stream);
         cudaMemsetAsync(st->acc, 0, sizeof(AdjAcc), a.stream);
         launchObjective<R>(a, o, ck + (long long)(T / K) * sz, st->uT, lam, gF, st->acc);
         int cur = 0;   // lam + cur * sz holds lambda^{t+1}
+        if (overlap) recompute(T / K - 1, a.stream);
         for (int s = T / K - 1; s >= 0; --s) {
-            // f^{sK} is checkpoint s; recompute f^{sK+1} .. f^{sK+K-1} into seg
-            auto state = [&](int k) {
-                return k == 0 ? ck + (long long)s * sz : (k == K ? ck + (long long)(s + 1) * sz : sg + k * sz);
-            };
-            for (int k = 0; k + 1 < K; ++k) {
-                pushStepKernel<R><<<cellGrid(a.L), cellBlock(a.L), 0, a.stream>>>(
-                    a.L, D, state(k), state(k + 1), omega, invRho0, nullptr, st->pendingAt((long long)s * K + k));
-                *a.launches += 1;
-                launchSurfaceNat<R, R>(a, st->surf, st->nEdges, st->nCorners, state(k + 1), omega);
+            auto state = [&](int k) { return stateOf(s, k); };
+            if (!overlap) {
+                recompute(s, a.stream);
+            } else if (s > 0) {
+                // segment s-1 goes into the buffer segment s+1 used, whose reverse is done
+                cudaEventRecord(st->fork, a.stream);
+                cudaStreamWaitEvent(st->side, st->fork, 0);
+                recompute(s - 1, st->side);
+                cudaEventRecord(st->join, st->side);
             }
             for (int k = K - 1; k >= 0; --k) {
                 // the edge and corner processors that finished step k, reversed at the state they produced
@@ -1235,6 +1262,7 @@ int backwardImpl(DomainAccess& a, AdjointState* st, const Objective& o, double* 
                                      st->pendingAt((long long)s * K + k), st->acc);
                 cur = 1 - cur;
             }
+            if (overlap && s > 0) cudaStreamWaitEvent(a.stream, st->join, 0);   // segment s-1 is ready
         }
     };
     // The sweep is captured once into a CUDA graph and launched as one unit
@@ -1497,7 +1525,20 @@ int plbgpu_adjoint_forward(plbgpu_ctx* c, int h, int T, int K) {
         st->nckpt = nckpt;
         st->K = K;
         ADJ_TRY(cudaMalloc(&st->ckpt, rs * sz * nckpt));
-        if (K > 1) ADJ_TRY(cudaMalloc(&st->seg, rs * sz * std::max(K, 2)));
+        if (K > 1) {
+            ADJ_TRY(cudaMalloc(&st->seg, rs * sz * std::max(K, 2)));
+            // a second segment where memory allows: recomputation beside the reverse
+            size_t freeB = 0, totalB = 0;
+            if (cudaMemGetInfo(&freeB, &totalB) == cudaSuccess &&
+                (double)freeB > 1.25 * (double)(rs * sz * (size_t)std::max(K, 2)) &&
+                cudaMalloc(&st->seg2, rs * sz * std::max(K, 2)) == cudaSuccess &&
+                cudaStreamCreateWithFlags(&st->side, cudaStreamNonBlocking) == cudaSuccess &&
+                cudaEventCreateWithFlags(&st->fork, cudaEventDisableTiming) == cudaSuccess &&
+                cudaEventCreateWithFlags(&st->join, cudaEventDisableTiming) == cudaSuccess) {
+            } else {
+                (void)cudaGetLastError();
+            }
+        }
         ADJ_TRY(cudaMalloc(&st->lam, rs * sz * 2));
         ADJ_TRY(cudaMalloc(&st->gF, rs * 3 * n));
         ADJ_TRY(cudaMalloc(&st->uT, sizeof(double) * 3 * n));
