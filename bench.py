@@ -16,9 +16,12 @@ Prints one JSON line (rank 0).  `value` = MLUPS of the FP64 form with the
 state resident in HBM; `e2e` = the same metric through the C ABI with host
 buffers (the FP64 state in pinned host memory allocated before the timed
 region -- sent at the start, drag read back every 100 steps, state received at
-the end into the same buffer, all inside the timed region; on a GB300 the
-transfer kernels read and write the host buffer directly over NVLink-C2C;
-`e2e.pageable` repeats the run with an ordinary numpy array).  The FP64 form is bound by the
+the end into the same buffer, all inside the timed region, in one
+plbgpu_run_host call that overlaps the send with the first step and the
+receive with the last; on a GB300 the transfer kernels read and write the host
+buffer directly over NVLink-C2C; `e2e.sequential` times plbgpu_send,
+plbgpu_collide_and_stream and plbgpu_receive one after another and
+`e2e.pageable` repeats both with an ordinary numpy array).  The FP64 form is bound by the
 FP64 pipe, not by HBM: its `roofline` compares the algorithmic FP64 adds and
 multiplies per second with the pipe rate the library measures in the same run
 (plbgpu_measure_fp64_rate), and carries the HBM fraction beside it.
@@ -397,6 +400,18 @@ def run_gpu(args):
         return (round(ws * cells * e2e_steps / e2e_s / 1e6, 2), round(state_bytes / (t_sent - t0) / 1e9, 1),
                 round(state_bytes / (t1 - t_recv) / 1e9, 1))
 
+    def e2e_overlapped(f_host):
+        # plbgpu_run_host: the same send, K steps with the drag every 100
+        # steps and receive in one call; the send overlaps the first step and
+        # the receive the last, slab by slab
+        lat.receive(out=f_host)
+        barrier(dist)
+        t0 = time.perf_counter()
+        _, recs = lat.run_host(f_host, e2e_steps, STATS_EVERY, out=f_host)
+        t1 = time.perf_counter()
+        assert len(recs) == nread
+        return round(ws * cells * e2e_steps / max_over_ranks(dist, t1 - t0) / 1e6, 2)
+
     try:
         import torch
         pinned = torch.empty(SHAPE + (19,), dtype=torch.float64, pin_memory=True).numpy()
@@ -404,17 +419,23 @@ def run_gpu(args):
         host_kind = "pinned"
     except Exception:   # no torch or no pinned allocation: pageable only
         pinned, host_kind = np.zeros(SHAPE + (19,)), "pageable"
-    v_e2e, h2d, d2h = e2e_run(pinned)
+    v_seq, h2d, d2h = e2e_run(pinned)
+    v_e2e = e2e_overlapped(pinned)
     pageable = np.zeros(SHAPE + (19,))
-    v_pg, h2d_pg, d2h_pg = e2e_run(pageable)
+    v_pg_seq, h2d_pg, d2h_pg = e2e_run(pageable)
+    v_pg = e2e_overlapped(pageable)
     e2e = {"value": v_e2e, "unit": "MLUPS",
            "h2d_bytes_per_step": round(state_bytes / e2e_steps, 1),
            "d2h_bytes_per_step": round((state_bytes + 56 * nread) / e2e_steps, 1),
-           "h2d_gbs": h2d, "d2h_gbs": d2h, "host_memory": host_kind,
-           "pageable": {"value": v_pg, "h2d_gbs": h2d_pg, "d2h_gbs": d2h_pg},
+           "host_memory": host_kind,
+           "sequential": {"value": v_seq, "h2d_gbs": h2d, "d2h_gbs": d2h},
+           "pageable": {"value": v_pg, "sequential": v_pg_seq, "h2d_gbs": h2d_pg, "d2h_gbs": d2h_pg},
            "note": f"FP64 state in {host_kind} host memory, sent once and received once per run of K steps "
-                   "(the transfer kernels read and write the host buffer directly over NVLink-C2C); drag read "
-                   "every 100 steps; 'pageable' repeats it with an ordinary numpy array"}
+                   "through plbgpu_run_host (x-slabs copied over NVLink-C2C by a copy kernel on a few SMs, the send "
+                   "overlapped with a ramp of the first two steps and the receive with a ramp of the last two); "
+                   "drag read every 100 steps; 'sequential' = plbgpu_send, plbgpu_collide_and_stream "
+                   "and plbgpu_receive called one after another; 'pageable' repeats both with an ordinary "
+                   "numpy array"}
     del pinned, pageable
     lat.close()
 

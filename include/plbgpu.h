@@ -265,6 +265,28 @@ int plbgpu_receive_f32(plbgpu_ctx* ctx, int handle, int x0, int x1, int y0, int 
  * of the nsteps steps.  Asynchronous: returns once the work is queued. */
 int plbgpu_collide_and_stream(plbgpu_ctx* ctx, int handle, int nsteps, int collect_stats);
 
+/* The co-processor cycle transferToCoProcessors -> nsteps x collideAndStream
+ * -> transferFromCoProcessors (coProcessors/coProcessorCommunication3D.hh:
+ * 34-70, multiBlock/multiBlockLattice3D.hh:318-357) in one call: the whole
+ * domain's records `in` (n = 19 per cell, the plbgpu_send layout) are sent,
+ * nsteps steps run, and the state is received into `out` (which may be `in`).
+ * With stats_every > 0 the statistics of every stats_every-th step and of the
+ * last step are written to `stats`, 7 doubles each in the plbgpu_get_stats
+ * layout (ceil(nsteps / stats_every) records, nstats doubles available).  The
+ * result is bit for bit that of plbgpu_send, plbgpu_collide_and_stream and
+ * plbgpu_receive.  When the GPU addresses both buffers directly (device or
+ * pinned memory, or any host memory on a GB300), the domain has no edges,
+ * corners or dropped blocks and its form is not PLBGPU_BF16_SR (whose random
+ * rounding bits depend on the kernel that stores a slot), the transfers
+ * overlap the steps: the domain is cut into x-slabs moved by a copy kernel
+ * on a few SMs through a ring of four slab-sized staging slots; slab j takes
+ * its first step once its records are in and step s once slabs j - 1 .. j + 1
+ * took step s - 1, so the first steps run as a ramp behind the send, and the
+ * last steps as a ramp that finishes slab 0 first, each slab received while
+ * the later ones step. */
+int plbgpu_run_host(plbgpu_ctx* ctx, int handle, const double* in, double* out, size_t n, int nsteps,
+                    int stats_every, double* stats, size_t nstats);
+
 /* Statistics of the last step that gathered them (BlockStatistics::evaluate,
  * core/blockStatistics.cpp:77-110; MultiBlock3D::getInternalStatistics):
  * out[0] average rho-bar, out[1] average u^2, out[2] max u^2,

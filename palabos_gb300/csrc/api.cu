@@ -121,6 +121,8 @@ struct Domain {
         L.n = n;
         L.status = status;
         L.rowForm = 0;
+        L.xRow0 = 0;
+        L.xRows = nx - 2;
         L.rowFacesDone = 0;
         const bool lists = sparse && tileLists;
         L.denseTiles = lists && nDense ? tileLists : nullptr;
@@ -149,6 +151,8 @@ struct plbgpu_ctx {
     bool pageableAccess = false; // kernels may dereference pageable host memory (host page tables)
     bool forceStaged = false;    // PLBGPU_STAGED_TRANSFERS=1: always go through the staging buffer
     int rowForm = 0;             // PLBGPU_ROW_KERNEL=cell: one-cell interior-row kernels (DevLattice::rowForm)
+    std::vector<cudaEvent_t> slabEvents;   // plbgpu_run_host: four per slab, created on first use
+    cudaStream_t xfer = nullptr;           // plbgpu_run_host: the host copies (highest priority, created on first use)
 };
 
 namespace {
@@ -652,6 +656,10 @@ int buildSurface(plbgpu_ctx* c, Domain* d) {
 constexpr int kGraphSteps = 16;
 constexpr int kGraphMinReplays = 2;
 
+// Salt of the stochastically rounded stores of the step that follows
+// `steps` steps.
+unsigned stepSeed(long long steps) { return (unsigned)(steps * 0x9E3779B97F4A7C15ull >> 32); }
+
 StepConsts consts(const Domain* d) {
     StepConsts s;
     // bgk_ma2_collision_base (dynamicsTemplates3D.h:2290-2293) with
@@ -663,7 +671,7 @@ StepConsts consts(const Domain* d) {
     s.t4_omega = ((double)1 / (double)36) * d->omega;
     s.invRho0 = (double)1 / d->rho0;
     s.pending = d->pending ? 1 : 0;
-    s.seed = (unsigned)(d->steps * 0x9E3779B97F4A7C15ull >> 32);
+    s.seed = stepSeed(d->steps);
     s.external = 0;
     return s;
 }
@@ -926,6 +934,11 @@ int plbgpu_destroy(plbgpu_ctx* c) {
     for (auto& kv : c->domains) hs.push_back(kv.first);
     for (int h : hs) plbgpu_remove_domain(c, h);
     if (c->staging) cudaFree(c->staging);
+    if (c->xfer) {
+        cudaStreamSynchronize(c->xfer);
+        cudaStreamDestroy(c->xfer);
+    }
+    for (cudaEvent_t e : c->slabEvents) cudaEventDestroy(e);
     cudaStreamSynchronize(c->side.stream);
     cudaEventDestroy(c->side.fork);
     cudaEventDestroy(c->side.join);
@@ -1469,6 +1482,54 @@ int extractRecords(const Launchers& L, const DevLattice& v, bool odd, const Box&
     else return L.extractF32(v, odd, b, pending, out, s);
 }
 
+// A contiguous copy between the caller's buffer and a device staging slot,
+// run by the SMs: few blocks, each thread with UNROLL vectors in flight, so
+// that a small share of the SMs saturates the host link while the others
+// keep stepping.  (Copy-engine copies of a page-locked buffer that has gone
+// untouched by them for some tens of milliseconds were measured 7-15 times
+// slower on GB300; loads and stores from the SMs were not.)
+template <typename V, int UNROLL>
+__global__ void __launch_bounds__(256) bulkCopyKernel(const V* __restrict__ src, V* __restrict__ dst, long long n) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + (UNROLL - 1) * stride < n; i += UNROLL * stride) {
+        V v[UNROLL];
+#pragma unroll
+        for (int u = 0; u < UNROLL; ++u) v[u] = src[i + u * stride];
+#pragma unroll
+        for (int u = 0; u < UNROLL; ++u) dst[i + u * stride] = v[u];
+    }
+    for (; i < n; i += stride) dst[i] = src[i];
+}
+
+// One double of every 4 KB of a host buffer read and written back by the
+// whole GPU: the first touch of a page after a long pause is slow, and many
+// threads take those misses side by side, where the few blocks of
+// bulkCopyKernel would take them one after another (an 80 MB slab copy then
+// ran several times slower).
+__global__ void touchPagesKernel(double* p, long long values) {
+    const long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 512;
+    if (i < values) {
+        volatile double* q = p + i;
+        *q = *q;
+    }
+}
+
+// Blocks of bulkCopyKernel (640 KB in flight): on GB300 beside FP64 steps 20
+// blocks hid the transfers best of 12 to 128.
+constexpr int kBulkCopyBlocks = 20;
+
+int bulkCopy(plbgpu_ctx* c, void* dst, const void* src, size_t bytes, cudaStream_t s) {
+    const uintptr_t a = reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src) | bytes;
+    if (a % 16 == 0)
+        bulkCopyKernel<uint4, 8><<<kBulkCopyBlocks, 256, 0, s>>>(static_cast<const uint4*>(src),
+                                                                static_cast<uint4*>(dst), (long long)(bytes / 16));
+    else
+        bulkCopyKernel<unsigned long long, 16><<<kBulkCopyBlocks, 256, 0, s>>>(
+            static_cast<const unsigned long long*>(src), static_cast<unsigned long long*>(dst), (long long)(bytes / 8));
+    return launchBox(c);
+}
+
 template <typename B>
 int sendRecords(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, const B* buf, size_t n) {
     ProfRange prof("io");
@@ -1669,6 +1730,243 @@ int plbgpu_get_stats(plbgpu_ctx* c, int h, double out[7]) {
     out[5] = a.drag[2];
     out[6] = cnt;
     return PLBGPU_OK;
+}
+
+int plbgpu_run_host(plbgpu_ctx* c, int h, const double* in, double* out, size_t n, int nsteps, int stats_every,
+                    double* stats, size_t nstats) {
+    ProfRange prof("cycle", (unsigned long long)(nsteps > 0 ? nsteps : 0));
+    Domain* d;
+    int rc = lookup(c, h, &d);
+    if (rc) return rc;
+    if (!in || !out || (long long)n != 19 * d->n)
+        return fail(c, PLBGPU_ERR_ARG, "run_host: %zu values for %lld cells", n, d->n);
+    if (nsteps < 1 || stats_every < 0) return fail(c, PLBGPU_ERR_ARG, "run_host: nsteps %d, stats_every %d", nsteps,
+                                                   stats_every);
+    const int nrec = stats_every > 0 ? (nsteps + stats_every - 1) / stats_every : 0;
+    if (nrec && (!stats || nstats < (size_t)7 * nrec))
+        return fail(c, PLBGPU_ERR_ARG, "run_host: %d statistics records need %d doubles", nrec, 7 * nrec);
+    auto statsAt = [&](int t) { return stats_every > 0 && ((t + 1) % stats_every == 0 || t == nsteps - 1); };
+    int rec = 0;
+    auto saveStats = [&]() { return plbgpu_get_stats(c, h, stats + 7 * rec++); };
+    // steps [t, end) with the statistics records they owe, through the ordinary step call
+    auto steps = [&](int t, int end) -> int {
+        while (t < end) {
+            int next = t;
+            while (next < end && !statsAt(next)) ++next;
+            if (next == end) return plbgpu_collide_and_stream(c, h, end - t, 0);
+            int r = plbgpu_collide_and_stream(c, h, next - t + 1, 1);
+            if (r || (r = saveStats())) return r;
+            t = next + 1;
+        }
+        return PLBGPU_OK;
+    };
+    const int nx = d->nx, ny = d->ny, nz = d->nz;
+    if ((rc = materialize(c, d))) return rc;
+    if (d->surfDirty && (rc = buildSurface(c, d))) return rc;
+    // The pipelined transfers are SM copies of the caller's buffers, which
+    // the GPU must address directly (device or pinned memory, or any host
+    // memory on a GB300).  Stochastically rounded BF16 draws its random bits
+    // per kernel form (the paired stores hash one address for two slots):
+    // slab steps would round differently from whole steps, so that form
+    // steps in sequence.
+    const double* din = static_cast<const double*>(directPointer(c, in));
+    double* dout = static_cast<double*>(const_cast<void*>(directPointer(c, out)));
+    const bool pipe = din && dout && !d->sparse && d->nEdges + d->nCorners == 0 && nsteps >= 2 && nx >= 4 &&
+                      ny >= 3 && 2 * ny + 2 * nx <= 65535 && d->precision != PLBGPU_BF16_SR && c->side.stream;
+    if (!pipe) {   // the three calls in sequence
+        if ((rc = plbgpu_send(c, h, 0, nx - 1, 0, ny - 1, 0, nz - 1, in, n))) return rc;
+        if ((rc = steps(0, nsteps))) return rc;
+        return plbgpu_receive(c, h, 0, nx - 1, 0, ny - 1, 0, nz - 1, out, n);
+    }
+    // The domain is cut into x-slabs.  In the in-place (AA) layout a cell's
+    // records, inserted at either parity, fill exactly the slots that the
+    // cell's next step reads and writes; a step of a cell touches slots that
+    // only the steps of its neighbours touch before and after it.  So slab j
+    // takes its first step once its own records are in, step s once slabs
+    // j - 1 .. j + 1 took step s - 1, and its records are final once slabs
+    // j - 1 .. j + 1 took the last step.  The first steps run as a ramp
+    // behind the send (slab j - k takes step k as soon as slab j is in), the
+    // steps between as whole-domain steps, and the last steps as a ramp that
+    // finishes slab 0 first, each slab received while the later ones step.
+    const int width = std::max(2, (nx + 15) / 16), nslab = (nx + width - 1) / width;
+    while ((int)c->slabEvents.size() < 4 * nslab + 1) {
+        cudaEvent_t e;
+        CUDA_TRY(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        c->slabEvents.push_back(e);
+    }
+    if (!c->xfer) {   // the copies' blocks take the first SM slots that free up
+        int least = 0, greatest = 0;
+        cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        CUDA_TRY(c, cudaStreamCreateWithPriority(&c->xfer, cudaStreamNonBlocking, greatest));
+    }
+    cudaEvent_t* copiedEv = c->slabEvents.data();   // slab j's records copied into the staging slot
+    cudaEvent_t* insertedEv = copiedEv + nslab;     // ... inserted: the slot is free
+    cudaEvent_t* extractedEv = insertedEv + nslab;  // the m-th slab received extracted into its slot
+    cudaEvent_t* sentBackEv = extractedEv + nslab;  // ... copied out: the slot is free
+    cudaEvent_t forkEv = c->slabEvents[4 * nslab];
+    // staging: a ring of slab-sized slots between the copies and the kernels
+    const int nSlots = std::min(4, nslab);
+    const size_t slabValues = (size_t)width * ny * nz * 19;
+    if ((rc = ensureStaging(c, sizeof(double) * slabValues * nSlots))) return rc;
+    auto slot = [&](int m) { return static_cast<double*>(c->staging) + (size_t)(m % nSlots) * slabValues; };
+    const Launchers& L = launchers(d->precision);
+    const bool hasFaces = d->bc != nullptr;
+    cudaStream_t xs = c->xfer;
+    auto x0of = [&](int j) { return j * width; };
+    auto x1of = [&](int j) { return std::min(nx - 1, j * width + width - 1); };
+    auto records = [&](int j) { return (size_t)x0of(j) * ny * nz * 19; };
+    auto bytesOf = [&](int j) { return sizeof(double) * (size_t)(x1of(j) - x0of(j) + 1) * ny * nz * 19; };
+    auto box = [&](int j) { return Box{x0of(j), x1of(j), 0, ny - 1, 0, nz - 1}; };
+    int nReceived = 0;
+    // Steps per ramp: a transfer of the state (19 FP64 values per cell over
+    // the host link) lasts about two FP64 steps and tens of steps of the
+    // narrower forms, but the copies share the SMs with the steps; on GB300
+    // ramps of 2 FP64 steps (3 of the other forms) hid them best of 1 to 12.
+    // A ramp's statistics step (at most one) gathers into the domain's
+    // accumulator while the other steps of the ramp run.
+    auto statsIn = [&](int a, int b) {
+        int k = 0;
+        for (int t = a; t < b; ++t) k += statsAt(t) ? 1 : 0;
+        return k;
+    };
+    const int rMax = d->precision == PLBGPU_FP64 ? 2 : 3;
+    int rTail = std::min(rMax, nsteps - 1);
+    while (rTail > 1 && statsIn(nsteps - rTail, nsteps) > 1) --rTail;
+    int rHead = std::min(rMax, nsteps - rTail);
+    while (rHead > 1 && statsIn(0, rHead) > 1) --rHead;
+    const bool odd0 = d->odd, pending0 = d->pending;
+    const long long steps0 = d->steps;
+    DevLattice v = d->view();
+    v.rowForm = c->rowForm;
+    std::vector<int> done(nslab, 0), target(nslab, 0);
+    std::vector<char> sent(nslab, 0), received(nslab, 0);
+    auto nbr = [&](int j, int side) {
+        const int q = j + side;
+        if (q >= 0 && q < nslab) return q;
+        return d->per[0] ? (q + nslab) % nslab : -1;
+    };
+    auto ready = [&](int j) {
+        if (!sent[j] || done[j] >= target[j]) return false;
+        for (int sd = -1; sd <= 1; sd += 2) {
+            const int q = nbr(j, sd);
+            if (q >= 0 && done[q] < done[j]) return false;
+        }
+        return true;
+    };
+    auto final_ = [&](int j) {
+        if (done[j] < nsteps) return false;
+        for (int sd = -1; sd <= 1; sd += 2) {
+            const int q = nbr(j, sd);
+            if (q >= 0 && done[q] < nsteps) return false;
+        }
+        return true;
+    };
+    // slab j's final records into the next slot (on the step stream), then
+    // copied out behind the steps that follow
+    auto extract = [&](int j) -> int {
+        const int m = nReceived++;
+        if (m >= nSlots) CUDA_TRY(c, cudaStreamWaitEvent(c->stream, sentBackEv[m - nSlots], 0));
+        const int nl = extractRecords<double>(L, v, odd0 ^ (nsteps & 1), box(j), hasFaces ? 1 : 0, slot(m),
+                                              c->stream);
+        c->launches += nl - 1;
+        int r = launchBox(c);
+        if (r) return r;
+        CUDA_TRY(c, cudaEventRecord(extractedEv[m], c->stream));
+        CUDA_TRY(c, cudaStreamWaitEvent(xs, extractedEv[m], 0));
+        if ((r = bulkCopy(c, dout + records(j), slot(m), bytesOf(j), xs))) return r;
+        CUDA_TRY(c, cudaEventRecord(sentBackEv[m], xs));
+        received[j] = 1;
+        return PLBGPU_OK;
+    };
+    auto issue = [&](int j) -> int {
+        const int t = done[j];
+        StepConsts k = consts(d);
+        k.pending = (t == 0 ? pending0 : hasFaces) ? 1 : 0;
+        k.seed = stepSeed(steps0 + t);
+        const int nl = L.slabStep(v, odd0 ^ (t & 1), statsAt(t), k, d->stats, x0of(j), x1of(j), c->stream, &c->side);
+        c->launches += nl - 1;
+        ++done[j];
+        int r = launchBox(c);
+        if (r || done[j] < nsteps) return r;
+        for (int sd = -1; sd <= 1; ++sd) {   // the slabs this step may have made final
+            const int q = sd == 0 ? j : nbr(j, sd);
+            if (q >= 0 && !received[q] && final_(q) && (r = extract(q))) return r;
+        }
+        return PLBGPU_OK;
+    };
+    // every ready step, the lowest (slab + steps since base) first and the
+    // higher slab on ties: the diagonals of the ramps
+    auto drain = [&](int base) -> int {
+        for (;;) {
+            int best = -1;
+            long long bestKey = 0;
+            for (int j = 0; j < nslab; ++j) {
+                if (!ready(j)) continue;
+                const long long key = (long long)(j + done[j] - base) * (nslab + 1) + (nslab - j);
+                if (best < 0 || key < bestKey) { best = j; bestKey = key; }
+            }
+            if (best < 0) return PLBGPU_OK;
+            int r = issue(best);
+            if (r) return r;
+        }
+    };
+    auto settle = [&](int t1, bool gathered) -> int {
+        d->odd = odd0 ^ (t1 & 1);
+        d->pending = hasFaces;
+        d->steps = steps0 + t1;
+        if (gathered) d->statsValid = true;
+        int r = finishSurface(c, d);
+        if (r || !gathered) return r;
+        return saveStats();
+    };
+    {   // the send behind a ramp of rHead steps
+        ProfRange io("io");
+        const bool st = statsIn(0, rHead) > 0;
+        if (st) CUDA_TRY(c, cudaMemsetAsync(d->stats, 0, sizeof(StatsAcc) * kStatsSlots, c->stream));
+        CUDA_TRY(c, cudaEventRecord(forkEv, c->stream));
+        CUDA_TRY(c, cudaStreamWaitEvent(xs, forkEv, 0));
+        std::fill(target.begin(), target.end(), rHead);
+        for (int j = 0; j < nslab; ++j) {
+            // the copy runs up to nSlots slabs ahead of the inserts
+            if (j >= nSlots) CUDA_TRY(c, cudaStreamWaitEvent(xs, insertedEv[j - nSlots], 0));
+            if ((rc = bulkCopy(c, slot(j), din + records(j), bytesOf(j), xs))) return rc;
+            CUDA_TRY(c, cudaEventRecord(copiedEv[j], xs));
+            CUDA_TRY(c, cudaStreamWaitEvent(c->stream, copiedEv[j], 0));
+            const int nl = insertRecords<double>(L, v, odd0, box(j), slot(j), c->stream);
+            c->launches += nl - 1;
+            if ((rc = launchBox(c))) return rc;
+            CUDA_TRY(c, cudaEventRecord(insertedEv[j], c->stream));
+            sent[j] = 1;
+            if ((rc = drain(0))) return rc;
+        }
+        for (int j = 0; j < nslab; ++j)
+            if (done[j] != rHead) return fail(c, PLBGPU_ERR_STATE, "run_host: slab %d took %d steps", j, done[j]);
+        if ((rc = settle(rHead, st))) return rc;
+    }
+    if ((rc = steps(rHead, nsteps - rTail))) return rc;
+    {   // the pages of `out` touched beside the first steps of the last ramp
+        // (the send has read `in`, which may be `out`, before the middle)
+        CUDA_TRY(c, cudaEventRecord(forkEv, c->stream));
+        CUDA_TRY(c, cudaStreamWaitEvent(xs, forkEv, 0));
+        const long long values = (long long)n, pages = (values + 511) / 512;
+        touchPagesKernel<<<(unsigned)((pages + 255) / 256), 256, 0, xs>>>(dout, values);
+        if ((rc = launchBox(c))) return rc;
+    }
+    {   // a ramp of rTail steps, each slab received once final
+        ProfRange io("io");
+        const int base = nsteps - rTail;
+        const bool st = statsIn(base, nsteps) > 0;
+        if (st) CUDA_TRY(c, cudaMemsetAsync(d->stats, 0, sizeof(StatsAcc) * kStatsSlots, c->stream));
+        std::fill(done.begin(), done.end(), base);
+        std::fill(target.begin(), target.end(), nsteps);
+        if ((rc = drain(base))) return rc;
+        for (int j = 0; j < nslab; ++j)
+            if (!received[j]) return fail(c, PLBGPU_ERR_STATE, "run_host: slab %d was not received", j);
+        CUDA_TRY(c, cudaStreamSynchronize(xs));
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+        if ((rc = settle(nsteps, st))) return rc;
+    }
+    return checkStatus(c, d);
 }
 
 int plbgpu_reduce(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, double* avg_energy,

@@ -152,6 +152,8 @@ struct DevLattice {
     int per[3];
     long long n;
     unsigned* status;       // device error word (kStatusNonFinite)
+    int xRow0, xRows;       // interior rows stepped: 1 + xRow0 <= x <= xRow0 + xRows (0 and nx - 2 for
+                            // a whole step; an x-slab of the domain for plbgpu_run_host)
     int rowFacesDone;       // the face cells of interior rows were completed before this launch
                             // (completeFaceListKernel): the interior-row kernels skip their completion
     int rowForm;            // interior-row kernel: 0 the default (two cells per thread for the 2-byte
@@ -611,7 +613,7 @@ __global__ void __launch_bounds__(128, RowShape<S>::blocks)
     using R = typename StoreT<S>::R;
     constexpr int NC = RowShape<S>::cells;
     static_assert(!MASKED || NC == 1, "masked tiles: one cell per thread");
-    int x = blockIdx.z + 1, y = blockIdx.y + 1;
+    int x = blockIdx.z + 1 + L.xRow0, y = blockIdx.y + 1;
     int z0 = blockIdx.x * blockDim.x * NC + threadIdx.x, zEnd = L.nz;
     unsigned gone = 0;
     const int4* tiles = MASKED ? L.maskedTiles : L.denseTiles;
@@ -675,7 +677,7 @@ template <typename S, bool ODD, bool STATS, bool EXT>
 __global__ void __launch_bounds__(128, 8)
     pairRowStepKernel(DevLattice L, Planes<S> Pl, Deltas D, StepParams<typename StoreT<S>::R> P, StatsAcc* acc) {
     using R = typename StoreT<S>::R;
-    int x = blockIdx.z + 1, y = blockIdx.y + 1;
+    int x = blockIdx.z + 1 + L.xRow0, y = blockIdx.y + 1;
     int zA = 2 * (blockIdx.x * blockDim.x + threadIdx.x), zEnd = L.nz;
     if (L.denseTiles) {   // blockDim / (kTileCells / 2) tiles per block
         constexpr int TT = kTileCells / 2;

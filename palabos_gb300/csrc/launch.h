@@ -49,6 +49,10 @@ struct Launchers {
     int (*insertF32)(const DevLattice&, bool odd, Box, const float* in, cudaStream_t);
     // Face cells (x, y, z, kind) of interior rows completed in place before a step.
     int (*completeFaceList)(const DevLattice&, bool odd, const int4* cells, int count, cudaStream_t);
+    // One step of the slab x0 <= x <= x1 only, for steps pipelined with transfers (border rows on the
+    // side stream when one is given).
+    int (*slabStep)(const DevLattice&, bool odd, bool stats, const StepConsts&, StatsAcc*, int x0, int x1,
+                    cudaStream_t, const SideStream*);
 };
 
 const Launchers& launchersFp64();

@@ -47,14 +47,24 @@ __global__ void equilibriumKernel(DevLattice L, Box b, const double* rhou, doubl
 template <typename S, bool ODD>
 int stepParity(const DevLattice& L, bool stats, const StepParams<typename StoreT<S>::R>& p, StatsAcc* acc,
                cudaStream_t s, const SideStream* side);
+// One step of the slab x0 <= x <= x1: its interior rows with the interior-row
+// kernels on s, its border rows beside them on the side stream.
+template <typename S, bool ODD>
+int slabParity(const DevLattice& L, bool stats, const StepParams<typename StoreT<S>::R>& p, StatsAcc* acc, int x0,
+               int x1, cudaStream_t s, const SideStream* side);
 
 template <typename S>
 struct LaunchImpl {
     using R = typename StoreT<S>::R;
     static constexpr int kBlock = 128;
 
-    static int step(const DevLattice& L, bool odd, bool stats, const StepConsts& c, StatsAcc* acc,
-                    cudaStream_t s, const SideStream* side) {
+    static int slabStep(const DevLattice& L, bool odd, bool stats, const StepConsts& c, StatsAcc* acc, int x0, int x1,
+                        cudaStream_t s, const SideStream* side) {
+        const StepParams<R> p = params(c);
+        return odd ? slabParity<S, true>(L, stats, p, acc, x0, x1, s, side)
+                   : slabParity<S, false>(L, stats, p, acc, x0, x1, s, side);
+    }
+    static StepParams<R> params(const StepConsts& c) {
         StepParams<R> p;
         p.bgk.omega = (R)c.omega;
         p.bgk.one_m_omega = (R)c.one_m_omega;
@@ -65,6 +75,11 @@ struct LaunchImpl {
         p.pending = c.pending;
         p.seed = c.seed;
         p.external = c.external;
+        return p;
+    }
+    static int step(const DevLattice& L, bool odd, bool stats, const StepConsts& c, StatsAcc* acc,
+                    cudaStream_t s, const SideStream* side) {
+        const StepParams<R> p = params(c);
         return odd ? stepParity<S, true>(L, stats, p, acc, s, side) : stepParity<S, false>(L, stats, p, acc, s, side);
     }
     static int completeFaces(const DevLattice& L, bool odd, cudaStream_t s) {
@@ -150,7 +165,7 @@ struct LaunchImpl {
     static const Launchers& table() {
         static const Launchers t = {step,  completeFaces, extract, insert, reduce,
                                     equilibrium, field, rhoBarJ, surface, extractF32, insertF32,
-                                    completeFaceList};
+                                    completeFaceList, slabStep};
         return t;
     }
 };

@@ -4,4 +4,6 @@
 namespace plbgpu {
 template int stepParity<bf16sr, false>(const DevLattice&, bool, const StepParams<StoreT<bf16sr>::R>&, StatsAcc*,
                                         cudaStream_t, const SideStream*);
+template int slabParity<bf16sr, false>(const DevLattice&, bool, const StepParams<StoreT<bf16sr>::R>&, StatsAcc*, int,
+                                      int, cudaStream_t, const SideStream*);
 }  // namespace plbgpu

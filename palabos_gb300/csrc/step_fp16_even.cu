@@ -4,4 +4,6 @@
 namespace plbgpu {
 template int stepParity<__half, false>(const DevLattice&, bool, const StepParams<StoreT<__half>::R>&, StatsAcc*,
                                         cudaStream_t, const SideStream*);
+template int slabParity<__half, false>(const DevLattice&, bool, const StepParams<StoreT<__half>::R>&, StatsAcc*, int,
+                                      int, cudaStream_t, const SideStream*);
 }  // namespace plbgpu

@@ -4,4 +4,6 @@
 namespace plbgpu {
 template int stepParity<float, true>(const DevLattice&, bool, const StepParams<StoreT<float>::R>&, StatsAcc*,
                                         cudaStream_t, const SideStream*);
+template int slabParity<float, true>(const DevLattice&, bool, const StepParams<StoreT<float>::R>&, StatsAcc*, int,
+                                      int, cudaStream_t, const SideStream*);
 }  // namespace plbgpu

@@ -4,4 +4,6 @@
 namespace plbgpu {
 template int stepParity<double, false>(const DevLattice&, bool, const StepParams<StoreT<double>::R>&, StatsAcc*,
                                         cudaStream_t, const SideStream*);
+template int slabParity<double, false>(const DevLattice&, bool, const StepParams<StoreT<double>::R>&, StatsAcc*, int,
+                                      int, cudaStream_t, const SideStream*);
 }  // namespace plbgpu

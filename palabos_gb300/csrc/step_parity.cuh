@@ -33,8 +33,10 @@ struct StepLaunch {
     }
 
     template <bool ODD, bool STATS, bool EXT>
+    // slab: the interior rows of L's x-range only (xRow0, xRows), on s alone;
+    // the caller steps the slab's border rows
     static int stepSplit(const DevLattice& L, const StepParams<R>& p, StatsAcc* acc, cudaStream_t s,
-                         const SideStream* side) {
+                         const SideStream* side, bool slab = false) {
         int launched = 0;
         // A sparse domain with tile lists runs its dense tiles (no cell outside
         // the lattice in the 3x3 rows around them, one cell beyond each end)
@@ -44,13 +46,13 @@ struct StepLaunch {
         const bool lists = L.sparse && (L.denseTiles || L.generalTiles || L.maskedTiles);
         const bool general = (L.sparse && !lists) || L.nx < 3 || L.ny < 3;
         const int edgeRows = lists ? L.nGeneral : general ? L.nx * L.ny : 2 * L.ny + 2 * (L.nx - 2);
-        const long long interiorRows = lists ? L.nDense : (long long)(L.nx - 2) * (L.ny - 2);
+        const long long interiorRows = lists ? L.nDense : (long long)L.xRows * (L.ny - 2);
         // grid over the interior rows: (blocksPerRow, ny-2, nx-2), the row
         // being (blockIdx.z + 1, blockIdx.y + 1); or one block per dense tile,
         // entry blockIdx.y + gridDim.y * blockIdx.z of the list
         // tilesPerBlock: the tiles one block of the list steps
         auto interiorGrid = [&](int blocksPerRow, int tilesPerBlock) {
-            if (!lists) return dim3((unsigned)blocksPerRow, (unsigned)(L.ny - 2), (unsigned)(L.nx - 2));
+            if (!lists) return dim3((unsigned)blocksPerRow, (unsigned)(L.ny - 2), (unsigned)L.xRows);
             const int blocks = (L.nDense + tilesPerBlock - 1) / tilesPerBlock;
             const unsigned gy = (unsigned)(blocks < 65535 ? blocks : 65535);
             return dim3(1u, gy, (unsigned)((blocks + gy - 1) / gy));
@@ -63,7 +65,7 @@ struct StepLaunch {
         // (2% faster); FP64 is bound by its FP64 pipe either way.
         constexpr bool interiorFirst = sizeof(S) == 2;
         cudaStream_t es = s;
-        if (side && !general && cudaEventRecord(side->fork, s) == cudaSuccess &&
+        if (side && !general && !slab && cudaEventRecord(side->fork, s) == cudaSuccess &&
             cudaStreamWaitEvent(side->stream, side->fork, 0) == cudaSuccess)
             es = side->stream;
         auto interior = [&]() {
@@ -143,7 +145,7 @@ struct StepLaunch {
             ++launched;
         };
         auto border = [&]() {
-            if (edgeRows == 0) return;
+            if (edgeRows == 0 || slab) return;
             // rows, or blocks of kBlock / kTileCells tiles of the general-tile list
             const int blocks = lists ? (edgeRows + kBlock / kTileCells - 1) / (kBlock / kTileCells) : edgeRows;
             const int gy = blocks < 65535 ? blocks : 65535;
@@ -171,6 +173,77 @@ struct StepLaunch {
     }
 
 };
+
+// The border rows of the x-slab [x0, x1] of one AA step: whole planes x = 0
+// and x = nx - 1 where the slab holds them, rows y = 0 and y = ny - 1 of its
+// other planes (grid.y = rows: the planes' rows first, then two rows per
+// interior plane), with the general addressing.  The slab's interior rows
+// take the interior-row kernels (stepSplit over xRow0, xRows); slabs of a
+// step launched separately beside host transfers (plbgpu_run_host).  Each
+// slot is read and written by one cell per step, so the slabs of a step may
+// run in any order once their inputs are final.
+template <typename S, bool ODD, bool STATS, bool EXT>
+__global__ void __launch_bounds__(128) slabBorderKernel(DevLattice L, StepParams<typename StoreT<S>::R> P,
+                                                        StatsAcc* acc, int x0, int x1) {
+    using R = typename StoreT<S>::R;
+    const int z = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lo = x0 == 0 ? 1 : 0, hi = x1 == L.nx - 1 ? 1 : 0;
+    int r = blockIdx.y, x, y;
+    if (r < lo * L.ny) {
+        x = 0; y = r;
+    } else if ((r -= lo * L.ny) < hi * L.ny) {
+        x = L.nx - 1; y = r;
+    } else {
+        r -= hi * L.ny;
+        x = x0 + lo + (r >> 1);
+        y = (r & 1) ? L.ny - 1 : 0;
+    }
+    R rhoBar = R(0), uSqr = R(0);
+    bool g = false;
+    if (z < L.nz) g = processCellGeneral<S, ODD, STATS, EXT, false>(L, P, x, y, z, acc, rhoBar, uSqr);
+    accumulateStats<STATS>(g, (double)rhoBar, (double)uSqr, acc, L.status);
+}
+
+template <typename S, bool ODD, bool STATS, bool EXT>
+int slabSplit(const DevLattice& L, const StepParams<typename StoreT<S>::R>& p, StatsAcc* acc, int x0, int x1,
+              cudaStream_t s, const SideStream* side) {
+    constexpr int kBlock = 128;
+    int launched = 0;
+    const int lo = x0 == 0 ? 1 : 0, hi = x1 == L.nx - 1 ? 1 : 0;
+    const int a = x0 + lo, b = x1 - hi;          // the slab's planes with interior rows
+    const int rows = (lo + hi) * L.ny + 2 * (b - a + 1);
+    // the border rows beside the interior rows, on the side stream
+    cudaStream_t es = s;
+    if (side && b >= a && cudaEventRecord(side->fork, s) == cudaSuccess &&
+        cudaStreamWaitEvent(side->stream, side->fork, 0) == cudaSuccess)
+        es = side->stream;
+    if (rows > 0) {
+        const dim3 g((unsigned)((L.nz + kBlock - 1) / kBlock), (unsigned)rows, 1u);
+        slabBorderKernel<S, ODD, STATS, EXT><<<g, kBlock, 0, es>>>(L, p, acc, x0, x1);
+        ++launched;
+    }
+    if (b >= a) {
+        DevLattice Ls = L;
+        Ls.xRow0 = a - 1;
+        Ls.xRows = b - a + 1;
+        launched += StepLaunch<S>::template stepSplit<ODD, STATS, EXT>(Ls, p, acc, s, nullptr, true);
+    }
+    if (es != s) {   // join: the next launch on s waits for both kernels
+        if (cudaEventRecord(side->join, es) != cudaSuccess || cudaStreamWaitEvent(s, side->join, 0) != cudaSuccess)
+            cudaStreamSynchronize(es);
+    }
+    return launched;
+}
+
+template <typename S, bool ODD>
+int slabParity(const DevLattice& L, bool stats, const StepParams<typename StoreT<S>::R>& p, StatsAcc* acc, int x0,
+               int x1, cudaStream_t s, const SideStream* side) {
+    if (p.external)
+        return stats ? slabSplit<S, ODD, true, true>(L, p, acc, x0, x1, s, side)
+                     : slabSplit<S, ODD, false, true>(L, p, acc, x0, x1, s, side);
+    return stats ? slabSplit<S, ODD, true, false>(L, p, acc, x0, x1, s, side)
+                 : slabSplit<S, ODD, false, false>(L, p, acc, x0, x1, s, side);
+}
 
 template <typename S, bool ODD>
 int stepParity(const DevLattice& L, bool stats, const StepParams<typename StoreT<S>::R>& p, StatsAcc* acc,

@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(128, VecShape<CPT>::blocks)
         downOk = s + 1 < TS && z0 + CPT < t.w && lane < 31;
     } else {
         const int row = (int)(gg / RS), seg = (int)(gg - (long long)row * RS);
-        x = 1 + row / (L.ny - 2);
+        x = 1 + L.xRow0 + row / (L.ny - 2);
         y = 1 + row % (L.ny - 2);
         z0 = seg * CPT;
         upOk = seg > 0 && lane > 0;                 // lane - 1 holds the CPT cells below z0 in this row

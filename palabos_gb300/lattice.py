@@ -256,6 +256,21 @@ class DeviceLattice3D:
         return out.reshape(shape)
 
     # ----------------------------------------------------------------- stepping
+    def run_host(self, f, nsteps, stats_every=0, out=None):
+        """Send f, run nsteps steps and receive the state (plbgpu_run_host: the
+        transfers overlap the first and the last step).  Returns (state,
+        statistics records (k, 7) of every stats_every-th and the last step)."""
+        a = np.ascontiguousarray(f, np.float64).reshape(-1)
+        if out is None:
+            out = np.empty(self.shape + (19,))
+        if not (out.flags["C_CONTIGUOUS"] and out.dtype == np.float64 and out.size == a.size):
+            raise ValueError("out must be a C-contiguous float64 array of the domain's size x 19")
+        nrec = (nsteps + stats_every - 1) // stats_every if stats_every > 0 else 0
+        st = np.zeros((max(nrec, 1), 7))
+        self._check(self.lib.plbgpu_run_host(self.ctx.h, self.handle, _dp(a), _dp(out.reshape(-1)), a.size,
+                                             int(nsteps), int(stats_every), _dp(st), st.size))
+        return out, st[:nrec]
+
     def collide_and_stream(self, nsteps=1, stats=False):
         self._check(self.lib.plbgpu_collide_and_stream(self.ctx.h, self.handle, int(nsteps), int(bool(stats))))
 
