@@ -168,6 +168,17 @@ public:
     void collideAndStream(int steps = 1, bool gatherStatistics = true) {
         ctx_.check(plbgpu_collide_and_stream(ctx_.get(), h_, steps, gatherStatistics));
     }
+    // The whole domain's populations f sent, `steps` steps run and the state
+    // received back into f, the transfers overlapped with the first and last
+    // steps (plbgpu_run_host).  Returns the statistics of every
+    // statsEvery-th step and of the last one, 7 values each.
+    std::vector<double> runHost(std::vector<double>& f, int steps, int statsEvery = 0) {
+        const size_t records = statsEvery > 0 ? (size_t)((steps + statsEvery - 1) / statsEvery) : 0;
+        std::vector<double> stats(7 * records);
+        ctx_.check(plbgpu_run_host(ctx_.get(), h_, f.data(), f.data(), f.size(), steps, statsEvery, stats.data(),
+                                   stats.size()));
+        return stats;
+    }
     // External rho-bar / j fields and ExternalRhoJcollideAndStream3D steps
     // (values: rho-bar, jx, jy, jz per cell, z fastest).
     void computeRhoBarJ() { ctx_.check(plbgpu_compute_rhobar_j(ctx_.get(), h_)); }
