@@ -287,6 +287,18 @@ int plbgpu_collide_and_stream(plbgpu_ctx* ctx, int handle, int nsteps, int colle
 int plbgpu_run_host(plbgpu_ctx* ctx, int handle, const double* in, double* out, size_t n, int nsteps,
                     int stats_every, double* stats, size_t nstats);
 
+/* The order of the operations of plbgpu_run_host's overlapped path for a
+ * domain of nx >= 4 x-planes (periodic_x non-zero: periodic along x), nsteps
+ * >= 2 steps, statistics every stats_every steps and storage form
+ * `precision`.  Host logic only (no context, no GPU).  Slab j holds the planes
+ * j * slab_width .. min(nx, (j + 1) * slab_width) - 1.  *count = the number of
+ * operations; with ops non-null (cap >= 3 * count ints) each is written as
+ * (kind, slab, step): kind 0 = slab sent (its records copied in and
+ * inserted), 1 = step `step` of the slab, 2 = slab received after the last
+ * step, 3 = the steps [slab, step) of the whole domain. */
+int plbgpu_run_host_plan(int nx, int periodic_x, int nsteps, int stats_every, int precision, int* slab_width,
+                         int* ops, size_t cap, size_t* count);
+
 /* Statistics of the last step that gathered them (BlockStatistics::evaluate,
  * core/blockStatistics.cpp:77-110; MultiBlock3D::getInternalStatistics):
  * out[0] average rho-bar, out[1] average u^2, out[2] max u^2,

@@ -1482,6 +1482,112 @@ int extractRecords(const Launchers& L, const DevLattice& v, bool odd, const Box&
     else return L.extractF32(v, odd, b, pending, out, s);
 }
 
+// The order of plbgpu_run_host's slab operations, host logic only.  The
+// domain is cut into x-slabs.  In the in-place (AA) layout a cell's records,
+// inserted at either parity, fill exactly the slots that the cell's next step
+// reads and writes; a step of a cell touches slots that only the steps of its
+// neighbours touch before and after it.  So slab j takes its first step once
+// its own records are in, step s once slabs j - 1 .. j + 1 took step s - 1,
+// and its records are final once slabs j - 1 .. j + 1 took the last step.
+// The first steps run as a ramp behind the send (slab j - k takes step k as
+// soon as slab j is in), the steps between as whole-domain steps, and the
+// last steps as a ramp that finishes slab 0 first, each slab received as soon
+// as it is final.
+enum : int { kSlabSend = 0, kSlabStep = 1, kSlabReceive = 2, kWholeSteps = 3 };
+struct SlabOp {
+    int kind, slab, step;   // kWholeSteps: steps [slab, step) of the whole domain
+};
+struct RunHostPlan {
+    int width = 0, nslab = 0, rHead = 0, rTail = 0;
+    bool statsHead = false, statsTail = false;   // a ramp holds a statistics step
+    std::vector<SlabOp> ops;
+};
+
+// nx >= 4, nsteps >= 2.  Steps per ramp: a transfer of the state (19 FP64
+// values per cell over the host link) lasts about two FP64 steps and tens of
+// steps of the narrower forms, but the copies share the SMs with the steps;
+// on GB300 ramps of 2 FP64 steps (3 of the other forms) hid them best of 1 to
+// 12.  A ramp holds at most one statistics step, which gathers into the
+// domain's accumulator while the other steps of the ramp run.
+RunHostPlan planRunHost(int nx, bool periodicX, int nsteps, int statsEvery, bool fp64) {
+    RunHostPlan p;
+    p.width = std::max(2, (nx + 15) / 16);
+    p.nslab = (nx + p.width - 1) / p.width;
+    const int S = p.nslab;
+    auto statsAt = [&](int t) { return statsEvery > 0 && ((t + 1) % statsEvery == 0 || t == nsteps - 1); };
+    auto statsIn = [&](int a, int b) {
+        int k = 0;
+        for (int t = a; t < b; ++t) k += statsAt(t) ? 1 : 0;
+        return k;
+    };
+    const int rMax = fp64 ? 2 : 3;
+    p.rTail = std::min(rMax, nsteps - 1);
+    while (p.rTail > 1 && statsIn(nsteps - p.rTail, nsteps) > 1) --p.rTail;
+    p.rHead = std::min(rMax, nsteps - p.rTail);
+    while (p.rHead > 1 && statsIn(0, p.rHead) > 1) --p.rHead;
+    p.statsHead = statsIn(0, p.rHead) > 0;
+    p.statsTail = statsIn(nsteps - p.rTail, nsteps) > 0;
+    std::vector<int> done(S, 0), target(S, p.rHead);
+    std::vector<char> sent(S, 0), received(S, 0);
+    auto nbr = [&](int j, int side) {
+        const int q = j + side;
+        if (q >= 0 && q < S) return q;
+        return periodicX ? (q + S) % S : -1;
+    };
+    auto ready = [&](int j) {
+        if (!sent[j] || done[j] >= target[j]) return false;
+        for (int sd = -1; sd <= 1; sd += 2) {
+            const int q = nbr(j, sd);
+            if (q >= 0 && done[q] < done[j]) return false;
+        }
+        return true;
+    };
+    auto final_ = [&](int j) {
+        if (done[j] < nsteps) return false;
+        for (int sd = -1; sd <= 1; sd += 2) {
+            const int q = nbr(j, sd);
+            if (q >= 0 && done[q] < nsteps) return false;
+        }
+        return true;
+    };
+    // every ready step, the lowest (slab + steps since base) first and the
+    // higher slab on ties: the diagonals of the ramps
+    auto drain = [&](int base) {
+        for (;;) {
+            int best = -1;
+            long long bestKey = 0;
+            for (int j = 0; j < S; ++j) {
+                if (!ready(j)) continue;
+                const long long key = (long long)(j + done[j] - base) * (S + 1) + (S - j);
+                if (best < 0 || key < bestKey) {
+                    best = j;
+                    bestKey = key;
+                }
+            }
+            if (best < 0) return;
+            p.ops.push_back({kSlabStep, best, done[best]});
+            if (++done[best] < nsteps) continue;
+            for (int sd = -1; sd <= 1; ++sd) {   // the slabs this step may have made final
+                const int q = sd == 0 ? best : nbr(best, sd);
+                if (q >= 0 && !received[q] && final_(q)) {
+                    p.ops.push_back({kSlabReceive, q, nsteps});
+                    received[q] = 1;
+                }
+            }
+        }
+    };
+    for (int j = 0; j < S; ++j) {
+        p.ops.push_back({kSlabSend, j, 0});
+        sent[j] = 1;
+        drain(0);
+    }
+    p.ops.push_back({kWholeSteps, p.rHead, nsteps - p.rTail});
+    std::fill(done.begin(), done.end(), nsteps - p.rTail);
+    std::fill(target.begin(), target.end(), nsteps);
+    drain(nsteps - p.rTail);
+    return p;
+}
+
 // A contiguous copy between the caller's buffer and a device staging slot,
 // run by the SMs: few blocks, each thread with UNROLL vectors in flight, so
 // that a small share of the SMs saturates the host link while the others
@@ -1778,17 +1884,8 @@ int plbgpu_run_host(plbgpu_ctx* c, int h, const double* in, double* out, size_t 
         if ((rc = steps(0, nsteps))) return rc;
         return plbgpu_receive(c, h, 0, nx - 1, 0, ny - 1, 0, nz - 1, out, n);
     }
-    // The domain is cut into x-slabs.  In the in-place (AA) layout a cell's
-    // records, inserted at either parity, fill exactly the slots that the
-    // cell's next step reads and writes; a step of a cell touches slots that
-    // only the steps of its neighbours touch before and after it.  So slab j
-    // takes its first step once its own records are in, step s once slabs
-    // j - 1 .. j + 1 took step s - 1, and its records are final once slabs
-    // j - 1 .. j + 1 took the last step.  The first steps run as a ramp
-    // behind the send (slab j - k takes step k as soon as slab j is in), the
-    // steps between as whole-domain steps, and the last steps as a ramp that
-    // finishes slab 0 first, each slab received while the later ones step.
-    const int width = std::max(2, (nx + 15) / 16), nslab = (nx + width - 1) / width;
+    const RunHostPlan plan = planRunHost(nx, d->per[0] != 0, nsteps, stats_every, d->precision == PLBGPU_FP64);
+    const int width = plan.width, nslab = plan.nslab;
     while ((int)c->slabEvents.size() < 4 * nslab + 1) {
         cudaEvent_t e;
         CUDA_TRY(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -1817,53 +1914,29 @@ int plbgpu_run_host(plbgpu_ctx* c, int h, const double* in, double* out, size_t 
     auto records = [&](int j) { return (size_t)x0of(j) * ny * nz * 19; };
     auto bytesOf = [&](int j) { return sizeof(double) * (size_t)(x1of(j) - x0of(j) + 1) * ny * nz * 19; };
     auto box = [&](int j) { return Box{x0of(j), x1of(j), 0, ny - 1, 0, nz - 1}; };
-    int nReceived = 0;
-    // Steps per ramp: a transfer of the state (19 FP64 values per cell over
-    // the host link) lasts about two FP64 steps and tens of steps of the
-    // narrower forms, but the copies share the SMs with the steps; on GB300
-    // ramps of 2 FP64 steps (3 of the other forms) hid them best of 1 to 12.
-    // A ramp's statistics step (at most one) gathers into the domain's
-    // accumulator while the other steps of the ramp run.
-    auto statsIn = [&](int a, int b) {
-        int k = 0;
-        for (int t = a; t < b; ++t) k += statsAt(t) ? 1 : 0;
-        return k;
-    };
-    const int rMax = d->precision == PLBGPU_FP64 ? 2 : 3;
-    int rTail = std::min(rMax, nsteps - 1);
-    while (rTail > 1 && statsIn(nsteps - rTail, nsteps) > 1) --rTail;
-    int rHead = std::min(rMax, nsteps - rTail);
-    while (rHead > 1 && statsIn(0, rHead) > 1) --rHead;
     const bool odd0 = d->odd, pending0 = d->pending;
     const long long steps0 = d->steps;
     DevLattice v = d->view();
     v.rowForm = c->rowForm;
-    std::vector<int> done(nslab, 0), target(nslab, 0);
-    std::vector<char> sent(nslab, 0), received(nslab, 0);
-    auto nbr = [&](int j, int side) {
-        const int q = j + side;
-        if (q >= 0 && q < nslab) return q;
-        return d->per[0] ? (q + nslab) % nslab : -1;
+    int nSent = 0, nReceived = 0;
+    // slab j's records copied into the next slot (the copy runs up to nSlots
+    // slabs ahead of the inserts), then inserted on the step stream
+    auto send = [&](int j) -> int {
+        const int m = nSent++;
+        if (m >= nSlots) CUDA_TRY(c, cudaStreamWaitEvent(xs, insertedEv[m - nSlots], 0));
+        int r = bulkCopy(c, slot(m), din + records(j), bytesOf(j), xs);
+        if (r) return r;
+        CUDA_TRY(c, cudaEventRecord(copiedEv[m], xs));
+        CUDA_TRY(c, cudaStreamWaitEvent(c->stream, copiedEv[m], 0));
+        const int nl = insertRecords<double>(L, v, odd0, box(j), slot(m), c->stream);
+        c->launches += nl - 1;
+        if ((r = launchBox(c))) return r;
+        CUDA_TRY(c, cudaEventRecord(insertedEv[m], c->stream));
+        return PLBGPU_OK;
     };
-    auto ready = [&](int j) {
-        if (!sent[j] || done[j] >= target[j]) return false;
-        for (int sd = -1; sd <= 1; sd += 2) {
-            const int q = nbr(j, sd);
-            if (q >= 0 && done[q] < done[j]) return false;
-        }
-        return true;
-    };
-    auto final_ = [&](int j) {
-        if (done[j] < nsteps) return false;
-        for (int sd = -1; sd <= 1; sd += 2) {
-            const int q = nbr(j, sd);
-            if (q >= 0 && done[q] < nsteps) return false;
-        }
-        return true;
-    };
-    // slab j's final records into the next slot (on the step stream), then
-    // copied out behind the steps that follow
-    auto extract = [&](int j) -> int {
+    // slab j's final records extracted into the next slot on the step stream,
+    // then copied out behind the steps that follow
+    auto receive = [&](int j) -> int {
         const int m = nReceived++;
         if (m >= nSlots) CUDA_TRY(c, cudaStreamWaitEvent(c->stream, sentBackEv[m - nSlots], 0));
         const int nl = extractRecords<double>(L, v, odd0 ^ (nsteps & 1), box(j), hasFaces ? 1 : 0, slot(m),
@@ -1875,40 +1948,15 @@ int plbgpu_run_host(plbgpu_ctx* c, int h, const double* in, double* out, size_t 
         CUDA_TRY(c, cudaStreamWaitEvent(xs, extractedEv[m], 0));
         if ((r = bulkCopy(c, dout + records(j), slot(m), bytesOf(j), xs))) return r;
         CUDA_TRY(c, cudaEventRecord(sentBackEv[m], xs));
-        received[j] = 1;
         return PLBGPU_OK;
     };
-    auto issue = [&](int j) -> int {
-        const int t = done[j];
+    auto stepSlab = [&](int j, int t) -> int {
         StepConsts k = consts(d);
         k.pending = (t == 0 ? pending0 : hasFaces) ? 1 : 0;
         k.seed = stepSeed(steps0 + t);
         const int nl = L.slabStep(v, odd0 ^ (t & 1), statsAt(t), k, d->stats, x0of(j), x1of(j), c->stream, &c->side);
         c->launches += nl - 1;
-        ++done[j];
-        int r = launchBox(c);
-        if (r || done[j] < nsteps) return r;
-        for (int sd = -1; sd <= 1; ++sd) {   // the slabs this step may have made final
-            const int q = sd == 0 ? j : nbr(j, sd);
-            if (q >= 0 && !received[q] && final_(q) && (r = extract(q))) return r;
-        }
-        return PLBGPU_OK;
-    };
-    // every ready step, the lowest (slab + steps since base) first and the
-    // higher slab on ties: the diagonals of the ramps
-    auto drain = [&](int base) -> int {
-        for (;;) {
-            int best = -1;
-            long long bestKey = 0;
-            for (int j = 0; j < nslab; ++j) {
-                if (!ready(j)) continue;
-                const long long key = (long long)(j + done[j] - base) * (nslab + 1) + (nslab - j);
-                if (best < 0 || key < bestKey) { best = j; bestKey = key; }
-            }
-            if (best < 0) return PLBGPU_OK;
-            int r = issue(best);
-            if (r) return r;
-        }
+        return launchBox(c);
     };
     auto settle = [&](int t1, bool gathered) -> int {
         d->odd = odd0 ^ (t1 & 1);
@@ -1919,54 +1967,58 @@ int plbgpu_run_host(plbgpu_ctx* c, int h, const double* in, double* out, size_t 
         if (r || !gathered) return r;
         return saveStats();
     };
-    {   // the send behind a ramp of rHead steps
+    {
         ProfRange io("io");
-        const bool st = statsIn(0, rHead) > 0;
-        if (st) CUDA_TRY(c, cudaMemsetAsync(d->stats, 0, sizeof(StatsAcc) * kStatsSlots, c->stream));
+        if (plan.statsHead) CUDA_TRY(c, cudaMemsetAsync(d->stats, 0, sizeof(StatsAcc) * kStatsSlots, c->stream));
         CUDA_TRY(c, cudaEventRecord(forkEv, c->stream));
         CUDA_TRY(c, cudaStreamWaitEvent(xs, forkEv, 0));
-        std::fill(target.begin(), target.end(), rHead);
-        for (int j = 0; j < nslab; ++j) {
-            // the copy runs up to nSlots slabs ahead of the inserts
-            if (j >= nSlots) CUDA_TRY(c, cudaStreamWaitEvent(xs, insertedEv[j - nSlots], 0));
-            if ((rc = bulkCopy(c, slot(j), din + records(j), bytesOf(j), xs))) return rc;
-            CUDA_TRY(c, cudaEventRecord(copiedEv[j], xs));
-            CUDA_TRY(c, cudaStreamWaitEvent(c->stream, copiedEv[j], 0));
-            const int nl = insertRecords<double>(L, v, odd0, box(j), slot(j), c->stream);
-            c->launches += nl - 1;
-            if ((rc = launchBox(c))) return rc;
-            CUDA_TRY(c, cudaEventRecord(insertedEv[j], c->stream));
-            sent[j] = 1;
-            if ((rc = drain(0))) return rc;
+        for (const SlabOp& op : plan.ops) {
+            switch (op.kind) {
+            case kSlabSend: rc = send(op.slab); break;
+            case kSlabStep: rc = stepSlab(op.slab, op.step); break;
+            case kSlabReceive: rc = receive(op.slab); break;
+            default:   // the ramp behind the send is done: the steps between, then the closing ramp
+                if ((rc = settle(plan.rHead, plan.statsHead))) return rc;
+                if ((rc = steps(op.slab, op.step))) return rc;
+                {   // the pages of `out` touched beside the first steps of the closing ramp
+                    // (the send has read `in`, which may be `out`, before the steps between)
+                    CUDA_TRY(c, cudaEventRecord(forkEv, c->stream));
+                    CUDA_TRY(c, cudaStreamWaitEvent(xs, forkEv, 0));
+                    const long long values = (long long)n, pages = (values + 511) / 512;
+                    touchPagesKernel<<<(unsigned)((pages + 255) / 256), 256, 0, xs>>>(dout, values);
+                    if ((rc = launchBox(c))) return rc;
+                }
+                if (plan.statsTail)
+                    CUDA_TRY(c, cudaMemsetAsync(d->stats, 0, sizeof(StatsAcc) * kStatsSlots, c->stream));
+                break;
+            }
+            if (rc) return rc;
         }
-        for (int j = 0; j < nslab; ++j)
-            if (done[j] != rHead) return fail(c, PLBGPU_ERR_STATE, "run_host: slab %d took %d steps", j, done[j]);
-        if ((rc = settle(rHead, st))) return rc;
-    }
-    if ((rc = steps(rHead, nsteps - rTail))) return rc;
-    {   // the pages of `out` touched beside the first steps of the last ramp
-        // (the send has read `in`, which may be `out`, before the middle)
-        CUDA_TRY(c, cudaEventRecord(forkEv, c->stream));
-        CUDA_TRY(c, cudaStreamWaitEvent(xs, forkEv, 0));
-        const long long values = (long long)n, pages = (values + 511) / 512;
-        touchPagesKernel<<<(unsigned)((pages + 255) / 256), 256, 0, xs>>>(dout, values);
-        if ((rc = launchBox(c))) return rc;
-    }
-    {   // a ramp of rTail steps, each slab received once final
-        ProfRange io("io");
-        const int base = nsteps - rTail;
-        const bool st = statsIn(base, nsteps) > 0;
-        if (st) CUDA_TRY(c, cudaMemsetAsync(d->stats, 0, sizeof(StatsAcc) * kStatsSlots, c->stream));
-        std::fill(done.begin(), done.end(), base);
-        std::fill(target.begin(), target.end(), nsteps);
-        if ((rc = drain(base))) return rc;
-        for (int j = 0; j < nslab; ++j)
-            if (!received[j]) return fail(c, PLBGPU_ERR_STATE, "run_host: slab %d was not received", j);
+        if (nSent != nslab || nReceived != nslab)
+            return fail(c, PLBGPU_ERR_STATE, "run_host: %d slabs sent and %d received of %d", nSent, nReceived,
+                        nslab);
         CUDA_TRY(c, cudaStreamSynchronize(xs));
         CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-        if ((rc = settle(nsteps, st))) return rc;
+        if ((rc = settle(nsteps, plan.statsTail))) return rc;
     }
     return checkStatus(c, d);
+}
+
+int plbgpu_run_host_plan(int nx, int periodic_x, int nsteps, int stats_every, int precision, int* slab_width,
+                         int* ops, size_t cap, size_t* count) {
+    if (nx < 4 || nsteps < 2 || stats_every < 0 || precision < PLBGPU_FP64 || precision > PLBGPU_BF16_SR || !count)
+        return PLBGPU_ERR_ARG;
+    const RunHostPlan plan = planRunHost(nx, periodic_x != 0, nsteps, stats_every, precision == PLBGPU_FP64);
+    *count = plan.ops.size();
+    if (slab_width) *slab_width = plan.width;
+    if (!ops) return PLBGPU_OK;
+    if (cap < 3 * plan.ops.size()) return PLBGPU_ERR_ARG;
+    for (size_t i = 0; i < plan.ops.size(); ++i) {
+        ops[3 * i] = plan.ops[i].kind;
+        ops[3 * i + 1] = plan.ops[i].slab;
+        ops[3 * i + 2] = plan.ops[i].step;
+    }
+    return PLBGPU_OK;
 }
 
 int plbgpu_reduce(plbgpu_ctx* c, int h, int x0, int x1, int y0, int y1, int z0, int z1, double* avg_energy,

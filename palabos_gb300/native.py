@@ -112,6 +112,7 @@ SIGNATURES = {
     "plbgpu_receive_f32": [_vp, _i, *BOX, ctypes.POINTER(ctypes.c_float), _sz],
     "plbgpu_collide_and_stream": [_vp, _i, _i, _i],
     "plbgpu_run_host": [_vp, _i, _c_dbl_p, _c_dbl_p, _sz, _i, _i, _c_dbl_p, _sz],
+    "plbgpu_run_host_plan": [_i, _i, _i, _i, _i, _c_int_p, _c_int_p, _sz, ctypes.POINTER(ctypes.c_size_t)],
     "plbgpu_get_stats": [_vp, _i, _c_dbl_p],
     "plbgpu_reduce": [_vp, _i, *BOX, _c_dbl_p, _c_dbl_p],
     "plbgpu_compute_velocity": [_vp, _i, *BOX, _c_dbl_p, _sz],
