@@ -257,9 +257,13 @@ class DeviceLattice3D:
 
     # ----------------------------------------------------------------- stepping
     def run_host(self, f, nsteps, stats_every=0, out=None):
-        """Send f, run nsteps steps and receive the state (plbgpu_run_host: the
-        transfers overlap the first and the last step).  Returns (state,
-        statistics records (k, 7) of every stats_every-th and the last step)."""
+        """Send f, run nsteps steps and receive the state into `out` (which may
+        be f) in one call (plbgpu_run_host): bit for bit send +
+        collide_and_stream + receive, with the transfers overlapped with ramps
+        of x-slab steps at both ends when the GPU addresses both buffers
+        directly.  Returns (state, statistics records (k, 7) of every
+        stats_every-th and of the last step, in the internal_statistics()
+        "raw" layout)."""
         a = np.ascontiguousarray(f, np.float64).reshape(-1)
         if out is None:
             out = np.empty(self.shape + (19,))
