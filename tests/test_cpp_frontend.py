@@ -38,6 +38,21 @@ def test_cpp_driver_reproduces_reference_golden(name):
     assert res["density"] == pytest.approx(float(g["density"]), rel=1e-12)
 
 
+@pytest.mark.gpu
+def test_cpp_run_host_matches_send_steps_receive():
+    """plbgpu::Lattice3D::runHost against send + collideAndStream + receive
+    from C++ (tests/cpp/run_host_check.cpp): bit for bit, statistics records
+    to summation rounding."""
+    exe = os.path.join(ROOT, "tests", "cpp", "_build", "run_host_check")
+    assert os.path.exists(exe), "build() compiles the C++ check"
+    out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
+    kv = dict(t.split("=") for t in out.split()[1:])
+    assert float(kv["maxabs"]) > 1e-3, out
+    assert float(kv["maxdiff"]) == 0.0, out
+    assert float(kv["statsrel"]) <= 1e-12, out
+    assert kv["records"] == "3/3", out
+
+
 @pytest.mark.slow
 def test_coprocessor_adapter_runs_reference_coprocessor_path():
     """plbgpu::GpuD3Q19CoProcessor3D<T> (include/plbgpu_coprocessor3d.hh)
